@@ -1,0 +1,519 @@
+"""Python mirror of the reference's pairwise API over the C ABI.
+
+Names, fields, defaults and error behaviour follow
+include/genoaligner/api.hpp of alrobles/genoaligner (AlignRequest,
+AlignResult, BatchResult, align, align_batch, SWScoring, SWRequest,
+SWAlignResult, SWBatchResult, align_sw, align_sw_batch, backend_name,
+device_name, device_available).  Every call goes through
+libgenoaligner_gb300.so (include/genoaligner_gb300.h); there is no Python or
+CPU fallback: if the library is missing, importing the binding raises.
+
+Besides the object API, ``align_batch_packed`` / ``align_sw_batch_packed``
+take sequences already concatenated in one buffer (offsets + lengths), the
+layout bulk callers and the benchmark hold; they build the C request arrays
+with numpy and return numpy result arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _build
+
+GA_OK, GA_INVALID_ARGUMENT, GA_DEVICE_ERROR = 0, 1, 2
+K_MAX_SMAX = 511
+SW_MAX_TRACE_CELLS = 1 << 26
+
+REQ_DT = np.dtype([("pattern", "<u8"), ("pattern_len", "<i4"), ("smax", "<i4"),
+                   ("text", "<u8"), ("text_len", "<i4"), ("with_cigar", "<i4")])
+RES_DT = np.dtype([("score", "<i4"), ("resolved", "<i4"), ("rescore_ok", "<i4"),
+                   ("wellformed_ok", "<i4"), ("cigar_offset", "<i8"), ("cigar_len", "<i4"),
+                   ("reserved", "<i4")])
+SWREQ_DT = np.dtype([("text", "<u8"), ("text_len", "<i4"), ("with_cigar", "<i4"),
+                     ("pattern", "<u8"), ("pattern_len", "<i4"), ("reserved", "<i4"),
+                     ("match", "<i4"), ("mismatch", "<i4"), ("gap_open", "<i4"),
+                     ("gap_extend", "<i4")])
+SWRES_DT = np.dtype([("score", "<i4"), ("resolved", "<i4"), ("start_i", "<i4"),
+                     ("start_j", "<i4"), ("end_i", "<i4"), ("end_j", "<i4"),
+                     ("rescore_ok", "<i4"), ("wellformed_ok", "<i4"), ("too_large", "<i4"),
+                     ("cigar_len", "<i4"), ("cigar_offset", "<i8")])
+assert REQ_DT.itemsize == 32 and RES_DT.itemsize == 32
+assert SWREQ_DT.itemsize == 48 and SWRES_DT.itemsize == 48
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("resolved_count", ctypes.c_int32),
+                ("unresolved_count", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("error", ctypes.c_char_p)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("max_smax", ctypes.c_int32), ("learned", ctypes.c_int32),
+                ("trace_cell_limit", ctypes.c_int64), ("reserved", ctypes.c_int32 * 4)]
+
+
+class SwScoringC(ctypes.Structure):
+    _fields_ = [("match", ctypes.c_int32), ("mismatch", ctypes.c_int32),
+                ("gap_open", ctypes.c_int32), ("gap_extend", ctypes.c_int32)]
+
+
+class DeviceBatch(ctypes.Structure):
+    _fields_ = [("seq", ctypes.c_void_p), ("seq_bytes", ctypes.c_int64),
+                ("a_off", ctypes.c_void_p), ("a_len", ctypes.c_void_p),
+                ("b_off", ctypes.c_void_p), ("b_len", ctypes.c_void_p),
+                ("out_off", ctypes.c_void_p), ("n", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", "ga_align_sw_batch",
+           "ga_align_batch_ex", "ga_align_sw_batch_ex", "ga_wfa_device", "ga_sw_device",
+           "ga_backend_name", "ga_device_name", "ga_device_available", "ga_kernel_launches",
+           "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
+           "ga_profile_kernel_name", "ga_bench_int_peak"]
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build: bool = True):
+    """Load (building first if needed) libgenoaligner_gb300.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise ImportError(f"libgenoaligner_gb300.so not built at {path}")
+    L = ctypes.CDLL(path)
+    p, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    L.ga_align_cigar_bytes.argtypes = [p, i32]
+    L.ga_align_cigar_bytes.restype = i64
+    L.ga_align_sw_cigar_bytes.argtypes = [p, i32]
+    L.ga_align_sw_cigar_bytes.restype = i64
+    L.ga_align_batch.argtypes = [p, i32, p, p, i64, ctypes.POINTER(BatchInfo)]
+    L.ga_align_batch.restype = i32
+    L.ga_align_batch_ex.argtypes = [p, i32, p, p, i64, ctypes.POINTER(Options), ctypes.POINTER(BatchInfo)]
+    L.ga_align_batch_ex.restype = i32
+    L.ga_align_sw_batch.argtypes = [p, i32, p, p, i64, ctypes.POINTER(BatchInfo)]
+    L.ga_align_sw_batch.restype = i32
+    L.ga_align_sw_batch_ex.argtypes = [p, i32, p, p, i64, ctypes.POINTER(Options), ctypes.POINTER(BatchInfo)]
+    L.ga_align_sw_batch_ex.restype = i32
+    L.ga_wfa_device.argtypes = [ctypes.POINTER(DeviceBatch), i32, i32, p, p, p, p, ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_wfa_device.restype = i32
+    L.ga_sw_device.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, i32, i64, p, p, p, p, p,
+                               ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_sw_device.restype = i32
+    L.ga_backend_name.restype = ctypes.c_char_p
+    L.ga_device_name.restype = ctypes.c_char_p
+    L.ga_device_available.restype = i32
+    L.ga_kernel_launches.restype = i64
+    L.ga_debug_fail_next.argtypes = [i32]
+    L.ga_last_transfer_bytes.argtypes = [ctypes.POINTER(i64), ctypes.POINTER(i64)]
+    L.ga_profile.argtypes = [i32]
+    L.ga_profile_read.argtypes = [i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64)]
+    L.ga_profile_read.restype = i32
+    L.ga_profile_kernel_name.argtypes = [i32]
+    L.ga_profile_kernel_name.restype = ctypes.c_char_p
+    L.ga_bench_int_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+    L.ga_bench_int_peak.restype = i32
+    _lib = L
+    return L
+
+
+# ----------------------------------------------------------------- types --
+class Status(enum.Enum):
+    ok = 0
+    invalid_argument = 1
+    device_error = 2
+
+
+@dataclass
+class AlignRequest:
+    pattern: bytes | None = None
+    pattern_len: int = 0
+    text: bytes | None = None
+    text_len: int = 0
+    smax: int = 64
+    with_cigar: bool = True
+
+
+@dataclass
+class AlignResult:
+    score: int = -1
+    resolved: bool = False
+    cigar: str = ""
+    rescore_ok: bool = False
+    wellformed_ok: bool = False
+
+
+@dataclass
+class BatchResult:
+    results: list = field(default_factory=list)
+    resolved_count: int = 0
+    unresolved_count: int = 0
+    status: Status = Status.ok
+    error: str | None = None
+
+    def ok(self) -> bool:
+        return self.status == Status.ok
+
+
+@dataclass
+class SWScoring:
+    match: int = 2
+    mismatch: int = -3
+    gap_open: int = 5
+    gap_extend: int = 2
+
+
+@dataclass
+class SWRequest:
+    text: bytes | None = None
+    text_len: int = 0
+    pattern: bytes | None = None
+    pattern_len: int = 0
+    scoring: SWScoring = field(default_factory=SWScoring)
+    with_cigar: bool = True
+
+
+@dataclass
+class SWAlignResult:
+    score: int = -1
+    resolved: bool = False
+    cigar: str = ""
+    start_i: int = -1
+    start_j: int = -1
+    end_i: int = -1
+    end_j: int = -1
+    rescore_ok: bool = False
+    wellformed_ok: bool = False
+    too_large: bool = False
+
+
+@dataclass
+class SWBatchResult:
+    results: list = field(default_factory=list)
+    resolved_count: int = 0
+    unresolved_count: int = 0
+    status: Status = Status.ok
+    error: str | None = None
+
+    def ok(self) -> bool:
+        return self.status == Status.ok
+
+
+def _addr(b):
+    """Address of a bytes object's buffer (None -> 0)."""
+    if b is None:
+        return 0
+    return ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p).value or 0
+
+
+def _opts(max_smax=0, learned=False, trace_cell_limit=0):
+    o = Options()
+    o.max_smax = max_smax
+    o.learned = 1 if learned else 0
+    o.trace_cell_limit = trace_cell_limit
+    return o
+
+
+def align_batch(reqs, max_smax: int = 0, learned: bool = False) -> BatchResult:
+    """genoaligner::align_batch (or align_batch_ex with max_smax / learned)."""
+    L = load()
+    n = len(reqs)
+    if n == 0:
+        return BatchResult()
+    keep = []
+    arr = np.zeros(n, REQ_DT)
+    for i, r in enumerate(reqs):
+        keep.append(r.pattern)
+        keep.append(r.text)
+        arr[i] = (_addr(r.pattern), r.pattern_len, r.smax, _addr(r.text), r.text_len, 1 if r.with_cigar else 0)
+    res = np.zeros(n, RES_DT)
+    nbytes = int(L.ga_align_cigar_bytes(arr.ctypes.data, n))
+    buf = ctypes.create_string_buffer(max(nbytes, 1))
+    info = BatchInfo()
+    if max_smax or learned:
+        o = _opts(max_smax, learned)
+        st = L.ga_align_batch_ex(arr.ctypes.data, n, res.ctypes.data, buf, nbytes, ctypes.byref(o), ctypes.byref(info))
+    else:
+        st = L.ga_align_batch(arr.ctypes.data, n, res.ctypes.data, buf, nbytes, ctypes.byref(info))
+    out = BatchResult(status=Status(st), error=info.error.decode() if info.error else None,
+                      resolved_count=info.resolved_count, unresolved_count=info.unresolved_count)
+    raw = buf.raw
+    for i in range(n):
+        r = res[i]
+        off, ln = int(r["cigar_offset"]), int(r["cigar_len"])
+        out.results.append(AlignResult(int(r["score"]), bool(r["resolved"]),
+                                       raw[off:off + ln].decode("latin-1") if ln else "",
+                                       bool(r["rescore_ok"]), bool(r["wellformed_ok"])))
+    return out
+
+
+def align(req: AlignRequest) -> AlignResult:
+    b = align_batch([req])
+    return b.results[0] if b.results else AlignResult()
+
+
+def align_sw_batch(reqs, trace_cell_limit: int = 0) -> SWBatchResult:
+    """genoaligner::align_sw_batch (or align_sw_batch_ex with a trace limit; < 0 = none)."""
+    L = load()
+    n = len(reqs)
+    if n == 0:
+        return SWBatchResult()
+    keep = []
+    arr = np.zeros(n, SWREQ_DT)
+    for i, r in enumerate(reqs):
+        keep.append(r.text)
+        keep.append(r.pattern)
+        s = r.scoring
+        arr[i] = (_addr(r.text), r.text_len, 1 if r.with_cigar else 0, _addr(r.pattern), r.pattern_len, 0,
+                  s.match, s.mismatch, s.gap_open, s.gap_extend)
+    res = np.zeros(n, SWRES_DT)
+    nbytes = int(L.ga_align_sw_cigar_bytes(arr.ctypes.data, n))
+    buf = ctypes.create_string_buffer(max(nbytes, 1))
+    info = BatchInfo()
+    if trace_cell_limit:
+        o = _opts(trace_cell_limit=trace_cell_limit)
+        st = L.ga_align_sw_batch_ex(arr.ctypes.data, n, res.ctypes.data, buf, nbytes, ctypes.byref(o),
+                                    ctypes.byref(info))
+    else:
+        st = L.ga_align_sw_batch(arr.ctypes.data, n, res.ctypes.data, buf, nbytes, ctypes.byref(info))
+    out = SWBatchResult(status=Status(st), error=info.error.decode() if info.error else None,
+                        resolved_count=info.resolved_count, unresolved_count=info.unresolved_count)
+    raw = buf.raw
+    for i in range(n):
+        r = res[i]
+        off, ln = int(r["cigar_offset"]), int(r["cigar_len"])
+        out.results.append(SWAlignResult(int(r["score"]), bool(r["resolved"]),
+                                         raw[off:off + ln].decode("latin-1") if ln else "",
+                                         int(r["start_i"]), int(r["start_j"]), int(r["end_i"]),
+                                         int(r["end_j"]), bool(r["rescore_ok"]), bool(r["wellformed_ok"]),
+                                         bool(r["too_large"])))
+    return out
+
+
+def align_sw(req: SWRequest) -> SWAlignResult:
+    b = align_sw_batch([req])
+    return b.results[0] if b.results else SWAlignResult()
+
+
+def backend_name() -> str:
+    return load().ga_backend_name().decode()
+
+
+def device_name() -> str:
+    return load().ga_device_name().decode()
+
+
+def device_available() -> bool:
+    return bool(load().ga_device_available())
+
+
+def kernel_launches() -> int:
+    return int(load().ga_kernel_launches())
+
+
+def last_transfer_bytes():
+    h, d = ctypes.c_int64(0), ctypes.c_int64(0)
+    load().ga_last_transfer_bytes(ctypes.byref(h), ctypes.byref(d))
+    return int(h.value), int(d.value)
+
+
+KERNEL_IDS = {"pack2": 0, "wfa_score": 1, "wfa_trace": 2, "sw8_score": 3, "sw16_score": 4, "sw32_score": 5,
+              "sw8_trace": 6, "sw16_trace": 7, "sw32_trace": 8, "int_peak": 9, "kmer_sketch": 10, "mlp": 11}
+
+
+def profile(on: bool):
+    load().ga_profile(1 if on else 0)
+
+
+def profile_read():
+    """{kernel name: (total device ms, launches)} for kernels that ran."""
+    L = load()
+    out = {}
+    for name, k in KERNEL_IDS.items():
+        ms, n = ctypes.c_double(0), ctypes.c_int64(0)
+        L.ga_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
+        if n.value:
+            out[name] = (float(ms.value), int(n.value))
+    return out
+
+
+def int_peak(variant: int = 0) -> float:
+    v = ctypes.c_double(0)
+    st = load().ga_bench_int_peak(variant, ctypes.byref(v))
+    if st != GA_OK:
+        raise RuntimeError("int peak microbenchmark failed")
+    return float(v.value)
+
+
+# -------------------------------------------------------- device-resident --
+def device_layout(a_buf, a_off, a_len, b_buf, b_off, b_len):
+    """Host-side plan of the device arena: every sequence at a 32-byte-aligned
+    offset, 64 bytes of padding at the end, CIGAR slots of a_len + b_len.
+    Returns (arena uint8, a_off, b_off, out_off, out_bytes)."""
+    n = a_len.shape[0]
+    ra = (a_len.astype(np.int64) + 31) & ~31
+    rb = (b_len.astype(np.int64) + 31) & ~31
+    step = ra + rb
+    base = np.zeros(n, np.int64)
+    if n > 1:
+        np.cumsum(step[:-1], out=base[1:])
+    na_off = base
+    nb_off = base + ra
+    total = int(step.sum()) + 64
+    arena = np.zeros(total, np.uint8)
+    _scatter(arena, na_off, a_buf, a_off, a_len)
+    _scatter(arena, nb_off, b_buf, b_off, b_len)
+    cap = a_len.astype(np.int64) + b_len
+    out_off = np.zeros(n, np.int64)
+    if n > 1:
+        np.cumsum(cap[:-1], out=out_off[1:])
+    return arena, na_off, nb_off, out_off, int(cap.sum())
+
+
+def _scatter(dst, dst_off, src, src_off, lens):
+    lens64 = lens.astype(np.int64)
+    tot = int(lens64.sum())
+    if tot == 0:
+        return
+    seg = np.repeat(np.arange(lens.shape[0]), lens64)
+    starts = np.zeros(lens.shape[0], np.int64)
+    if lens.shape[0] > 1:
+        np.cumsum(lens64[:-1], out=starts[1:])
+    within = np.arange(tot, dtype=np.int64) - starts[seg]
+    dst[dst_off[seg] + within] = src[src_off[seg] + within]
+
+
+class DeviceBatchT:
+    """A batch resident in device memory (torch tensors) for ga_wfa_device /
+    ga_sw_device."""
+
+    def __init__(self, a_buf, a_off, a_len, b_buf, b_off, b_len, device="cuda:0"):
+        import torch
+        arena, na, nb, oo, out_bytes = device_layout(a_buf, a_off, a_len, b_buf, b_off, b_len)
+        self.n = int(a_len.shape[0])
+        self.seq = torch.from_numpy(arena).to(device)
+        self.a_off = torch.from_numpy(na).to(device)
+        self.a_len = torch.from_numpy(a_len.astype(np.int32)).to(device)
+        self.b_off = torch.from_numpy(nb).to(device)
+        self.b_len = torch.from_numpy(b_len.astype(np.int32)).to(device)
+        self.out_off = torch.from_numpy(oo).to(device)
+        self.out_bytes = out_bytes
+        self.input_bytes = int(arena.nbytes + 8 * 3 * self.n + 4 * 2 * self.n)
+        self.c = DeviceBatch(self.seq.data_ptr(), int(arena.shape[0]), self.a_off.data_ptr(),
+                             self.a_len.data_ptr(), self.b_off.data_ptr(), self.b_len.data_ptr(),
+                             self.out_off.data_ptr(), self.n, 0)
+
+
+def wfa_device(batch: DeviceBatchT, smax, trace, out_score, out_len, out_cigar, stream=None):
+    err = ctypes.c_char_p()
+    st = load().ga_wfa_device(ctypes.byref(batch.c), smax, 1 if trace else 0, out_score.data_ptr(),
+                              out_len.data_ptr() if out_len is not None else None,
+                              out_cigar.data_ptr() if out_cigar is not None else None,
+                              stream, ctypes.byref(err))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_wfa_device failed: {err.value}")
+
+
+def sw_device(batch: DeviceBatchT, scoring, trace, out_score, out_pos, out_len, out_cigar, stream=None,
+              trace_cell_limit=-1):
+    err = ctypes.c_char_p()
+    sc = SwScoringC(*scoring)
+    st = load().ga_sw_device(ctypes.byref(batch.c), sc, 1 if trace else 0, trace_cell_limit,
+                             out_score.data_ptr(), out_pos.data_ptr(),
+                             out_len.data_ptr() if out_len is not None else None,
+                             out_cigar.data_ptr() if out_cigar is not None else None,
+                             stream, ctypes.byref(err))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_sw_device failed: {err.value}")
+
+
+# ------------------------------------------------------------ packed bulk --
+@dataclass
+class PackedResult:
+    """Result arrays of a packed batch call; CIGAR i = cigar_buf[off[i]:off[i]+len[i]]."""
+    status: Status
+    error: str | None
+    res: np.ndarray
+    cigar_buf: np.ndarray
+    resolved_count: int
+    unresolved_count: int
+
+    def cigar(self, i: int) -> bytes:
+        o, ln = int(self.res["cigar_offset"][i]), int(self.res["cigar_len"][i])
+        return self.cigar_buf[o:o + ln].tobytes()
+
+
+def align_batch_packed(p_buf, p_off, p_len, t_buf, t_off, t_len, smax=64, with_cigar=True,
+                       max_smax=0, learned=False, _reqs=None, _res=None, _cig=None) -> PackedResult:
+    """align_batch over sequences held in two byte buffers (pattern i =
+    p_buf[p_off[i]:p_off[i]+p_len[i]], text likewise).  ``smax`` and
+    ``with_cigar`` are scalars or per-request arrays.  The optional ``_reqs``,
+    ``_res``, ``_cig`` let a caller reuse its request/result/CIGAR arrays."""
+    L = load()
+    n = int(p_len.shape[0])
+    reqs = _reqs if _reqs is not None else make_requests(p_buf, p_off, p_len, t_buf, t_off, t_len, smax, with_cigar)
+    res = _res if _res is not None else np.zeros(n, RES_DT)
+    nbytes = int(L.ga_align_cigar_bytes(reqs.ctypes.data, n))
+    cig = _cig if _cig is not None and _cig.shape[0] >= nbytes else np.empty(max(nbytes, 1), np.uint8)
+    info = BatchInfo()
+    if max_smax or learned:
+        o = _opts(max_smax, learned)
+        st = L.ga_align_batch_ex(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes,
+                                 ctypes.byref(o), ctypes.byref(info))
+    else:
+        st = L.ga_align_batch(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes, ctypes.byref(info))
+    return PackedResult(Status(st), info.error.decode() if info.error else None, res, cig,
+                        info.resolved_count, info.unresolved_count)
+
+
+def make_requests(p_buf, p_off, p_len, t_buf, t_off, t_len, smax=64, with_cigar=True) -> np.ndarray:
+    n = int(p_len.shape[0])
+    reqs = np.zeros(n, REQ_DT)
+    reqs["pattern"] = p_buf.ctypes.data + p_off.astype(np.uint64)
+    reqs["pattern_len"] = p_len
+    reqs["smax"] = smax
+    reqs["text"] = t_buf.ctypes.data + t_off.astype(np.uint64)
+    reqs["text_len"] = t_len
+    reqs["with_cigar"] = np.asarray(with_cigar).astype(np.int32)
+    return reqs
+
+
+def make_sw_requests(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, -3, 5, 2), with_cigar=True) -> np.ndarray:
+    n = int(t_len.shape[0])
+    reqs = np.zeros(n, SWREQ_DT)
+    reqs["text"] = t_buf.ctypes.data + t_off.astype(np.uint64)
+    reqs["text_len"] = t_len
+    reqs["with_cigar"] = np.asarray(with_cigar).astype(np.int32)
+    reqs["pattern"] = p_buf.ctypes.data + p_off.astype(np.uint64)
+    reqs["pattern_len"] = p_len
+    reqs["match"], reqs["mismatch"], reqs["gap_open"], reqs["gap_extend"] = scoring
+    return reqs
+
+
+def align_sw_batch_packed(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, -3, 5, 2), with_cigar=True,
+                          trace_cell_limit=0, _reqs=None, _res=None, _cig=None) -> PackedResult:
+    """align_sw_batch over packed sequences (text = rows, pattern = columns)."""
+    L = load()
+    n = int(t_len.shape[0])
+    reqs = _reqs if _reqs is not None else make_sw_requests(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring,
+                                                            with_cigar)
+    res = _res if _res is not None else np.zeros(n, SWRES_DT)
+    nbytes = int(L.ga_align_sw_cigar_bytes(reqs.ctypes.data, n))
+    cig = _cig if _cig is not None and _cig.shape[0] >= nbytes else np.empty(max(nbytes, 1), np.uint8)
+    info = BatchInfo()
+    if trace_cell_limit:
+        o = _opts(trace_cell_limit=trace_cell_limit)
+        st = L.ga_align_sw_batch_ex(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes,
+                                    ctypes.byref(o), ctypes.byref(info))
+    else:
+        st = L.ga_align_sw_batch(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes, ctypes.byref(info))
+    return PackedResult(Status(st), info.error.decode() if info.error else None, res, cig,
+                        info.resolved_count, info.unresolved_count)

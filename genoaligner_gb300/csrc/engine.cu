@@ -1,0 +1,1118 @@
+// engine.cu -- host engine and C ABI of the GB300 pairwise aligner.
+//
+// Per call: validate the requests exactly as the reference's API does
+// (src/api/api.cpp:246-266, 600-616, 515-536), lay the sequences out in a
+// pinned staging arena at 32-byte-aligned offsets (the layout the kernels
+// take), copy once to the device, run the kernels on the call's own stream,
+// copy the outputs back once, and materialise results on the host thread pool.
+// Contexts (stream + grow-only device and pinned arenas) are pooled, so a
+// steady stream of calls allocates nothing; concurrent calls take different
+// contexts.
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "engine.hpp"
+#include "kernels.cuh"
+
+namespace ga {
+
+// ------------------------------------------------------------ accounting --
+static std::atomic<long long> g_launches{0};
+
+// Per-kernel event timing, on only between ga_profile(1) and ga_profile(0).
+struct ProfRec { int id; cudaEvent_t a, b; };
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<ProfRec> g_prof_open;      // begin recorded, end pending
+static std::vector<ProfRec> g_prof_done;
+static double g_prof_ms[K_COUNT];
+static long long g_prof_n[K_COUNT];
+thread_local ProfRec t_prof_cur{-1, nullptr, nullptr};
+
+void launch_begin(int kernel_id, cudaStream_t st)
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (!g_prof_on) return;
+    ProfRec r{kernel_id, nullptr, nullptr};
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, st);
+    t_prof_cur = r;
+}
+
+void launch_end(int kernel_id, cudaStream_t st)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (!g_prof_on || t_prof_cur.id != kernel_id) return;
+    cudaEventRecord(t_prof_cur.b, st);
+    g_prof_done.push_back(t_prof_cur);
+    t_prof_cur = ProfRec{-1, nullptr, nullptr};
+}
+
+// Host-to-device / device-to-host bytes of the calling thread's last batch call.
+thread_local int64_t t_h2d = 0, t_d2h = 0;
+
+static std::atomic<int> g_fail_next{0};
+
+// ----------------------------------------------------------- thread pool --
+class Pool {
+public:
+    Pool()
+    {
+        unsigned hc = std::thread::hardware_concurrency();
+        int nw = (int)(hc == 0 ? 1 : hc) - 1;
+        if (nw > 63) nw = 63;
+        for (int i = 0; i < nw; ++i) threads_.emplace_back([this] { worker(); });
+    }
+    ~Pool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : threads_) t.join();
+    }
+    void run(int64_t n, int64_t grain, const std::function<void(int64_t, int64_t)>& fn)
+    {
+        if (n <= 0) return;
+        if (grain < 1) grain = 1;
+        if (threads_.empty() || n <= grain) { fn(0, n); return; }
+        std::lock_guard<std::mutex> one(job_mu_);          // one parallel job at a time
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &fn;
+            n_ = n;
+            grain_ = grain;
+            next_.store(0);
+            busy_ = (int)threads_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return busy_ == 0; });
+        fn_ = nullptr;
+    }
+
+private:
+    void drain()
+    {
+        for (;;) {
+            const int64_t lo = next_.fetch_add(grain_);
+            if (lo >= n_) break;
+            (*fn_)(lo, std::min(n_, lo + grain_));
+        }
+    }
+    void worker()
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            drain();
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (--busy_ == 0) done_cv_.notify_all();
+            }
+        }
+    }
+    std::vector<std::thread> threads_;
+    std::mutex mu_, job_mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int64_t, int64_t)>* fn_ = nullptr;
+    int64_t n_ = 0, grain_ = 1;
+    std::atomic<int64_t> next_{0};
+    int busy_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+static Pool& pool()
+{
+    static Pool* p = new Pool();   // never destroyed: worker threads outlive static teardown safely
+    return *p;
+}
+
+void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, int64_t)>& fn)
+{
+    pool().run(n, grain, fn);
+}
+
+// -------------------------------------------------------------- contexts --
+struct Ctx {
+    int device = -1;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;     // last work enqueued on a caller's stream
+    bool pending = false;
+    char* dev = nullptr;
+    size_t dev_cap = 0;
+    char* host = nullptr;
+    size_t host_cap = 0;
+};
+
+static std::mutex g_ctx_mu;
+static std::vector<Ctx*> g_ctx_free;
+
+static const char* E_NODEV = "no CUDA device is available";
+
+static Ctx* acquire_ctx(const char** err)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_NODEV;
+        return nullptr;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_ctx_mu);
+        for (size_t i = 0; i < g_ctx_free.size(); ++i) {
+            if (g_ctx_free[i]->device == dev) {
+                Ctx* c = g_ctx_free[i];
+                g_ctx_free.erase(g_ctx_free.begin() + (long)i);
+                if (c->pending) { cudaEventSynchronize(c->done); c->pending = false; }
+                return c;
+            }
+        }
+    }
+    Ctx* c = new Ctx();
+    c->device = dev;
+    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        *err = E_NODEV;
+        return nullptr;
+    }
+    return c;
+}
+
+static void release_ctx(Ctx* c)
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    g_ctx_free.push_back(c);
+}
+
+static bool ensure_dev(Ctx* c, size_t bytes)
+{
+    if (bytes <= c->dev_cap) return true;
+    if (c->dev) { cudaStreamSynchronize(c->stream); cudaFree(c->dev); c->dev = nullptr; c->dev_cap = 0; }
+    size_t want = std::max(bytes, (size_t)(c->dev_cap * 3 / 2));
+    want = (want + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+    if (cudaMalloc(&c->dev, want) != cudaSuccess) {
+        cudaGetLastError();
+        if (cudaMalloc(&c->dev, bytes) != cudaSuccess) { cudaGetLastError(); c->dev = nullptr; return false; }
+        want = bytes;
+    }
+    c->dev_cap = want;
+    return true;
+}
+
+static bool ensure_host(Ctx* c, size_t bytes)
+{
+    if (bytes <= c->host_cap) return true;
+    if (c->host) { cudaStreamSynchronize(c->stream); cudaFreeHost(c->host); c->host = nullptr; c->host_cap = 0; }
+    size_t want = std::max(bytes, (size_t)(c->host_cap * 3 / 2));
+    want = (want + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+    if (cudaHostAlloc(&c->host, want, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        c->host = nullptr;
+        return false;
+    }
+    c->host_cap = want;
+    return true;
+}
+
+// Carves aligned sub-buffers out of one arena; a first pass with base null
+// only measures.
+struct Carve {
+    char* base;
+    size_t off = 0;
+    explicit Carve(char* b) : base(b) {}
+    template <class T>
+    T* take(size_t count, size_t align = 256)
+    {
+        off = (off + align - 1) & ~(align - 1);
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+static inline int64_t round32(int64_t x) { return (x + 31) & ~(int64_t)31; }
+
+static bool fail_here(int step)
+{
+    int want = g_fail_next.load();
+    if (want == step && g_fail_next.compare_exchange_strong(want, 0)) return true;
+    return false;
+}
+
+// ------------------------------------------------------------ validation --
+static const char* E_NULL = "null pointer with non-zero length";
+static const char* E_NEG = "negative length";
+static const char* E_SMAX = "smax out of range [0, 511]";
+static const char* E_SMAX_EX = "smax out of range [0, max_smax]";
+static const char* E_ALLOC = "device allocation failed";
+static const char* E_H2D = "host-to-device copy failed";
+static const char* E_LAUNCH = "kernel launch failed";
+static const char* E_D2H = "device-to-host copy failed";
+static const char* E_SYNC = "device execution failed";
+static const char* E_OVERFLOW = "internal error: CIGAR slot overflow";
+static const char* E_HOSTMEM = "pinned host allocation failed";
+
+// -------------------------------------------------------------------- WFA --
+int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err)
+{
+    for (int32_t i = 0; i < n; ++i) {
+        const ga_align_request& r = reqs[i];
+        if ((r.pattern_len > 0 && !r.pattern) || (r.text_len > 0 && !r.text)) { *err = E_NULL; return GA_INVALID_ARGUMENT; }
+        if (r.pattern_len < 0 || r.text_len < 0) { *err = E_NEG; return GA_INVALID_ARGUMENT; }
+        if (r.smax < 0 || r.smax > max_smax) {
+            *err = max_smax == GA_MAX_SMAX ? E_SMAX : E_SMAX_EX;
+            return GA_INVALID_ARGUMENT;
+        }
+    }
+    return GA_OK;
+}
+
+int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
+                  const WfaFinish& fin, const char** err)
+{
+    (void)learned;
+    *err = nullptr;
+    if (n <= 0) return GA_OK;
+    if (int32_t st = wfa_check(reqs, n, max_smax, err)) return st;
+    int smax = reqs[0].smax;
+    bool trace = false;
+    for (int32_t i = 0; i < n; ++i) {
+        smax = std::min(smax, (int)reqs[i].smax);
+        trace |= reqs[i].with_cigar != 0;
+    }
+
+    // plan: 32-aligned sequence offsets, CIGAR slot offsets
+    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    int64_t arena = 0, cig = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        a_off[i] = arena; arena += round32(reqs[i].pattern_len);
+        b_off[i] = arena; arena += round32(reqs[i].text_len);
+        out_off[i] = cig; cig += (int64_t)reqs[i].pattern_len + reqs[i].text_len;
+        slot_end[i] = cig;
+    }
+    arena += 64;                                     // read-past padding
+    if (!trace) cig = 0;
+
+    Ctx* c = acquire_ctx(err);
+    if (!c) return GA_DEVICE_ERROR;
+    struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
+
+    const int max_slots = wfa_max_slots(smax, trace, c->sm_count);
+    int slots = std::min<int64_t>(max_slots, ((int64_t)n + 3) / 4 * 4);
+    const int64_t stack_slot = (int64_t)(smax + 1) * (smax + 1);
+    if (trace) {
+        const int64_t budget = (int64_t)16 << 30;     // stack memory cap
+        const int64_t cap = std::max<int64_t>(4, budget / (stack_slot * 4) / 4 * 4);
+        slots = (int)std::min<int64_t>(slots, cap);
+    }
+
+    // device layout: [a_off a_len b_off b_len out_off | seq] [packed pure] [score len cigar | err] [stack counter]
+    auto layout = [&](char* base, bool host, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl,
+                      int64_t** po, uint8_t** seq, uint64_t** packed, uint8_t** pure, int32_t** sc,
+                      int32_t** ln, char** cg, int32_t** er, int32_t** stk, int32_t** ctr) -> size_t {
+        Carve k(base);
+        *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
+        *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
+        *po = k.take<int64_t>(n);
+        *seq = k.take<uint8_t>(arena);
+        const size_t in_end = k.off;
+        if (host) {
+            // host staging: inputs, then outputs
+            *sc = k.take<int32_t>(n); *ln = k.take<int32_t>(n); *cg = k.take<char>(cig + 1);
+            *er = k.take<int32_t>(1);
+            (void)in_end;
+            return k.off;
+        }
+        *packed = k.take<uint64_t>(arena / 32 + 2);
+        *pure = k.take<uint8_t>(2 * (size_t)n);
+        *sc = k.take<int32_t>(n); *ln = k.take<int32_t>(n); *cg = k.take<char>(cig + 1);
+        *er = k.take<int32_t>(1);
+        *ctr = k.take<int32_t>(1, 4);
+        *stk = trace ? k.take<int32_t>((size_t)slots * stack_slot) : nullptr;
+        return k.off;
+    };
+    int64_t *ha, *hb, *ho, *da, *db, *dout;
+    int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der, *dstk, *dctr, *dummy_i;
+    uint8_t *hseq, *dseq, *dpure, *dummy_u8;
+    uint64_t *dpacked, *dummy_u64;
+    char *hcg, *dcg;
+    const size_t host_bytes = layout(nullptr, true, &ha, &hal, &hb, &hbl, &ho, &hseq, &dummy_u64, &dummy_u8,
+                                     &hsc, &hln, &hcg, &her, &dummy_i, &dummy_i);
+    const size_t dev_bytes = layout(nullptr, false, &da, &dal, &db, &dbl, &dout, &dseq, &dpacked, &dpure,
+                                    &dsc, &dln, &dcg, &der, &dstk, &dctr);
+    if (fail_here(1) || !ensure_dev(c, dev_bytes)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    if (!ensure_host(c, host_bytes)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    layout(c->host, true, &ha, &hal, &hb, &hbl, &ho, &hseq, &dummy_u64, &dummy_u8, &hsc, &hln, &hcg, &her,
+           &dummy_i, &dummy_i);
+    layout(c->dev, false, &da, &dal, &db, &dbl, &dout, &dseq, &dpacked, &dpure, &dsc, &dln, &dcg, &der, &dstk,
+           &dctr);
+
+    // stage inputs
+    parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            const ga_align_request& r = reqs[i];
+            ha[i] = a_off[i]; hal[i] = r.pattern_len;
+            hb[i] = b_off[i]; hbl[i] = r.text_len;
+            ho[i] = out_off[i];
+            if (r.pattern_len) std::memcpy(hseq + a_off[i], r.pattern, (size_t)r.pattern_len);
+            if (r.text_len) std::memcpy(hseq + b_off[i], r.text, (size_t)r.text_len);
+        }
+    });
+    std::memset(hseq + arena - 64, 0, 64);
+    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);     // descriptors + arena, contiguous
+    t_h2d = (int64_t)in_bytes;
+    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+        cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_H2D;
+        return GA_DEVICE_ERROR;
+    }
+    cudaMemsetAsync(dctr, 0, sizeof(int32_t), c->stream);
+
+    PairDesc D;
+    D.seq = dseq; D.packed = dpacked; D.pure = dpure;
+    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
+    WfaArgs A;
+    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
+    A.out_score = dsc; A.out_len = dln; A.out_cigar = dcg;
+    A.stack = dstk; A.stack_slot = stack_slot; A.counter = dctr; A.err = der;
+    if (fail_here(3) || launch_pack(D, dpacked, dpure, c->stream) != cudaSuccess ||
+        launch_wfa(A, slots, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_LAUNCH;
+        return GA_DEVICE_ERROR;
+    }
+    // outputs are contiguous on both sides: score, len, cigar, err
+    const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
+    t_d2h = (int64_t)out_bytes;
+    if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_D2H;
+        return GA_DEVICE_ERROR;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_SYNC;
+        return GA_DEVICE_ERROR;
+    }
+    if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
+    WfaView v{hsc, hln, hcg, slot_end.data(), trace};
+    parallel_for(n, 1024, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
+    return GA_OK;
+}
+
+// --------------------------------------------------------------------- SW --
+static const char* E_SW_MATCH = "SW scoring: match must be > 0 (the score is 0 for every input otherwise)";
+static const char* E_SW_MISMATCH = "SW scoring: mismatch must be < match";
+static const char* E_SW_GAPS = "SW scoring: gap costs must be > 0";
+static const char* E_SW_GEGO =
+    "SW scoring: gap_extend > gap_open with with_cigar cannot re-score to its own score (api.hpp; "
+    "RESULTADO_H9_SW2_TRACE.md). Score-only requests may use it";
+static const char* E_SW_MIXED = "all requests in an SW batch must share one scoring scheme";
+static const char* E_SW_SMEM =
+    "pattern_len exceeds this device's shared-memory limit for the score kernel (see api.hpp "
+    "supported-size limits)";
+
+int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err)
+{
+    if (n <= 0) return GA_OK;
+    const ga_sw_scoring s0 = reqs[0].scoring;
+    for (int32_t i = 0; i < n; ++i) {
+        const ga_sw_request& r = reqs[i];
+        if ((r.text_len > 0 && !r.text) || (r.pattern_len > 0 && !r.pattern)) { *err = E_NULL; return GA_INVALID_ARGUMENT; }
+        if (r.text_len < 0 || r.pattern_len < 0) { *err = E_NEG; return GA_INVALID_ARGUMENT; }
+        const ga_sw_scoring& s = r.scoring;
+        if (s.match <= 0) { *err = E_SW_MATCH; return GA_INVALID_ARGUMENT; }
+        if (s.mismatch >= s.match) { *err = E_SW_MISMATCH; return GA_INVALID_ARGUMENT; }
+        if (s.gap_open <= 0 || s.gap_extend <= 0) { *err = E_SW_GAPS; return GA_INVALID_ARGUMENT; }
+        if (r.with_cigar && s.gap_extend > s.gap_open) { *err = E_SW_GEGO; return GA_INVALID_ARGUMENT; }
+        if (s.match != s0.match || s.mismatch != s0.mismatch || s.gap_open != s0.gap_open ||
+            s.gap_extend != s0.gap_extend) { *err = E_SW_MIXED; return GA_INVALID_ARGUMENT; }
+    }
+    return GA_OK;
+}
+
+int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
+                 const char** err)
+{
+    *err = nullptr;
+    if (n <= 0) return GA_OK;
+    const ga_sw_scoring s0 = reqs[0].scoring;
+    if (int32_t st = sw_check(reqs, n, err)) return st;
+    bool trace = false;
+    int max_n = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        trace |= reqs[i].with_cigar != 0;
+        max_n = std::max(max_n, (int)reqs[i].pattern_len);
+    }
+    // The reference's score-only kernel holds 4 warps x 2*(n+1) ints of shared
+    // memory per block and refuses the batch above the per-block limit the
+    // runtime reports, 48 KiB on CUDA devices (src/api/api.cpp:789-797).  The
+    // drop-in entry keeps that limit; the extension entry passes cell_limit < 0.
+    if (!trace && cell_limit >= 0 && (int64_t)4 * 2 * (max_n + 1) * 4 > 48 * 1024) {
+        *err = E_SW_SMEM;
+        return GA_INVALID_ARGUMENT;
+    }
+
+    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    std::vector<uint8_t> too_big(n, 0);
+    int64_t arena = 0, cig = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        const ga_sw_request& r = reqs[i];
+        a_off[i] = arena; arena += round32(r.text_len);
+        b_off[i] = arena; arena += round32(r.pattern_len);
+        out_off[i] = cig; cig += (int64_t)r.text_len + r.pattern_len;
+        slot_end[i] = cig;
+        if (trace && cell_limit >= 0 && r.text_len > 0 && r.pattern_len > 0 &&
+            ((int64_t)r.text_len + 1) * ((int64_t)r.pattern_len + 1) > cell_limit)
+            too_big[i] = 1;
+    }
+    arena += 64;
+    if (!trace) cig = 0;
+
+    // work lists by band width, largest first
+    std::vector<int32_t> work[3];
+    const int widths[3] = {8, 16, 32};
+    for (int32_t i = 0; i < n; ++i) {
+        if (too_big[i]) continue;
+        const int C = sw_width_for(reqs[i].pattern_len);
+        work[C == 8 ? 0 : (C == 16 ? 1 : 2)].push_back(i);
+    }
+    int64_t dir_slot[3] = {0, 0, 0}, edge_slot = 2;
+    for (int w = 0; w < 3; ++w) {
+        std::sort(work[w].begin(), work[w].end(), [&](int32_t x, int32_t y) {
+            const int64_t cx = (int64_t)(reqs[x].text_len + 31) * reqs[x].pattern_len;
+            const int64_t cy = (int64_t)(reqs[y].text_len + 31) * reqs[y].pattern_len;
+            return cx != cy ? cx > cy : x < y;
+        });
+        for (int32_t i : work[w]) {
+            dir_slot[w] = std::max(dir_slot[w], sw_dir_words(reqs[i].text_len, reqs[i].pattern_len, widths[w]));
+            edge_slot = std::max<int64_t>(edge_slot, 2 * (int64_t)reqs[i].text_len);
+        }
+        dir_slot[w] = (dir_slot[w] + 3) / 4 * 4;
+    }
+
+    Ctx* c = acquire_ctx(err);
+    if (!c) return GA_DEVICE_ERROR;
+    struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
+
+    int slots[3] = {0, 0, 0};
+    int64_t dir_words = 0, max_slots_all = 0;
+    const int64_t dir_budget = (int64_t)48 << 30;       // direction-table memory cap (bytes)
+    for (int w = 0; w < 3; ++w) {
+        if (work[w].empty()) continue;
+        int s = sw_max_slots(widths[w], trace, c->sm_count);
+        s = (int)std::min<int64_t>(s, ((int64_t)work[w].size() + 3) / 4 * 4);
+        if (trace && dir_slot[w] > 0)
+            s = (int)std::min<int64_t>(s, std::max<int64_t>(4, dir_budget / (dir_slot[w] * 4) / 4 * 4));
+        slots[w] = s;
+        if (trace) dir_words = std::max(dir_words, (int64_t)s * dir_slot[w]);
+        max_slots_all = std::max<int64_t>(max_slots_all, s);
+    }
+
+    int64_t *ha, *hb, *ho, *da, *db, *dout;
+    int32_t *hal, *hbl, *dal, *dbl, *hwork, *dwork, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der,
+        *dctr, *dedge;
+    uint8_t *hseq, *dseq;
+    uint32_t* ddirs;
+    char *hcg, *dcg;
+    const int64_t nwork = (int64_t)work[0].size() + work[1].size() + work[2].size();
+    auto layout = [&](char* base, bool host) -> size_t {
+        Carve k(base);
+        int64_t* pa = k.take<int64_t>(n); int32_t* pal = k.take<int32_t>(n);
+        int64_t* pb = k.take<int64_t>(n); int32_t* pbl = k.take<int32_t>(n);
+        int64_t* po = k.take<int64_t>(n);
+        int32_t* pw = k.take<int32_t>(nwork + 1);
+        uint8_t* ps = k.take<uint8_t>(arena);
+        int32_t* psc = k.take<int32_t>(n); int32_t* ppos = k.take<int32_t>(4 * (size_t)n);
+        int32_t* pln = k.take<int32_t>(n); char* pcg = k.take<char>(cig + 1);
+        int32_t* per = k.take<int32_t>(1, 4);
+        if (host) {
+            ha = pa; hal = pal; hb = pb; hbl = pbl; ho = po; hwork = pw; hseq = ps;
+            hsc = psc; hpos = ppos; hln = pln; hcg = pcg; her = per;
+            return k.off;
+        }
+        da = pa; dal = pal; db = pb; dbl = pbl; dout = po; dwork = pw; dseq = ps;
+        dsc = psc; dpos = ppos; dln = pln; dcg = pcg; der = per;
+        dctr = k.take<int32_t>(4, 4);
+        dedge = k.take<int32_t>((size_t)max_slots_all * edge_slot);
+        ddirs = trace ? k.take<uint32_t>((size_t)dir_words) : nullptr;
+        return k.off;
+    };
+    const size_t host_bytes = layout(nullptr, true);
+    const size_t dev_bytes = layout(nullptr, false);
+    if (fail_here(1) || !ensure_dev(c, dev_bytes)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    if (!ensure_host(c, host_bytes)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    layout(c->host, true);
+    layout(c->dev, false);
+
+    {
+        int64_t q = 0;
+        for (int w = 0; w < 3; ++w)
+            for (int32_t i : work[w]) hwork[q++] = i;
+    }
+    parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            const ga_sw_request& r = reqs[i];
+            ha[i] = a_off[i]; hal[i] = r.text_len;
+            hb[i] = b_off[i]; hbl[i] = r.pattern_len;
+            ho[i] = out_off[i];
+            if (r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
+            if (r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
+        }
+    });
+    std::memset(hseq + arena - 64, 0, 64);
+    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
+    t_h2d = (int64_t)in_bytes;
+    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_H2D;
+        return GA_DEVICE_ERROR;
+    }
+    // sentinel: too-large pairs keep score -1 (never written by a kernel)
+    cudaMemsetAsync(dsc, 0xff, sizeof(int32_t) * (size_t)n, c->stream);
+    cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, c->stream);
+    cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, c->stream);
+    cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream);
+    cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 4, c->stream);
+
+    PairDesc D;
+    D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
+    if (fail_here(3)) { *err = E_LAUNCH; return GA_DEVICE_ERROR; }
+    int64_t wbase = 0;
+    for (int w = 0; w < 3; ++w) {
+        if (work[w].empty()) continue;
+        SwArgs A;
+        A.D = D;
+        A.work = dwork + wbase;
+        A.nwork = (int32_t)work[w].size();
+        A.match = s0.match; A.mismatch = s0.mismatch; A.gap_open = s0.gap_open; A.gap_extend = s0.gap_extend;
+        A.out_score = dsc; A.out_pos = dpos; A.out_len = dln; A.out_cigar = dcg;
+        A.dirs = ddirs; A.dir_slot = dir_slot[w];
+        A.edge = dedge; A.edge_slot = edge_slot;
+        A.counter = dctr + w; A.err = der;
+        if (launch_sw(A, widths[w], trace, slots[w], c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *err = E_LAUNCH;
+            return GA_DEVICE_ERROR;
+        }
+        wbase += (int64_t)work[w].size();
+    }
+    const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
+    t_d2h = (int64_t)out_bytes;
+    if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_D2H;
+        return GA_DEVICE_ERROR;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_SYNC;
+        return GA_DEVICE_ERROR;
+    }
+    if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
+    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace};
+    parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
+    return GA_OK;
+}
+
+// ------------------------------------------------------------ validators --
+void wfa_validate(const char* cg, int len, int score, const char* P, int m, const char* T, int n,
+                  bool* rescore_ok, bool* wellformed_ok)
+{
+    int cost = 0, pi = 0, ti = 0;
+    bool ok = true;
+    for (int q = 0; q < len; ++q) {
+        const char op = cg[q];
+        if (op == 'M' || op == 'X') {
+            if (pi >= m || ti >= n || ((P[pi] == T[ti]) != (op == 'M'))) ok = false;
+            cost += op == 'X';
+            ++pi;
+            ++ti;
+        } else if (op == 'I') {
+            ++ti;
+            ++cost;
+        } else if (op == 'D') {
+            ++pi;
+            ++cost;
+        } else {
+            ok = false;
+        }
+    }
+    *wellformed_ok = ok && pi == m && ti == n;
+    *rescore_ok = cost == score;
+}
+
+void sw_validate(const char* cg, int len, const char* T, int m, int si, int ei, const char* P, int n,
+                 int sj, int ej, const ga_sw_scoring& sc, int score, bool* rescore_ok, bool* wellformed_ok)
+{
+    int i = si, j = sj, total = 0, gap = 0;   // gap > 0: run of I, < 0: run of D
+    bool ok = true;
+    auto close = [&] {
+        if (gap) {
+            const int L = gap > 0 ? gap : -gap;
+            total -= sc.gap_open + (L - 1) * sc.gap_extend;
+            gap = 0;
+        }
+    };
+    for (int q = 0; q < len; ++q) {
+        const char op = cg[q];
+        if (op == 'M' || op == 'X') {
+            close();
+            if (i > ei || j > ej || i >= m || j >= n || ((T[i] == P[j]) != (op == 'M'))) ok = false;
+            total += op == 'M' ? sc.match : sc.mismatch;
+            ++i;
+            ++j;
+        } else if (op == 'I') {
+            if (gap < 0) close();
+            if (i > ei || i >= m) ok = false;
+            ++i;
+            ++gap;
+        } else if (op == 'D') {
+            if (gap > 0) close();
+            if (j > ej || j >= n) ok = false;
+            ++j;
+            --gap;
+        } else {
+            ok = false;
+        }
+    }
+    close();
+    ok = ok && i == ei + 1 && j == ej + 1;
+    *wellformed_ok = ok;
+    *rescore_ok = ok && total == score;
+}
+
+}  // namespace ga
+
+// ================================================================== C ABI ==
+using namespace ga;
+
+static const char* E_CIGBUF = "cigar buffer is smaller than the batch needs";
+
+extern "C" {
+
+int64_t ga_align_cigar_bytes(const ga_align_request* reqs, int32_t n)
+{
+    int64_t s = 0;
+    for (int32_t i = 0; i < n; ++i) s += std::max(0, reqs[i].pattern_len) + (int64_t)std::max(0, reqs[i].text_len);
+    return s;
+}
+
+int64_t ga_align_sw_cigar_bytes(const ga_sw_request* reqs, int32_t n)
+{
+    int64_t s = 0;
+    for (int32_t i = 0; i < n; ++i) s += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
+    return s;
+}
+
+static void set_info(ga_batch_info* info, int32_t st, const char* e, int32_t res, int32_t unres)
+{
+    if (!info) return;
+    info->status = st;
+    info->error = e;
+    info->resolved_count = res;
+    info->unresolved_count = unres;
+    info->reserved = 0;
+}
+
+int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_result* results,
+                          char* cigar_buf, int64_t cigar_buf_bytes, const ga_options* opt,
+                          ga_batch_info* info)
+{
+    for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
+    const int32_t max_smax = (opt && opt->max_smax > 0) ? opt->max_smax : GA_MAX_SMAX;
+    bool any_cigar = false;
+    for (int32_t i = 0; i < n; ++i) any_cigar |= reqs[i].with_cigar != 0;
+    const char* err = nullptr;
+    std::atomic<int32_t> resolved{0};
+    auto fin = [&](int64_t lo, int64_t hi, const WfaView& v) {
+        int32_t res = 0;
+        for (int64_t i = lo; i < hi; ++i) {
+            ga_align_result& r = results[i];
+            r.score = v.score[i];
+            r.resolved = r.score >= 0;
+            res += r.resolved;
+            if (v.trace && r.resolved && v.len[i] > 0) {
+                const int64_t at = v.slot_end[i] - v.len[i];
+                std::memcpy(cigar_buf + at, v.cig + at, (size_t)v.len[i]);
+                r.cigar_offset = at;
+                r.cigar_len = v.len[i];
+                bool rs = false, wf = false;
+                wfa_validate(cigar_buf + at, v.len[i], r.score, reqs[i].pattern, reqs[i].pattern_len,
+                             reqs[i].text, reqs[i].text_len, &rs, &wf);
+                r.rescore_ok = rs;
+                r.wellformed_ok = wf;
+            }
+        }
+        resolved.fetch_add(res);
+    };
+    int32_t st;
+    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < ga_align_cigar_bytes(reqs, n))) {
+        // the reference's request checks come first, then the buffer contract
+        st = wfa_check(reqs, n, max_smax, &err);
+        if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
+        set_info(info, st, err, 0, 0);
+        return st;
+    }
+    st = wfa_batch(reqs, n, max_smax, opt && opt->learned, fin, &err);
+    if (st != GA_OK) {
+        for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
+        set_info(info, st, err, 0, 0);
+        return st;
+    }
+    set_info(info, GA_OK, nullptr, resolved.load(), n - resolved.load());
+    return GA_OK;
+}
+
+int32_t ga_align_batch(const ga_align_request* reqs, int32_t n, ga_align_result* results,
+                       char* cigar_buf, int64_t cigar_buf_bytes, ga_batch_info* info)
+{
+    return ga_align_batch_ex(reqs, n, results, cigar_buf, cigar_buf_bytes, nullptr, info);
+}
+
+int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result* results,
+                             char* cigar_buf, int64_t cigar_buf_bytes, const ga_options* opt,
+                             ga_batch_info* info)
+{
+    const ga_sw_result dflt{-1, 0, -1, -1, -1, -1, 0, 0, 0, 0, 0};
+    for (int32_t i = 0; i < n; ++i) results[i] = dflt;
+    int64_t limit = GA_SW_MAX_TRACE_CELLS;
+    if (opt && opt->trace_cell_limit != 0) limit = opt->trace_cell_limit;
+    bool any_cigar = false;
+    for (int32_t i = 0; i < n; ++i) any_cigar |= reqs[i].with_cigar != 0;
+    const char* err = nullptr;
+    std::atomic<int32_t> resolved{0};
+    auto fin = [&](int64_t lo, int64_t hi, const SwView& v) {
+        int32_t res = 0;
+        for (int64_t i = lo; i < hi; ++i) {
+            ga_sw_result& r = results[i];
+            const int s = v.score[i];
+            if (s < 0) {                            // declared size limit
+                if (v.trace) r.too_large = 1;
+                continue;
+            }
+            r.score = s;
+            r.resolved = 1;
+            ++res;
+            r.end_i = v.pos[4 * i + 2];
+            r.end_j = v.pos[4 * i + 3];
+            if (s == 0) { r.rescore_ok = r.wellformed_ok = 1; continue; }
+            if (!v.trace || !reqs[i].with_cigar) continue;
+            r.start_i = v.pos[4 * i];
+            r.start_j = v.pos[4 * i + 1];
+            const int len = v.len[i];
+            if (len > 0) {
+                const int64_t at = v.slot_end[i] - len;
+                std::memcpy(cigar_buf + at, v.cig + at, (size_t)len);
+                r.cigar_offset = at;
+                r.cigar_len = len;
+                bool rs = false, wf = false;
+                sw_validate(cigar_buf + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
+                            reqs[i].pattern, reqs[i].pattern_len, r.start_j, r.end_j, reqs[i].scoring, s,
+                            &rs, &wf);
+                r.rescore_ok = rs;
+                r.wellformed_ok = wf;
+            }
+        }
+        resolved.fetch_add(res);
+    };
+    int32_t st;
+    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < ga_align_sw_cigar_bytes(reqs, n))) {
+        st = sw_check(reqs, n, &err);
+        if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
+    } else {
+        st = sw_batch(reqs, n, limit, fin, &err);
+    }
+    if (st != GA_OK) {
+        for (int32_t i = 0; i < n; ++i) results[i] = dflt;
+        set_info(info, st, err, 0, 0);
+        return st;
+    }
+    set_info(info, GA_OK, nullptr, resolved.load(), n - resolved.load());
+    return GA_OK;
+}
+
+int32_t ga_align_sw_batch(const ga_sw_request* reqs, int32_t n, ga_sw_result* results, char* cigar_buf,
+                          int64_t cigar_buf_bytes, ga_batch_info* info)
+{
+    return ga_align_sw_batch_ex(reqs, n, results, cigar_buf, cigar_buf_bytes, nullptr, info);
+}
+
+// ------------------------------------------------------ device-resident --
+int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int32_t* out_score,
+                      int32_t* out_len, char* out_cigar, void* stream, const char** err)
+{
+    const char* e = nullptr;
+    if (!b || b->n < 0 || smax < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off ||
+                                                     !b->b_len || !out_score || (trace && (!out_len || !out_cigar || !b->out_off))))) {
+        if (err) *err = "invalid device batch";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (((uintptr_t)b->seq & 15) != 0) {
+        if (err) *err = "device batch arena must be 16-byte aligned";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (b->n == 0) return GA_OK;
+    Ctx* c = acquire_ctx(&e);
+    if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const int max_slots = wfa_max_slots(smax, trace != 0, c->sm_count);
+    int slots = (int)std::min<int64_t>(max_slots, ((int64_t)b->n + 3) / 4 * 4);
+    const int64_t stack_slot = (int64_t)(smax + 1) * (smax + 1);
+    if (trace) slots = (int)std::min<int64_t>(slots, std::max<int64_t>(4, ((int64_t)16 << 30) / (stack_slot * 4) / 4 * 4));
+    Carve k(nullptr);
+    k.take<uint64_t>(b->seq_bytes / 32 + 2);
+    k.take<uint8_t>(2 * (size_t)b->n);
+    k.take<int32_t>(64, 256);
+    if (trace) k.take<int32_t>((size_t)slots * stack_slot);
+    if (!ensure_dev(c, k.off)) { release_ctx(c); if (err) *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    Carve d(c->dev);
+    uint64_t* packed = d.take<uint64_t>(b->seq_bytes / 32 + 2);
+    uint8_t* pure = d.take<uint8_t>(2 * (size_t)b->n);
+    int32_t* ctr = d.take<int32_t>(64, 256);
+    int32_t* stk = trace ? d.take<int32_t>((size_t)slots * stack_slot) : nullptr;
+    cudaMemsetAsync(ctr, 0, 64 * sizeof(int32_t), st);
+    PairDesc D;
+    D.seq = b->seq; D.packed = packed; D.pure = pure;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = b->n;
+    WfaArgs A;
+    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
+    A.out_score = out_score; A.out_len = out_len; A.out_cigar = out_cigar;
+    A.stack = stk; A.stack_slot = stack_slot; A.counter = ctr; A.err = ctr + 1;
+    int32_t rc = GA_OK;
+    if (launch_pack(D, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = E_LAUNCH;
+        rc = GA_DEVICE_ERROR;
+    }
+    if (stream) {
+        cudaEventRecord(c->done, st);
+        c->pending = true;
+    } else if (cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = E_SYNC;
+        rc = GA_DEVICE_ERROR;
+    }
+    release_ctx(c);
+    return rc;
+}
+
+int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, int64_t cell_limit,
+                     int32_t* out_score, int32_t* out_pos, int32_t* out_len, char* out_cigar, void* stream,
+                     const char** err)
+{
+    const char* e = nullptr;
+    if (!b || b->n < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len ||
+                                         !out_score || !out_pos || (trace && (!out_len || !out_cigar || !b->out_off))))) {
+        if (err) *err = "invalid device batch";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (b->n == 0) return GA_OK;
+    // the lengths live on the device; plan from a host copy
+    std::vector<int32_t> al(b->n), bl(b->n);
+    if (cudaMemcpy(al.data(), b->a_len, sizeof(int32_t) * b->n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(bl.data(), b->b_len, sizeof(int32_t) * b->n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = E_D2H;
+        return GA_DEVICE_ERROR;
+    }
+    std::vector<int32_t> work[3];
+    const int widths[3] = {8, 16, 32};
+    std::vector<int32_t> too_big;
+    for (int32_t i = 0; i < b->n; ++i) {
+        if (cell_limit >= 0 && al[i] > 0 && bl[i] > 0 && ((int64_t)al[i] + 1) * ((int64_t)bl[i] + 1) > cell_limit) {
+            too_big.push_back(i);
+            continue;
+        }
+        const int C = sw_width_for(bl[i]);
+        work[C == 8 ? 0 : (C == 16 ? 1 : 2)].push_back(i);
+    }
+    int64_t dir_slot[3] = {0, 0, 0}, edge_slot = 2;
+    for (int w = 0; w < 3; ++w) {
+        std::sort(work[w].begin(), work[w].end(), [&](int32_t x, int32_t y) {
+            const int64_t cx = (int64_t)(al[x] + 31) * bl[x], cy = (int64_t)(al[y] + 31) * bl[y];
+            return cx != cy ? cx > cy : x < y;
+        });
+        for (int32_t i : work[w]) {
+            dir_slot[w] = std::max(dir_slot[w], sw_dir_words(al[i], bl[i], widths[w]));
+            edge_slot = std::max<int64_t>(edge_slot, 2 * (int64_t)al[i]);
+        }
+        dir_slot[w] = (dir_slot[w] + 3) / 4 * 4;
+    }
+    Ctx* c = acquire_ctx(&e);
+    if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    int slots[3] = {0, 0, 0};
+    int64_t dir_words = 0, max_slots_all = 4;
+    for (int w = 0; w < 3; ++w) {
+        if (work[w].empty()) continue;
+        int s = sw_max_slots(widths[w], trace != 0, c->sm_count);
+        s = (int)std::min<int64_t>(s, ((int64_t)work[w].size() + 3) / 4 * 4);
+        if (trace) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, ((int64_t)48 << 30) / (dir_slot[w] * 4) / 4 * 4));
+        slots[w] = s;
+        if (trace) dir_words = std::max(dir_words, (int64_t)s * dir_slot[w]);
+        max_slots_all = std::max<int64_t>(max_slots_all, s);
+    }
+    const int64_t nwork = (int64_t)work[0].size() + work[1].size() + work[2].size();
+    auto layout = [&](char* base, int32_t** wk, int32_t** ctr, int32_t** edge, uint32_t** dirs, int32_t** tb) {
+        Carve k(base);
+        *wk = k.take<int32_t>(nwork + 1);
+        *tb = k.take<int32_t>(too_big.size() + 1);
+        *ctr = k.take<int32_t>(64, 256);
+        *edge = k.take<int32_t>((size_t)max_slots_all * edge_slot);
+        *dirs = trace ? k.take<uint32_t>((size_t)dir_words) : nullptr;
+        return k.off;
+    };
+    int32_t *dwork, *dctr, *dedge, *dtb;
+    uint32_t* ddirs;
+    const size_t need = layout(nullptr, &dwork, &dctr, &dedge, &ddirs, &dtb);
+    if (!ensure_dev(c, need)) { release_ctx(c); if (err) *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    layout(c->dev, &dwork, &dctr, &dedge, &ddirs, &dtb);
+    std::vector<int32_t> hw;
+    hw.reserve(nwork);
+    for (int w = 0; w < 3; ++w) hw.insert(hw.end(), work[w].begin(), work[w].end());
+    if (!hw.empty()) cudaMemcpyAsync(dwork, hw.data(), sizeof(int32_t) * hw.size(), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+    cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * b->n, st);
+    cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)b->n, st);
+    if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * b->n, st);
+    // too-large pairs: score -2
+    if (!too_big.empty()) {
+        std::vector<int32_t> m2(1, -2);
+        for (int32_t i : too_big) cudaMemcpyAsync(out_score + i, &m2[0], sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);
+    }
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = b->n;
+    int32_t rc = GA_OK;
+    int64_t wbase = 0;
+    for (int w = 0; w < 3; ++w) {
+        if (work[w].empty()) continue;
+        SwArgs A;
+        A.D = D; A.work = dwork + wbase; A.nwork = (int32_t)work[w].size();
+        A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
+        A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
+        A.dirs = ddirs; A.dir_slot = dir_slot[w]; A.edge = dedge; A.edge_slot = edge_slot;
+        A.counter = dctr + w; A.err = dctr + 8;
+        if (launch_sw(A, widths[w], trace != 0, slots[w], st) != cudaSuccess) {
+            cudaGetLastError();
+            if (err) *err = E_LAUNCH;
+            rc = GA_DEVICE_ERROR;
+            break;
+        }
+        wbase += (int64_t)work[w].size();
+    }
+    if (stream) {
+        cudaEventRecord(c->done, st);
+        c->pending = true;
+    } else if (cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = E_SYNC;
+        rc = GA_DEVICE_ERROR;
+    }
+    release_ctx(c);
+    return rc;
+}
+
+// ------------------------------------------------------------ provenance --
+const char* ga_backend_name(void) { return "cuda-sm_103a"; }
+
+const char* ga_device_name(void)
+{
+    static std::once_flag once;
+    static char name[256] = "none";
+    std::call_once(once, [] {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) == cudaSuccess && n > 0) {
+            cudaDeviceProp p;
+            if (cudaGetDeviceProperties(&p, 0) == cudaSuccess) std::snprintf(name, sizeof(name), "%s", p.name);
+        }
+        cudaGetLastError();
+    });
+    return name;
+}
+
+int32_t ga_device_available(void)
+{
+    int n = 0;
+    const bool ok = cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+    cudaGetLastError();
+    return ok ? 1 : 0;
+}
+
+int64_t ga_kernel_launches(void) { return g_launches.load(); }
+
+void ga_last_transfer_bytes(int64_t* h2d, int64_t* d2h)
+{
+    if (h2d) *h2d = t_h2d;
+    if (d2h) *d2h = t_d2h;
+}
+
+void ga_profile(int32_t on)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (on) {
+        for (int k = 0; k < K_COUNT; ++k) { g_prof_ms[k] = 0; g_prof_n[k] = 0; }
+        g_prof_done.clear();
+    }
+    g_prof_on = on != 0;
+}
+
+int32_t ga_profile_read(int32_t kernel_id, double* total_ms, int64_t* launches)
+{
+    if (kernel_id < 0 || kernel_id >= K_COUNT) return GA_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (ProfRec& r : g_prof_done) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            g_prof_ms[r.id] += ms;
+            g_prof_n[r.id] += 1;
+        }
+        cudaGetLastError();
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    g_prof_done.clear();
+    if (total_ms) *total_ms = g_prof_ms[kernel_id];
+    if (launches) *launches = g_prof_n[kernel_id];
+    return GA_OK;
+}
+
+const char* ga_profile_kernel_name(int32_t kernel_id)
+{
+    static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
+                                         "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
+                                         "kmer_sketch", "mlp"};
+    return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
+}
+
+void ga_debug_fail_next(int32_t step) { g_fail_next.store(step); }
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// engine.hpp -- internal C++ interface of the host engine (shared by the C ABI
+// in engine.cu and the C++ drop-in API in api.cpp).
+#pragma once
+
+#include <cstdint>
+#include <functional>
+
+#include "../../include/genoaligner_gb300.h"
+
+namespace ga {
+
+// Run fn(lo, hi) over [0, n) in chunks of `grain` on the host thread pool
+// (the calling thread participates).
+void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, int64_t)>& fn);
+
+// Per-pair outputs of a WFA batch, valid during the finish callback.  The
+// CIGAR of pair i is cig[slot_end[i] - len[i] .. slot_end[i]).
+struct WfaView {
+    const int32_t* score;
+    const int32_t* len;
+    const char* cig;
+    const int64_t* slot_end;
+    bool trace;
+};
+using WfaFinish = std::function<void(int64_t lo, int64_t hi, const WfaView& v)>;
+
+// The reference's request checks, in its order and with its messages
+// (src/api/api.cpp:246-266 and 600-616 with sw_scheme_ok :515-536).
+int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err);
+int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err);
+
+// The align_batch pipeline: validation, planning, transfer, kernels, and the
+// finish callback over every pair (in parallel).  Returns a GA_* status; on
+// failure *err is a static string and the callback has not run.
+int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
+                  const WfaFinish& fin, const char** err);
+
+struct SwView {
+    const int32_t* score;     // -1 = too large
+    const int32_t* pos;       // start_i, start_j, end_i, end_j per pair
+    const int32_t* len;
+    const char* cig;
+    const int64_t* slot_end;
+    bool trace;
+};
+using SwFinish = std::function<void(int64_t lo, int64_t hi, const SwView& v)>;
+
+int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
+                 const char** err);
+
+// Result checks computed in the library (the reference's validate and
+// sw_validate semantics, src/api/api.cpp:84-156).
+void wfa_validate(const char* cigar, int len, int score, const char* P, int m, const char* T, int n,
+                  bool* rescore_ok, bool* wellformed_ok);
+void sw_validate(const char* cigar, int len, const char* T, int m, int si, int ei, const char* P,
+                 int n, int sj, int ej, const ga_sw_scoring& sc, int score, bool* rescore_ok,
+                 bool* wellformed_ok);
+
+}  // namespace ga

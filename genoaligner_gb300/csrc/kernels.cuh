@@ -1,0 +1,49 @@
+// kernels.cuh -- argument blocks and launchers of the device kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace ga {
+
+struct WfaArgs {
+    PairDesc D;              // a = pattern, b = text
+    int32_t smax;
+    int32_t trace;
+    int32_t* out_score;
+    int32_t* out_len;
+    char* out_cigar;
+    int32_t* stack;          // per warp slot: (smax+1)^2 offsets (trace only)
+    int64_t stack_slot;
+    int32_t* counter;        // next pair index
+    int32_t* err;
+};
+
+struct SwArgs {
+    PairDesc D;              // a = text (rows), b = pattern (columns)
+    const int32_t* work;     // pair indices handled by this launch
+    int32_t nwork;
+    int32_t match, mismatch, gap_open, gap_extend;
+    int32_t* out_score;
+    int32_t* out_pos;        // 4 per pair: start_i, start_j, end_i, end_j
+    int32_t* out_len;
+    char* out_cigar;
+    uint32_t* dirs;          // per warp slot, dir_slot words
+    int64_t dir_slot;
+    int32_t* edge;           // per warp slot, 2 ints per row (band edge H, E)
+    int64_t edge_slot;
+    int32_t* counter;
+    int32_t* err;
+};
+
+cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st);
+
+size_t wfa_smem_bytes(int smax);
+int wfa_max_slots(int smax, bool trace, int sm_count);
+cudaError_t launch_wfa(const WfaArgs& A, int slots, cudaStream_t st);
+
+int64_t sw_dir_words(int m, int n, int C);
+int sw_width_for(int n);
+int sw_max_slots(int C, bool trace, int sm_count);
+cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
+
+}  // namespace ga

@@ -1,0 +1,268 @@
+// wfa.cu -- sequence packing and the WFA edit-distance kernels (sm_103a).
+//
+// Algorithm: the wavefront recurrence of the reference's wfa_trace_kernel /
+// wfa_score_kernel_flat (include/genoaligner/backend/wfa_kernel.hip:119-145,
+// 467-592; wfa_score_flat.hip:63-140).  Offsets are text coordinates h,
+// v = h - k, the alignment diagonal is n - m; compute-next takes
+// max(del, max(ins, mism) + 1) and clips to NULL past either end before
+// extending; the walk prefers mismatch on ties, then insertion, then deletion
+// (strictly).  These steps are fixed by the result contract -- the scores and
+// CIGAR strings must be the reference's -- so they are kept, expressed for a
+// warp:
+//
+//   * one warp per pair, persistent: warps pull pair indices from a counter,
+//     so long and short pairs balance across the grid;
+//   * the diagonals of wavefront s are spread over the 32 lanes; the previous
+//     and current wavefront live in a per-warp shared-memory ping-pong;
+//   * extension compares 32 bases per step on the 2-bit arena (XOR +
+//     find-first-set); pairs with any byte outside ACGT compare 8 raw bytes
+//     per step instead, so byte-equality semantics hold for N, lowercase, etc.;
+//   * for CIGARs every wavefront is also written to a per-warp triangular stack
+//     in global memory (wavefront s at s*s, 2s+1 entries); the walk then runs
+//     warp-uniformly over it and writes the CIGAR back to front into the
+//     pair's output slot, runs of matches written by all lanes at once.
+#include "kernels.cuh"
+
+namespace ga {
+
+// ---------------------------------------------------------------- packing --
+// One warp per sequence: 32 ASCII bytes -> one 64-bit word of 2-bit codes
+// (A=0 C=1 G=2 T=3, little-endian), plus a purity flag per sequence.  The
+// sequence set is the a-sides (q < n) followed by the b-sides (q >= n).
+__global__ void __launch_bounds__(256) pack2_kernel(PairDesc D, uint64_t* __restrict__ packed,
+                                                    uint8_t* __restrict__ pure)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < 2 * D.n; q += nwarps) {
+        const bool is_a = q < D.n;
+        const int p = is_a ? q : q - D.n;
+        const int64_t off = is_a ? D.a_off[p] : D.b_off[p];
+        const int len = is_a ? D.a_len[p] : D.b_len[p];
+        const int words = (len + 31) >> 5;
+        bool bad = false;
+        for (int w = lane; w < words; w += 32) {
+            const uint4* src = reinterpret_cast<const uint4*>(D.seq + off + 32 * (int64_t)w);
+            const uint4 x0 = __ldg(src), x1 = __ldg(src + 1);
+            const uint32_t parts[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+            const int valid = min(32, len - 32 * w);
+            uint64_t word = 0;
+#pragma unroll
+            for (int b = 0; b < 32; ++b) {
+                const uint32_t c = (parts[b >> 2] >> (8 * (b & 3))) & 0xffu;
+                // A=0x41 C=0x43 G=0x47 T=0x54 map to 0,1,2,3 under ((c>>1)^(c>>2))&3
+                const uint64_t code = ((c >> 1) ^ (c >> 2)) & 3u;
+                const bool acgt = (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
+                if (b < valid) {
+                    bad |= !acgt;
+                    word |= code << (2 * b);
+                }
+            }
+            packed[(off >> 5) + w] = word;
+        }
+        bad = __any_sync(FULL, bad);
+        if (lane == 0) pure[q] = bad ? 0 : 1;
+    }
+}
+
+// ------------------------------------------------------------------- WFA --
+// Cooperative emission of a run of `len` copies of `c` ending just before
+// slot[pos]; returns the new (lower) position.
+__device__ __forceinline__ int emit_run(char* slot, int pos, int len, char c, int lane, int* err)
+{
+    if (len <= 0) return pos;
+    if (len > pos) {
+        if (lane == 0) atomicOr(err, ERR_CIGAR_OVERFLOW);
+        len = pos;
+    }
+    for (int q = lane; q < len; q += 32) slot[pos - len + q] = c;
+    return pos - len;
+}
+
+template <bool TRACE, int BITS>
+__device__ void wfa_pair(const WfaArgs& A, int p, const uint64_t* __restrict__ P,
+                         const uint64_t* __restrict__ T, int m, int n, int32_t* wf0, int32_t* wf1,
+                         int32_t* stk, int lane)
+{
+    const int smax = A.smax;
+    const int WS = 2 * smax + 3;
+    const int base = smax + 1;                 // slot of diagonal 0
+    for (int t = lane; t < WS; t += 32) { wf0[t] = WFA_NULL; wf1[t] = WFA_NULL; }
+    const int off0 = match_run<BITS>(P, T, 0, 0, m, n);   // computed redundantly by every lane
+    __syncwarp();
+    if (lane == 0) {
+        wf0[base] = off0;
+        if (TRACE) stk[0] = off0;
+    }
+    const int kfinal = n - m;
+    int score = -1;
+    if (kfinal == 0 && off0 >= n) {
+        score = 0;
+    } else {
+        int32_t* prev = wf0;
+        int32_t* cur = wf1;
+        for (int s = 1; s <= smax; ++s) {
+            __syncwarp();
+            for (int k = lane - s; k <= s; k += 32) {
+                const int ins = prev[base + k - 1];
+                const int del = prev[base + k + 1];
+                const int mis = prev[base + k];
+                int x = max(del, max(ins, mis) + 1);
+                if (!wfa_live(x) || x > n || x - k > m) x = WFA_NULL;
+                else x += match_run<BITS>(P, T, x - k, x, m, n);
+                cur[base + k] = x;
+                if (TRACE) stk[s * s + s + k] = x;
+            }
+            __syncwarp();
+            if (kfinal >= -s && kfinal <= s) {
+                const int fo = cur[base + kfinal];
+                if (wfa_live(fo) && fo >= n) { score = s; break; }
+            }
+            int32_t* t = prev; prev = cur; cur = t;
+        }
+    }
+    if (!TRACE || score < 0) {
+        if (lane == 0) {
+            A.out_score[p] = score;
+            if (A.out_len) A.out_len[p] = 0;
+        }
+        return;
+    }
+    char* slot = A.out_cigar + A.D.out_off[p];
+    int pos = m + n;
+    if (score == 0) {
+        pos = emit_run(slot, pos, n, 'M', lane, A.err);
+    } else {
+        __syncwarp();                      // stack writes of every lane are visible below
+        int s = score, k = kfinal;
+        int off = stk[s * s + s + k];
+        int h = off, v = off - k;
+        pos = emit_run(slot, pos, v - m, 'D', lane, A.err);
+        pos = emit_run(slot, pos, h - n, 'I', lane, A.err);
+        v = min(v, m);
+        h = min(h, n);
+        while (v > 0 && h > 0 && s > 0) {
+            const int sp = s - 1;
+            const int32_t* W = stk + sp * sp + sp;     // W[k] = offset of diagonal k at score sp
+            const int c_mis = (k >= -sp && k <= sp) ? W[k] + 1 : WFA_NULL;
+            const int c_ins = (k - 1 >= -sp && k - 1 <= sp) ? W[k - 1] + 1 : WFA_NULL;
+            const int c_del = (k + 1 >= -sp && k + 1 <= sp) ? W[k + 1] : WFA_NULL;
+            int best = WFA_NULL;
+            char op = 0;
+            if (wfa_live(c_mis) && c_mis >= best) { best = c_mis; op = 'X'; }
+            if (wfa_live(c_ins) && c_ins > best)  { best = c_ins; op = 'I'; }
+            if (wfa_live(c_del) && c_del > best)  { best = c_del; op = 'D'; }
+            if (!op) break;
+            pos = emit_run(slot, pos, off - best, 'M', lane, A.err);
+            pos = emit_run(slot, pos, 1, op, lane, A.err);
+            off = best;
+            if (op == 'X')      { off -= 1; }
+            else if (op == 'I') { k -= 1; off -= 1; }
+            else                { k += 1; }
+            h = off;
+            v = off - k;
+            --s;
+        }
+        if (v > 0 && h > 0) {
+            const int run = min(v, h);
+            pos = emit_run(slot, pos, run, 'M', lane, A.err);
+            v -= run;
+            h -= run;
+        }
+        pos = emit_run(slot, pos, v, 'D', lane, A.err);
+        pos = emit_run(slot, pos, h, 'I', lane, A.err);
+    }
+    if (lane == 0) {
+        A.out_score[p] = score;
+        A.out_len[p] = m + n - pos;
+    }
+}
+
+template <bool TRACE>
+__global__ void __launch_bounds__(128) wfa_kernel(WfaArgs A)
+{
+    extern __shared__ int32_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int WS = 2 * A.smax + 3;
+    int32_t* wf0 = smem + wib * 2 * WS;
+    int32_t* wf1 = wf0 + WS;
+    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    int32_t* stk = TRACE ? A.stack + slot * A.stack_slot : nullptr;
+    for (;;) {
+        int p = 0;
+        if (lane == 0) p = atomicAdd(A.counter, 1);
+        p = __shfl_sync(FULL, p, 0);
+        if (p >= A.D.n) break;
+        __syncwarp();
+        const int m = A.D.a_len[p];       // pattern
+        const int n = A.D.b_len[p];       // text
+        if (m <= 0 || n <= 0) {
+            // one side empty: the score is the other length, whatever smax is;
+            // the CIGAR is all insertions (empty pattern) or all deletions
+            // (wfa_kernel.hip:480-502)
+            const int len = m <= 0 ? max(n, 0) : m;
+            if (TRACE) emit_run(A.out_cigar + A.D.out_off[p], len, len, m <= 0 ? 'I' : 'D', lane, A.err);
+            if (lane == 0) {
+                A.out_score[p] = len;
+                if (A.out_len) A.out_len[p] = TRACE ? len : 0;
+            }
+            continue;
+        }
+        const bool pure = A.D.pure[p] && A.D.pure[A.D.n + p];
+        if (pure) {
+            const uint64_t* P = A.D.packed + (A.D.a_off[p] >> 5);
+            const uint64_t* T = A.D.packed + (A.D.b_off[p] >> 5);
+            wfa_pair<TRACE, 2>(A, p, P, T, m, n, wf0, wf1, stk, lane);
+        } else {
+            const uint64_t* P = reinterpret_cast<const uint64_t*>(A.D.seq + A.D.a_off[p]);
+            const uint64_t* T = reinterpret_cast<const uint64_t*>(A.D.seq + A.D.b_off[p]);
+            wfa_pair<TRACE, 8>(A, p, P, T, m, n, wf0, wf1, stk, lane);
+        }
+    }
+}
+
+// --------------------------------------------------------------- launchers --
+cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    const int warps = 2 * D.n;
+    int blocks = (warps + 7) / 8;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    launch_begin(K_PACK, st);
+    pack2_kernel<<<blocks, 256, 0, st>>>(D, packed, pure);
+    launch_end(K_PACK, st);
+    return cudaGetLastError();
+}
+
+size_t wfa_smem_bytes(int smax) { return (size_t)4 * 2 * (2 * smax + 3) * sizeof(int32_t); }
+
+int wfa_max_slots(int smax, bool trace, int sm_count)
+{
+    int per_sm = 0;
+    const size_t smem = wfa_smem_bytes(smax);
+    if (trace) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_kernel<true>, 128, smem);
+    } else {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_kernel<false>, 128, smem);
+    }
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * sm_count * 4;
+}
+
+cudaError_t launch_wfa(const WfaArgs& A, int slots, cudaStream_t st)
+{
+    if (A.D.n <= 0) return cudaSuccess;
+    const int blocks = (slots + 3) / 4;
+    const size_t smem = wfa_smem_bytes(A.smax);
+    const int id = A.trace ? K_WFA_TRACE : K_WFA_SCORE;
+    launch_begin(id, st);
+    if (A.trace) wfa_kernel<true><<<blocks, 128, smem, st>>>(A);
+    else         wfa_kernel<false><<<blocks, 128, smem, st>>>(A);
+    launch_end(id, st);
+    return cudaGetLastError();
+}
+
+}  // namespace ga

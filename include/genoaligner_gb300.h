@@ -1,0 +1,233 @@
+/*
+ * genoaligner_gb300.h -- C ABI of the GB300-native batched pairwise aligner.
+ *
+ * This is the drop-in boundary for the reference's pairwise API
+ * (include/genoaligner/api.hpp of alrobles/genoaligner).  Plain C: pointers,
+ * sizes and fixed-layout structs only, so any FFI (ctypes, cgo, JNI, N-API)
+ * can bind it.  The C++ API in include/genoaligner/api.hpp is implemented on
+ * top of the same engine and keeps the reference's declarations.
+ *
+ * Conventions, shared by every entry point:
+ *   - status codes map 1:1 onto the reference's Status enums
+ *     (api.hpp:158, 306): GA_OK, GA_INVALID_ARGUMENT, GA_DEVICE_ERROR;
+ *   - error strings are static, non-NULL iff status != GA_OK (api.hpp:160);
+ *   - invalid_argument is decided before any device work and fails the whole
+ *     batch; on device_error every result is reset to its defaults and both
+ *     counters are 0 (src/api/api.cpp:331-339, 724-732);
+ *   - inputs are borrowed for the duration of the call; outputs go to
+ *     caller-owned arrays; nothing is retained;
+ *   - concurrent calls on disjoint inputs are safe: each call runs on its own
+ *     CUDA stream with its own buffers.
+ */
+#ifndef GENOALIGNER_GB300_H
+#define GENOALIGNER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GA_OK               0
+#define GA_INVALID_ARGUMENT 1
+#define GA_DEVICE_ERROR     2
+
+/* Largest smax the drop-in entry accepts (src/api/api.cpp:227). */
+#define GA_MAX_SMAX 511
+/* Per-pair direction-table limit of the drop-in SW entry, in cells
+ * (include/genoaligner/api.hpp:256). */
+#define GA_SW_MAX_TRACE_CELLS (1 << 26)
+
+/* ------------------------------------------------------------------ WFA -- */
+
+/* One pair to align; mirrors genoaligner::AlignRequest (api.hpp:81-88). */
+typedef struct ga_align_request {
+    const char* pattern;
+    int32_t     pattern_len;
+    int32_t     smax;          /* max edit distance searched (reference default 64) */
+    const char* text;
+    int32_t     text_len;
+    int32_t     with_cigar;    /* 0 = score only */
+} ga_align_request;
+
+/* Result of one pair; mirrors genoaligner::AlignResult (api.hpp:64-76).  The
+ * CIGAR (one char per op over M,X,I,D) is cigar_buf[cigar_offset ..
+ * cigar_offset + cigar_len). */
+typedef struct ga_align_result {
+    int32_t score;             /* edit distance; -1 = unresolved (distance > smax) */
+    int32_t resolved;
+    int32_t rescore_ok;
+    int32_t wellformed_ok;
+    int64_t cigar_offset;
+    int32_t cigar_len;
+    int32_t reserved;
+} ga_align_result;
+
+/* Batch outcome; mirrors the counters and status of BatchResult
+ * (api.hpp:148-163) and SWBatchResult (api.hpp:301-311). */
+typedef struct ga_batch_info {
+    int32_t     status;
+    int32_t     resolved_count;
+    int32_t     unresolved_count;
+    int32_t     reserved;
+    const char* error;
+} ga_batch_info;
+
+/* Bytes of CIGAR storage a batch needs: sum over requests of
+ * pattern_len + text_len (negative lengths count as 0). */
+int64_t ga_align_cigar_bytes(const ga_align_request* reqs, int32_t n);
+
+/* Replaces genoaligner::align_batch (api.hpp:164, src/api/api.cpp:234-497).
+ * One smax for the whole batch, the minimum over the requests; smax outside
+ * [0, 511] fails the batch; any with_cigar request puts every resolved pair on
+ * the CIGAR path.  results[n]; cigar_buf of ga_align_cigar_bytes() bytes (may
+ * be NULL when no request has with_cigar).  Returns the status. */
+int32_t ga_align_batch(const ga_align_request* reqs, int32_t n, ga_align_result* results,
+                       char* cigar_buf, int64_t cigar_buf_bytes, ga_batch_info* info);
+
+/* ------------------------------------------------------------------- SW -- */
+
+/* Affine scheme; mirrors genoaligner::SWScoring (api.hpp:246-251). */
+typedef struct ga_sw_scoring {
+    int32_t match;
+    int32_t mismatch;
+    int32_t gap_open;
+    int32_t gap_extend;
+} ga_sw_scoring;
+
+/* One pair to locally align; mirrors genoaligner::SWRequest (api.hpp:261-268).
+ * text is the row axis, pattern the column axis. */
+typedef struct ga_sw_request {
+    const char*   text;
+    int32_t       text_len;
+    int32_t       with_cigar;
+    const char*   pattern;
+    int32_t       pattern_len;
+    int32_t       reserved;
+    ga_sw_scoring scoring;
+} ga_sw_request;
+
+/* Result of one pair; mirrors genoaligner::SWAlignResult (api.hpp:273-294). */
+typedef struct ga_sw_result {
+    int32_t score;             /* >= 0 when resolved; -1 when not computed */
+    int32_t resolved;
+    int32_t start_i, start_j;  /* 0-based first aligned char of text / pattern */
+    int32_t end_i, end_j;      /* 0-based last aligned char */
+    int32_t rescore_ok;
+    int32_t wellformed_ok;
+    int32_t too_large;
+    int32_t cigar_len;
+    int64_t cigar_offset;
+} ga_sw_result;
+
+/* Bytes of CIGAR storage an SW batch needs: sum of text_len + pattern_len. */
+int64_t ga_align_sw_cigar_bytes(const ga_sw_request* reqs, int32_t n);
+
+/* Replaces genoaligner::align_sw_batch (api.hpp:312, src/api/api.cpp:584-847).
+ * One scoring scheme per batch; any with_cigar request runs the trace path for
+ * the batch; a pair whose (text_len+1)(pattern_len+1) exceeds 2^26 comes back
+ * too_large.  A score-only batch reports score and end cell only, with the end
+ * cell the reference's warp kernel reports. */
+int32_t ga_align_sw_batch(const ga_sw_request* reqs, int32_t n, ga_sw_result* results,
+                          char* cigar_buf, int64_t cigar_buf_bytes, ga_batch_info* info);
+
+/* ------------------------------------------------------ extension entries -- */
+
+/* Options of the extension entries (include/genoaligner/ext.hpp).  Zero
+ * fields take the defaults noted. */
+typedef struct ga_options {
+    int32_t max_smax;          /* accepted smax bound; 0 = 511 (the drop-in bound) */
+    int32_t learned;           /* 1 = route pairs by the learned cost model */
+    int64_t trace_cell_limit;  /* SW per-pair trace limit in cells; 0 = 2^26, <0 = none */
+    int32_t reserved[4];
+} ga_options;
+
+/* align_batch with the options above (no reference counterpart: the
+ * reference caps smax at 511).  Results identical to ga_align_batch whenever
+ * the options are the defaults. */
+int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_result* results,
+                          char* cigar_buf, int64_t cigar_buf_bytes, const ga_options* opt,
+                          ga_batch_info* info);
+
+/* align_sw_batch with the options above (no reference counterpart: the
+ * reference caps the trace at 2^26 cells per pair). */
+int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result* results,
+                             char* cigar_buf, int64_t cigar_buf_bytes, const ga_options* opt,
+                             ga_batch_info* info);
+
+/* -------------------------------------------------- device-resident entry -- */
+
+/* A batch whose sequences already sit in device memory (no reference
+ * counterpart; used when the data is produced on the device).  seq is one
+ * byte arena; sequence a of pair i is seq[a_off[i] .. a_off[i]+a_len[i]), b
+ * likewise.  Every offset must be a multiple of 32 and the arena must extend
+ * at least 64 bytes past the last sequence.  For WFA a = pattern, b = text;
+ * for SW a = text (rows), b = pattern (columns).  All arrays are device
+ * pointers.  out_off[i] is the byte offset of pair i's CIGAR slot in
+ * out_cigar (capacity a_len[i] + b_len[i]); the CIGAR is written at the END of
+ * the slot: out_cigar[out_off[i] + cap - len .. out_off[i] + cap). */
+typedef struct ga_device_batch {
+    const uint8_t* seq;
+    int64_t        seq_bytes;
+    const int64_t* a_off;
+    const int32_t* a_len;
+    const int64_t* b_off;
+    const int32_t* b_len;
+    const int64_t* out_off;
+    int32_t        n;
+    int32_t        reserved;
+} ga_device_batch;
+
+/* WFA over a device batch.  out_score[i] (-1 unresolved), out_len[i] (CIGAR
+ * length, 0 when trace == 0 or unresolved), out_cigar as above.  Enqueued on
+ * `stream` (a cudaStream_t; NULL = this call's own stream, synchronised before
+ * return).  Returns a status; `err` gets a static string on failure. */
+int32_t ga_wfa_device(const ga_device_batch* batch, int32_t smax, int32_t trace,
+                      int32_t* out_score, int32_t* out_len, char* out_cigar,
+                      void* stream, const char** err);
+
+/* SW over a device batch, score + end cell + start cell + CIGAR.
+ * out_pos[4*i .. 4*i+3] = start_i, start_j, end_i, end_j.  Pairs above
+ * trace_cell_limit cells (< 0: no limit) get out_score = -2 (too large). */
+int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_t trace,
+                     int64_t trace_cell_limit, int32_t* out_score, int32_t* out_pos,
+                     int32_t* out_len, char* out_cigar, void* stream, const char** err);
+
+/* ------------------------------------------------------------ provenance -- */
+
+/* Mirror backend_name / device_name / device_available (api.hpp:485-487). */
+const char* ga_backend_name(void);
+const char* ga_device_name(void);
+int32_t     ga_device_available(void);
+
+/* Kernel launches this library issued since load (for launch accounting). */
+int64_t ga_kernel_launches(void);
+
+/* Bytes the calling thread's last ga_align_batch / ga_align_sw_batch call
+ * copied host-to-device and device-to-host. */
+void ga_last_transfer_bytes(int64_t* h2d, int64_t* d2h);
+
+/* Per-kernel timing: ga_profile(1) resets the totals and records a CUDA event
+ * pair around every launch on its launch stream until ga_profile(0);
+ * ga_profile_read returns the summed device milliseconds and the launch count
+ * of one kernel id (0 .. 11, names from ga_profile_kernel_name). */
+void        ga_profile(int32_t on);
+int32_t     ga_profile_read(int32_t kernel_id, double* total_ms, int64_t* launches);
+const char* ga_profile_kernel_name(int32_t kernel_id);
+
+/* Integer-pipe throughput of this GPU, in lane-operations per second, from a
+ * microbenchmark kernel (variant 0: add + max in plain C; 1: __viaddmax_s32;
+ * 2: __vimax3_s32_relu).  The Smith-Waterman roofline is built on it. */
+int32_t ga_bench_int_peak(int32_t variant, double* lane_ops_per_s);
+
+/* Test hook: make the next batch call fail at the named host step
+ * (1 = device allocation, 2 = host-to-device copy, 3 = kernel launch,
+ * 4 = device-to-host copy; 0 = off).  The call then reports device_error with
+ * defaults in every result, as a real failure there would. */
+void ga_debug_fail_next(int32_t step);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GENOALIGNER_GB300_H */

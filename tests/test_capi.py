@@ -1,0 +1,100 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol the header
+declares, and refuses invalid batches before any device work, with the
+reference's messages."""
+import os
+import re
+
+import pytest
+
+from genoaligner_gb300 import api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "genoaligner_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)          # drop comments
+    return sorted(set(re.findall(r"\b(ga_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = api.load()
+    names = declared_symbols()
+    assert len(names) >= 13
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(api.EXPORTS) <= set(names)
+
+
+def test_provenance_without_device():
+    assert api.backend_name() == "cuda-sm_103a"
+    assert isinstance(api.device_name(), str)
+
+
+@pytest.mark.parametrize("smax", [512, -1])
+def test_wfa_smax_refused(smax):
+    b = api.align_batch([api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=smax)])
+    assert b.status == api.Status.invalid_argument
+    assert b.error == "smax out of range [0, 511]"
+    assert len(b.results) == 1 and b.results[0].score == -1
+
+
+def test_wfa_null_and_negative_refused():
+    b = api.align_batch([api.AlignRequest(None, 5, b"ACGT", 4, smax=8)])
+    assert b.status == api.Status.invalid_argument and b.error == "null pointer with non-zero length"
+    b = api.align_batch([api.AlignRequest(b"ACGT", -1, b"ACGT", 4, smax=8)])
+    assert b.status == api.Status.invalid_argument and b.error == "negative length"
+    # the first failing request decides, in request order
+    b = api.align_batch([api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=600),
+                         api.AlignRequest(None, 3, b"A", 1)])
+    assert b.error == "smax out of range [0, 511]"
+
+
+def test_ext_accepts_larger_smax_bound():
+    b = api.align_batch([api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=2048)], max_smax=4096)
+    assert b.status != api.Status.invalid_argument
+
+
+@pytest.mark.parametrize("sc,msg", [
+    ((0, -1, 2, 1), "SW scoring: match must be > 0 (the score is 0 for every input otherwise)"),
+    ((2, 2, 5, 2), "SW scoring: mismatch must be < match"),
+    ((2, -3, 0, 2), "SW scoring: gap costs must be > 0"),
+    ((2, -3, 5, 0), "SW scoring: gap costs must be > 0"),
+    ((2, -3, 1, 2), "SW scoring: gap_extend > gap_open with with_cigar cannot re-score to its own score "
+                    "(api.hpp; RESULTADO_H9_SW2_TRACE.md). Score-only requests may use it"),
+])
+def test_sw_scheme_refusals(sc, msg):
+    b = api.align_sw_batch([api.SWRequest(b"ACGT", 4, b"ACGT", 4, api.SWScoring(*sc))])
+    assert b.status == api.Status.invalid_argument and b.error == msg
+
+
+def test_sw_mixed_scheme_and_null_refused():
+    r1 = api.SWRequest(b"ACGT", 4, b"ACGT", 4, api.SWScoring(2, -3, 5, 2))
+    r2 = api.SWRequest(b"ACGT", 4, b"ACGT", 4, api.SWScoring(1, -1, 2, 1))
+    b = api.align_sw_batch([r1, r2])
+    assert b.error == "all requests in an SW batch must share one scoring scheme"
+    b = api.align_sw_batch([api.SWRequest(b"ACGT", 4, None, 5)])
+    assert b.error == "null pointer with non-zero length"
+    b = api.align_sw_batch([api.SWRequest(b"ACGT", -1, b"ACGT", 4)])
+    assert b.error == "negative length"
+
+
+def test_sw_score_only_pattern_limit_refused():
+    # 4 warps x 2*(n+1) ints above 48 KiB: the reference's score-only limit
+    p = b"A" * 1600
+    b = api.align_sw_batch([api.SWRequest(b"ACGT", 4, p, len(p), with_cigar=False)])
+    assert b.status == api.Status.invalid_argument
+    assert b.error.startswith("pattern_len exceeds this device's shared-memory limit")
+
+
+def test_empty_batch_is_ok():
+    assert api.align_batch([]).ok()
+    assert api.align_sw_batch([]).ok()
+
+
+def test_no_device_is_device_error():
+    if api.device_available():
+        pytest.skip("a device is present")
+    b = api.align_batch([api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=8)])
+    assert b.status == api.Status.device_error and b.error
+    assert b.resolved_count == 0 and b.unresolved_count == 0

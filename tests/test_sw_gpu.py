@@ -1,0 +1,115 @@
+"""Smith-Waterman on the GPU through the C ABI, bit-exact against the reference."""
+import numpy as np
+import pytest
+
+import oracle
+from genoaligner_gb300 import api, workloads
+from helpers import assert_sw_equal, sw_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def _enc(s):
+    return s.encode("latin-1")
+
+
+def test_sw_golden(sw_golden):
+    for rec in sw_golden:
+        ts = [_enc(t) for t, _ in rec["pairs"]]
+        ps = [_enc(p) for _, p in rec["pairs"]]
+        got = sw_gpu(ts, ps, scoring=tuple(rec["scoring"]), with_cigar=np.array(rec["with_cigar"]))
+        assert got.status.name == rec["status"], (rec["name"], got.error)
+        res = got.res
+        for i, want in enumerate(rec["results"]):
+            for f in ("score", "start_i", "start_j", "end_i", "end_j"):
+                assert res[f][i] == want[f], (rec["name"], i, f, res[f][i], want[f])
+            for f in ("resolved", "rescore_ok", "wellformed_ok", "too_large"):
+                assert bool(res[f][i]) == bool(want[f]), (rec["name"], i, f)
+            assert got.cigar(i).decode() == want["cigar"], (rec["name"], i)
+
+
+def test_sw_documented_example():
+    r = api.align_sw(api.SWRequest(b"TTTACGTGTT", 10, b"ACGTGT", 6, api.SWScoring(2, -3, 5, 2)))
+    assert r.resolved and r.score == 12 and r.cigar == "MMMMMM"
+    assert (r.start_i, r.end_i, r.start_j, r.end_j) == (3, 8, 0, 5)
+
+
+def test_sw_uneven_sample_vs_oracle():
+    ps = workloads.sw_uneven_200k(n=3000, seed=21)
+    ts, pp = ps.lists()
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=True)
+    got = api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len,
+                                    scoring=(2, -3, 3, 1), with_cigar=True)
+    assert_sw_equal(got, want, "sw_uneven sample")
+
+
+@pytest.mark.parametrize("scheme", [(2, -3, 3, 1), (1, -1, 2, 1), (2, -3, 5, 2), (5, -4, 10, 1)])
+def test_sw_random_vs_oracle(scheme):
+    rng = np.random.default_rng(sum(scheme) + 100)
+    ts, ps = [], []
+    for _ in range(400):
+        core = workloads.random_bases(rng, int(rng.integers(1, 700))).tobytes()
+        ts.append(workloads.random_bases(rng, int(rng.integers(0, 300))).tobytes() + core +
+                  workloads.random_bases(rng, int(rng.integers(0, 300))).tobytes())
+        ps.append(core[: max(1, len(core) - int(rng.integers(0, 20)))])
+    want = oracle.sw_batch(ts, ps, scoring=scheme, with_cigar=True)
+    got = sw_gpu(ts, ps, scoring=scheme)
+    assert_sw_equal(got, want, f"random {scheme}")
+
+
+def test_sw_multiband_vs_oracle():
+    """Patterns wider than one band (1024 columns) cross band edges."""
+    rng = np.random.default_rng(77)
+    ts, ps = [], []
+    for k in range(24):
+        n = int(rng.integers(1025, 3500))
+        core = workloads.random_bases(rng, n).tobytes()
+        ts.append(workloads.random_bases(rng, int(rng.integers(0, 200))).tobytes() + core[: n // 2] +
+                  workloads.random_bases(rng, 3).tobytes() + core[n // 2:])
+        ps.append(core)
+    want = oracle.sw_batch(ts, ps, scoring=(2, -3, 3, 1), with_cigar=True)
+    got = sw_gpu(ts, ps, scoring=(2, -3, 3, 1))
+    assert_sw_equal(got, want, "multiband")
+
+
+def test_sw_score_only_end_cell_vs_oracle():
+    rng = np.random.default_rng(3)
+    ts, ps = [], []
+    for _ in range(500):
+        ts.append(workloads.random_bases(rng, int(rng.integers(0, 400))).tobytes())
+        ps.append(workloads.random_bases(rng, int(rng.integers(0, 400))).tobytes())
+    for i in range(100):                       # repeats: many tied maxima
+        ts.append(b"AC" * int(rng.integers(1, 100)))
+        ps.append(b"AC" * int(rng.integers(1, 100)))
+    for scheme in [(2, -3, 3, 1), (1, -1, 2, 1), (2, -3, 1, 2)]:
+        want = oracle.sw_batch(ts, ps, scoring=scheme, with_cigar=False)
+        got = sw_gpu(ts, ps, scoring=scheme, with_cigar=False)
+        assert_sw_equal(got, want, f"score-only {scheme}")
+
+
+def test_sw_too_large_and_ext_limit():
+    big_t, big_p = b"A" * 8192, b"A" * 8193
+    r = api.align_sw(api.SWRequest(big_t, len(big_t), big_p, len(big_p)))
+    assert not r.resolved and r.too_large and r.score == -1
+    got = sw_gpu([big_t], [big_p], scoring=(2, -3, 5, 2), trace_cell_limit=-1)
+    assert got.status == api.Status.ok and got.res["score"][0] == 2 * 8192
+    assert got.res["rescore_ok"][0] and got.res["wellformed_ok"][0]
+
+
+def test_sw_mixed_with_cigar_batch():
+    ps = workloads.sw_uneven_200k(n=300, seed=8)
+    ts, pp = ps.lists()
+    wc = np.arange(300) % 3 == 0
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=wc)
+    got = sw_gpu(ts, pp, scoring=(2, -3, 3, 1), with_cigar=wc)
+    assert_sw_equal(got, want, "mixed with_cigar")
+
+
+def test_sw_fault_injection_reports_device_error():
+    for step in (1, 2, 3, 4):
+        api.load().ga_debug_fail_next(step)
+        got = sw_gpu([b"ACGTACGT"], [b"ACGT"])
+        assert got.status == api.Status.device_error
+        assert got.res["score"][0] == -1 and not got.res["resolved"][0]
+    got = sw_gpu([b"ACGTACGT"], [b"ACGT"])
+    assert got.status == api.Status.ok and got.res["score"][0] == 8
