@@ -269,9 +269,10 @@ def sw_batch(texts, patterns, scoring=(2, -3, 5, 2), with_cigar=True, threads=No
     cigbuf = np.zeros(int(per.sum()) + 8, np.uint8)
     out = np.zeros(n, SW_OUT)
     m_, x_, go, ge = schemes[0]
+    want_u8 = wants.astype(np.uint8)            # must outlive the call below
     rc = lib().ora_sw_batch(n, _ptr(tbuf), _ptr(toff), _ptr(tlen), _ptr(pbuf), _ptr(poff),
                             _ptr(plen), m_, x_, go, ge, int(trace),
-                            _ptr(wants.astype(np.uint8)), dir_limit, cap, _ptr(cigbuf),
+                            _ptr(want_u8), dir_limit, cap, _ptr(cigbuf),
                             _ptr(cig_off), _ptr(out), threads or os.cpu_count() or 1)
     if rc != 0:
         raise MemoryError("oracle worker allocation failed")
