@@ -1,0 +1,128 @@
+// noalloc.cu -- WFA over a device-resident batch without any device allocation.
+//
+// Some callers cannot call cudaMalloc at the moment they need an alignment:
+// an application whose device memory is fully handed to its own pool
+// allocator (a fresh cudaMalloc there fails or fragments the pool), or a
+// latency-bound loop that cannot take cudaMalloc's implicit device-wide
+// synchronisation.  ga_wfa_device_noalloc serves them: the caller passes the
+// inputs and outputs, and every piece of scratch the WFA kernels need (the
+// 2-bit sequence arena, purity flags, the per-warp wavefront stacks, the work
+// counter and error word) lives in one file-scope __device__ array of
+// NOALLOC_SCRATCH_BYTES, which each GPU that loads this library holds until the
+// process exits.  Batches whose scratch does not fit are refused.
+#include <algorithm>
+#include <mutex>
+
+#include "../../include/genoaligner_gb300.h"
+#include "kernels.cuh"
+
+namespace ga {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)16 << 20;   // 16 MiB per GPU
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch per device ordinal, looked up on the
+// first call made with that device current.  The name is a host-side stand-in
+// in host code, so only this address may be handed to a kernel.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_addr[NOALLOC_MAX_DEVICES];
+
+static unsigned char* noalloc_scratch(int dev)
+{
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_noalloc_addr[dev];
+}
+
+static inline size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace ga
+
+using namespace ga;
+
+extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax, int32_t trace,
+                                         int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream,
+                                         const char** err)
+{
+    if (!b || b->n < 0 || smax < 0 ||
+        (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len || !out_score ||
+                      (trace && (!out_len || !out_cigar || !b->out_off))))) {
+        if (err) *err = "invalid device batch";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (((uintptr_t)b->seq & 15) != 0) {
+        if (err) *err = "device batch arena must be 16-byte aligned";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (b->n == 0) return GA_OK;
+
+    // scratch layout: [counter, error word | purity flags | 2-bit arena | wavefront stacks]
+    const size_t head = 256;
+    const size_t pure_bytes = round256(2 * (size_t)b->n);
+    const size_t packed_bytes = round256(((size_t)b->seq_bytes / 32 + 2) * sizeof(uint64_t));
+    const size_t fixed = head + pure_bytes + packed_bytes;
+    const size_t slot_bytes = (size_t)(smax + 1) * (size_t)(smax + 1) * sizeof(int32_t);
+    if (fixed + (trace ? 4 * slot_bytes : 0) > NOALLOC_SCRATCH_BYTES) {
+        if (err) *err = "batch needs more than the 16 MiB no-allocation scratch: split it or use ga_wfa_device";
+        return GA_INVALID_ARGUMENT;
+    }
+
+    int dev = -1, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = "no CUDA device is available";
+        return GA_DEVICE_ERROR;
+    }
+    unsigned char* base = noalloc_scratch(dev);
+    if (!base) {
+        if (err) *err = "cannot resolve the no-allocation scratch on this device";
+        return GA_DEVICE_ERROR;
+    }
+    int32_t* ctr = reinterpret_cast<int32_t*>(base);
+    uint8_t* pure = base + head;
+    uint64_t* packed = reinterpret_cast<uint64_t*>(base + head + pure_bytes);
+    int32_t* stk = trace ? reinterpret_cast<int32_t*>(base + fixed) : nullptr;
+
+    int slots = (int)std::min<int64_t>(wfa_max_slots(smax, trace != 0, sms), ((int64_t)b->n + 3) / 4 * 4);
+    if (trace) {
+        const int64_t fit = (int64_t)((NOALLOC_SCRATCH_BYTES - fixed) / slot_bytes) / 4 * 4;
+        slots = (int)std::min<int64_t>(slots, fit);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // the counter and error word keep the previous call's values: clear them
+    if (cudaMemsetAsync(ctr, 0, head, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = "device memset failed";
+        return GA_DEVICE_ERROR;
+    }
+    PairDesc D;
+    D.seq = b->seq; D.packed = packed; D.pure = pure;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = b->n;
+    WfaArgs A;
+    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
+    A.out_score = out_score; A.out_len = out_len; A.out_cigar = out_cigar;
+    A.stack = stk; A.stack_slot = (int64_t)(smax + 1) * (smax + 1);
+    A.counter = ctr; A.err = ctr + 1;
+    if (launch_pack(D, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = "kernel launch failed";
+        return GA_DEVICE_ERROR;
+    }
+    if (!stream && cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = "device execution failed";
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
+}

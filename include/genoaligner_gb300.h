@@ -193,6 +193,32 @@ int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_
                      int64_t trace_cell_limit, int32_t* out_score, int32_t* out_pos,
                      int32_t* out_len, char* out_cigar, void* stream, const char** err);
 
+/* WFA over a device batch, like ga_wfa_device, but without allocating any
+ * device memory.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc when they align: an application that
+ * has handed all device memory to its own pool allocator, or a latency-bound
+ * loop that cannot take cudaMalloc's implicit device-wide synchronisation.
+ * The caller passes inputs and outputs exactly as for ga_wfa_device; all
+ * scratch (2-bit arena, purity flags, wavefront stacks, work counter) comes
+ * from one 16 MiB array in the library's device image, which every GPU that
+ * loads this library holds until the process exits.
+ *
+ * Limit: 256 + 2n + (seq_bytes/32 + 2)*8 bytes (each rounded up to 256) must
+ * fit in 16 MiB, plus, when trace != 0, four wavefront stacks of
+ * (smax+1)^2 * 4 bytes; a larger batch is refused with GA_INVALID_ARGUMENT and
+ * a message, before any device work.
+ *
+ * The first call on a device, made with that device current, resolves the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Every call shares the one array: calls whose work can
+ * overlap on the GPU (different streams, or threads that do not order their
+ * calls) race on it and must be serialised by the caller.  stream NULL runs on
+ * the legacy default stream and synchronises before returning. */
+int32_t ga_wfa_device_noalloc(const ga_device_batch* batch, int32_t smax, int32_t trace,
+                              int32_t* out_score, int32_t* out_len, char* out_cigar,
+                              void* stream, const char** err);
+
 /* ------------------------------------------------------------ provenance -- */
 
 /* Mirror backend_name / device_name / device_available (api.hpp:485-487). */
