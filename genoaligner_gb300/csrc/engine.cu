@@ -454,6 +454,134 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err)
     return GA_OK;
 }
 
+// Work plan of one SW batch: pairs routed to the two-pairs-per-warp 16-bit
+// trace kernel (eligible pure-ACGT pairs) or to the 32-bit kernel, per band
+// width, largest first; per-slot direction-table and band-edge sizes.
+struct SwPlan {
+    std::vector<int32_t> w32[3];     // pair indices, 32-bit kernel, widths 8 / 16 / 32
+    std::vector<int32_t> w16[3];     // 2 pair indices per item, 16-bit kernel
+    int64_t dir32[3] = {0, 0, 0}, dir16[3] = {0, 0, 0};
+    int64_t edge_slot = 2;
+    int64_t words() const
+    {
+        int64_t s = 0;
+        for (int k = 0; k < 3; ++k) s += (int64_t)w32[k].size() + (int64_t)w16[k].size();
+        return s;
+    }
+};
+
+static const int kWidths[3] = {8, 16, 32};
+static int width_index(int C) { return C == 8 ? 0 : (C == 16 ? 1 : 2); }
+
+static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8_t* pure, const uint8_t* skip,
+                    const ga_sw_scoring& sc, bool trace, SwPlan& P)
+{
+    std::vector<int32_t> e16[3];
+    for (int32_t i = 0; i < n; ++i) {
+        if (skip && skip[i]) continue;
+        const int k = width_index(sw_width_for(pl[i]));
+        const bool use16 = trace && pure && pure[i] && pure[n + i] &&
+                           sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
+        (use16 ? e16[k] : P.w32[k]).push_back(i);
+    }
+    auto cells = [&](int32_t x) { return (int64_t)(tl[x] + 31) * pl[x]; };
+    auto bigger = [&](int32_t x, int32_t y) { const int64_t a = cells(x), b = cells(y); return a != b ? a > b : x < y; };
+    for (int k = 0; k < 3; ++k) {
+        std::sort(P.w32[k].begin(), P.w32[k].end(), bigger);
+        for (int32_t i : P.w32[k]) {
+            if (trace) P.dir32[k] = std::max(P.dir32[k], sw_dir_words(tl[i], pl[i], kWidths[k]));
+            P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
+        }
+        P.dir32[k] = (P.dir32[k] + 3) / 4 * 4;
+        std::sort(e16[k].begin(), e16[k].end(), bigger);
+        for (size_t q = 0; q < e16[k].size(); q += 2) {
+            const int32_t a = e16[k][q], b = q + 1 < e16[k].size() ? e16[k][q + 1] : -1;
+            P.w16[k].push_back(a);
+            P.w16[k].push_back(b);
+            const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
+            P.dir16[k] = std::max(P.dir16[k], sw16_dir_words(M, N, kWidths[k]));
+            P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
+        }
+        P.dir16[k] = (P.dir16[k] + 3) / 4 * 4;
+    }
+}
+
+// Slots (resident warps) per launch and the direction-table words the launches
+// need (they run one after another on one stream and share the table).
+struct SwSlots {
+    int s32[3] = {0, 0, 0}, s16[3] = {0, 0, 0};
+    int64_t dir_words = 0, max_slots = 4;
+};
+
+static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
+{
+    SwSlots S;
+    const int64_t budget = (int64_t)48 << 30;          // direction-table cap, bytes
+    for (int k = 0; k < 3; ++k) {
+        if (!P.w32[k].empty()) {
+            int s = sw_max_slots(kWidths[k], trace, sm_count);
+            s = (int)std::min<int64_t>(s, ((int64_t)P.w32[k].size() + 3) / 4 * 4);
+            if (trace && P.dir32[k] > 0) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir32[k] * 4) / 4 * 4));
+            S.s32[k] = s;
+            if (trace) S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir32[k]);
+            S.max_slots = std::max<int64_t>(S.max_slots, s);
+        }
+        if (!P.w16[k].empty()) {
+            int s = sw16_max_slots(kWidths[k], sm_count);
+            s = (int)std::min<int64_t>(s, ((int64_t)P.w16[k].size() / 2 + 3) / 4 * 4);
+            s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
+            S.s16[k] = s;
+            S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir16[k]);
+            S.max_slots = std::max<int64_t>(S.max_slots, s);
+        }
+    }
+    return S;
+}
+
+// Enqueue every SW launch of a plan.  `dwork` holds the plan's lists
+// concatenated in the order w16[0..2] then w32[0..2]; `ctr` has 6 zeroed ints.
+static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc& D, const ga_sw_scoring& sc,
+                               bool trace, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
+                               int32_t* out_len, char* out_cigar, uint32_t* dirs, int32_t* edge, int32_t* ctr,
+                               int32_t* err, cudaStream_t st)
+{
+    int64_t base = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (!P.w16[k].empty()) {
+            Sw16Args A;
+            A.D = D; A.work = dwork + base; A.nwork = (int32_t)(P.w16[k].size() / 2);
+            A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
+            A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
+            A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
+            A.counter = ctr + k; A.err = err;
+            const cudaError_t e = launch_sw16(A, kWidths[k], S.s16[k], st);
+            if (e != cudaSuccess) return e;
+        }
+        base += (int64_t)P.w16[k].size();
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (!P.w32[k].empty()) {
+            SwArgs A;
+            A.D = D; A.work = dwork + base; A.nwork = (int32_t)P.w32[k].size();
+            A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
+            A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
+            A.dirs = dirs; A.dir_slot = P.dir32[k]; A.edge = edge; A.edge_slot = P.edge_slot;
+            A.counter = ctr + 3 + k; A.err = err;
+            const cudaError_t e = launch_sw(A, kWidths[k], trace, S.s32[k], st);
+            if (e != cudaSuccess) return e;
+        }
+        base += (int64_t)P.w32[k].size();
+    }
+    return cudaSuccess;
+}
+
+static void flatten_plan(const SwPlan& P, int32_t* out)
+{
+    int64_t q = 0;
+    for (int k = 0; k < 3; ++k) for (int32_t x : P.w16[k]) out[q++] = x;
+    for (int k = 0; k < 3; ++k) for (int32_t x : P.w32[k]) out[q++] = x;
+}
+
 int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
                  const char** err)
 {
@@ -477,10 +605,13 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     }
 
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    std::vector<int32_t> tl(n), pl(n);
     std::vector<uint8_t> too_big(n, 0);
     int64_t arena = 0, cig = 0;
     for (int32_t i = 0; i < n; ++i) {
         const ga_sw_request& r = reqs[i];
+        tl[i] = r.text_len;
+        pl[i] = r.pattern_len;
         a_off[i] = arena; arena += round32(r.text_len);
         b_off[i] = arena; arena += round32(r.pattern_len);
         out_off[i] = cig; cig += (int64_t)r.text_len + r.pattern_len;
@@ -492,86 +623,39 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     arena += 64;
     if (!trace) cig = 0;
 
-    // work lists by band width, largest first
-    std::vector<int32_t> work[3];
-    const int widths[3] = {8, 16, 32};
-    for (int32_t i = 0; i < n; ++i) {
-        if (too_big[i]) continue;
-        const int C = sw_width_for(reqs[i].pattern_len);
-        work[C == 8 ? 0 : (C == 16 ? 1 : 2)].push_back(i);
-    }
-    int64_t dir_slot[3] = {0, 0, 0}, edge_slot = 2;
-    for (int w = 0; w < 3; ++w) {
-        std::sort(work[w].begin(), work[w].end(), [&](int32_t x, int32_t y) {
-            const int64_t cx = (int64_t)(reqs[x].text_len + 31) * reqs[x].pattern_len;
-            const int64_t cy = (int64_t)(reqs[y].text_len + 31) * reqs[y].pattern_len;
-            return cx != cy ? cx > cy : x < y;
-        });
-        for (int32_t i : work[w]) {
-            dir_slot[w] = std::max(dir_slot[w], sw_dir_words(reqs[i].text_len, reqs[i].pattern_len, widths[w]));
-            edge_slot = std::max<int64_t>(edge_slot, 2 * (int64_t)reqs[i].text_len);
-        }
-        dir_slot[w] = (dir_slot[w] + 3) / 4 * 4;
-    }
-
     Ctx* c = acquire_ctx(err);
     if (!c) return GA_DEVICE_ERROR;
     struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
 
-    int slots[3] = {0, 0, 0};
-    int64_t dir_words = 0, max_slots_all = 0;
-    const int64_t dir_budget = (int64_t)48 << 30;       // direction-table memory cap (bytes)
-    for (int w = 0; w < 3; ++w) {
-        if (work[w].empty()) continue;
-        int s = sw_max_slots(widths[w], trace, c->sm_count);
-        s = (int)std::min<int64_t>(s, ((int64_t)work[w].size() + 3) / 4 * 4);
-        if (trace && dir_slot[w] > 0)
-            s = (int)std::min<int64_t>(s, std::max<int64_t>(4, dir_budget / (dir_slot[w] * 4) / 4 * 4));
-        slots[w] = s;
-        if (trace) dir_words = std::max(dir_words, (int64_t)s * dir_slot[w]);
-        max_slots_all = std::max<int64_t>(max_slots_all, s);
-    }
-
+    // Host staging: [descriptors | arena] in, [purity] back, [work lists] in,
+    // [score pos len cigar err] back.  Device: the same blocks plus scratch.
+    const int64_t max_work = 2 * (int64_t)n + 8;
     int64_t *ha, *hb, *ho, *da, *db, *dout;
-    int32_t *hal, *hbl, *dal, *dbl, *hwork, *dwork, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der,
-        *dctr, *dedge;
-    uint8_t *hseq, *dseq;
-    uint32_t* ddirs;
+    int32_t *hal, *hbl, *dal, *dbl, *hwork, *dwork, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der;
+    uint8_t *hseq, *dseq, *hpure, *dpure;
     char *hcg, *dcg;
-    const int64_t nwork = (int64_t)work[0].size() + work[1].size() + work[2].size();
-    auto layout = [&](char* base, bool host) -> size_t {
-        Carve k(base);
-        int64_t* pa = k.take<int64_t>(n); int32_t* pal = k.take<int32_t>(n);
-        int64_t* pb = k.take<int64_t>(n); int32_t* pbl = k.take<int32_t>(n);
-        int64_t* po = k.take<int64_t>(n);
-        int32_t* pw = k.take<int32_t>(nwork + 1);
-        uint8_t* ps = k.take<uint8_t>(arena);
-        int32_t* psc = k.take<int32_t>(n); int32_t* ppos = k.take<int32_t>(4 * (size_t)n);
-        int32_t* pln = k.take<int32_t>(n); char* pcg = k.take<char>(cig + 1);
-        int32_t* per = k.take<int32_t>(1, 4);
-        if (host) {
-            ha = pa; hal = pal; hb = pb; hbl = pbl; ho = po; hwork = pw; hseq = ps;
-            hsc = psc; hpos = ppos; hln = pln; hcg = pcg; her = per;
-            return k.off;
-        }
-        da = pa; dal = pal; db = pb; dbl = pbl; dout = po; dwork = pw; dseq = ps;
-        dsc = psc; dpos = ppos; dln = pln; dcg = pcg; der = per;
-        dctr = k.take<int32_t>(4, 4);
-        dedge = k.take<int32_t>((size_t)max_slots_all * edge_slot);
-        ddirs = trace ? k.take<uint32_t>((size_t)dir_words) : nullptr;
-        return k.off;
+    auto in_layout = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
+                         uint8_t** ps, uint8_t** pp, int32_t** pw, int32_t** psc, int32_t** ppos, int32_t** pln,
+                         char** pcg, int32_t** per) {
+        *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
+        *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
+        *po = k.take<int64_t>(n);
+        *ps = k.take<uint8_t>(arena);
+        *pp = k.take<uint8_t>(2 * (size_t)n);
+        *pw = k.take<int32_t>(max_work);
+        *psc = k.take<int32_t>(n); *ppos = k.take<int32_t>(4 * (size_t)n);
+        *pln = k.take<int32_t>(n); *pcg = k.take<char>(cig + 1);
+        *per = k.take<int32_t>(1, 4);
     };
-    const size_t host_bytes = layout(nullptr, true);
-    const size_t dev_bytes = layout(nullptr, false);
-    if (fail_here(1) || !ensure_dev(c, dev_bytes)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    if (!ensure_host(c, host_bytes)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
-    layout(c->host, true);
-    layout(c->dev, false);
-
+    Carve hk(nullptr), dk(nullptr);
+    in_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hcg, &her);
+    in_layout(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+    const size_t dev_fixed = dk.off;
+    if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    // stage inputs (device scratch is sized after planning)
     {
-        int64_t q = 0;
-        for (int w = 0; w < 3; ++w)
-            for (int32_t i : work[w]) hwork[q++] = i;
+        Carve k(c->host);
+        in_layout(k, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hcg, &her);
     }
     parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
         for (int64_t i = lo; i < hi; ++i) {
@@ -584,9 +668,64 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         }
     });
     std::memset(hseq + arena - 64, 0, 64);
+
+    // device memory: fixed blocks, then counters, band edges and direction tables
+    // (sized from the plan; a first pass reserves the fixed part)
+    if (fail_here(1) || !ensure_dev(c, dev_fixed + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    {
+        Carve k(c->dev);
+        in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+    }
     const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
     t_h2d = (int64_t)in_bytes;
     if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_H2D;
+        return GA_DEVICE_ERROR;
+    }
+    PairDesc D;
+    D.seq = dseq; D.packed = nullptr; D.pure = dpure;
+    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
+    if (fail_here(3) || launch_pack(D, nullptr, dpure, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(hpure, dpure, 2 * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_LAUNCH;
+        return GA_DEVICE_ERROR;
+    }
+    SwPlan P;
+    plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, P);
+    const SwSlots S = size_sw(P, trace, c->sm_count);
+    Carve extra(nullptr);
+    extra.off = dev_fixed;
+    int32_t* dctr = extra.take<int32_t>(8, 4);
+    int32_t* dedge = extra.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+    uint32_t* ddirs = trace ? extra.take<uint32_t>((size_t)S.dir_words) : nullptr;
+    if (!ensure_dev(c, extra.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    // ensure_dev may have moved the arena: re-carve and re-send if so
+    {
+        Carve k(c->dev);
+        int64_t* old_da = da;
+        in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+        if (da != old_da) {
+            if (cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+                cudaGetLastError();
+                *err = E_H2D;
+                return GA_DEVICE_ERROR;
+            }
+            D.seq = dseq; D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
+            D.pure = dpure;
+            cudaMemcpyAsync(dpure, hpure, 2 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+        }
+        Carve e(c->dev);
+        e.off = dev_fixed;
+        dctr = e.take<int32_t>(8, 4);
+        dedge = e.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+        ddirs = trace ? e.take<uint32_t>((size_t)S.dir_words) : nullptr;
+    }
+    flatten_plan(P, hwork);
+    const int64_t nw = P.words();
+    if ((nw > 0 && cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)nw, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)) {
         cudaGetLastError();
         *err = E_H2D;
         return GA_DEVICE_ERROR;
@@ -596,30 +735,11 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, c->stream);
     cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, c->stream);
     cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream);
-    cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 4, c->stream);
-
-    PairDesc D;
-    D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
-    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
-    if (fail_here(3)) { *err = E_LAUNCH; return GA_DEVICE_ERROR; }
-    int64_t wbase = 0;
-    for (int w = 0; w < 3; ++w) {
-        if (work[w].empty()) continue;
-        SwArgs A;
-        A.D = D;
-        A.work = dwork + wbase;
-        A.nwork = (int32_t)work[w].size();
-        A.match = s0.match; A.mismatch = s0.mismatch; A.gap_open = s0.gap_open; A.gap_extend = s0.gap_extend;
-        A.out_score = dsc; A.out_pos = dpos; A.out_len = dln; A.out_cigar = dcg;
-        A.dirs = ddirs; A.dir_slot = dir_slot[w];
-        A.edge = dedge; A.edge_slot = edge_slot;
-        A.counter = dctr + w; A.err = der;
-        if (launch_sw(A, widths[w], trace, slots[w], c->stream) != cudaSuccess) {
-            cudaGetLastError();
-            *err = E_LAUNCH;
-            return GA_DEVICE_ERROR;
-        }
-        wbase += (int64_t)work[w].size();
+    cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
+    if (launch_plan(P, S, D, s0, trace, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_LAUNCH;
+        return GA_DEVICE_ERROR;
     }
     const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
     t_d2h = (int64_t)out_bytes;
@@ -933,101 +1053,95 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         return GA_INVALID_ARGUMENT;
     }
     if (b->n == 0) return GA_OK;
-    // the lengths live on the device; plan from a host copy
-    std::vector<int32_t> al(b->n), bl(b->n);
-    if (cudaMemcpy(al.data(), b->a_len, sizeof(int32_t) * b->n, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(bl.data(), b->b_len, sizeof(int32_t) * b->n, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        if (err) *err = E_D2H;
-        return GA_DEVICE_ERROR;
-    }
-    std::vector<int32_t> work[3];
-    const int widths[3] = {8, 16, 32};
-    std::vector<int32_t> too_big;
-    for (int32_t i = 0; i < b->n; ++i) {
-        if (cell_limit >= 0 && al[i] > 0 && bl[i] > 0 && ((int64_t)al[i] + 1) * ((int64_t)bl[i] + 1) > cell_limit) {
-            too_big.push_back(i);
-            continue;
-        }
-        const int C = sw_width_for(bl[i]);
-        work[C == 8 ? 0 : (C == 16 ? 1 : 2)].push_back(i);
-    }
-    int64_t dir_slot[3] = {0, 0, 0}, edge_slot = 2;
-    for (int w = 0; w < 3; ++w) {
-        std::sort(work[w].begin(), work[w].end(), [&](int32_t x, int32_t y) {
-            const int64_t cx = (int64_t)(al[x] + 31) * bl[x], cy = (int64_t)(al[y] + 31) * bl[y];
-            return cx != cy ? cx > cy : x < y;
-        });
-        for (int32_t i : work[w]) {
-            dir_slot[w] = std::max(dir_slot[w], sw_dir_words(al[i], bl[i], widths[w]));
-            edge_slot = std::max<int64_t>(edge_slot, 2 * (int64_t)al[i]);
-        }
-        dir_slot[w] = (dir_slot[w] + 3) / 4 * 4;
-    }
+    const int32_t n = b->n;
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    int slots[3] = {0, 0, 0};
-    int64_t dir_words = 0, max_slots_all = 4;
-    for (int w = 0; w < 3; ++w) {
-        if (work[w].empty()) continue;
-        int s = sw_max_slots(widths[w], trace != 0, c->sm_count);
-        s = (int)std::min<int64_t>(s, ((int64_t)work[w].size() + 3) / 4 * 4);
-        if (trace) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, ((int64_t)48 << 30) / (dir_slot[w] * 4) / 4 * 4));
-        slots[w] = s;
-        if (trace) dir_words = std::max(dir_words, (int64_t)s * dir_slot[w]);
-        max_slots_all = std::max<int64_t>(max_slots_all, s);
-    }
-    const int64_t nwork = (int64_t)work[0].size() + work[1].size() + work[2].size();
-    auto layout = [&](char* base, int32_t** wk, int32_t** ctr, int32_t** edge, uint32_t** dirs, int32_t** tb) {
-        Carve k(base);
-        *wk = k.take<int32_t>(nwork + 1);
-        *tb = k.take<int32_t>(too_big.size() + 1);
-        *ctr = k.take<int32_t>(64, 256);
-        *edge = k.take<int32_t>((size_t)max_slots_all * edge_slot);
-        *dirs = trace ? k.take<uint32_t>((size_t)dir_words) : nullptr;
-        return k.off;
-    };
-    int32_t *dwork, *dctr, *dedge, *dtb;
-    uint32_t* ddirs;
-    const size_t need = layout(nullptr, &dwork, &dctr, &dedge, &ddirs, &dtb);
-    if (!ensure_dev(c, need)) { release_ctx(c); if (err) *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    layout(c->dev, &dwork, &dctr, &dedge, &ddirs, &dtb);
-    std::vector<int32_t> hw;
-    hw.reserve(nwork);
-    for (int w = 0; w < 3; ++w) hw.insert(hw.end(), work[w].begin(), work[w].end());
-    if (!hw.empty()) cudaMemcpyAsync(dwork, hw.data(), sizeof(int32_t) * hw.size(), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
-    cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * b->n, st);
-    cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)b->n, st);
-    if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * b->n, st);
-    // too-large pairs: score -2
-    if (!too_big.empty()) {
-        std::vector<int32_t> m2(1, -2);
-        for (int32_t i : too_big) cudaMemcpyAsync(out_score + i, &m2[0], sizeof(int32_t), cudaMemcpyHostToDevice, st);
-        cudaStreamSynchronize(st);
+    // purity flags on the device, then lengths and flags to the host for the plan
+    {
+        Carve k(nullptr);
+        k.take<uint8_t>(2 * (size_t)n);
+        if (!ensure_dev(c, k.off) || !ensure_host(c, 2 * (size_t)n + 8 * (size_t)n + 1024)) {
+            release_ctx(c);
+            if (err) *err = E_ALLOC;
+            return GA_DEVICE_ERROR;
+        }
     }
     PairDesc D;
-    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.seq = b->seq; D.packed = nullptr; D.pure = reinterpret_cast<uint8_t*>(c->dev);
     D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
-    D.out_off = b->out_off; D.n = b->n;
-    int32_t rc = GA_OK;
-    int64_t wbase = 0;
-    for (int w = 0; w < 3; ++w) {
-        if (work[w].empty()) continue;
-        SwArgs A;
-        A.D = D; A.work = dwork + wbase; A.nwork = (int32_t)work[w].size();
-        A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
-        A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
-        A.dirs = ddirs; A.dir_slot = dir_slot[w]; A.edge = dedge; A.edge_slot = edge_slot;
-        A.counter = dctr + w; A.err = dctr + 8;
-        if (launch_sw(A, widths[w], trace != 0, slots[w], st) != cudaSuccess) {
-            cudaGetLastError();
-            if (err) *err = E_LAUNCH;
-            rc = GA_DEVICE_ERROR;
-            break;
+    D.out_off = b->out_off; D.n = n;
+    uint8_t* hpure = reinterpret_cast<uint8_t*>(c->host);
+    int32_t* hlen = reinterpret_cast<int32_t*>(c->host + ((2 * (size_t)n + 255) & ~(size_t)255));
+    if (launch_pack(D, nullptr, const_cast<uint8_t*>(D.pure), st) != cudaSuccess ||
+        cudaMemcpyAsync(hpure, D.pure, 2 * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(hlen, b->a_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(hlen + n, b->b_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        release_ctx(c);
+        if (err) *err = E_D2H;
+        return GA_DEVICE_ERROR;
+    }
+    std::vector<uint8_t> pure(hpure, hpure + 2 * (size_t)n), skip(n, 0);
+    std::vector<int32_t> al(hlen, hlen + n), bl(hlen + n, hlen + 2 * n);
+    std::vector<int32_t> too_big;
+    for (int32_t i = 0; i < n; ++i)
+        if (cell_limit >= 0 && al[i] > 0 && bl[i] > 0 && ((int64_t)al[i] + 1) * ((int64_t)bl[i] + 1) > cell_limit) {
+            skip[i] = 1;
+            too_big.push_back(i);
         }
-        wbase += (int64_t)work[w].size();
+    SwPlan P;
+    plan_sw(n, al.data(), bl.data(), pure.data(), skip.data(), sc, trace != 0, P);
+    const SwSlots S = size_sw(P, trace != 0, c->sm_count);
+    const int64_t nw = P.words();
+    auto layout = [&](char* base, uint8_t** pp, int32_t** wk, int32_t** tb, int32_t** ctr, int32_t** edge,
+                      uint32_t** dirs) {
+        Carve k(base);
+        *pp = k.take<uint8_t>(2 * (size_t)n);
+        *wk = k.take<int32_t>(nw + 1);
+        *tb = k.take<int32_t>(too_big.size() + 1);
+        *ctr = k.take<int32_t>(64, 256);
+        *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+        *dirs = trace ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        return k.off;
+    };
+    uint8_t* dpure;
+    int32_t *dwork, *dtb, *dctr, *dedge;
+    uint32_t* ddirs;
+    const size_t need = layout(nullptr, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
+    const size_t host_need = sizeof(int32_t) * (size_t)(nw + too_big.size() + 2);
+    char* old_dev = c->dev;
+    if (!ensure_dev(c, need) || !ensure_host(c, host_need)) {
+        release_ctx(c);
+        if (err) *err = E_ALLOC;
+        return GA_DEVICE_ERROR;
+    }
+    layout(c->dev, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
+    if (c->dev != old_dev) cudaMemcpyAsync(dpure, pure.data(), 2 * (size_t)n, cudaMemcpyHostToDevice, st);
+    D.pure = dpure;
+    int32_t* hwork = reinterpret_cast<int32_t*>(c->host);
+    flatten_plan(P, hwork);
+    for (size_t q = 0; q < too_big.size(); ++q) hwork[nw + q] = too_big[q];
+    if (nw + (int64_t)too_big.size() > 0)
+        cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)nw, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+    cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
+    cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
+    if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
+    int32_t rc = GA_OK;
+    if (!too_big.empty()) {
+        // too-large pairs report score -2
+        std::vector<int32_t> m2(too_big.size(), -2);
+        for (size_t q = 0; q < too_big.size(); ++q)
+            cudaMemcpyAsync(out_score + too_big[q], &m2[q], sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);
+    }
+    if (launch_plan(P, S, D, sc, trace != 0, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+                    dctr + 32, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = E_LAUNCH;
+        rc = GA_DEVICE_ERROR;
     }
     if (stream) {
         cudaEventRecord(c->done, st);
@@ -1109,7 +1223,7 @@ const char* ga_profile_kernel_name(int32_t kernel_id)
 {
     static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
                                          "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
-                                         "kmer_sketch", "mlp"};
+                                         "kmer_sketch", "mlp", "sw16x2_trace"};
     return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
 }
 

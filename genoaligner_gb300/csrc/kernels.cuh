@@ -35,6 +35,25 @@ struct SwArgs {
     int32_t* err;
 };
 
+// Two pairs per warp in 16-bit lanes (sw16.cu): work holds 2 pair indices per
+// item, the second -1 when the item carries one pair.
+struct Sw16Args {
+    PairDesc D;
+    const int32_t* work;
+    int32_t nwork;
+    int32_t match, mismatch, gap_open, gap_extend;
+    int32_t* out_score;
+    int32_t* out_pos;
+    int32_t* out_len;
+    char* out_cigar;
+    uint32_t* dirs;
+    int64_t dir_slot;
+    int32_t* edge;
+    int64_t edge_slot;
+    int32_t* counter;
+    int32_t* err;
+};
+
 cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 
 size_t wfa_smem_bytes(int smax);
@@ -45,5 +64,10 @@ int64_t sw_dir_words(int m, int n, int C);
 int sw_width_for(int n);
 int sw_max_slots(int C, bool trace, int sm_count);
 cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
+
+bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge);
+int64_t sw16_dir_words(int M, int N, int C);
+int sw16_max_slots(int C, int sm_count);
+cudaError_t launch_sw16(const Sw16Args& A, int C, int slots, cudaStream_t st);
 
 }  // namespace ga

@@ -25,7 +25,19 @@ __global__ void __launch_bounds__(256) int_peak_kernel(int iters, int x, int* ou
             for (int k = 0; k < 8; ++k) {
                 if constexpr (V == 0) a[k] = max(a[k] + x, y + k);
                 else if constexpr (V == 1) a[k] = __viaddmax_s32(a[k], x, y + k);
-                else a[k] = __vimax3_s32_relu(a[k], x - k, y);
+                else if constexpr (V == 2) a[k] = __vimax3_s32_relu(a[k], x - k, y);
+                else if constexpr (V == 3) a[k] = max(a[k], y + k) ^ x;             // max + xor
+                else if constexpr (V == 4) a[k] = a[k] + (y + k);                   // add
+                else if constexpr (V == 5) a[k] = (int)__vmaxs2((unsigned)a[k], (unsigned)(y + k)) ^ x;
+                else if constexpr (V == 6) a[k] = (int)__viaddmax_s16x2((unsigned)a[k], (unsigned)x, (unsigned)(y + k));
+                else if constexpr (V == 7) {
+                    bool ph, pl;
+                    a[k] = (int)__vibmax_s16x2((unsigned)a[k], (unsigned)(y + k), &ph, &pl) + (ph ? 1 : 0) + (pl ? 2 : 0);
+                } else if constexpr (V == 8) {
+                    bool p;
+                    a[k] = __vibmax_s32(a[k], y + k, &p) + (p ? 1 : 0);
+                } else if constexpr (V == 9) a[k] = (int)__vcmpgtu2((unsigned)a[k], (unsigned)(y + k)) ^ x;
+                else a[k] = (a[k] & (y + k)) | (x ^ k);                              // logic
             }
         }
     }
@@ -56,9 +68,19 @@ extern "C" int32_t ga_bench_int_peak(int32_t variant, double* lane_ops_per_s)
     const int blocks = sms * 8, threads = 256, iters = 2048;
     auto launch = [&] {
         launch_begin(K_PEAK, st);
-        if (variant == 0) int_peak_kernel<0><<<blocks, threads, 0, st>>>(iters, 3, out);
-        else if (variant == 1) int_peak_kernel<1><<<blocks, threads, 0, st>>>(iters, 3, out);
-        else int_peak_kernel<2><<<blocks, threads, 0, st>>>(iters, 3, out);
+        switch (variant) {
+            case 0: int_peak_kernel<0><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 1: int_peak_kernel<1><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 2: int_peak_kernel<2><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 3: int_peak_kernel<3><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 4: int_peak_kernel<4><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 5: int_peak_kernel<5><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 6: int_peak_kernel<6><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 7: int_peak_kernel<7><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 8: int_peak_kernel<8><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 9: int_peak_kernel<9><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            default: int_peak_kernel<10><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+        }
         launch_end(K_PEAK, st);
     };
     launch();                                   // warm-up

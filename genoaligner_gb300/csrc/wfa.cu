@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) pack2_kernel(PairDesc D, uint64_t* __rest
                     word |= code << (2 * b);
                 }
             }
-            packed[(off >> 5) + w] = word;
+            if (packed) packed[(off >> 5) + w] = word;
         }
         bad = __any_sync(FULL, bad);
         if (lane == 0) pure[q] = bad ? 0 : 1;
