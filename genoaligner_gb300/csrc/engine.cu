@@ -9,6 +9,8 @@
 // steady stream of calls allocates nothing; concurrent calls take different
 // contexts.
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <atomic>
 #include <condition_variable>
 #include <cstdio>
@@ -159,6 +161,7 @@ struct Ctx {
     bool pending = false;
     char* dev = nullptr;
     size_t dev_cap = 0;
+    uint64_t dev_gen = 0;           // bumped whenever the device arena is reallocated
     char* host = nullptr;
     size_t host_cap = 0;
 };
@@ -218,6 +221,7 @@ static bool ensure_dev(Ctx* c, size_t bytes)
         want = bytes;
     }
     c->dev_cap = want;
+    ++c->dev_gen;
     return true;
 }
 
@@ -473,27 +477,50 @@ struct SwPlan {
 static const int kWidths[3] = {8, 16, 32};
 static int width_index(int C) { return C == 8 ? 0 : (C == 16 ? 1 : 2); }
 
+// Largest first, in O(n): a counting sort on a log-scale size key (64 buckets
+// per doubling of (m + 31) * n, so pairs sharing a bucket differ by < 1.1 %),
+// index order within a bucket.
+static void order_by_size(std::vector<int32_t>& v, const int32_t* tl, const int32_t* pl)
+{
+    if (v.size() < 2) return;
+    constexpr int NB = 64 * 48;
+    std::vector<uint16_t> key(v.size());
+    std::vector<int32_t> cnt(NB + 1, 0);
+    for (size_t q = 0; q < v.size(); ++q) {
+        const double c = (double)(tl[v[q]] + 31) * (double)std::max(pl[v[q]], 1);
+        const int b = std::min(NB - 1, std::max(0, (int)(std::log2(c) * 64.0)));
+        key[q] = (uint16_t)(NB - 1 - b);                 // descending size
+        ++cnt[key[q] + 1];
+    }
+    for (int b = 0; b < NB; ++b) cnt[b + 1] += cnt[b];
+    std::vector<int32_t> out(v.size());
+    for (size_t q = 0; q < v.size(); ++q) out[cnt[key[q]]++] = v[q];
+    v.swap(out);
+}
+
 static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8_t* pure, const uint8_t* skip,
                     const ga_sw_scoring& sc, bool trace, SwPlan& P)
 {
     std::vector<int32_t> e16[3];
+    static const bool use16_ok = [] {
+        const char* e = getenv("GA_SW16");
+        return !(e && e[0] == '0');
+    }();
     for (int32_t i = 0; i < n; ++i) {
         if (skip && skip[i]) continue;
         const int k = width_index(sw_width_for(pl[i]));
-        const bool use16 = trace && pure && pure[i] && pure[n + i] &&
+        const bool use16 = use16_ok && trace && pure && pure[i] && pure[n + i] &&
                            sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
         (use16 ? e16[k] : P.w32[k]).push_back(i);
     }
-    auto cells = [&](int32_t x) { return (int64_t)(tl[x] + 31) * pl[x]; };
-    auto bigger = [&](int32_t x, int32_t y) { const int64_t a = cells(x), b = cells(y); return a != b ? a > b : x < y; };
     for (int k = 0; k < 3; ++k) {
-        std::sort(P.w32[k].begin(), P.w32[k].end(), bigger);
+        order_by_size(P.w32[k], tl, pl);
         for (int32_t i : P.w32[k]) {
             if (trace) P.dir32[k] = std::max(P.dir32[k], sw_dir_words(tl[i], pl[i], kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
         }
         P.dir32[k] = (P.dir32[k] + 3) / 4 * 4;
-        std::sort(e16[k].begin(), e16[k].end(), bigger);
+        order_by_size(e16[k], tl, pl);
         for (size_t q = 0; q < e16[k].size(); q += 2) {
             const int32_t a = e16[k][q], b = q + 1 < e16[k].size() ? e16[k][q + 1] : -1;
             P.w16[k].push_back(a);
@@ -696,6 +723,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     SwPlan P;
     plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, P);
     const SwSlots S = size_sw(P, trace, c->sm_count);
+    const uint64_t gen_before = c->dev_gen;
     Carve extra(nullptr);
     extra.off = dev_fixed;
     int32_t* dctr = extra.take<int32_t>(8, 4);
@@ -705,9 +733,8 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     // ensure_dev may have moved the arena: re-carve and re-send if so
     {
         Carve k(c->dev);
-        int64_t* old_da = da;
         in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
-        if (da != old_da) {
+        if (c->dev_gen != gen_before) {          // the arena moved: send the inputs again
             if (cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
                 cudaGetLastError();
                 *err = E_H2D;
@@ -1111,14 +1138,14 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     uint32_t* ddirs;
     const size_t need = layout(nullptr, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
     const size_t host_need = sizeof(int32_t) * (size_t)(nw + too_big.size() + 2);
-    char* old_dev = c->dev;
+    const uint64_t gen_before = c->dev_gen;
     if (!ensure_dev(c, need) || !ensure_host(c, host_need)) {
         release_ctx(c);
         if (err) *err = E_ALLOC;
         return GA_DEVICE_ERROR;
     }
     layout(c->dev, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
-    if (c->dev != old_dev) cudaMemcpyAsync(dpure, pure.data(), 2 * (size_t)n, cudaMemcpyHostToDevice, st);
+    if (c->dev_gen != gen_before) cudaMemcpyAsync(dpure, pure.data(), 2 * (size_t)n, cudaMemcpyHostToDevice, st);
     D.pure = dpure;
     int32_t* hwork = reinterpret_cast<int32_t*>(c->host);
     flatten_plan(P, hwork);

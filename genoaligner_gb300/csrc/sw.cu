@@ -312,7 +312,7 @@ int sw_width_for(int n)
 {
     static const int maxc = [] {
         const char* e = getenv("GA_SW_MAXC");
-        const int v = e ? atoi(e) : 32;
+        const int v = e ? atoi(e) : 8;
         return (v == 8 || v == 16) ? v : 32;
     }();
     if (n <= 256 || maxc == 8) return 8;
