@@ -72,7 +72,9 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_align_batch_ex", "ga_align_sw_batch_ex", "ga_wfa_device", "ga_sw_device",
            "ga_backend_name", "ga_device_name", "ga_device_available", "ga_kernel_launches",
            "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
-           "ga_profile_kernel_name", "ga_bench_int_peak"]
+           "ga_profile_kernel_name", "ga_bench_int_peak", "ga_cost_model_nparams", "ga_cost_model_set",
+           "ga_cost_model_get", "ga_wfa_features", "ga_mlp_forward", "ga_mlp_gradient", "ga_mlp_train_step",
+           "ga_wfa_device_ex", "ga_wfa_route_stats"]
 
 _lib = None
 
@@ -121,6 +123,24 @@ def load(build: bool = True):
     L.ga_profile_kernel_name.restype = ctypes.c_char_p
     L.ga_bench_int_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.ga_bench_int_peak.restype = i32
+    L.ga_cost_model_nparams.restype = i32
+    L.ga_cost_model_set.argtypes = [p, i32]
+    L.ga_cost_model_set.restype = i32
+    L.ga_cost_model_get.argtypes = [p, i32]
+    L.ga_cost_model_get.restype = i32
+    L.ga_wfa_features.argtypes = [ctypes.POINTER(DeviceBatch), p, p, p]
+    L.ga_wfa_features.restype = i32
+    L.ga_mlp_forward.argtypes = [p, i32, p, p]
+    L.ga_mlp_forward.restype = i32
+    L.ga_mlp_gradient.argtypes = [p, p, i32, p, p]
+    L.ga_mlp_gradient.restype = i32
+    L.ga_mlp_train_step.argtypes = [p, p, i32, ctypes.c_float, p, p]
+    L.ga_mlp_train_step.restype = i32
+    L.ga_wfa_device_ex.argtypes = [ctypes.POINTER(DeviceBatch), i32, i32, ctypes.POINTER(Options), p, p, p, p,
+                                   ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_wfa_device_ex.restype = i32
+    L.ga_wfa_route_stats.argtypes = [p, i32]
+    L.ga_wfa_route_stats.restype = i32
     _lib = L
     return L
 
@@ -327,7 +347,7 @@ def last_transfer_bytes():
 
 KERNEL_IDS = {"pack2": 0, "wfa_score": 1, "wfa_trace": 2, "sw8_score": 3, "sw16_score": 4, "sw32_score": 5,
               "sw8_trace": 6, "sw16_trace": 7, "sw32_trace": 8, "int_peak": 9, "kmer_sketch": 10, "mlp": 11,
-              "sw16x2_trace": 12}
+              "sw16x2_trace": 12, "route": 13}
 
 
 def profile(on: bool):
@@ -413,12 +433,14 @@ class DeviceBatchT:
                              self.out_off.data_ptr(), self.n, 0)
 
 
-def wfa_device(batch: DeviceBatchT, smax, trace, out_score, out_len, out_cigar, stream=None):
+def wfa_device(batch: DeviceBatchT, smax, trace, out_score, out_len, out_cigar, stream=None, learned=False):
     err = ctypes.c_char_p()
-    st = load().ga_wfa_device(ctypes.byref(batch.c), smax, 1 if trace else 0, out_score.data_ptr(),
-                              out_len.data_ptr() if out_len is not None else None,
-                              out_cigar.data_ptr() if out_cigar is not None else None,
-                              stream, ctypes.byref(err))
+    o = _opts(0, learned)
+    st = load().ga_wfa_device_ex(ctypes.byref(batch.c), smax, 1 if trace else 0, ctypes.byref(o),
+                                 out_score.data_ptr(),
+                                 out_len.data_ptr() if out_len is not None else None,
+                                 out_cigar.data_ptr() if out_cigar is not None else None,
+                                 stream, ctypes.byref(err))
     if st != GA_OK:
         raise RuntimeError(f"ga_wfa_device failed: {err.value}")
 
@@ -518,3 +540,82 @@ def align_sw_batch_packed(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, 
         st = L.ga_align_sw_batch(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes, ctypes.byref(info))
     return PackedResult(Status(st), info.error.decode() if info.error else None, res, cig,
                         info.resolved_count, info.unresolved_count)
+
+
+# ---------------------------------------------------------- learned model --
+def cost_model_nparams() -> int:
+    return int(load().ga_cost_model_nparams())
+
+
+def cost_model_set(params: np.ndarray):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    st = load().ga_cost_model_set(p.ctypes.data, int(p.shape[0]))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_cost_model_set failed ({st})")
+
+
+def cost_model_get() -> np.ndarray:
+    p = np.zeros(cost_model_nparams(), np.float32)
+    st = load().ga_cost_model_get(p.ctypes.data, int(p.shape[0]))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_cost_model_get failed ({st})")
+    return p
+
+
+def cost_model_init(seed: int = 0) -> np.ndarray:
+    """He-initialised parameters in the library's layout."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_in, fan_out in ((66, 128), (128, 128), (128, 2)):
+        parts.append(rng.normal(0, np.sqrt(2.0 / fan_in), size=fan_out * fan_in).astype(np.float32))
+        parts.append(np.zeros(fan_out, np.float32))
+    return np.concatenate(parts)
+
+
+def wfa_features(batch: "DeviceBatchT"):
+    """(features [n,66] float32, lower bound [n] int32) as torch tensors on the batch's device."""
+    import torch
+    dev = batch.seq.device
+    feat = torch.empty((batch.n, 66), dtype=torch.float32, device=dev)
+    lb = torch.empty(batch.n, dtype=torch.int32, device=dev)
+    st = load().ga_wfa_features(ctypes.byref(batch.c), feat.data_ptr(), lb.data_ptr(), None)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_wfa_features failed ({st})")
+    return feat, lb
+
+
+def mlp_forward(feat):
+    import torch
+    y = torch.empty((feat.shape[0], 2), dtype=torch.float32, device=feat.device)
+    st = load().ga_mlp_forward(feat.data_ptr(), int(feat.shape[0]), y.data_ptr(), None)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_mlp_forward failed ({st})")
+    return y
+
+
+def mlp_gradient(feat, target):
+    g = np.zeros(cost_model_nparams(), np.float32)
+    loss = np.zeros(1, np.float32)
+    st = load().ga_mlp_gradient(feat.data_ptr(), target.data_ptr(), int(feat.shape[0]), g.ctypes.data,
+                                loss.ctypes.data)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_mlp_gradient failed ({st})")
+    return g, float(loss[0])
+
+
+def mlp_train_step(feat, target, lr: float) -> float:
+    loss = np.zeros(1, np.float32)
+    st = load().ga_mlp_train_step(feat.data_ptr(), target.data_ptr(), int(feat.shape[0]), ctypes.c_float(lr),
+                                  loss.ctypes.data, None)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_mlp_train_step failed ({st})")
+    return float(loss[0])
+
+
+def wfa_route_stats(rounds: int = 12):
+    """(small queue, big queue, [escalated after round r ...]) of the last learned call."""
+    out = np.zeros(2 + rounds, np.int32)
+    st = load().ga_wfa_route_stats(out.ctypes.data, int(out.shape[0]))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_wfa_route_stats failed ({st})")
+    return int(out[0]), int(out[1]), [int(x) for x in out[2:]]

@@ -49,6 +49,15 @@ void launch_begin(int kernel_id, cudaStream_t st)
     t_prof_cur = r;
 }
 
+static bool profiling_on()
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    return g_prof_on;
+}
+
+// Launches replayed through a CUDA graph count like direct ones.
+static void note_graph_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
 void launch_end(int kernel_id, cudaStream_t st)
 {
     std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -162,6 +171,8 @@ struct Ctx {
     char* dev = nullptr;
     size_t dev_cap = 0;
     uint64_t dev_gen = 0;           // bumped whenever the device arena is reallocated
+    cudaGraphExec_t gexec = nullptr;  // the learned WFA path, captured once per launch shape
+    uint64_t gkey[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     char* host = nullptr;
     size_t host_cap = 0;
 };
@@ -293,10 +304,154 @@ int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, con
     return GA_OK;
 }
 
+// Device scratch of one WFA batch: the 2-bit arena and purity flags, the
+// per-warp wavefront stacks, the work counter; for the learned path also the
+// features, lower bounds, predictions, bucket counts and the queues.
+struct WfaScratch {
+    uint64_t* packed = nullptr;
+    uint8_t* pure = nullptr;
+    int32_t* stack = nullptr;
+    int32_t* ctr = nullptr;          // 64 ints: plain counter; learned: round counters
+    float* feat = nullptr;
+    int32_t* lb = nullptr;
+    float* y = nullptr;
+    int32_t* counts = nullptr;       // 2*buckets + 2
+    int32_t* starts = nullptr;       // 2*buckets
+    int2* big = nullptr;
+    int2* small = nullptr;
+    int2* esc[2] = {nullptr, nullptr};
+    int slots = 0;
+    int64_t stack_slot = 0;
+    int warp_smem = 0;
+    int rounds = 0;
+};
+
+static int bit_length(int x) { int b = 0; while (x > 0) { ++b; x >>= 1; } return b; }
+
+static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, int sm_count)
+{
+    if (learned) {
+        prepare_mlp();
+        S.slots = (int)std::min<int64_t>(routed_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
+        S.stack_slot = routed_stack_slot(smax);
+        S.warp_smem = routed_warp_smem(smax);
+        S.rounds = bit_length(smax) + 1;
+    } else {
+        S.slots = (int)std::min<int64_t>(wfa_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
+        S.stack_slot = (int64_t)(smax + 1) * (smax + 1);
+    }
+    if (trace) {
+        const int64_t budget = (int64_t)16 << 30;     // stack memory cap
+        S.slots = (int)std::min<int64_t>(S.slots, std::max<int64_t>(4, budget / (S.stack_slot * 4) / 4 * 4));
+    }
+}
+
+static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace, bool learned)
+{
+    S.packed = k.take<uint64_t>(arena / 32 + 2);
+    S.pure = k.take<uint8_t>(2 * (size_t)n);
+    S.ctr = k.take<int32_t>(64, 256);
+    S.stack = trace ? k.take<int32_t>((size_t)S.slots * S.stack_slot) : nullptr;
+    if (learned) {
+        S.feat = k.take<float>((size_t)n * 66);
+        S.lb = k.take<int32_t>(n);
+        S.y = k.take<float>(2 * (size_t)n);
+        S.counts = k.take<int32_t>(2 * route_buckets() + 2);
+        S.starts = k.take<int32_t>(2 * route_buckets());
+        S.big = k.take<int2>(n);
+        S.small = k.take<int2>(n);
+        S.esc[0] = k.take<int2>(n);
+        S.esc[1] = k.take<int2>(n);
+    }
+}
+
+// Every launch of one WFA batch on stream st (inputs already on the device).
+static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool trace, bool learned,
+                               int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
+{
+    D.packed = S.packed;
+    D.pure = S.pure;
+    WfaArgs A;
+    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
+    A.out_score = score; A.out_len = len; A.out_cigar = cig;
+    A.stack = S.stack; A.stack_slot = S.stack_slot; A.counter = S.ctr; A.err = err;
+    cudaError_t e = cudaMemsetAsync(S.ctr, 0, 64 * sizeof(int32_t), st);
+    if (e == cudaSuccess) e = launch_pack(D, S.packed, S.pure, st);
+    if (e != cudaSuccess) return e;
+    if (!learned) return launch_wfa(A, S.slots, st);
+    const int NB = route_buckets();
+    if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 2), st)) != cudaSuccess) return e;
+    if ((e = launch_sketch(D, S.feat, S.lb, st)) != cudaSuccess) return e;
+    if ((e = launch_mlp_forward(S.feat, D.n, S.y, st)) != cudaSuccess) return e;
+    if ((e = launch_route(D, S.y, S.lb, smax, score, len, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess)
+        return e;
+    // ctr layout: [0..31] next counters (2 per round), [32..63] escalation counts
+    for (int r = 0; r < S.rounds; ++r) {
+        RoutedArgs R;
+        R.A = A;
+        R.warp_smem = S.warp_smem;
+        R.big = r == 0 ? S.big : S.esc[(r - 1) & 1];
+        R.big_count = r == 0 ? S.counts + 2 * NB : S.ctr + 32 + (r - 1);
+        R.big_next = S.ctr + 2 * r;
+        R.small = r == 0 ? S.small : nullptr;
+        R.small_count = r == 0 ? S.counts + 2 * NB + 1 : nullptr;
+        R.small_next = S.ctr + 2 * r + 1;
+        R.esc = S.esc[r & 1];
+        R.esc_count = S.ctr + 32 + r;
+        if ((e = launch_routed(R, S.slots, st)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Learned path as one CUDA graph, cached per context by everything the
+// launches bake in.
+static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace,
+                                 int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
+{
+    const uint64_t key[8] = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
+                             (uint64_t)trace, (uint64_t)(uintptr_t)score, (uint64_t)(uintptr_t)cig,
+                             (uint64_t)(uintptr_t)D.a_off};
+    if (!c->gexec || std::memcmp(key, c->gkey, sizeof(key)) != 0) {
+        if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, true, score, len, cig, err, st);
+        e = cudaStreamEndCapture(st, &g);
+        if (e1 != cudaSuccess || e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e1 != cudaSuccess ? e1 : e; }
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { c->gexec = nullptr; return e; }
+        std::memcpy(c->gkey, key, sizeof(key));
+    }
+    note_graph_launches(S.rounds + 6);
+    return cudaGraphLaunch(c->gexec, st);
+}
+
+static bool profiling_on();
+
+// Where the calling thread's last learned WFA run left its queue counters.
+struct RouteRecord {
+    Ctx* c = nullptr;
+    uint64_t gen = 0;
+    const int32_t* counts = nullptr;
+    const int32_t* ctr = nullptr;
+    int rounds = 0;
+};
+static thread_local RouteRecord t_route;
+
+static void note_route(Ctx* c, const WfaScratch& S)
+{
+    t_route.c = c;
+    t_route.gen = c->dev_gen;
+    t_route.counts = S.counts;
+    t_route.ctr = S.ctr;
+    t_route.rounds = S.rounds;
+}
+
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
                   const WfaFinish& fin, const char** err)
 {
-    (void)learned;
     *err = nullptr;
     if (n <= 0) return GA_OK;
     if (int32_t st = wfa_check(reqs, n, max_smax, err)) return st;
@@ -306,6 +461,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
         smax = std::min(smax, (int)reqs[i].smax);
         trace |= reqs[i].with_cigar != 0;
     }
+    learned = learned && cost_model_loaded();
 
     // plan: 32-aligned sequence offsets, CIGAR slot offsets
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
@@ -323,55 +479,34 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
     if (!c) return GA_DEVICE_ERROR;
     struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
 
-    const int max_slots = wfa_max_slots(smax, trace, c->sm_count);
-    int slots = std::min<int64_t>(max_slots, ((int64_t)n + 3) / 4 * 4);
-    const int64_t stack_slot = (int64_t)(smax + 1) * (smax + 1);
-    if (trace) {
-        const int64_t budget = (int64_t)16 << 30;     // stack memory cap
-        const int64_t cap = std::max<int64_t>(4, budget / (stack_slot * 4) / 4 * 4);
-        slots = (int)std::min<int64_t>(slots, cap);
-    }
-
-    // device layout: [a_off a_len b_off b_len out_off | seq] [packed pure] [score len cigar | err] [stack counter]
-    auto layout = [&](char* base, bool host, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl,
-                      int64_t** po, uint8_t** seq, uint64_t** packed, uint8_t** pure, int32_t** sc,
-                      int32_t** ln, char** cg, int32_t** er, int32_t** stk, int32_t** ctr) -> size_t {
-        Carve k(base);
+    WfaScratch S;
+    size_wfa(S, n, smax, trace, learned, c->sm_count);
+    // layout: [a_off a_len b_off b_len out_off | seq] [score len cigar | err] then device scratch
+    int64_t *ha, *hb, *ho, *da, *db, *dout;
+    int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
+    uint8_t *hseq, *dseq;
+    char *hcg, *dcg;
+    auto io = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po, uint8_t** ps,
+                  int32_t** psc, int32_t** pln, char** pcg, int32_t** per) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
         *po = k.take<int64_t>(n);
-        *seq = k.take<uint8_t>(arena);
-        const size_t in_end = k.off;
-        if (host) {
-            // host staging: inputs, then outputs
-            *sc = k.take<int32_t>(n); *ln = k.take<int32_t>(n); *cg = k.take<char>(cig + 1);
-            *er = k.take<int32_t>(1);
-            (void)in_end;
-            return k.off;
-        }
-        *packed = k.take<uint64_t>(arena / 32 + 2);
-        *pure = k.take<uint8_t>(2 * (size_t)n);
-        *sc = k.take<int32_t>(n); *ln = k.take<int32_t>(n); *cg = k.take<char>(cig + 1);
-        *er = k.take<int32_t>(1);
-        *ctr = k.take<int32_t>(1, 4);
-        *stk = trace ? k.take<int32_t>((size_t)slots * stack_slot) : nullptr;
-        return k.off;
+        *ps = k.take<uint8_t>(arena);
+        *psc = k.take<int32_t>(n); *pln = k.take<int32_t>(n); *pcg = k.take<char>(cig + 1);
+        *per = k.take<int32_t>(1, 4);
     };
-    int64_t *ha, *hb, *ho, *da, *db, *dout;
-    int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der, *dstk, *dctr, *dummy_i;
-    uint8_t *hseq, *dseq, *dpure, *dummy_u8;
-    uint64_t *dpacked, *dummy_u64;
-    char *hcg, *dcg;
-    const size_t host_bytes = layout(nullptr, true, &ha, &hal, &hb, &hbl, &ho, &hseq, &dummy_u64, &dummy_u8,
-                                     &hsc, &hln, &hcg, &her, &dummy_i, &dummy_i);
-    const size_t dev_bytes = layout(nullptr, false, &da, &dal, &db, &dbl, &dout, &dseq, &dpacked, &dpure,
-                                    &dsc, &dln, &dcg, &der, &dstk, &dctr);
-    if (fail_here(1) || !ensure_dev(c, dev_bytes)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    if (!ensure_host(c, host_bytes)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
-    layout(c->host, true, &ha, &hal, &hb, &hbl, &ho, &hseq, &dummy_u64, &dummy_u8, &hsc, &hln, &hcg, &her,
-           &dummy_i, &dummy_i);
-    layout(c->dev, false, &da, &dal, &db, &dbl, &dout, &dseq, &dpacked, &dpure, &dsc, &dln, &dcg, &der, &dstk,
-           &dctr);
+    Carve hk(nullptr), dk(nullptr);
+    io(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &her);
+    io(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &der);
+    carve_wfa(dk, S, n, arena, trace, learned);
+    if (fail_here(1) || !ensure_dev(c, dk.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    {
+        Carve h(c->host), d(c->dev);
+        io(h, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &her);
+        io(d, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &der);
+        carve_wfa(d, S, n, arena, trace, learned);
+    }
 
     // stage inputs
     parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
@@ -393,17 +528,15 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
         *err = E_H2D;
         return GA_DEVICE_ERROR;
     }
-    cudaMemsetAsync(dctr, 0, sizeof(int32_t), c->stream);
-
     PairDesc D;
-    D.seq = dseq; D.packed = dpacked; D.pure = dpure;
+    D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
     D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
-    WfaArgs A;
-    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
-    A.out_score = dsc; A.out_len = dln; A.out_cigar = dcg;
-    A.stack = dstk; A.stack_slot = stack_slot; A.counter = dctr; A.err = der;
-    if (fail_here(3) || launch_pack(D, dpacked, dpure, c->stream) != cudaSuccess ||
-        launch_wfa(A, slots, c->stream) != cudaSuccess) {
+    cudaError_t le;
+    if (fail_here(3)) le = cudaErrorLaunchFailure;
+    else if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace, dsc, dln, dcg, der, c->stream);
+    else le = enqueue_wfa(S, D, smax, trace, learned, dsc, dln, dcg, der, c->stream);
+    if (learned) note_route(c, S);
+    if (le != cudaSuccess) {
         cudaGetLastError();
         *err = E_LAUNCH;
         return GA_DEVICE_ERROR;
@@ -1010,8 +1143,8 @@ int32_t ga_align_sw_batch(const ga_sw_request* reqs, int32_t n, ga_sw_result* re
 }
 
 // ------------------------------------------------------ device-resident --
-int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int32_t* out_score,
-                      int32_t* out_len, char* out_cigar, void* stream, const char** err)
+int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, const ga_options* opt,
+                         int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream, const char** err)
 {
     const char* e = nullptr;
     if (!b || b->n < 0 || smax < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off ||
@@ -1024,35 +1157,31 @@ int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int
         return GA_INVALID_ARGUMENT;
     }
     if (b->n == 0) return GA_OK;
+    const bool learned = opt && opt->learned && cost_model_loaded();
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    const int max_slots = wfa_max_slots(smax, trace != 0, c->sm_count);
-    int slots = (int)std::min<int64_t>(max_slots, ((int64_t)b->n + 3) / 4 * 4);
-    const int64_t stack_slot = (int64_t)(smax + 1) * (smax + 1);
-    if (trace) slots = (int)std::min<int64_t>(slots, std::max<int64_t>(4, ((int64_t)16 << 30) / (stack_slot * 4) / 4 * 4));
+    WfaScratch S;
+    size_wfa(S, b->n, smax, trace != 0, learned, c->sm_count);
     Carve k(nullptr);
-    k.take<uint64_t>(b->seq_bytes / 32 + 2);
-    k.take<uint8_t>(2 * (size_t)b->n);
-    k.take<int32_t>(64, 256);
-    if (trace) k.take<int32_t>((size_t)slots * stack_slot);
+    carve_wfa(k, S, b->n, b->seq_bytes, trace != 0, learned);
+    k.take<int32_t>(1, 4);                                           // error word
     if (!ensure_dev(c, k.off)) { release_ctx(c); if (err) *err = E_ALLOC; return GA_DEVICE_ERROR; }
     Carve d(c->dev);
-    uint64_t* packed = d.take<uint64_t>(b->seq_bytes / 32 + 2);
-    uint8_t* pure = d.take<uint8_t>(2 * (size_t)b->n);
-    int32_t* ctr = d.take<int32_t>(64, 256);
-    int32_t* stk = trace ? d.take<int32_t>((size_t)slots * stack_slot) : nullptr;
-    cudaMemsetAsync(ctr, 0, 64 * sizeof(int32_t), st);
+    carve_wfa(d, S, b->n, b->seq_bytes, trace != 0, learned);
+    int32_t* derr = d.take<int32_t>(1, 4);
     PairDesc D;
-    D.seq = b->seq; D.packed = packed; D.pure = pure;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
     D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
     D.out_off = b->out_off; D.n = b->n;
-    WfaArgs A;
-    A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
-    A.out_score = out_score; A.out_len = out_len; A.out_cigar = out_cigar;
-    A.stack = stk; A.stack_slot = stack_slot; A.counter = ctr; A.err = ctr + 1;
     int32_t rc = GA_OK;
-    if (launch_pack(D, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
+    cudaError_t le = cudaMemsetAsync(derr, 0, sizeof(int32_t), st);
+    if (le == cudaSuccess) {
+        if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace != 0, out_score, out_len, out_cigar, derr, st);
+        else le = enqueue_wfa(S, D, smax, trace != 0, learned, out_score, out_len, out_cigar, derr, st);
+        if (learned) note_route(c, S);
+    }
+    if (le != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = E_LAUNCH;
         rc = GA_DEVICE_ERROR;
@@ -1067,6 +1196,33 @@ int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int
     }
     release_ctx(c);
     return rc;
+}
+
+int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
+{
+    const RouteRecord r = t_route;
+    if (!r.c || !out || max < 2) return GA_INVALID_ARGUMENT;
+    if (r.c->dev_gen != r.gen) return GA_INVALID_ARGUMENT;
+    const int NB = route_buckets();
+    int32_t counts[64], esc[32];
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(counts, r.counts, sizeof(int32_t) * (2 * NB + 2), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(esc, r.ctr + 32, sizeof(int32_t) * 32, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    out[0] = counts[2 * NB + 1];              // small queue (8-lane groups)
+    out[1] = counts[2 * NB];                  // big queue (whole warps)
+    int k = 2;
+    for (int q = 0; q < r.rounds && k < max; ++q) out[k++] = esc[q];
+    for (; k < max; ++k) out[k] = 0;
+    return GA_OK;
+}
+
+int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int32_t* out_score,
+                      int32_t* out_len, char* out_cigar, void* stream, const char** err)
+{
+    return ga_wfa_device_ex(b, smax, trace, nullptr, out_score, out_len, out_cigar, stream, err);
 }
 
 int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, int64_t cell_limit,
@@ -1250,7 +1406,7 @@ const char* ga_profile_kernel_name(int32_t kernel_id)
 {
     static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
                                          "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
-                                         "kmer_sketch", "mlp", "sw16x2_trace"};
+                                         "kmer_sketch", "mlp", "sw16x2_trace", "route"};
     return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
 }
 

@@ -54,7 +54,32 @@ struct Sw16Args {
     int32_t* err;
 };
 
+// The learned-bucketed WFA path (wfa_routed.cu).
+struct RoutedArgs {
+    WfaArgs A;                   // A.smax = the batch smax
+    const int2* big;             // (pair, first smax), served by whole warps
+    const int32_t* big_count;    // device-side count
+    int32_t* big_next;
+    const int2* small;           // served by 8-lane groups (null: none)
+    const int32_t* small_count;
+    int32_t* small_next;
+    int2* esc;                   // escalations: (pair, doubled smax)
+    int32_t* esc_count;
+    int32_t warp_smem;           // shared-memory ints per warp
+};
+
 cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st);
+cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
+cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
+bool cost_model_loaded();
+void prepare_mlp();
+int route_buckets();
+int64_t routed_stack_slot(int smax);
+int routed_warp_smem(int smax);
+int routed_max_slots(int smax, bool trace, int sm_count);
+cudaError_t launch_route(const PairDesc& D, const float* y, const int32_t* lb, int smax, int32_t* out_score,
+                         int32_t* out_len, int32_t* counts, int32_t* starts, int2* big, int2* small, cudaStream_t st);
+cudaError_t launch_routed(const RoutedArgs& R, int slots, cudaStream_t st);
 
 size_t wfa_smem_bytes(int smax);
 int wfa_max_slots(int smax, bool trace, int sm_count);

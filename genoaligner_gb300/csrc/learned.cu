@@ -1,0 +1,477 @@
+// learned.cu -- the learned cost model: k-mer sketch, MLP forward/backward,
+// Adam, all hand-written kernels.
+//
+// Features of one pair (66 floats): for each of the 64 DNA 3-mers, (count in
+// a - count in b) / 8, then len(a) / 256 and len(b) / 256.  3-mers are taken
+// on the 2-bit codes ((c >> 1) ^ (c >> 2)) & 3 of the raw bytes, so A/C/G/T
+// map to 0..3 and any other byte aliases onto one of them.
+//
+// The sketch also yields an exact lower bound on the edit distance: an edit
+// changes at most 3 3-mers of each string, so d >= L1(count difference) / 6,
+// and d >= |len(a) - len(b)|.  Aliasing only merges characters, which can only
+// lower the distance of the aliased strings, so the bound holds for the
+// original strings.  A pair whose bound exceeds the batch smax is unresolved
+// without running WFA -- the same answer the full search gives.
+//
+// MLP: 66 -> 128 (ReLU) -> 128 (ReLU) -> 2, weights stored as bf16 and
+// computed in fp32 (fp32 master copy for Adam).  Outputs: log2(d + 1) and
+// log2(wavefront cells + 1) with wavefront cells = (d + 1)^2.  It is a tiny
+// GEMM (25k multiply-adds per pair), run as shared-memory-tiled FMA: 64 pairs
+// per block, 256 threads, every thread 32 outputs of one pair.
+#include <mutex>
+#include <vector>
+
+#include "../../include/genoaligner_gb300.h"
+#include "kernels.cuh"
+#include <cuda_bf16.h>
+
+namespace ga {
+
+constexpr int NF = 66, NH1 = 128, NH2 = 128, NO = 2;
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH1 * NF, OFF_W2 = OFF_B1 + NH1, OFF_B2 = OFF_W2 + NH2 * NH1,
+              OFF_W3 = OFF_B2 + NH2, OFF_B3 = OFF_W3 + NO * NH2, NPARAM = OFF_B3 + NO;
+constexpr int TILE = 64;
+
+// ------------------------------------------------------------------ sketch --
+// One warp per pair: 3-mer histograms of both sides in shared memory.
+__global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restrict__ feat,
+                                                     int32_t* __restrict__ lower_bound)
+{
+    __shared__ int hist[8][64];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nwarps) {
+        hist[wib][lane] = 0;
+        hist[wib][lane + 32] = 0;
+        __syncwarp();
+        for (int side = 0; side < 2; ++side) {
+            const uint8_t* s = D.seq + (side ? D.b_off[p] : D.a_off[p]);
+            const int L = side ? D.b_len[p] : D.a_len[p];
+            const int sign = side ? -1 : 1;
+            for (int q = lane; q + 2 < L; q += 32) {
+                const uint32_t c0 = __ldg(s + q), c1 = __ldg(s + q + 1), c2 = __ldg(s + q + 2);
+                const int k = (int)((((c0 >> 1) ^ (c0 >> 2)) & 3u) * 16 + (((c1 >> 1) ^ (c1 >> 2)) & 3u) * 4 +
+                                    (((c2 >> 1) ^ (c2 >> 2)) & 3u));
+                atomicAdd(&hist[wib][k], sign);
+            }
+        }
+        __syncwarp();
+        const int d0 = hist[wib][lane], d1 = hist[wib][lane + 32];
+        feat[(int64_t)p * NF + lane] = d0 * 0.125f;
+        feat[(int64_t)p * NF + lane + 32] = d1 * 0.125f;
+        int l1 = abs(d0) + abs(d1);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL, l1, o);
+        if (lane == 0) {
+            const int m = D.a_len[p], n = D.b_len[p];
+            feat[(int64_t)p * NF + 64] = m * (1.0f / 256.0f);
+            feat[(int64_t)p * NF + 65] = n * (1.0f / 256.0f);
+            if (lower_bound) lower_bound[p] = max(abs(m - n), (l1 + 5) / 6);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------- MLP --
+struct MlpParams {
+    const __nv_bfloat16* w;   // NPARAM bf16 (weights and biases)
+};
+
+// Shared-memory image of one tile's layers.
+struct MlpSmem {
+    float W[NH2 * NH1];        // the current layer's weights, transposed [in][out]
+    float X[TILE * (NF + 2)];
+    float H1[TILE * (NH1 + 1)];
+    float H2[TILE * (NH2 + 1)];
+};
+
+// out[r][o] = act(sum_i in[r][i] * W[o][i] + b[o]) for the tile's rows; W is
+// staged transposed in smem with outputs interleaved by 4 (o = 4k + oq) so the
+// four output groups of a warp read four different banks.
+template <int IN, int OUT, bool RELU>
+__device__ __forceinline__ void dense(const __nv_bfloat16* __restrict__ w, const __nv_bfloat16* __restrict__ b,
+                                      float* Ws, const float* in, int in_stride, float* out, int out_stride,
+                                      int rows)
+{
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < IN * OUT; idx += blockDim.x) {
+        const int o = idx / IN, i = idx - o * IN;
+        Ws[i * OUT + o] = __bfloat162float(w[idx]);
+    }
+    __syncthreads();
+    constexpr int PER = OUT / 4;                  // outputs per thread (4 threads per row)
+    const int r = threadIdx.x >> 2, oq = threadIdx.x & 3;
+    if (r < rows) {
+        float acc[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) acc[k] = __bfloat162float(b[4 * k + oq]);
+        for (int i = 0; i < IN; ++i) {
+            const float x = in[r * in_stride + i];
+            const float* wr = Ws + i * OUT;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) acc[k] = fmaf(x, wr[4 * k + oq], acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) out[r * out_stride + 4 * k + oq] = RELU ? fmaxf(acc[k], 0.f) : acc[k];
+    }
+}
+
+// The output layer (2 outputs) by one thread per row.
+__device__ __forceinline__ void dense_out(const __nv_bfloat16* __restrict__ w, const float* H2, float* y, int rows)
+{
+    const int r = threadIdx.x;
+    if (r < rows) {
+        float a0 = __bfloat162float(w[OFF_B3]), a1 = __bfloat162float(w[OFF_B3 + 1]);
+        for (int i = 0; i < NH2; ++i) {
+            const float h = H2[r * (NH2 + 1) + i];
+            a0 = fmaf(h, __bfloat162float(w[OFF_W3 + i]), a0);
+            a1 = fmaf(h, __bfloat162float(w[OFF_W3 + NH2 + i]), a1);
+        }
+        y[2 * r] = a0;
+        y[2 * r + 1] = a1;
+    }
+}
+
+__device__ __forceinline__ void forward_tile(const __nv_bfloat16* w, const float* __restrict__ feat, int64_t base,
+                                             int rows, MlpSmem& S, float* ytile)
+{
+    for (int idx = threadIdx.x; idx < rows * NF; idx += blockDim.x) {
+        const int r = idx / NF, i = idx - r * NF;
+        S.X[r * (NF + 2) + i] = feat[(base + r) * NF + i];
+    }
+    dense<NF, NH1, true>(w + OFF_W1, w + OFF_B1, S.W, S.X, NF + 2, S.H1, NH1 + 1, rows);
+    dense<NH1, NH2, true>(w + OFF_W2, w + OFF_B2, S.W, S.H1, NH1 + 1, S.H2, NH2 + 1, rows);
+    __syncthreads();
+    dense_out(w, S.H2, ytile, rows);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16* __restrict__ w,
+                                                          const float* __restrict__ feat, int n, float* __restrict__ y)
+{
+    extern __shared__ float mlp_smem[];
+    MlpSmem& S = *reinterpret_cast<MlpSmem*>(mlp_smem);
+    __shared__ float ytile[2 * TILE];
+    for (int64_t base = (int64_t)blockIdx.x * TILE; base < n; base += (int64_t)gridDim.x * TILE) {
+        const int rows = (n - base < TILE) ? (int)(n - base) : TILE;
+        forward_tile(w, feat, base, rows, S, ytile);
+        for (int idx = threadIdx.x; idx < 2 * rows; idx += blockDim.x) y[2 * base + idx] = ytile[idx];
+        __syncthreads();
+    }
+}
+
+// Forward + backward of the mean squared error over the batch; gradients of
+// every parameter (with respect to the bf16-rounded weights) accumulate into
+// grad (fp32) and the summed squared error into loss.
+__global__ void __launch_bounds__(256) mlp_backward_kernel(const __nv_bfloat16* __restrict__ w,
+                                                           const float* __restrict__ feat,
+                                                           const float* __restrict__ target, int n,
+                                                           float inv_batch, float* __restrict__ grad,
+                                                           float* __restrict__ loss)
+{
+    extern __shared__ float mlp_smem[];
+    MlpSmem& S = *reinterpret_cast<MlpSmem*>(mlp_smem);
+    __shared__ float ytile[2 * TILE];
+    __shared__ float dy[2 * TILE];
+    for (int64_t base = (int64_t)blockIdx.x * TILE; base < n; base += (int64_t)gridDim.x * TILE) {
+        const int rows = (n - base < TILE) ? (int)(n - base) : TILE;
+        forward_tile(w, feat, base, rows, S, ytile);
+        // dL/dy = 2 (y - t) / B
+        float lsum = 0.f;
+        for (int idx = threadIdx.x; idx < 2 * TILE; idx += blockDim.x) {
+            float g = 0.f;
+            if (idx < 2 * rows) {
+                const float e = ytile[idx] - target[2 * base + idx];
+                lsum += e * e;
+                g = 2.f * e * inv_batch;
+            }
+            dy[idx] = g;
+        }
+        for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(FULL, lsum, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(loss, lsum);
+        __syncthreads();
+        // output layer: dW3, db3; dH2 = dy W3 * relu'(H2) (H2 overwritten in place)
+        for (int idx = threadIdx.x; idx < NO * NH2; idx += blockDim.x) {
+            const int o = idx / NH2, i = idx - o * NH2;
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g = fmaf(dy[2 * r + o], S.H2[r * (NH2 + 1) + i], g);
+            atomicAdd(&grad[OFF_W3 + idx], g);
+        }
+        if (threadIdx.x < NO) {
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g += dy[2 * r + threadIdx.x];
+            atomicAdd(&grad[OFF_B3 + threadIdx.x], g);
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < rows * NH2; idx += blockDim.x) {
+            const int r = idx / NH2, i = idx - r * NH2;
+            float* h = &S.H2[r * (NH2 + 1) + i];
+            const float g = dy[2 * r] * __bfloat162float(w[OFF_W3 + i]) + dy[2 * r + 1] * __bfloat162float(w[OFF_W3 + NH2 + i]);
+            *h = (*h > 0.f) ? g : 0.f;
+        }
+        __syncthreads();
+        // layer 2: dW2[o][i] = sum_r dH2[r][o] H1[r][i]; db2; dH1 = dH2 W2 * relu'(H1)
+        for (int idx = threadIdx.x; idx < NH2 * NH1; idx += blockDim.x) {
+            const int o = idx / NH1, i = idx - o * NH1;
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g = fmaf(S.H2[r * (NH2 + 1) + o], S.H1[r * (NH1 + 1) + i], g);
+            atomicAdd(&grad[OFF_W2 + idx], g);
+        }
+        for (int o = threadIdx.x; o < NH2; o += blockDim.x) {
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g += S.H2[r * (NH2 + 1) + o];
+            atomicAdd(&grad[OFF_B2 + o], g);
+        }
+        // W2 (not transposed) into S.W: W[o][i]
+        for (int idx = threadIdx.x; idx < NH2 * NH1; idx += blockDim.x) S.W[idx] = __bfloat162float(w[OFF_W2 + idx]);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < rows * NH1; idx += blockDim.x) {
+            const int r = idx / NH1, i = idx - r * NH1;
+            float g = 0.f;
+            for (int o = 0; o < NH2; ++o) g = fmaf(S.H2[r * (NH2 + 1) + o], S.W[o * NH1 + i], g);
+            // each thread reads and overwrites only its own H1 entry: dH1 in place
+            const float h = S.H1[r * (NH1 + 1) + i];
+            S.H1[r * (NH1 + 1) + i] = (h > 0.f) ? g : 0.f;
+        }
+        __syncthreads();
+        // layer 1: dW1[o][i] = sum_r dH1[r][o] X[r][i]; db1
+        for (int idx = threadIdx.x; idx < NH1 * NF; idx += blockDim.x) {
+            const int o = idx / NF, i = idx - o * NF;
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g = fmaf(S.H1[r * (NH1 + 1) + o], S.X[r * (NF + 2) + i], g);
+            atomicAdd(&grad[OFF_W1 + idx], g);
+        }
+        for (int o = threadIdx.x; o < NH1; o += blockDim.x) {
+            float g = 0.f;
+            for (int r = 0; r < rows; ++r) g += S.H1[r * (NH1 + 1) + o];
+            atomicAdd(&grad[OFF_B1 + o], g);
+        }
+        __syncthreads();
+    }
+}
+
+// Adam on the fp32 master copy, then the bf16 copy the forward pass reads.
+__global__ void adam_kernel(float* __restrict__ master, __nv_bfloat16* __restrict__ w, const float* __restrict__ grad,
+                            float* __restrict__ m1, float* __restrict__ m2, int n, float lr, float b1, float b2,
+                            float eps, float c1, float c2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float g = grad[i];
+        const float a = b1 * m1[i] + (1.f - b1) * g;
+        const float v = b2 * m2[i] + (1.f - b2) * g * g;
+        m1[i] = a;
+        m2[i] = v;
+        const float p = master[i] - lr * (a * c1) / (sqrtf(v * c2) + eps);
+        master[i] = p;
+        w[i] = __float2bfloat16(p);
+    }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = __float2bfloat16(src[i]);
+}
+
+// --------------------------------------------------------- model state --
+// One model per device: fp32 master, bf16 working copy, Adam moments, grads.
+struct Model {
+    float* master = nullptr;
+    __nv_bfloat16* w = nullptr;
+    float *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *loss = nullptr;
+    int step = 0;
+    bool ready = false;
+};
+static std::mutex g_model_mu;
+static Model g_models[16];
+
+static Model* model_for_current(bool create)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) { cudaGetLastError(); return nullptr; }
+    Model& M = g_models[dev];
+    if (!M.master && create) {
+        if (cudaMalloc(&M.master, NPARAM * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&M.w, NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess ||
+            cudaMalloc(&M.m1, NPARAM * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&M.m2, NPARAM * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&M.grad, NPARAM * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&M.loss, sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    return M.master ? &M : nullptr;
+}
+
+static size_t mlp_smem_bytes() { return sizeof(MlpSmem); }
+
+// Kernel attributes are set outside any stream capture (prepare_mlp is called
+// while planning a batch).
+void prepare_mlp()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
+        cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
+    });
+}
+
+static cudaError_t run_forward(const __nv_bfloat16* w, const float* feat, int n, float* y, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    prepare_mlp();
+    int blocks = (n + TILE - 1) / TILE;
+    if (blocks > 152 * 2) blocks = 152 * 2;
+    launch_begin(K_MLP, st);
+    mlp_forward_kernel<<<blocks, 256, mlp_smem_bytes(), st>>>(w, feat, n, y);
+    launch_end(K_MLP, st);
+    return cudaGetLastError();
+}
+
+static cudaError_t run_backward(const __nv_bfloat16* w, const float* feat, const float* target, int n, float* grad,
+                                float* loss, cudaStream_t st)
+{
+    prepare_mlp();
+    cudaMemsetAsync(grad, 0, NPARAM * sizeof(float), st);
+    cudaMemsetAsync(loss, 0, sizeof(float), st);
+    int blocks = (n + TILE - 1) / TILE;
+    if (blocks > 152 * 2) blocks = 152 * 2;
+    launch_begin(K_MLP, st);
+    mlp_backward_kernel<<<blocks, 256, mlp_smem_bytes(), st>>>(w, feat, target, n, 1.0f / (float)n, grad, loss);
+    launch_end(K_MLP, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    int blocks = (D.n + 7) / 8;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    launch_begin(K_SKETCH, st);
+    sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
+    launch_end(K_SKETCH, st);
+    return cudaGetLastError();
+}
+
+// The current device's model weights for inference, or null when none is loaded.
+const __nv_bfloat16* cost_model_weights()
+{
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    Model* M = model_for_current(false);
+    return (M && M->ready) ? M->w : nullptr;
+}
+
+bool cost_model_loaded() { return cost_model_weights() != nullptr; }
+
+cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st)
+{
+    const __nv_bfloat16* w = cost_model_weights();
+    if (!w) return cudaErrorNotReady;
+    return run_forward(w, feat, n, y, st);
+}
+
+}  // namespace ga
+
+using namespace ga;
+
+extern "C" {
+
+int32_t ga_cost_model_nparams(void) { return NPARAM; }
+
+int32_t ga_cost_model_set(const float* params, int32_t n)
+{
+    if (!params || n != NPARAM) return GA_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    Model* M = model_for_current(true);
+    if (!M) return GA_DEVICE_ERROR;
+    if (cudaMemcpy(M->master, params, NPARAM * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(M->m1, 0, NPARAM * sizeof(float)) != cudaSuccess ||
+        cudaMemset(M->m2, 0, NPARAM * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    to_bf16_kernel<<<64, 256>>>(M->master, M->w, NPARAM);
+    if (cudaDeviceSynchronize() != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    M->step = 0;
+    M->ready = true;
+    return GA_OK;
+}
+
+int32_t ga_cost_model_get(float* params, int32_t n)
+{
+    if (!params || n != NPARAM) return GA_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    Model* M = model_for_current(false);
+    if (!M || !M->ready) return GA_INVALID_ARGUMENT;
+    if (cudaMemcpy(params, M->master, NPARAM * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
+}
+
+int32_t ga_wfa_features(const ga_device_batch* b, float* feat, int32_t* lower_bound, void* stream)
+{
+    if (!b || b->n < 0 || !feat) return GA_INVALID_ARGUMENT;
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len; D.out_off = b->out_off; D.n = b->n;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (launch_sketch(D, feat, lower_bound, st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    if (!stream && cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    return GA_OK;
+}
+
+int32_t ga_mlp_forward(const float* feat, int32_t n, float* y, void* stream)
+{
+    if (!feat || !y || n < 0) return GA_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const cudaError_t e = launch_mlp_forward(feat, n, y, st);
+    if (e == cudaErrorNotReady) return GA_INVALID_ARGUMENT;
+    if (e != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    if (!stream && cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    return GA_OK;
+}
+
+int32_t ga_mlp_gradient(const float* feat, const float* target, int32_t n, float* grad_host, float* loss_host)
+{
+    if (!feat || !target || n <= 0 || !grad_host) return GA_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    Model* M = model_for_current(false);
+    if (!M || !M->ready) return GA_INVALID_ARGUMENT;
+    if (run_backward(M->w, feat, target, n, M->grad, M->loss, 0) != cudaSuccess ||
+        cudaMemcpy(grad_host, M->grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (loss_host && cudaMemcpy(loss_host, M->loss, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
+}
+
+int32_t ga_mlp_train_step(const float* feat, const float* target, int32_t n, float lr, float* loss_host, void* stream)
+{
+    if (!feat || !target || n <= 0) return GA_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    Model* M = model_for_current(false);
+    if (!M || !M->ready) return GA_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (run_backward(M->w, feat, target, n, M->grad, M->loss, st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    M->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f / (1.f - powf(b1, (float)M->step)), c2 = 1.f / (1.f - powf(b2, (float)M->step));
+    launch_begin(K_MLP, st);
+    adam_kernel<<<64, 256, 0, st>>>(M->master, M->w, M->grad, M->m1, M->m2, NPARAM, lr, b1, b2, 1e-8f, c1, c2);
+    launch_end(K_MLP, st);
+    if (cudaGetLastError() != cudaSuccess) return GA_DEVICE_ERROR;
+    if (loss_host) {
+        if (cudaMemcpyAsync(loss_host, M->loss, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            cudaGetLastError();
+            return GA_DEVICE_ERROR;
+        }
+        *loss_host /= (float)n;
+    }
+    return GA_OK;
+}
+
+}  // extern "C"

@@ -186,12 +186,51 @@ int32_t ga_wfa_device(const ga_device_batch* batch, int32_t smax, int32_t trace,
                       int32_t* out_score, int32_t* out_len, char* out_cigar,
                       void* stream, const char** err);
 
+/* ga_wfa_device with extension options (opt may be NULL): opt->learned = 1
+ * routes pairs by the cost model (loaded with ga_cost_model_set) through the
+ * bucketed persistent kernel, replayed as one CUDA graph; results are the
+ * same as without it. */
+int32_t ga_wfa_device_ex(const ga_device_batch* batch, int32_t smax, int32_t trace, const ga_options* opt,
+                         int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream,
+                         const char** err);
+
+/* Routing record of the calling thread's last learned WFA call: out[0] = pairs
+ * in the small queue (8-lane groups), out[1] = pairs in the big queue,
+ * out[2 + r] = pairs escalated after round r.  Synchronises the device. */
+int32_t ga_wfa_route_stats(int32_t* out, int32_t max);
+
 /* SW over a device batch, score + end cell + start cell + CIGAR.
  * out_pos[4*i .. 4*i+3] = start_i, start_j, end_i, end_j.  Pairs above
  * trace_cell_limit cells (< 0: no limit) get out_score = -2 (too large). */
 int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_t trace,
                      int64_t trace_cell_limit, int32_t* out_score, int32_t* out_pos,
                      int32_t* out_len, char* out_cigar, void* stream, const char** err);
+
+/* ------------------------------------------------------- learned model -- */
+
+/* The learned cost model (no counterpart in the reference): a k-mer sketch
+ * and an MLP 66 -> 128 -> 128 -> 2 that predicts log2(edit distance + 1) and
+ * log2(wavefront cells + 1) of a pair.  It only routes work (the smax tried
+ * first, the lane-group size, the queue); results never depend on it. */
+int32_t ga_cost_model_nparams(void);
+/* Load / read the fp32 parameters of the current device's model (layout: W1
+ * [128][66], b1 [128], W2 [128][128], b2 [128], W3 [2][128], b3 [2]). */
+int32_t ga_cost_model_set(const float* params, int32_t n);
+int32_t ga_cost_model_get(float* params, int32_t n);
+/* Features [n][66] and the exact q-gram lower bound of the edit distance of
+ * every pair of a device batch (a = pattern, b = text).  Device pointers. */
+int32_t ga_wfa_features(const ga_device_batch* batch, float* features, int32_t* lower_bound, void* stream);
+/* Inference: y[n][2] from features[n][66] (device pointers). */
+int32_t ga_mlp_forward(const float* features, int32_t n, float* y, void* stream);
+/* Gradient of the mean squared error over a batch (device features and
+ * targets [n][2]) with respect to every parameter, copied to grad_host
+ * (ga_cost_model_nparams() floats); loss_host gets the summed squared error. */
+int32_t ga_mlp_gradient(const float* features, const float* targets, int32_t n, float* grad_host,
+                        float* loss_host);
+/* One Adam step on a batch (device pointers); loss_host (optional) gets the
+ * batch mean squared error before the step. */
+int32_t ga_mlp_train_step(const float* features, const float* targets, int32_t n, float lr,
+                          float* loss_host, void* stream);
 
 /* WFA over a device batch, like ga_wfa_device, but without allocating any
  * device memory.  No counterpart in the reference.

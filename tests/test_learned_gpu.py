@@ -1,0 +1,113 @@
+"""The learned cost model on the GPU: exactness of the sketch bound, gradients
+of the hand-written backward kernel against a float64 reference, training,
+and the rule that routing never changes a result."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlp_ref
+from genoaligner_gb300 import api, cost_model, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(ps):
+    return api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
+
+
+def test_lower_bound_never_exceeds_distance():
+    ps = workloads.wfa_mixed(n=3000, seed=71)
+    f, lb = api.wfa_features(_batch(ps))
+    pats, txts = ps.lists()
+    ed = oracle.edit_distance(pats, txts)
+    lb = lb.cpu().numpy()
+    assert (lb <= ed).all()
+    assert (lb > 0).mean() > 0.5                 # the bound is not vacuous
+    feat = f.cpu().numpy()
+    assert np.allclose(feat[:, 64], ps.a_len / 256.0) and np.allclose(feat[:, 65], ps.b_len / 256.0)
+
+
+def test_mlp_forward_and_gradient_match_float64_reference():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5)
+    params = api.cost_model_init(seed=3)
+    params[-2:] = [1.0, -0.5]
+    api.cost_model_set(params)
+    x = rng.normal(0, 1, size=(300, 66)).astype(np.float32)
+    t = rng.normal(2, 1, size=(300, 2)).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    tt = torch.from_numpy(t).cuda()
+    y = api.mlp_forward(xt).cpu().numpy()
+    y_ref, _ = mlp_ref.forward(params, x)
+    assert np.allclose(y, y_ref, rtol=1e-4, atol=1e-4)
+    g, loss = api.mlp_gradient(xt, tt)
+    g_ref, loss_ref = mlp_ref.gradient(params, x, t)
+    assert abs(loss - loss_ref) <= 1e-4 * abs(loss_ref) + 1e-4
+    # tolerance: fp32 accumulation over a batch of 300 against float64
+    err = np.abs(g - g_ref)
+    assert err.max() <= 1e-3 * np.abs(g_ref).max() + 1e-5, (err.max(), np.abs(g_ref).max())
+    rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert rel < 1e-4, rel
+
+
+def test_training_reduces_loss():
+    ps = cost_model.training_pairs(n=60_000, seed=77)
+    feat, targ, dist, lb = cost_model.labels_and_features(ps)
+    rec = cost_model.train(feat, targ, epochs=2, batch=2048, lr=3e-3, seed=5)
+    first, last = np.mean(rec["losses"][:5]), np.mean(rec["losses"][-5:])
+    assert last < 0.2 * first, (first, last)
+    ev = cost_model.evaluate(feat, dist, lb)
+    assert ev["mae_distance"] < ev["mae_distance_lower_bound_only"]
+
+
+@pytest.mark.parametrize("model", ["zero", "trained"])
+def test_learned_routing_is_bit_exact(model):
+    torch = pytest.importorskip("torch")
+    if model == "zero":
+        api.cost_model_set(np.zeros(api.cost_model_nparams(), np.float32))   # predicts d = 0: many escalations
+    else:
+        assert cost_model.load_default(), "the committed model is missing"
+    ps = workloads.wfa_mixed(n=40_000, seed=72)
+    b = _batch(ps)
+    for smax, trace in ((64, True), (20, True), (64, False)):
+        out = []
+        for learned in (False, True):
+            sc = torch.full((b.n,), -7, dtype=torch.int32, device="cuda")
+            ln = torch.zeros(b.n, dtype=torch.int32, device="cuda")
+            cg = torch.zeros(b.out_bytes, dtype=torch.uint8, device="cuda")
+            api.wfa_device(b, smax, trace, sc, ln, cg, learned=learned)
+            torch.cuda.synchronize()
+            out.append((sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy()))
+        (s0, l0, c0), (s1, l1, c1) = out
+        assert np.array_equal(s0, s1), (model, smax, trace)
+        if trace:
+            assert np.array_equal(l0, l1) and np.array_equal(c0, c1), (model, smax, trace)
+        small, big, esc = api.wfa_route_stats()
+        assert small + big <= b.n
+        if model == "zero" and smax == 64:
+            assert esc[0] > 0                     # the poor model escalates, results unchanged
+
+
+def test_learned_host_entry_matches_oracle():
+    assert cost_model.load_default()
+    ps = workloads.wfa_mixed(n=5000, seed=73)
+    pats, txts = ps.lists()
+    want = oracle.wfa_batch(pats, txts, smax=64, with_cigar=True)
+    got = api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=64,
+                                 with_cigar=True, learned=True)
+    assert got.status == api.Status.ok
+    assert np.array_equal(got.res["score"], want.score)
+    assert all(got.cigar(i) == want.cigars[i] for i in range(ps.n))
+    assert np.array_equal(got.res["rescore_ok"].astype(bool), want.rescore_ok)
+
+
+def test_trained_model_beats_lower_bound_rule():
+    """What the trained network gains over routing without it: its distance
+    estimate is closer and far fewer pairs escalate past their first smax."""
+    assert cost_model.load_default()
+    hold = workloads.wfa_mixed(n=100_000, seed=4041)
+    feat, targ, dist, lb = cost_model.labels_and_features(hold)
+    ev = cost_model.evaluate(feat, dist, lb)
+    assert ev["mae_distance"] < 0.5 * ev["mae_distance_lower_bound_only"], ev
+    assert ev["escalation_rate"] < ev["escalation_rate_lower_bound_only"], ev
+    assert ev["escalation_rate"] < 0.05, ev
