@@ -74,7 +74,7 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
            "ga_profile_kernel_name", "ga_bench_int_peak", "ga_cost_model_nparams", "ga_cost_model_set",
            "ga_cost_model_get", "ga_wfa_features", "ga_mlp_forward", "ga_mlp_gradient", "ga_mlp_train_step",
-           "ga_wfa_device_ex", "ga_wfa_route_stats"]
+           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_mlp_forward_fast"]
 
 _lib = None
 
@@ -139,6 +139,8 @@ def load(build: bool = True):
     L.ga_wfa_device_ex.argtypes = [ctypes.POINTER(DeviceBatch), i32, i32, ctypes.POINTER(Options), p, p, p, p,
                                    ctypes.POINTER(ctypes.c_char_p)]
     L.ga_wfa_device_ex.restype = i32
+    L.ga_mlp_forward_fast.argtypes = [p, i32, p, p]
+    L.ga_mlp_forward_fast.restype = i32
     L.ga_wfa_route_stats.argtypes = [p, i32]
     L.ga_wfa_route_stats.restype = i32
     _lib = L
@@ -590,6 +592,16 @@ def mlp_forward(feat):
     st = load().ga_mlp_forward(feat.data_ptr(), int(feat.shape[0]), y.data_ptr(), None)
     if st != GA_OK:
         raise RuntimeError(f"ga_mlp_forward failed ({st})")
+    return y
+
+
+def mlp_forward_fast(feat):
+    """The tensor-core routing forward pass."""
+    import torch
+    y = torch.empty((feat.shape[0], 2), dtype=torch.float32, device=feat.device)
+    st = load().ga_mlp_forward_fast(feat.data_ptr(), int(feat.shape[0]), y.data_ptr(), None)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_mlp_forward_fast failed ({st})")
     return y
 
 

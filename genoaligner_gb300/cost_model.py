@@ -106,7 +106,7 @@ def load_default() -> bool:
 def evaluate(feat, dist, lb) -> dict:
     """Prediction quality of the loaded model against the lower-bound-only rule."""
     import torch
-    y = api.mlp_forward(feat)
+    y = api.mlp_forward_fast(feat)              # the pass routing uses
     pred = torch.clamp(torch.exp2(torch.clamp(y[:, 0], min=0)) - 1, min=0)
     d = dist.to(torch.float32)
     first = torch.maximum(torch.ceil(pred * 1.25 + 2), lb.to(torch.float32))

@@ -324,6 +324,8 @@ struct WfaScratch {
     int64_t stack_slot = 0;
     int warp_smem = 0;
     int rounds = 0;
+    int64_t seq_bytes = 0;
+    int chunk = 1;
 };
 
 static int bit_length(int x) { int b = 0; while (x > 0) { ++b; x >>= 1; } return b; }
@@ -344,10 +346,13 @@ static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, i
         const int64_t budget = (int64_t)16 << 30;     // stack memory cap
         S.slots = (int)std::min<int64_t>(S.slots, std::max<int64_t>(4, budget / (S.stack_slot * 4) / 4 * 4));
     }
+    // pairs per counter increment: keep >= 8 grabs per warp
+    S.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, (int64_t)n / ((int64_t)S.slots * 8)));
 }
 
 static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace, bool learned)
 {
+    S.seq_bytes = arena;
     S.packed = k.take<uint64_t>(arena / 32 + 2);
     S.pure = k.take<uint8_t>(2 * (size_t)n);
     S.ctr = k.take<int32_t>(64, 256);
@@ -375,8 +380,9 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
     A.out_score = score; A.out_len = len; A.out_cigar = cig;
     A.stack = S.stack; A.stack_slot = S.stack_slot; A.counter = S.ctr; A.err = err;
+    A.chunk = S.chunk;
     cudaError_t e = cudaMemsetAsync(S.ctr, 0, 64 * sizeof(int32_t), st);
-    if (e == cudaSuccess) e = launch_pack(D, S.packed, S.pure, st);
+    if (e == cudaSuccess) e = launch_pack(D, S.seq_bytes, S.packed, S.pure, st);
     if (e != cudaSuccess) return e;
     if (!learned) return launch_wfa(A, S.slots, st);
     const int NB = route_buckets();
@@ -437,6 +443,8 @@ struct RouteRecord {
     const int32_t* counts = nullptr;
     const int32_t* ctr = nullptr;
     int rounds = 0;
+    int64_t seq_bytes = 0;
+    int chunk = 1;
 };
 static thread_local RouteRecord t_route;
 
@@ -846,7 +854,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     PairDesc D;
     D.seq = dseq; D.packed = nullptr; D.pure = dpure;
     D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
-    if (fail_here(3) || launch_pack(D, nullptr, dpure, c->stream) != cudaSuccess ||
+    if (fail_here(3) || launch_pack(D, arena, nullptr, dpure, c->stream) != cudaSuccess ||
         cudaMemcpyAsync(hpure, dpure, 2 * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -1256,7 +1264,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     D.out_off = b->out_off; D.n = n;
     uint8_t* hpure = reinterpret_cast<uint8_t*>(c->host);
     int32_t* hlen = reinterpret_cast<int32_t*>(c->host + ((2 * (size_t)n + 255) & ~(size_t)255));
-    if (launch_pack(D, nullptr, const_cast<uint8_t*>(D.pure), st) != cudaSuccess ||
+    if (launch_pack(D, b->seq_bytes, nullptr, const_cast<uint8_t*>(D.pure), st) != cudaSuccess ||
         cudaMemcpyAsync(hpure, D.pure, 2 * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(hlen, b->a_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(hlen + n, b->b_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||

@@ -16,6 +16,7 @@ struct WfaArgs {
     int64_t stack_slot;
     int32_t* counter;        // next pair index
     int32_t* err;
+    int32_t chunk = 1;       // pairs taken per counter increment
 };
 
 struct SwArgs {
@@ -68,7 +69,7 @@ struct RoutedArgs {
     int32_t warp_smem;           // shared-memory ints per warp
 };
 
-cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st);
+cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
 bool cost_model_loaded();

@@ -32,6 +32,8 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH1 * NF, OFF_W2 = OFF_B1 + NH1, OFF
               OFF_W3 = OFF_B2 + NH2, OFF_B3 = OFF_W3 + NO * NH2, NPARAM = OFF_B3 + NO;
 constexpr int TILE = 64;
 
+void prepare_mlp();
+
 // ------------------------------------------------------------------ sketch --
 // One warp per pair: 3-mer histograms of both sides in shared memory.
 __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restrict__ feat,
@@ -52,6 +54,48 @@ __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restri
                 const uint32_t c0 = __ldg(s + q), c1 = __ldg(s + q + 1), c2 = __ldg(s + q + 2);
                 const int k = (int)((((c0 >> 1) ^ (c0 >> 2)) & 3u) * 16 + (((c1 >> 1) ^ (c1 >> 2)) & 3u) * 4 +
                                     (((c2 >> 1) ^ (c2 >> 2)) & 3u));
+                atomicAdd(&hist[wib][k], sign);
+            }
+        }
+        __syncwarp();
+        const int d0 = hist[wib][lane], d1 = hist[wib][lane + 32];
+        feat[(int64_t)p * NF + lane] = d0 * 0.125f;
+        feat[(int64_t)p * NF + lane + 32] = d1 * 0.125f;
+        int l1 = abs(d0) + abs(d1);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL, l1, o);
+        if (lane == 0) {
+            const int m = D.a_len[p], n = D.b_len[p];
+            feat[(int64_t)p * NF + 64] = m * (1.0f / 256.0f);
+            feat[(int64_t)p * NF + 65] = n * (1.0f / 256.0f);
+            if (lower_bound) lower_bound[p] = max(abs(m - n), (l1 + 5) / 6);
+        }
+        __syncwarp();
+    }
+}
+
+// The same sketch from the 2-bit arena (D.packed): each 3-mer is six bits of
+// the packed stream, two 8-byte loads instead of three byte loads.
+__global__ void __launch_bounds__(256) sketch_packed_kernel(PairDesc D, float* __restrict__ feat,
+                                                            int32_t* __restrict__ lower_bound)
+{
+    __shared__ int hist[8][64];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nwarps) {
+        hist[wib][lane] = 0;
+        hist[wib][lane + 32] = 0;
+        __syncwarp();
+        for (int side = 0; side < 2; ++side) {
+            const uint64_t* P = D.packed + ((side ? D.b_off[p] : D.a_off[p]) >> 5);
+            const int L = side ? D.b_len[p] : D.a_len[p];
+            const int sign = side ? -1 : 1;
+            for (int q = lane; q + 2 < L; q += 32) {
+                const uint64_t lo = __ldg(P + (q >> 5)), hi = __ldg(P + (q >> 5) + 1);
+                const unsigned sh = 2u * (unsigned)(q & 31);
+                const uint64_t v = sh ? ((lo >> sh) | (hi << (64u - sh))) : lo;
+                // k = 16*c[q] + 4*c[q+1] + c[q+2]: codes sit low-first in the stream
+                const int k = (int)(((v & 3u) << 4) | (v & 0xcu) | ((v >> 4) & 3u));
                 atomicAdd(&hist[wib][k], sign);
             }
         }
@@ -272,6 +316,134 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, __nv_bfloat16* __r
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = __float2bfloat16(src[i]);
 }
 
+// ------------------------------------------------- tensor-core inference --
+// The routing forward pass on the tensor cores: mma.sync m16n8k16 bf16 with
+// fp32 accumulation, one warp per 16 pairs; the inputs and each hidden layer
+// are rounded to bf16 as they enter a multiply.  Layer outputs go from the
+// accumulator registers straight into the next layer's A fragments (the m16n8
+// accumulator layout of two adjacent n-tiles is the A layout of one k16 step).
+// Weights are staged once per block in shared memory, rows padded (88 and 136
+// bf16) so the eight row groups of a fragment load hit eight bank groups.
+constexpr int TK1 = 80, TS1 = 88, TS2 = 136;
+
+struct TcSmem {
+    __nv_bfloat16 W1[NH1 * TS1];
+    __nv_bfloat16 W2[NH2 * TS2];
+    __nv_bfloat16 W3[8 * TS2];
+    float b1[NH1], b2[NH2], b3[8];
+};
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16* __restrict__ w,
+                                                             const float* __restrict__ feat, int n,
+                                                             float* __restrict__ y)
+{
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw);
+    for (int idx = threadIdx.x; idx < NH1 * TS1; idx += blockDim.x) {
+        const int o = idx / TS1, i = idx - o * TS1;
+        S.W1[idx] = i < NF ? w[OFF_W1 + o * NF + i] : __float2bfloat16(0.f);
+    }
+    for (int idx = threadIdx.x; idx < NH2 * TS2; idx += blockDim.x) {
+        const int o = idx / TS2, i = idx - o * TS2;
+        S.W2[idx] = i < NH1 ? w[OFF_W2 + o * NH1 + i] : __float2bfloat16(0.f);
+    }
+    for (int idx = threadIdx.x; idx < 8 * TS2; idx += blockDim.x) {
+        const int o = idx / TS2, i = idx - o * TS2;
+        S.W3[idx] = (o < NO && i < NH2) ? w[OFF_W3 + o * NH2 + i] : __float2bfloat16(0.f);
+    }
+    for (int i = threadIdx.x; i < NH1; i += blockDim.x) S.b1[i] = __bfloat162float(w[OFF_B1 + i]);
+    for (int i = threadIdx.x; i < NH2; i += blockDim.x) S.b2[i] = __bfloat162float(w[OFF_B2 + i]);
+    if (threadIdx.x < 8) S.b3[threadIdx.x] = threadIdx.x < NO ? __bfloat162float(w[OFF_B3 + threadIdx.x]) : 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile * 16 < n; tile += warps) {
+        const int r0 = tile * 16 + g, r1 = r0 + 8;
+        auto X = [&](int r, int c) -> float { return (r < n && c < NF) ? __ldg(feat + (int64_t)r * NF + c) : 0.f; };
+        uint32_t a[TK1 / 16][4];
+#pragma unroll
+        for (int kt = 0; kt < TK1 / 16; ++kt) {
+            const int c0 = 16 * kt + 2 * tg, c1 = c0 + 8;
+            a[kt][0] = pack_bf16(X(r0, c0), X(r0, c0 + 1));
+            a[kt][1] = pack_bf16(X(r1, c0), X(r1, c0 + 1));
+            a[kt][2] = pack_bf16(X(r0, c1), X(r0, c1 + 1));
+            a[kt][3] = pack_bf16(X(r1, c1), X(r1, c1 + 1));
+        }
+        float c[16][4];
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const float b0 = S.b1[8 * nt + 2 * tg], bb1 = S.b1[8 * nt + 2 * tg + 1];
+            c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
+            const __nv_bfloat16* wr = S.W1 + (8 * nt + g) * TS1 + 2 * tg;
+#pragma unroll
+            for (int kt = 0; kt < TK1 / 16; ++kt)
+                mma_bf16(c[nt], a[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                         *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+        }
+        uint32_t h[8][4];
+#pragma unroll
+        for (int kt = 0; kt < 8; ++kt) {
+            h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+            h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+            h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+            h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+        }
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const float b0 = S.b2[8 * nt + 2 * tg], bb1 = S.b2[8 * nt + 2 * tg + 1];
+            c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
+            const __nv_bfloat16* wr = S.W2 + (8 * nt + g) * TS2 + 2 * tg;
+#pragma unroll
+            for (int kt = 0; kt < 8; ++kt)
+                mma_bf16(c[nt], h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                         *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+        }
+#pragma unroll
+        for (int kt = 0; kt < 8; ++kt) {
+            h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+            h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+            h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+            h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+        }
+        float o[4] = {S.b3[2 * tg], S.b3[2 * tg + 1], S.b3[2 * tg], S.b3[2 * tg + 1]};
+        const __nv_bfloat16* wr = S.W3 + g * TS2 + 2 * tg;
+#pragma unroll
+        for (int kt = 0; kt < 8; ++kt)
+            mma_bf16(o, h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                     *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+        if (tg == 0) {
+            if (r0 < n) { y[2 * (int64_t)r0] = o[0]; y[2 * (int64_t)r0 + 1] = o[1]; }
+            if (r1 < n) { y[2 * (int64_t)r1] = o[2]; y[2 * (int64_t)r1 + 1] = o[3]; }
+        }
+    }
+}
+
+static cudaError_t run_forward_tc(const __nv_bfloat16* w, const float* feat, int n, float* y, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    prepare_mlp();
+    int blocks = (n + 127) / 128;
+    if (blocks > 152 * 2) blocks = 152 * 2;
+    launch_begin(K_MLP, st);
+    mlp_forward_tc_kernel<<<blocks, 256, sizeof(TcSmem), st>>>(w, feat, n, y);
+    launch_end(K_MLP, st);
+    return cudaGetLastError();
+}
+
 // --------------------------------------------------------- model state --
 // One model per device: fp32 master, bf16 working copy, Adam moments, grads.
 struct Model {
@@ -313,6 +485,7 @@ void prepare_mlp()
     std::call_once(once, [] {
         cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
         cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
+        cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
     });
 }
 
@@ -348,7 +521,8 @@ cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStrea
     int blocks = (D.n + 7) / 8;
     if (blocks > 152 * 16) blocks = 152 * 16;
     launch_begin(K_SKETCH, st);
-    sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
+    if (D.packed) sketch_packed_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
+    else sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
     launch_end(K_SKETCH, st);
     return cudaGetLastError();
 }
@@ -363,11 +537,12 @@ const __nv_bfloat16* cost_model_weights()
 
 bool cost_model_loaded() { return cost_model_weights() != nullptr; }
 
+// Routing inference: the tensor-core forward pass.
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st)
 {
     const __nv_bfloat16* w = cost_model_weights();
     if (!w) return cudaErrorNotReady;
-    return run_forward(w, feat, n, y, st);
+    return run_forward_tc(w, feat, n, y, st);
 }
 
 }  // namespace ga
@@ -423,6 +598,19 @@ int32_t ga_wfa_features(const ga_device_batch* b, float* feat, int32_t* lower_bo
 }
 
 int32_t ga_mlp_forward(const float* feat, int32_t n, float* y, void* stream)
+{
+    if (!feat || !y || n < 0) return GA_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const __nv_bfloat16* w = cost_model_weights();
+    if (!w) return GA_INVALID_ARGUMENT;
+    const cudaError_t e = run_forward(w, feat, n, y, st);
+    if (e == cudaErrorNotReady) return GA_INVALID_ARGUMENT;
+    if (e != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    if (!stream && cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    return GA_OK;
+}
+
+int32_t ga_mlp_forward_fast(const float* feat, int32_t n, float* y, void* stream)
 {
     if (!feat || !y || n < 0) return GA_INVALID_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;

@@ -114,7 +114,7 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
     A.out_score = out_score; A.out_len = out_len; A.out_cigar = out_cigar;
     A.stack = stk; A.stack_slot = (int64_t)(smax + 1) * (smax + 1);
     A.counter = ctr; A.err = ctr + 1;
-    if (launch_pack(D, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
+    if (launch_pack(D, b->seq_bytes, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = "kernel launch failed";
         return GA_DEVICE_ERROR;

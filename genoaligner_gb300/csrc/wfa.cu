@@ -26,42 +26,54 @@
 namespace ga {
 
 // ---------------------------------------------------------------- packing --
-// One warp per sequence: 32 ASCII bytes -> one 64-bit word of 2-bit codes
-// (A=0 C=1 G=2 T=3, little-endian), plus a purity flag per sequence.  The
-// sequence set is the a-sides (q < n) followed by the b-sides (q >= n).
-__global__ void __launch_bounds__(256) pack2_kernel(PairDesc D, uint64_t* __restrict__ packed,
-                                                    uint8_t* __restrict__ pure)
+// The 2-bit arena: one thread per 32-byte chunk of the byte arena -> one
+// 64-bit word (A=0 C=1 G=2 T=3 under ((c>>1)^(c>>2))&3, little-endian).
+// Sequences start on 32-byte boundaries, so word index = byte offset / 32 and
+// no per-sequence bookkeeping is needed.
+__global__ void __launch_bounds__(256) pack_chunks_kernel(const uint8_t* __restrict__ seq, int64_t nchunks,
+                                                          uint64_t* __restrict__ packed)
 {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < 2 * D.n; q += nwarps) {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint4* src = reinterpret_cast<const uint4*>(seq + 32 * c);
+        const uint4 x0 = __ldg(src), x1 = __ldg(src + 1);
+        const uint32_t parts[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        uint64_t word = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t v = parts[q];
+            // four codes of one 32-bit part: ((c >> 1) ^ (c >> 2)) & 3 per byte
+            const uint32_t codes = ((v >> 1) ^ (v >> 2)) & 0x03030303u;
+            const uint32_t packed4 = (codes & 3u) | ((codes >> 6) & 0xcu) | ((codes >> 12) & 0x30u) | ((codes >> 18) & 0xc0u);
+            word |= (uint64_t)packed4 << (8 * q);
+        }
+        packed[c] = word;
+    }
+}
+
+// 1 when byte c is one of A, C, G, T.
+__device__ __forceinline__ uint32_t acgt_byte(uint32_t c)
+{
+    // 'A'=0x41 'C'=0x43 'G'=0x47 'T'=0x54: all in 0x40..0x5f; low 5 bits 1, 3, 7, 20
+    return ((c >> 5) == 2u) & ((0x0010008au >> (c & 31u)) & 1u);
+}
+
+// Purity flag per sequence (a-sides q < n, then b-sides), one thread each.
+__global__ void __launch_bounds__(256) purity_kernel(PairDesc D, uint8_t* __restrict__ pure)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * D.n; q += gridDim.x * blockDim.x) {
         const bool is_a = q < D.n;
         const int p = is_a ? q : q - D.n;
-        const int64_t off = is_a ? D.a_off[p] : D.b_off[p];
+        const uint8_t* s = D.seq + (is_a ? D.a_off[p] : D.b_off[p]);
         const int len = is_a ? D.a_len[p] : D.b_len[p];
-        const int words = (len + 31) >> 5;
-        bool bad = false;
-        for (int w = lane; w < words; w += 32) {
-            const uint4* src = reinterpret_cast<const uint4*>(D.seq + off + 32 * (int64_t)w);
-            const uint4 x0 = __ldg(src), x1 = __ldg(src + 1);
-            const uint32_t parts[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-            const int valid = min(32, len - 32 * w);
-            uint64_t word = 0;
+        uint32_t ok = 1;
+        for (int o = 0; o < len && ok; o += 16) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(s + o));
+            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-            for (int b = 0; b < 32; ++b) {
-                const uint32_t c = (parts[b >> 2] >> (8 * (b & 3))) & 0xffu;
-                // A=0x41 C=0x43 G=0x47 T=0x54 map to 0,1,2,3 under ((c>>1)^(c>>2))&3
-                const uint64_t code = ((c >> 1) ^ (c >> 2)) & 3u;
-                const bool acgt = (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
-                if (b < valid) {
-                    bad |= !acgt;
-                    word |= code << (2 * b);
-                }
-            }
-            if (packed) packed[(off >> 5) + w] = word;
+            for (int b = 0; b < 16; ++b)
+                if (o + b < len) ok &= acgt_byte((w[b >> 2] >> (8 * (b & 3))) & 0xffu);
         }
-        bad = __any_sync(FULL, bad);
-        if (lane == 0) pure[q] = bad ? 0 : 1;
+        pure[q] = (uint8_t)ok;
     }
 }
 
@@ -190,10 +202,12 @@ __global__ void __launch_bounds__(128) wfa_kernel(WfaArgs A)
     const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     int32_t* stk = TRACE ? A.stack + slot * A.stack_slot : nullptr;
     for (;;) {
-        int p = 0;
-        if (lane == 0) p = atomicAdd(A.counter, 1);
-        p = __shfl_sync(FULL, p, 0);
-        if (p >= A.D.n) break;
+        int p0 = 0;
+        if (lane == 0) p0 = atomicAdd(A.counter, A.chunk);
+        p0 = __shfl_sync(FULL, p0, 0);
+        if (p0 >= A.D.n) break;
+        const int pend = min(p0 + A.chunk, A.D.n);
+        for (int p = p0; p < pend; ++p) {
         __syncwarp();
         const int m = A.D.a_len[p];       // pattern
         const int n = A.D.b_len[p];       // text
@@ -219,18 +233,28 @@ __global__ void __launch_bounds__(128) wfa_kernel(WfaArgs A)
             const uint64_t* T = reinterpret_cast<const uint64_t*>(A.D.seq + A.D.b_off[p]);
             wfa_pair<TRACE, 8>(A, p, P, T, m, n, wf0, wf1, stk, lane);
         }
+        }
     }
 }
 
 // --------------------------------------------------------------- launchers --
-cudaError_t launch_pack(const PairDesc& D, uint64_t* packed, uint8_t* pure, cudaStream_t st)
+cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st)
 {
     if (D.n <= 0) return cudaSuccess;
-    const int warps = 2 * D.n;
-    int blocks = (warps + 7) / 8;
-    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (packed) {
+        // every sequence ends >= 64 bytes before the arena's end, so the whole
+        // chunks cover them all and no read passes seq_bytes
+        const int64_t nchunks = seq_bytes / 32;
+        int64_t blocks = (nchunks + 255) / 256;
+        if (blocks > 152 * 32) blocks = 152 * 32;
+        launch_begin(K_PACK, st);
+        pack_chunks_kernel<<<(int)blocks, 256, 0, st>>>(D.seq, nchunks, packed);
+        launch_end(K_PACK, st);
+    }
+    int blocks = (2 * D.n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
     launch_begin(K_PACK, st);
-    pack2_kernel<<<blocks, 256, 0, st>>>(D, packed, pure);
+    purity_kernel<<<blocks, 256, 0, st>>>(D, pure);
     launch_end(K_PACK, st);
     return cudaGetLastError();
 }

@@ -275,17 +275,32 @@ __global__ void route_scan_kernel(int32_t* counts, int32_t* starts)
     }
 }
 
+// Warp-aggregated: lanes with the same (queue, bucket) take one atomic.
 __global__ void route_scatter_kernel(PairDesc D, const float* __restrict__ y, const int32_t* __restrict__ lb, int smax,
                                      int32_t* __restrict__ starts, int2* __restrict__ big, int2* __restrict__ small)
 {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
-        const int m = D.a_len[p], n = D.b_len[p];
-        if (m > 0 && n > 0 && lb[p] > smax) continue;
-        const int s = (m > 0 && n > 0) ? first_smax(y[2 * p], lb[p], smax) : smax;
-        const int isb = (s <= SMALL_SMAX && m > 0 && n > 0) ? 1 : 0;
-        const int b = min(bitlen((unsigned)s), ROUTE_BUCKETS - 1);
-        const int at = atomicAdd(&starts[isb * ROUTE_BUCKETS + b], 1);
-        (isb ? small : big)[at] = make_int2(p, s);
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); p0 < D.n; p0 += stride) {
+        const int p = p0 + lane;
+        int key = -1, s = 0;
+        if (p < D.n) {
+            const int m = D.a_len[p], n = D.b_len[p];
+            if (!(m > 0 && n > 0 && lb[p] > smax)) {
+                s = (m > 0 && n > 0) ? first_smax(y[2 * p], lb[p], smax) : smax;
+                const int isb = (s <= SMALL_SMAX && m > 0 && n > 0) ? 1 : 0;
+                key = isb * ROUTE_BUCKETS + min(bitlen((unsigned)s), ROUTE_BUCKETS - 1);
+            }
+        }
+        const unsigned same = __match_any_sync(FULL, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (lane == leader && key >= 0) base = atomicAdd(&starts[key], __popc(same));
+        base = __shfl_sync(FULL, base, leader);
+        if (key >= 0) {
+            const int at = base + __popc(same & ((1u << lane) - 1u));
+            (key >= ROUTE_BUCKETS ? small : big)[at] = make_int2(p, s);
+        }
     }
 }
 

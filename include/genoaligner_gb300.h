@@ -220,8 +220,12 @@ int32_t ga_cost_model_get(float* params, int32_t n);
 /* Features [n][66] and the exact q-gram lower bound of the edit distance of
  * every pair of a device batch (a = pattern, b = text).  Device pointers. */
 int32_t ga_wfa_features(const ga_device_batch* batch, float* features, int32_t* lower_bound, void* stream);
-/* Inference: y[n][2] from features[n][66] (device pointers). */
+/* Inference: y[n][2] from features[n][66] (device pointers), fp32 activations
+ * (the training forward pass). */
 int32_t ga_mlp_forward(const float* features, int32_t n, float* y, void* stream);
+/* The routing forward pass on the tensor cores (mma.sync bf16, fp32
+ * accumulate; inputs and activations rounded to bf16 at each multiply). */
+int32_t ga_mlp_forward_fast(const float* features, int32_t n, float* y, void* stream);
 /* Gradient of the mean squared error over a batch (device features and
  * targets [n][2]) with respect to every parameter, copied to grad_host
  * (ga_cost_model_nparams() floats); loss_host gets the summed squared error. */

@@ -51,3 +51,13 @@ def gradient(params, x, t):
     gb1 = dh1.sum(0)
     g = np.concatenate([a.ravel() for a in (gW1, gb1, gW2, gb2, gW3, gb3)])
     return g, float((e * e).sum())
+
+
+def forward_bf16_activations(params, x):
+    """The tensor-core routing pass: inputs and hidden activations rounded to
+    bf16 where they enter a multiply, fp32-or-better accumulation."""
+    W1, b1, W2, b2, W3, b3 = unpack(bf16_round(params))
+    r = lambda a: bf16_round(np.asarray(a, np.float32))
+    h1 = r(np.maximum(r(x) @ W1.T + b1, 0))
+    h2 = r(np.maximum(h1 @ W2.T + b2, 0))
+    return h2 @ W3.T + b3

@@ -50,6 +50,20 @@ def test_mlp_forward_and_gradient_match_float64_reference():
     assert rel < 1e-4, rel
 
 
+def test_tensor_core_forward_matches_bf16_reference():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(6)
+    params = api.cost_model_init(seed=4)
+    api.cost_model_set(params)
+    x = (rng.integers(-40, 41, size=(1000, 66)) / 8.0).astype(np.float32)    # count differences / 8
+    x[:, 64:] = rng.uniform(0.5, 1.0, size=(1000, 2))
+    y = api.mlp_forward_fast(torch.from_numpy(x).cuda()).cpu().numpy()
+    y_ref = mlp_ref.forward_bf16_activations(params, x)
+    # tolerance: fp32 accumulation order against float64, on bf16-rounded operands
+    scale = np.abs(y_ref).max()
+    assert np.abs(y - y_ref).max() <= 2e-3 * scale + 1e-3, (np.abs(y - y_ref).max(), scale)
+
+
 def test_training_reduces_loss():
     ps = cost_model.training_pairs(n=60_000, seed=77)
     feat, targ, dist, lb = cost_model.labels_and_features(ps)
