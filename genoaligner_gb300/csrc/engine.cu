@@ -306,38 +306,37 @@ int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, con
 
 // Device scratch of one WFA batch: the 2-bit arena and purity flags, the
 // per-warp wavefront stacks, the work counter; for the learned path also the
-// features, lower bounds, predictions, bucket counts and the queues.
+// queue items, lower bounds, predictions, bucket counts and the queues.
 struct WfaScratch {
     uint64_t* packed = nullptr;
     uint8_t* pure = nullptr;
     int32_t* stack = nullptr;
     int32_t* ctr = nullptr;          // 64 ints: plain counter; learned: round counters
-    float* feat = nullptr;
+    int32_t* item = nullptr;         // queue item per pair (bucket | first smax << 8, or -1)
     int32_t* lb = nullptr;
     float* y = nullptr;
     int32_t* counts = nullptr;       // 2*buckets + 2
     int32_t* starts = nullptr;       // 2*buckets
     int2* big = nullptr;
     int2* small = nullptr;
-    int2* esc[2] = {nullptr, nullptr};
-    int slots = 0;
+    int2* esc = nullptr;
+    uint16_t* lane_rec = nullptr;
+    int slots = 0;                   // warp slots of the WFA (or warp-queue) kernel
+    int lane_slots = 0;              // learned: warp slots of the lane kernel
     int64_t stack_slot = 0;
     int warp_smem = 0;
-    int rounds = 0;
     int64_t seq_bytes = 0;
     int chunk = 1;
 };
-
-static int bit_length(int x) { int b = 0; while (x > 0) { ++b; x >>= 1; } return b; }
 
 static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, int sm_count)
 {
     if (learned) {
         prepare_mlp();
         S.slots = (int)std::min<int64_t>(routed_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
+        S.lane_slots = (int)std::min<int64_t>(lane_max_slots(trace, sm_count), ((int64_t)n + 127) / 128 * 4);
         S.stack_slot = routed_stack_slot(smax);
         S.warp_smem = routed_warp_smem(smax);
-        S.rounds = bit_length(smax) + 1;
     } else {
         S.slots = (int)std::min<int64_t>(wfa_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
         S.stack_slot = (int64_t)(smax + 1) * (smax + 1);
@@ -353,20 +352,20 @@ static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, i
 static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace, bool learned)
 {
     S.seq_bytes = arena;
-    S.packed = k.take<uint64_t>(arena / 32 + 2);
+    S.packed = k.take<uint64_t>(packed_arena_words(arena));
     S.pure = k.take<uint8_t>(2 * (size_t)n);
     S.ctr = k.take<int32_t>(64, 256);
     S.stack = trace ? k.take<int32_t>((size_t)S.slots * S.stack_slot) : nullptr;
     if (learned) {
-        S.feat = k.take<float>((size_t)n * 66);
+        S.item = k.take<int32_t>(n);
         S.lb = k.take<int32_t>(n);
         S.y = k.take<float>(2 * (size_t)n);
         S.counts = k.take<int32_t>(2 * route_buckets() + 2);
         S.starts = k.take<int32_t>(2 * route_buckets());
         S.big = k.take<int2>(n);
         S.small = k.take<int2>(n);
-        S.esc[0] = k.take<int2>(n);
-        S.esc[1] = k.take<int2>(n);
+        S.esc = k.take<int2>(n);
+        S.lane_rec = trace ? k.take<uint16_t>((size_t)S.lane_slots * lane_rec_slot()) : nullptr;
     }
 }
 
@@ -387,26 +386,24 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     if (!learned) return launch_wfa(A, S.slots, st);
     const int NB = route_buckets();
     if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 2), st)) != cudaSuccess) return e;
-    if ((e = launch_sketch(D, S.feat, S.lb, st)) != cudaSuccess) return e;
-    if ((e = launch_mlp_forward(S.feat, D.n, S.y, st)) != cudaSuccess) return e;
-    if ((e = launch_route(D, S.y, S.lb, smax, score, len, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess)
-        return e;
-    // ctr layout: [0..31] next counters (2 per round), [32..63] escalation counts
-    for (int r = 0; r < S.rounds; ++r) {
-        RoutedArgs R;
-        R.A = A;
-        R.warp_smem = S.warp_smem;
-        R.big = r == 0 ? S.big : S.esc[(r - 1) & 1];
-        R.big_count = r == 0 ? S.counts + 2 * NB : S.ctr + 32 + (r - 1);
-        R.big_next = S.ctr + 2 * r;
-        R.small = r == 0 ? S.small : nullptr;
-        R.small_count = r == 0 ? S.counts + 2 * NB + 1 : nullptr;
-        R.small_next = S.ctr + 2 * r + 1;
-        R.esc = S.esc[r & 1];
-        R.esc_count = S.ctr + 32 + r;
-        if ((e = launch_routed(R, S.slots, st)) != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    if ((e = launch_route_model(D, smax, S.item, S.lb, S.y, S.counts, score, len, st)) != cudaSuccess) return e;
+    if ((e = launch_route(D.n, S.item, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess) return e;
+    // ctr layout: [0] warp-queue next, [1] lane-queue next, [2] escalation
+    // next, [32] escalation count
+    RoutedArgs R;
+    R.A = A;
+    R.warp_smem = S.warp_smem;
+    R.big = S.big;
+    R.big_count = S.counts + 2 * NB;
+    R.big_next = S.ctr;
+    R.small = S.small;
+    R.small_count = S.counts + 2 * NB + 1;
+    R.small_next = S.ctr + 1;
+    R.esc = S.esc;
+    R.esc_count = S.ctr + 32;
+    R.esc_next = S.ctr + 2;
+    R.lane_rec = S.lane_rec;
+    return launch_routed(R, S.lane_slots, S.slots, st);
 }
 
 // Learned path as one CUDA graph, cached per context by everything the
@@ -430,7 +427,7 @@ static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D,
         if (e != cudaSuccess) { c->gexec = nullptr; return e; }
         std::memcpy(c->gkey, key, sizeof(key));
     }
-    note_graph_launches(S.rounds + 6);
+    note_graph_launches(7);          // pack, purity, route model, scan, scatter, lane, warp
     return cudaGraphLaunch(c->gexec, st);
 }
 
@@ -442,7 +439,6 @@ struct RouteRecord {
     uint64_t gen = 0;
     const int32_t* counts = nullptr;
     const int32_t* ctr = nullptr;
-    int rounds = 0;
     int64_t seq_bytes = 0;
     int chunk = 1;
 };
@@ -454,7 +450,6 @@ static void note_route(Ctx* c, const WfaScratch& S)
     t_route.gen = c->dev_gen;
     t_route.counts = S.counts;
     t_route.ctr = S.ctr;
-    t_route.rounds = S.rounds;
 }
 
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
@@ -1219,10 +1214,10 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
         cudaGetLastError();
         return GA_DEVICE_ERROR;
     }
-    out[0] = counts[2 * NB + 1];              // small queue (8-lane groups)
-    out[1] = counts[2 * NB];                  // big queue (whole warps)
+    out[0] = counts[2 * NB + 1];              // lane queue (one pair per lane)
+    out[1] = counts[2 * NB];                  // warp queue (one pair per warp)
     int k = 2;
-    for (int q = 0; q < r.rounds && k < max; ++q) out[k++] = esc[q];
+    if (k < max) out[k++] = esc[0];
     for (; k < max; ++k) out[k] = 0;
     return GA_OK;
 }

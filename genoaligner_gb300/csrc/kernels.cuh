@@ -58,29 +58,42 @@ struct Sw16Args {
 // The learned-bucketed WFA path (wfa_routed.cu).
 struct RoutedArgs {
     WfaArgs A;                   // A.smax = the batch smax
-    const int2* big;             // (pair, first smax), served by whole warps
+    const int2* big;             // warp queue: (pair, smax), one pair per warp
     const int32_t* big_count;    // device-side count
     int32_t* big_next;
-    const int2* small;           // served by 8-lane groups (null: none)
+    const int2* small;           // lane queue: (pair, first smax), one pair per lane (null: none)
     const int32_t* small_count;
     int32_t* small_next;
-    int2* esc;                   // escalations: (pair, doubled smax)
+    int2* esc;                   // escalations from the lane queue: (pair, batch smax)
     int32_t* esc_count;
-    int32_t warp_smem;           // shared-memory ints per warp
+    int32_t* esc_next;
+    uint16_t* lane_rec;          // lane kernel: per warp slot, lane_rec_slot() walk records (trace only)
+    int32_t warp_smem;           // warp kernel: shared-memory ints per warp
 };
 
+// Packs seq into the 2-bit arena `packed` (packed_arena_words(seq_bytes)
+// words; null: purity flags only) and sets pure[2n].
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
+int64_t packed_arena_words(int64_t seq_bytes);
 cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
 bool cost_model_loaded();
 void prepare_mlp();
 int route_buckets();
 int64_t routed_stack_slot(int smax);
+int64_t lane_rec_slot();
 int routed_warp_smem(int smax);
 int routed_max_slots(int smax, bool trace, int sm_count);
-cudaError_t launch_route(const PairDesc& D, const float* y, const int32_t* lb, int smax, int32_t* out_score,
-                         int32_t* out_len, int32_t* counts, int32_t* starts, int2* big, int2* small, cudaStream_t st);
-cudaError_t launch_routed(const RoutedArgs& R, int slots, cudaStream_t st);
+int lane_max_slots(bool trace, int sm_count);
+// Fused sketch + lower bound + cost model + queue choice (learned.cu); then
+// the queues from the per-pair items (wfa_routed.cu).
+cudaError_t launch_route_model(const PairDesc& D, int smax, int32_t* item, int32_t* lb, float* y, int32_t* counts,
+                               int32_t* out_score, int32_t* out_len, cudaStream_t st);
+cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* starts, int2* big, int2* small,
+                         cudaStream_t st);
+// The lane kernel over R.small, then the warp kernel over R.big and the
+// lane kernel's escalations.
+cudaError_t launch_routed(const RoutedArgs& R, int lane_slots, int slots, cudaStream_t st);
 
 size_t wfa_smem_bytes(int smax);
 int wfa_max_slots(int smax, bool trace, int sm_count);

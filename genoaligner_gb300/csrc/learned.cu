@@ -23,6 +23,7 @@
 
 #include "../../include/genoaligner_gb300.h"
 #include "kernels.cuh"
+#include "route.cuh"
 #include <cuda_bf16.h>
 
 namespace ga {
@@ -33,6 +34,7 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH1 * NF, OFF_W2 = OFF_B1 + NH1, OFF
 constexpr int TILE = 64;
 
 void prepare_mlp();
+const __nv_bfloat16* cost_model_weights();
 
 // ------------------------------------------------------------------ sketch --
 // One warp per pair: 3-mer histograms of both sides in shared memory.
@@ -74,35 +76,39 @@ __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restri
     }
 }
 
-// The same sketch from the 2-bit arena (D.packed): each 3-mer is six bits of
-// the packed stream, two 8-byte loads instead of three byte loads.
+// The same sketch from the 2-bit arena (D.packed).  Lanes 0-15 take side a,
+// lanes 16-31 side b; a lane counts the 16 3-mers starting in its 16-base
+// stretch from one 64-bit window (3-mer i is bits [2i, 2i+6) of the window).
+// The histogram is indexed by the window's own order, c0 + 4 c1 + 16 c2; the
+// feature order 16 c0 + 4 c1 + c2 is applied when the features are written.
 __global__ void __launch_bounds__(256) sketch_packed_kernel(PairDesc D, float* __restrict__ feat,
                                                             int32_t* __restrict__ lower_bound)
 {
     __shared__ int hist[8][64];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int side = lane >> 4, sl = lane & 15;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nwarps) {
         hist[wib][lane] = 0;
         hist[wib][lane + 32] = 0;
         __syncwarp();
-        for (int side = 0; side < 2; ++side) {
-            const uint64_t* P = D.packed + ((side ? D.b_off[p] : D.a_off[p]) >> 5);
-            const int L = side ? D.b_len[p] : D.a_len[p];
-            const int sign = side ? -1 : 1;
-            for (int q = lane; q + 2 < L; q += 32) {
-                const uint64_t lo = __ldg(P + (q >> 5)), hi = __ldg(P + (q >> 5) + 1);
-                const unsigned sh = 2u * (unsigned)(q & 31);
-                const uint64_t v = sh ? ((lo >> sh) | (hi << (64u - sh))) : lo;
-                // k = 16*c[q] + 4*c[q+1] + c[q+2]: codes sit low-first in the stream
-                const int k = (int)(((v & 3u) << 4) | (v & 0xcu) | ((v >> 4) & 3u));
-                atomicAdd(&hist[wib][k], sign);
-            }
+        const uint64_t* P = D.packed + ((side ? D.b_off[p] : D.a_off[p]) >> 5);
+        const int L = side ? D.b_len[p] : D.a_len[p];
+        const int sign = side ? -1 : 1;
+        for (int q = 16 * sl; q + 2 < L; q += 256) {
+            const uint64_t v = fetch_syms<2>(P, q);
+            const int cnt = min(16, L - 2 - q);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                if (i < cnt) atomicAdd(&hist[wib][(int)((v >> (2 * i)) & 63u)], sign);
         }
         __syncwarp();
-        const int d0 = hist[wib][lane], d1 = hist[wib][lane + 32];
-        feat[(int64_t)p * NF + lane] = d0 * 0.125f;
-        feat[(int64_t)p * NF + lane + 32] = d1 * 0.125f;
+        // feature k = 16 c0 + 4 c1 + c2 lives in bin c0 + 4 c1 + 16 c2
+        const int k0 = lane, k1 = lane + 32;
+        const int d0 = hist[wib][((k0 & 3) << 4) | (k0 & 12) | (k0 >> 4)];
+        const int d1 = hist[wib][((k1 & 3) << 4) | (k1 & 12) | (k1 >> 4)];
+        feat[(int64_t)p * NF + k0] = d0 * 0.125f;
+        feat[(int64_t)p * NF + k1] = d1 * 0.125f;
         int l1 = abs(d0) + abs(d1);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL, l1, o);
@@ -347,12 +353,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-__global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16* __restrict__ w,
-                                                             const float* __restrict__ feat, int n,
-                                                             float* __restrict__ y)
+// Weights and biases of a bf16 model into a block's shared memory.
+__device__ void load_tc_weights(TcSmem& S, const __nv_bfloat16* __restrict__ w)
 {
-    extern __shared__ __align__(16) unsigned char tc_raw[];
-    TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw);
     for (int idx = threadIdx.x; idx < NH1 * TS1; idx += blockDim.x) {
         const int o = idx / TS1, i = idx - o * TS1;
         S.W1[idx] = i < NF ? w[OFF_W1 + o * NF + i] : __float2bfloat16(0.f);
@@ -368,6 +371,65 @@ __global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16
     for (int i = threadIdx.x; i < NH1; i += blockDim.x) S.b1[i] = __bfloat162float(w[OFF_B1 + i]);
     for (int i = threadIdx.x; i < NH2; i += blockDim.x) S.b2[i] = __bfloat162float(w[OFF_B2 + i]);
     if (threadIdx.x < 8) S.b3[threadIdx.x] = threadIdx.x < NO ? __bfloat162float(w[OFF_B3 + threadIdx.x]) : 0.f;
+}
+
+// One 16-pair tile through the network.  a: the input A fragments (rows g
+// and g + 8 of the tile, columns 16 kt + 2 tg (+1, +8, +9)); o: outputs of
+// rows g (o[0], o[1]) and g + 8 (o[2], o[3]), valid in lanes with tg == 0.
+__device__ __forceinline__ void tc_tile_forward(const TcSmem& S, const uint32_t (&a)[TK1 / 16][4], float (&o)[4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
+    float c[16][4];
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+        const float b0 = S.b1[8 * nt + 2 * tg], bb1 = S.b1[8 * nt + 2 * tg + 1];
+        c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
+        const __nv_bfloat16* wr = S.W1 + (8 * nt + g) * TS1 + 2 * tg;
+#pragma unroll
+        for (int kt = 0; kt < TK1 / 16; ++kt)
+            mma_bf16(c[nt], a[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                     *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+    }
+    uint32_t h[8][4];
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt) {
+        h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+        h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+        h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+        h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+    }
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+        const float b0 = S.b2[8 * nt + 2 * tg], bb1 = S.b2[8 * nt + 2 * tg + 1];
+        c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
+        const __nv_bfloat16* wr = S.W2 + (8 * nt + g) * TS2 + 2 * tg;
+#pragma unroll
+        for (int kt = 0; kt < 8; ++kt)
+            mma_bf16(c[nt], h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                     *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+    }
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt) {
+        h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+        h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+        h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+        h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+    }
+    o[0] = S.b3[2 * tg]; o[1] = S.b3[2 * tg + 1]; o[2] = S.b3[2 * tg]; o[3] = S.b3[2 * tg + 1];
+    const __nv_bfloat16* wr = S.W3 + g * TS2 + 2 * tg;
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt)
+        mma_bf16(o, h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
+                 *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+}
+
+__global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16* __restrict__ w,
+                                                             const float* __restrict__ feat, int n,
+                                                             float* __restrict__ y)
+{
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw);
+    load_tc_weights(S, w);
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -383,53 +445,148 @@ __global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16
             a[kt][2] = pack_bf16(X(r0, c1), X(r0, c1 + 1));
             a[kt][3] = pack_bf16(X(r1, c1), X(r1, c1 + 1));
         }
-        float c[16][4];
-#pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const float b0 = S.b1[8 * nt + 2 * tg], bb1 = S.b1[8 * nt + 2 * tg + 1];
-            c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
-            const __nv_bfloat16* wr = S.W1 + (8 * nt + g) * TS1 + 2 * tg;
-#pragma unroll
-            for (int kt = 0; kt < TK1 / 16; ++kt)
-                mma_bf16(c[nt], a[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
-                         *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
-        }
-        uint32_t h[8][4];
-#pragma unroll
-        for (int kt = 0; kt < 8; ++kt) {
-            h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
-            h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
-            h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
-            h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
-        }
-#pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const float b0 = S.b2[8 * nt + 2 * tg], bb1 = S.b2[8 * nt + 2 * tg + 1];
-            c[nt][0] = b0; c[nt][1] = bb1; c[nt][2] = b0; c[nt][3] = bb1;
-            const __nv_bfloat16* wr = S.W2 + (8 * nt + g) * TS2 + 2 * tg;
-#pragma unroll
-            for (int kt = 0; kt < 8; ++kt)
-                mma_bf16(c[nt], h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
-                         *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
-        }
-#pragma unroll
-        for (int kt = 0; kt < 8; ++kt) {
-            h[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
-            h[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
-            h[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
-            h[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
-        }
-        float o[4] = {S.b3[2 * tg], S.b3[2 * tg + 1], S.b3[2 * tg], S.b3[2 * tg + 1]};
-        const __nv_bfloat16* wr = S.W3 + g * TS2 + 2 * tg;
-#pragma unroll
-        for (int kt = 0; kt < 8; ++kt)
-            mma_bf16(o, h[kt], *reinterpret_cast<const uint32_t*>(wr + 16 * kt),
-                     *reinterpret_cast<const uint32_t*>(wr + 16 * kt + 8));
+        float o[4];
+        tc_tile_forward(S, a, o);
         if (tg == 0) {
             if (r0 < n) { y[2 * (int64_t)r0] = o[0]; y[2 * (int64_t)r0 + 1] = o[1]; }
             if (r1 < n) { y[2 * (int64_t)r1] = o[2]; y[2 * (int64_t)r1 + 1] = o[3]; }
         }
     }
+}
+
+// ------------------------------------------ fused routing inference --
+// Sketch, lower bound, tensor-core forward pass and queue choice of every pair
+// of a WFA batch in one pass, one warp per 16 pairs: lane l < 16 counts the
+// 3-mers of side a of pair l of the tile, lane l + 16 those of side b, into a
+// private histogram column hist[bin][lane] (bin = c0 + 4 c1 + 16 c2, the 2-bit
+// window's own order); the A fragments read feature k = 16 c0 + 4 c1 + c2 as
+// hist[bin][r] - hist[bin][r + 16].  Features, bf16 rounding and the network
+// are those of ga_wfa_features + ga_mlp_forward_fast, so the prediction is the
+// same; nothing but the queue item (route.cuh) leaves the kernel.
+constexpr int RM_WARPS = 16;
+
+__global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* __restrict__ w, PairDesc D, int smax,
+                                                          int32_t* __restrict__ item, int32_t* __restrict__ lb_out,
+                                                          float* __restrict__ y_out, int32_t* __restrict__ counts,
+                                                          int32_t* __restrict__ out_score, int32_t* __restrict__ out_len)
+{
+    extern __shared__ __align__(16) unsigned char rm_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(rm_raw);
+    int* hist_all = reinterpret_cast<int*>(rm_raw + sizeof(TcSmem));
+    __shared__ int local[2 * ROUTE_BUCKETS];
+    load_tc_weights(S, w);
+    if (threadIdx.x < 2 * ROUTE_BUCKETS) local[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, g = lane >> 2, tg = lane & 3;
+    const int side = lane >> 4, sl = lane & 15;
+    int* H = hist_all + wib * 64 * 32 + lane;                 // H[bin * 32]: this lane's column
+    const int* Hw = hist_all + wib * 64 * 32;
+    const int n = D.n;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile * 16 < n; tile += warps) {
+#pragma unroll 8
+        for (int b = 0; b < 64; ++b) H[b * 32] = 0;
+        const int p = tile * 16 + sl;
+        int m = 0, nn = 0;
+        if (p < n) {
+            m = D.a_len[p];
+            nn = D.b_len[p];
+            const uint64_t* P = D.packed + ((side ? D.b_off[p] : D.a_off[p]) >> 5);
+            const int L = side ? nn : m;
+            // 256 symbols at a time: the 8 words that hold them and the next
+            // one (3-mers straddle it) are loaded together, then counted
+            for (int q0 = 0; q0 + 2 < L; q0 += 256) {
+                uint64_t wd[9];
+                const int wlast = ((L - 1) >> 5) - (q0 >> 5) + 1;     // words past this lie beyond the arena's spare
+#pragma unroll
+                for (int j = 0; j < 9; ++j) wd[j] = j <= wlast ? __ldg(P + (q0 >> 5) + j) : 0ull;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int q = q0 + 16 * j;
+                    if (q + 2 >= L) break;
+                    const uint64_t v = (j & 1) ? ((wd[j >> 1] >> 32) | (wd[(j >> 1) + 1] << 32)) : wd[j >> 1];
+                    const int cnt = min(16, L - 2 - q);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (i < cnt) atomicAdd(&H[(int)((v >> (2 * i)) & 63u) * 32], 1);   // no return: no wait
+                }
+            }
+        }
+        __syncwarp();
+        // exact lower bound: lanes l and l + 16 each sum half the bins of pair l
+        int l1 = 0;
+#pragma unroll 8
+        for (int b = side * 32; b < side * 32 + 32; ++b) l1 += abs(Hw[b * 32 + sl] - Hw[b * 32 + sl + 16]);
+        l1 += __shfl_xor_sync(FULL, l1, 16);
+        const int lb = max(abs(m - nn), (l1 + 5) / 6);
+        // A fragments
+        const int r0 = g, r1 = g + 8;
+        const int m0 = __shfl_sync(FULL, m, r0), n0 = __shfl_sync(FULL, nn, r0);
+        const int m1 = __shfl_sync(FULL, m, r1), n1 = __shfl_sync(FULL, nn, r1);
+        auto X = [&](int r, int c, int mr, int nr) -> float {
+            if (c < 64) {
+                const int bin = ((c & 3) << 4) | (c & 12) | (c >> 4);
+                return (float)(Hw[bin * 32 + r] - Hw[bin * 32 + r + 16]) * 0.125f;
+            }
+            if (c == 64) return mr * (1.0f / 256.0f);
+            if (c == 65) return nr * (1.0f / 256.0f);
+            return 0.f;
+        };
+        uint32_t a[TK1 / 16][4];
+#pragma unroll
+        for (int kt = 0; kt < TK1 / 16; ++kt) {
+            const int c0 = 16 * kt + 2 * tg, c1 = c0 + 8;
+            a[kt][0] = pack_bf16(X(r0, c0, m0, n0), X(r0, c0 + 1, m0, n0));
+            a[kt][1] = pack_bf16(X(r1, c0, m1, n1), X(r1, c0 + 1, m1, n1));
+            a[kt][2] = pack_bf16(X(r0, c1, m0, n0), X(r0, c1 + 1, m0, n0));
+            a[kt][3] = pack_bf16(X(r1, c1, m1, n1), X(r1, c1 + 1, m1, n1));
+        }
+        float o[4];
+        tc_tile_forward(S, a, o);
+        const int lb0 = __shfl_sync(FULL, lb, r0), lb1 = __shfl_sync(FULL, lb, r1);
+        if (tg == 0) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = h ? r1 : r0;
+                const int pr = tile * 16 + r;
+                if (pr >= n) continue;
+                const int mr = h ? m1 : m0, nr = h ? n1 : n0, lbr = h ? lb1 : lb0;
+                const float y0 = h ? o[2] : o[0];
+                const int it = route_item(mr, nr, D.pure[pr] != 0, D.pure[n + pr] != 0, lbr, y0, smax);
+                item[pr] = it;
+                if (lb_out) lb_out[pr] = lbr;
+                if (y_out) { y_out[2 * (int64_t)pr] = y0; y_out[2 * (int64_t)pr + 1] = h ? o[3] : o[1]; }
+                if (it < 0) {
+                    out_score[pr] = -1;
+                    if (out_len) out_len[pr] = 0;
+                } else {
+                    atomicAdd(&local[it & 0xff], 1);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * ROUTE_BUCKETS && local[threadIdx.x]) atomicAdd(&counts[threadIdx.x], local[threadIdx.x]);
+}
+
+static size_t route_model_smem() { return sizeof(TcSmem) + (size_t)RM_WARPS * 64 * 32 * sizeof(int); }
+
+// The fused routing pass over a WFA batch (D.packed and D.pure set): per pair
+// the queue item, lower bound and prediction; bucket totals into counts.
+cudaError_t launch_route_model(const PairDesc& D, int smax, int32_t* item, int32_t* lb, float* y, int32_t* counts,
+                               int32_t* out_score, int32_t* out_len, cudaStream_t st)
+{
+    const __nv_bfloat16* w = cost_model_weights();
+    if (!w) return cudaErrorNotReady;
+    if (D.n <= 0) return cudaSuccess;
+    int blocks = (D.n + 16 * RM_WARPS - 1) / (16 * RM_WARPS);
+    if (blocks > 152) blocks = 152;
+    launch_begin(K_MLP, st);
+    route_model_kernel<<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, item, lb, y, counts,
+                                                                          out_score, out_len);
+    launch_end(K_MLP, st);
+    return cudaGetLastError();
 }
 
 static cudaError_t run_forward_tc(const __nv_bfloat16* w, const float* feat, int n, float* y, cudaStream_t st)
@@ -486,6 +643,7 @@ void prepare_mlp()
         cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
         cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
         cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
+        cudaFuncSetAttribute(route_model_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)route_model_smem());
     });
 }
 

@@ -6,7 +6,7 @@
 // latency-bound loop that cannot take cudaMalloc's implicit device-wide
 // synchronisation.  ga_wfa_device_noalloc serves them: the caller passes the
 // inputs and outputs, and every piece of scratch the WFA kernels need (the
-// 2-bit sequence arena, purity flags, the per-warp wavefront stacks, the work
+// 2-bit sequence arena with its per-chunk masks, purity flags, the per-warp wavefront stacks, the work
 // counter and error word) lives in one file-scope __device__ array of
 // NOALLOC_SCRATCH_BYTES, which each GPU that loads this library holds until the
 // process exits.  Batches whose scratch does not fit are refused.
@@ -68,7 +68,7 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
     // scratch layout: [counter, error word | purity flags | 2-bit arena | wavefront stacks]
     const size_t head = 256;
     const size_t pure_bytes = round256(2 * (size_t)b->n);
-    const size_t packed_bytes = round256(((size_t)b->seq_bytes / 32 + 2) * sizeof(uint64_t));
+    const size_t packed_bytes = round256((size_t)packed_arena_words(b->seq_bytes) * sizeof(uint64_t));
     const size_t fixed = head + pure_bytes + packed_bytes;
     const size_t slot_bytes = (size_t)(smax + 1) * (size_t)(smax + 1) * sizeof(int32_t);
     if (fixed + (trace ? 4 * slot_bytes : 0) > NOALLOC_SCRATCH_BYTES) {

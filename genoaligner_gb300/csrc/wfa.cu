@@ -31,13 +31,14 @@ namespace ga {
 // Sequences start on 32-byte boundaries, so word index = byte offset / 32 and
 // no per-sequence bookkeeping is needed.
 __global__ void __launch_bounds__(256) pack_chunks_kernel(const uint8_t* __restrict__ seq, int64_t nchunks,
-                                                          uint64_t* __restrict__ packed)
+                                                          uint64_t* __restrict__ packed, uint32_t* __restrict__ bad)
 {
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += (int64_t)gridDim.x * blockDim.x) {
         const uint4* src = reinterpret_cast<const uint4*>(seq + 32 * c);
         const uint4 x0 = __ldg(src), x1 = __ldg(src + 1);
         const uint32_t parts[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
         uint64_t word = 0;
+        uint32_t badbits = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const uint32_t v = parts[q];
@@ -45,8 +46,14 @@ __global__ void __launch_bounds__(256) pack_chunks_kernel(const uint8_t* __restr
             const uint32_t codes = ((v >> 1) ^ (v >> 2)) & 0x03030303u;
             const uint32_t packed4 = (codes & 3u) | ((codes >> 6) & 0xcu) | ((codes >> 12) & 0x30u) | ((codes >> 18) & 0xc0u);
             word |= (uint64_t)packed4 << (8 * q);
+            // a byte is A, C, G or T iff it equals "ACGT"[its code]
+            const uint32_t sel = (codes & 3u) | ((codes >> 4) & 0x30u) | ((codes >> 8) & 0x300u) | ((codes >> 12) & 0x3000u);
+            const uint32_t diff = __byte_perm(0x54474341u, 0u, sel) ^ v;
+            const uint32_t nz = ((((diff & 0x7f7f7f7fu) + 0x7f7f7f7fu) | diff) >> 7) & 0x01010101u;
+            badbits |= ((nz * 0x10204080u) >> 28) << (4 * q);       // bit 8q+b of nz -> bit 4q+b
         }
         packed[c] = word;
+        bad[c] = badbits;
     }
 }
 
@@ -57,7 +64,26 @@ __device__ __forceinline__ uint32_t acgt_byte(uint32_t c)
     return ((c >> 5) == 2u) & ((0x0010008au >> (c & 31u)) & 1u);
 }
 
-// Purity flag per sequence (a-sides q < n, then b-sides), one thread each.
+// Purity flag per sequence (a-sides q < n, then b-sides) from the per-chunk
+// masks of pack_chunks_kernel: bit b of bad[c] = byte 32c + b is not A/C/G/T.
+__global__ void __launch_bounds__(256) purity_mask_kernel(PairDesc D, const uint32_t* __restrict__ bad,
+                                                          uint8_t* __restrict__ pure)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * D.n; q += gridDim.x * blockDim.x) {
+        const bool is_a = q < D.n;
+        const int p = is_a ? q : q - D.n;
+        const int64_t c0 = (is_a ? D.a_off[p] : D.b_off[p]) >> 5;
+        const int len = is_a ? D.a_len[p] : D.b_len[p];
+        const int full = len >> 5, rest = len & 31;
+        uint32_t acc = 0;
+        for (int w = 0; w < full; ++w) acc |= __ldg(bad + c0 + w);
+        if (rest) acc |= __ldg(bad + c0 + full) & ((1u << rest) - 1u);
+        pure[q] = (uint8_t)(acc == 0);
+    }
+}
+
+// Purity flag per sequence straight from the bytes, one thread each (the
+// Smith-Waterman paths, which read bytes and build no 2-bit arena).
 __global__ void __launch_bounds__(256) purity_kernel(PairDesc D, uint8_t* __restrict__ pure)
 {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * D.n; q += gridDim.x * blockDim.x) {
@@ -241,22 +267,35 @@ __global__ void __launch_bounds__(128) wfa_kernel(WfaArgs A)
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st)
 {
     if (D.n <= 0) return cudaSuccess;
+    int blocks = (2 * D.n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
     if (packed) {
         // every sequence ends >= 64 bytes before the arena's end, so the whole
         // chunks cover them all and no read passes seq_bytes
         const int64_t nchunks = seq_bytes / 32;
-        int64_t blocks = (nchunks + 255) / 256;
-        if (blocks > 152 * 32) blocks = 152 * 32;
+        uint32_t* bad = reinterpret_cast<uint32_t*>(packed + nchunks + 2);
+        int64_t cblocks = (nchunks + 255) / 256;
+        if (cblocks > 152 * 32) cblocks = 152 * 32;
         launch_begin(K_PACK, st);
-        pack_chunks_kernel<<<(int)blocks, 256, 0, st>>>(D.seq, nchunks, packed);
+        pack_chunks_kernel<<<(int)cblocks, 256, 0, st>>>(D.seq, nchunks, packed, bad);
         launch_end(K_PACK, st);
+        launch_begin(K_PACK, st);
+        purity_mask_kernel<<<blocks, 256, 0, st>>>(D, bad, pure);
+        launch_end(K_PACK, st);
+        return cudaGetLastError();
     }
-    int blocks = (2 * D.n + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
     launch_begin(K_PACK, st);
     purity_kernel<<<blocks, 256, 0, st>>>(D, pure);
     launch_end(K_PACK, st);
     return cudaGetLastError();
+}
+
+// 64-bit words of a packed arena for seq_bytes of sequence: the 2-bit words
+// (+2 spare, read by two-word fetch windows) then one 32-bit mask per chunk.
+int64_t packed_arena_words(int64_t seq_bytes)
+{
+    const int64_t nchunks = seq_bytes / 32;
+    return nchunks + 2 + (nchunks + 1) / 2;
 }
 
 size_t wfa_smem_bytes(int smax) { return (size_t)4 * 2 * (2 * smax + 3) * sizeof(int32_t); }

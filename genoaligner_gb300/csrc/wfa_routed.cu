@@ -1,5 +1,6 @@
 // wfa_routed.cu -- the learned-bucketed WFA path: routing and a persistent
-// kernel over bucketed queues with 32-lane and 8-lane groups.
+// kernel over two bucketed queues, one served by whole warps, one by single
+// lanes.
 //
 // Same recurrence and walk as wfa.cu (the reference's wfa_trace_kernel,
 // include/genoaligner/backend/wfa_kernel.hip:119-145, 338-437); what changes is
@@ -9,28 +10,42 @@
 //     sketch an exact lower bound; a pair whose bound exceeds the batch smax is
 //     unresolved at once (the full search would prove the same);
 //   * every other pair gets a first smax -- the prediction with a margin,
-//     never below the bound, never above the batch smax -- and a queue: first
-//     smax <= SMALL_SMAX goes to the small queue, served by 8-lane groups (four
-//     pairs per warp), the rest to the big queue, served by whole warps;
+//     never below the bound, never above the batch smax -- and a queue.  A
+//     pure-ACGT pair of at most LANE_MAXLEN bases a side whose first smax is
+//     <= LANE_SMAX goes to the lane queue: one pair per lane, 32 pairs per
+//     warp in lockstep over (s, k), sequences and wavefront staged in shared
+//     memory.  Every other pair goes to the warp queue (one pair per warp,
+//     lanes over the diagonals of a wavefront);
 //   * the router sorts both queues by first smax, largest first (a counting
-//     sort in three kernels), so neighbours in a queue cost alike;
+//     sort in three kernels), so the 32 pairs of a lane batch cost alike;
 //   * a pair not resolved within its first smax escalates: it is appended to
 //     an escalation list with smax doubled (capped at the batch smax) and the
-//     next launch of the same kernel takes that list as its big queue; a pair
-//     still unresolved at the batch smax is final.
+//     next launch of the same kernel takes that list as its warp queue; a
+//     pair still unresolved at the batch smax is final.
 //
 // Results do not depend on the smax a pair is tried with: wavefront s is the
 // same for every smax >= s, so a pair resolved at any smax >= d returns the
 // reference's score and CIGAR.  All counts live in device memory, so the
 // whole sequence of launches is a fixed graph.
 #include "kernels.cuh"
+#include "route.cuh"
 
 namespace ga {
 
-constexpr int SMALL_SMAX = 15;
-constexpr int ROUTE_BUCKETS = 16;        // by first smax: bucket = bit length of smax
-
-__device__ __forceinline__ int bitlen(unsigned x) { return 32 - __clz(x); }
+// Lane queue (route.cuh): per warp in shared memory, both sequences of its
+// 32 pairs as 32-bit words of 16 2-bit codes [word][lane] (LANE_WORDS = 16
+// data words + 1 read by the two-word fetch window) and one wavefront
+// [k][lane], updated in place.  The walk reads a 16-bit record per (s, k):
+// the predecessor (0 mismatch, 1 insertion, 2 deletion) and the extension
+// length, [idx][lane] in the warp's global stack slot.
+constexpr int LANE_WORDS = LANE_MAXLEN / 16 + 1;
+constexpr int LANE_WS = 2 * LANE_SMAX + 3;
+constexpr int LANE_STACK = (LANE_SMAX + 1) * (LANE_SMAX + 1);
+constexpr int LANE_WARP_SMEM = 2 * LANE_WORDS * 32 + LANE_WS * 32;    // ints per warp
+// Hand-over rule: past wavefront LANE_HAND_S, once at most 1/LANE_HAND_DIV of
+// a warp's pairs are still unresolved, they move to the warp queue.
+constexpr int LANE_HAND_S = 6;
+constexpr int LANE_HAND_DIV = 16;
 
 template <int G>
 __device__ __forceinline__ void gsync(unsigned gmask)
@@ -49,6 +64,200 @@ __device__ __forceinline__ int emit_run_g(char* slot, int pos, int len, char c, 
     }
     for (int q = gl; q < len; q += G) slot[pos - len + q] = c;
     return pos - len;
+}
+
+// ------------------------------------------------------------ lane queue --
+// One lane writes ops [pos - len, pos) of its own slot: bytes up to a 4-byte
+// boundary, then words, then bytes.
+__device__ __forceinline__ int emit_lane(char* slot, int pos, int len, char c, int* err)
+{
+    if (len <= 0) return pos;
+    if (len > pos) {
+        atomicOr(err, ERR_CIGAR_OVERFLOW);
+        len = pos;
+    }
+    char* lo = slot + (pos - len);
+    char* const hi = slot + pos;
+    while (lo < hi && ((uintptr_t)lo & 3u)) *lo++ = c;
+    const uint32_t w4 = (uint32_t)(uint8_t)c * 0x01010101u;
+    while (hi - lo >= 4) { *reinterpret_cast<uint32_t*>(lo) = w4; lo += 4; }
+    while (lo < hi) *lo++ = c;
+    return pos - len;
+}
+
+// 16 codes of a staged sequence from position p (p < LANE_MAXLEN).
+__device__ __forceinline__ uint32_t lane_fetch(const uint32_t* S, int p)
+{
+    const int w = p >> 4;
+    return __funnelshift_r(S[w * 32], S[(w + 1) * 32], 2u * (unsigned)(p & 15));
+}
+
+// Match run of P from v and T from h; SP, ST point at this lane's column.
+__device__ __forceinline__ int lane_run(const uint32_t* SP, const uint32_t* ST, int v, int h, int m, int n)
+{
+    int run = 0;
+    for (;;) {
+        const int lim = min(m - v, n - h);
+        if (lim <= 0) break;
+        const uint32_t x = lane_fetch(SP, v) ^ lane_fetch(ST, h);
+        int eq = x ? (__ffs((int)x) - 1) >> 1 : 16;
+        eq = min(eq, lim);
+        run += eq;
+        v += eq;
+        h += eq;
+        if (eq < 16) break;
+    }
+    return run;
+}
+
+// Pairs of the lane queue, 32 per warp: each lane runs the whole forward
+// pass and walk of its own pair.  All lanes of a warp step through the same
+// (s, k) until the last of them resolves or reaches its first smax, so the
+// shared-memory wavefront [k][lane] and sequences [word][lane] are read
+// without bank conflicts and the walk records coalesce.  The predecessor code
+// the forward pass stores is the argmax the reference's walk recomputes
+// (mismatch on >=, insertion on >, deletion on >), so the walk needs no
+// wavefront values: the offset before extension is the offset minus the
+// stored extension length.
+template <bool TRACE>
+__device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, int lane)
+{
+    const WfaArgs& A = R.A;
+    const uint32_t* SP = smem + lane;
+    const uint32_t* ST = smem + LANE_WORDS * 32 + lane;
+    int32_t* WF = reinterpret_cast<int32_t*>(smem + 2 * LANE_WORDS * 32) + (LANE_SMAX + 1) * 32 + lane;   // WF[k * 32]
+    const int nlane = R.small_count ? *R.small_count : 0;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(R.small_next, 32);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= nlane) break;
+        const int q = base + lane;
+        const bool have = q < nlane;
+        int p = 0, smx = 0, m = 0, n = 0;
+        bool misrouted = false;
+        if (have) {
+            const int2 it = R.small[q];
+            p = it.x;
+            smx = it.y;
+            m = A.D.a_len[p];
+            n = A.D.b_len[p];
+            // the router sends only pairs that fit; anything else goes back to
+            // the warp queue at the same smax
+            misrouted = m <= 0 || n <= 0 || m > LANE_MAXLEN || n > LANE_MAXLEN || smx < 1 || smx > LANE_SMAX ||
+                        !A.D.pure[p] || !A.D.pure[A.D.n + p];
+        }
+        const bool run = have && !misrouted;
+        // stage both sequences: 32-bit words 0 .. (len-1)/16 + 1 lie in the arena
+        {
+            const uint32_t* gP = reinterpret_cast<const uint32_t*>(A.D.packed + (run ? (A.D.a_off[p] >> 5) : 0));
+            const uint32_t* gT = reinterpret_cast<const uint32_t*>(A.D.packed + (run ? (A.D.b_off[p] >> 5) : 0));
+            const int lastP = run ? ((m - 1) >> 4) + 1 : -1, lastT = run ? ((n - 1) >> 4) + 1 : -1;
+            uint32_t* sp = smem + lane;
+#pragma unroll
+            for (int w = 0; w < LANE_WORDS; ++w) {
+                sp[w * 32] = w <= lastP ? __ldg(gP + w) : 0u;
+                sp[(LANE_WORDS + w) * 32] = w <= lastT ? __ldg(gT + w) : 0u;
+            }
+        }
+        const int kfinal = n - m;
+        int score = -1;
+        bool act = run;
+        if (run) {
+            const int off0 = lane_run(SP, ST, 0, 0, m, n);
+            WF[0] = off0;
+            WF[-32] = WFA_NULL;
+            WF[32] = WFA_NULL;
+            if (TRACE) rec[lane] = (uint16_t)(off0 << 2);
+            if (kfinal == 0 && off0 >= n) { score = 0; act = false; }
+        }
+        // When only a few lanes are still running well after the others have
+        // resolved, they are handed to the warp queue (rerun from s = 0
+        // there): the other lanes would otherwise idle.
+        const int started = __popc(__ballot_sync(FULL, act));
+        bool handed = false;
+        for (int s = 1;; ++s) {
+            const unsigned am = __ballot_sync(FULL, act);
+            if (!am) break;
+            if (s > LANE_HAND_S && __popc(am) * LANE_HAND_DIV <= started) {
+                handed = act;
+                act = false;
+                break;
+            }
+            if (act) {
+                WF[(s + 1) * 32] = WFA_NULL;
+                WF[-(s + 1) * 32] = WFA_NULL;
+                int carry = WFA_NULL;                            // wavefront s-1 at k-1
+                for (int k = -s; k <= s; ++k) {
+                    const int mis = WF[k * 32];
+                    const int del = WF[(k + 1) * 32];
+                    int x = mis + 1, code = 0;
+                    if (carry + 1 > x) { x = carry + 1; code = 1; }
+                    if (del > x) { x = del; code = 2; }
+                    carry = mis;
+                    int ext = 0;
+                    if (!wfa_live(x) || x > n || x - k > m) x = WFA_NULL;
+                    else { ext = lane_run(SP, ST, x - k, x, m, n); x += ext; }
+                    WF[k * 32] = x;
+                    if (TRACE) rec[(s * s + s + k) * 32 + lane] = (uint16_t)(code | (ext << 2));
+                }
+                if (kfinal >= -s && kfinal <= s) {
+                    const int fo = WF[kfinal * 32];
+                    if (wfa_live(fo) && fo >= n) { score = s; act = false; }
+                }
+                if (act && s >= smx) act = false;
+            }
+        }
+        // unresolved within the first smax (or handed over): escalate to the
+        // warp queue at the batch smax, warp-aggregated; unresolved at the
+        // batch smax itself: final
+        const bool esc = misrouted || handed || (run && score < 0 && smx < A.smax);
+        const unsigned em = __ballot_sync(FULL, esc);
+        if (em) {
+            int eb = 0;
+            if (lane == 0) eb = atomicAdd(R.esc_count, __popc(em));
+            eb = __shfl_sync(FULL, eb, 0);
+            if (esc) R.esc[eb + __popc(em & ((1u << lane) - 1u))] = make_int2(p, A.smax);
+        }
+        if (!have || esc) continue;
+        if (!TRACE || score < 0) {
+            A.out_score[p] = score;
+            if (A.out_len) A.out_len[p] = 0;
+            continue;
+        }
+        char* slot = A.out_cigar + A.D.out_off[p];
+        int pos = m + n;
+        if (score == 0) {
+            pos = emit_lane(slot, pos, n, 'M', A.err);
+        } else {
+            // the final cell's offset is n (clipped at n, reached >= n)
+            int s = score, k = kfinal, off = n;
+            int h = off, v = off - k;
+            while (v > 0 && h > 0 && s > 0) {
+                const uint32_t r = rec[(s * s + s + k) * 32 + lane];
+                const int ext = (int)(r >> 2), code = (int)(r & 3u);
+                pos = emit_lane(slot, pos, ext, 'M', A.err);
+                pos = emit_lane(slot, pos, 1, code == 0 ? 'X' : (code == 1 ? 'I' : 'D'), A.err);
+                off -= ext;
+                if (code == 0)      { off -= 1; }
+                else if (code == 1) { k -= 1; off -= 1; }
+                else                { k += 1; }
+                h = off;
+                v = off - k;
+                --s;
+            }
+            if (v > 0 && h > 0) {
+                const int r = min(v, h);
+                pos = emit_lane(slot, pos, r, 'M', A.err);
+                v -= r;
+                h -= r;
+            }
+            pos = emit_lane(slot, pos, v, 'D', A.err);
+            pos = emit_lane(slot, pos, h, 'I', A.err);
+        }
+        A.out_score[p] = score;
+        A.out_len[p] = m + n - pos;
+    }
 }
 
 // One pair on a group of G lanes with the given smax.  Returns the score
@@ -183,83 +392,55 @@ __device__ void run_item(const RoutedArgs& R, int2 item, int32_t* wf0, int32_t* 
     }
     if (score < 0 && !final && gl == 0) {
         const int q = atomicAdd(R.esc_count, 1);
-        R.esc[q] = make_int2(p, min(2 * smax, A.smax));
+        R.esc[q] = make_int2(p, A.smax);
     }
 }
 
-// Persistent: whole warps drain the big queue, then 8-lane groups the small one.
+// Lane queue, one pair per lane (persistent, 32 pairs per grab).  Runs
+// before the warp kernel so that its escalations are complete when that
+// kernel reaches them.
+template <bool TRACE>
+__global__ void __launch_bounds__(128) wfa_lane_kernel(RoutedArgs R)
+{
+    extern __shared__ __align__(16) uint32_t lsmem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    uint16_t* rec = TRACE ? R.lane_rec + slot * (int64_t)LANE_STACK * 32 : nullptr;
+    lane_phase<TRACE>(R, lsmem + wib * LANE_WARP_SMEM, rec, lane);
+}
+
+// Warp queue, one pair per warp (persistent): the routed pairs largest first,
+// then the lane queue's escalations.  Every item runs with the batch smax and
+// is final.
 template <bool TRACE>
 __global__ void __launch_bounds__(128) wfa_routed_kernel(RoutedArgs R)
 {
-    extern __shared__ int32_t rsmem[];
+    extern __shared__ __align__(16) int32_t rsmem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int wsz = R.warp_smem;
-    int32_t* wsm = rsmem + wib * wsz;
+    int32_t* wsm = rsmem + wib * R.warp_smem;
     const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     int32_t* stk = TRACE ? R.A.stack + slot * R.A.stack_slot : nullptr;
-    const int nbig = *R.big_count;
-    for (;;) {
-        int q = 0;
-        if (lane == 0) q = atomicAdd(R.big_next, 1);
-        q = __shfl_sync(FULL, q, 0);
-        if (q >= nbig) break;
+    for (int list = 0; list < 2; ++list) {
+        const int2* items = list ? R.esc : R.big;
+        const int cnt = list ? *R.esc_count : *R.big_count;
+        int32_t* next = list ? R.esc_next : R.big_next;
+        for (;;) {
+            int q = 0;
+            if (lane == 0) q = atomicAdd(next, 1);
+            q = __shfl_sync(FULL, q, 0);
+            if (q >= cnt) break;
+            __syncwarp();
+            const int2 it = items[q];
+            run_item<TRACE, 32>(R, it, wsm, wsm + 2 * it.y + 3, stk, lane, FULL);
+        }
         __syncwarp();
-        const int2 it = R.big[q];
-        const int WS = 2 * it.y + 3;
-        run_item<TRACE, 32>(R, it, wsm, wsm + WS, stk, lane, FULL);
-    }
-    // small queue: four independent 8-lane groups per warp
-    const int g = lane >> 3, gl = lane & 7;
-    const unsigned gmask = 0xffu << (8 * g);
-    const int WSs = 2 * SMALL_SMAX + 3;
-    int32_t* gsm = wsm + g * 2 * WSs;
-    int32_t* gstk = TRACE ? stk + g * (SMALL_SMAX + 1) * (SMALL_SMAX + 1) : nullptr;
-    const int nsmall = R.small_count ? *R.small_count : 0;
-    __syncwarp();
-    for (;;) {
-        int q = 0;
-        if (gl == 0) q = atomicAdd(R.small_next, 1);
-        q = __shfl_sync(gmask, q, 8 * g);
-        if (q >= nsmall) break;
-        __syncwarp(gmask);
-        const int2 it = R.small[q];
-        run_item<TRACE, 8>(R, it, gsm, gsm + 2 * it.y + 3, gstk, gl, gmask);
     }
 }
 
 // ------------------------------------------------------------- routing --
-// First smax of pair p from the cost model's log2(d + 1) and the bound.
-__device__ __forceinline__ int first_smax(float y, int lb, int smax)
-{
-    const float dhat = exp2f(fmaxf(y, 0.f)) - 1.f;
-    int s = (int)ceilf(dhat * 1.25f + 2.f);
-    s = max(s, lb);
-    s = max(s, 1);
-    return min(s, smax);
-}
-
-__global__ void route_count_kernel(PairDesc D, const float* __restrict__ y, const int32_t* __restrict__ lb, int smax,
-                                   int32_t* __restrict__ out_score, int32_t* __restrict__ out_len,
-                                   int32_t* __restrict__ counts)
-{
-    __shared__ int local[2 * ROUTE_BUCKETS];
-    if (threadIdx.x < 2 * ROUTE_BUCKETS) local[threadIdx.x] = 0;
-    __syncthreads();
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
-        const int m = D.a_len[p], n = D.b_len[p];
-        if (m > 0 && n > 0 && lb[p] > smax) {             // provably beyond smax
-            out_score[p] = -1;
-            if (out_len) out_len[p] = 0;
-            continue;
-        }
-        const int s = (m > 0 && n > 0) ? first_smax(y[2 * p], lb[p], smax) : smax;
-        const int small = (s <= SMALL_SMAX && m > 0 && n > 0) ? 1 : 0;
-        atomicAdd(&local[small * ROUTE_BUCKETS + min(bitlen((unsigned)s), ROUTE_BUCKETS - 1)], 1);
-    }
-    __syncthreads();
-    if (threadIdx.x < 2 * ROUTE_BUCKETS && local[threadIdx.x]) atomicAdd(&counts[threadIdx.x], local[threadIdx.x]);
-}
-
+// The fused kernel in learned.cu writes every pair's queue item (route.cuh)
+// and the bucket counts; a scan turns counts into queue offsets and a scatter
+// fills the queues.
 // counts[2*NB] -> start offsets (largest bucket first within each queue) and
 // the two queue totals (counts[2*NB], counts[2*NB+1]).
 __global__ void route_scan_kernel(int32_t* counts, int32_t* starts)
@@ -276,22 +457,15 @@ __global__ void route_scan_kernel(int32_t* counts, int32_t* starts)
 }
 
 // Warp-aggregated: lanes with the same (queue, bucket) take one atomic.
-__global__ void route_scatter_kernel(PairDesc D, const float* __restrict__ y, const int32_t* __restrict__ lb, int smax,
-                                     int32_t* __restrict__ starts, int2* __restrict__ big, int2* __restrict__ small)
+__global__ void route_scatter_kernel(int n, const int32_t* __restrict__ item, int32_t* __restrict__ starts,
+                                     int2* __restrict__ big, int2* __restrict__ small)
 {
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    for (int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); p0 < D.n; p0 += stride) {
+    for (int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); p0 < n; p0 += stride) {
         const int p = p0 + lane;
-        int key = -1, s = 0;
-        if (p < D.n) {
-            const int m = D.a_len[p], n = D.b_len[p];
-            if (!(m > 0 && n > 0 && lb[p] > smax)) {
-                s = (m > 0 && n > 0) ? first_smax(y[2 * p], lb[p], smax) : smax;
-                const int isb = (s <= SMALL_SMAX && m > 0 && n > 0) ? 1 : 0;
-                key = isb * ROUTE_BUCKETS + min(bitlen((unsigned)s), ROUTE_BUCKETS - 1);
-            }
-        }
+        const int it = p < n ? item[p] : -1;
+        const int key = it < 0 ? -1 : (it & 0xff), s = it >> 8;
         const unsigned same = __match_any_sync(FULL, key);
         const int leader = __ffs(same) - 1;
         int base = 0;
@@ -305,64 +479,67 @@ __global__ void route_scatter_kernel(PairDesc D, const float* __restrict__ y, co
 }
 
 int route_buckets() { return ROUTE_BUCKETS; }
-int routed_small_smax() { return SMALL_SMAX; }
 
-// Stack ints per warp slot: one big item at the batch smax, or four small ones.
-int64_t routed_stack_slot(int smax)
-{
-    const int64_t big = (int64_t)(smax + 1) * (smax + 1);
-    const int64_t small = 4 * (int64_t)(SMALL_SMAX + 1) * (SMALL_SMAX + 1);
-    return big > small ? big : small;
-}
+// Stack ints per warp slot of the warp kernel: one pair at the batch smax.
+int64_t routed_stack_slot(int smax) { return (int64_t)(smax + 1) * (smax + 1); }
 
-cudaError_t launch_route(const PairDesc& D, const float* y, const int32_t* lb, int smax, int32_t* out_score,
-                         int32_t* out_len, int32_t* counts, int32_t* starts, int2* big, int2* small, cudaStream_t st)
+// 16-bit walk records per warp slot of the lane kernel.
+int64_t lane_rec_slot() { return (int64_t)LANE_STACK * 32; }
+
+cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* starts, int2* big, int2* small,
+                         cudaStream_t st)
 {
-    if (D.n <= 0) return cudaSuccess;
-    int blocks = (D.n + 255) / 256;
+    if (n <= 0) return cudaSuccess;
+    int blocks = (n + 255) / 256;
     if (blocks > 152 * 8) blocks = 152 * 8;
-    launch_begin(K_ROUTE, st);
-    route_count_kernel<<<blocks, 256, 0, st>>>(D, y, lb, smax, out_score, out_len, counts);
-    launch_end(K_ROUTE, st);
     launch_begin(K_ROUTE, st);
     route_scan_kernel<<<1, 32, 0, st>>>(counts, starts);
     launch_end(K_ROUTE, st);
     launch_begin(K_ROUTE, st);
-    route_scatter_kernel<<<blocks, 256, 0, st>>>(D, y, lb, smax, starts, big, small);
+    route_scatter_kernel<<<blocks, 256, 0, st>>>(n, item, starts, big, small);
     launch_end(K_ROUTE, st);
     return cudaGetLastError();
 }
 
-int routed_warp_smem(int smax)
+// Shared-memory ints per warp of the warp kernel (a multiple of 4, so every
+// warp's area is 16-byte aligned).
+int routed_warp_smem(int smax) { return (2 * (2 * smax + 3) + 3) / 4 * 4; }
+
+template <typename K>
+static int per_sm_for(K kernel, size_t smem)
 {
-    const int big = 2 * (2 * smax + 3);
-    const int small = 4 * 2 * (2 * SMALL_SMAX + 3);
-    return big > small ? big : small;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem);
+    return per_sm < 1 ? 1 : per_sm;
 }
 
 int routed_max_slots(int smax, bool trace, int sm_count)
 {
     const size_t smem = (size_t)4 * routed_warp_smem(smax) * sizeof(int32_t);
-    int per_sm = 0;
-    if (trace) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_routed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_routed_kernel<true>, 128, smem);
-    } else {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_routed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_routed_kernel<false>, 128, smem);
-    }
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = trace ? per_sm_for(wfa_routed_kernel<true>, smem) : per_sm_for(wfa_routed_kernel<false>, smem);
     return per_sm * sm_count * 4;
 }
 
-cudaError_t launch_routed(const RoutedArgs& R, int slots, cudaStream_t st)
+int lane_max_slots(bool trace, int sm_count)
 {
-    const int blocks = (slots + 3) / 4;
-    const size_t smem = (size_t)4 * R.warp_smem * sizeof(int32_t);
+    const size_t smem = (size_t)4 * LANE_WARP_SMEM * sizeof(uint32_t);
+    const int per_sm = trace ? per_sm_for(wfa_lane_kernel<true>, smem) : per_sm_for(wfa_lane_kernel<false>, smem);
+    return per_sm * sm_count * 4;
+}
+
+cudaError_t launch_routed(const RoutedArgs& R, int lane_slots, int slots, cudaStream_t st)
+{
     const int id = R.A.trace ? K_WFA_TRACE : K_WFA_SCORE;
+    const size_t lsm = (size_t)4 * LANE_WARP_SMEM * sizeof(uint32_t);
     launch_begin(id, st);
-    if (R.A.trace) wfa_routed_kernel<true><<<blocks, 128, smem, st>>>(R);
-    else wfa_routed_kernel<false><<<blocks, 128, smem, st>>>(R);
+    if (R.A.trace) wfa_lane_kernel<true><<<(lane_slots + 3) / 4, 128, lsm, st>>>(R);
+    else wfa_lane_kernel<false><<<(lane_slots + 3) / 4, 128, lsm, st>>>(R);
+    launch_end(id, st);
+    const size_t smem = (size_t)4 * R.warp_smem * sizeof(int32_t);
+    launch_begin(id, st);
+    if (R.A.trace) wfa_routed_kernel<true><<<(slots + 3) / 4, 128, smem, st>>>(R);
+    else wfa_routed_kernel<false><<<(slots + 3) / 4, 128, smem, st>>>(R);
     launch_end(id, st);
     return cudaGetLastError();
 }

@@ -187,16 +187,19 @@ int32_t ga_wfa_device(const ga_device_batch* batch, int32_t smax, int32_t trace,
                       void* stream, const char** err);
 
 /* ga_wfa_device with extension options (opt may be NULL): opt->learned = 1
- * routes pairs by the cost model (loaded with ga_cost_model_set) through the
- * bucketed persistent kernel, replayed as one CUDA graph; results are the
- * same as without it. */
+ * routes pairs by the cost model (loaded with ga_cost_model_set) into two
+ * bucketed queues served by persistent kernels (one pair per lane for small
+ * predicted distances, one pair per warp otherwise), replayed as one CUDA
+ * graph; results are the same as without it. */
 int32_t ga_wfa_device_ex(const ga_device_batch* batch, int32_t smax, int32_t trace, const ga_options* opt,
                          int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream,
                          const char** err);
 
 /* Routing record of the calling thread's last learned WFA call: out[0] = pairs
- * in the small queue (8-lane groups), out[1] = pairs in the big queue,
- * out[2 + r] = pairs escalated after round r.  Synchronises the device. */
+ * in the lane queue (one pair per lane), out[1] = pairs in the warp queue (one
+ * pair per warp), out[2] = pairs the lane queue escalated to the warp queue
+ * (unresolved within their first smax, or handed over); out[3..] = 0.
+ * Synchronises the device. */
 int32_t ga_wfa_route_stats(int32_t* out, int32_t max);
 
 /* SW over a device batch, score + end cell + start cell + CIGAR.
@@ -211,7 +214,7 @@ int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_
 /* The learned cost model (no counterpart in the reference): a k-mer sketch
  * and an MLP 66 -> 128 -> 128 -> 2 that predicts log2(edit distance + 1) and
  * log2(wavefront cells + 1) of a pair.  It only routes work (the smax tried
- * first, the lane-group size, the queue); results never depend on it. */
+ * first, the kernel variant, the queue); results never depend on it. */
 int32_t ga_cost_model_nparams(void);
 /* Load / read the fp32 parameters of the current device's model (layout: W1
  * [128][66], b1 [128], W2 [128][128], b2 [128], W3 [2][128], b3 [2]). */
@@ -247,8 +250,9 @@ int32_t ga_mlp_train_step(const float* features, const float* targets, int32_t n
  * from one 16 MiB array in the library's device image, which every GPU that
  * loads this library holds until the process exits.
  *
- * Limit: 256 + 2n + (seq_bytes/32 + 2)*8 bytes (each rounded up to 256) must
- * fit in 16 MiB, plus, when trace != 0, four wavefront stacks of
+ * Limit: 256 + 2n + (seq_bytes/32 + 2)*8 + ceil(seq_bytes/64)*8 bytes (each
+ * term rounded up to 256; the last is the 2-bit arena's per-32-byte masks of
+ * non-ACGT bytes) must fit in 16 MiB, plus, when trace != 0, four wavefront stacks of
  * (smax+1)^2 * 4 bytes; a larger batch is refused with GA_INVALID_ARGUMENT and
  * a message, before any device work.
  *

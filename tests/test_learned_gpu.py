@@ -100,6 +100,11 @@ def test_learned_routing_is_bit_exact(model):
         assert small + big <= b.n
         if model == "zero" and smax == 64:
             assert esc[0] > 0                     # the poor model escalates, results unchanged
+        if model == "trained" and smax == 64:
+            # the routed path computes its features from the 2-bit arena: a
+            # wrong feature order there would show up as mispredictions
+            assert small > 0.5 * b.n, (small, big)
+            assert esc[0] < 0.05 * (small + big), esc
 
 
 def test_learned_host_entry_matches_oracle():
