@@ -634,6 +634,18 @@ static void order_by_size(std::vector<int32_t>& v, const int32_t* tl, const int3
     v.swap(out);
 }
 
+// The two-pairs-per-warp kernel at 8 columns per lane: the checkpointed
+// form (sw16ck.cu) unless GA_SW16CK=0 selects the one that stores every
+// cell's direction bits (sw16.cu, also the form at 16 and 32 columns).
+static bool use_sw16ck()
+{
+    static const bool on = [] {
+        const char* e = getenv("GA_SW16CK");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8_t* pure, const uint8_t* skip,
                     const ga_sw_scoring& sc, bool trace, SwPlan& P)
 {
@@ -662,7 +674,8 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
             P.w16[k].push_back(a);
             P.w16[k].push_back(b);
             const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
-            P.dir16[k] = std::max(P.dir16[k], sw16_dir_words(M, N, kWidths[k]));
+            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0) ? sw16ck_dir_words(M, N)
+                                                                        : sw16_dir_words(M, N, kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
         }
         P.dir16[k] = (P.dir16[k] + 3) / 4 * 4;
@@ -690,7 +703,7 @@ static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
             S.max_slots = std::max<int64_t>(S.max_slots, s);
         }
         if (!P.w16[k].empty()) {
-            int s = sw16_max_slots(kWidths[k], sm_count);
+            int s = (use_sw16ck() && k == 0) ? sw16ck_max_slots(sm_count) : sw16_max_slots(kWidths[k], sm_count);
             s = (int)std::min<int64_t>(s, ((int64_t)P.w16[k].size() / 2 + 3) / 4 * 4);
             s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
             S.s16[k] = s;
@@ -717,7 +730,8 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + k; A.err = err;
-            const cudaError_t e = launch_sw16(A, kWidths[k], S.s16[k], st);
+            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], st)
+                                                           : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
         }
         base += (int64_t)P.w16[k].size();

@@ -105,6 +105,11 @@ int sw_max_slots(int C, bool trace, int sm_count);
 cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
 
 bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge);
+// Checkpointed variant (sw16ck.cu), 8 columns per lane only: same arguments,
+// dir_slot = sw16ck_dir_words.
+int64_t sw16ck_dir_words(int M, int N);
+int sw16ck_max_slots(int sm_count);
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st);
 int64_t sw16_dir_words(int M, int N, int C);
 int sw16_max_slots(int C, int sm_count);
 cudaError_t launch_sw16(const Sw16Args& A, int C, int slots, cudaStream_t st);

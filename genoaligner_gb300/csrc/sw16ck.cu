@@ -1,0 +1,529 @@
+// sw16ck.cu -- Smith-Waterman with traceback, two pairs per warp in 16-bit
+// lanes: a score-only forward pass that keeps checkpoints, then the walk over
+// 64 x 64 tiles recomputed with direction bits.
+//
+// Same recurrence, tie rules and walk as sw.cu and sw16.cu (the reference's
+// trace recurrence, include/genoaligner/backend/sw_kernel_impl.hip:286-329,
+// walk :198-242, best cell = first strict maximum in row-major order).  What
+// changes is where the direction bits come from.  Storing four predicate bits
+// for every cell costs three integer instructions per bit and 4 bits of HBM
+// traffic per cell, while the walk reads a thin path through the matrix.  So:
+//
+//   1. forward: H, E, F for every cell with DPX 16x2 max-plus instructions
+//      (__viaddmax_s16x2, __vimax3_s16x2_relu), no predicates.  Kept on the
+//      way: every CK_K-th row, each column's (H - gap_open, F) (checkpoint
+//      rows); every TW-th column, each row's (H - gap_open, E) (column
+//      edges); per lane the best value with its first row and column;
+//   2. the best cell is the warp's (max value, min row, min column);
+//   3. walk: the tile [i0, i] x [TW*b + 1, TW*b + TW] holding the walk's
+//      current cell (i0 = the first row of its CK_K-row block) is recomputed
+//      from the checkpoint row above it and the column edge left of it,
+//      exactly as sw16.cu computes cells (biased 16-bit values, predicate
+//      bits from sign bits), and the walk proceeds inside it; leaving the
+//      tile at its top or left edge, the tile there is recomputed.  Both
+//      pairs of a warp recompute their current tiles in one pass, each half
+//      of a register at its own rows and columns.
+//
+// Recomputed values equal the forward pass's, so the predicates and the walk
+// are those of sw16.cu.  Eligibility is sw16.cu's (host-side check).
+#include "kernels.cuh"
+
+namespace ga {
+
+constexpr int CK_K = 64;                 // rows per checkpoint block
+constexpr int TW = 64;                   // tile width: 32 lanes x 2 columns
+constexpr int CK_BIAS = 1024;            // value bias of the recompute pass
+constexpr int CK_C = 16;                 // forward columns per lane, full bands
+constexpr int CK_BW = 32 * CK_C;         // forward band width, full bands
+
+__host__ __device__ inline int ck_rows(int M) { return M > 1 ? (M - 1) / CK_K : 0; }
+
+// Forward bands: full bands of CK_BW columns while more than CK_BW columns
+// remain, then one band of 32 * CB columns with the smallest CB in
+// {2, 4, 8, 16} that reaches column N.
+__host__ __device__ inline int ck_last_cb(int rest)
+{
+    return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : (rest > 2 * 32 ? 4 : 2));
+}
+// Columns the forward bands cover (the column extent of the checkpoints).
+__host__ __device__ inline int ck_ncol(int N)
+{
+    const int full = N > 0 ? (N - 1) / CK_BW : 0;
+    return full * CK_BW + 32 * ck_last_cb(N - full * CK_BW);
+}
+
+__device__ __forceinline__ int ck_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
+__device__ __forceinline__ int lo16s(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
+__device__ __forceinline__ int hi16s(uint32_t x) { return (int)(int16_t)(x >> 16); }
+
+// (value, row, column) order of the best cell: larger value, then smaller row,
+// then smaller column.
+__device__ __forceinline__ bool ck_better(int v, int r, int c, int bv, int br, int bc)
+{
+    return v > bv || (v == bv && (r < br || (r == br && c < bc)));
+}
+
+// Forward profile of a band at CB columns per lane:
+// prof[((pair * 4 + letter) * (CB / 2) + h) * 32 + t] holds the 16-bit scores
+// (s + gap_open) of this lane's columns 2h, 2h+1.  Past a pattern's end: a
+// score far below any reachable value, so padding columns never hold a row's
+// maximum.
+template <int CB>
+__device__ __forceinline__ void ck_profile_fwd(uint32_t* prof, const uint8_t* patA, const uint8_t* patB, int j0,
+                                               int nvA, int nvB, int sm, int sx, int t)
+{
+    constexpr int PAD = -16384;
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < CB / 2; ++h) {
+        const int c0 = 2 * h, c1 = 2 * h + 1;
+        const int a0 = c0 < nvA ? ck_code(__ldg(patA + j0 + c0)) : 4;
+        const int a1 = c1 < nvA ? ck_code(__ldg(patA + j0 + c1)) : 4;
+        const int b0 = c0 < nvB ? ck_code(__ldg(patB + j0 + c0)) : 4;
+        const int b1 = c1 < nvB ? ck_code(__ldg(patB + j0 + c1)) : 4;
+#pragma unroll
+        for (int L = 0; L < 4; ++L) {
+            const int va0 = a0 == 4 ? PAD : (a0 == L ? sm : sx), va1 = a1 == 4 ? PAD : (a1 == L ? sm : sx);
+            const int vb0 = b0 == 4 ? PAD : (b0 == L ? sm : sx), vb1 = b1 == 4 ? PAD : (b1 == L ? sm : sx);
+            prof[((0 * 4 + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)va0 & 0xffffu) | ((uint32_t)va1 << 16);
+            prof[((1 * 4 + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)vb0 & 0xffffu) | ((uint32_t)vb1 << 16);
+        }
+    }
+    __syncwarp();
+}
+
+// What one forward band pass reads and writes.
+struct FwdCtx {
+    const uint8_t *textA, *textB, *patA, *patB;
+    int mA, nA, mB, nB, M, ncol;
+    uint32_t* ck;            // checkpoint rows [q][col][2]
+    uint32_t* ce;            // column edges [k][row][2]
+    uint32_t* prof;
+    int sm, sx;
+    uint32_t NGO2, NGE2, GO2;
+};
+
+// Band starting at column b0 (0-based), CB columns per lane (the band covers
+// 32 CB columns; the last band of a pair takes the smallest CB that reaches
+// its last column).  Updates the lane's best (value, row, column) per pair.
+template <int CB>
+__device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& cA, int& vB, int& rB, int& cB)
+{
+    constexpr int NH = CB / 2;
+    const uint32_t MIN2 = 0x80008000u, K2 = 0x80008000u;
+    const uint32_t NGO2 = X.NGO2, NGE2 = X.NGE2, GO2 = X.GO2;
+    const int M = X.M, mA = X.mA, mB = X.mB;
+    const int j0 = b0 + t * CB;
+    const int nvA = max(0, min(CB, X.nA - j0)), nvB = max(0, min(CB, X.nB - j0));
+    ck_profile_fwd<CB>(X.prof, X.patA, X.patB, j0, nvA, nvB, X.sm, X.sx, t);
+    uint32_t hgu[CB], fv[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) { hgu[c] = NGO2; fv[c] = 0u; }
+    uint32_t diag_in = NGO2, out_hg = NGO2, out_e = 0u;
+    // left boundary: the column edge at column b0
+    const uint32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / TW - 1) * M : nullptr;
+    uint32_t nxt_hg = NGO2, nxt_e = 0u;
+    if (t == 0 && left) { nxt_hg = left[0]; nxt_e = left[1]; }
+    // this lane writes the column edge after its last column when that column is a multiple of TW
+    const int kout = (j0 + CB) % TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / TW : 0;
+    uint32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * M : nullptr;
+    // text characters travel along the lanes with the boundary values; lane 0 reads them
+    uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.textA) | ((uint32_t)__ldg(X.textB) << 8) : 0u;
+    uint32_t bmax = 0u, brow = 0u, bcol = 0u;             // this band: per half
+    const int steps = M + 31;
+    for (int tau = 0; tau < steps; ++tau) {
+        uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
+        uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
+        ch = __shfl_up_sync(FULL, ch, 1);
+        const int i = tau - t + 1;
+        if (t == 0) {
+            ch = ch_next;
+            if (i < M)
+                ch_next = (uint32_t)(i < mA ? __ldg(X.textA + i) : 'A') | ((uint32_t)(i < mB ? __ldg(X.textB + i) : 'A') << 8);
+            in_hg = nxt_hg;
+            in_e = nxt_e;
+            if (left && i < M) { nxt_hg = left[2 * i]; nxt_e = left[2 * i + 1]; }
+        }
+        if (i < 1 || i > M) continue;
+        const uint32_t* pA = X.prof + ((0 * 4 + ck_code(ch & 0xffu)) * NH) * 32 + t;
+        const uint32_t* pB = X.prof + ((1 * 4 + ck_code(ch >> 8)) * NH) * 32 + t;
+        uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
+        uint32_t rowmax = 0u;
+#pragma unroll
+        for (int cc = 0; cc < CB; cc += 2) {
+            const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
+            const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
+            uint32_t hh2[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int cu = cc + u;
+                const uint32_t S = u ? S1 : S0;
+                const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);         // max(E_left - ge, H_left - go)
+                const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]); // max(F_up - ge, H_up - go)
+                const uint32_t h1 = __viaddmax_s16x2(hgd, S, e);            // max(H_diag + s, E)
+                const uint32_t hh = __vimax3_s16x2_relu(h1, f, f);          // max(h1, F, 0)
+                const uint32_t hg = __viaddmax_s16x2(hh, NGO2, MIN2);       // H - go
+                hh2[u] = hh;
+                hgd = hgu[cu];
+                hgu[cu] = hg;
+                fv[cu] = f;
+                hgl = hg;
+                el = e;
+            }
+            rowmax = __vimax3_s16x2(rowmax, hh2[0], hh2[1]);
+        }
+        diag_in = in_hg;
+        out_hg = hgl;
+        out_e = el;
+        if (eout) { eout[2 * (i - 1)] = out_hg; eout[2 * (i - 1) + 1] = out_e; }
+        if ((i & (CK_K - 1)) == 0 && i < M) {                     // checkpoint row i
+            uint4* dst = reinterpret_cast<uint4*>(X.ck + 2 * ((int64_t)(i / CK_K - 1) * X.ncol + j0));
+#pragma unroll
+            for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_uint4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
+        }
+        // rows past a pair's text do not count
+        rowmax &= (i <= mA ? 0x0000ffffu : 0u) | (i <= mB ? 0xffff0000u : 0u);
+        // strict improvement per half: bit 15 / 31 of d clear
+        const uint32_t d = bmax - rowmax + K2;
+        const uint32_t imp = ((~d & K2) >> 15) * 0xffffu;
+        if (imp) {
+            // first column of this row holding the new maximum, per half
+            uint32_t acc = 0;
+#pragma unroll
+            for (int c = 0; c < CB; ++c) {
+                const uint32_t h = __viaddmax_s16x2(hgu[c], GO2, MIN2);
+                acc = (acc >> 1) | ((h - rowmax + K2) & K2);
+            }
+            constexpr uint32_t CM = (1u << CB) - 1u;
+            const int fa = __ffs((int)((acc >> (16 - CB)) & CM)) - 1, fb = __ffs((int)((acc >> (32 - CB)) & CM)) - 1;
+            const uint32_t colp = ((uint32_t)(j0 + fa + 1) & 0xffffu) | ((uint32_t)(j0 + fb + 1) << 16);
+            bmax = __vmaxs2(bmax, rowmax);
+            brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
+            bcol = (bcol & ~imp) | (colp & imp);
+        }
+    }
+    // merge the band into the lane's best
+    const int v = lo16s(bmax), r = (int)(brow & 0xffffu), c = (int)(bcol & 0xffffu);
+    if (v > 0 && ck_better(v, r, c, vA, rA, cA)) { vA = v; rA = r; cA = c; }
+    const int v2 = hi16s(bmax), r2 = (int)(brow >> 16), c2 = (int)(bcol >> 16);
+    if (v2 > 0 && ck_better(v2, r2, c2, vB, rB, cB)) { vB = v2; rB = r2; cB = c2; }
+    __syncwarp();
+}
+
+// Tile profile of one pair: prof[(pair * 4 + letter) * 32 + t] for the
+// tile's columns col0 + 2t, col0 + 2t + 1 (0-based); past the end: mismatch.
+__device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* pat, int n, int col0, int pair,
+                                                int sm, int sx, int t)
+{
+    const int c0 = col0 + 2 * t, c1 = c0 + 1;
+    const int a0 = c0 < n ? ck_code(__ldg(pat + c0)) : 4;
+    const int a1 = c1 < n ? ck_code(__ldg(pat + c1)) : 4;
+#pragma unroll
+    for (int L = 0; L < 4; ++L) {
+        const int v0 = a0 == L ? sm : sx, v1 = a1 == L ? sm : sx;
+        prof[(pair * 4 + L) * 32 + t] = ((uint32_t)v0 & 0xffffu) | ((uint32_t)v1 << 16);
+    }
+}
+
+__global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
+{
+    constexpr int NH = CK_C / 2;
+    constexpr int TSTEPS = CK_K + 31;
+    extern __shared__ uint32_t ck_smem[];
+    const int t = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    uint32_t* wslot = A.dirs + slot * A.dir_slot;
+    uint32_t* prof = ck_smem + wib * (2 * 4 * NH * 32);
+    const int go = A.gap_open, ge = A.gap_extend;
+    const int sm = A.match + go, sx = A.mismatch + go;
+    // unbiased forward constants (per half)
+    const uint32_t NGO2 = ((uint32_t)(-go) & 0xffffu) * 0x10001u;
+    const uint32_t NGE2 = ((uint32_t)(-ge) & 0xffffu) * 0x10001u;
+    const uint32_t GO2 = (uint32_t)go * 0x10001u;
+    const uint32_t MIN2 = 0x80008000u;
+    const uint32_t K2 = 0x80008000u;
+    // biased recompute constants (sw16.cu)
+    const uint32_t B2 = (uint32_t)CK_BIAS * 0x10001u;
+    const uint32_t KGE2 = K2 + (uint32_t)ge * 0x10001u;
+
+    for (;;) {
+        int w = 0;
+        if (t == 0) w = atomicAdd(A.counter, 1);
+        w = __shfl_sync(FULL, w, 0);
+        if (w >= A.nwork) break;
+        __syncwarp();
+        const int pa = A.work[2 * w];
+        const bool has_b = A.work[2 * w + 1] >= 0;
+        const int pb = has_b ? A.work[2 * w + 1] : pa;
+        const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
+        const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
+        const uint8_t* textA = A.D.seq + A.D.a_off[pa];
+        const uint8_t* patA = A.D.seq + A.D.b_off[pa];
+        const uint8_t* textB = A.D.seq + A.D.a_off[pb];
+        const uint8_t* patB = A.D.seq + A.D.b_off[pb];
+        const int M = max(mA, mB), N = max(nA, nB);
+        const int ncol = ck_ncol(N);
+        const int nq = ck_rows(M);
+        // slot layout: checkpoint rows [q][col][2], column edges [k][row][2],
+        // tile tables [pair][step][lane]
+        uint32_t* ck = wslot;
+        uint32_t* ce = ck + 2 * (int64_t)nq * ncol;
+        uint32_t* tiles = ce + 2 * (int64_t)(ncol / TW) * M;
+
+        // ------------------------------------------------ forward pass --
+        int vA = 0, rA = 0, cA = 0, vB = 0, rB = 0, cB = 0;          // lane's best per pair
+        {
+            FwdCtx X{textA, textB, patA, patB, mA, nA, mB, nB, M, ncol, ck, ce, prof, sm, sx, NGO2, NGE2, GO2};
+            for (int b0 = 0; b0 < N;) {
+                const int rest = N - b0;                              // columns from this band on
+                const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
+                if (cb == 16) fwd_band<16>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 8) fwd_band<8>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 4) fwd_band<4>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else fwd_band<2>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                b0 += 32 * cb;
+            }
+        }
+        // per pair over the warp: (max value, min row, min column)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const int ov = __shfl_xor_sync(FULL, vA, o), orr = __shfl_xor_sync(FULL, rA, o), oc = __shfl_xor_sync(FULL, cA, o);
+            if (ov > 0 && ck_better(ov, orr, oc, vA, rA, cA)) { vA = ov; rA = orr; cA = oc; }
+            const int ov2 = __shfl_xor_sync(FULL, vB, o), orr2 = __shfl_xor_sync(FULL, rB, o), oc2 = __shfl_xor_sync(FULL, cB, o);
+            if (ov2 > 0 && ck_better(ov2, orr2, oc2, vB, rB, cB)) { vB = ov2; rB = orr2; cB = oc2; }
+        }
+
+        // ----------------------------------------------------- the walks --
+        // per pair: cell, state (0 H, 1 E, 2 F), tracked value, CIGAR cursor, tile
+        int wi[2] = {rA, rB}, wj[2] = {cA, cB}, wst[2] = {0, 0}, wv[2] = {vA, vB};
+        int wpos[2] = {mA + nA, mB + nB};
+        bool done[2] = {vA <= 0, !has_b || vB <= 0};
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+            if (x == 1 && !has_b) break;
+            if (t == 0) {
+                const int p = x ? pb : pa;
+                if (done[x]) {
+                    A.out_score[p] = 0;
+                    A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+                    A.out_len[p] = 0;
+                } else {
+                    A.out_score[p] = x ? vB : vA;
+                    A.out_pos[4 * p + 2] = (x ? rB : rA) - 1;
+                    A.out_pos[4 * p + 3] = (x ? cB : cA) - 1;
+                }
+            }
+        }
+        int ti0[2] = {1, 1}, tb[2] = {0, 0};
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+            ti0[x] = done[x] ? 1 : ((wi[x] - 1) / CK_K) * CK_K + 1;
+            tb[x] = done[x] ? 0 : (wj[x] - 1) / TW;
+        }
+        uint32_t* tileA = tiles;
+        uint32_t* tileB = tiles + TSTEPS * 32;
+        while (!(done[0] && done[1])) {
+            // ---- recompute both pairs' tiles: pair x rows [ti0, wi], columns [TW*tb, TW*tb + TW)
+            const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
+            const int R = max(rows0, rows1);
+            const int steps = R + 31;
+            __syncwarp();
+            ck_profile_tile(prof, patA, nA, TW * tb[0], 0, sm, sx, t);
+            ck_profile_tile(prof, patB, nB, TW * tb[1], 1, sm, sx, t);
+            __syncwarp();
+            uint32_t hgu[2], fv[2];
+            uint32_t diag_in;
+            {
+                const int qa = (ti0[0] - 1) / CK_K - 1, qb = (ti0[1] - 1) / CK_K - 1;
+                const uint32_t* ca = ck + 2 * (int64_t)max(qa, 0) * ncol;
+                const uint32_t* cb = ck + 2 * (int64_t)max(qb, 0) * ncol;
+                const int colA = TW * tb[0] + 2 * t, colB = TW * tb[1] + 2 * t;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const uint32_t ha = qa >= 0 ? ca[2 * (colA + c)] : NGO2, fa = qa >= 0 ? ca[2 * (colA + c) + 1] : 0u;
+                    const uint32_t hb = qb >= 0 ? cb[2 * (colB + c)] : NGO2, fb = qb >= 0 ? cb[2 * (colB + c) + 1] : 0u;
+                    hgu[c] = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
+                    fv[c] = __viaddmax_s16x2(__byte_perm(fa, fb, 0x7610), B2, MIN2);
+                }
+                // H[i0-1][first column - 1] - go: the left lane's last column; for lane 0
+                // the checkpoint left of the tile (0 on row 0 and column 0)
+                uint32_t lft = __shfl_up_sync(FULL, hgu[1], 1);
+                if (t == 0) {
+                    const uint32_t ha = (qa >= 0 && tb[0] > 0) ? ca[2 * (TW * tb[0] - 1)] : NGO2;
+                    const uint32_t hb = (qb >= 0 && tb[1] > 0) ? cb[2 * (TW * tb[1] - 1)] : NGO2;
+                    lft = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
+                }
+                diag_in = lft;
+            }
+            // lane 0's left boundary per tile row: the column edges at TW*tb,
+            // combined and biased into shared memory first
+            uint32_t* edg = prof + 2 * 4 * 32;                           // [row][2], after the tile profile
+            {
+                const uint32_t* la = tb[0] > 0 ? ce + 2 * ((int64_t)(tb[0] - 1) * M + (ti0[0] - 1)) : nullptr;
+                const uint32_t* lb = tb[1] > 0 ? ce + 2 * ((int64_t)(tb[1] - 1) * M + (ti0[1] - 1)) : nullptr;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int r = t + 32 * h;
+                    const bool ina = la && r < rows0, inb = lb && r < rows1;
+                    const uint32_t ha = ina ? la[2 * r] : NGO2, ea = ina ? la[2 * r + 1] : 0u;
+                    const uint32_t hb = inb ? lb[2 * r] : NGO2, eb = inb ? lb[2 * r + 1] : 0u;
+                    edg[2 * r] = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
+                    edg[2 * r + 1] = __viaddmax_s16x2(__byte_perm(ea, eb, 0x7610), B2, MIN2);
+                }
+            }
+            __syncwarp();
+            uint32_t out_hg = B2 - GO2, out_e = B2;
+            const uint8_t* tA = textA + (ti0[0] - 1);
+            const uint8_t* tB = textB + (ti0[1] - 1);
+            uint32_t ch = 0;
+            uint32_t ch_next = t == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
+            for (int tau = 0; tau < steps; ++tau) {
+                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
+                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
+                ch = __shfl_up_sync(FULL, ch, 1);
+                const int i = tau - t + 1;                                   // tile row, 1-based
+                if (t == 0) {
+                    ch = ch_next;
+                    if (i < R)
+                        ch_next = (uint32_t)(i < rows0 ? __ldg(tA + i) : 'A') | ((uint32_t)(i < rows1 ? __ldg(tB + i) : 'A') << 8);
+                    if (i <= R) { in_hg = edg[2 * (i - 1)]; in_e = edg[2 * (i - 1) + 1]; }
+                }
+                if (i < 1 || i > R) continue;
+                const uint32_t wa = prof[(0 * 4 + ck_code(ch & 0xffu)) * 32 + t], wb = prof[(1 * 4 + ck_code(ch >> 8)) * 32 + t];
+                uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
+                uint32_t acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const uint32_t S = __byte_perm(wa, wb, u ? 0x7632 : 0x5410);
+                    const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
+                    const uint32_t f = __viaddmax_s16x2(fv[u], NGE2, hgu[u]);
+                    const uint32_t h0 = hgd + S;
+                    const uint32_t h1 = __vmaxs2(h0, e);
+                    const uint32_t hh = __vimax3_s16x2(h1, f, B2);
+                    acc0 = (acc0 >> 1) | ((h0 - e + K2) & K2);
+                    acc1 = (acc1 >> 1) | ((h1 - f + K2) & K2);
+                    acc2 = (acc2 >> 1) | ((hgl - el + KGE2) & K2);
+                    acc3 = (acc3 >> 1) | ((hgu[u] - fv[u] + KGE2) & K2);
+                    const uint32_t hg = hh - GO2;
+                    hgd = hgu[u];
+                    hgu[u] = hg;
+                    fv[u] = f;
+                    hgl = hg;
+                    el = e;
+                }
+                // cell c at bits 14 + c / 30 + c: move to 8 + c / 24 + c, then
+                // byte k = predicate k per pair as in sw16.cu
+                acc0 >>= 6; acc1 >>= 6; acc2 >>= 6; acc3 >>= 6;
+                const uint32_t t01 = __byte_perm(acc0, acc1, 0x7351);
+                const uint32_t t23 = __byte_perm(acc2, acc3, 0x7351);
+                tileA[tau * 32 + t] = __byte_perm(t01, t23, 0x5410);
+                tileB[tau * 32 + t] = __byte_perm(t01, t23, 0x7632);
+                diag_in = in_hg;
+                out_hg = hgl;
+                out_e = el;
+            }
+            __syncwarp();
+            // ---- walk each pair inside its tile
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                if (done[x]) continue;
+                const int p = x ? pb : pa;
+                const int m = x ? mB : mA, n = x ? nB : nA;
+                const uint8_t* text = x ? textB : textA;
+                const uint8_t* pat = x ? patB : patA;
+                const uint32_t* tt_tab = x ? tileB : tileA;
+                char* slotc = A.out_cigar + A.D.out_off[p];
+                const int i0 = ti0[x], jlo = TW * tb[x] + 1;
+                int i = wi[x], j = wj[x], state = wst[x], v = wv[x], pos = wpos[x];
+                bool fin = false;
+                for (;;) {
+                    if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
+                    if (i < i0 || j < jlo) break;                          // left the tile
+                    const int jj = j - jlo;
+                    const int tt = jj >> 1, c = jj & 1;
+                    const uint32_t word = tt_tab[((i - i0) + tt) * 32 + tt];
+                    const bool notE = (word >> c) & 1u, notF = (word >> (8 + c)) & 1u;
+                    const bool eopen = (word >> (16 + c)) & 1u, fopen = (word >> (24 + c)) & 1u;
+                    char op;
+                    if (state == 0) {
+                        if (!notF) {
+                            op = 'I';
+                            if (!fopen) { state = 2; v += ge; } else { v += go; }
+                            --i;
+                        } else if (!notE) {
+                            op = 'D';
+                            if (!eopen) { state = 1; v += ge; } else { v += go; }
+                            --j;
+                        } else {
+                            const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
+                            op = ta == pc ? 'M' : 'X';
+                            v -= ta == pc ? A.match : A.mismatch;
+                            --i;
+                            --j;
+                        }
+                    } else if (state == 1) {
+                        op = 'D';
+                        if (!eopen) { v += ge; } else { v += go; state = 0; }
+                        --j;
+                    } else {
+                        op = 'I';
+                        if (!fopen) { v += ge; } else { v += go; state = 0; }
+                        --i;
+                    }
+                    if (pos <= 0) {
+                        if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
+                        fin = true;
+                        break;
+                    }
+                    --pos;
+                    if (t == 0) slotc[pos] = op;
+                }
+                wi[x] = i; wj[x] = j; wst[x] = state; wv[x] = v; wpos[x] = pos;
+                if (fin) {
+                    done[x] = true;
+                    if (t == 0) {
+                        A.out_pos[4 * p] = i;
+                        A.out_pos[4 * p + 1] = j;
+                        A.out_len[p] = m + n - pos;
+                    }
+                } else {
+                    // next tile: the block above (left its top) or the tile to the left
+                    if (i < i0) ti0[x] = ((i - 1) / CK_K) * CK_K + 1;
+                    tb[x] = (j - 1) / TW;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Words of one warp slot for an item of at most M rows and N columns:
+// checkpoint rows, column edges, the two tile tables.  The kernel runs 8
+// columns per lane; other widths are not served.
+int64_t sw16ck_dir_words(int M, int N)
+{
+    const int64_t ncol = ck_ncol(N);
+    return 2 * (int64_t)ck_rows(M) * ncol + 2 * (ncol / TW) * (int64_t)M + 2 * (int64_t)(CK_K + 31) * 32;
+}
+
+static size_t sw16ck_smem() { return (size_t)4 * 2 * 4 * (CK_C / 2) * 32 * sizeof(uint32_t); }
+
+int sw16ck_max_slots(int sm_count)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel, 128, sw16ck_smem());
+    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+}
+
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st)
+{
+    if (A.nwork <= 0) return cudaSuccess;
+    const int blocks = (slots + 3) / 4;
+    launch_begin(K_SW16X2_TRACE, st);
+    sw16ck_kernel<<<blocks, 128, sw16ck_smem(), st>>>(A);
+    launch_end(K_SW16X2_TRACE, st);
+    return cudaGetLastError();
+}
+
+}  // namespace ga
