@@ -1,24 +1,27 @@
 #!/usr/bin/env python3
 """Benchmark of the batched pairwise-alignment hot path on GB300.
 
-Default workload: the uneven Smith-Waterman batch -- 200,000 DNA pairs,
+Headline workload: the uneven Smith-Waterman batch -- 200,000 DNA pairs,
 query log-uniform 50-1,000 bp, target = query at 5 % divergence between
 uniform 0-500 bp flanks, scoring {2,-3,3,1}, score + end + start + CIGAR for
-every pair.  A step is one pass of the aligner over the whole batch.
+every pair, all pairs in one persistent launch.  A step is one pass of the
+aligner over the whole batch.
 
 * ``value``: GCUPS (sum of text_len * pattern_len over the batch / step time)
-  with the batch already resident in HBM, through the device-resident entry
+  with the batch resident in HBM, through the device-resident entry
   (ga_sw_device), timed with CUDA events on the launch stream.
 * ``e2e``: the same metric through the public C ABI call (ga_align_sw_batch)
-  with host buffers: staging, host-to-device copy, kernels, device-to-host copy
-  and CIGAR/validation materialisation are inside every step.
+  with host buffers: staging, host-to-device copy, kernels, device-to-host
+  copy and CIGAR/validation materialisation are inside every step.
 * ``roofline``: the dominant kernel's cells per launch over its average
-  event-timed launch duration, against the integer-pipe peak measured by a
-  microbenchmark kernel on this GPU (6 integer operations per cell).
+  event-timed launch duration, against the DPX rate this GPU retires
+  (__viaddmax_s32, measured by peak.cu) divided by 6 instructions per cell;
+  ``traffic`` is its DRAM bytes per launch from the committed ncu summary.
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's CPU path)
   on a bounded sample, on this host's cores.
-* ``extra.wfa``: WFA pairs/s on the 10,000-pair 150 bp / 2 % batch (smax 64,
-  CIGAR) the same two ways.
+* ``extra``: the WFA workloads (150 bp / 2 %; the 1,000,000-pair mixed batch,
+  plain fixed smax 64 against the learned-bucketed form; the long 1-10 kb
+  batch at smax 2048) and a sample of the long Smith-Waterman batch.
 
 ``--impl reference`` times the reference's CPU path (the oracle port) on the
 host cores on bounded samples of the same workload and prints the same line
@@ -44,6 +47,12 @@ sys.path.insert(0, ROOT)
 METRIC = "WFA pairs/s & SW GCUPS on 1 GB300, learned-bucketed vs plain, bit-exact"
 SCORING = (2, -3, 3, 1)
 OPS_PER_CELL = 6
+# DRAM bytes per cell of the two-pairs-per-warp trace kernel, from
+# profiles/sw16ck_trace_sw_uneven.md (ncu, 20,000-pair sample of the same
+# batch: read + write bytes / cells; traffic grows with the cells processed)
+SW16CK_DRAM_BYTES_PER_CELL = 0.0528
+SW_WORKLOAD = ("sw_uneven_200k: 200,000 pairs, query log-uniform 50-1,000 bp, target = query at 5% "
+               "(sub/ins/del 60/20/20) between U{0..500} flanks, scoring {2,-3,3,1}, score+end+start+CIGAR")
 
 
 def parse():
@@ -55,17 +64,20 @@ def parse():
     ap.add_argument("--pairs", type=int, default=200_000)
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long_sample"],
+                    help="run one of the extra workloads alone (no CPU baseline) and print its JSON")
     return ap.parse_args()
 
 
-def dist_setup(n):
+def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world, local
 
@@ -94,7 +106,6 @@ class Clocks:
 
     def __init__(self, gpu_index):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.gpu = gpu_index
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                        "-i", str(gpu_index), "-lms", "200"], stdout=self.f,
@@ -140,8 +151,7 @@ def cpu_baseline_sw(ps, seconds, threads):
     order = np.random.default_rng(123).permutation(ps.n)
     done_cells, t_used, k, chunk = 0, 0.0, 0, 256
     while t_used < seconds and k < ps.n:
-        idx = order[k:k + chunk]
-        sub = ps.subset(idx)
+        sub = ps.subset(order[k:k + chunk])
         ts, pp = sub.lists()
         t0 = time.perf_counter()
         oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=threads)
@@ -152,15 +162,20 @@ def cpu_baseline_sw(ps, seconds, threads):
     return done_cells / t_used / 1e9, k, done_cells
 
 
-def cpu_baseline_wfa(ps, seconds, threads):
+def cpu_baseline_wfa(ps, seconds, threads, smax=64):
+    """The oracle on a bounded sample of a WFA batch: pairs/s."""
     import oracle
-    pats, txts = ps.lists()
-    done, t_used = 0, 0.0
-    while t_used < seconds and done < 4 * ps.n:
+    order = np.random.default_rng(321).permutation(ps.n)
+    done, t_used, k, chunk = 0, 0.0, 0, 2048
+    while t_used < seconds and k < ps.n:
+        sub = ps.subset(order[k:k + chunk])
+        pats, txts = sub.lists()
         t0 = time.perf_counter()
-        oracle.wfa_batch(pats, txts, smax=64, with_cigar=True, threads=threads)
+        oracle.wfa_batch(pats, txts, smax=smax, with_cigar=True, threads=threads, max_smax=max(smax, 511))
         t_used += time.perf_counter() - t0
-        done += ps.n
+        done += sub.n
+        k += chunk
+        chunk = min(chunk * 2, 65536)
     return done / t_used, done
 
 
@@ -171,8 +186,7 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     ps = workloads.sw_uneven_200k(n=args.pairs)
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
-    vals = []
-    samples = []
+    vals, samples = [], []
     for s in range(args.warmup + args.steps):
         g, k, cells = cpu_baseline_sw(ps, per_step, threads)
         if s >= args.warmup:
@@ -184,9 +198,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sw_cells(ps) / (v * 1e9) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, seed 2)",
-        "config": {"workload": "sw_uneven_200k: 200,000 pairs, query log-uniform 50-1,000 bp, target = query at "
-                               "5% (sub/ins/del 60/20/20) between U{0..500} flanks, scoring {2,-3,3,1}, "
-                               "score+end+start+CIGAR", "pairs": ps.n, "cells": sw_cells(ps)},
+        "config": {"workload": SW_WORKLOAD, "pairs": ps.n, "cells": sw_cells(ps)},
         "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
                          "sample": f"per step: pairs from a fixed random permutation until ~{per_step:.0f} s of "
                                    f"CPU time (last step {samples[-1][0]} pairs, {samples[-1][1] / 1e9:.2f} Gcells)"},
@@ -195,9 +207,135 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def timed(fn, stream, steps, flush=None):
+    """Median CUDA-event time of `steps` calls of fn on `stream` (ms)."""
+    import torch
+    ts = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def bench_wfa_150(api, workloads, torch, dev, stream, args, cpu):
+    ps = workloads.wfa_150bp_2pct()
+    n = ps.n
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    sc = torch.empty(n, dtype=torch.int32, device=dev)
+    ln = torch.empty(n, dtype=torch.int32, device=dev)
+    cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream)
+    for _ in range(3):
+        fn()
+    dev_ms = timed(fn, stream, max(args.steps, 5), flush)
+    reqs = api.make_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, 64, True)
+    res = np.zeros(n, api.RES_DT)
+    cig = np.empty(int(api.load().ga_align_cigar_bytes(reqs.ctypes.data, n)), np.uint8)
+    call = lambda: api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, _reqs=reqs,
+                                          _res=res, _cig=cig)
+    for _ in range(3):
+        call()
+    t = []
+    for _ in range(max(args.steps, 5)):
+        t0 = time.perf_counter()
+        call()
+        t.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(t) * 1e3
+    out = {"workload": "wfa_150bp_2pct: 10,000 pairs, 150 bp, 2% (sub/ins/del equal), smax 64, CIGAR",
+           "pairs_per_s": n / (dev_ms * 1e-3), "ms_per_step": dev_ms,
+           "e2e_pairs_per_s": n / (e2e_ms * 1e-3), "e2e_ms_per_step": e2e_ms,
+           "l2": "256 MB buffer written between steps"}
+    if cpu:
+        pps, done = cpu_baseline_wfa(ps, 4.0, os.cpu_count() or 1)
+        out.update({"cpu_baseline_pairs_per_s": pps, "cpu_cores": os.cpu_count(), "cpu_kind": "port",
+                    "cpu_sample": f"{done} pairs"})
+    return out
+
+
+def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
+    """1,000,000 mixed-divergence pairs: plain fixed smax 64 against the
+    learned-bucketed form, both through ga_wfa_device_ex, bit-exact check."""
+    ps = workloads.wfa_mixed()
+    n = ps.n
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    have_model = cost_model.load_default()
+    out = {"workload": "wfa_mixed_1m: 1,000,000 pairs, 150-250 bp, error 70% U[0,2%] / 25% U[2,10%] / "
+                       "5% U[10,30%], smax 64, CIGAR", "model_loaded": have_model}
+    scores = {}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for learned in ((False, True) if have_model else (False,)):
+        sc = torch.empty(n, dtype=torch.int32, device=dev)
+        ln = torch.empty(n, dtype=torch.int32, device=dev)
+        cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
+        fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
+        for _ in range(3):
+            fn()
+        ms = timed(fn, stream, max(args.steps, 5), flush)
+        key = "learned" if learned else "plain"
+        out[key] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms}
+        scores[key] = (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy())
+        if learned:
+            small, big, esc = api.wfa_route_stats()
+            resolved = int((scores[key][0] >= 0).sum())
+            out[key].update({"lane_queue_pairs": small, "warp_queue_pairs": big, "escalated": int(esc[0]),
+                             "escalation_rate": esc[0] / max(1, small),
+                             "unresolved_by_bound_or_search": n - resolved})
+    if "learned" in scores:
+        a, b = scores["plain"], scores["learned"]
+        out["bit_identical"] = bool(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and
+                                    np.array_equal(a[2], b[2]))
+        out["learned_over_plain"] = out["learned"]["pairs_per_s"] / out["plain"]["pairs_per_s"]
+    if cpu:
+        pps, done = cpu_baseline_wfa(ps, 4.0, os.cpu_count() or 1)
+        out.update({"cpu_baseline_pairs_per_s": pps, "cpu_cores": os.cpu_count(), "cpu_kind": "port",
+                    "cpu_sample": f"{done} pairs"})
+    return out
+
+
+def bench_wfa_long(api, workloads, torch, dev, stream, args):
+    ps = workloads.wfa_long_1k_10k()
+    n = ps.n
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    sc = torch.empty(n, dtype=torch.int32, device=dev)
+    ln = torch.empty(n, dtype=torch.int32, device=dev)
+    cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
+    fn = lambda: api.wfa_device(batch, 2048, True, sc, ln, cg, stream=stream.cuda_stream)
+    fn()
+    ms = timed(fn, stream, 2)
+    s = sc.cpu().numpy()
+    return {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR",
+            "pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms, "unresolved": int((s < 0).sum())}
+
+
+def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
+    """A sample of the long SW batch (2-30 kb queries, 0-5 kb flanks)."""
+    ps = workloads.sw_long_4k(n=n_pairs)
+    cells = sw_cells(ps)
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    n = ps.n
+    sc = torch.empty(n, dtype=torch.int32, device=dev)
+    pos = torch.empty(4 * n, dtype=torch.int32, device=dev)
+    ln = torch.empty(n, dtype=torch.int32, device=dev)
+    cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
+    fn = lambda: api.sw_device(batch, SCORING, True, sc, pos, ln, cg, stream=stream.cuda_stream,
+                               trace_cell_limit=-1)
+    fn()
+    ms = timed(fn, stream, 1)
+    return {"workload": f"sw_long_4k (first {n} of 4,096 pairs): query 2-30 kb at 10%, 0-5 kb flanks, "
+                        "scoring {2,-3,3,1}, score+CIGAR, no trace-cell limit",
+            "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "cells": cells}
+
+
 def main():
     args = parse()
-    rank, world, local = dist_setup(args.gpus)
+    rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -205,9 +343,19 @@ def main():
 
     import __graft_entry__
     __graft_entry__.build()
-    from genoaligner_gb300 import api, workloads
+    from genoaligner_gb300 import api, cost_model, workloads
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+
+    if args.only:
+        stream = torch.cuda.current_stream(dev)
+        run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, False),
+               "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, False),
+               "wfa_long": lambda: bench_wfa_long(api, workloads, torch, dev, stream, args),
+               "sw_long_sample": lambda: bench_sw_long(api, workloads, torch, dev, stream, 256)}[args.only]
+        if rank == 0:
+            print(json.dumps({args.only: run()}), flush=True)
+        return
 
     ps = workloads.sw_uneven_200k(n=args.pairs)
     cells = sw_cells(ps)
@@ -222,7 +370,7 @@ def main():
     def step():
         api.sw_device(batch, SCORING, True, out_score, out_pos, out_len, out_cig, stream=stream.cuda_stream)
 
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
     clocks = Clocks(local)
@@ -245,23 +393,26 @@ def main():
     prof = api.profile_read()
     value = world * cells / (ms * 1e-3) / 1e9
 
-    # dominant kernel and its roofline
-    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 1))
-    top_name, (top_ms, top_n) = top
-    widths = {"sw8_trace": 8, "sw16_trace": 16, "sw32_trace": 32}
-    C = widths.get(top_name, 32)
-    sel = np.array([api_width(int(x)) == C for x in ps.b_len])
-    top_cells = int((ps.a_len.astype(np.int64)[sel] * ps.b_len.astype(np.int64)[sel]).sum())
-    achieved_gcups = top_cells / (top_ms / top_n * 1e-3) / 1e9 if top_ms > 0 else 0.0
-    peak_ops = api.int_peak(0)
-    peak_gcups = peak_ops / OPS_PER_CELL / 1e9
-    roofline = {"bound": "int32", "achieved": achieved_gcups, "peak": peak_gcups, "unit": "GCUPS",
-                "frac": achieved_gcups / peak_gcups if peak_gcups else None, "traffic": None,
-                "kernel": top_name, "ops_per_cell": OPS_PER_CELL,
-                "peak_source": f"measured int32 microbenchmark: {peak_ops / 1e12:.2f} T lane-ops/s (add+max)",
-                "kernel_ms_per_launch": top_ms / top_n, "kernel_share": top_ms / sum(v[0] for v in prof.values())}
+    # dominant kernel and its roofline: the trace kernels together process
+    # every cell of the batch once per step (one launch each per step)
+    total_ms = sum(v[0] for v in prof.values())
+    top_name, (top_ms, top_n) = max(prof.items(), key=lambda kv: kv[1][0])
+    sw_names = [k for k in prof if k.startswith("sw")]
+    sw_ms = sum(prof[k][0] for k in sw_names)
+    achieved = cells * args.steps / (sw_ms * 1e-3) / 1e9 if sw_ms > 0 else 0.0
+    dpx = api.int_peak(1)
+    peak = dpx / OPS_PER_CELL / 1e9
+    roofline = {"bound": "dpx", "achieved": achieved, "peak": peak, "unit": "GCUPS",
+                "frac": achieved / peak if peak else None,
+                "traffic": SW16CK_DRAM_BYTES_PER_CELL * cells if top_name == "sw16x2_trace" else None,
+                "kernel": top_name, "kernels_counted": sw_names, "ops_per_cell": OPS_PER_CELL,
+                "peak_source": f"measured by peak.cu on this GPU: __viaddmax_s32 at {dpx / 1e12:.2f} T "
+                               "lane-instructions/s, / 6 per cell (not in MEASURED_PEAKS.json, which holds "
+                               "HBM and bf16 peaks)",
+                "kernel_ms_per_launch": top_ms / max(1, top_n), "kernel_share": top_ms / total_ms if total_ms else None,
+                "traffic_source": "profiles/sw16ck_trace_sw_uneven.md (bytes/cell x cells per launch)"}
 
-    # correctness gate of the measured run: CIGAR strings of a sample vs the oracle
+    # correctness gate of the measured run: a sample vs the oracle
     import oracle
     idx = np.random.default_rng(7).choice(n, 64, replace=False)
     sc = out_score.cpu().numpy()
@@ -274,14 +425,14 @@ def main():
     reqs = api.make_sw_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING, True)
     res = np.zeros(n, api.SWRES_DT)
     cig = np.empty(int(api.load().ga_align_sw_cigar_bytes(reqs.ctypes.data, n)), np.uint8)
-    for _ in range(max(1, args.warmup - 1)):
-        api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING,
-                                  _reqs=reqs, _res=res, _cig=cig)
+    call = lambda: api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING,
+                                             _reqs=reqs, _res=res, _cig=cig)
+    for _ in range(2):
+        call()
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r = api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING,
-                                      _reqs=reqs, _res=res, _cig=cig)
+        r = call()
     e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
     e2e_ms = max_over_ranks(e2e_ms, world)
     h2d, d2h = api.last_transfer_bytes()
@@ -291,7 +442,10 @@ def main():
 
     extra = {}
     if not args.no_extra:
-        extra["wfa"] = bench_wfa(api, workloads, torch, dev, stream, args)
+        extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, rank == 0)
+        extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, rank == 0)
+        extra["wfa_long"] = bench_wfa_long(api, workloads, torch, dev, stream, args)
+        extra["sw_long_sample"] = bench_sw_long(api, workloads, torch, dev, stream, 256)
 
     cpu = None
     if rank == 0:
@@ -304,12 +458,11 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, seed 2)",
-            "config": {"workload": "sw_uneven_200k: 200,000 pairs, query log-uniform 50-1,000 bp, target = query "
-                                   "at 5% (sub/ins/del 60/20/20) between U{0..500} flanks, scoring {2,-3,3,1}, "
-                                   "score+end+start+CIGAR", "pairs": n, "cells": cells,
+            "vs_baseline": None, "dtype": "int16x2/int32", "data": "synthetic (seeded generator, seed 2)",
+            "config": {"workload": SW_WORKLOAD, "pairs": n, "cells": cells,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs (%.0f MB) and direction tables exceed the 129 MB L2" % (batch.input_bytes / 1e6)},
+                       "l2": "inputs (%.0f MB) and checkpoint/edge stores exceed the 129 MB L2" %
+                             (batch.input_bytes / 1e6)},
             "e2e": {"value": world * cells / (e2e_ms * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -321,56 +474,6 @@ def main():
             "extra": extra,
         }
         print(json.dumps(line), flush=True)
-
-
-def api_width(n):
-    if n <= 256:
-        return 8
-    if n <= 512:
-        return 16
-    return 32
-
-
-def bench_wfa(api, workloads, torch, dev, stream, args):
-    ps = workloads.wfa_150bp_2pct()
-    n = ps.n
-    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
-    sc = torch.empty(n, dtype=torch.int32, device=dev)
-    ln = torch.empty(n, dtype=torch.int32, device=dev)
-    cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(3):
-        api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream)
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(max(args.steps, 5)):
-        flush.zero_()                                   # evict the batch from L2
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream)
-        b.record(stream)
-        torch.cuda.synchronize()
-        times.append(a.elapsed_time(b))
-    dev_ms = statistics.median(times)
-    reqs = api.make_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, 64, True)
-    res = np.zeros(n, api.RES_DT)
-    cig = np.empty(int(api.load().ga_align_cigar_bytes(reqs.ctypes.data, n)), np.uint8)
-    for _ in range(3):
-        api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, _reqs=reqs, _res=res,
-                               _cig=cig)
-    t = []
-    for _ in range(max(args.steps, 5)):
-        t0 = time.perf_counter()
-        api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, _reqs=reqs, _res=res,
-                               _cig=cig)
-        t.append(time.perf_counter() - t0)
-    e2e_ms = statistics.median(t) * 1e3
-    cpu_pps, done = cpu_baseline_wfa(ps, 4.0, os.cpu_count() or 1)
-    return {"workload": "wfa_150bp_2pct: 10,000 pairs, 150 bp, 2% (sub/ins/del equal), smax 64, CIGAR",
-            "pairs_per_s": n / (dev_ms * 1e-3), "ms_per_step": dev_ms,
-            "e2e_pairs_per_s": n / (e2e_ms * 1e-3), "e2e_ms_per_step": e2e_ms,
-            "cpu_baseline_pairs_per_s": cpu_pps, "cpu_cores": os.cpu_count(), "cpu_kind": "port",
-            "l2": "256 MB buffer written between steps"}
 
 
 if __name__ == "__main__":

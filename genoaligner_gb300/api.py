@@ -625,7 +625,8 @@ def mlp_train_step(feat, target, lr: float) -> float:
 
 
 def wfa_route_stats(rounds: int = 12):
-    """(small queue, big queue, [escalated after round r ...]) of the last learned call."""
+    """(lane-queue pairs, warp-queue pairs, [pairs escalated from the lane queue
+    to the warp queue, 0, ...]) of the calling thread's last learned call."""
     out = np.zeros(2 + rounds, np.int32)
     st = load().ga_wfa_route_stats(out.ctypes.data, int(out.shape[0]))
     if st != GA_OK:
