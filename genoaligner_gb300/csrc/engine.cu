@@ -634,9 +634,9 @@ static void order_by_size(std::vector<int32_t>& v, const int32_t* tl, const int3
     v.swap(out);
 }
 
-// The two-pairs-per-warp kernel at 8 columns per lane: the checkpointed
-// form (sw16ck.cu) unless GA_SW16CK=0 selects the one that stores every
-// cell's direction bits (sw16.cu, also the form at 16 and 32 columns).
+// Traceback kernels: the checkpointed forms (sw16ck.cu for two 16-bit pairs
+// per warp, sw32ck.cu for one 32-bit pair per warp) unless GA_SW16CK=0
+// selects the forms that store every cell's direction bits (sw16.cu, sw.cu).
 static bool use_sw16ck()
 {
     static const bool on = [] {
@@ -654,17 +654,22 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
         const char* e = getenv("GA_SW16");
         return !(e && e[0] == '0');
     }();
+    const bool ck = use_sw16ck();
     for (int32_t i = 0; i < n; ++i) {
         if (skip && skip[i]) continue;
-        const int k = width_index(sw_width_for(pl[i]));
+        // the checkpointed traceback kernels choose their own lane widths: list 0
+        // (list 1: 32-bit pairs for the long-pair shape)
+        const int k = (ck && trace) ? 0 : width_index(sw_width_for(pl[i]));
         const bool use16 = use16_ok && trace && pure && pure[i] && pure[n + i] &&
                            sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
-        (use16 ? e16[k] : P.w32[k]).push_back(i);
+        if (use16) e16[k].push_back(i);
+        else P.w32[(ck && trace && sw32ck_long(tl[i], pl[i])) ? 1 : k].push_back(i);
     }
     for (int k = 0; k < 3; ++k) {
         order_by_size(P.w32[k], tl, pl);
         for (int32_t i : P.w32[k]) {
-            if (trace) P.dir32[k] = std::max(P.dir32[k], sw_dir_words(tl[i], pl[i], kWidths[k]));
+            if (trace) P.dir32[k] = std::max(P.dir32[k], (ck && k < 2) ? sw32ck_dir_words(tl[i], pl[i])
+                                                                       : sw_dir_words(tl[i], pl[i], kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
         }
         P.dir32[k] = (P.dir32[k] + 3) / 4 * 4;
@@ -692,10 +697,11 @@ struct SwSlots {
 static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
 {
     SwSlots S;
-    const int64_t budget = (int64_t)48 << 30;          // direction-table cap, bytes
+    const int64_t budget = (int64_t)96 << 30;          // direction-table / checkpoint cap, bytes
     for (int k = 0; k < 3; ++k) {
         if (!P.w32[k].empty()) {
-            int s = sw_max_slots(kWidths[k], trace, sm_count);
+            int s = (trace && use_sw16ck() && k < 2) ? sw32ck_max_slots(k == 1, sm_count)
+                                                     : sw_max_slots(kWidths[k], trace, sm_count);
             s = (int)std::min<int64_t>(s, ((int64_t)P.w32[k].size() + 3) / 4 * 4);
             if (trace && P.dir32[k] > 0) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir32[k] * 4) / 4 * 4));
             S.s32[k] = s;
@@ -744,7 +750,8 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir32[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + 3 + k; A.err = err;
-            const cudaError_t e = launch_sw(A, kWidths[k], trace, S.s32[k], st);
+            const cudaError_t e = (trace && use_sw16ck() && k < 2) ? launch_sw32ck(A, k == 1, S.s32[k], st)
+                                                                   : launch_sw(A, kWidths[k], trace, S.s32[k], st);
             if (e != cudaSuccess) return e;
         }
         base += (int64_t)P.w32[k].size();

@@ -105,8 +105,13 @@ int sw_max_slots(int C, bool trace, int sm_count);
 cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
 
 bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge);
-// Checkpointed variant (sw16ck.cu), 8 columns per lane only: same arguments,
-// dir_slot = sw16ck_dir_words.
+// Checkpointed traceback kernels (sw16ck.cu: two 16-bit pairs per warp;
+// sw32ck.cu: one 32-bit pair per warp); dir_slot = their *_dir_words.
+// sw32ck has a short-pair shape and a long-pair shape (sw32ck_long).
+bool sw32ck_long(int m, int n);
+int64_t sw32ck_dir_words(int m, int n);
+int sw32ck_max_slots(bool long_pairs, int sm_count);
+cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st);
 int64_t sw16ck_dir_words(int M, int N);
 int sw16ck_max_slots(int sm_count);
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st);

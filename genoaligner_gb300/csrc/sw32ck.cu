@@ -1,0 +1,469 @@
+// sw32ck.cu -- Smith-Waterman with traceback in 32-bit lanes, one pair per
+// warp: a score-only forward pass that keeps checkpoints, then the walk over
+// 64 x 64 tiles recomputed with direction bits.
+//
+// The 32-bit form of sw16ck.cu, for pairs the 16-bit kernels cannot take
+// (bytes other than A/C/G/T, or scores that could pass 16 bits: long pairs).
+// Same recurrence, tie rules and walk as sw.cu (the reference's trace
+// recurrence, include/genoaligner/backend/sw_kernel_impl.hip:286-329, walk
+// :198-242, best cell = first strict maximum in row-major order):
+//
+//   1. forward: lanes of CB columns (16 in full bands; the last band takes the
+//      smallest of 4, 8, 16 that reaches the last column), H/E/F with DPX
+//      (__viaddmax_s32, __vimax3_s32_relu), no predicates; every CK_K-th row
+//      each column's (H - gap_open, F) goes to a checkpoint row, every TW-th
+//      column each row's (H - gap_open, E) to a column edge; per lane the best
+//      value with its first row and column;
+//   2. the best cell is the warp's (max value, min row, min column);
+//   3. the walk recomputes the K x TW tile holding its current cell from the
+//      checkpoint row above and the column edge left of it, with the nibble
+//      of predicates sw.cu stores (E chosen, F chosen, E extended, F
+//      extended, from __vibmax_s32), and walks inside it.
+//
+// Two shapes: K = TW = 64 (2 columns per lane in a tile) for pairs up to a
+// few million cells, and K = TW = 512 (16 columns per lane) for long pairs,
+// whose checkpoints would otherwise take hundreds of MB per warp: the
+// checkpoint memory per cell is 16 B / K + 16 B / TW.
+//
+// Substitution scores: a shared-memory profile for pure-ACGT pairs, byte
+// equality otherwise (the reference compares bytes).
+#include "kernels.cuh"
+
+namespace ga {
+
+constexpr int C32_C = 16;                // forward columns per lane, full bands
+constexpr int C32_BW = 32 * C32_C;
+constexpr int C32_PAD = -(1 << 28);      // score past a pattern's end: below any reachable value
+
+__host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
+__host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }
+__host__ __device__ inline int c32_ncol(int n)
+{
+    const int full = n > 0 ? (n - 1) / C32_BW : 0;
+    return full * C32_BW + 32 * c32_last_cb(n - full * C32_BW);
+}
+
+__device__ __forceinline__ int c32_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
+
+__device__ __forceinline__ bool c32_better(int v, int r, int c, int bv, int br, int bc)
+{
+    return v > bv || (v == bv && (r < br || (r == br && c < bc)));
+}
+
+struct Fwd32 {
+    const uint8_t *text, *pat;
+    int m, n, ncol;          // ncol: columns the forward bands cover
+    int stride;              // checkpoint row stride: ncol rounded up to TW
+    int K, TW;               // checkpoint interval (rows), column-edge interval (columns); powers of 2
+    int32_t* ck;             // checkpoint rows [q][col][2]
+    int32_t* ce;             // column edges [k][row][2]
+    int4* prof;              // per warp: 4 letters x CB/4 quads x 32 lanes
+    int sm, sx, go, ge;
+};
+
+template <int CB, bool PROF>
+__device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int& cb)
+{
+    constexpr int NQ = CB / 4;
+    const int go = X.go, ge = X.ge, m = X.m;
+    const int j0 = b0 + t * CB;
+    const int nv = max(0, min(CB, X.n - j0));
+    uint32_t pb[PROF ? 1 : CB];
+    if constexpr (PROF) {
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            int code[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) code[k] = (4 * q + k < nv) ? c32_code(__ldg(X.pat + j0 + 4 * q + k)) : 4;
+#pragma unroll
+            for (int L = 0; L < 4; ++L) {
+                int v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = code[k] == 4 ? C32_PAD : (code[k] == L ? X.sm : X.sx);
+                X.prof[(L * NQ + q) * 32 + t] = make_int4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        __syncwarp();
+    } else {
+#pragma unroll
+        for (int c = 0; c < CB; ++c) pb[c] = (c < nv) ? __ldg(X.pat + j0 + c) : 0x100u;
+    }
+    int hgu[CB], fv[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) { hgu[c] = -go; fv[c] = 0; }
+    int diag_in = -go, out_hg = -go, out_e = 0;
+    const int32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / X.TW - 1) * m : nullptr;
+    int nxt_hg = -go, nxt_e = 0;
+    if (t == 0 && left) { nxt_hg = left[0]; nxt_e = left[1]; }
+    const int kout = (j0 + CB) % X.TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / X.TW : 0;
+    int32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * m : nullptr;
+    uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.text) : 0u;
+    int bv = 0, br = 0, bc = 0;                       // this band's best: value, first row, first column
+    const int steps = m + 31;
+    for (int tau = 0; tau < steps; ++tau) {
+        int in_hg = __shfl_up_sync(FULL, out_hg, 1);
+        int in_e = __shfl_up_sync(FULL, out_e, 1);
+        ch = __shfl_up_sync(FULL, ch, 1);
+        const int i = tau - t + 1;
+        if (t == 0) {
+            ch = ch_next;
+            if (i < m) ch_next = __ldg(X.text + i);
+            in_hg = nxt_hg;
+            in_e = nxt_e;
+            if (left && i < m) { nxt_hg = left[2 * i]; nxt_e = left[2 * i + 1]; }
+        }
+        if (i < 1 || i > m) continue;
+        int s[CB];
+        if constexpr (PROF) {
+            const int L = c32_code(ch);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const int4 v = X.prof[(L * NQ + q) * 32 + t];
+                s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < CB; ++c) s[c] = c < nv ? (ch == pb[c] ? X.sm : X.sx) : C32_PAD;
+        }
+        int hgd = diag_in, hgl = in_hg, el = in_e;
+        int rowmax = 0;
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int e = __viaddmax_s32(el, -ge, hgl);           // max(E_left - ge, H_left - go)
+            const int f = __viaddmax_s32(fv[c], -ge, hgu[c]);     // max(F_up - ge, H_up - go)
+            const int h = __vimax3_s32_relu(hgd + s[c], e, f);    // max(H_diag + s, E, F, 0)
+            const int hg = h - go;
+            rowmax = max(rowmax, h);
+            hgd = hgu[c];
+            hgu[c] = hg;
+            fv[c] = f;
+            hgl = hg;
+            el = e;
+        }
+        diag_in = in_hg;
+        out_hg = hgl;
+        out_e = el;
+        if (eout) { eout[2 * (i - 1)] = out_hg; eout[2 * (i - 1) + 1] = out_e; }
+        if ((i & (X.K - 1)) == 0 && i < m) {
+            int4* dst = reinterpret_cast<int4*>(X.ck + 2 * ((int64_t)(i / X.K - 1) * X.stride + j0));
+#pragma unroll
+            for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_int4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
+        }
+        if (rowmax > bv) {                                   // first column of this row holding it
+            int first = 0;
+#pragma unroll
+            for (int c = CB - 1; c >= 0; --c)
+                if (hgu[c] + go == rowmax) first = c;
+            bv = rowmax;
+            br = i;
+            bc = j0 + first + 1;
+        }
+    }
+    if (bv > 0 && c32_better(bv, br, bc, vb, rb, cb)) { vb = bv; rb = br; cb = bc; }
+    __syncwarp();
+}
+
+template <bool PROF>
+__device__ void fwd32(const Fwd32& X, int t, int& vb, int& rb, int& cb)
+{
+    for (int b0 = 0; b0 < X.n;) {
+        const int rest = X.n - b0;
+        const int w = rest > C32_BW ? C32_C : c32_last_cb(rest);
+        if (w == 16) fwd32_band<16, PROF>(X, b0, t, vb, rb, cb);
+        else if (w == 8) fwd32_band<8, PROF>(X, b0, t, vb, rb, cb);
+        else fwd32_band<4, PROF>(X, b0, t, vb, rb, cb);
+        b0 += 32 * w;
+    }
+}
+
+// Shared memory per warp: the forward profile (4 letters x 4 quads x 32
+// lanes of int4), reused by a tile's profile (4 letters x CT/4 quads x 32
+// lanes, or int2 pairs for CT = 2) followed by its K left-edge rows.
+__host__ __device__ constexpr int c32_warp_smem_bytes(int K, int CT)
+{
+    return (4 * (C32_C / 4) * 32 * 16) > (4 * CT * 32 * 4 + K * 8) ? (4 * (C32_C / 4) * 32 * 16)
+                                                                      : (4 * CT * 32 * 4 + K * 8);
+}
+
+template <int K, int CT>
+__global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
+{
+    constexpr int TW = 32 * CT;
+    constexpr int NWT = CT >= 8 ? CT / 8 : 1;            // nibble words per lane and step
+    constexpr int WSB = c32_warp_smem_bytes(K, CT);
+    extern __shared__ int4 c32_smem[];
+    const int t = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    uint32_t* wslot = A.dirs + slot * A.dir_slot;
+    unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
+    int4* prof = reinterpret_cast<int4*>(wsm);
+    const int go = A.gap_open, ge = A.gap_extend;
+    const int sm = A.match + go, sx = A.mismatch + go;
+
+    for (;;) {
+        int w = 0;
+        if (t == 0) w = atomicAdd(A.counter, 1);
+        w = __shfl_sync(FULL, w, 0);
+        if (w >= A.nwork) break;
+        __syncwarp();
+        const int p = A.work[w];
+        const int m = A.D.a_len[p], n = A.D.b_len[p];
+        const uint8_t* text = A.D.seq + A.D.a_off[p];
+        const uint8_t* pat = A.D.seq + A.D.b_off[p];
+        if (m <= 0 || n <= 0) {
+            if (t == 0) {
+                A.out_score[p] = 0;
+                A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+                A.out_len[p] = 0;
+            }
+            continue;
+        }
+        const bool pure = A.D.pure && A.D.pure[p] && A.D.pure[A.D.n + p];
+        // tiles reach up to a multiple of TW: checkpoint rows are that wide (the
+        // columns past the forward bands are padding, never read into a real cell)
+        const int ncol = c32_ncol(n);
+        const int stride = (ncol + TW - 1) / TW * TW;
+        const int nq = c32_rows(m, K);
+        int32_t* ck = reinterpret_cast<int32_t*>(wslot);
+        int32_t* ce = ck + 2 * (int64_t)nq * stride;
+        uint32_t* tile = reinterpret_cast<uint32_t*>(ce + 2 * (int64_t)(stride / TW) * m);
+
+        // ------------------------------------------------ forward pass --
+        int vb = 0, rb = 0, cb = 0;
+        {
+            Fwd32 X{text, pat, m, n, ncol, stride, K, TW, ck, ce, prof, sm, sx, go, ge};
+            if (pure) fwd32<true>(X, t, vb, rb, cb);
+            else fwd32<false>(X, t, vb, rb, cb);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const int ov = __shfl_xor_sync(FULL, vb, o), orr = __shfl_xor_sync(FULL, rb, o), oc = __shfl_xor_sync(FULL, cb, o);
+            if (ov > 0 && c32_better(ov, orr, oc, vb, rb, cb)) { vb = ov; rb = orr; cb = oc; }
+        }
+        if (vb <= 0) {
+            if (t == 0) {
+                A.out_score[p] = 0;
+                A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+                A.out_len[p] = 0;
+            }
+            continue;
+        }
+
+        // ----------------------------------------------------- the walk --
+        char* slotc = A.out_cigar + A.D.out_off[p];
+        int pos = m + n;
+        int i = rb, j = cb, state = 0, v = vb;
+        int ti0 = ((i - 1) / K) * K + 1, tb = (j - 1) / TW;
+        int* edg = reinterpret_cast<int*>(wsm + 4 * CT * 32 * 4);     // [row][2], after the tile profile
+        bool fin = false;
+        while (!fin) {
+            const int rows = i - ti0 + 1;
+            const int steps = rows + 31;
+            const int col0 = TW * tb;
+            __syncwarp();
+            // tile profile (pure pairs) or bytes, top state, left edges
+            uint32_t pbt[CT];
+            {
+                const int cl = col0 + CT * t;
+                if (pure) {
+                    int code[CT];
+#pragma unroll
+                    for (int c = 0; c < CT; ++c) code[c] = cl + c < n ? c32_code(__ldg(pat + cl + c)) : 4;
+                    if constexpr (CT == 2) {
+                        int2* tp = reinterpret_cast<int2*>(wsm);
+#pragma unroll
+                        for (int L = 0; L < 4; ++L) tp[L * 32 + t] = make_int2(code[0] == L ? sm : sx, code[1] == L ? sm : sx);
+                    } else {
+                        int4* tp = reinterpret_cast<int4*>(wsm);
+#pragma unroll
+                        for (int L = 0; L < 4; ++L)
+#pragma unroll
+                            for (int q4 = 0; q4 < CT / 4; ++q4)
+                                tp[(L * (CT / 4) + q4) * 32 + t] =
+                                    make_int4(code[4 * q4] == L ? sm : sx, code[4 * q4 + 1] == L ? sm : sx,
+                                              code[4 * q4 + 2] == L ? sm : sx, code[4 * q4 + 3] == L ? sm : sx);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < CT; ++c) pbt[c] = (!pure && cl + c < n) ? __ldg(pat + cl + c) : 0x100u;
+            }
+            const int q = (ti0 - 1) / K - 1;
+            const int32_t* crow = ck + 2 * (int64_t)max(q, 0) * stride;
+            int hgu[CT], fv[CT];
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                hgu[c] = q >= 0 ? crow[2 * (col0 + CT * t + c)] : -go;
+                fv[c] = q >= 0 ? crow[2 * (col0 + CT * t + c) + 1] : 0;
+            }
+            int diag_in = __shfl_up_sync(FULL, hgu[CT - 1], 1);
+            if (t == 0) diag_in = (q >= 0 && tb > 0) ? crow[2 * (col0 - 1)] : -go;
+            {
+                const int32_t* le = tb > 0 ? ce + 2 * ((int64_t)(tb - 1) * m + (ti0 - 1)) : nullptr;
+                for (int r = t; r < K; r += 32) {
+                    edg[2 * r] = (le && r < rows) ? le[2 * r] : -go;
+                    edg[2 * r + 1] = (le && r < rows) ? le[2 * r + 1] : 0;
+                }
+            }
+            __syncwarp();
+            int out_hg = -go, out_e = 0;
+            const uint8_t* tx = text + (ti0 - 1);
+            uint32_t ch = 0, ch_next = t == 0 ? (uint32_t)__ldg(tx) : 0u;
+            for (int tau = 0; tau < steps; ++tau) {
+                int in_hg = __shfl_up_sync(FULL, out_hg, 1);
+                int in_e = __shfl_up_sync(FULL, out_e, 1);
+                ch = __shfl_up_sync(FULL, ch, 1);
+                const int r = tau - t + 1;                                  // tile row, 1-based
+                if (t == 0) {
+                    ch = ch_next;
+                    if (r < rows) ch_next = __ldg(tx + r);
+                    if (r <= rows) { in_hg = edg[2 * (r - 1)]; in_e = edg[2 * (r - 1) + 1]; }
+                }
+                if (r < 1 || r > rows) continue;
+                int s[CT];
+                if (pure) {
+                    const int L = c32_code(ch);
+                    if constexpr (CT == 2) {
+                        const int2 v2 = reinterpret_cast<const int2*>(wsm)[L * 32 + t];
+                        s[0] = v2.x;
+                        s[1] = v2.y;
+                    } else {
+#pragma unroll
+                        for (int q4 = 0; q4 < CT / 4; ++q4) {
+                            const int4 v4 = reinterpret_cast<const int4*>(wsm)[(L * (CT / 4) + q4) * 32 + t];
+                            s[4 * q4] = v4.x; s[4 * q4 + 1] = v4.y; s[4 * q4 + 2] = v4.z; s[4 * q4 + 3] = v4.w;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CT; ++c) s[c] = ch == pbt[c] ? sm : sx;
+                }
+                int hgd = diag_in, hgl = in_hg, el = in_e;
+                uint32_t nib[NWT];
+#pragma unroll
+                for (int wq = 0; wq < NWT; ++wq) nib[wq] = 0;
+#pragma unroll
+                for (int c = 0; c < CT; ++c) {
+                    bool pe, pf, p1, p2;
+                    const int h0 = hgd + s[c];
+                    const int e = __vibmax_s32(hgl, el - ge, &pe);            // open wins ties
+                    const int f = __vibmax_s32(hgu[c], fv[c] - ge, &pf);
+                    const int h1 = __vibmax_s32(h0, e, &p1);                  // diagonal wins ties
+                    const int h2 = __vibmax_s32(h1, f, &p2);
+                    const int h = max(h2, 0);
+                    nib[c >> 3] |= ((uint32_t)!p1 | ((uint32_t)!p2 << 1) | ((uint32_t)!pe << 2) | ((uint32_t)!pf << 3))
+                                   << (4 * (c & 7));
+                    const int hg = h - go;
+                    hgd = hgu[c];
+                    hgu[c] = hg;
+                    fv[c] = f;
+                    hgl = hg;
+                    el = e;
+                }
+#pragma unroll
+                for (int wq = 0; wq < NWT; ++wq) tile[(tau * 32 + t) * NWT + wq] = nib[wq];
+                diag_in = in_hg;
+                out_hg = hgl;
+                out_e = el;
+            }
+            __syncwarp();
+            // walk inside the tile: state 0 on H, 1 in an E run ('D'), 2 in an F run ('I')
+            const int jlo = col0 + 1;
+            for (;;) {
+                if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
+                if (i < ti0 || j < jlo) break;
+                const int jj = j - jlo;
+                const int tt = jj / CT, c = jj - tt * CT;
+                const uint32_t nb4 = (tile[(((i - ti0) + tt) * 32 + tt) * NWT + (c >> 3)] >> (4 * (c & 7))) & 15u;
+                char op;
+                if (state == 0) {
+                    if (nb4 & 2u) {
+                        op = 'I';
+                        if (nb4 & 8u) { state = 2; v += ge; } else { v += go; }
+                        --i;
+                    } else if (nb4 & 1u) {
+                        op = 'D';
+                        if (nb4 & 4u) { state = 1; v += ge; } else { v += go; }
+                        --j;
+                    } else {
+                        const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
+                        op = ta == pc ? 'M' : 'X';
+                        v -= ta == pc ? A.match : A.mismatch;
+                        --i;
+                        --j;
+                    }
+                } else if (state == 1) {
+                    op = 'D';
+                    if (nb4 & 4u) { v += ge; } else { v += go; state = 0; }
+                    --j;
+                } else {
+                    op = 'I';
+                    if (nb4 & 8u) { v += ge; } else { v += go; state = 0; }
+                    --i;
+                }
+                if (pos <= 0) {
+                    if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
+                    fin = true;
+                    break;
+                }
+                --pos;
+                if (t == 0) slotc[pos] = op;
+            }
+            if (!fin) {
+                if (i < ti0) ti0 = ((i - 1) / K) * K + 1;
+                tb = (j - 1) / TW;
+            }
+        }
+        if (t == 0) {
+            A.out_score[p] = vb;
+            A.out_pos[4 * p] = i;
+            A.out_pos[4 * p + 1] = j;
+            A.out_pos[4 * p + 2] = rb - 1;
+            A.out_pos[4 * p + 3] = cb - 1;
+            A.out_len[p] = m + n - pos;
+        }
+    }
+}
+
+// The long-pair shape serves pairs above this many cells.
+constexpr int64_t C32_LONG_CELLS = (int64_t)1 << 24;
+
+bool sw32ck_long(int m, int n) { return (int64_t)m * n > C32_LONG_CELLS; }
+
+// Words of one warp slot for a pair of m rows and n columns: checkpoint rows,
+// column edges, the tile table.
+int64_t sw32ck_dir_words(int m, int n)
+{
+    const bool lg = sw32ck_long(m, n);
+    const int K = lg ? 512 : 64, CT = lg ? 16 : 2, TW = 32 * CT, NWT = CT >= 8 ? CT / 8 : 1;
+    const int64_t stride = ((int64_t)c32_ncol(n) + TW - 1) / TW * TW;
+    return 2 * (int64_t)c32_rows(m, K) * stride + 2 * (stride / TW) * (int64_t)m + (int64_t)(K + 31) * 32 * NWT;
+}
+
+template <int K, int CT>
+static size_t c32_smem() { return (size_t)4 * c32_warp_smem_bytes(K, CT); }
+
+int sw32ck_max_slots(bool long_pairs, int sm_count)
+{
+    int per_sm = 0;
+    if (long_pairs) {
+        cudaFuncSetAttribute(sw32ck_kernel<512, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c32_smem<512, 16>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<512, 16>, 128, c32_smem<512, 16>());
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<64, 2>, 128, c32_smem<64, 2>());
+    }
+    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+}
+
+cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st)
+{
+    if (A.nwork <= 0) return cudaSuccess;
+    launch_begin(K_SW32_TRACE, st);
+    if (long_pairs) sw32ck_kernel<512, 16><<<(slots + 3) / 4, 128, c32_smem<512, 16>(), st>>>(A);
+    else sw32ck_kernel<64, 2><<<(slots + 3) / 4, 128, c32_smem<64, 2>(), st>>>(A);
+    launch_end(K_SW32_TRACE, st);
+    return cudaGetLastError();
+}
+
+}  // namespace ga

@@ -260,7 +260,7 @@ def sw_batch(texts, patterns, scoring=(2, -3, 5, 2), with_cigar=True, threads=No
                                "pattern_len exceeds this device's shared-memory limit "
                                "for the score kernel (see api.hpp supported-size limits)")
     max_cells = int(((tlen.astype(np.int64) + 1) * (plen.astype(np.int64) + 1)).max())
-    dir_limit = min(max_cells, int(trace_cell_limit))
+    dir_limit = max_cells if trace_cell_limit is None or trace_cell_limit < 0 else min(max_cells, int(trace_cell_limit))
     cap = max_m + max_n + 4
     per = tlen.astype(np.int64) + plen + 4
     cig_off = np.zeros(n, np.int64)

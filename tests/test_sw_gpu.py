@@ -96,6 +96,28 @@ def test_sw_too_large_and_ext_limit():
     assert got.res["rescore_ok"][0] and got.res["wellformed_ok"][0]
 
 
+def _long_pair(rng, qlen, flank, rate, with_n):
+    q = workloads.random_bases(rng, qlen)
+    core, _ = workloads.mutate_point(rng, q, np.array([qlen]), rate, (0.5, 0.25, 0.25))
+    t = np.concatenate([workloads.random_bases(rng, flank), core, workloads.random_bases(rng, flank)])
+    if with_n:                                    # a few bytes outside A/C/G/T: the byte-compare path
+        t[rng.integers(0, t.shape[0], size=5)] = ord("N")
+    return t.tobytes(), q.tobytes()
+
+
+@pytest.mark.parametrize("scheme,with_n", [((2, -3, 3, 1), True), ((12, -3, 5, 2), False)])
+def test_sw_long_pairs_vs_oracle(scheme, with_n):
+    """Pairs above 2^24 cells take the 32-bit checkpointed kernel's long shape
+    (512-row blocks, 512-column tiles); one below it the short shape."""
+    rng = np.random.default_rng(91 if with_n else 92)
+    pairs = [_long_pair(rng, 4200, 1000, 0.10, with_n), _long_pair(rng, 3000, 700, 0.10, with_n),
+             _long_pair(rng, 1500, 300, 0.10, with_n)]
+    ts, pp = [x[0] for x in pairs], [x[1] for x in pairs]
+    want = oracle.sw_batch(ts, pp, scoring=scheme, with_cigar=True, trace_cell_limit=-1)
+    got = sw_gpu(ts, pp, scoring=scheme, trace_cell_limit=-1)
+    assert_sw_equal(got, want, f"long {scheme}")
+
+
 def test_sw_mixed_with_cigar_batch():
     ps = workloads.sw_uneven_200k(n=300, seed=8)
     ts, pp = ps.lists()
