@@ -6,6 +6,8 @@
 //   variant 0: a = max(a + x, y) written as plain C    (2 ops per step)
 //   variant 1: a = __viaddmax_s32(a, x, y)              (1 op per step)
 //   variant 2: a = __vimax3_s32_relu(a, x, y)           (1 op per step)
+//   3-10 and 11-13: other integer/DPX forms, one C-level operation each
+//   (11: __vimax3_s16x2_relu, 12: __vimax3_s16x2, 13: __vmaxs2)
 #include "common.cuh"
 #include "../../include/genoaligner_gb300.h"
 
@@ -37,6 +39,9 @@ __global__ void __launch_bounds__(256) int_peak_kernel(int iters, int x, int* ou
                     bool p;
                     a[k] = __vibmax_s32(a[k], y + k, &p) + (p ? 1 : 0);
                 } else if constexpr (V == 9) a[k] = (int)__vcmpgtu2((unsigned)a[k], (unsigned)(y + k)) ^ x;
+                else if constexpr (V == 11) a[k] = (int)__vimax3_s16x2_relu((unsigned)a[k], (unsigned)(y + k), (unsigned)x);
+                else if constexpr (V == 12) a[k] = (int)__vimax3_s16x2((unsigned)a[k], (unsigned)(y + k), (unsigned)x);
+                else if constexpr (V == 13) a[k] = (int)__vmaxs2((unsigned)a[k], (unsigned)(y + k));
                 else a[k] = (a[k] & (y + k)) | (x ^ k);                              // logic
             }
         }
@@ -79,6 +84,9 @@ extern "C" int32_t ga_bench_int_peak(int32_t variant, double* lane_ops_per_s)
             case 7: int_peak_kernel<7><<<blocks, threads, 0, st>>>(iters, 3, out); break;
             case 8: int_peak_kernel<8><<<blocks, threads, 0, st>>>(iters, 3, out); break;
             case 9: int_peak_kernel<9><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 11: int_peak_kernel<11><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 12: int_peak_kernel<12><<<blocks, threads, 0, st>>>(iters, 3, out); break;
+            case 13: int_peak_kernel<13><<<blocks, threads, 0, st>>>(iters, 3, out); break;
             default: int_peak_kernel<10><<<blocks, threads, 0, st>>>(iters, 3, out); break;
         }
         launch_end(K_PEAK, st);

@@ -111,7 +111,7 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
 {
     constexpr int NH = CB / 2;
     const uint32_t MIN2 = 0x80008000u, K2 = 0x80008000u;
-    const uint32_t NGO2 = X.NGO2, NGE2 = X.NGE2, GO2 = X.GO2;
+    const uint32_t NGO2 = X.NGO2, NGE2 = X.NGE2;
     const int M = X.M, mA = X.mA, mB = X.mB;
     const int j0 = b0 + t * CB;
     const int nvA = max(0, min(CB, X.nA - j0)), nvB = max(0, min(CB, X.nB - j0));
@@ -129,7 +129,7 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     uint32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * M : nullptr;
     // text characters travel along the lanes with the boundary values; lane 0 reads them
     uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.textA) | ((uint32_t)__ldg(X.textB) << 8) : 0u;
-    uint32_t bmax = 0u, brow = 0u, bcol = 0u;             // this band: per half
+    uint32_t bmax = 0u, brow = 0u;                        // this band: best and its first row, per half
     const int steps = M + 31;
     for (int tau = 0; tau < steps; ++tau) {
         uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
@@ -142,7 +142,11 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
                 ch_next = (uint32_t)(i < mA ? __ldg(X.textA + i) : 'A') | ((uint32_t)(i < mB ? __ldg(X.textB + i) : 'A') << 8);
             in_hg = nxt_hg;
             in_e = nxt_e;
-            if (left && i < M) { nxt_hg = left[2 * i]; nxt_e = left[2 * i + 1]; }
+            if (left && i < M) {
+                const uint2 lv = *reinterpret_cast<const uint2*>(left + 2 * i);
+                nxt_hg = lv.x;
+                nxt_e = lv.y;
+            }
         }
         if (i < 1 || i > M) continue;
         const uint32_t* pA = X.prof + ((0 * 4 + ck_code(ch & 0xffu)) * NH) * 32 + t;
@@ -175,7 +179,7 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         diag_in = in_hg;
         out_hg = hgl;
         out_e = el;
-        if (eout) { eout[2 * (i - 1)] = out_hg; eout[2 * (i - 1) + 1] = out_e; }
+        if (eout) *reinterpret_cast<uint2*>(eout + 2 * (i - 1)) = make_uint2(out_hg, out_e);
         if ((i & (CK_K - 1)) == 0 && i < M) {                     // checkpoint row i
             uint4* dst = reinterpret_cast<uint4*>(X.ck + 2 * ((int64_t)(i / CK_K - 1) * X.ncol + j0));
 #pragma unroll
@@ -183,30 +187,20 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         }
         // rows past a pair's text do not count
         rowmax &= (i <= mA ? 0x0000ffffu : 0u) | (i <= mB ? 0xffff0000u : 0u);
-        // strict improvement per half: bit 15 / 31 of d clear
+        // strict improvement per half (bits 15 / 31 of d clear): this band's
+        // best and the first row holding it; the column is found when the walk
+        // recomputes that row
         const uint32_t d = bmax - rowmax + K2;
         const uint32_t imp = ((~d & K2) >> 15) * 0xffffu;
-        if (imp) {
-            // first column of this row holding the new maximum, per half
-            uint32_t acc = 0;
-#pragma unroll
-            for (int c = 0; c < CB; ++c) {
-                const uint32_t h = __viaddmax_s16x2(hgu[c], GO2, MIN2);
-                acc = (acc >> 1) | ((h - rowmax + K2) & K2);
-            }
-            constexpr uint32_t CM = (1u << CB) - 1u;
-            const int fa = __ffs((int)((acc >> (16 - CB)) & CM)) - 1, fb = __ffs((int)((acc >> (32 - CB)) & CM)) - 1;
-            const uint32_t colp = ((uint32_t)(j0 + fa + 1) & 0xffffu) | ((uint32_t)(j0 + fb + 1) << 16);
-            bmax = __vmaxs2(bmax, rowmax);
-            brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
-            bcol = (bcol & ~imp) | (colp & imp);
-        }
+        bmax = __vmaxs2(bmax, rowmax);
+        brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
     }
-    // merge the band into the lane's best
-    const int v = lo16s(bmax), r = (int)(brow & 0xffffu), c = (int)(bcol & 0xffffu);
-    if (v > 0 && ck_better(v, r, c, vA, rA, cA)) { vA = v; rA = r; cA = c; }
-    const int v2 = hi16s(bmax), r2 = (int)(brow >> 16), c2 = (int)(bcol >> 16);
-    if (v2 > 0 && ck_better(v2, r2, c2, vB, rB, cB)) { vB = v2; rB = r2; cB = c2; }
+    // merge the band into the lane's best; the column kept is the first of the
+    // lane's span in this band (spans order like their columns)
+    const int v = lo16s(bmax), r = (int)(brow & 0xffffu);
+    if (v > 0 && ck_better(v, r, j0 + 1, vA, rA, cA)) { vA = v; rA = r; cA = j0 + 1; }
+    const int v2 = hi16s(bmax), r2 = (int)(brow >> 16);
+    if (v2 > 0 && ck_better(v2, r2, j0 + 1, vB, rB, cB)) { vB = v2; rB = r2; cB = j0 + 1; }
     __syncwarp();
 }
 
@@ -285,7 +279,9 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
                 b0 += 32 * cb;
             }
         }
-        // per pair over the warp: (max value, min row, min column)
+        // per pair over the warp: (max value, min row, min span); the best cell
+        // is the first column of that row holding the value -- in that span, as
+        // any earlier column holding it would belong to an earlier span
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const int ov = __shfl_xor_sync(FULL, vA, o), orr = __shfl_xor_sync(FULL, rA, o), oc = __shfl_xor_sync(FULL, cA, o);
@@ -311,10 +307,11 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
                 } else {
                     A.out_score[p] = x ? vB : vA;
                     A.out_pos[4 * p + 2] = (x ? rB : rA) - 1;
-                    A.out_pos[4 * p + 3] = (x ? cB : cA) - 1;
                 }
             }
         }
+        bool first[2] = {!done[0], !done[1]};                // the best cell's column not yet found
+        const int best_of[2] = {vA, vB};
         int ti0[2] = {1, 1}, tb[2] = {0, 0};
 #pragma unroll
         for (int x = 0; x < 2; ++x) {
@@ -378,6 +375,7 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
             const uint8_t* tB = textB + (ti0[1] - 1);
             uint32_t ch = 0;
             uint32_t ch_next = t == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
+            int jfound0 = INT32_MAX, jfound1 = INT32_MAX;
             for (int tau = 0; tau < steps; ++tau) {
                 uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
                 uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
@@ -419,11 +417,42 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
                 const uint32_t t23 = __byte_perm(acc2, acc3, 0x7351);
                 tileA[tau * 32 + t] = __byte_perm(t01, t23, 0x5410);
                 tileB[tau * 32 + t] = __byte_perm(t01, t23, 0x7632);
+                // the best cell's row: first column holding the best value
+                if (first[0] && i == rows0) {
+#pragma unroll
+                    for (int c = 1; c >= 0; --c) {
+                        const int col = TW * tb[0] + 2 * t + c;            // 0-based
+                        if (col < nA && (int)(hgu[c] & 0xffffu) - CK_BIAS + go == best_of[0]) jfound0 = col + 1;
+                    }
+                }
+                if (first[1] && i == rows1) {
+#pragma unroll
+                    for (int c = 1; c >= 0; --c) {
+                        const int col = TW * tb[1] + 2 * t + c;
+                        if (col < nB && (int)(hgu[c] >> 16) - CK_BIAS + go == best_of[1]) jfound1 = col + 1;
+                    }
+                }
                 diag_in = in_hg;
                 out_hg = hgl;
                 out_e = el;
             }
             __syncwarp();
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                if (!first[x]) continue;
+                int jf = x ? jfound1 : jfound0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) jf = min(jf, __shfl_xor_sync(FULL, jf, o));
+                first[x] = false;
+                const int p = x ? pb : pa;
+                if (jf == INT32_MAX) {                 // cannot happen: the forward pass saw the value here
+                    if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
+                    done[x] = true;
+                    continue;
+                }
+                wj[x] = jf;
+                if (t == 0) A.out_pos[4 * p + 3] = jf - 1;
+            }
             // ---- walk each pair inside its tile
 #pragma unroll
             for (int x = 0; x < 2; ++x) {

@@ -99,7 +99,7 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
     const int kout = (j0 + CB) % X.TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / X.TW : 0;
     int32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * m : nullptr;
     uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.text) : 0u;
-    int bv = 0, br = 0, bc = 0;                       // this band's best: value, first row, first column
+    int bv = 0, br = 0;                               // this band's best and the first row holding it
     const int steps = m + 31;
     for (int tau = 0; tau < steps; ++tau) {
         int in_hg = __shfl_up_sync(FULL, out_hg, 1);
@@ -111,7 +111,11 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
             if (i < m) ch_next = __ldg(X.text + i);
             in_hg = nxt_hg;
             in_e = nxt_e;
-            if (left && i < m) { nxt_hg = left[2 * i]; nxt_e = left[2 * i + 1]; }
+            if (left && i < m) {
+                const int2 lv = *reinterpret_cast<const int2*>(left + 2 * i);
+                nxt_hg = lv.x;
+                nxt_e = lv.y;
+            }
         }
         if (i < 1 || i > m) continue;
         int s[CB];
@@ -144,23 +148,17 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
         diag_in = in_hg;
         out_hg = hgl;
         out_e = el;
-        if (eout) { eout[2 * (i - 1)] = out_hg; eout[2 * (i - 1) + 1] = out_e; }
+        if (eout) *reinterpret_cast<int2*>(eout + 2 * (i - 1)) = make_int2(out_hg, out_e);
         if ((i & (X.K - 1)) == 0 && i < m) {
             int4* dst = reinterpret_cast<int4*>(X.ck + 2 * ((int64_t)(i / X.K - 1) * X.stride + j0));
 #pragma unroll
             for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_int4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
         }
-        if (rowmax > bv) {                                   // first column of this row holding it
-            int first = 0;
-#pragma unroll
-            for (int c = CB - 1; c >= 0; --c)
-                if (hgu[c] + go == rowmax) first = c;
-            bv = rowmax;
-            br = i;
-            bc = j0 + first + 1;
-        }
+        if (rowmax > bv) { bv = rowmax; br = i; }          // first row holding this lane's best
     }
-    if (bv > 0 && c32_better(bv, br, bc, vb, rb, cb)) { vb = bv; rb = br; cb = bc; }
+    // the column kept is the first of the lane's span in this band (spans
+    // order like their columns); the walk finds the cell's column in that row
+    if (bv > 0 && c32_better(bv, br, j0 + 1, vb, rb, cb)) { vb = bv; rb = br; cb = j0 + 1; }
     __syncwarp();
 }
 
@@ -256,6 +254,7 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
         int pos = m + n;
         int i = rb, j = cb, state = 0, v = vb;
         int ti0 = ((i - 1) / K) * K + 1, tb = (j - 1) / TW;
+        bool first = true;                                          // the best cell's column not yet found
         int* edg = reinterpret_cast<int*>(wsm + 4 * CT * 32 * 4);     // [row][2], after the tile profile
         bool fin = false;
         while (!fin) {
@@ -308,6 +307,7 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
             }
             __syncwarp();
             int out_hg = -go, out_e = 0;
+            int jfound = INT32_MAX;
             const uint8_t* tx = text + (ti0 - 1);
             uint32_t ch = 0, ch_next = t == 0 ? (uint32_t)__ldg(tx) : 0u;
             for (int tau = 0; tau < steps; ++tau) {
@@ -363,11 +363,29 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
                 }
 #pragma unroll
                 for (int wq = 0; wq < NWT; ++wq) tile[(tau * 32 + t) * NWT + wq] = nib[wq];
+                if (first && r == rows) {                           // the best cell's row
+#pragma unroll
+                    for (int c = CT - 1; c >= 0; --c) {
+                        const int col = col0 + CT * t + c;
+                        if (col < n && hgu[c] + go == vb) jfound = col + 1;
+                    }
+                }
                 diag_in = in_hg;
                 out_hg = hgl;
                 out_e = el;
             }
             __syncwarp();
+            if (first) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) jfound = min(jfound, __shfl_xor_sync(FULL, jfound, o));
+                first = false;
+                if (jfound == INT32_MAX) {             // cannot happen: the forward pass saw the value here
+                    if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
+                    break;
+                }
+                j = jfound;
+                cb = jfound;
+            }
             // walk inside the tile: state 0 on H, 1 in an E run ('D'), 2 in an F run ('I')
             const int jlo = col0 + 1;
             for (;;) {
