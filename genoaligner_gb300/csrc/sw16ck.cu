@@ -16,13 +16,15 @@
 //      edges); per lane the best value with its first row and column;
 //   2. the best cell is the warp's (max value, min row, min column);
 //   3. walk: the tile [i0, i] x [TW*b + 1, TW*b + TW] holding the walk's
-//      current cell (i0 = the first row of its CK_K-row block) is recomputed
-//      from the checkpoint row above it and the column edge left of it,
-//      exactly as sw16.cu computes cells (biased 16-bit values, predicate
-//      bits from sign bits), and the walk proceeds inside it; leaving the
-//      tile at its top or left edge, the tile there is recomputed.  Both
-//      pairs of a warp recompute their current tiles in one pass, each half
-//      of a register at its own rows and columns.
+//      current cell (i0 = the first row of its CK_K-row block) and the three
+//      tiles to its left are recomputed from the checkpoint row above them
+//      and the column edges left of them -- four groups of 8 lanes, one tile
+//      each, so the lanes' one-step lag costs 7 steps, not 31 -- exactly as
+//      sw16.cu computes cells (biased 16-bit values, predicate bits from sign
+//      bits), and the walk proceeds inside them; leaving them at the top or
+//      the left, the tiles there are recomputed.  Both pairs of a warp
+//      recompute their tiles in one pass, each half of a register at its own
+//      rows and columns.
 //
 // Recomputed values equal the forward pass's, so the predicates and the walk
 // are those of sw16.cu.  Eligibility is sw16.cu's (host-side check).
@@ -31,7 +33,8 @@
 namespace ga {
 
 constexpr int CK_K = 64;                 // rows per checkpoint block
-constexpr int TW = 64;                   // tile width: 32 lanes x 2 columns
+constexpr int TW = 64;                   // tile width: a group of 8 lanes x 8 columns
+constexpr int TG = 4;                    // tiles recomputed per pass: the walk's and the 3 to its left
 constexpr int CK_BIAS = 1024;            // value bias of the recompute pass
 constexpr int CK_C = 16;                 // forward columns per lane, full bands
 constexpr int CK_BW = 32 * CK_C;         // forward band width, full bands
@@ -204,25 +207,30 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     __syncwarp();
 }
 
-// Tile profile of one pair: prof[(pair * 4 + letter) * 32 + t] for the
-// tile's columns col0 + 2t, col0 + 2t + 1 (0-based); past the end: mismatch.
+// Tile profile of one pair for a lane of a tile group: prof[((pair * 4 +
+// letter) * 4 + h) * 32 + t] holds the 16-bit scores of the lane's columns
+// col0 + 2h, col0 + 2h + 1 (0-based); past the pattern's end or left of
+// column 0: mismatch.
 __device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* pat, int n, int col0, int pair,
                                                 int sm, int sx, int t)
 {
-    const int c0 = col0 + 2 * t, c1 = c0 + 1;
-    const int a0 = c0 < n ? ck_code(__ldg(pat + c0)) : 4;
-    const int a1 = c1 < n ? ck_code(__ldg(pat + c1)) : 4;
 #pragma unroll
-    for (int L = 0; L < 4; ++L) {
-        const int v0 = a0 == L ? sm : sx, v1 = a1 == L ? sm : sx;
-        prof[(pair * 4 + L) * 32 + t] = ((uint32_t)v0 & 0xffffu) | ((uint32_t)v1 << 16);
+    for (int h = 0; h < 4; ++h) {
+        const int c0 = col0 + 2 * h, c1 = c0 + 1;
+        const int a0 = (c0 >= 0 && c0 < n) ? ck_code(__ldg(pat + c0)) : 4;
+        const int a1 = (c1 >= 0 && c1 < n) ? ck_code(__ldg(pat + c1)) : 4;
+#pragma unroll
+        for (int L = 0; L < 4; ++L) {
+            const int v0 = a0 == L ? sm : sx, v1 = a1 == L ? sm : sx;
+            prof[((pair * 4 + L) * 4 + h) * 32 + t] = ((uint32_t)v0 & 0xffffu) | ((uint32_t)v1 << 16);
+        }
     }
 }
 
-__global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
+__global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 {
     constexpr int NH = CK_C / 2;
-    constexpr int TSTEPS = CK_K + 31;
+    constexpr int TSTEPS = CK_K + 7;             // tile pass: rows + the 8-lane group's lag
     extern __shared__ uint32_t ck_smem[];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -320,117 +328,122 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
         }
         uint32_t* tileA = tiles;
         uint32_t* tileB = tiles + TSTEPS * 32;
+        const int g = t >> 3, tl = t & 7;                           // tile group, lane in group
         while (!(done[0] && done[1])) {
-            // ---- recompute both pairs' tiles: pair x rows [ti0, wi], columns [TW*tb, TW*tb + TW)
+            // ---- recompute, per pair x, the TG tiles tb-3 .. tb over rows [ti0, wi]:
+            // group g takes tile tb - 3 + g, lane tl its columns 8 tl .. 8 tl + 7
             const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
             const int R = max(rows0, rows1);
-            const int steps = R + 31;
+            const int steps = R + 7;
+            const int tgA = tb[0] - (TG - 1) + g, tgB = tb[1] - (TG - 1) + g;   // this group's tiles
+            const int colA = TW * tgA + 8 * tl, colB = TW * tgB + 8 * tl;      // this lane's first columns
             __syncwarp();
-            ck_profile_tile(prof, patA, nA, TW * tb[0], 0, sm, sx, t);
-            ck_profile_tile(prof, patB, nB, TW * tb[1], 1, sm, sx, t);
-            __syncwarp();
-            uint32_t hgu[2], fv[2];
+            ck_profile_tile(prof, patA, nA, colA, 0, sm, sx, t);
+            ck_profile_tile(prof, patB, nB, colB, 1, sm, sx, t);
+            uint32_t hgu[8], fv[8];
             uint32_t diag_in;
             {
                 const int qa = (ti0[0] - 1) / CK_K - 1, qb = (ti0[1] - 1) / CK_K - 1;
                 const uint32_t* ca = ck + 2 * (int64_t)max(qa, 0) * ncol;
                 const uint32_t* cb = ck + 2 * (int64_t)max(qb, 0) * ncol;
-                const int colA = TW * tb[0] + 2 * t, colB = TW * tb[1] + 2 * t;
+                const bool oka = qa >= 0 && tgA >= 0, okb = qb >= 0 && tgB >= 0;
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    const uint32_t ha = qa >= 0 ? ca[2 * (colA + c)] : NGO2, fa = qa >= 0 ? ca[2 * (colA + c) + 1] : 0u;
-                    const uint32_t hb = qb >= 0 ? cb[2 * (colB + c)] : NGO2, fb = qb >= 0 ? cb[2 * (colB + c) + 1] : 0u;
-                    hgu[c] = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
-                    fv[c] = __viaddmax_s16x2(__byte_perm(fa, fb, 0x7610), B2, MIN2);
+                for (int c = 0; c < 8; ++c) {
+                    const uint2 va = oka ? *reinterpret_cast<const uint2*>(ca + 2 * (colA + c)) : make_uint2(NGO2, 0u);
+                    const uint2 vb = okb ? *reinterpret_cast<const uint2*>(cb + 2 * (colB + c)) : make_uint2(NGO2, 0u);
+                    hgu[c] = __viaddmax_s16x2(__byte_perm(va.x, vb.x, 0x7610), B2, MIN2);
+                    fv[c] = __viaddmax_s16x2(__byte_perm(va.y, vb.y, 0x7610), B2, MIN2);
                 }
-                // H[i0-1][first column - 1] - go: the left lane's last column; for lane 0
-                // the checkpoint left of the tile (0 on row 0 and column 0)
-                uint32_t lft = __shfl_up_sync(FULL, hgu[1], 1);
-                if (t == 0) {
-                    const uint32_t ha = (qa >= 0 && tb[0] > 0) ? ca[2 * (TW * tb[0] - 1)] : NGO2;
-                    const uint32_t hb = (qb >= 0 && tb[1] > 0) ? cb[2 * (TW * tb[1] - 1)] : NGO2;
+                // H[i0-1][first column - 1] - go: the left lane's last column; for a
+                // group's first lane the checkpoint left of its tile (0 on row 0 and column 0)
+                uint32_t lft = __shfl_up_sync(FULL, hgu[7], 1, 8);
+                if (tl == 0) {
+                    const uint32_t ha = (qa >= 0 && tgA > 0) ? ca[2 * (colA - 1)] : NGO2;
+                    const uint32_t hb = (qb >= 0 && tgB > 0) ? cb[2 * (colB - 1)] : NGO2;
                     lft = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
                 }
                 diag_in = lft;
             }
-            // lane 0's left boundary per tile row: the column edges at TW*tb,
-            // combined and biased into shared memory first
-            uint32_t* edg = prof + 2 * 4 * 32;                           // [row][2], after the tile profile
-            {
-                const uint32_t* la = tb[0] > 0 ? ce + 2 * ((int64_t)(tb[0] - 1) * M + (ti0[0] - 1)) : nullptr;
-                const uint32_t* lb = tb[1] > 0 ? ce + 2 * ((int64_t)(tb[1] - 1) * M + (ti0[1] - 1)) : nullptr;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int r = t + 32 * h;
-                    const bool ina = la && r < rows0, inb = lb && r < rows1;
-                    const uint32_t ha = ina ? la[2 * r] : NGO2, ea = ina ? la[2 * r + 1] : 0u;
-                    const uint32_t hb = inb ? lb[2 * r] : NGO2, eb = inb ? lb[2 * r + 1] : 0u;
-                    edg[2 * r] = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
-                    edg[2 * r + 1] = __viaddmax_s16x2(__byte_perm(ea, eb, 0x7610), B2, MIN2);
-                }
+            // the groups' left boundaries per tile row (column edges at TW * tile),
+            // combined and biased into shared memory: edg[(group * CK_K + row) * 2]
+            uint32_t* edg = prof + 2 * 4 * 4 * 32;
+            for (int idx = t; idx < TG * CK_K; idx += 32) {
+                const int gg = idx / CK_K, r = idx - gg * CK_K;
+                const int ka = tb[0] - (TG - 1) + gg, kb = tb[1] - (TG - 1) + gg;
+                const bool ina = ka > 0 && r < rows0, inb = kb > 0 && r < rows1;
+                const uint2 la = ina ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(ka - 1) * M + (ti0[0] - 1 + r)))
+                                     : make_uint2(NGO2, 0u);
+                const uint2 lb = inb ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(kb - 1) * M + (ti0[1] - 1 + r)))
+                                     : make_uint2(NGO2, 0u);
+                edg[2 * idx] = __viaddmax_s16x2(__byte_perm(la.x, lb.x, 0x7610), B2, MIN2);
+                edg[2 * idx + 1] = __viaddmax_s16x2(__byte_perm(la.y, lb.y, 0x7610), B2, MIN2);
             }
             __syncwarp();
+            const uint32_t* eg = edg + 2 * g * CK_K;
             uint32_t out_hg = B2 - GO2, out_e = B2;
             const uint8_t* tA = textA + (ti0[0] - 1);
             const uint8_t* tB = textB + (ti0[1] - 1);
             uint32_t ch = 0;
-            uint32_t ch_next = t == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
+            uint32_t ch_next = tl == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
             int jfound0 = INT32_MAX, jfound1 = INT32_MAX;
+            const uint32_t* pA0 = prof + (0 * 4 * 4) * 32 + t;
+            const uint32_t* pB0 = prof + (1 * 4 * 4) * 32 + t;
             for (int tau = 0; tau < steps; ++tau) {
-                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
-                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
-                ch = __shfl_up_sync(FULL, ch, 1);
-                const int i = tau - t + 1;                                   // tile row, 1-based
-                if (t == 0) {
+                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, 8);
+                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, 8);
+                ch = __shfl_up_sync(FULL, ch, 1, 8);
+                const int i = tau - tl + 1;                                  // tile row, 1-based
+                if (tl == 0) {
                     ch = ch_next;
                     if (i < R)
                         ch_next = (uint32_t)(i < rows0 ? __ldg(tA + i) : 'A') | ((uint32_t)(i < rows1 ? __ldg(tB + i) : 'A') << 8);
-                    if (i <= R) { in_hg = edg[2 * (i - 1)]; in_e = edg[2 * (i - 1) + 1]; }
+                    if (i <= R) { in_hg = eg[2 * (i - 1)]; in_e = eg[2 * (i - 1) + 1]; }
                 }
                 if (i < 1 || i > R) continue;
-                const uint32_t wa = prof[(0 * 4 + ck_code(ch & 0xffu)) * 32 + t], wb = prof[(1 * 4 + ck_code(ch >> 8)) * 32 + t];
+                const uint32_t* pA = pA0 + ck_code(ch & 0xffu) * 4 * 32;
+                const uint32_t* pB = pB0 + ck_code(ch >> 8) * 4 * 32;
                 uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
                 uint32_t acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const uint32_t S = __byte_perm(wa, wb, u ? 0x7632 : 0x5410);
-                    const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
-                    const uint32_t f = __viaddmax_s16x2(fv[u], NGE2, hgu[u]);
-                    const uint32_t h0 = hgd + S;
-                    const uint32_t h1 = __vmaxs2(h0, e);
-                    const uint32_t hh = __vimax3_s16x2(h1, f, B2);
-                    acc0 = (acc0 >> 1) | ((h0 - e + K2) & K2);
-                    acc1 = (acc1 >> 1) | ((h1 - f + K2) & K2);
-                    acc2 = (acc2 >> 1) | ((hgl - el + KGE2) & K2);
-                    acc3 = (acc3 >> 1) | ((hgu[u] - fv[u] + KGE2) & K2);
-                    const uint32_t hg = hh - GO2;
-                    hgd = hgu[u];
-                    hgu[u] = hg;
-                    fv[u] = f;
-                    hgl = hg;
-                    el = e;
+                for (int cc = 0; cc < 8; cc += 2) {
+                    const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
+                    const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int cu = cc + u;
+                        const uint32_t S = u ? S1 : S0;
+                        const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
+                        const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
+                        const uint32_t h0 = hgd + S;
+                        const uint32_t h1 = __vmaxs2(h0, e);
+                        const uint32_t hh = __vimax3_s16x2(h1, f, B2);
+                        acc0 = (acc0 >> 1) | ((h0 - e + K2) & K2);
+                        acc1 = (acc1 >> 1) | ((h1 - f + K2) & K2);
+                        acc2 = (acc2 >> 1) | ((hgl - el + KGE2) & K2);
+                        acc3 = (acc3 >> 1) | ((hgu[cu] - fv[cu] + KGE2) & K2);
+                        const uint32_t hg = hh - GO2;
+                        hgd = hgu[cu];
+                        hgu[cu] = hg;
+                        fv[cu] = f;
+                        hgl = hg;
+                        el = e;
+                    }
                 }
-                // cell c at bits 14 + c / 30 + c: move to 8 + c / 24 + c, then
-                // byte k = predicate k per pair as in sw16.cu
-                acc0 >>= 6; acc1 >>= 6; acc2 >>= 6; acc3 >>= 6;
+                // byte k = predicate k of the lane's 8 cells, per pair (as sw16.cu)
                 const uint32_t t01 = __byte_perm(acc0, acc1, 0x7351);
                 const uint32_t t23 = __byte_perm(acc2, acc3, 0x7351);
                 tileA[tau * 32 + t] = __byte_perm(t01, t23, 0x5410);
                 tileB[tau * 32 + t] = __byte_perm(t01, t23, 0x7632);
                 // the best cell's row: first column holding the best value
-                if (first[0] && i == rows0) {
+                if (first[0] && i == rows0 && tgA >= 0) {
 #pragma unroll
-                    for (int c = 1; c >= 0; --c) {
-                        const int col = TW * tb[0] + 2 * t + c;            // 0-based
-                        if (col < nA && (int)(hgu[c] & 0xffffu) - CK_BIAS + go == best_of[0]) jfound0 = col + 1;
-                    }
+                    for (int c = 7; c >= 0; --c)
+                        if (colA + c < nA && (int)(hgu[c] & 0xffffu) - CK_BIAS + go == best_of[0]) jfound0 = colA + c + 1;
                 }
-                if (first[1] && i == rows1) {
+                if (first[1] && i == rows1 && tgB >= 0) {
 #pragma unroll
-                    for (int c = 1; c >= 0; --c) {
-                        const int col = TW * tb[1] + 2 * t + c;
-                        if (col < nB && (int)(hgu[c] >> 16) - CK_BIAS + go == best_of[1]) jfound1 = col + 1;
-                    }
+                    for (int c = 7; c >= 0; --c)
+                        if (colB + c < nB && (int)(hgu[c] >> 16) - CK_BIAS + go == best_of[1]) jfound1 = colB + c + 1;
                 }
                 diag_in = in_hg;
                 out_hg = hgl;
@@ -463,15 +476,15 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
                 const uint8_t* pat = x ? patB : patA;
                 const uint32_t* tt_tab = x ? tileB : tileA;
                 char* slotc = A.out_cigar + A.D.out_off[p];
-                const int i0 = ti0[x], jlo = TW * tb[x] + 1;
+                const int i0 = ti0[x], jlo = TW * (tb[x] - (TG - 1)) + 1;     // leftmost recomputed column
                 int i = wi[x], j = wj[x], state = wst[x], v = wv[x], pos = wpos[x];
                 bool fin = false;
                 for (;;) {
                     if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
-                    if (i < i0 || j < jlo) break;                          // left the tile
-                    const int jj = j - jlo;
-                    const int tt = jj >> 1, c = jj & 1;
-                    const uint32_t word = tt_tab[((i - i0) + tt) * 32 + tt];
+                    if (i < i0 || j < jlo) break;                          // left the tiles
+                    const int jj = j - jlo;                                 // 0 .. TG*TW-1
+                    const int ln = jj >> 3, c = jj & 7;                     // lane (group * 8 + lane in group)
+                    const uint32_t word = tt_tab[((i - i0) + (ln & 7)) * 32 + ln];
                     const bool notE = (word >> c) & 1u, notF = (word >> (8 + c)) & 1u;
                     const bool eopen = (word >> (16 + c)) & 1u, fopen = (word >> (24 + c)) & 1u;
                     char op;
@@ -533,7 +546,7 @@ __global__ void __launch_bounds__(128) sw16ck_kernel(Sw16Args A)
 int64_t sw16ck_dir_words(int M, int N)
 {
     const int64_t ncol = ck_ncol(N);
-    return 2 * (int64_t)ck_rows(M) * ncol + 2 * (ncol / TW) * (int64_t)M + 2 * (int64_t)(CK_K + 31) * 32;
+    return 2 * (int64_t)ck_rows(M) * ncol + 2 * (ncol / TW) * (int64_t)M + 2 * (int64_t)(CK_K + 7) * 32;
 }
 
 static size_t sw16ck_smem() { return (size_t)4 * 2 * 4 * (CK_C / 2) * 32 * sizeof(uint32_t); }
