@@ -19,15 +19,18 @@
 //      current cell (i0 = the first row of its CK_K-row block) and the three
 //      tiles to its left are recomputed from the checkpoint row above them
 //      and the column edges left of them -- four groups of 8 lanes, one tile
-//      each, so the lanes' one-step lag costs 7 steps, not 31 -- exactly as
-//      sw16.cu computes cells (biased 16-bit values, predicate bits from sign
-//      bits), and the walk proceeds inside them; leaving them at the top or
-//      the left, the tiles there are recomputed.  Both pairs of a warp
-//      recompute their tiles in one pass, each half of a register at its own
-//      rows and columns.
+//      each, so the lanes' one-step lag costs 7 steps, not 31 -- and their H
+//      values are kept; the walk proceeds inside them, reading every decision
+//      off H values with the reference's tie rules (diagonal, then E, then F;
+//      a gap cell opened when its neighbour's H - gap_open equals it, E from
+//      a warp-wide max over the row); leaving the window at the top or the
+//      left, the tiles there are recomputed.  Both pairs of a warp recompute
+//      their windows in one pass, each half of a register at its own rows and
+//      columns.
 //
-// Recomputed values equal the forward pass's, so the predicates and the walk
-// are those of sw16.cu.  Eligibility is sw16.cu's (host-side check).
+// Recomputed values equal the forward pass's, so every decision is the one
+// the reference's stored direction bits give.  Eligibility is sw16.cu's
+// (host-side check).
 #include "kernels.cuh"
 
 namespace ga {
@@ -230,7 +233,6 @@ __device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* p
 __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 {
     constexpr int NH = CK_C / 2;
-    constexpr int TSTEPS = CK_K + 7;             // tile pass: rows + the 8-lane group's lag
     extern __shared__ uint32_t ck_smem[];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -244,10 +246,8 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
     const uint32_t NGE2 = ((uint32_t)(-ge) & 0xffffu) * 0x10001u;
     const uint32_t GO2 = (uint32_t)go * 0x10001u;
     const uint32_t MIN2 = 0x80008000u;
-    const uint32_t K2 = 0x80008000u;
     // biased recompute constants (sw16.cu)
     const uint32_t B2 = (uint32_t)CK_BIAS * 0x10001u;
-    const uint32_t KGE2 = K2 + (uint32_t)ge * 0x10001u;
 
     for (;;) {
         int w = 0;
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
         // tile tables [pair][step][lane]
         uint32_t* ck = wslot;
         uint32_t* ce = ck + 2 * (int64_t)nq * ncol;
-        uint32_t* tiles = ce + 2 * (int64_t)(ncol / TW) * M;
+        uint32_t* tiles = ce + (2 * (int64_t)(ncol / TW) * M + 3) / 4 * 4;     // 16-byte aligned
 
         // ------------------------------------------------ forward pass --
         int vA = 0, rA = 0, cA = 0, vB = 0, rB = 0, cB = 0;          // lane's best per pair
@@ -326,12 +326,14 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
             ti0[x] = done[x] ? 1 : ((wi[x] - 1) / CK_K) * CK_K + 1;
             tb[x] = done[x] ? 0 : (wj[x] - 1) / TW;
         }
-        uint32_t* tileA = tiles;
-        uint32_t* tileB = tiles + TSTEPS * 32;
+        // window table: H of the window's cells, [row][TG * TW columns], both
+        // pairs in the 16-bit halves (biased)
+        constexpr int WCOL = TG * TW;
+        uint32_t* Ht = tiles;
         const int g = t >> 3, tl = t & 7;                           // tile group, lane in group
         while (!(done[0] && done[1])) {
-            // ---- recompute, per pair x, the TG tiles tb-3 .. tb over rows [ti0, wi]:
-            // group g takes tile tb - 3 + g, lane tl its columns 8 tl .. 8 tl + 7
+            // ---- recompute, per pair x, the window of TG tiles tb-3 .. tb over rows
+            // [ti0, wi]: group g takes tile tb - 3 + g, lane tl its columns 8 tl .. 8 tl + 7
             const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
             const int R = max(rows0, rows1);
             const int steps = R + 7;
@@ -385,14 +387,14 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
             const uint8_t* tB = textB + (ti0[1] - 1);
             uint32_t ch = 0;
             uint32_t ch_next = tl == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
-            int jfound0 = INT32_MAX, jfound1 = INT32_MAX;
             const uint32_t* pA0 = prof + (0 * 4 * 4) * 32 + t;
             const uint32_t* pB0 = prof + (1 * 4 * 4) * 32 + t;
+            uint32_t* hrow = Ht + g * TW + 8 * tl;                          // + (row - 1) * WCOL
             for (int tau = 0; tau < steps; ++tau) {
                 uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, 8);
                 uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, 8);
                 ch = __shfl_up_sync(FULL, ch, 1, 8);
-                const int i = tau - tl + 1;                                  // tile row, 1-based
+                const int i = tau - tl + 1;                                  // window row, 1-based
                 if (tl == 0) {
                     ch = ch_next;
                     if (i < R)
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 const uint32_t* pA = pA0 + ck_code(ch & 0xffu) * 4 * 32;
                 const uint32_t* pB = pB0 + ck_code(ch >> 8) * 4 * 32;
                 uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
-                uint32_t acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+                uint32_t hv[8];
 #pragma unroll
                 for (int cc = 0; cc < 8; cc += 2) {
                     const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
@@ -411,17 +413,12 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 #pragma unroll
                     for (int u = 0; u < 2; ++u) {
                         const int cu = cc + u;
-                        const uint32_t S = u ? S1 : S0;
                         const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
                         const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
-                        const uint32_t h0 = hgd + S;
-                        const uint32_t h1 = __vmaxs2(h0, e);
+                        const uint32_t h1 = __viaddmax_s16x2(hgd, u ? S1 : S0, e);
                         const uint32_t hh = __vimax3_s16x2(h1, f, B2);
-                        acc0 = (acc0 >> 1) | ((h0 - e + K2) & K2);
-                        acc1 = (acc1 >> 1) | ((h1 - f + K2) & K2);
-                        acc2 = (acc2 >> 1) | ((hgl - el + KGE2) & K2);
-                        acc3 = (acc3 >> 1) | ((hgu[cu] - fv[cu] + KGE2) & K2);
                         const uint32_t hg = hh - GO2;
+                        hv[cu] = hh;
                         hgd = hgu[cu];
                         hgu[cu] = hg;
                         fv[cu] = f;
@@ -429,31 +426,30 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                         el = e;
                     }
                 }
-                // byte k = predicate k of the lane's 8 cells, per pair (as sw16.cu)
-                const uint32_t t01 = __byte_perm(acc0, acc1, 0x7351);
-                const uint32_t t23 = __byte_perm(acc2, acc3, 0x7351);
-                tileA[tau * 32 + t] = __byte_perm(t01, t23, 0x5410);
-                tileB[tau * 32 + t] = __byte_perm(t01, t23, 0x7632);
-                // the best cell's row: first column holding the best value
-                if (first[0] && i == rows0 && tgA >= 0) {
-#pragma unroll
-                    for (int c = 7; c >= 0; --c)
-                        if (colA + c < nA && (int)(hgu[c] & 0xffffu) - CK_BIAS + go == best_of[0]) jfound0 = colA + c + 1;
-                }
-                if (first[1] && i == rows1 && tgB >= 0) {
-#pragma unroll
-                    for (int c = 7; c >= 0; --c)
-                        if (colB + c < nB && (int)(hgu[c] >> 16) - CK_BIAS + go == best_of[1]) jfound1 = colB + c + 1;
-                }
+                uint4* dst = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
+                dst[0] = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                dst[1] = make_uint4(hv[4], hv[5], hv[6], hv[7]);
                 diag_in = in_hg;
                 out_hg = hgl;
                 out_e = el;
             }
             __syncwarp();
+            // the best cell's column (a pair's first window): first column of row i*
+            // holding the best value -- row i* is the window's last row
 #pragma unroll
             for (int x = 0; x < 2; ++x) {
                 if (!first[x]) continue;
-                int jf = x ? jfound1 : jfound0;
+                const int rows = x ? rows1 : rows0, n = x ? nB : nA;
+                const int wc0 = TW * (tb[x] - (TG - 1));                    // 0-based column of window column 0
+                int jf = INT32_MAX;
+#pragma unroll
+                for (int c = 7; c >= 0; --c) {
+                    const int col = wc0 + 8 * t + c;
+                    if (col >= 0 && col < n) {
+                        const uint32_t w = Ht[(rows - 1) * WCOL + 8 * t + c];
+                        if ((int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS == best_of[x]) jf = col + 1;
+                    }
+                }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) jf = min(jf, __shfl_xor_sync(FULL, jf, o));
                 first[x] = false;
@@ -466,7 +462,12 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 wj[x] = jf;
                 if (t == 0) A.out_pos[4 * p + 3] = jf - 1;
             }
-            // ---- walk each pair inside its tile
+            // ---- walk each pair inside its window, tracking the exact value of the
+            // current cell's H (state 0), E (1) or F (2).  Every decision is the
+            // reference's tie rule read off H values: H came from the diagonal iff
+            // H[i-1][j-1] + s == H (the diagonal wins ties), else from E iff E == H
+            // (E wins ties with F), else from F; a gap cell was opened iff the
+            // neighbour's H - gap_open equals it (opening wins ties).
 #pragma unroll
             for (int x = 0; x < 2; ++x) {
                 if (done[x]) continue;
@@ -474,43 +475,65 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 const int m = x ? mB : mA, n = x ? nB : nA;
                 const uint8_t* text = x ? textB : textA;
                 const uint8_t* pat = x ? patB : patA;
-                const uint32_t* tt_tab = x ? tileB : tileA;
                 char* slotc = A.out_cigar + A.D.out_off[p];
-                const int i0 = ti0[x], jlo = TW * (tb[x] - (TG - 1)) + 1;     // leftmost recomputed column
+                const int i0 = ti0[x], jlo = TW * (tb[x] - (TG - 1)) + 1;     // first window row / column
+                const int q = (i0 - 1) / CK_K - 1;                              // checkpoint row i0 - 1
+                const uint32_t* crow = ck + 2 * (int64_t)max(q, 0) * ncol;
+                const int kedge = (jlo - 1) / TW;                               // column edge at jlo - 1 (if >= 1)
+                const uint32_t* cedge = kedge > 0 ? ce + 2 * (int64_t)(kedge - 1) * M : nullptr;
+                auto half = [x](uint32_t w) { return x ? hi16s(w) : lo16s(w); };
+                // H[ii][jj] for ii in [i0 - 1, i], jj in [jlo - 1, j]
+                auto Hv = [&](int ii, int jj) -> int {
+                    if (ii <= 0 || jj <= 0) return 0;
+                    if (ii == i0 - 1) return half(crow[2 * (jj - 1)]) + go;
+                    if (jj == jlo - 1) return half(cedge[2 * (ii - 1)]) + go;
+                    const uint32_t w = Ht[(ii - i0) * WCOL + (jj - jlo)];
+                    return (int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS;
+                };
+                // E[ii][jj] from the row's H values left of jj within the window and the
+                // column edge's E (E[ii][0] = 0): warp-parallel max over the gap lengths
+                auto Ev = [&](int ii, int jj) -> int {
+                    const int kl = max(jlo - 1, 0);
+                    int e = INT32_MIN / 2;
+                    for (int k = jj - 1 - t; k >= kl; k -= 32) e = max(e, Hv(ii, k) - go - (jj - 1 - k) * ge);
+                    if (t == 0) {
+                        const int eb = (kl > 0) ? half(cedge[2 * (ii - 1) + 1]) : 0;
+                        e = max(e, eb - (jj - kl) * ge);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(FULL, e, o));
+                    return e;
+                };
                 int i = wi[x], j = wj[x], state = wst[x], v = wv[x], pos = wpos[x];
                 bool fin = false;
                 for (;;) {
                     if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
-                    if (i < i0 || j < jlo) break;                          // left the tiles
-                    const int jj = j - jlo;                                 // 0 .. TG*TW-1
-                    const int ln = jj >> 3, c = jj & 7;                     // lane (group * 8 + lane in group)
-                    const uint32_t word = tt_tab[((i - i0) + (ln & 7)) * 32 + ln];
-                    const bool notE = (word >> c) & 1u, notF = (word >> (8 + c)) & 1u;
-                    const bool eopen = (word >> (16 + c)) & 1u, fopen = (word >> (24 + c)) & 1u;
+                    if (i < i0 || j < jlo) break;                               // left the window
                     char op;
                     if (state == 0) {
-                        if (!notF) {
-                            op = 'I';
-                            if (!fopen) { state = 2; v += ge; } else { v += go; }
+                        const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
+                        const int hd = Hv(i - 1, j - 1);
+                        if (hd + (ta == pc ? A.match : A.mismatch) == v) {
+                            op = ta == pc ? 'M' : 'X';
+                            v = hd;
                             --i;
-                        } else if (!notE) {
+                            --j;
+                        } else if (Ev(i, j) == v) {
                             op = 'D';
-                            if (!eopen) { state = 1; v += ge; } else { v += go; }
+                            if (Hv(i, j - 1) - go == v) { v += go; } else { state = 1; v += ge; }
                             --j;
                         } else {
-                            const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
-                            op = ta == pc ? 'M' : 'X';
-                            v -= ta == pc ? A.match : A.mismatch;
+                            op = 'I';
+                            if (Hv(i - 1, j) - go == v) { v += go; } else { state = 2; v += ge; }
                             --i;
-                            --j;
                         }
                     } else if (state == 1) {
                         op = 'D';
-                        if (!eopen) { v += ge; } else { v += go; state = 0; }
+                        if (Hv(i, j - 1) - go == v) { v += go; state = 0; } else { v += ge; }
                         --j;
                     } else {
                         op = 'I';
-                        if (!fopen) { v += ge; } else { v += go; state = 0; }
+                        if (Hv(i - 1, j) - go == v) { v += go; state = 0; } else { v += ge; }
                         --i;
                     }
                     if (pos <= 0) {
@@ -530,7 +553,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                         A.out_len[p] = m + n - pos;
                     }
                 } else {
-                    // next tile: the block above (left its top) or the tile to the left
+                    // next window: the block above (left its top) or the tiles to the left
                     if (i < i0) ti0[x] = ((i - 1) / CK_K) * CK_K + 1;
                     tb[x] = (j - 1) / TW;
                 }
@@ -546,7 +569,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 int64_t sw16ck_dir_words(int M, int N)
 {
     const int64_t ncol = ck_ncol(N);
-    return 2 * (int64_t)ck_rows(M) * ncol + 2 * (ncol / TW) * (int64_t)M + 2 * (int64_t)(CK_K + 7) * 32;
+    return 2 * (int64_t)ck_rows(M) * ncol + (2 * (ncol / TW) * (int64_t)M + 3) / 4 * 4 + (int64_t)CK_K * TG * TW;
 }
 
 static size_t sw16ck_smem() { return (size_t)4 * 2 * 4 * (CK_C / 2) * 32 * sizeof(uint32_t); }
