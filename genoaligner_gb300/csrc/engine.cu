@@ -598,14 +598,15 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err)
 // trace kernel (eligible pure-ACGT pairs) or to the 32-bit kernel, per band
 // width, largest first; per-slot direction-table and band-edge sizes.
 struct SwPlan {
-    std::vector<int32_t> w32[3];     // pair indices, 32-bit kernel, widths 8 / 16 / 32
-    std::vector<int32_t> w16[3];     // 2 pair indices per item, 16-bit kernel
+    std::vector<int32_t> w32[3];     // pair indices, 32-bit kernel, widths 8 / 16 / 32 (host-built plans)
+    std::vector<int32_t> w16[3];     // 2 pair indices per item, 16-bit kernel (host-built plans)
+    int64_t n32[3] = {0, 0, 0}, n16[3] = {0, 0, 0};   // ints of each list in the flattened work array
     int64_t dir32[3] = {0, 0, 0}, dir16[3] = {0, 0, 0};
     int64_t edge_slot = 2;
     int64_t words() const
     {
         int64_t s = 0;
-        for (int k = 0; k < 3; ++k) s += (int64_t)w32[k].size() + (int64_t)w16[k].size();
+        for (int k = 0; k < 3; ++k) s += n32[k] + n16[k];
         return s;
     }
 };
@@ -685,6 +686,44 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
         }
         P.dir16[k] = (P.dir16[k] + 3) / 4 * 4;
     }
+    for (int k = 0; k < 3; ++k) {
+        P.n32[k] = (int64_t)P.w32[k].size();
+        P.n16[k] = (int64_t)P.w16[k].size();
+    }
+}
+
+// The checkpointed kernels' plan, built on the device (sw_plan.cu) into
+// `dwork`; reads back its record and fills P's list lengths and sizes.
+static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, int64_t cell_limit,
+                                  int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
+                                  long long* dres, long long* hres, cudaStream_t st, SwPlan& P)
+{
+    static const bool use16_ok = [] {
+        const char* e = getenv("GA_SW16");
+        return !(e && e[0] == '0');
+    }();
+    SwPlanArgs A;
+    A.D = D;
+    A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
+    A.cell_limit = cell_limit;
+    A.use16 = use16_ok ? 1 : 0;
+    A.too_large_score = too_large_score;
+    A.out_score = out_score;
+    A.work = dwork;
+    A.res = dres;
+    cudaError_t e = launch_sw_plan(A, scratch, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hres, dres, sizeof(long long) * SP_RES, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    P = SwPlan();
+    for (int k = 0; k < 3; ++k) {
+        P.n16[k] = hres[SP_INTS + k];
+        P.n32[k] = hres[SP_INTS + 3 + k];
+        P.dir16[k] = (hres[SP_DIR + k] + 3) / 4 * 4;
+        P.dir32[k] = (hres[SP_DIR + 3 + k] + 3) / 4 * 4;
+    }
+    P.edge_slot = std::max<int64_t>(2, hres[SP_EDGE]);
+    return cudaSuccess;
 }
 
 // Slots (resident warps) per launch and the direction-table words the launches
@@ -699,18 +738,18 @@ static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
     SwSlots S;
     const int64_t budget = (int64_t)96 << 30;          // direction-table / checkpoint cap, bytes
     for (int k = 0; k < 3; ++k) {
-        if (!P.w32[k].empty()) {
+        if (P.n32[k] > 0) {
             int s = (trace && use_sw16ck() && k < 2) ? sw32ck_max_slots(k == 1, sm_count)
                                                      : sw_max_slots(kWidths[k], trace, sm_count);
-            s = (int)std::min<int64_t>(s, ((int64_t)P.w32[k].size() + 3) / 4 * 4);
+            s = (int)std::min<int64_t>(s, (P.n32[k] + 3) / 4 * 4);
             if (trace && P.dir32[k] > 0) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir32[k] * 4) / 4 * 4));
             S.s32[k] = s;
             if (trace) S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir32[k]);
             S.max_slots = std::max<int64_t>(S.max_slots, s);
         }
-        if (!P.w16[k].empty()) {
+        if (P.n16[k] > 0) {
             int s = (use_sw16ck() && k == 0) ? sw16ck_max_slots(sm_count) : sw16_max_slots(kWidths[k], sm_count);
-            s = (int)std::min<int64_t>(s, ((int64_t)P.w16[k].size() / 2 + 3) / 4 * 4);
+            s = (int)std::min<int64_t>(s, (P.n16[k] / 2 + 3) / 4 * 4);
             s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
             S.s16[k] = s;
             S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir16[k]);
@@ -729,9 +768,9 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
 {
     int64_t base = 0;
     for (int k = 0; k < 3; ++k) {
-        if (!P.w16[k].empty()) {
+        if (P.n16[k] > 0) {
             Sw16Args A;
-            A.D = D; A.work = dwork + base; A.nwork = (int32_t)(P.w16[k].size() / 2);
+            A.D = D; A.work = dwork + base; A.nwork = (int32_t)(P.n16[k] / 2);
             A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
@@ -740,12 +779,12 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
                                                            : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
         }
-        base += (int64_t)P.w16[k].size();
+        base += P.n16[k];
     }
     for (int k = 0; k < 3; ++k) {
-        if (!P.w32[k].empty()) {
+        if (P.n32[k] > 0) {
             SwArgs A;
-            A.D = D; A.work = dwork + base; A.nwork = (int32_t)P.w32[k].size();
+            A.D = D; A.work = dwork + base; A.nwork = (int32_t)P.n32[k];
             A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir32[k]; A.edge = edge; A.edge_slot = P.edge_slot;
@@ -754,7 +793,7 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
                                                                    : launch_sw(A, kWidths[k], trace, S.s32[k], st);
             if (e != cudaSuccess) return e;
         }
-        base += (int64_t)P.w32[k].size();
+        base += P.n32[k];
     }
     return cudaSuccess;
 }
@@ -835,7 +874,8 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     in_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hcg, &her);
     in_layout(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
     const size_t dev_fixed = dk.off;
-    if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    // (+ room after the staging blocks for the device plan's record)
+    if (!ensure_host(c, hk.off + 512 + sizeof(long long) * SP_RES)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
     // stage inputs (device scratch is sized after planning)
     {
         Carve k(c->host);
@@ -853,72 +893,105 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     });
     std::memset(hseq + arena - 64, 0, 64);
 
-    // device memory: fixed blocks, then counters, band edges and direction tables
-    // (sized from the plan; a first pass reserves the fixed part)
-    if (fail_here(1) || !ensure_dev(c, dev_fixed + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    {
-        Carve k(c->dev);
-        in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+    // device memory: fixed blocks, then (device-built plans) the planner's scratch,
+    // then counters, band edges and direction tables (sized from the plan; a
+    // first pass reserves the fixed part)
+    const bool dplan = trace && use_sw16ck();
+    const size_t plan_off = dev_fixed;
+    size_t plan_end = plan_off;
+    int32_t* dscr = nullptr;
+    long long* dres = nullptr;
+    if (dplan) {
+        Carve k(nullptr);
+        k.off = plan_off;
+        k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+        k.take<long long>(SP_RES);
+        plan_end = k.off;
     }
+    const size_t hres_off = ((size_t)((char*)(her + 1) - c->host) + 255) & ~(size_t)255;
+    if (fail_here(1) || !ensure_dev(c, plan_end + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    long long* hres = dplan ? reinterpret_cast<long long*>(c->host + hres_off) : nullptr;
     const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
     t_h2d = (int64_t)in_bytes;
-    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_H2D;
-        return GA_DEVICE_ERROR;
-    }
     PairDesc D;
-    D.seq = dseq; D.packed = nullptr; D.pure = dpure;
-    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
-    if (fail_here(3) || launch_pack(D, arena, nullptr, dpure, c->stream) != cudaSuccess ||
-        cudaMemcpyAsync(hpure, dpure, 2 * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-        cudaStreamSynchronize(c->stream) != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_LAUNCH;
-        return GA_DEVICE_ERROR;
-    }
+    D.packed = nullptr;
+    D.n = n;
     SwPlan P;
-    plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, P);
-    const SwSlots S = size_sw(P, trace, c->sm_count);
-    const uint64_t gen_before = c->dev_gen;
-    Carve extra(nullptr);
-    extra.off = dev_fixed;
-    int32_t* dctr = extra.take<int32_t>(8, 4);
-    int32_t* dedge = extra.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-    uint32_t* ddirs = trace ? extra.take<uint32_t>((size_t)S.dir_words) : nullptr;
-    if (!ensure_dev(c, extra.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    // ensure_dev may have moved the arena: re-carve and re-send if so
-    {
-        Carve k(c->dev);
-        in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
-        if (c->dev_gen != gen_before) {          // the arena moved: send the inputs again
-            if (cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+    // inputs to the device, purity flags, and the plan (host-built, or on the
+    // device for the checkpointed kernels); again from the start if the arena moves
+    auto stage = [&](bool first_time) -> int32_t {
+        {
+            Carve k(c->dev);
+            in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+            if (dplan) {
+                k.off = plan_off;
+                dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+                dres = k.take<long long>(SP_RES);
+            }
+        }
+        D.seq = dseq; D.pure = dpure;
+        D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
+        if ((first_time && fail_here(2)) ||
+            cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *err = E_H2D;
+            return GA_DEVICE_ERROR;
+        }
+        // sentinel: too-large pairs keep score -1 (never written by a kernel)
+        cudaMemsetAsync(dsc, 0xff, sizeof(int32_t) * (size_t)n, c->stream);
+        cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, c->stream);
+        cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, c->stream);
+        cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream);
+        if ((first_time && fail_here(3)) || launch_pack(D, arena, nullptr, dpure, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *err = E_LAUNCH;
+            return GA_DEVICE_ERROR;
+        }
+        if (dplan) {
+            if (device_plan_sw(D, s0, cell_limit, -1, dsc, dwork, dscr, dres, hres, c->stream, P) != cudaSuccess) {
                 cudaGetLastError();
-                *err = E_H2D;
+                *err = E_LAUNCH;
                 return GA_DEVICE_ERROR;
             }
-            D.seq = dseq; D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
-            D.pure = dpure;
-            cudaMemcpyAsync(dpure, hpure, 2 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+            return GA_OK;
         }
-        Carve e(c->dev);
-        e.off = dev_fixed;
-        dctr = e.take<int32_t>(8, 4);
-        dedge = e.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-        ddirs = trace ? e.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        if (first_time) {
+            if (cudaMemcpyAsync(hpure, dpure, 2 * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess) {
+                cudaGetLastError();
+                *err = E_LAUNCH;
+                return GA_DEVICE_ERROR;
+            }
+            plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, P);
+            flatten_plan(P, hwork);
+        }
+        if (P.words() > 0 &&
+            cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)P.words(), cudaMemcpyHostToDevice, c->stream) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            *err = E_H2D;
+            return GA_DEVICE_ERROR;
+        }
+        return GA_OK;
+    };
+    if (int32_t rs = stage(true)) return rs;
+    const SwSlots S = size_sw(P, trace, c->sm_count);
+    const uint64_t gen_before = c->dev_gen;
+    auto extra_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
+        Carve k(base);
+        k.off = plan_end;
+        *ctr = k.take<int32_t>(8, 4);
+        *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+        *dirs = trace ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        return k.off;
+    };
+    int32_t *dctr, *dedge;
+    uint32_t* ddirs;
+    if (!ensure_dev(c, extra_layout(nullptr, &dctr, &dedge, &ddirs))) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
+    if (c->dev_gen != gen_before) {              // the arena moved: everything again in the new one
+        if (int32_t rs = stage(false)) return rs;
     }
-    flatten_plan(P, hwork);
-    const int64_t nw = P.words();
-    if ((nw > 0 && cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)nw, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)) {
-        cudaGetLastError();
-        *err = E_H2D;
-        return GA_DEVICE_ERROR;
-    }
-    // sentinel: too-large pairs keep score -1 (never written by a kernel)
-    cudaMemsetAsync(dsc, 0xff, sizeof(int32_t) * (size_t)n, c->stream);
-    cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, c->stream);
-    cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, c->stream);
-    cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream);
+    extra_layout(c->dev, &dctr, &dedge, &ddirs);
     cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
     if (launch_plan(P, S, D, s0, trace, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -1264,6 +1337,90 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (trace && use_sw16ck()) {
+        // the checkpointed kernels: purity and the plan on the device, one small
+        // record back, then the launches
+        auto plan_layout = [&](char* base, uint8_t** pp, int32_t** scr, int32_t** wk, long long** res) {
+            Carve k(base);
+            *pp = k.take<uint8_t>(2 * (size_t)n);
+            *scr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+            *wk = k.take<int32_t>(2 * (size_t)n + 8);
+            *res = k.take<long long>(SP_RES);
+            return k.off;
+        };
+        uint8_t* dpure;
+        int32_t *dscr, *dwork;
+        long long* dres;
+        const size_t plan_bytes = plan_layout(nullptr, &dpure, &dscr, &dwork, &dres);
+        if (!ensure_dev(c, plan_bytes + 4096) || !ensure_host(c, sizeof(long long) * SP_RES)) {
+            release_ctx(c);
+            if (err) *err = E_ALLOC;
+            return GA_DEVICE_ERROR;
+        }
+        long long* hres = reinterpret_cast<long long*>(c->host);
+        PairDesc D;
+        D.seq = b->seq; D.packed = nullptr;
+        D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+        D.out_off = b->out_off; D.n = n;
+        cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
+        cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
+        cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
+        SwPlan P;
+        auto plan = [&]() {
+            plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
+            D.pure = dpure;
+            if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
+            return device_plan_sw(D, sc, cell_limit, -2, out_score, dwork, dscr, dres, hres, st, P) == cudaSuccess;
+        };
+        if (!plan()) {
+            cudaGetLastError();
+            release_ctx(c);
+            if (err) *err = E_LAUNCH;
+            return GA_DEVICE_ERROR;
+        }
+        const SwSlots S = size_sw(P, true, c->sm_count);
+        auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
+            Carve k(base);
+            k.off = plan_bytes;
+            *ctr = k.take<int32_t>(64, 256);
+            *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+            *dirs = k.take<uint32_t>((size_t)S.dir_words);
+            return k.off;
+        };
+        int32_t *dctr, *dedge;
+        uint32_t* ddirs;
+        const uint64_t gen_before = c->dev_gen;
+        if (!ensure_dev(c, run_layout(nullptr, &dctr, &dedge, &ddirs))) {
+            release_ctx(c);
+            if (err) *err = E_ALLOC;
+            return GA_DEVICE_ERROR;
+        }
+        if (c->dev_gen != gen_before && !plan()) {      // the arena moved: plan again in the new one
+            cudaGetLastError();
+            release_ctx(c);
+            if (err) *err = E_LAUNCH;
+            return GA_DEVICE_ERROR;
+        }
+        run_layout(c->dev, &dctr, &dedge, &ddirs);
+        cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+        int32_t rc = GA_OK;
+        if (launch_plan(P, S, D, sc, true, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+                        dctr + 32, st) != cudaSuccess) {
+            cudaGetLastError();
+            if (err) *err = E_LAUNCH;
+            rc = GA_DEVICE_ERROR;
+        }
+        if (stream) {
+            cudaEventRecord(c->done, st);
+            c->pending = true;
+        } else if (cudaStreamSynchronize(st) != cudaSuccess) {
+            cudaGetLastError();
+            if (err) *err = E_SYNC;
+            rc = GA_DEVICE_ERROR;
+        }
+        release_ctx(c);
+        return rc;
+    }
     // purity flags on the device, then lengths and flags to the host for the plan
     {
         Carve k(nullptr);
@@ -1430,7 +1587,7 @@ const char* ga_profile_kernel_name(int32_t kernel_id)
 {
     static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
                                          "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
-                                         "kmer_sketch", "mlp", "sw16x2_trace", "route"};
+                                         "kmer_sketch", "mlp", "sw16x2_trace", "route", "sw_plan"};
     return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
 }
 

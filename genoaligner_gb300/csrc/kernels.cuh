@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "sw_sizes.cuh"
 
 namespace ga {
 
@@ -104,15 +105,35 @@ int sw_width_for(int n);
 int sw_max_slots(int C, bool trace, int sm_count);
 cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
 
-bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge);
 // Checkpointed traceback kernels (sw16ck.cu: two 16-bit pairs per warp;
 // sw32ck.cu: one 32-bit pair per warp); dir_slot = their *_dir_words.
-// sw32ck has a short-pair shape and a long-pair shape (sw32ck_long).
-bool sw32ck_long(int m, int n);
-int64_t sw32ck_dir_words(int m, int n);
+// The device-built traceback plan (sw_plan.cu).  Lists, in launch order: the
+// 16-bit lists of widths 8 / 16 / 32 columns per lane, then the 32-bit ones;
+// with the checkpointed kernels only list 0 (sw16ck), 3 (sw32ck short shape)
+// and 4 (sw32ck long shape) are used.  The record `res` (SP_RES long longs):
+// per list its pair count, its length in the flattened work array and its
+// offset there, the largest per-warp memory of its items (32-bit words), and
+// the band-edge slot (2 * the longest text).
+constexpr int SP_LISTS = 6, SP_L16 = 0, SP_L32 = 3, SP_L32LONG = 4;
+constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_RES = 25;
+struct SwPlanArgs {
+    PairDesc D;                  // a = text (rows), b = pattern (columns); D.pure set
+    int32_t match, mismatch, gap_open, gap_extend;
+    int64_t cell_limit;          // traceback limit in cells, < 0: none
+    int32_t use16;               // the 16-bit kernels may be used
+    int32_t too_large_score;     // score written for pairs above cell_limit
+    int32_t* out_score;
+    int32_t* work;               // flattened work lists (2n + 8 ints)
+    long long* res;              // the record above
+    int32_t *item, *counts, *starts, *sorted;   // scratch, set by launch_sw_plan
+};
+int64_t sw_plan_scratch_ints(int n);
+cudaError_t launch_sw_plan(SwPlanArgs P, int32_t* scratch, cudaStream_t st);
+
+// sw32ck has a short-pair shape and a long-pair shape (sw32ck_long); sizes
+// in sw_sizes.cuh.
 int sw32ck_max_slots(bool long_pairs, int sm_count);
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st);
-int64_t sw16ck_dir_words(int M, int N);
 int sw16ck_max_slots(int sm_count);
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st);
 int64_t sw16_dir_words(int M, int N, int C);

@@ -28,7 +28,6 @@
 
 namespace ga {
 
-constexpr int BIAS16 = 1024;
 
 __device__ __forceinline__ int code2_16(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
 
@@ -284,14 +283,6 @@ __global__ void __launch_bounds__(128) sw16_kernel(Sw16Args A)
             }
         }
     }
-}
-
-bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge)
-{
-    if (m <= 0 || n <= 0) return false;
-    if (go + ge >= BIAS16 || mismatch + go < 0 || match + go > 32000) return false;
-    const int64_t top = (int64_t)match * (m < n ? m : n) + BIAS16 + go;
-    return top < 32000;
 }
 
 int64_t sw16_dir_words(int M, int N, int C)

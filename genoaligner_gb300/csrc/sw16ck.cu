@@ -35,28 +35,9 @@
 
 namespace ga {
 
-constexpr int CK_K = 64;                 // rows per checkpoint block
-constexpr int TW = 64;                   // tile width: a group of 8 lanes x 8 columns
-constexpr int TG = 4;                    // tiles recomputed per pass: the walk's and the 3 to its left
-constexpr int CK_BIAS = 1024;            // value bias of the recompute pass
-constexpr int CK_C = 16;                 // forward columns per lane, full bands
-constexpr int CK_BW = 32 * CK_C;         // forward band width, full bands
-
-__host__ __device__ inline int ck_rows(int M) { return M > 1 ? (M - 1) / CK_K : 0; }
-
-// Forward bands: full bands of CK_BW columns while more than CK_BW columns
-// remain, then one band of 32 * CB columns with the smallest CB in
-// {2, 4, 8, 16} that reaches column N.
-__host__ __device__ inline int ck_last_cb(int rest)
-{
-    return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : (rest > 2 * 32 ? 4 : 2));
-}
-// Columns the forward bands cover (the column extent of the checkpoints).
-__host__ __device__ inline int ck_ncol(int N)
-{
-    const int full = N > 0 ? (N - 1) / CK_BW : 0;
-    return full * CK_BW + 32 * ck_last_cb(N - full * CK_BW);
-}
+constexpr int TW = CK_TW;                // tile width: a group of 8 lanes x 8 columns
+constexpr int TG = CK_TG;                // tiles recomputed per pass: the walk's and the 3 to its left
+constexpr int CK_BIAS = BIAS16;          // value bias of the recompute pass
 
 __device__ __forceinline__ int ck_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
 __device__ __forceinline__ int lo16s(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
@@ -561,15 +542,6 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
             __syncwarp();
         }
     }
-}
-
-// Words of one warp slot for an item of at most M rows and N columns:
-// checkpoint rows, column edges, the two tile tables.  The kernel runs 8
-// columns per lane; other widths are not served.
-int64_t sw16ck_dir_words(int M, int N)
-{
-    const int64_t ncol = ck_ncol(N);
-    return 2 * (int64_t)ck_rows(M) * ncol + (2 * (ncol / TW) * (int64_t)M + 3) / 4 * 4 + (int64_t)CK_K * TG * TW;
 }
 
 static size_t sw16ck_smem() { return (size_t)4 * 2 * 4 * (CK_C / 2) * 32 * sizeof(uint32_t); }

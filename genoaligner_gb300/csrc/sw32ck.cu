@@ -31,17 +31,7 @@
 
 namespace ga {
 
-constexpr int C32_C = 16;                // forward columns per lane, full bands
-constexpr int C32_BW = 32 * C32_C;
 constexpr int C32_PAD = -(1 << 28);      // score past a pattern's end: below any reachable value
-
-__host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
-__host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }
-__host__ __device__ inline int c32_ncol(int n)
-{
-    const int full = n > 0 ? (n - 1) / C32_BW : 0;
-    return full * C32_BW + 32 * c32_last_cb(n - full * C32_BW);
-}
 
 __device__ __forceinline__ int c32_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
 
@@ -442,21 +432,6 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
             A.out_len[p] = m + n - pos;
         }
     }
-}
-
-// The long-pair shape serves pairs above this many cells.
-constexpr int64_t C32_LONG_CELLS = (int64_t)1 << 24;
-
-bool sw32ck_long(int m, int n) { return (int64_t)m * n > C32_LONG_CELLS; }
-
-// Words of one warp slot for a pair of m rows and n columns: checkpoint rows,
-// column edges, the tile table.
-int64_t sw32ck_dir_words(int m, int n)
-{
-    const bool lg = sw32ck_long(m, n);
-    const int K = lg ? 512 : 64, CT = lg ? 16 : 2, TW = 32 * CT, NWT = CT >= 8 ? CT / 8 : 1;
-    const int64_t stride = ((int64_t)c32_ncol(n) + TW - 1) / TW * TW;
-    return 2 * (int64_t)c32_rows(m, K) * stride + 2 * (stride / TW) * (int64_t)m + (int64_t)(K + 31) * 32 * NWT;
 }
 
 template <int K, int CT>

@@ -1,0 +1,172 @@
+// sw_plan.cu -- the Smith-Waterman traceback work plan, built on the device.
+//
+// The plan sorts the pairs of a batch into the kernels' work lists, largest
+// first: the two-pairs-per-warp 16-bit list (pure-ACGT pairs whose scores fit
+// 16 bits; consecutive entries share a warp) and the 32-bit lists (short and
+// long shapes of sw32ck.cu).  It is a counting sort on a log-scale size key
+// (64 buckets per doubling of (m + 31) * n) in four kernels -- classify and
+// count, scan, scatter, pack -- and leaves on the device the work lists in
+// the order the launches read them plus, per list, its length and the largest
+// per-warp memory its items need; the host reads back that one small record.
+#include "kernels.cuh"
+
+namespace ga {
+
+constexpr int SP_NB = 4096;              // size buckets per list
+
+// Bucket of a pair of m rows and n columns, largest first.
+__device__ __forceinline__ int sp_key(int m, int n)
+{
+    const uint64_t c = (uint64_t)(max(m, 0) + 31) * (uint64_t)max(n, 1);
+    const int lz = __clzll((long long)c), e = 63 - lz;
+    const int frac = (int)(((c << lz) >> 57) & 63u);
+    return SP_NB - 1 - min(SP_NB - 1, e * 64 + frac);
+}
+
+__global__ void sp_classify_kernel(SwPlanArgs P)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = P.D.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); p0 < n; p0 += stride) {
+        const int p = p0 + lane;
+        int it = -1;
+        if (p < n) {
+            const int m = P.D.a_len[p], nn = P.D.b_len[p];
+            if (P.cell_limit >= 0 && m > 0 && nn > 0 && ((int64_t)m + 1) * ((int64_t)nn + 1) > P.cell_limit) {
+                P.out_score[p] = P.too_large_score;                  // too large: no trace
+            } else {
+                const bool u16 = P.use16 && P.D.pure[p] && P.D.pure[n + p] &&
+                                 sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
+                const int list = u16 ? SP_L16 : (sw32ck_long(m, nn) ? SP_L32LONG : SP_L32);
+                it = list * SP_NB + sp_key(m, nn);
+                atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_EDGE), (unsigned long long)(2 * max(m, 0)));
+            }
+            P.item[p] = it;
+        }
+        const unsigned same = __match_any_sync(FULL, it);
+        if (it >= 0 && lane == __ffs(same) - 1) atomicAdd(&P.counts[it], __popc(same));
+    }
+}
+
+// One warp per list: exclusive scan of its bucket counts (bucket order is
+// largest first), then the lists' lengths in the flattened work array and
+// their offsets there (16-bit lists hold two entries per warp item).
+__global__ void sp_scan_kernel(SwPlanArgs P)
+{
+    __shared__ long long total[SP_LISTS];
+    const int lane = threadIdx.x & 31, L = threadIdx.x >> 5;
+    if (L < SP_LISTS) {
+        const int per = SP_NB / 32;
+        const int32_t* cnt = P.counts + L * SP_NB + lane * per;
+        int32_t* st = P.starts + L * SP_NB + lane * per;
+        int sum = 0;
+        for (int b = 0; b < per; ++b) sum += cnt[b];
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int acc = incl - sum;
+        for (int b = 0; b < per; ++b) {
+            st[b] = acc;
+            acc += cnt[b];
+        }
+        if (lane == 31) total[L] = incl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long base = 0;
+        for (int l = 0; l < SP_LISTS; ++l) {
+            const long long ints = l < 3 ? 2 * ((total[l] + 1) / 2) : total[l];
+            P.res[SP_COUNT + l] = total[l];
+            P.res[SP_INTS + l] = ints;
+            P.res[SP_BASE + l] = base;
+            base += ints;
+        }
+    }
+}
+
+__global__ void sp_scatter_kernel(SwPlanArgs P)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = P.D.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); p0 < n; p0 += stride) {
+        const int p = p0 + lane;
+        const int it = p < n ? P.item[p] : -1;
+        const unsigned same = __match_any_sync(FULL, it);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (it >= 0 && lane == leader) base = atomicAdd(&P.starts[it], __popc(same));
+        base = __shfl_sync(FULL, base, leader);
+        if (it >= 0) P.sorted[(int64_t)(it / SP_NB) * n + base + __popc(same & ((1u << lane) - 1u))] = p;
+    }
+}
+
+// Work items in launch order, and each list's largest per-warp memory.
+__global__ void sp_pack_kernel(SwPlanArgs P)
+{
+    const int n = P.D.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int l = 0; l < SP_LISTS; ++l) {
+        const long long cnt = P.res[SP_COUNT + l];
+        if (cnt == 0) continue;
+        const int32_t* srt = P.sorted + (int64_t)l * n;
+        int32_t* w = P.work + P.res[SP_BASE + l];
+        unsigned long long* mx = reinterpret_cast<unsigned long long*>(P.res + SP_DIR + l);
+        unsigned long long local = 0;
+        if (l < 3) {
+            const long long items = (cnt + 1) / 2;
+            for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < items; q += stride) {
+                const int a = srt[2 * q], b = 2 * q + 1 < cnt ? srt[2 * q + 1] : -1;
+                w[2 * q] = a;
+                w[2 * q + 1] = b;
+                const int M = max(P.D.a_len[a], b >= 0 ? P.D.a_len[b] : 0);
+                const int N = max(P.D.b_len[a], b >= 0 ? P.D.b_len[b] : 0);
+                local = max(local, (unsigned long long)sw16ck_dir_words(M, N));
+            }
+        } else {
+            for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += stride) {
+                const int a = srt[q];
+                w[q] = a;
+                local = max(local, (unsigned long long)sw32ck_dir_words(P.D.a_len[a], P.D.b_len[a]));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) local = max(local, __shfl_xor_sync(FULL, local, o));
+        if ((threadIdx.x & 31) == 0 && local) atomicMax(mx, local);
+    }
+}
+
+int64_t sw_plan_scratch_ints(int n) { return (int64_t)n + 2 * SP_LISTS * SP_NB + (int64_t)SP_LISTS * n; }
+
+cudaError_t launch_sw_plan(SwPlanArgs P, int32_t* scratch, cudaStream_t st)
+{
+    const int n = P.D.n;
+    P.item = scratch;
+    P.counts = scratch + n;
+    P.starts = P.counts + SP_LISTS * SP_NB;
+    P.sorted = P.starts + SP_LISTS * SP_NB;
+    cudaError_t e = cudaMemsetAsync(P.counts, 0, sizeof(int32_t) * SP_LISTS * SP_NB, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P.res, 0, sizeof(long long) * SP_RES, st);
+    if (e != cudaSuccess || n <= 0) return e;
+    int blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    launch_begin(K_SWPLAN, st);
+    sp_classify_kernel<<<blocks, 256, 0, st>>>(P);
+    launch_end(K_SWPLAN, st);
+    launch_begin(K_SWPLAN, st);
+    sp_scan_kernel<<<1, 32 * SP_LISTS, 0, st>>>(P);
+    launch_end(K_SWPLAN, st);
+    launch_begin(K_SWPLAN, st);
+    sp_scatter_kernel<<<blocks, 256, 0, st>>>(P);
+    launch_end(K_SWPLAN, st);
+    launch_begin(K_SWPLAN, st);
+    sp_pack_kernel<<<blocks, 256, 0, st>>>(P);
+    launch_end(K_SWPLAN, st);
+    return cudaGetLastError();
+}
+
+}  // namespace ga

@@ -1,0 +1,82 @@
+// sw_sizes.cuh -- shapes, eligibility and per-warp memory of the
+// Smith-Waterman traceback kernels, shared by the kernels (sw16.cu,
+// sw16ck.cu, sw32ck.cu), the device planner (sw_plan.cu) and the host.
+#pragma once
+
+#include <cstdint>
+
+namespace ga {
+
+// ---- 16-bit two-pairs-per-warp kernels --------------------------------------
+// Every value is stored as value + BIAS16 so each 16-bit half stays in
+// [0, 32767].  A pair qualifies when both sides are pure ACGT and
+// match * min(m, n) + BIAS16 + gap_open < 32000, gap_open + gap_extend < BIAS16
+// and mismatch + gap_open >= 0 (host-side check; purity comes from the device).
+constexpr int BIAS16 = 1024;
+
+__host__ __device__ inline bool sw16_eligible(int m, int n, int match, int mismatch, int go, int ge)
+{
+    if (m <= 0 || n <= 0) return false;
+    if (go + ge >= BIAS16 || mismatch + go < 0 || match + go > 32000) return false;
+    const int64_t top = (int64_t)match * (m < n ? m : n) + BIAS16 + go;
+    return top < 32000;
+}
+
+// sw16ck.cu: checkpoint rows every CK_K rows, column edges every CK_TW
+// columns, recompute windows of CK_TG tiles of CK_K x CK_TW cells.
+constexpr int CK_K = 64;
+constexpr int CK_TW = 64;
+constexpr int CK_TG = 4;
+constexpr int CK_C = 16;                 // forward columns per lane, full bands
+constexpr int CK_BW = 32 * CK_C;         // forward band width, full bands
+
+__host__ __device__ inline int ck_rows(int M) { return M > 1 ? (M - 1) / CK_K : 0; }
+
+// Forward bands: full bands of CK_BW columns while more than CK_BW columns
+// remain, then one band of 32 * CB columns with the smallest CB in
+// {2, 4, 8, 16} that reaches column N.
+__host__ __device__ inline int ck_last_cb(int rest)
+{
+    return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : (rest > 2 * 32 ? 4 : 2));
+}
+// Columns the forward bands cover (the column extent of the checkpoints).
+__host__ __device__ inline int ck_ncol(int N)
+{
+    const int full = N > 0 ? (N - 1) / CK_BW : 0;
+    return full * CK_BW + 32 * ck_last_cb(N - full * CK_BW);
+}
+
+// 32-bit words of one warp slot for an item of at most M rows and N columns:
+// checkpoint rows, column edges (16-byte aligned end), the window table.
+__host__ __device__ inline int64_t sw16ck_dir_words(int M, int N)
+{
+    const int64_t ncol = ck_ncol(N);
+    return 2 * (int64_t)ck_rows(M) * ncol + (2 * (ncol / CK_TW) * (int64_t)M + 3) / 4 * 4 +
+           (int64_t)CK_K * CK_TG * CK_TW;
+}
+
+// ---- 32-bit one-pair-per-warp checkpointed kernel (sw32ck.cu) ---------------
+constexpr int C32_C = 16;                // forward columns per lane, full bands
+constexpr int C32_BW = 32 * C32_C;
+constexpr int64_t C32_LONG_CELLS = (int64_t)1 << 24;   // the long-pair shape above this many cells
+
+__host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
+__host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }
+__host__ __device__ inline int c32_ncol(int n)
+{
+    const int full = n > 0 ? (n - 1) / C32_BW : 0;
+    return full * C32_BW + 32 * c32_last_cb(n - full * C32_BW);
+}
+__host__ __device__ inline bool sw32ck_long(int m, int n) { return (int64_t)m * n > C32_LONG_CELLS; }
+
+// 32-bit words of one warp slot for a pair of m rows and n columns:
+// checkpoint rows, column edges, the tile table.
+__host__ __device__ inline int64_t sw32ck_dir_words(int m, int n)
+{
+    const bool lg = sw32ck_long(m, n);
+    const int K = lg ? 512 : 64, CT = lg ? 16 : 2, TW = 32 * CT, NWT = CT >= 8 ? CT / 8 : 1;
+    const int64_t stride = ((int64_t)c32_ncol(n) + TW - 1) / TW * TW;
+    return 2 * (int64_t)c32_rows(m, K) * stride + 2 * (stride / TW) * (int64_t)m + (int64_t)(K + 31) * 32 * NWT;
+}
+
+}  // namespace ga
