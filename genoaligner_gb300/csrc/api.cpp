@@ -117,9 +117,15 @@ SWBatchResult align_sw_batch_ex(const std::vector<SWRequest>& reqs, const AlignO
             r.start_j = v.pos[4 * i + 1];
             if (v.len[i] > 0) {
                 r.cigar.assign(v.cig + v.slot_end[i] - v.len[i], (size_t)v.len[i]);
-                ga::sw_validate(r.cigar.data(), (int)r.cigar.size(), reqs[(size_t)i].text, reqs[(size_t)i].text_len,
-                                r.start_i, r.end_i, reqs[(size_t)i].pattern, reqs[(size_t)i].pattern_len, r.start_j,
-                                r.end_j, cr[(size_t)i].scoring, s, &r.rescore_ok, &r.wellformed_ok);
+                if (v.vflags) {
+                    r.rescore_ok = v.vflags[i] & 1;
+                    r.wellformed_ok = (v.vflags[i] >> 1) & 1;
+                } else {
+                    ga::sw_validate(r.cigar.data(), (int)r.cigar.size(), reqs[(size_t)i].text,
+                                    reqs[(size_t)i].text_len, r.start_i, r.end_i, reqs[(size_t)i].pattern,
+                                    reqs[(size_t)i].pattern_len, r.start_j, r.end_j, cr[(size_t)i].scoring, s,
+                                    &r.rescore_ok, &r.wellformed_ok);
+                }
             }
         }
         resolved.fetch_add(res);

@@ -855,11 +855,11 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     const int64_t max_work = 2 * (int64_t)n + 8;
     int64_t *ha, *hb, *ho, *da, *db, *dout;
     int32_t *hal, *hbl, *dal, *dbl, *hwork, *dwork, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der;
-    uint8_t *hseq, *dseq, *hpure, *dpure;
+    uint8_t *hseq, *dseq, *hpure, *dpure, *hvf, *dvf;
     char *hcg, *dcg;
     auto in_layout = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
                          uint8_t** ps, uint8_t** pp, int32_t** pw, int32_t** psc, int32_t** ppos, int32_t** pln,
-                         char** pcg, int32_t** per) {
+                         uint8_t** pvf, char** pcg, int32_t** per) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
         *po = k.take<int64_t>(n);
@@ -867,19 +867,20 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         *pp = k.take<uint8_t>(2 * (size_t)n);
         *pw = k.take<int32_t>(max_work);
         *psc = k.take<int32_t>(n); *ppos = k.take<int32_t>(4 * (size_t)n);
-        *pln = k.take<int32_t>(n); *pcg = k.take<char>(cig + 1);
+        *pln = k.take<int32_t>(n); *pvf = k.take<uint8_t>(n);
+        *pcg = k.take<char>(cig + 1);
         *per = k.take<int32_t>(1, 4);
     };
     Carve hk(nullptr), dk(nullptr);
-    in_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hcg, &her);
-    in_layout(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+    in_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hvf, &hcg, &her);
+    in_layout(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dvf, &dcg, &der);
     const size_t dev_fixed = dk.off;
     // (+ room after the staging blocks for the device plan's record)
     if (!ensure_host(c, hk.off + 512 + sizeof(long long) * SP_RES)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
     // stage inputs (device scratch is sized after planning)
     {
         Carve k(c->host);
-        in_layout(k, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hcg, &her);
+        in_layout(k, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hvf, &hcg, &her);
     }
     parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
         for (int64_t i = lo; i < hi; ++i) {
@@ -922,7 +923,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     auto stage = [&](bool first_time) -> int32_t {
         {
             Carve k(c->dev);
-            in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dcg, &der);
+            in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dvf, &dcg, &der);
             if (dplan) {
                 k.off = plan_off;
                 dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
@@ -993,7 +994,9 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     }
     extra_layout(c->dev, &dctr, &dedge, &ddirs);
     cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
-    if (launch_plan(P, S, D, s0, trace, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess) {
+    if (launch_plan(P, S, D, s0, trace, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess ||
+        (trace && launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
+                                     dln, dcg, dvf, c->stream) != cudaSuccess)) {
         cudaGetLastError();
         *err = E_LAUNCH;
         return GA_DEVICE_ERROR;
@@ -1011,7 +1014,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace};
+    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr};
     parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
     return GA_OK;
 }
@@ -1208,9 +1211,14 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
                 r.cigar_offset = at;
                 r.cigar_len = len;
                 bool rs = false, wf = false;
-                sw_validate(cigar_buf + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
-                            reqs[i].pattern, reqs[i].pattern_len, r.start_j, r.end_j, reqs[i].scoring, s,
-                            &rs, &wf);
+                if (v.vflags) {
+                    rs = v.vflags[i] & 1;
+                    wf = (v.vflags[i] >> 1) & 1;
+                } else {
+                    sw_validate(cigar_buf + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
+                                reqs[i].pattern, reqs[i].pattern_len, r.start_j, r.end_j, reqs[i].scoring, s,
+                                &rs, &wf);
+                }
                 r.rescore_ok = rs;
                 r.wellformed_ok = wf;
             }

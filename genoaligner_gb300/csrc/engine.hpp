@@ -42,6 +42,7 @@ struct SwView {
     const char* cig;
     const int64_t* slot_end;
     bool trace;
+    const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
 };
 using SwFinish = std::function<void(int64_t lo, int64_t hi, const SwView& v)>;
 

@@ -129,6 +129,11 @@ struct SwPlanArgs {
 };
 int64_t sw_plan_scratch_ints(int n);
 cudaError_t launch_sw_plan(SwPlanArgs P, int32_t* scratch, cudaStream_t st);
+// Result checks of every pair with a CIGAR (sw_plan.cu): flags[p] =
+// rescore_ok | wellformed_ok << 1.
+struct ga_sw_scoring_t { int32_t match, mismatch, gap_open, gap_extend; };
+cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, const int32_t* score, const int32_t* pos,
+                               const int32_t* len, const char* cig, uint8_t* flags, cudaStream_t st);
 
 // sw32ck has a short-pair shape and a long-pair shape (sw32ck_long); sizes
 // in sw_sizes.cuh.

@@ -140,6 +140,69 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
     }
 }
 
+// ------------------------------------------------------------ validation --
+// The result checks of the reference's sw_validate (src/api/api.cpp:114-156),
+// one thread per pair over its CIGAR (written at the end of its slot): the
+// ops must consume exactly the span [start, end] of both sequences, M only on
+// equal bytes and X on unequal ones (wellformed), and re-score, with each gap
+// run costing gap_open + (L - 1) * gap_extend, to the reported score
+// (rescore).  flags[p] = rescore_ok | wellformed_ok << 1 for pairs with a
+// CIGAR, 0 otherwise.
+__global__ void sw_validate_kernel(PairDesc D, int match, int mismatch, int go, int ge, const int32_t* __restrict__ score,
+                                   const int32_t* __restrict__ pos, const int32_t* __restrict__ len,
+                                   const char* __restrict__ cig, uint8_t* __restrict__ flags)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
+        const int s = score[p], L = len[p];
+        if (s <= 0 || L <= 0) { flags[p] = 0; continue; }
+        const int m = D.a_len[p], n = D.b_len[p];
+        const uint8_t* T = D.seq + D.a_off[p];
+        const uint8_t* P = D.seq + D.b_off[p];
+        const char* cg = cig + D.out_off[p] + (m + n) - L;
+        const int si = pos[4 * p], sj = pos[4 * p + 1], ei = pos[4 * p + 2], ej = pos[4 * p + 3];
+        int i = si, j = sj, total = 0, gap = 0;            // gap > 0: run of I, < 0: run of D
+        bool ok = true;
+        for (int q = 0; q < L; ++q) {
+            const char op = cg[q];
+            if (op == 'M' || op == 'X') {
+                if (gap) { total -= go + ((gap > 0 ? gap : -gap) - 1) * ge; gap = 0; }
+                if (i > ei || j > ej || i >= m || j >= n || ((T[i] == P[j]) != (op == 'M'))) ok = false;
+                total += op == 'M' ? match : mismatch;
+                ++i;
+                ++j;
+            } else if (op == 'I') {
+                if (gap < 0) { total -= go + (-gap - 1) * ge; gap = 0; }
+                if (i > ei || i >= m) ok = false;
+                ++i;
+                ++gap;
+            } else if (op == 'D') {
+                if (gap > 0) { total -= go + (gap - 1) * ge; gap = 0; }
+                if (j > ej || j >= n) ok = false;
+                ++j;
+                --gap;
+            } else {
+                ok = false;
+            }
+        }
+        if (gap) total -= go + ((gap > 0 ? gap : -gap) - 1) * ge;
+        ok = ok && i == ei + 1 && j == ej + 1;
+        flags[p] = (uint8_t)((ok && total == s ? 1 : 0) | (ok ? 2 : 0));
+    }
+}
+
+cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, const int32_t* score, const int32_t* pos,
+                               const int32_t* len, const char* cig, uint8_t* flags, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    int blocks = (D.n + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    launch_begin(K_SWPLAN, st);
+    sw_validate_kernel<<<blocks, 128, 0, st>>>(D, sc.match, sc.mismatch, sc.gap_open, sc.gap_extend, score, pos, len,
+                                               cig, flags);
+    launch_end(K_SWPLAN, st);
+    return cudaGetLastError();
+}
+
 int64_t sw_plan_scratch_ints(int n) { return (int64_t)n + 2 * SP_LISTS * SP_NB + (int64_t)SP_LISTS * n; }
 
 cudaError_t launch_sw_plan(SwPlanArgs P, int32_t* scratch, cudaStream_t st)
