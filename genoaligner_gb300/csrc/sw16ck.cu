@@ -16,10 +16,11 @@
 //      edges); per lane the best value with its first row and column;
 //   2. the best cell is the warp's (max value, min row, min column);
 //   3. walk: the tile [i0, i] x [TW*b + 1, TW*b + TW] holding the walk's
-//      current cell (i0 = the first row of its CK_K-row block) and the three
+//      current cell (i0 = the first row of its CK_K-row block) and the TG - 1
 //      tiles to its left are recomputed from the checkpoint row above them
-//      and the column edges left of them -- four groups of 8 lanes, one tile
-//      each, so the lanes' one-step lag costs 7 steps, not 31 -- and their H
+//      and the column edges left of them -- TG groups of 32 / TG lanes, one
+//      tile each, so the lanes' one-step lag costs 32 / TG - 1 steps, not
+//      31 -- and their H
 //      values are kept; the walk proceeds inside them, reading every decision
 //      off H values with the reference's tie rules (diagonal, then E, then F;
 //      a gap cell opened when its neighbour's H - gap_open equals it, E from
@@ -35,9 +36,16 @@
 
 namespace ga {
 
-constexpr int TW = CK_TW;                // tile width: a group of 8 lanes x 8 columns
-constexpr int TG = CK_TG;                // tiles recomputed per pass: the walk's and the 3 to its left
+constexpr int TW = CK_TW;                // tile width: a group of 32 / TG lanes x TW * TG / 32 columns
+constexpr int TG = CK_TG;                // tiles recomputed per pass: the walk's and the TG - 1 to its left
 constexpr int CK_BIAS = BIAS16;          // value bias of the recompute pass
+// shared memory words per warp: the forward band profile, or the window
+// profile (TW * TG / 32 columns per lane) plus the window's column edges
+constexpr int CK_FWD_WORDS = 2 * 4 * (CK_C / 2) * 32;
+constexpr int CK_WIN_WORDS = 2 * 4 * (TW * TG / 64) * 32 + 2 * TG * CK_K;
+constexpr int CK_WARP_WORDS = CK_FWD_WORDS > CK_WIN_WORDS ? CK_FWD_WORDS : CK_WIN_WORDS;
+static_assert(TG == 1 || TG == 2 || TG == 4 || TG == 8, "tile groups split the warp evenly");
+static_assert((TW * TG / 32) % 4 == 0, "window rows are stored as 16-byte vectors");
 
 __device__ __forceinline__ int ck_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
 __device__ __forceinline__ int lo16s(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
@@ -191,35 +199,35 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     __syncwarp();
 }
 
-// Tile profile of one pair for a lane of a tile group: prof[((pair * 4 +
-// letter) * 4 + h) * 32 + t] holds the 16-bit scores of the lane's columns
-// col0 + 2h, col0 + 2h + 1 (0-based); past the pattern's end or left of
-// column 0: mismatch.
+// Tile profile of one pair for a lane of a tile group (CT columns per lane):
+// prof[((pair * 4 + letter) * CT/2 + h) * 32 + t] holds the 16-bit scores of
+// the lane's columns col0 + 2h, col0 + 2h + 1 (0-based); past the pattern's
+// end or left of column 0: mismatch.
+template <int CT>
 __device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* pat, int n, int col0, int pair,
                                                 int sm, int sx, int t)
 {
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
+    for (int h = 0; h < CT / 2; ++h) {
         const int c0 = col0 + 2 * h, c1 = c0 + 1;
         const int a0 = (c0 >= 0 && c0 < n) ? ck_code(__ldg(pat + c0)) : 4;
         const int a1 = (c1 >= 0 && c1 < n) ? ck_code(__ldg(pat + c1)) : 4;
 #pragma unroll
         for (int L = 0; L < 4; ++L) {
             const int v0 = a0 == L ? sm : sx, v1 = a1 == L ? sm : sx;
-            prof[((pair * 4 + L) * 4 + h) * 32 + t] = ((uint32_t)v0 & 0xffffu) | ((uint32_t)v1 << 16);
+            prof[((pair * 4 + L) * (CT / 2) + h) * 32 + t] = ((uint32_t)v0 & 0xffffu) | ((uint32_t)v1 << 16);
         }
     }
 }
 
 __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 {
-    constexpr int NH = CK_C / 2;
     extern __shared__ uint32_t ck_smem[];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     uint32_t* wslot = A.dirs + slot * A.dir_slot;
-    uint32_t* prof = ck_smem + wib * (2 * 4 * NH * 32);
+    uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
     const int go = A.gap_open, ge = A.gap_extend;
     const int sm = A.match + go, sx = A.mismatch + go;
     // unbiased forward constants (per half)
@@ -311,19 +319,21 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
         // pairs in the 16-bit halves (biased)
         constexpr int WCOL = TG * TW;
         uint32_t* Ht = tiles;
-        const int g = t >> 3, tl = t & 7;                           // tile group, lane in group
+        constexpr int LG = 32 / TG, CT = TW / LG;                   // lanes per tile group, columns per lane
+        const int g = t / LG, tl = t % LG;                          // tile group, lane in group
         while (!(done[0] && done[1])) {
-            // ---- recompute, per pair x, the window of TG tiles tb-3 .. tb over rows
-            // [ti0, wi]: group g takes tile tb - 3 + g, lane tl its columns 8 tl .. 8 tl + 7
+            // ---- recompute, per pair x, the window of TG tiles tb-TG+1 .. tb over rows
+            // [ti0, wi]: group g takes tile tb - TG + 1 + g, lane tl its columns
+            // CT tl .. CT tl + CT - 1
             const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
             const int R = max(rows0, rows1);
-            const int steps = R + 7;
+            const int steps = R + LG - 1;
             const int tgA = tb[0] - (TG - 1) + g, tgB = tb[1] - (TG - 1) + g;   // this group's tiles
-            const int colA = TW * tgA + 8 * tl, colB = TW * tgB + 8 * tl;      // this lane's first columns
+            const int colA = TW * tgA + CT * tl, colB = TW * tgB + CT * tl;    // this lane's first columns
             __syncwarp();
-            ck_profile_tile(prof, patA, nA, colA, 0, sm, sx, t);
-            ck_profile_tile(prof, patB, nB, colB, 1, sm, sx, t);
-            uint32_t hgu[8], fv[8];
+            ck_profile_tile<CT>(prof, patA, nA, colA, 0, sm, sx, t);
+            ck_profile_tile<CT>(prof, patB, nB, colB, 1, sm, sx, t);
+            uint32_t hgu[CT], fv[CT];
             uint32_t diag_in;
             {
                 const int qa = (ti0[0] - 1) / CK_K - 1, qb = (ti0[1] - 1) / CK_K - 1;
@@ -331,7 +341,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 const uint32_t* cb = ck + 2 * (int64_t)max(qb, 0) * ncol;
                 const bool oka = qa >= 0 && tgA >= 0, okb = qb >= 0 && tgB >= 0;
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
+                for (int c = 0; c < CT; ++c) {
                     const uint2 va = oka ? *reinterpret_cast<const uint2*>(ca + 2 * (colA + c)) : make_uint2(NGO2, 0u);
                     const uint2 vb = okb ? *reinterpret_cast<const uint2*>(cb + 2 * (colB + c)) : make_uint2(NGO2, 0u);
                     hgu[c] = __viaddmax_s16x2(__byte_perm(va.x, vb.x, 0x7610), B2, MIN2);
@@ -339,7 +349,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 }
                 // H[i0-1][first column - 1] - go: the left lane's last column; for a
                 // group's first lane the checkpoint left of its tile (0 on row 0 and column 0)
-                uint32_t lft = __shfl_up_sync(FULL, hgu[7], 1, 8);
+                uint32_t lft = __shfl_up_sync(FULL, hgu[CT - 1], 1, LG);
                 if (tl == 0) {
                     const uint32_t ha = (qa >= 0 && tgA > 0) ? ca[2 * (colA - 1)] : NGO2;
                     const uint32_t hb = (qb >= 0 && tgB > 0) ? cb[2 * (colB - 1)] : NGO2;
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
             }
             // the groups' left boundaries per tile row (column edges at TW * tile),
             // combined and biased into shared memory: edg[(group * CK_K + row) * 2]
-            uint32_t* edg = prof + 2 * 4 * 4 * 32;
+            uint32_t* edg = prof + 2 * 4 * (CT / 2) * 32;
             for (int idx = t; idx < TG * CK_K; idx += 32) {
                 const int gg = idx / CK_K, r = idx - gg * CK_K;
                 const int ka = tb[0] - (TG - 1) + gg, kb = tb[1] - (TG - 1) + gg;
@@ -368,13 +378,13 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
             const uint8_t* tB = textB + (ti0[1] - 1);
             uint32_t ch = 0;
             uint32_t ch_next = tl == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
-            const uint32_t* pA0 = prof + (0 * 4 * 4) * 32 + t;
-            const uint32_t* pB0 = prof + (1 * 4 * 4) * 32 + t;
-            uint32_t* hrow = Ht + g * TW + 8 * tl;                          // + (row - 1) * WCOL
+            const uint32_t* pA0 = prof + (0 * 4 * (CT / 2)) * 32 + t;
+            const uint32_t* pB0 = prof + (1 * 4 * (CT / 2)) * 32 + t;
+            uint32_t* hrow = Ht + g * TW + CT * tl;                         // + (row - 1) * WCOL
             for (int tau = 0; tau < steps; ++tau) {
-                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, 8);
-                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, 8);
-                ch = __shfl_up_sync(FULL, ch, 1, 8);
+                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, LG);
+                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, LG);
+                ch = __shfl_up_sync(FULL, ch, 1, LG);
                 const int i = tau - tl + 1;                                  // window row, 1-based
                 if (tl == 0) {
                     ch = ch_next;
@@ -383,12 +393,12 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                     if (i <= R) { in_hg = eg[2 * (i - 1)]; in_e = eg[2 * (i - 1) + 1]; }
                 }
                 if (i < 1 || i > R) continue;
-                const uint32_t* pA = pA0 + ck_code(ch & 0xffu) * 4 * 32;
-                const uint32_t* pB = pB0 + ck_code(ch >> 8) * 4 * 32;
+                const uint32_t* pA = pA0 + ck_code(ch & 0xffu) * (CT / 2) * 32;
+                const uint32_t* pB = pB0 + ck_code(ch >> 8) * (CT / 2) * 32;
                 uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
-                uint32_t hv[8];
+                uint32_t hv[CT];
 #pragma unroll
-                for (int cc = 0; cc < 8; cc += 2) {
+                for (int cc = 0; cc < CT; cc += 2) {
                     const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
                     const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
 #pragma unroll
@@ -408,8 +418,8 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                     }
                 }
                 uint4* dst = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
-                dst[0] = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-                dst[1] = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+#pragma unroll
+                for (int c = 0; c < CT; c += 4) dst[c >> 2] = make_uint4(hv[c], hv[c + 1], hv[c + 2], hv[c + 3]);
                 diag_in = in_hg;
                 out_hg = hgl;
                 out_e = el;
@@ -423,11 +433,12 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 const int rows = x ? rows1 : rows0, n = x ? nB : nA;
                 const int wc0 = TW * (tb[x] - (TG - 1));                    // 0-based column of window column 0
                 int jf = INT32_MAX;
+                constexpr int PER = WCOL / 32;
 #pragma unroll
-                for (int c = 7; c >= 0; --c) {
-                    const int col = wc0 + 8 * t + c;
+                for (int c = PER - 1; c >= 0; --c) {
+                    const int col = wc0 + PER * t + c;
                     if (col >= 0 && col < n) {
-                        const uint32_t w = Ht[(rows - 1) * WCOL + 8 * t + c];
+                        const uint32_t w = Ht[(rows - 1) * WCOL + PER * t + c];
                         if ((int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS == best_of[x]) jf = col + 1;
                     }
                 }
@@ -544,7 +555,7 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
     }
 }
 
-static size_t sw16ck_smem() { return (size_t)4 * 2 * 4 * (CK_C / 2) * 32 * sizeof(uint32_t); }
+static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t); }
 
 int sw16ck_max_slots(int sm_count)
 {

@@ -26,7 +26,7 @@ __host__ __device__ inline bool sw16_eligible(int m, int n, int match, int misma
 // columns, recompute windows of CK_TG tiles of CK_K x CK_TW cells.
 constexpr int CK_K = 64;
 constexpr int CK_TW = 64;
-constexpr int CK_TG = 4;
+constexpr int CK_TG = 2;
 constexpr int CK_C = 16;                 // forward columns per lane, full bands
 constexpr int CK_BW = 32 * CK_C;         // forward band width, full bands
 
