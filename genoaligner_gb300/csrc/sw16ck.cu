@@ -501,6 +501,31 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
                 for (;;) {
                     if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
                     if (i < i0 || j < jlo) break;                               // left the window
+                    if (state == 0) {
+                        // a run of diagonal steps resolved at once: lane u takes the step from
+                        // cell (i - u, j - u), whose value is the H lane u - 1 read; the run
+                        // ends at the first step that is not diagonal or starts at H = 0
+                        const int U = min(min(32, pos), min(i - max(i0, 1), j - max(jlo, 1)) + 1);
+                        int hd = 0;
+                        bool eq = false;
+                        if (t < U) {
+                            eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
+                            hd = Hv(i - 1 - t, j - 1 - t);
+                        }
+                        int vu = __shfl_up_sync(FULL, hd, 1);
+                        if (t == 0) vu = v;
+                        const bool ok = t < U && vu != 0 && hd + (eq ? A.match : A.mismatch) == vu;
+                        const unsigned run = __ballot_sync(FULL, ok);
+                        const int r = run == FULL ? 32 : __ffs(~run) - 1;
+                        if (r > 0) {
+                            if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
+                            v = __shfl_sync(FULL, hd, r - 1);
+                            i -= r;
+                            j -= r;
+                            pos -= r;
+                            continue;
+                        }
+                    }
                     char op;
                     if (state == 0) {
                         const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);

@@ -381,6 +381,38 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
             for (;;) {
                 if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
                 if (i < ti0 || j < jlo) break;
+                if (state == 0) {
+                    // a run of diagonal steps resolved at once: lane u takes the step from
+                    // cell (i - u, j - u); its value is v less the scores of steps 0 .. u-1
+                    const int U = min(min(32, pos), min(i - max(ti0, 1), j - max(jlo, 1)) + 1);
+                    bool diag = false, eq = false;
+                    int s = 0;
+                    if (t < U) {
+                        const int jq = j - t - jlo;
+                        const int tq = jq / CT, cq = jq - tq * CT;
+                        const uint32_t nq = tile[(((i - t - ti0) + tq) * 32 + tq) * NWT + (cq >> 3)] >> (4 * (cq & 7));
+                        diag = (nq & 3u) == 0u;
+                        eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
+                        s = eq ? A.match : A.mismatch;
+                    }
+                    int incl = s;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y = __shfl_up_sync(FULL, incl, o);
+                        if (t >= o) incl += y;
+                    }
+                    const bool ok = t < U && diag && v - (incl - s) != 0;
+                    const unsigned run = __ballot_sync(FULL, ok);
+                    const int r = run == FULL ? 32 : __ffs(~run) - 1;
+                    if (r > 0) {
+                        if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
+                        v -= __shfl_sync(FULL, incl, r - 1);
+                        i -= r;
+                        j -= r;
+                        pos -= r;
+                        continue;
+                    }
+                }
                 const int jj = j - jlo;
                 const int tt = jj / CT, c = jj - tt * CT;
                 const uint32_t nb4 = (tile[(((i - ti0) + tt) * 32 + tt) * NWT + (c >> 3)] >> (4 * (c & 7))) & 15u;
