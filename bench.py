@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--pairs", type=int, default=200_000)
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the device's current kernel setting instead of autotuning on the batch")
     ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long"],
                     help="run one of the extra workloads alone (no CPU baseline) and print its JSON")
     return ap.parse_args()
@@ -275,6 +277,9 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
         ln = torch.empty(n, dtype=torch.int32, device=dev)
         cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
         fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
+        if learned and not args.no_tune:
+            chosen, trials = api.autotune_wfa(batch, 64, True, sc, ln, cg, reps=2)
+            out["tune"] = {"chosen": chosen, "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials]}
         for _ in range(3):
             fn()
         ms = timed(fn, stream, max(args.steps, 5), flush)
@@ -370,6 +375,15 @@ def main():
     def step():
         api.sw_device(batch, SCORING, True, out_score, out_pos, out_len, out_cig, stream=stream.cuda_stream)
 
+    # the autotuner picks this device's kernel setting on the batch itself
+    # (untimed, like the warm-up; every setting gives the same results)
+    if args.no_tune:
+        tune = {"chosen": api.tune_get(), "trials": [], "by": "built-in default"}
+    else:
+        chosen, trials = api.autotune_sw(batch, SCORING, out_score, out_pos, out_len, out_cig, reps=2)
+        tune = {"chosen": chosen, "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials],
+                "by": "ga_autotune_sw on this batch (wall time per call, coordinate search)"}
+
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
@@ -459,7 +473,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int16x2/int32", "data": "synthetic (seeded generator, seed 2)",
-            "config": {"workload": SW_WORKLOAD, "pairs": n, "cells": cells,
+            "config": {"workload": SW_WORKLOAD, "pairs": n, "cells": cells, "tune": tune,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "inputs (%.0f MB) and checkpoint/edge stores exceed the 129 MB L2" %
                              (batch.input_bytes / 1e6)},

@@ -61,6 +61,19 @@ class SwScoringC(ctypes.Structure):
                 ("gap_open", ctypes.c_int32), ("gap_extend", ctypes.c_int32)]
 
 
+class TuneC(ctypes.Structure):
+    _fields_ = [("sw_pack16", ctypes.c_int32), ("sw_window", ctypes.c_int32),
+                ("sw_long_log2", ctypes.c_int32), ("wfa_lane_smax", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
+
+
+class TuneTrialC(ctypes.Structure):
+    _fields_ = [("tune", TuneC), ("ms", ctypes.c_double)]
+
+
+TUNE_FIELDS = ("sw_pack16", "sw_window", "sw_long_log2", "wfa_lane_smax")
+
+
 class DeviceBatch(ctypes.Structure):
     _fields_ = [("seq", ctypes.c_void_p), ("seq_bytes", ctypes.c_int64),
                 ("a_off", ctypes.c_void_p), ("a_len", ctypes.c_void_p),
@@ -74,7 +87,11 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
            "ga_profile_kernel_name", "ga_bench_int_peak", "ga_cost_model_nparams", "ga_cost_model_set",
            "ga_cost_model_get", "ga_wfa_features", "ga_mlp_forward", "ga_mlp_gradient", "ga_mlp_train_step",
-           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_mlp_forward_fast"]
+           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_mlp_forward_fast", "ga_tune_default", "ga_tune_get",
+           "ga_tune_set", "ga_autotune_sw", "ga_autotune_wfa", "ga_tune_save", "ga_tune_load",
+           "ga_fasta_read", "ga_fasta_parse", "ga_fasta_count", "ga_fasta_id", "ga_fasta_description",
+           "ga_fasta_arena", "ga_fasta_offsets", "ga_fasta_lengths", "ga_fasta_pinned", "ga_fasta_upload",
+           "ga_fasta_free", "ga_pack_2bit_device", "ga_sw_qc_device", "ga_sw_validate_device"]
 
 _lib = None
 
@@ -143,6 +160,49 @@ def load(build: bool = True):
     L.ga_mlp_forward_fast.restype = i32
     L.ga_wfa_route_stats.argtypes = [p, i32]
     L.ga_wfa_route_stats.restype = i32
+    for f in ("ga_tune_default", "ga_tune_get"):
+        getattr(L, f).argtypes = [ctypes.POINTER(TuneC)]
+        getattr(L, f).restype = i32
+    L.ga_tune_set.argtypes = [ctypes.POINTER(TuneC)]
+    L.ga_tune_set.restype = i32
+    L.ga_autotune_sw.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, i64, p, p, p, p, i32,
+                                 ctypes.POINTER(TuneC), p, i32, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_autotune_sw.restype = i32
+    L.ga_autotune_wfa.argtypes = [ctypes.POINTER(DeviceBatch), i32, i32, p, p, p, i32,
+                                  ctypes.POINTER(TuneC), p, i32, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_autotune_wfa.restype = i32
+    L.ga_tune_save.argtypes = [ctypes.c_char_p]
+    L.ga_tune_save.restype = i32
+    L.ga_tune_load.argtypes = [ctypes.c_char_p]
+    L.ga_tune_load.restype = i32
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    L.ga_fasta_read.argtypes = [ctypes.c_char_p, pp, ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_fasta_read.restype = i32
+    L.ga_fasta_parse.argtypes = [ctypes.c_char_p, i64, pp, ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_fasta_parse.restype = i32
+    L.ga_fasta_count.argtypes = [p]
+    L.ga_fasta_count.restype = i32
+    for f in ("ga_fasta_id", "ga_fasta_description"):
+        getattr(L, f).argtypes = [p, i32]
+        getattr(L, f).restype = ctypes.c_char_p
+    L.ga_fasta_arena.argtypes = [p, ctypes.POINTER(i64)]
+    L.ga_fasta_arena.restype = p
+    L.ga_fasta_offsets.argtypes = [p]
+    L.ga_fasta_offsets.restype = p
+    L.ga_fasta_lengths.argtypes = [p]
+    L.ga_fasta_lengths.restype = p
+    L.ga_fasta_pinned.argtypes = [p]
+    L.ga_fasta_pinned.restype = i32
+    L.ga_fasta_upload.argtypes = [p, p, p]
+    L.ga_fasta_upload.restype = i32
+    L.ga_fasta_free.argtypes = [p]
+    L.ga_fasta_free.restype = None
+    L.ga_pack_2bit_device.argtypes = [p, i64, p, p, p]
+    L.ga_pack_2bit_device.restype = i32
+    L.ga_sw_qc_device.argtypes = [ctypes.POINTER(DeviceBatch), p, p, p, p, i32, i32, p, p]
+    L.ga_sw_qc_device.restype = i32
+    L.ga_sw_validate_device.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, p, p, p, p, p, p]
+    L.ga_sw_validate_device.restype = i32
     _lib = L
     return L
 
@@ -434,6 +494,33 @@ class DeviceBatchT:
                              self.a_len.data_ptr(), self.b_off.data_ptr(), self.b_len.data_ptr(),
                              self.out_off.data_ptr(), self.n, 0)
 
+    @classmethod
+    def from_device_arena(cls, seq, a_off, a_len, b_off, b_len):
+        """A batch over a byte arena already in device memory (a uint8 tensor,
+        sequences at 32-byte-aligned offsets, 64 spare bytes at the end): numpy
+        offsets and lengths; CIGAR slots of a_len + b_len bytes in pair order."""
+        import torch
+        self = cls.__new__(cls)
+        dev = seq.device
+        a_len = np.asarray(a_len, np.int32)
+        b_len = np.asarray(b_len, np.int32)
+        self.n = int(a_len.shape[0])
+        cap = a_len.astype(np.int64) + b_len
+        oo = np.zeros(self.n, np.int64)
+        if self.n:
+            oo[1:] = np.cumsum(cap)[:-1]
+        self.seq = seq
+        self.a_off = torch.from_numpy(np.ascontiguousarray(a_off, np.int64)).to(dev)
+        self.a_len = torch.from_numpy(a_len).to(dev)
+        self.b_off = torch.from_numpy(np.ascontiguousarray(b_off, np.int64)).to(dev)
+        self.b_len = torch.from_numpy(b_len).to(dev)
+        self.out_off = torch.from_numpy(oo).to(dev)
+        self.out_bytes = int(cap.sum())
+        self.input_bytes = int(seq.numel() + 8 * 3 * self.n + 4 * 2 * self.n)
+        self.c = DeviceBatch(seq.data_ptr(), int(seq.numel()), self.a_off.data_ptr(), self.a_len.data_ptr(),
+                             self.b_off.data_ptr(), self.b_len.data_ptr(), self.out_off.data_ptr(), self.n, 0)
+        return self
+
 
 def wfa_device(batch: DeviceBatchT, smax, trace, out_score, out_len, out_cigar, stream=None, learned=False):
     err = ctypes.c_char_p()
@@ -632,3 +719,180 @@ def wfa_route_stats(rounds: int = 12):
     if st != GA_OK:
         raise RuntimeError(f"ga_wfa_route_stats failed ({st})")
     return int(out[0]), int(out[1]), [int(x) for x in out[2:]]
+
+
+# -------------------------------------------------------------- autotuner --
+def _tune_dict(t: TuneC) -> dict:
+    return {f: int(getattr(t, f)) for f in TUNE_FIELDS}
+
+
+def tune_default() -> dict:
+    """The built-in kernel setting (ga_tune_default)."""
+    t = TuneC()
+    load().ga_tune_default(ctypes.byref(t))
+    return _tune_dict(t)
+
+
+def tune_get() -> dict:
+    """The current device's kernel setting (ga_tune_get)."""
+    t = TuneC()
+    load().ga_tune_get(ctypes.byref(t))
+    return _tune_dict(t)
+
+
+def tune_set(**fields):
+    """Replace fields of the current device's setting (ga_tune_set); raises
+    ValueError for values out of range."""
+    cur = tune_get()
+    for k, v in fields.items():
+        if k not in TUNE_FIELDS:
+            raise ValueError(f"unknown tune field {k}")
+        cur[k] = int(v)
+    t = TuneC(*[cur[f] for f in TUNE_FIELDS])
+    st = load().ga_tune_set(ctypes.byref(t))
+    if st != GA_OK:
+        raise ValueError(f"ga_tune_set refused {cur}")
+
+
+def _trials(buf, n):
+    return [(_tune_dict(buf[i].tune), float(buf[i].ms)) for i in range(n)]
+
+
+def autotune_sw(batch: "DeviceBatchT", scoring, out_score, out_pos, out_len, out_cigar, reps: int = 2,
+                trace_cell_limit: int = -1):
+    """Time candidate settings on an SW traceback batch and keep the fastest for
+    the current device (ga_autotune_sw).  Returns (chosen, [(setting, ms)])."""
+    t = TuneC()
+    buf = (TuneTrialC * 32)()
+    nt = ctypes.c_int32(0)
+    err = ctypes.c_char_p()
+    st = load().ga_autotune_sw(ctypes.byref(batch.c), SwScoringC(*scoring), trace_cell_limit,
+                               out_score.data_ptr(), out_pos.data_ptr(), out_len.data_ptr(), out_cigar.data_ptr(),
+                               reps, ctypes.byref(t), ctypes.cast(buf, ctypes.c_void_p), 32, ctypes.byref(nt),
+                               ctypes.byref(err))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_autotune_sw failed: {err.value}")
+    return _tune_dict(t), _trials(buf, nt.value)
+
+
+def autotune_wfa(batch: "DeviceBatchT", smax, trace, out_score, out_len, out_cigar, reps: int = 2):
+    """The same for the learned WFA path (ga_autotune_wfa; the cost model must be
+    loaded)."""
+    t = TuneC()
+    buf = (TuneTrialC * 32)()
+    nt = ctypes.c_int32(0)
+    err = ctypes.c_char_p()
+    st = load().ga_autotune_wfa(ctypes.byref(batch.c), smax, 1 if trace else 0, out_score.data_ptr(),
+                                out_len.data_ptr() if out_len is not None else None,
+                                out_cigar.data_ptr() if out_cigar is not None else None,
+                                reps, ctypes.byref(t), ctypes.cast(buf, ctypes.c_void_p), 32, ctypes.byref(nt),
+                                ctypes.byref(err))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_autotune_wfa failed: {err.value}")
+    return _tune_dict(t), _trials(buf, nt.value)
+
+
+def tune_save(path: str):
+    if load().ga_tune_save(path.encode()) != GA_OK:
+        raise OSError(f"ga_tune_save failed for {path}")
+
+
+def tune_load(path: str):
+    if load().ga_tune_load(path.encode()) != GA_OK:
+        raise ValueError(f"ga_tune_load refused {path}")
+
+
+# ----------------------------------------------------------------- ingest --
+class FastaSet:
+    """A FASTA file parsed into one device-ready arena (ga_fasta_*): ids,
+    descriptions, and per record an offset (multiple of 32) and a length into
+    `arena` (a numpy view of the library's pinned host buffer, valid while this
+    object lives)."""
+
+    def __init__(self, handle):
+        L = load()
+        self._h = handle
+        n = L.ga_fasta_count(handle)
+        self.n = n
+        self.ids = [L.ga_fasta_id(handle, i).decode("latin-1") for i in range(n)]
+        self.descriptions = [L.ga_fasta_description(handle, i).decode("latin-1") for i in range(n)]
+        nb = ctypes.c_int64(0)
+        ptr = L.ga_fasta_arena(handle, ctypes.byref(nb))
+        self.arena = np.ctypeslib.as_array((ctypes.c_uint8 * nb.value).from_address(ptr))
+        self.offsets = np.ctypeslib.as_array((ctypes.c_int64 * n).from_address(L.ga_fasta_offsets(handle))) \
+            if n else np.zeros(0, np.int64)
+        self.lengths = np.ctypeslib.as_array((ctypes.c_int32 * n).from_address(L.ga_fasta_lengths(handle))) \
+            if n else np.zeros(0, np.int32)
+        self.pinned = bool(L.ga_fasta_pinned(handle))
+
+    def sequence(self, i: int) -> bytes:
+        o, n = int(self.offsets[i]), int(self.lengths[i])
+        return self.arena[o:o + n].tobytes()
+
+    def upload(self, device_tensor, stream=None):
+        """Copy the arena into a device tensor of at least arena.nbytes bytes."""
+        if device_tensor.numel() * device_tensor.element_size() < self.arena.nbytes:
+            raise ValueError("device buffer smaller than the arena")
+        if load().ga_fasta_upload(self._h, device_tensor.data_ptr(), stream) != GA_OK:
+            raise RuntimeError("ga_fasta_upload failed")
+
+    def close(self):
+        if self._h:
+            self.arena = self.offsets = self.lengths = None
+            load().ga_fasta_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _fasta_open(call):
+    h = ctypes.c_void_p()
+    err = ctypes.c_char_p()
+    st = call(ctypes.byref(h), ctypes.byref(err))
+    if st != GA_OK:
+        raise ValueError(err.value.decode() if err.value else f"status {st}")
+    return FastaSet(h.value)
+
+
+def fasta_read(path: str) -> FastaSet:
+    """Read a FASTA file into a pinned, device-ready arena (ga_fasta_read);
+    raises ValueError with the reader's message on a malformed file."""
+    return _fasta_open(lambda h, e: load().ga_fasta_read(path.encode(), h, e))
+
+
+def fasta_parse(data: bytes) -> FastaSet:
+    """The same from bytes in memory (ga_fasta_parse)."""
+    return _fasta_open(lambda h, e: load().ga_fasta_parse(data, len(data), h, e))
+
+
+def pack_2bit_device(seq, packed, mask, stream=None):
+    """2-bit codes and non-ACGT masks of a device byte arena (ga_pack_2bit_device):
+    seq uint8 (length a multiple of 32), packed int64 and mask int32 tensors of
+    len(seq) // 32 elements."""
+    st = load().ga_pack_2bit_device(seq.data_ptr(), int(seq.numel()), packed.data_ptr(), mask.data_ptr(), stream)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_pack_2bit_device failed ({st})")
+
+
+def sw_validate_device(batch: "DeviceBatchT", scoring, out_score, out_pos, out_len, out_cigar, flags, stream=None):
+    """rescore_ok | wellformed_ok << 1 per pair into the uint8 device tensor
+    `flags` (ga_sw_validate_device), from ga_sw_device's outputs."""
+    st = load().ga_sw_validate_device(ctypes.byref(batch.c), SwScoringC(*scoring), out_score.data_ptr(),
+                                      out_pos.data_ptr(), out_len.data_ptr(), out_cigar.data_ptr(), flags.data_ptr(),
+                                      stream)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_sw_validate_device failed ({st})")
+
+
+def sw_qc_device(batch: "DeviceBatchT", out_score, out_pos, out_len, out_cigar, frame: int, code: int, out,
+                 stream=None):
+    """Per pair (fs_runs, fs_net, stops, stop_end) into the int32 device tensor
+    `out` of 4 n elements (ga_sw_qc_device)."""
+    st = load().ga_sw_qc_device(ctypes.byref(batch.c), out_score.data_ptr(), out_pos.data_ptr(), out_len.data_ptr(),
+                                out_cigar.data_ptr(), int(frame), int(code), out.data_ptr(), stream)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_sw_qc_device failed ({st})")

@@ -21,6 +21,7 @@
 
 #include "engine.hpp"
 #include "kernels.cuh"
+#include "tune.hpp"
 
 namespace ga {
 
@@ -370,7 +371,7 @@ static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace,
 }
 
 // Every launch of one WFA batch on stream st (inputs already on the device).
-static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool trace, bool learned,
+static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool trace, bool learned, int lane_smax,
                                int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
     D.packed = S.packed;
@@ -386,7 +387,7 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     if (!learned) return launch_wfa(A, S.slots, st);
     const int NB = route_buckets();
     if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 2), st)) != cudaSuccess) return e;
-    if ((e = launch_route_model(D, smax, S.item, S.lb, S.y, S.counts, score, len, st)) != cudaSuccess) return e;
+    if ((e = launch_route_model(D, smax, lane_smax, S.item, S.lb, S.y, S.counts, score, len, st)) != cudaSuccess) return e;
     if ((e = launch_route(D.n, S.item, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess) return e;
     // ctr layout: [0] warp-queue next, [1] lane-queue next, [2] escalation
     // next, [32] escalation count
@@ -408,18 +409,18 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
 
 // Learned path as one CUDA graph, cached per context by everything the
 // launches bake in.
-static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace,
+static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace, int lane_smax,
                                  int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
     const uint64_t key[8] = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
-                             (uint64_t)trace, (uint64_t)(uintptr_t)score, (uint64_t)(uintptr_t)cig,
-                             (uint64_t)(uintptr_t)D.a_off};
+                             (uint64_t)trace | (uint64_t)lane_smax << 8, (uint64_t)(uintptr_t)score,
+                             (uint64_t)(uintptr_t)cig, (uint64_t)(uintptr_t)D.a_off};
     if (!c->gexec || std::memcmp(key, c->gkey, sizeof(key)) != 0) {
         if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, true, score, len, cig, err, st);
+        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, true, lane_smax, score, len, cig, err, st);
         e = cudaStreamEndCapture(st, &g);
         if (e1 != cudaSuccess || e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e1 != cudaSuccess ? e1 : e; }
         e = cudaGraphInstantiate(&c->gexec, g, 0);
@@ -468,10 +469,15 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
 
     // plan: 32-aligned sequence offsets, CIGAR slot offsets
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    std::vector<uint8_t> own(n, 0);
     int64_t arena = 0, cig = 0;
     for (int32_t i = 0; i < n; ++i) {
-        a_off[i] = arena; arena += round32(reqs[i].pattern_len);
-        b_off[i] = arena; arena += round32(reqs[i].text_len);
+        // a side that repeats the previous request's (same pointer and length) is staged once
+        const ga_align_request& r = reqs[i];
+        if (i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len) a_off[i] = a_off[i - 1];
+        else { a_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 1; }
+        if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) b_off[i] = b_off[i - 1];
+        else { b_off[i] = arena; arena += round32(r.text_len); own[i] |= 2; }
         out_off[i] = cig; cig += (int64_t)reqs[i].pattern_len + reqs[i].text_len;
         slot_end[i] = cig;
     }
@@ -481,6 +487,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
     Ctx* c = acquire_ctx(err);
     if (!c) return GA_DEVICE_ERROR;
     struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
+    const int lane_smax = tune_current().wfa_lane_smax;
 
     WfaScratch S;
     size_wfa(S, n, smax, trace, learned, c->sm_count);
@@ -518,8 +525,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
             ha[i] = a_off[i]; hal[i] = r.pattern_len;
             hb[i] = b_off[i]; hbl[i] = r.text_len;
             ho[i] = out_off[i];
-            if (r.pattern_len) std::memcpy(hseq + a_off[i], r.pattern, (size_t)r.pattern_len);
-            if (r.text_len) std::memcpy(hseq + b_off[i], r.text, (size_t)r.text_len);
+            if ((own[i] & 1) && r.pattern_len) std::memcpy(hseq + a_off[i], r.pattern, (size_t)r.pattern_len);
+            if ((own[i] & 2) && r.text_len) std::memcpy(hseq + b_off[i], r.text, (size_t)r.text_len);
         }
     });
     std::memset(hseq + arena - 64, 0, 64);
@@ -536,8 +543,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
     D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
     cudaError_t le;
     if (fail_here(3)) le = cudaErrorLaunchFailure;
-    else if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace, dsc, dln, dcg, der, c->stream);
-    else le = enqueue_wfa(S, D, smax, trace, learned, dsc, dln, dcg, der, c->stream);
+    else if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace, lane_smax, dsc, dln, dcg, der, c->stream);
+    else le = enqueue_wfa(S, D, smax, trace, learned, lane_smax, dsc, dln, dcg, der, c->stream);
     if (learned) note_route(c, S);
     if (le != cudaSuccess) {
         cudaGetLastError();
@@ -648,13 +655,10 @@ static bool use_sw16ck()
 }
 
 static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8_t* pure, const uint8_t* skip,
-                    const ga_sw_scoring& sc, bool trace, SwPlan& P)
+                    const ga_sw_scoring& sc, bool trace, const ga_tune& T, SwPlan& P)
 {
     std::vector<int32_t> e16[3];
-    static const bool use16_ok = [] {
-        const char* e = getenv("GA_SW16");
-        return !(e && e[0] == '0');
-    }();
+    const bool use16_ok = T.sw_pack16 != 0;
     const bool ck = use_sw16ck();
     for (int32_t i = 0; i < n; ++i) {
         if (skip && skip[i]) continue;
@@ -664,12 +668,12 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
         const bool use16 = use16_ok && trace && pure && pure[i] && pure[n + i] &&
                            sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
         if (use16) e16[k].push_back(i);
-        else P.w32[(ck && trace && sw32ck_long(tl[i], pl[i])) ? 1 : k].push_back(i);
+        else P.w32[(ck && trace && sw32ck_long(tl[i], pl[i], T.sw_long_log2)) ? 1 : k].push_back(i);
     }
     for (int k = 0; k < 3; ++k) {
         order_by_size(P.w32[k], tl, pl);
         for (int32_t i : P.w32[k]) {
-            if (trace) P.dir32[k] = std::max(P.dir32[k], (ck && k < 2) ? sw32ck_dir_words(tl[i], pl[i])
+            if (trace) P.dir32[k] = std::max(P.dir32[k], (ck && k < 2) ? sw32ck_dir_words(tl[i], pl[i], T.sw_long_log2)
                                                                        : sw_dir_words(tl[i], pl[i], kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
         }
@@ -680,7 +684,7 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
             P.w16[k].push_back(a);
             P.w16[k].push_back(b);
             const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
-            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0) ? sw16ck_dir_words(M, N)
+            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0) ? sw16ck_dir_words(M, N, T.sw_window)
                                                                         : sw16_dir_words(M, N, kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
         }
@@ -696,17 +700,15 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
 // `dwork`; reads back its record and fills P's list lengths and sizes.
 static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, int64_t cell_limit,
                                   int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
-                                  long long* dres, long long* hres, cudaStream_t st, SwPlan& P)
+                                  long long* dres, long long* hres, const ga_tune& T, cudaStream_t st, SwPlan& P)
 {
-    static const bool use16_ok = [] {
-        const char* e = getenv("GA_SW16");
-        return !(e && e[0] == '0');
-    }();
     SwPlanArgs A;
     A.D = D;
     A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
     A.cell_limit = cell_limit;
-    A.use16 = use16_ok ? 1 : 0;
+    A.use16 = T.sw_pack16 ? 1 : 0;
+    A.window = T.sw_window;
+    A.long_log2 = T.sw_long_log2;
     A.too_large_score = too_large_score;
     A.out_score = out_score;
     A.work = dwork;
@@ -733,7 +735,7 @@ struct SwSlots {
     int64_t dir_words = 0, max_slots = 4;
 };
 
-static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
+static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_count)
 {
     SwSlots S;
     const int64_t budget = (int64_t)96 << 30;          // direction-table / checkpoint cap, bytes
@@ -748,7 +750,7 @@ static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
             S.max_slots = std::max<int64_t>(S.max_slots, s);
         }
         if (P.n16[k] > 0) {
-            int s = (use_sw16ck() && k == 0) ? sw16ck_max_slots(sm_count) : sw16_max_slots(kWidths[k], sm_count);
+            int s = (use_sw16ck() && k == 0) ? sw16ck_max_slots(sm_count, T.sw_window) : sw16_max_slots(kWidths[k], sm_count);
             s = (int)std::min<int64_t>(s, (P.n16[k] / 2 + 3) / 4 * 4);
             s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
             S.s16[k] = s;
@@ -762,7 +764,7 @@ static SwSlots size_sw(const SwPlan& P, bool trace, int sm_count)
 // Enqueue every SW launch of a plan.  `dwork` holds the plan's lists
 // concatenated in the order w16[0..2] then w32[0..2]; `ctr` has 6 zeroed ints.
 static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc& D, const ga_sw_scoring& sc,
-                               bool trace, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
+                               bool trace, const ga_tune& T, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
                                int32_t* out_len, char* out_cigar, uint32_t* dirs, int32_t* edge, int32_t* ctr,
                                int32_t* err, cudaStream_t st)
 {
@@ -775,7 +777,7 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + k; A.err = err;
-            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], st)
+            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], T.sw_window, st)
                                                            : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
         }
@@ -812,6 +814,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     if (n <= 0) return GA_OK;
     const ga_sw_scoring s0 = reqs[0].scoring;
     if (int32_t st = sw_check(reqs, n, err)) return st;
+    const ga_tune T = tune_current();
     bool trace = false;
     int max_n = 0;
     for (int32_t i = 0; i < n; ++i) {
@@ -829,14 +832,18 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
 
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
     std::vector<int32_t> tl(n), pl(n);
-    std::vector<uint8_t> too_big(n, 0);
+    std::vector<uint8_t> too_big(n, 0), own(n, 0);
     int64_t arena = 0, cig = 0;
     for (int32_t i = 0; i < n; ++i) {
         const ga_sw_request& r = reqs[i];
         tl[i] = r.text_len;
         pl[i] = r.pattern_len;
-        a_off[i] = arena; arena += round32(r.text_len);
-        b_off[i] = arena; arena += round32(r.pattern_len);
+        // a side that repeats the previous request's (same pointer and length:
+        // one reference against many, or many against one) is staged once
+        if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) a_off[i] = a_off[i - 1];
+        else { a_off[i] = arena; arena += round32(r.text_len); own[i] |= 1; }
+        if (i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len) b_off[i] = b_off[i - 1];
+        else { b_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 2; }
         out_off[i] = cig; cig += (int64_t)r.text_len + r.pattern_len;
         slot_end[i] = cig;
         if (trace && cell_limit >= 0 && r.text_len > 0 && r.pattern_len > 0 &&
@@ -888,8 +895,8 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
             ha[i] = a_off[i]; hal[i] = r.text_len;
             hb[i] = b_off[i]; hbl[i] = r.pattern_len;
             ho[i] = out_off[i];
-            if (r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
-            if (r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
+            if ((own[i] & 1) && r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
+            if ((own[i] & 2) && r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
         }
     });
     std::memset(hseq + arena - 64, 0, 64);
@@ -949,7 +956,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
             return GA_DEVICE_ERROR;
         }
         if (dplan) {
-            if (device_plan_sw(D, s0, cell_limit, -1, dsc, dwork, dscr, dres, hres, c->stream, P) != cudaSuccess) {
+            if (device_plan_sw(D, s0, cell_limit, -1, dsc, dwork, dscr, dres, hres, T, c->stream, P) != cudaSuccess) {
                 cudaGetLastError();
                 *err = E_LAUNCH;
                 return GA_DEVICE_ERROR;
@@ -963,7 +970,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
                 *err = E_LAUNCH;
                 return GA_DEVICE_ERROR;
             }
-            plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, P);
+            plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, T, P);
             flatten_plan(P, hwork);
         }
         if (P.words() > 0 &&
@@ -976,7 +983,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         return GA_OK;
     };
     if (int32_t rs = stage(true)) return rs;
-    const SwSlots S = size_sw(P, trace, c->sm_count);
+    const SwSlots S = size_sw(P, trace, T, c->sm_count);
     const uint64_t gen_before = c->dev_gen;
     auto extra_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
         Carve k(base);
@@ -994,7 +1001,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     }
     extra_layout(c->dev, &dctr, &dedge, &ddirs);
     cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
-    if (launch_plan(P, S, D, s0, trace, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess ||
+    if (launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess ||
         (trace && launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
                                      dln, dcg, dvf, c->stream) != cudaSuccess)) {
         cudaGetLastError();
@@ -1282,8 +1289,10 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
     int32_t rc = GA_OK;
     cudaError_t le = cudaMemsetAsync(derr, 0, sizeof(int32_t), st);
     if (le == cudaSuccess) {
-        if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace != 0, out_score, out_len, out_cigar, derr, st);
-        else le = enqueue_wfa(S, D, smax, trace != 0, learned, out_score, out_len, out_cigar, derr, st);
+        const int lane_smax = tune_current().wfa_lane_smax;
+        if (learned && !profiling_on())
+            le = run_wfa_graph(c, S, D, smax, trace != 0, lane_smax, out_score, out_len, out_cigar, derr, st);
+        else le = enqueue_wfa(S, D, smax, trace != 0, learned, lane_smax, out_score, out_len, out_cigar, derr, st);
         if (learned) note_route(c, S);
     }
     if (le != cudaSuccess) {
@@ -1345,6 +1354,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const ga_tune T = tune_current();
     if (trace && use_sw16ck()) {
         // the checkpointed kernels: purity and the plan on the device, one small
         // record back, then the launches
@@ -1378,7 +1388,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
             D.pure = dpure;
             if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
-            return device_plan_sw(D, sc, cell_limit, -2, out_score, dwork, dscr, dres, hres, st, P) == cudaSuccess;
+            return device_plan_sw(D, sc, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) == cudaSuccess;
         };
         if (!plan()) {
             cudaGetLastError();
@@ -1386,7 +1396,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             if (err) *err = E_LAUNCH;
             return GA_DEVICE_ERROR;
         }
-        const SwSlots S = size_sw(P, true, c->sm_count);
+        const SwSlots S = size_sw(P, true, T, c->sm_count);
         auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
             Carve k(base);
             k.off = plan_bytes;
@@ -1412,7 +1422,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         run_layout(c->dev, &dctr, &dedge, &ddirs);
         cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
         int32_t rc = GA_OK;
-        if (launch_plan(P, S, D, sc, true, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+        if (launch_plan(P, S, D, sc, true, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
                         dctr + 32, st) != cudaSuccess) {
             cudaGetLastError();
             if (err) *err = E_LAUNCH;
@@ -1464,8 +1474,8 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             too_big.push_back(i);
         }
     SwPlan P;
-    plan_sw(n, al.data(), bl.data(), pure.data(), skip.data(), sc, trace != 0, P);
-    const SwSlots S = size_sw(P, trace != 0, c->sm_count);
+    plan_sw(n, al.data(), bl.data(), pure.data(), skip.data(), sc, trace != 0, T, P);
+    const SwSlots S = size_sw(P, trace != 0, T, c->sm_count);
     const int64_t nw = P.words();
     auto layout = [&](char* base, uint8_t** pp, int32_t** wk, int32_t** tb, int32_t** ctr, int32_t** edge,
                       uint32_t** dirs) {
@@ -1509,7 +1519,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             cudaMemcpyAsync(out_score + too_big[q], &m2[q], sizeof(int32_t), cudaMemcpyHostToDevice, st);
         cudaStreamSynchronize(st);
     }
-    if (launch_plan(P, S, D, sc, trace != 0, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+    if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
                     dctr + 32, st) != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = E_LAUNCH;
@@ -1543,6 +1553,42 @@ const char* ga_device_name(void)
         cudaGetLastError();
     });
     return name;
+}
+
+int32_t ga_sw_validate_device(const ga_device_batch* b, ga_sw_scoring sc, const int32_t* score, const int32_t* pos,
+                              const int32_t* len, const char* cigar, uint8_t* flags, void* stream)
+{
+    if (!b || b->n < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len ||
+                                         !b->out_off || !score || !pos || !len || !cigar || !flags)))
+        return GA_INVALID_ARGUMENT;
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = b->n;
+    const ga_sw_scoring_t s{sc.match, sc.mismatch, sc.gap_open, sc.gap_extend};
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = launch_sw_validate(D, s, score, pos, len, cigar, flags, st);
+    if (e == cudaSuccess && !stream) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
+}
+
+int32_t ga_pack_2bit_device(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* mask, void* stream)
+{
+    if (seq_bytes < 0 || (seq_bytes & 31) != 0 || (seq_bytes > 0 && (!seq || !packed || !mask)) ||
+        ((uintptr_t)seq & 15) != 0)
+        return GA_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = launch_pack_arena(seq, seq_bytes, packed, mask, st);
+    if (e == cudaSuccess && !stream) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
 }
 
 int32_t ga_device_available(void)

@@ -76,6 +76,7 @@ struct RoutedArgs {
 // words; null: purity flags only) and sets pure[2n].
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 int64_t packed_arena_words(int64_t seq_bytes);
+cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* bad, cudaStream_t st);
 cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
 bool cost_model_loaded();
@@ -88,8 +89,8 @@ int routed_max_slots(int smax, bool trace, int sm_count);
 int lane_max_slots(bool trace, int sm_count);
 // Fused sketch + lower bound + cost model + queue choice (learned.cu); then
 // the queues from the per-pair items (wfa_routed.cu).
-cudaError_t launch_route_model(const PairDesc& D, int smax, int32_t* item, int32_t* lb, float* y, int32_t* counts,
-                               int32_t* out_score, int32_t* out_len, cudaStream_t st);
+cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, int32_t* item, int32_t* lb, float* y,
+                               int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st);
 cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* starts, int2* big, int2* small,
                          cudaStream_t st);
 // The lane kernel over R.small, then the warp kernel over R.big and the
@@ -121,6 +122,8 @@ struct SwPlanArgs {
     int32_t match, mismatch, gap_open, gap_extend;
     int64_t cell_limit;          // traceback limit in cells, < 0: none
     int32_t use16;               // the 16-bit kernels may be used
+    int32_t window;              // sw16ck recompute window, tiles (2 or 4)
+    int32_t long_log2;           // sw32ck long shape above 2^long_log2 cells
     int32_t too_large_score;     // score written for pairs above cell_limit
     int32_t* out_score;
     int32_t* work;               // flattened work lists (2n + 8 ints)
@@ -139,8 +142,8 @@ cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, con
 // in sw_sizes.cuh.
 int sw32ck_max_slots(bool long_pairs, int sm_count);
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st);
-int sw16ck_max_slots(int sm_count);
-cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st);
+int sw16ck_max_slots(int sm_count, int window);
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, cudaStream_t st);
 int64_t sw16_dir_words(int M, int N, int C);
 int sw16_max_slots(int C, int sm_count);
 cudaError_t launch_sw16(const Sw16Args& A, int C, int slots, cudaStream_t st);

@@ -466,6 +466,7 @@ __global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16
 constexpr int RM_WARPS = 16;
 
 __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* __restrict__ w, PairDesc D, int smax,
+                                                          int lane_smax,
                                                           int32_t* __restrict__ item, int32_t* __restrict__ lb_out,
                                                           float* __restrict__ y_out, int32_t* __restrict__ counts,
                                                           int32_t* __restrict__ out_score, int32_t* __restrict__ out_len)
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* _
                 if (pr >= n) continue;
                 const int mr = h ? m1 : m0, nr = h ? n1 : n0, lbr = h ? lb1 : lb0;
                 const float y0 = h ? o[2] : o[0];
-                const int it = route_item(mr, nr, D.pure[pr] != 0, D.pure[n + pr] != 0, lbr, y0, smax);
+                const int it = route_item(mr, nr, D.pure[pr] != 0, D.pure[n + pr] != 0, lbr, y0, smax, lane_smax);
                 item[pr] = it;
                 if (lb_out) lb_out[pr] = lbr;
                 if (y_out) { y_out[2 * (int64_t)pr] = y0; y_out[2 * (int64_t)pr + 1] = h ? o[3] : o[1]; }
@@ -574,8 +575,8 @@ static size_t route_model_smem() { return sizeof(TcSmem) + (size_t)RM_WARPS * 64
 
 // The fused routing pass over a WFA batch (D.packed and D.pure set): per pair
 // the queue item, lower bound and prediction; bucket totals into counts.
-cudaError_t launch_route_model(const PairDesc& D, int smax, int32_t* item, int32_t* lb, float* y, int32_t* counts,
-                               int32_t* out_score, int32_t* out_len, cudaStream_t st)
+cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, int32_t* item, int32_t* lb, float* y,
+                               int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st)
 {
     const __nv_bfloat16* w = cost_model_weights();
     if (!w) return cudaErrorNotReady;
@@ -583,7 +584,7 @@ cudaError_t launch_route_model(const PairDesc& D, int smax, int32_t* item, int32
     int blocks = (D.n + 16 * RM_WARPS - 1) / (16 * RM_WARPS);
     if (blocks > 152) blocks = 152;
     launch_begin(K_MLP, st);
-    route_model_kernel<<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, item, lb, y, counts,
+    route_model_kernel<<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, lane_smax, item, lb, y, counts,
                                                                           out_score, out_len);
     launch_end(K_MLP, st);
     return cudaGetLastError();

@@ -8,7 +8,8 @@
 namespace ga {
 
 // Lane queue: pairs run one per lane, 32 per warp.  Eligible: both sides pure
-// ACGT, at most LANE_MAXLEN bases, first smax <= LANE_SMAX.
+// ACGT, at most LANE_MAXLEN bases, first smax <= the tuned lane_smax, itself
+// at most LANE_SMAX (the lane kernel's shared-memory wavefront bound).
 constexpr int LANE_SMAX = 15;
 constexpr int LANE_MAXLEN = 256;
 // Buckets: keys 0 .. ROUTE_BUCKETS-1 are the warp queue by bit length of the
@@ -32,12 +33,13 @@ __device__ __forceinline__ int first_smax(float y, int lb, int smax)
 // (bucket key) | (smax the pair is first run with) << 8.  A warp-queue pair
 // runs with the batch smax: the warp kernel stops at s = d whatever its smax,
 // so a smaller budget there could only add reruns.
-__device__ __forceinline__ int route_item(int m, int n, bool pure_a, bool pure_b, int lb, float y0, int smax)
+__device__ __forceinline__ int route_item(int m, int n, bool pure_a, bool pure_b, int lb, float y0, int smax,
+                                          int lane_smax)
 {
     if (m <= 0 || n <= 0) return min(bitlen((unsigned)smax), ROUTE_BUCKETS - 1) | (smax << 8);
     if (lb > smax) return -1;
     const int s = first_smax(y0, lb, smax);
-    if (s <= LANE_SMAX && m <= LANE_MAXLEN && n <= LANE_MAXLEN && pure_a && pure_b)
+    if (s <= lane_smax && s <= LANE_SMAX && m <= LANE_MAXLEN && n <= LANE_MAXLEN && pure_a && pure_b)
         return (ROUTE_BUCKETS + s) | (s << 8);
     return min(bitlen((unsigned)s), ROUTE_BUCKETS - 1) | (smax << 8);
 }

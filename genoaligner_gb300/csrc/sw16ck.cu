@@ -1,6 +1,6 @@
 // sw16ck.cu -- Smith-Waterman with traceback, two pairs per warp in 16-bit
 // lanes: a score-only forward pass that keeps checkpoints, then the walk over
-// 64 x 64 tiles recomputed with direction bits.
+// windows of 64 x 64 tiles recomputed from them.
 //
 // Same recurrence, tie rules and walk as sw.cu and sw16.cu (the reference's
 // trace recurrence, include/genoaligner/backend/sw_kernel_impl.hip:286-329,
@@ -20,8 +20,8 @@
 //      tiles to its left are recomputed from the checkpoint row above them
 //      and the column edges left of them -- TG groups of 32 / TG lanes, one
 //      tile each, so the lanes' one-step lag costs 32 / TG - 1 steps, not
-//      31 -- and their H
-//      values are kept; the walk proceeds inside them, reading every decision
+//      31 -- and their H values are kept; the walk proceeds inside them
+//      (runs of diagonal steps 32 at a time), reading every decision
 //      off H values with the reference's tie rules (diagonal, then E, then F;
 //      a gap cell opened when its neighbour's H - gap_open equals it, E from
 //      a warp-wide max over the row); leaving the window at the top or the
@@ -37,15 +37,14 @@
 namespace ga {
 
 constexpr int TW = CK_TW;                // tile width: a group of 32 / TG lanes x TW * TG / 32 columns
-constexpr int TG = CK_TG;                // tiles recomputed per pass: the walk's and the TG - 1 to its left
 constexpr int CK_BIAS = BIAS16;          // value bias of the recompute pass
+constexpr int CK_MAX_TG = 4;             // widest recompute window, tiles
 // shared memory words per warp: the forward band profile, or the window
 // profile (TW * TG / 32 columns per lane) plus the window's column edges
-constexpr int CK_FWD_WORDS = 2 * 4 * (CK_C / 2) * 32;
-constexpr int CK_WIN_WORDS = 2 * 4 * (TW * TG / 64) * 32 + 2 * TG * CK_K;
+constexpr int CK_LETTERS = 5;           // forward profile rows per pair: A C G T, then the padding row
+constexpr int CK_FWD_WORDS = 2 * CK_LETTERS * (CK_C / 2) * 32;
+constexpr int CK_WIN_WORDS = 2 * 4 * (TW * CK_MAX_TG / 64) * 32 + 2 * CK_MAX_TG * CK_K;
 constexpr int CK_WARP_WORDS = CK_FWD_WORDS > CK_WIN_WORDS ? CK_FWD_WORDS : CK_WIN_WORDS;
-static_assert(TG == 1 || TG == 2 || TG == 4 || TG == 8, "tile groups split the warp evenly");
-static_assert((TW * TG / 32) % 4 == 0, "window rows are stored as 16-byte vectors");
 
 __device__ __forceinline__ int ck_code(uint32_t c) { return (int)(((c >> 1) ^ (c >> 2)) & 3u); }
 __device__ __forceinline__ int lo16s(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
@@ -59,10 +58,11 @@ __device__ __forceinline__ bool ck_better(int v, int r, int c, int bv, int br, i
 }
 
 // Forward profile of a band at CB columns per lane:
-// prof[((pair * 4 + letter) * (CB / 2) + h) * 32 + t] holds the 16-bit scores
-// (s + gap_open) of this lane's columns 2h, 2h+1.  Past a pattern's end: a
-// score far below any reachable value, so padding columns never hold a row's
-// maximum.
+// prof[((pair * 5 + letter) * (CB / 2) + h) * 32 + t] holds the 16-bit scores
+// (s + gap_open) of this lane's columns 2h, 2h+1.  Past a pattern's end, and
+// in the padding letter 4 (the rows past a pair's text), a score far below any
+// reachable value: there H is at most the best of the rows above less
+// gap_open, so padding cells never hold a new best.
 template <int CB>
 __device__ __forceinline__ void ck_profile_fwd(uint32_t* prof, const uint8_t* patA, const uint8_t* patB, int j0,
                                                int nvA, int nvB, int sm, int sx, int t)
@@ -80,9 +80,12 @@ __device__ __forceinline__ void ck_profile_fwd(uint32_t* prof, const uint8_t* pa
         for (int L = 0; L < 4; ++L) {
             const int va0 = a0 == 4 ? PAD : (a0 == L ? sm : sx), va1 = a1 == 4 ? PAD : (a1 == L ? sm : sx);
             const int vb0 = b0 == 4 ? PAD : (b0 == L ? sm : sx), vb1 = b1 == 4 ? PAD : (b1 == L ? sm : sx);
-            prof[((0 * 4 + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)va0 & 0xffffu) | ((uint32_t)va1 << 16);
-            prof[((1 * 4 + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)vb0 & 0xffffu) | ((uint32_t)vb1 << 16);
+            prof[((0 * CK_LETTERS + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)va0 & 0xffffu) | ((uint32_t)va1 << 16);
+            prof[((1 * CK_LETTERS + L) * (CB / 2) + h) * 32 + t] = ((uint32_t)vb0 & 0xffffu) | ((uint32_t)vb1 << 16);
         }
+        const uint32_t pad2 = ((uint32_t)PAD & 0xffffu) * 0x10001u;
+        prof[((0 * CK_LETTERS + 4) * (CB / 2) + h) * 32 + t] = pad2;
+        prof[((1 * CK_LETTERS + 4) * (CB / 2) + h) * 32 + t] = pad2;
     }
     __syncwarp();
 }
@@ -122,8 +125,15 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     // this lane writes the column edge after its last column when that column is a multiple of TW
     const int kout = (j0 + CB) % TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / TW : 0;
     uint32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * M : nullptr;
-    // text characters travel along the lanes with the boundary values; lane 0 reads them
-    uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.textA) | ((uint32_t)__ldg(X.textB) << 8) : 0u;
+    // each row's profile offsets (per pair, its text letter's rows; the padding
+    // letter past the pair's text) travel along the lanes with the boundary
+    // values; lane 0 reads the text
+    auto row_off = [&](int r) -> uint32_t {
+        const int la = r < mA ? ck_code(__ldg(X.textA + r)) : CK_LETTERS - 1;
+        const int lb = r < mB ? ck_code(__ldg(X.textB + r)) : CK_LETTERS - 1;
+        return (uint32_t)(la * NH * 32) | ((uint32_t)((CK_LETTERS + lb) * NH * 32) << 16);
+    };
+    uint32_t ch = 0, ch_next = (t == 0) ? row_off(0) : 0u;
     uint32_t bmax = 0u, brow = 0u;                        // this band: best and its first row, per half
     const int steps = M + 31;
     for (int tau = 0; tau < steps; ++tau) {
@@ -133,8 +143,7 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         const int i = tau - t + 1;
         if (t == 0) {
             ch = ch_next;
-            if (i < M)
-                ch_next = (uint32_t)(i < mA ? __ldg(X.textA + i) : 'A') | ((uint32_t)(i < mB ? __ldg(X.textB + i) : 'A') << 8);
+            if (i < M) ch_next = row_off(i);
             in_hg = nxt_hg;
             in_e = nxt_e;
             if (left && i < M) {
@@ -144,8 +153,8 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
             }
         }
         if (i < 1 || i > M) continue;
-        const uint32_t* pA = X.prof + ((0 * 4 + ck_code(ch & 0xffu)) * NH) * 32 + t;
-        const uint32_t* pB = X.prof + ((1 * 4 + ck_code(ch >> 8)) * NH) * 32 + t;
+        const uint32_t* pA = X.prof + (ch & 0xffffu) + t;
+        const uint32_t* pB = X.prof + (ch >> 16) + t;
         uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
         uint32_t rowmax = 0u;
 #pragma unroll
@@ -180,8 +189,6 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
 #pragma unroll
             for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_uint4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
         }
-        // rows past a pair's text do not count
-        rowmax &= (i <= mA ? 0x0000ffffu : 0u) | (i <= mB ? 0xffff0000u : 0u);
         // strict improvement per half (bits 15 / 31 of d clear): this band's
         // best and the first row holding it; the column is found when the walk
         // recomputes that row
@@ -220,8 +227,11 @@ __device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* p
     }
 }
 
-__global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
+// TG: tiles recomputed per window pass, the walk's and the TG - 1 to its left.
+template <int TG>
+__global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
 {
+    static_assert(TG == 2 || TG == 4, "tile groups split the warp evenly, window rows are 16-byte vectors");
     extern __shared__ uint32_t ck_smem[];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -582,19 +592,22 @@ __global__ void __launch_bounds__(128, 5) sw16ck_kernel(Sw16Args A)
 
 static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t); }
 
-int sw16ck_max_slots(int sm_count)
+int sw16ck_max_slots(int sm_count, int window)
 {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel, 128, sw16ck_smem());
+    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4>, 128, sw16ck_smem());
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2>, 128, sw16ck_smem());
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
-cudaError_t launch_sw16ck(const Sw16Args& A, int slots, cudaStream_t st)
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, cudaStream_t st)
 {
     if (A.nwork <= 0) return cudaSuccess;
+    if (window != 2 && window != 4) return cudaErrorInvalidValue;
     const int blocks = (slots + 3) / 4;
     launch_begin(K_SW16X2_TRACE, st);
-    sw16ck_kernel<<<blocks, 128, sw16ck_smem(), st>>>(A);
+    if (window == 4) sw16ck_kernel<4><<<blocks, 128, sw16ck_smem(), st>>>(A);
+    else sw16ck_kernel<2><<<blocks, 128, sw16ck_smem(), st>>>(A);
     launch_end(K_SW16X2_TRACE, st);
     return cudaGetLastError();
 }

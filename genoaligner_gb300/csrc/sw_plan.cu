@@ -3,8 +3,9 @@
 // The plan sorts the pairs of a batch into the kernels' work lists, largest
 // first: the two-pairs-per-warp 16-bit list (pure-ACGT pairs whose scores fit
 // 16 bits; consecutive entries share a warp) and the 32-bit lists (short and
-// long shapes of sw32ck.cu).  It is a counting sort on a log-scale size key
-// (64 buckets per doubling of (m + 31) * n) in four kernels -- classify and
+// long shapes of sw32ck.cu).  It is a counting sort on a size key (16-bit
+// pairs: forward column extent, then rows; 32-bit pairs: 64 buckets per
+// doubling of (m + 31) * n) in four kernels -- classify and
 // count, scan, scatter, pack -- and leaves on the device the work lists in
 // the order the launches read them plus, per list, its length and the largest
 // per-warp memory its items need; the host reads back that one small record.
@@ -14,7 +15,20 @@ namespace ga {
 
 constexpr int SP_NB = 4096;              // size buckets per list
 
-// Bucket of a pair of m rows and n columns, largest first.
+// Bucket of a 16-bit pair: consecutive entries share a warp and run with the
+// larger of their row counts and forward column extents, so the key orders by
+// column extent (ck_ncol, in 64-column steps, widest first), then by rows
+// (18 buckets per doubling, most first): neighbours then have near-equal
+// shapes, not only near-equal cell counts.
+__device__ __forceinline__ int sp_key16(int m, int n)
+{
+    const int ncls = min(31, ck_ncol(max(n, 1)) / 64);
+    const float lm = log2f((float)max(m, 16) * (1.0f / 16.0f));
+    const int mb = min(127, (int)(18.0f * lm));
+    return (31 - ncls) * 128 + (127 - mb);
+}
+
+// Bucket of a 32-bit pair of m rows and n columns, largest first.
 __device__ __forceinline__ int sp_key(int m, int n)
 {
     const uint64_t c = (uint64_t)(max(m, 0) + 31) * (uint64_t)max(n, 1);
@@ -38,8 +52,8 @@ __global__ void sp_classify_kernel(SwPlanArgs P)
             } else {
                 const bool u16 = P.use16 && P.D.pure[p] && P.D.pure[n + p] &&
                                  sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
-                const int list = u16 ? SP_L16 : (sw32ck_long(m, nn) ? SP_L32LONG : SP_L32);
-                it = list * SP_NB + sp_key(m, nn);
+                const int list = u16 ? SP_L16 : (sw32ck_long(m, nn, P.long_log2) ? SP_L32LONG : SP_L32);
+                it = list * SP_NB + (u16 ? sp_key16(m, nn) : sp_key(m, nn));
                 atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_EDGE), (unsigned long long)(2 * max(m, 0)));
             }
             P.item[p] = it;
@@ -125,13 +139,13 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
                 w[2 * q + 1] = b;
                 const int M = max(P.D.a_len[a], b >= 0 ? P.D.a_len[b] : 0);
                 const int N = max(P.D.b_len[a], b >= 0 ? P.D.b_len[b] : 0);
-                local = max(local, (unsigned long long)sw16ck_dir_words(M, N));
+                local = max(local, (unsigned long long)sw16ck_dir_words(M, N, P.window));
             }
         } else {
             for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += stride) {
                 const int a = srt[q];
                 w[q] = a;
-                local = max(local, (unsigned long long)sw32ck_dir_words(P.D.a_len[a], P.D.b_len[a]));
+                local = max(local, (unsigned long long)sw32ck_dir_words(P.D.a_len[a], P.D.b_len[a], P.long_log2));
             }
         }
 #pragma unroll

@@ -23,7 +23,8 @@ __host__ __device__ inline bool sw16_eligible(int m, int n, int match, int misma
 }
 
 // sw16ck.cu: checkpoint rows every CK_K rows, column edges every CK_TW
-// columns, recompute windows of CK_TG tiles of CK_K x CK_TW cells.
+// columns, recompute windows of `window` tiles of CK_K x CK_TW cells (2 or 4;
+// CK_TG is the default).
 constexpr int CK_K = 64;
 constexpr int CK_TW = 64;
 constexpr int CK_TG = 2;
@@ -48,17 +49,17 @@ __host__ __device__ inline int ck_ncol(int N)
 
 // 32-bit words of one warp slot for an item of at most M rows and N columns:
 // checkpoint rows, column edges (16-byte aligned end), the window table.
-__host__ __device__ inline int64_t sw16ck_dir_words(int M, int N)
+__host__ __device__ inline int64_t sw16ck_dir_words(int M, int N, int window)
 {
     const int64_t ncol = ck_ncol(N);
     return 2 * (int64_t)ck_rows(M) * ncol + (2 * (ncol / CK_TW) * (int64_t)M + 3) / 4 * 4 +
-           (int64_t)CK_K * CK_TG * CK_TW;
+           (int64_t)CK_K * window * CK_TW;
 }
 
 // ---- 32-bit one-pair-per-warp checkpointed kernel (sw32ck.cu) ---------------
 constexpr int C32_C = 16;                // forward columns per lane, full bands
 constexpr int C32_BW = 32 * C32_C;
-constexpr int64_t C32_LONG_CELLS = (int64_t)1 << 24;   // the long-pair shape above this many cells
+constexpr int C32_LONG_LOG2 = 24;       // default: the long-pair shape above 2^24 cells
 
 __host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
 __host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }
@@ -67,13 +68,18 @@ __host__ __device__ inline int c32_ncol(int n)
     const int full = n > 0 ? (n - 1) / C32_BW : 0;
     return full * C32_BW + 32 * c32_last_cb(n - full * C32_BW);
 }
-__host__ __device__ inline bool sw32ck_long(int m, int n) { return (int64_t)m * n > C32_LONG_CELLS; }
+// The long-pair shape (512-row blocks, 512-column tiles) for pairs above
+// 2^long_log2 cells, the short one (64 x 64) below.
+__host__ __device__ inline bool sw32ck_long(int m, int n, int long_log2)
+{
+    return (int64_t)m * n > ((int64_t)1 << long_log2);
+}
 
 // 32-bit words of one warp slot for a pair of m rows and n columns:
 // checkpoint rows, column edges, the tile table.
-__host__ __device__ inline int64_t sw32ck_dir_words(int m, int n)
+__host__ __device__ inline int64_t sw32ck_dir_words(int m, int n, int long_log2)
 {
-    const bool lg = sw32ck_long(m, n);
+    const bool lg = sw32ck_long(m, n, long_log2);
     const int K = lg ? 512 : 64, CT = lg ? 16 : 2, TW = 32 * CT, NWT = CT >= 8 ? CT / 8 : 1;
     const int64_t stride = ((int64_t)c32_ncol(n) + TW - 1) / TW * TW;
     return 2 * (int64_t)c32_rows(m, K) * stride + 2 * (stride / TW) * (int64_t)m + (int64_t)(K + 31) * 32 * NWT;

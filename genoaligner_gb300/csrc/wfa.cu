@@ -290,6 +290,20 @@ cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, 
     return cudaGetLastError();
 }
 
+// The 2-bit words and non-ACGT masks of a whole byte arena (seq_bytes a
+// multiple of 32, seq 16-byte aligned): packed[c], bad[c] for every chunk c.
+cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* bad, cudaStream_t st)
+{
+    const int64_t nchunks = seq_bytes / 32;
+    if (nchunks <= 0) return cudaSuccess;
+    int64_t cblocks = (nchunks + 255) / 256;
+    if (cblocks > 152 * 32) cblocks = 152 * 32;
+    launch_begin(K_PACK, st);
+    pack_chunks_kernel<<<(int)cblocks, 256, 0, st>>>(seq, nchunks, packed, bad);
+    launch_end(K_PACK, st);
+    return cudaGetLastError();
+}
+
 // 64-bit words of a packed arena for seq_bytes of sequence: the 2-bit words
 // (+2 spare, read by two-word fetch windows) then one 32-bit mask per chunk.
 int64_t packed_arena_words(int64_t seq_bytes)

@@ -251,3 +251,70 @@ WORKLOADS = {
     "wfa_mixed_1m": wfa_mixed,
     "sw_long_4k": sw_long_4k,
 }
+
+
+# ------------------------------------------------------------ gene families --
+_STOPS1 = {b"TAA", b"TAG", b"TGA"}
+_SENSE = [bytes(c) for c in (a + b + c for a in (b"A", b"C", b"G", b"T") for b in (b"A", b"C", b"G", b"T")
+                             for c in (b"A", b"C", b"G", b"T")) if bytes(c) not in _STOPS1 | {b"AGA", b"AGG"}]
+
+
+def gene_family(n_records=200, codons=300, seed=6):
+    """A seeded protein-coding gene family for one-reference-against-many work.
+
+    Returns (records, baits): lists of (id, sequence bytes).  The bait file
+    holds a clean CDS (ATG, `codons` sense codons, TAA) and a fragment of it
+    shifted by one base with an inserted stop; the records are copies of the
+    CDS at 0-4 % substitutions with, by class: nothing else; an in-frame
+    3-base deletion; a 1- or 2-base indel (frameshift); a premature stop;
+    a 40-70 % fragment; bases outside ACGT; 0-200 bp flanks; or an unrelated
+    random sequence."""
+    rng = np.random.default_rng(seed)
+    sense = np.array([np.frombuffer(c, np.uint8) for c in _SENSE])
+    cds = np.concatenate([np.frombuffer(b"ATG", np.uint8),
+                          sense[rng.integers(0, len(_SENSE), size=codons)].reshape(-1),
+                          np.frombuffer(b"TAA", np.uint8)])
+    frag = np.concatenate([random_bases(rng, 1), cds[30: len(cds) // 2], np.frombuffer(b"TGA", np.uint8),
+                           cds[len(cds) // 2: -60]])
+    baits = [("bait_frag shifted fragment", frag.tobytes()), ("bait_cds clean CDS", cds.tobytes())]
+    records = []
+    for r in range(n_records):
+        cls = r % 9
+        s = cds.copy()
+        rate = float(rng.uniform(0.0, 0.04))
+        sub = np.nonzero(rng.random(s.shape[0]) < rate)[0]
+        s[sub] = ACGT[(_LUT[s[sub]] + rng.integers(1, 4, size=sub.size)) % 4]
+        if cls == 1:
+            k = 3 * int(rng.integers(10, codons - 10))
+            s = np.concatenate([s[:k], s[k + 3:]])
+        elif cls == 2:
+            k = int(rng.integers(30, s.shape[0] - 30))
+            d = int(rng.integers(1, 3))
+            s = np.concatenate([s[:k], s[k + d:]]) if rng.random() < 0.5 else \
+                np.concatenate([s[:k], random_bases(rng, d), s[k:]])
+        elif cls == 3:
+            k = 3 * int(rng.integers(20, codons - 20))
+            s[k:k + 3] = np.frombuffer(b"TAG", np.uint8)
+        elif cls == 4:
+            L = int(s.shape[0] * rng.uniform(0.4, 0.7))
+            a = int(rng.integers(0, s.shape[0] - L))
+            s = s[a:a + L]
+        elif cls == 5:
+            s[rng.integers(0, s.shape[0], size=int(rng.integers(1, 6)))] = ord("N")
+        elif cls == 6:
+            s = np.concatenate([random_bases(rng, int(rng.integers(0, 200))), s,
+                                random_bases(rng, int(rng.integers(0, 200)))])
+        elif cls == 7:
+            s = random_bases(rng, int(rng.integers(300, 1200)))
+        records.append((f"rec{r:04d} class{cls}", s.tobytes()))
+    return records, baits
+
+
+def write_fasta(path, records, width=60, crlf=False):
+    """Write (id-and-description, sequence) records as FASTA, `width` bases per line."""
+    end = b"\r\n" if crlf else b"\n"
+    with open(path, "wb") as f:
+        for head, seq in records:
+            f.write(b">" + head.encode() + end)
+            for k in range(0, len(seq), width):
+                f.write(seq[k:k + width] + end)

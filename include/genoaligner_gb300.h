@@ -266,6 +266,128 @@ int32_t ga_wfa_device_noalloc(const ga_device_batch* batch, int32_t smax, int32_
                               int32_t* out_score, int32_t* out_len, char* out_cigar,
                               void* stream, const char** err);
 
+/* --------------------------------------------------------------- ingest -- */
+
+/* A FASTA file read into one device-ready arena (no counterpart in the
+ * reference, whose reader, include/genoaligner/io/fasta.hpp, returns
+ * std::strings; that reader is kept in include/genoaligner/io/fasta.hpp with
+ * the same rules).  Record i's sequence (raw bytes, line breaks removed) is
+ * arena[offsets[i] .. offsets[i] + lengths[i]); offsets are multiples of 32,
+ * padding is zero and the arena ends with 64 spare bytes, so the arena can be
+ * uploaded as the `seq` of a ga_device_batch as is.  The arena is pinned host
+ * memory when a CUDA device is present (ga_fasta_pinned).  Parsing follows the
+ * reference's reader rules; a malformed input fails with GA_INVALID_ARGUMENT
+ * and the reference's message and line in *err (valid until the calling
+ * thread's next failing ga_fasta call). */
+typedef struct ga_fasta ga_fasta;
+int32_t        ga_fasta_read(const char* path, ga_fasta** out, const char** err);
+int32_t        ga_fasta_parse(const char* data, int64_t bytes, ga_fasta** out, const char** err);
+int32_t        ga_fasta_count(const ga_fasta* f);
+const char*    ga_fasta_id(const ga_fasta* f, int32_t i);
+const char*    ga_fasta_description(const ga_fasta* f, int32_t i);
+const uint8_t* ga_fasta_arena(const ga_fasta* f, int64_t* bytes);
+const int64_t* ga_fasta_offsets(const ga_fasta* f);
+const int32_t* ga_fasta_lengths(const ga_fasta* f);
+int32_t        ga_fasta_pinned(const ga_fasta* f);
+/* Copy the whole arena to device memory (one host-to-device copy on `stream`;
+ * NULL: the default stream, synchronised before return). */
+int32_t        ga_fasta_upload(const ga_fasta* f, void* device_arena, void* stream);
+void           ga_fasta_free(ga_fasta* f);
+
+/* Device-side 2-bit packing of a byte arena (seq: device, 16-byte aligned;
+ * seq_bytes a multiple of 32): for every 32-byte chunk c, packed[c] holds its
+ * 32 codes, 2 bits each, first byte lowest (A 0, C 1, G 2, T 3 under
+ * ((b >> 1) ^ (b >> 2)) & 3), and bit k of mask[c] is set when byte 32c + k is
+ * not one of A, C, G, T (upper case).  The WFA path packs its arena this way. */
+int32_t ga_pack_2bit_device(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* mask,
+                            void* stream);
+
+/* The reference's SW result checks (sw_validate, src/api/api.cpp:114-156) on
+ * the device, after ga_sw_device with trace = 1: flags[i] = rescore_ok |
+ * wellformed_ok << 1 for pairs with a CIGAR (the ops consume exactly the
+ * reported span, M only on equal bytes and X on unequal ones, and re-score to
+ * the reported score), 0 for the others.  Device pointers. */
+int32_t ga_sw_validate_device(const ga_device_batch* batch, ga_sw_scoring scoring, const int32_t* score,
+                              const int32_t* pos, const int32_t* len, const char* cigar, uint8_t* flags,
+                              void* stream);
+
+/* CIGAR post-processing of an SW batch of records against one reference
+ * (the per-record checks of the reference's tools/gene_qc.cpp), on the
+ * device, after ga_sw_device with trace = 1 (a = record text, b = the
+ * reference, read in frame `frame` 0..2; genetic code `code` 1 = standard,
+ * 2 = vertebrate mitochondrial).  out[4*i .. 4*i+3] = fs_runs (indel runs
+ * whose length is not a multiple of 3), fs_net ((inserted - deleted) mod 3,
+ * as -1, 0, +1), stops (stop codons read in reference codons fully paired
+ * with contiguous text bases, the span's own terminator excluded), stop_end
+ * (1 when that terminator was found); zeros for pairs without a positive
+ * score.  All pointers are device pointers; score/pos/len/cigar are
+ * ga_sw_device's outputs. */
+int32_t ga_sw_qc_device(const ga_device_batch* batch, const int32_t* score, const int32_t* pos,
+                        const int32_t* len, const char* cigar, int32_t frame, int32_t code, int32_t* out,
+                        void* stream);
+
+/* ------------------------------------------------------------- autotuner -- */
+
+/* How work is laid onto the GPU (no counterpart in the reference).  These
+ * settings pick kernel variants, tile widths and lanes per pair, never what is
+ * computed: every setting gives the same results.  One setting per device,
+ * used by every later call on that device (ga_sw_device, ga_align_sw_batch,
+ * the learned WFA path). */
+typedef struct ga_tune {
+    int32_t sw_pack16;      /* SW traceback, pure-ACGT pairs whose scores fit 16 bits:
+                               1 = two pairs per warp in 16-bit halves (inter-sequence),
+                               0 = one pair per warp in 32 bits (intra-sequence) */
+    int32_t sw_window;      /* 16-bit traceback: tiles of 64 columns recomputed per
+                               window of the walk, 2 (16 lanes x 4 columns per tile)
+                               or 4 (8 lanes x 8 columns) */
+    int32_t sw_long_log2;   /* 32-bit traceback: pairs above 2^sw_long_log2 cells take
+                               the 512 x 512 tile shape, the rest 64 x 64; 16 .. 30 */
+    int32_t wfa_lane_smax;  /* learned WFA: pairs whose first smax is <= this run one
+                               per lane, 32 per warp (0 = none: one pair per warp); 0 .. 15 */
+    int32_t reserved[4];
+} ga_tune;
+
+/* One timed candidate of an autotuning run. */
+typedef struct ga_tune_trial {
+    ga_tune tune;
+    double  ms;             /* mean device time of one call over the timed repetitions */
+} ga_tune_trial;
+
+/* The built-in setting (chosen by this tuner on a GB300). */
+int32_t ga_tune_default(ga_tune* out);
+/* Read / replace the current device's setting; ga_tune_set refuses values out
+ * of range with GA_INVALID_ARGUMENT and keeps the old setting. */
+int32_t ga_tune_get(ga_tune* out);
+int32_t ga_tune_set(const ga_tune* t);
+
+/* Time candidate settings on an SW traceback batch (arguments and outputs as
+ * ga_sw_device with trace = 1) and keep the fastest for the current device.
+ * Each candidate runs once untimed, then `reps` timed calls (reps <= 0: 2) on
+ * the library's own stream.  Coordinate search: sw_pack16, then sw_window
+ * (when pack16 is chosen), then sw_long_log2 (when the batch has pairs above
+ * 2^20 cells).  chosen (may be NULL) gets the setting kept; trials[0 ..
+ * *n_trials) (may be NULL) every candidate timed.  The outputs hold the batch's
+ * results on return. */
+int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int64_t trace_cell_limit,
+                       int32_t* out_score, int32_t* out_pos, int32_t* out_len, char* out_cigar,
+                       int32_t reps, ga_tune* chosen, ga_tune_trial* trials, int32_t max_trials,
+                       int32_t* n_trials, const char** err);
+
+/* The same for the learned WFA path (arguments as ga_wfa_device_ex with
+ * opt->learned = 1; the cost model must be loaded): candidates for
+ * wfa_lane_smax. */
+int32_t ga_autotune_wfa(const ga_device_batch* batch, int32_t smax, int32_t trace,
+                        int32_t* out_score, int32_t* out_len, char* out_cigar,
+                        int32_t reps, ga_tune* chosen, ga_tune_trial* trials, int32_t max_trials,
+                        int32_t* n_trials, const char** err);
+
+/* Write every device's setting that differs from the default to a text file
+ * (one line per device: name, then the four fields), or load such a file:
+ * lines naming the current device's model set its setting.  GA_INVALID_ARGUMENT
+ * on an unreadable / malformed file (nothing is changed then). */
+int32_t ga_tune_save(const char* path);
+int32_t ga_tune_load(const char* path);
+
 /* ------------------------------------------------------------ provenance -- */
 
 /* Mirror backend_name / device_name / device_available (api.hpp:485-487). */
