@@ -91,7 +91,8 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_tune_set", "ga_autotune_sw", "ga_autotune_wfa", "ga_tune_save", "ga_tune_load",
            "ga_fasta_read", "ga_fasta_parse", "ga_fasta_count", "ga_fasta_id", "ga_fasta_description",
            "ga_fasta_arena", "ga_fasta_offsets", "ga_fasta_lengths", "ga_fasta_pinned", "ga_fasta_upload",
-           "ga_fasta_free", "ga_pack_2bit_device", "ga_sw_qc_device", "ga_sw_validate_device"]
+           "ga_fasta_free", "ga_pack_2bit_device", "ga_sw_qc_device", "ga_sw_validate_device",
+           "ga_wfa_validate_device"]
 
 _lib = None
 
@@ -203,6 +204,8 @@ def load(build: bool = True):
     L.ga_sw_qc_device.restype = i32
     L.ga_sw_validate_device.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, p, p, p, p, p, p]
     L.ga_sw_validate_device.restype = i32
+    L.ga_wfa_validate_device.argtypes = [ctypes.POINTER(DeviceBatch), p, p, p, p, p]
+    L.ga_wfa_validate_device.restype = i32
     _lib = L
     return L
 
@@ -896,3 +899,12 @@ def sw_qc_device(batch: "DeviceBatchT", out_score, out_pos, out_len, out_cigar, 
                                 out_cigar.data_ptr(), int(frame), int(code), out.data_ptr(), stream)
     if st != GA_OK:
         raise RuntimeError(f"ga_sw_qc_device failed ({st})")
+
+
+def wfa_validate_device(batch: "DeviceBatchT", out_score, out_len, out_cigar, flags, stream=None):
+    """rescore_ok | wellformed_ok << 1 per pair into the uint8 device tensor
+    `flags` (ga_wfa_validate_device), from ga_wfa_device's outputs."""
+    st = load().ga_wfa_validate_device(ctypes.byref(batch.c), out_score.data_ptr(), out_len.data_ptr(),
+                                       out_cigar.data_ptr(), flags.data_ptr(), stream)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_wfa_validate_device failed ({st})")

@@ -46,9 +46,14 @@ BatchResult align_batch_ex(const std::vector<AlignRequest>& reqs, const AlignOpt
             res += r.resolved;
             if (v.trace && r.resolved && v.len[i] > 0) {
                 r.cigar.assign(v.cig + v.slot_end[i] - v.len[i], (size_t)v.len[i]);
-                ga::wfa_validate(r.cigar.data(), (int)r.cigar.size(), r.score, reqs[(size_t)i].pattern,
-                                 reqs[(size_t)i].pattern_len, reqs[(size_t)i].text, reqs[(size_t)i].text_len,
-                                 &r.rescore_ok, &r.wellformed_ok);
+                if (v.vflags) {
+                    r.rescore_ok = v.vflags[i] & 1;
+                    r.wellformed_ok = (v.vflags[i] >> 1) & 1;
+                } else {
+                    ga::wfa_validate(r.cigar.data(), (int)r.cigar.size(), r.score, reqs[(size_t)i].pattern,
+                                     reqs[(size_t)i].pattern_len, reqs[(size_t)i].text, reqs[(size_t)i].text_len,
+                                     &r.rescore_ok, &r.wellformed_ok);
+                }
             }
         }
         resolved.fetch_add(res);

@@ -491,30 +491,31 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
 
     WfaScratch S;
     size_wfa(S, n, smax, trace, learned, c->sm_count);
-    // layout: [a_off a_len b_off b_len out_off | seq] [score len cigar | err] then device scratch
+    // layout: [a_off a_len b_off b_len out_off | seq] [score len cigar checks | err] then device scratch
     int64_t *ha, *hb, *ho, *da, *db, *dout;
     int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
-    uint8_t *hseq, *dseq;
+    uint8_t *hseq, *dseq, *hvf, *dvf;
     char *hcg, *dcg;
     auto io = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po, uint8_t** ps,
-                  int32_t** psc, int32_t** pln, char** pcg, int32_t** per) {
+                  int32_t** psc, int32_t** pln, char** pcg, uint8_t** pvf, int32_t** per) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
         *po = k.take<int64_t>(n);
         *ps = k.take<uint8_t>(arena);
         *psc = k.take<int32_t>(n); *pln = k.take<int32_t>(n); *pcg = k.take<char>(cig + 1);
+        *pvf = k.take<uint8_t>(trace ? n : 0);
         *per = k.take<int32_t>(1, 4);
     };
     Carve hk(nullptr), dk(nullptr);
-    io(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &her);
-    io(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &der);
+    io(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &hvf, &her);
+    io(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &dvf, &der);
     carve_wfa(dk, S, n, arena, trace, learned);
     if (fail_here(1) || !ensure_dev(c, dk.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
     if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
     {
         Carve h(c->host), d(c->dev);
-        io(h, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &her);
-        io(d, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &der);
+        io(h, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &hvf, &her);
+        io(d, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &dvf, &der);
         carve_wfa(d, S, n, arena, trace, learned);
     }
 
@@ -546,12 +547,13 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
     else if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace, lane_smax, dsc, dln, dcg, der, c->stream);
     else le = enqueue_wfa(S, D, smax, trace, learned, lane_smax, dsc, dln, dcg, der, c->stream);
     if (learned) note_route(c, S);
+    if (le == cudaSuccess && trace) le = launch_wfa_validate(D, dsc, dln, dcg, dvf, c->stream);
     if (le != cudaSuccess) {
         cudaGetLastError();
         *err = E_LAUNCH;
         return GA_DEVICE_ERROR;
     }
-    // outputs are contiguous on both sides: score, len, cigar, err
+    // outputs are contiguous on both sides: score, len, cigar, checks, err
     const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
     t_d2h = (int64_t)out_bytes;
     if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
@@ -565,7 +567,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    WfaView v{hsc, hln, hcg, slot_end.data(), trace};
+    WfaView v{hsc, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr};
     parallel_for(n, 1024, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
     return GA_OK;
 }
@@ -1149,8 +1151,13 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
                 r.cigar_offset = at;
                 r.cigar_len = v.len[i];
                 bool rs = false, wf = false;
-                wfa_validate(cigar_buf + at, v.len[i], r.score, reqs[i].pattern, reqs[i].pattern_len,
-                             reqs[i].text, reqs[i].text_len, &rs, &wf);
+                if (v.vflags) {
+                    rs = v.vflags[i] & 1;
+                    wf = (v.vflags[i] >> 1) & 1;
+                } else {
+                    wfa_validate(cigar_buf + at, v.len[i], r.score, reqs[i].pattern, reqs[i].pattern_len,
+                                 reqs[i].text, reqs[i].text_len, &rs, &wf);
+                }
                 r.rescore_ok = rs;
                 r.wellformed_ok = wf;
             }
@@ -1553,6 +1560,26 @@ const char* ga_device_name(void)
         cudaGetLastError();
     });
     return name;
+}
+
+int32_t ga_wfa_validate_device(const ga_device_batch* b, const int32_t* score, const int32_t* len, const char* cigar,
+                               uint8_t* flags, void* stream)
+{
+    if (!b || b->n < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len ||
+                                         !b->out_off || !score || !len || !cigar || !flags)))
+        return GA_INVALID_ARGUMENT;
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = b->n;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = launch_wfa_validate(D, score, len, cigar, flags, st);
+    if (e == cudaSuccess && !stream) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
 }
 
 int32_t ga_sw_validate_device(const ga_device_batch* b, ga_sw_scoring sc, const int32_t* score, const int32_t* pos,

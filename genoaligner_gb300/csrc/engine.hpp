@@ -21,6 +21,7 @@ struct WfaView {
     const char* cig;
     const int64_t* slot_end;
     bool trace;
+    const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
 };
 using WfaFinish = std::function<void(int64_t lo, int64_t hi, const WfaView& v)>;
 

@@ -77,6 +77,9 @@ struct RoutedArgs {
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 int64_t packed_arena_words(int64_t seq_bytes);
 cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* bad, cudaStream_t st);
+// WFA result checks on the device (wfa.cu): flags[p] = rescore_ok | wellformed_ok << 1.
+cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const int32_t* len, const char* cig,
+                                uint8_t* flags, cudaStream_t st);
 cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
 bool cost_model_loaded();

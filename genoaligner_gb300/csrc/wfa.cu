@@ -304,6 +304,57 @@ cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* p
     return cudaGetLastError();
 }
 
+// The reference's WFA result checks (validate, src/api/api.cpp:84-112), one
+// thread per pair over its CIGAR (at the end of its slot): wellformed when
+// the ops consume exactly the pattern and the text with M only on equal bytes
+// and X only on unequal ones; rescore when the X, I and D ops number the
+// score.  flags[p] = rescore_ok | wellformed_ok << 1 for pairs with a CIGAR,
+// 0 for the others.
+__global__ void wfa_validate_kernel(PairDesc D, const int32_t* __restrict__ score, const int32_t* __restrict__ len,
+                                    const char* __restrict__ cig, uint8_t* __restrict__ flags)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
+        const int s = score[p], L = len[p];
+        if (s < 0 || L <= 0) { flags[p] = 0; continue; }
+        const int m = D.a_len[p], n = D.b_len[p];
+        const uint8_t* P = D.seq + D.a_off[p];
+        const uint8_t* T = D.seq + D.b_off[p];
+        const char* cg = cig + D.out_off[p] + (m + n) - L;
+        int cost = 0, pi = 0, ti = 0;
+        bool ok = true;
+        for (int q = 0; q < L; ++q) {
+            const char op = cg[q];
+            if (op == 'M' || op == 'X') {
+                if (pi >= m || ti >= n || ((P[pi] == T[ti]) != (op == 'M'))) ok = false;
+                cost += op == 'X';
+                ++pi;
+                ++ti;
+            } else if (op == 'I') {
+                ++ti;
+                ++cost;
+            } else if (op == 'D') {
+                ++pi;
+                ++cost;
+            } else {
+                ok = false;
+            }
+        }
+        flags[p] = (uint8_t)((cost == s ? 1 : 0) | (ok && pi == m && ti == n ? 2 : 0));
+    }
+}
+
+cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const int32_t* len, const char* cig,
+                                uint8_t* flags, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    int blocks = (D.n + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    launch_begin(K_PACK, st);
+    wfa_validate_kernel<<<blocks, 128, 0, st>>>(D, score, len, cig, flags);
+    launch_end(K_PACK, st);
+    return cudaGetLastError();
+}
+
 // 64-bit words of a packed arena for seq_bytes of sequence: the 2-bit words
 // (+2 spare, read by two-word fetch windows) then one 32-bit mask per chunk.
 int64_t packed_arena_words(int64_t seq_bytes)

@@ -302,6 +302,13 @@ void           ga_fasta_free(ga_fasta* f);
 int32_t ga_pack_2bit_device(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* mask,
                             void* stream);
 
+/* The reference's WFA result checks (validate, src/api/api.cpp:84-112) on the
+ * device, after ga_wfa_device with trace = 1: flags[i] = rescore_ok |
+ * wellformed_ok << 1 for pairs with a CIGAR, 0 for the others.  The host entry
+ * ga_align_batch runs the same kernel.  Device pointers. */
+int32_t ga_wfa_validate_device(const ga_device_batch* batch, const int32_t* score, const int32_t* len,
+                               const char* cigar, uint8_t* flags, void* stream);
+
 /* The reference's SW result checks (sw_validate, src/api/api.cpp:114-156) on
  * the device, after ga_sw_device with trace = 1: flags[i] = rescore_ok |
  * wellformed_ok << 1 for pairs with a CIGAR (the ops consume exactly the

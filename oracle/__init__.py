@@ -78,8 +78,36 @@ def lib():
         L.ora_sw_batch.restype = ctypes.c_int
         L.ora_edit_distance_batch.argtypes = [i32, p, p, p, p, p, p, p]
         L.ora_edit_distance_batch.restype = ctypes.c_int
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.ora_wfa_validate.argtypes = [ctypes.c_char_p, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, i32, ip, ip]
+        L.ora_wfa_validate.restype = None
+        L.ora_sw_validate.argtypes = [ctypes.c_char_p, i32, ctypes.c_char_p, i32, i32, i32, ctypes.c_char_p, i32,
+                                      i32, i32, _OraScoring, i32, ip, ip]
+        L.ora_sw_validate.restype = None
         _lib = L
     return _lib
+
+
+class _OraScoring(ctypes.Structure):
+    _fields_ = [("match", ctypes.c_int), ("mismatch", ctypes.c_int), ("gap_open", ctypes.c_int),
+                ("gap_extend", ctypes.c_int)]
+
+
+def wfa_validate(cigar: bytes, score: int, pattern: bytes, text: bytes):
+    """(rescore_ok, wellformed_ok) of one WFA CIGAR (validate, src/api/api.cpp:84-106)."""
+    rs, wf = ctypes.c_int(0), ctypes.c_int(0)
+    lib().ora_wfa_validate(cigar, len(cigar), score, pattern, len(pattern), text, len(text), ctypes.byref(rs),
+                           ctypes.byref(wf))
+    return bool(rs.value), bool(wf.value)
+
+
+def sw_validate(cigar: bytes, text: bytes, si: int, ei: int, pattern: bytes, sj: int, ej: int, scoring, score: int):
+    """(rescore_ok, wellformed_ok) of one SW CIGAR over its span (sw_validate,
+    src/api/api.cpp:114-156)."""
+    rs, wf = ctypes.c_int(0), ctypes.c_int(0)
+    lib().ora_sw_validate(cigar, len(cigar), text, len(text), si, ei, pattern, len(pattern), sj, ej,
+                          _OraScoring(*scoring), score, ctypes.byref(rs), ctypes.byref(wf))
+    return bool(rs.value), bool(wf.value)
 
 
 def _ptr(a: np.ndarray):
