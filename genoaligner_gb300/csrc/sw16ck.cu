@@ -120,37 +120,46 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     uint32_t diag_in = NGO2, out_hg = NGO2, out_e = 0u;
     // left boundary: the column edge at column b0
     const uint32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / TW - 1) * M : nullptr;
-    uint32_t nxt_hg = NGO2, nxt_e = 0u;
-    if (t == 0 && left) { nxt_hg = left[0]; nxt_e = left[1]; }
     // this lane writes the column edge after its last column when that column is a multiple of TW
     const int kout = (j0 + CB) % TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / TW : 0;
     uint32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * M : nullptr;
     // each row's profile offsets (per pair, its text letter's rows; the padding
     // letter past the pair's text) travel along the lanes with the boundary
-    // values; lane 0 reads the text
+    // values.  Lane 0's inputs of 32 rows at a time -- the offsets and the left
+    // edge -- are read by all lanes together (lane u: row 32k + u) and handed
+    // to lane 0 by a shuffle each step, so no step runs a lane-0-only branch.
     auto row_off = [&](int r) -> uint32_t {
         const int la = r < mA ? ck_code(__ldg(X.textA + r)) : CK_LETTERS - 1;
         const int lb = r < mB ? ck_code(__ldg(X.textB + r)) : CK_LETTERS - 1;
         return (uint32_t)(la * NH * 32) | ((uint32_t)((CK_LETTERS + lb) * NH * 32) << 16);
     };
-    uint32_t ch = 0, ch_next = (t == 0) ? row_off(0) : 0u;
+    uint32_t rb_off = 0u, rb_hg = NGO2, rb_e = 0u;       // this lane's row of the current 32
+    uint32_t ch = 0;
     uint32_t bmax = 0u, brow = 0u;                        // this band: best and its first row, per half
     const int steps = M + 31;
     for (int tau = 0; tau < steps; ++tau) {
+        if ((tau & 31) == 0 && tau < M) {
+            const int r = tau + t;
+            if (r < M) {
+                rb_off = row_off(r);
+                if (left) {
+                    const uint2 lv = *reinterpret_cast<const uint2*>(left + 2 * r);
+                    rb_hg = lv.x;
+                    rb_e = lv.y;
+                }
+            }
+        }
         uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
         uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
         ch = __shfl_up_sync(FULL, ch, 1);
+        const uint32_t l_off = __shfl_sync(FULL, rb_off, tau & 31);
+        const uint32_t l_hg = __shfl_sync(FULL, rb_hg, tau & 31);
+        const uint32_t l_e = __shfl_sync(FULL, rb_e, tau & 31);
         const int i = tau - t + 1;
         if (t == 0) {
-            ch = ch_next;
-            if (i < M) ch_next = row_off(i);
-            in_hg = nxt_hg;
-            in_e = nxt_e;
-            if (left && i < M) {
-                const uint2 lv = *reinterpret_cast<const uint2*>(left + 2 * i);
-                nxt_hg = lv.x;
-                nxt_e = lv.y;
-            }
+            ch = l_off;
+            in_hg = l_hg;
+            in_e = l_e;
         }
         if (i < 1 || i > M) continue;
         const uint32_t* pA = X.prof + (ch & 0xffffu) + t;
@@ -386,25 +395,38 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
             uint32_t out_hg = B2 - GO2, out_e = B2;
             const uint8_t* tA = textA + (ti0[0] - 1);
             const uint8_t* tB = textB + (ti0[1] - 1);
-            uint32_t ch = 0;
-            uint32_t ch_next = tl == 0 ? (uint32_t)(rows0 > 0 ? __ldg(tA) : 'A') | ((uint32_t)(rows1 > 0 ? __ldg(tB) : 'A') << 8) : 0u;
+            // each row's profile offsets travel along a group's lanes with the
+            // boundary values; the groups' first lanes get theirs, and the row's
+            // left edge, without a branch of their own: the offsets of 32 rows at
+            // a time are read by all lanes (lane u: row 32k + u) and shuffled out
+            uint32_t ch = 0, rb_ch = 0;
             const uint32_t* pA0 = prof + (0 * 4 * (CT / 2)) * 32 + t;
             const uint32_t* pB0 = prof + (1 * 4 * (CT / 2)) * 32 + t;
             uint32_t* hrow = Ht + g * TW + CT * tl;                         // + (row - 1) * WCOL
             for (int tau = 0; tau < steps; ++tau) {
+                if ((tau & 31) == 0 && tau < R) {
+                    const int r = tau + t;
+                    if (r < R) {
+                        const int la = r < rows0 ? ck_code(__ldg(tA + r)) : 0;
+                        const int lb = r < rows1 ? ck_code(__ldg(tB + r)) : 0;
+                        rb_ch = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
+                    }
+                }
                 uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, LG);
                 uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, LG);
                 ch = __shfl_up_sync(FULL, ch, 1, LG);
+                const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
+                const int er = min(tau, CK_K - 1);
+                const uint32_t l_hg = eg[2 * er], l_e = eg[2 * er + 1];
                 const int i = tau - tl + 1;                                  // window row, 1-based
                 if (tl == 0) {
-                    ch = ch_next;
-                    if (i < R)
-                        ch_next = (uint32_t)(i < rows0 ? __ldg(tA + i) : 'A') | ((uint32_t)(i < rows1 ? __ldg(tB + i) : 'A') << 8);
-                    if (i <= R) { in_hg = eg[2 * (i - 1)]; in_e = eg[2 * (i - 1) + 1]; }
+                    ch = l_ch;
+                    in_hg = l_hg;
+                    in_e = l_e;
                 }
                 if (i < 1 || i > R) continue;
-                const uint32_t* pA = pA0 + ck_code(ch & 0xffu) * (CT / 2) * 32;
-                const uint32_t* pB = pB0 + ck_code(ch >> 8) * (CT / 2) * 32;
+                const uint32_t* pA = pA0 + (ch & 0xffffu);
+                const uint32_t* pB = pB0 + (ch >> 16);
                 uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
                 uint32_t hv[CT];
 #pragma unroll

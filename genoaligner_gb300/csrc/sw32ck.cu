@@ -84,36 +84,47 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
     for (int c = 0; c < CB; ++c) { hgu[c] = -go; fv[c] = 0; }
     int diag_in = -go, out_hg = -go, out_e = 0;
     const int32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / X.TW - 1) * m : nullptr;
-    int nxt_hg = -go, nxt_e = 0;
-    if (t == 0 && left) { nxt_hg = left[0]; nxt_e = left[1]; }
     const int kout = (j0 + CB) % X.TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / X.TW : 0;
     int32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * m : nullptr;
-    uint32_t ch = 0, ch_next = (t == 0) ? (uint32_t)__ldg(X.text) : 0u;
+    // each row's text byte (its profile offset with PROF) travels along the lanes
+    // with the boundary values; lane 0's inputs of 32 rows at a time -- that and
+    // the left edge -- are read by all lanes (lane u: row 32k + u) and shuffled
+    // to lane 0 each step, so no step runs a lane-0-only branch
+    uint32_t ch = 0, rb_ch = 0;
+    int rb_hg = -go, rb_e = 0;
     int bv = 0, br = 0;                               // this band's best and the first row holding it
     const int steps = m + 31;
     for (int tau = 0; tau < steps; ++tau) {
+        if ((tau & 31) == 0 && tau < m) {
+            const int r = tau + t;
+            if (r < m) {
+                const uint32_t c = __ldg(X.text + r);
+                rb_ch = PROF ? (uint32_t)(c32_code(c) * NQ * 32) : c;
+                if (left) {
+                    const int2 lv = *reinterpret_cast<const int2*>(left + 2 * r);
+                    rb_hg = lv.x;
+                    rb_e = lv.y;
+                }
+            }
+        }
         int in_hg = __shfl_up_sync(FULL, out_hg, 1);
         int in_e = __shfl_up_sync(FULL, out_e, 1);
         ch = __shfl_up_sync(FULL, ch, 1);
+        const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
+        const int l_hg = __shfl_sync(FULL, rb_hg, tau & 31);
+        const int l_e = __shfl_sync(FULL, rb_e, tau & 31);
         const int i = tau - t + 1;
         if (t == 0) {
-            ch = ch_next;
-            if (i < m) ch_next = __ldg(X.text + i);
-            in_hg = nxt_hg;
-            in_e = nxt_e;
-            if (left && i < m) {
-                const int2 lv = *reinterpret_cast<const int2*>(left + 2 * i);
-                nxt_hg = lv.x;
-                nxt_e = lv.y;
-            }
+            ch = l_ch;
+            in_hg = l_hg;
+            in_e = l_e;
         }
         if (i < 1 || i > m) continue;
         int s[CB];
         if constexpr (PROF) {
-            const int L = c32_code(ch);
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
-                const int4 v = X.prof[(L * NQ + q) * 32 + t];
+                const int4 v = X.prof[ch + q * 32 + t];
                 s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
             }
         } else {
