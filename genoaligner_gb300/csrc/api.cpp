@@ -106,7 +106,8 @@ SWBatchResult align_sw_batch_ex(const std::vector<SWRequest>& reqs, const AlignO
         int res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             SWAlignResult& r = out.results[(size_t)i];
-            const int s = v.score[i];
+            const int64_t q = i - v.base;           // index in the range's outputs
+            const int s = v.score[q];
             if (s < 0) {
                 if (v.trace) r.too_large = true;
                 continue;
@@ -114,17 +115,17 @@ SWBatchResult align_sw_batch_ex(const std::vector<SWRequest>& reqs, const AlignO
             r.score = s;
             r.resolved = true;
             ++res;
-            r.end_i = v.pos[4 * i + 2];
-            r.end_j = v.pos[4 * i + 3];
+            r.end_i = v.pos[4 * q + 2];
+            r.end_j = v.pos[4 * q + 3];
             if (s == 0) { r.rescore_ok = r.wellformed_ok = true; continue; }
             if (!v.trace || !reqs[(size_t)i].with_cigar) continue;
-            r.start_i = v.pos[4 * i];
-            r.start_j = v.pos[4 * i + 1];
-            if (v.len[i] > 0) {
-                r.cigar.assign(v.cig + v.slot_end[i] - v.len[i], (size_t)v.len[i]);
+            r.start_i = v.pos[4 * q];
+            r.start_j = v.pos[4 * q + 1];
+            if (v.len[q] > 0) {
+                r.cigar.assign(v.cig + v.slot_end[q] - v.len[q], (size_t)v.len[q]);
                 if (v.vflags) {
-                    r.rescore_ok = v.vflags[i] & 1;
-                    r.wellformed_ok = (v.vflags[i] >> 1) & 1;
+                    r.rescore_ok = v.vflags[q] & 1;
+                    r.wellformed_ok = (v.vflags[q] >> 1) & 1;
                 } else {
                     ga::sw_validate(r.cigar.data(), (int)r.cigar.size(), reqs[(size_t)i].text,
                                     reqs[(size_t)i].text_len, r.start_i, r.end_i, reqs[(size_t)i].pattern,

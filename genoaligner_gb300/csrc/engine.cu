@@ -793,6 +793,7 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir32[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + 3 + k; A.err = err;
+            A.coop_cells = (k == 1 && T.sw_coop_log2 < 40) ? ((int64_t)1 << T.sw_coop_log2) : -1;
             const cudaError_t e = (trace && use_sw16ck() && k < 2) ? launch_sw32ck(A, k == 1, S.s32[k], st)
                                                                    : launch_sw(A, kWidths[k], trace, S.s32[k], st);
             if (e != cudaSuccess) return e;
@@ -809,28 +810,17 @@ static void flatten_plan(const SwPlan& P, int32_t* out)
     for (int k = 0; k < 3; ++k) for (int32_t x : P.w32[k]) out[q++] = x;
 }
 
-int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
-                 const char** err)
+// One contiguous range of a checked SW batch: requests [base, base + n) of
+// the caller's batch, whose CIGAR slots start at byte cig_base of the caller's
+// buffer; `trace` is the whole batch's.  The finish callback gets the batch's
+// own indices.  Transfer byte counts go to *h2d / *d2h.
+static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base, int64_t cig_base, bool trace,
+                              const ga_tune& T, int64_t cell_limit, const SwFinish& fin, const char** err,
+                              int64_t* h2d, int64_t* d2h)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
     const ga_sw_scoring s0 = reqs[0].scoring;
-    if (int32_t st = sw_check(reqs, n, err)) return st;
-    const ga_tune T = tune_current();
-    bool trace = false;
-    int max_n = 0;
-    for (int32_t i = 0; i < n; ++i) {
-        trace |= reqs[i].with_cigar != 0;
-        max_n = std::max(max_n, (int)reqs[i].pattern_len);
-    }
-    // The reference's score-only kernel holds 4 warps x 2*(n+1) ints of shared
-    // memory per block and refuses the batch above the per-block limit the
-    // runtime reports, 48 KiB on CUDA devices (src/api/api.cpp:789-797).  The
-    // drop-in entry keeps that limit; the extension entry passes cell_limit < 0.
-    if (!trace && cell_limit >= 0 && (int64_t)4 * 2 * (max_n + 1) * 4 > 48 * 1024) {
-        *err = E_SW_SMEM;
-        return GA_INVALID_ARGUMENT;
-    }
 
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
     std::vector<int32_t> tl(n), pl(n);
@@ -922,7 +912,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     if (fail_here(1) || !ensure_dev(c, plan_end + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
     long long* hres = dplan ? reinterpret_cast<long long*>(c->host + hres_off) : nullptr;
     const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
-    t_h2d = (int64_t)in_bytes;
+    *h2d = (int64_t)in_bytes;
     PairDesc D;
     D.packed = nullptr;
     D.n = n;
@@ -1011,7 +1001,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         return GA_DEVICE_ERROR;
     }
     const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
-    t_d2h = (int64_t)out_bytes;
+    *d2h = (int64_t)out_bytes;
     if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
         cudaGetLastError();
         *err = E_D2H;
@@ -1023,8 +1013,86 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr};
-    parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
+    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr, base, cig_base};
+    parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(base + lo, base + hi, v); });
+    return GA_OK;
+}
+
+int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
+                 const char** err)
+{
+    *err = nullptr;
+    if (n <= 0) return GA_OK;
+    if (int32_t st = sw_check(reqs, n, err)) return st;
+    const ga_tune T = tune_current();
+    bool trace = false;
+    int max_n = 0;
+    double cells = 0.0;
+    for (int32_t i = 0; i < n; ++i) {
+        trace |= reqs[i].with_cigar != 0;
+        max_n = std::max(max_n, (int)reqs[i].pattern_len);
+        cells += (double)reqs[i].text_len * (double)reqs[i].pattern_len;
+    }
+    // The reference's score-only kernel holds 4 warps x 2*(n+1) ints of shared
+    // memory per block and refuses the batch above the per-block limit the
+    // runtime reports, 48 KiB on CUDA devices (src/api/api.cpp:789-797).  The
+    // drop-in entry keeps that limit; the extension entry passes cell_limit < 0.
+    if (!trace && cell_limit >= 0 && (int64_t)4 * 2 * (max_n + 1) * 4 > 48 * 1024) {
+        *err = E_SW_SMEM;
+        return GA_INVALID_ARGUMENT;
+    }
+    // Large traceback batches run as up to SW_CHUNKS contiguous ranges of about
+    // equal cells (one per 2 Gcells), each on its own thread, context and
+    // stream: one range's staging and copies, and its results' finish on the
+    // host, overlap the others' kernels, whose blocks also fill the SMs a
+    // range's tail leaves idle.
+    constexpr int SW_CHUNKS = 8;
+    const int K = (trace && n >= 8 * 1024) ? (int)std::max(1.0, std::min((double)SW_CHUNKS, cells / 2e9)) : 1;
+    if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h);
+    int32_t cut[SW_CHUNKS + 1];
+    int64_t cig_at[SW_CHUNKS + 1];
+    cut[0] = 0;
+    cig_at[0] = 0;
+    {
+        double acc = 0.0;
+        int k = 1;
+        int64_t cg = 0;
+        for (int32_t i = 0; i < n && k < K; ++i) {
+            acc += (double)reqs[i].text_len * (double)reqs[i].pattern_len;
+            cg += (int64_t)reqs[i].text_len + reqs[i].pattern_len;
+            if (acc >= cells * k / K) {
+                cut[k] = i + 1;
+                cig_at[k] = cg;
+                ++k;
+            }
+        }
+        for (; k < K; ++k) { cut[k] = n; cig_at[k] = cg; }
+        cut[K] = n;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int32_t st[SW_CHUNKS];
+    const char* errs[SW_CHUNKS];
+    int64_t h2d[SW_CHUNKS], d2h[SW_CHUNKS];
+    auto run = [&](int k) {
+        cudaSetDevice(dev);
+        st[k] = sw_batch_range(reqs + cut[k], cut[k + 1] - cut[k], cut[k], cig_at[k], trace, T, cell_limit, fin,
+                               &errs[k], &h2d[k], &d2h[k]);
+    };
+    std::vector<std::thread> th;
+    for (int k = 0; k + 1 < K; ++k) th.emplace_back(run, k);
+    run(K - 1);
+    for (std::thread& x : th) x.join();
+    t_h2d = t_d2h = 0;
+    for (int k = 0; k < K; ++k) {
+        t_h2d += h2d[k];
+        t_d2h += d2h[k];
+    }
+    for (int k = 0; k < K; ++k)
+        if (st[k] != GA_OK) {
+            *err = errs[k];
+            return st[k];
+        }
     return GA_OK;
 }
 
@@ -1204,7 +1272,8 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
         int32_t res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             ga_sw_result& r = results[i];
-            const int s = v.score[i];
+            const int64_t q = i - v.base;           // index in the range's outputs
+            const int s = v.score[q];
             if (s < 0) {                            // declared size limit
                 if (v.trace) r.too_large = 1;
                 continue;
@@ -1212,22 +1281,22 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
             r.score = s;
             r.resolved = 1;
             ++res;
-            r.end_i = v.pos[4 * i + 2];
-            r.end_j = v.pos[4 * i + 3];
+            r.end_i = v.pos[4 * q + 2];
+            r.end_j = v.pos[4 * q + 3];
             if (s == 0) { r.rescore_ok = r.wellformed_ok = 1; continue; }
             if (!v.trace || !reqs[i].with_cigar) continue;
-            r.start_i = v.pos[4 * i];
-            r.start_j = v.pos[4 * i + 1];
-            const int len = v.len[i];
+            r.start_i = v.pos[4 * q];
+            r.start_j = v.pos[4 * q + 1];
+            const int len = v.len[q];
             if (len > 0) {
-                const int64_t at = v.slot_end[i] - len;
-                std::memcpy(cigar_buf + at, v.cig + at, (size_t)len);
-                r.cigar_offset = at;
+                const int64_t at = v.slot_end[q] - len;
+                std::memcpy(cigar_buf + v.cig_base + at, v.cig + at, (size_t)len);
+                r.cigar_offset = v.cig_base + at;
                 r.cigar_len = len;
                 bool rs = false, wf = false;
                 if (v.vflags) {
-                    rs = v.vflags[i] & 1;
-                    wf = (v.vflags[i] >> 1) & 1;
+                    rs = v.vflags[q] & 1;
+                    wf = (v.vflags[q] >> 1) & 1;
                 } else {
                     sw_validate(cigar_buf + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
                                 reqs[i].pattern, reqs[i].pattern_len, r.start_j, r.end_j, reqs[i].scoring, s,

@@ -36,6 +36,11 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err);
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
                   const WfaFinish& fin, const char** err);
 
+// Per-pair outputs of one range of an SW batch (requests [base, base + n)),
+// valid during the finish callback, which gets the batch's own indices: pair i
+// reads score[i - base] and so on; its CIGAR is cig[e - len .. e) with
+// e = slot_end[i - base], and goes to byte cig_base + e - len of the caller's
+// CIGAR buffer.
 struct SwView {
     const int32_t* score;     // -1 = too large
     const int32_t* pos;       // start_i, start_j, end_i, end_j per pair
@@ -44,6 +49,8 @@ struct SwView {
     const int64_t* slot_end;
     bool trace;
     const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
+    int64_t base;
+    int64_t cig_base;
 };
 using SwFinish = std::function<void(int64_t lo, int64_t hi, const SwView& v)>;
 

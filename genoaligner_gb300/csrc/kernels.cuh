@@ -35,6 +35,7 @@ struct SwArgs {
     int64_t edge_slot;
     int32_t* counter;
     int32_t* err;
+    int64_t coop_cells = -1; // sw32ck: items above this many cells run on a whole block (< 0: none)
 };
 
 // Two pairs per warp in 16-bit lanes (sw16.cu): work holds 2 pair indices per

@@ -51,7 +51,10 @@ struct Fwd32 {
     int sm, sx, go, ge;
 };
 
-template <int CB, bool PROF>
+// One band of the forward pass.  COOP: the band is one of a pair's bands run
+// by the warps of a block together (fwd32_coop); the warp then meets the
+// block's barrier after every 32 steps, ceil((m + 31) / 32) times per band.
+template <int CB, bool PROF, bool COOP>
 __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int& cb)
 {
     constexpr int NQ = CB / 4;
@@ -119,7 +122,7 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
             in_hg = l_hg;
             in_e = l_e;
         }
-        if (i < 1 || i > m) continue;
+        if (i >= 1 && i <= m) {
         int s[CB];
         if constexpr (PROF) {
 #pragma unroll
@@ -156,6 +159,8 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
             for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_int4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
         }
         if (rowmax > bv) { bv = rowmax; br = i; }          // first row holding this lane's best
+        }
+        if (COOP && ((tau & 31) == 31 || tau == steps - 1)) __syncthreads();
     }
     // the column kept is the first of the lane's span in this band (spans
     // order like their columns); the walk finds the cell's column in that row
@@ -169,11 +174,43 @@ __device__ void fwd32(const Fwd32& X, int t, int& vb, int& rb, int& cb)
     for (int b0 = 0; b0 < X.n;) {
         const int rest = X.n - b0;
         const int w = rest > C32_BW ? C32_C : c32_last_cb(rest);
-        if (w == 16) fwd32_band<16, PROF>(X, b0, t, vb, rb, cb);
-        else if (w == 8) fwd32_band<8, PROF>(X, b0, t, vb, rb, cb);
-        else fwd32_band<4, PROF>(X, b0, t, vb, rb, cb);
+        if (w == 16) fwd32_band<16, PROF, false>(X, b0, t, vb, rb, cb);
+        else if (w == 8) fwd32_band<8, PROF, false>(X, b0, t, vb, rb, cb);
+        else fwd32_band<4, PROF, false>(X, b0, t, vb, rb, cb);
         b0 += 32 * w;
     }
+}
+
+// The forward pass of one pair by the 4 warps of a block: band b runs on warp
+// b % 4, starting at 32-step chunk start(b) = max(start(b-1) + 2, start(b-4) +
+// chunks per band), so each band's first lane reads the left edge of rows
+// 32c+1 .. 32c+32 (written by the band before it up to its step 32c + 62)
+// after the barrier that closed that band's chunk c + 1, and each warp runs
+// its bands one after the other.  Every warp meets the block barrier once per
+// chunk, idle or not: start(last band) + chunks per band times in all.
+template <bool PROF>
+__device__ void fwd32_coop(const Fwd32& X, int t, int wib, int& vb, int& rb, int& cb)
+{
+    const int nck = (X.m + 62) / 32;                  // ceil((m + 31) / 32)
+    int g = 0, prev = -2, b = 0;
+    int st4[4] = {0, 0, 0, 0};
+    for (int b0 = 0; b0 < X.n; ++b) {
+        const int rest = X.n - b0;
+        const int w = rest > C32_BW ? C32_C : c32_last_cb(rest);
+        const int s = max(prev + 2, b >= 4 ? st4[b & 3] + nck : 0);
+        prev = s;
+        st4[b & 3] = s;
+        if ((b & 3) == wib) {
+            for (; g < s; ++g) __syncthreads();
+            if (w == 16) fwd32_band<16, PROF, true>(X, b0, t, vb, rb, cb);
+            else if (w == 8) fwd32_band<8, PROF, true>(X, b0, t, vb, rb, cb);
+            else fwd32_band<4, PROF, true>(X, b0, t, vb, rb, cb);
+            g += nck;
+        }
+        b0 += 32 * w;
+    }
+    const int G = prev + nck;
+    for (; g < G; ++g) __syncthreads();
 }
 
 // Shared memory per warp: the forward profile (4 letters x 4 quads x 32
@@ -185,295 +222,346 @@ __host__ __device__ constexpr int c32_warp_smem_bytes(int K, int CT)
                                                                       : (4 * CT * 32 * 4 + K * 8);
 }
 
+// One pair: the forward pass (by this warp, or by the block's 4 warps when
+// coop), the best cell, the walk (this warp, or warp 0 of the block) and the
+// outputs.  wslot: the pair's checkpoint/tile memory (warp 0's slot when
+// coop); wsm: this warp's shared memory.  In coop every warp returns after
+// the same barriers; the caller closes the pair with one more barrier.
 template <int K, int CT>
-__global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
+__device__ void c32_pair(const SwArgs& A, int p, bool coop, int wib, int t, uint32_t* wslot, unsigned char* wsm,
+                         int (*s_best)[3])
 {
     constexpr int TW = 32 * CT;
     constexpr int NWT = CT >= 8 ? CT / 8 : 1;            // nibble words per lane and step
-    constexpr int WSB = c32_warp_smem_bytes(K, CT);
-    extern __shared__ int4 c32_smem[];
-    const int t = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    uint32_t* wslot = A.dirs + slot * A.dir_slot;
-    unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
     int4* prof = reinterpret_cast<int4*>(wsm);
     const int go = A.gap_open, ge = A.gap_extend;
     const int sm = A.match + go, sx = A.mismatch + go;
-
-    for (;;) {
-        int w = 0;
-        if (t == 0) w = atomicAdd(A.counter, 1);
-        w = __shfl_sync(FULL, w, 0);
-        if (w >= A.nwork) break;
-        __syncwarp();
-        const int p = A.work[w];
-        const int m = A.D.a_len[p], n = A.D.b_len[p];
-        const uint8_t* text = A.D.seq + A.D.a_off[p];
-        const uint8_t* pat = A.D.seq + A.D.b_off[p];
-        if (m <= 0 || n <= 0) {
-            if (t == 0) {
-                A.out_score[p] = 0;
-                A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
-                A.out_len[p] = 0;
-            }
-            continue;
+    const int m = A.D.a_len[p], n = A.D.b_len[p];
+    const uint8_t* text = A.D.seq + A.D.a_off[p];
+    const uint8_t* pat = A.D.seq + A.D.b_off[p];
+    if (m <= 0 || n <= 0) {
+        if (t == 0 && (!coop || wib == 0)) {
+            A.out_score[p] = 0;
+            A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+            A.out_len[p] = 0;
         }
-        const bool pure = A.D.pure && A.D.pure[p] && A.D.pure[A.D.n + p];
-        // tiles reach up to a multiple of TW: checkpoint rows are that wide (the
-        // columns past the forward bands are padding, never read into a real cell)
-        const int ncol = c32_ncol(n);
-        const int stride = (ncol + TW - 1) / TW * TW;
-        const int nq = c32_rows(m, K);
-        int32_t* ck = reinterpret_cast<int32_t*>(wslot);
-        int32_t* ce = ck + 2 * (int64_t)nq * stride;
-        uint32_t* tile = reinterpret_cast<uint32_t*>(ce + 2 * (int64_t)(stride / TW) * m);
+        return;
+    }
+    const bool pure = A.D.pure && A.D.pure[p] && A.D.pure[A.D.n + p];
+    // tiles reach up to a multiple of TW: checkpoint rows are that wide (the
+    // columns past the forward bands are padding, never read into a real cell)
+    const int ncol = c32_ncol(n);
+    const int stride = (ncol + TW - 1) / TW * TW;
+    const int nq = c32_rows(m, K);
+    int32_t* ck = reinterpret_cast<int32_t*>(wslot);
+    int32_t* ce = ck + 2 * (int64_t)nq * stride;
+    uint32_t* tile = reinterpret_cast<uint32_t*>(ce + 2 * (int64_t)(stride / TW) * m);
 
-        // ------------------------------------------------ forward pass --
-        int vb = 0, rb = 0, cb = 0;
-        {
-            Fwd32 X{text, pat, m, n, ncol, stride, K, TW, ck, ce, prof, sm, sx, go, ge};
+    // ------------------------------------------------ forward pass --
+    int vb = 0, rb = 0, cb = 0;
+    {
+        Fwd32 X{text, pat, m, n, ncol, stride, K, TW, ck, ce, prof, sm, sx, go, ge};
+        if (coop) {
+            if (pure) fwd32_coop<true>(X, t, wib, vb, rb, cb);
+            else fwd32_coop<false>(X, t, wib, vb, rb, cb);
+        } else {
             if (pure) fwd32<true>(X, t, vb, rb, cb);
             else fwd32<false>(X, t, vb, rb, cb);
         }
+    }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const int ov = __shfl_xor_sync(FULL, vb, o), orr = __shfl_xor_sync(FULL, rb, o), oc = __shfl_xor_sync(FULL, cb, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        const int ov = __shfl_xor_sync(FULL, vb, o), orr = __shfl_xor_sync(FULL, rb, o), oc = __shfl_xor_sync(FULL, cb, o);
+        if (ov > 0 && c32_better(ov, orr, oc, vb, rb, cb)) { vb = ov; rb = orr; cb = oc; }
+    }
+    if (coop) {
+        // the block's best: every warp reduces the four warps' bests in the same order
+        if (t == 0) { s_best[wib][0] = vb; s_best[wib][1] = rb; s_best[wib][2] = cb; }
+        __syncthreads();
+        vb = s_best[0][0]; rb = s_best[0][1]; cb = s_best[0][2];
+        for (int q = 1; q < 4; ++q) {
+            const int ov = s_best[q][0], orr = s_best[q][1], oc = s_best[q][2];
             if (ov > 0 && c32_better(ov, orr, oc, vb, rb, cb)) { vb = ov; rb = orr; cb = oc; }
         }
-        if (vb <= 0) {
-            if (t == 0) {
-                A.out_score[p] = 0;
-                A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
-                A.out_len[p] = 0;
-            }
-            continue;
+        if (wib != 0) return;                     // the walk is warp 0's
+    }
+    if (vb <= 0) {
+        if (t == 0) {
+            A.out_score[p] = 0;
+            A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+            A.out_len[p] = 0;
         }
+        return;
+    }
 
-        // ----------------------------------------------------- the walk --
-        char* slotc = A.out_cigar + A.D.out_off[p];
-        int pos = m + n;
-        int i = rb, j = cb, state = 0, v = vb;
-        int ti0 = ((i - 1) / K) * K + 1, tb = (j - 1) / TW;
-        bool first = true;                                          // the best cell's column not yet found
-        int* edg = reinterpret_cast<int*>(wsm + 4 * CT * 32 * 4);     // [row][2], after the tile profile
-        bool fin = false;
-        while (!fin) {
-            const int rows = i - ti0 + 1;
-            const int steps = rows + 31;
-            const int col0 = TW * tb;
-            __syncwarp();
-            // tile profile (pure pairs) or bytes, top state, left edges
-            uint32_t pbt[CT];
-            {
-                const int cl = col0 + CT * t;
-                if (pure) {
-                    int code[CT];
+    // ----------------------------------------------------- the walk --
+    char* slotc = A.out_cigar + A.D.out_off[p];
+    int pos = m + n;
+    int i = rb, j = cb, state = 0, v = vb;
+    int ti0 = ((i - 1) / K) * K + 1, tb = (j - 1) / TW;
+    bool first = true;                                          // the best cell's column not yet found
+    int* edg = reinterpret_cast<int*>(wsm + 4 * CT * 32 * 4);     // [row][2], after the tile profile
+    bool fin = false;
+    while (!fin) {
+        const int rows = i - ti0 + 1;
+        const int steps = rows + 31;
+        const int col0 = TW * tb;
+        __syncwarp();
+        // tile profile (pure pairs) or bytes, top state, left edges
+        uint32_t pbt[CT];
+        {
+            const int cl = col0 + CT * t;
+            if (pure) {
+                int code[CT];
 #pragma unroll
-                    for (int c = 0; c < CT; ++c) code[c] = cl + c < n ? c32_code(__ldg(pat + cl + c)) : 4;
-                    if constexpr (CT == 2) {
-                        int2* tp = reinterpret_cast<int2*>(wsm);
+                for (int c = 0; c < CT; ++c) code[c] = cl + c < n ? c32_code(__ldg(pat + cl + c)) : 4;
+                if constexpr (CT == 2) {
+                    int2* tp = reinterpret_cast<int2*>(wsm);
 #pragma unroll
-                        for (int L = 0; L < 4; ++L) tp[L * 32 + t] = make_int2(code[0] == L ? sm : sx, code[1] == L ? sm : sx);
-                    } else {
-                        int4* tp = reinterpret_cast<int4*>(wsm);
+                    for (int L = 0; L < 4; ++L) tp[L * 32 + t] = make_int2(code[0] == L ? sm : sx, code[1] == L ? sm : sx);
+                } else {
+                    int4* tp = reinterpret_cast<int4*>(wsm);
 #pragma unroll
-                        for (int L = 0; L < 4; ++L)
+                    for (int L = 0; L < 4; ++L)
 #pragma unroll
-                            for (int q4 = 0; q4 < CT / 4; ++q4)
-                                tp[(L * (CT / 4) + q4) * 32 + t] =
-                                    make_int4(code[4 * q4] == L ? sm : sx, code[4 * q4 + 1] == L ? sm : sx,
-                                              code[4 * q4 + 2] == L ? sm : sx, code[4 * q4 + 3] == L ? sm : sx);
+                        for (int q4 = 0; q4 < CT / 4; ++q4)
+                            tp[(L * (CT / 4) + q4) * 32 + t] =
+                                make_int4(code[4 * q4] == L ? sm : sx, code[4 * q4 + 1] == L ? sm : sx,
+                                          code[4 * q4 + 2] == L ? sm : sx, code[4 * q4 + 3] == L ? sm : sx);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < CT; ++c) pbt[c] = (!pure && cl + c < n) ? __ldg(pat + cl + c) : 0x100u;
+        }
+        const int q = (ti0 - 1) / K - 1;
+        const int32_t* crow = ck + 2 * (int64_t)max(q, 0) * stride;
+        int hgu[CT], fv[CT];
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+            hgu[c] = q >= 0 ? crow[2 * (col0 + CT * t + c)] : -go;
+            fv[c] = q >= 0 ? crow[2 * (col0 + CT * t + c) + 1] : 0;
+        }
+        int diag_in = __shfl_up_sync(FULL, hgu[CT - 1], 1);
+        if (t == 0) diag_in = (q >= 0 && tb > 0) ? crow[2 * (col0 - 1)] : -go;
+        {
+            const int32_t* le = tb > 0 ? ce + 2 * ((int64_t)(tb - 1) * m + (ti0 - 1)) : nullptr;
+            for (int r = t; r < K; r += 32) {
+                edg[2 * r] = (le && r < rows) ? le[2 * r] : -go;
+                edg[2 * r + 1] = (le && r < rows) ? le[2 * r + 1] : 0;
+            }
+        }
+        __syncwarp();
+        int out_hg = -go, out_e = 0;
+        int jfound = INT32_MAX;
+        const uint8_t* tx = text + (ti0 - 1);
+        uint32_t ch = 0, ch_next = t == 0 ? (uint32_t)__ldg(tx) : 0u;
+        for (int tau = 0; tau < steps; ++tau) {
+            int in_hg = __shfl_up_sync(FULL, out_hg, 1);
+            int in_e = __shfl_up_sync(FULL, out_e, 1);
+            ch = __shfl_up_sync(FULL, ch, 1);
+            const int r = tau - t + 1;                                  // tile row, 1-based
+            if (t == 0) {
+                ch = ch_next;
+                if (r < rows) ch_next = __ldg(tx + r);
+                if (r <= rows) { in_hg = edg[2 * (r - 1)]; in_e = edg[2 * (r - 1) + 1]; }
+            }
+            if (r < 1 || r > rows) continue;
+            int s[CT];
+            if (pure) {
+                const int L = c32_code(ch);
+                if constexpr (CT == 2) {
+                    const int2 v2 = reinterpret_cast<const int2*>(wsm)[L * 32 + t];
+                    s[0] = v2.x;
+                    s[1] = v2.y;
+                } else {
+#pragma unroll
+                    for (int q4 = 0; q4 < CT / 4; ++q4) {
+                        const int4 v4 = reinterpret_cast<const int4*>(wsm)[(L * (CT / 4) + q4) * 32 + t];
+                        s[4 * q4] = v4.x; s[4 * q4 + 1] = v4.y; s[4 * q4 + 2] = v4.z; s[4 * q4 + 3] = v4.w;
                     }
                 }
+            } else {
 #pragma unroll
-                for (int c = 0; c < CT; ++c) pbt[c] = (!pure && cl + c < n) ? __ldg(pat + cl + c) : 0x100u;
+                for (int c = 0; c < CT; ++c) s[c] = ch == pbt[c] ? sm : sx;
             }
-            const int q = (ti0 - 1) / K - 1;
-            const int32_t* crow = ck + 2 * (int64_t)max(q, 0) * stride;
-            int hgu[CT], fv[CT];
+            int hgd = diag_in, hgl = in_hg, el = in_e;
+            uint32_t nib[NWT];
+#pragma unroll
+            for (int wq = 0; wq < NWT; ++wq) nib[wq] = 0;
 #pragma unroll
             for (int c = 0; c < CT; ++c) {
-                hgu[c] = q >= 0 ? crow[2 * (col0 + CT * t + c)] : -go;
-                fv[c] = q >= 0 ? crow[2 * (col0 + CT * t + c) + 1] : 0;
+                bool pe, pf, p1, p2;
+                const int h0 = hgd + s[c];
+                const int e = __vibmax_s32(hgl, el - ge, &pe);            // open wins ties
+                const int f = __vibmax_s32(hgu[c], fv[c] - ge, &pf);
+                const int h1 = __vibmax_s32(h0, e, &p1);                  // diagonal wins ties
+                const int h2 = __vibmax_s32(h1, f, &p2);
+                const int h = max(h2, 0);
+                nib[c >> 3] |= ((uint32_t)!p1 | ((uint32_t)!p2 << 1) | ((uint32_t)!pe << 2) | ((uint32_t)!pf << 3))
+                               << (4 * (c & 7));
+                const int hg = h - go;
+                hgd = hgu[c];
+                hgu[c] = hg;
+                fv[c] = f;
+                hgl = hg;
+                el = e;
             }
-            int diag_in = __shfl_up_sync(FULL, hgu[CT - 1], 1);
-            if (t == 0) diag_in = (q >= 0 && tb > 0) ? crow[2 * (col0 - 1)] : -go;
-            {
-                const int32_t* le = tb > 0 ? ce + 2 * ((int64_t)(tb - 1) * m + (ti0 - 1)) : nullptr;
-                for (int r = t; r < K; r += 32) {
-                    edg[2 * r] = (le && r < rows) ? le[2 * r] : -go;
-                    edg[2 * r + 1] = (le && r < rows) ? le[2 * r + 1] : 0;
+#pragma unroll
+            for (int wq = 0; wq < NWT; ++wq) tile[(tau * 32 + t) * NWT + wq] = nib[wq];
+            if (first && r == rows) {                           // the best cell's row
+#pragma unroll
+                for (int c = CT - 1; c >= 0; --c) {
+                    const int col = col0 + CT * t + c;
+                    if (col < n && hgu[c] + go == vb) jfound = col + 1;
                 }
             }
-            __syncwarp();
-            int out_hg = -go, out_e = 0;
-            int jfound = INT32_MAX;
-            const uint8_t* tx = text + (ti0 - 1);
-            uint32_t ch = 0, ch_next = t == 0 ? (uint32_t)__ldg(tx) : 0u;
-            for (int tau = 0; tau < steps; ++tau) {
-                int in_hg = __shfl_up_sync(FULL, out_hg, 1);
-                int in_e = __shfl_up_sync(FULL, out_e, 1);
-                ch = __shfl_up_sync(FULL, ch, 1);
-                const int r = tau - t + 1;                                  // tile row, 1-based
-                if (t == 0) {
-                    ch = ch_next;
-                    if (r < rows) ch_next = __ldg(tx + r);
-                    if (r <= rows) { in_hg = edg[2 * (r - 1)]; in_e = edg[2 * (r - 1) + 1]; }
-                }
-                if (r < 1 || r > rows) continue;
-                int s[CT];
-                if (pure) {
-                    const int L = c32_code(ch);
-                    if constexpr (CT == 2) {
-                        const int2 v2 = reinterpret_cast<const int2*>(wsm)[L * 32 + t];
-                        s[0] = v2.x;
-                        s[1] = v2.y;
-                    } else {
+            diag_in = in_hg;
+            out_hg = hgl;
+            out_e = el;
+        }
+        __syncwarp();
+        if (first) {
 #pragma unroll
-                        for (int q4 = 0; q4 < CT / 4; ++q4) {
-                            const int4 v4 = reinterpret_cast<const int4*>(wsm)[(L * (CT / 4) + q4) * 32 + t];
-                            s[4 * q4] = v4.x; s[4 * q4 + 1] = v4.y; s[4 * q4 + 2] = v4.z; s[4 * q4 + 3] = v4.w;
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < CT; ++c) s[c] = ch == pbt[c] ? sm : sx;
-                }
-                int hgd = diag_in, hgl = in_hg, el = in_e;
-                uint32_t nib[NWT];
-#pragma unroll
-                for (int wq = 0; wq < NWT; ++wq) nib[wq] = 0;
-#pragma unroll
-                for (int c = 0; c < CT; ++c) {
-                    bool pe, pf, p1, p2;
-                    const int h0 = hgd + s[c];
-                    const int e = __vibmax_s32(hgl, el - ge, &pe);            // open wins ties
-                    const int f = __vibmax_s32(hgu[c], fv[c] - ge, &pf);
-                    const int h1 = __vibmax_s32(h0, e, &p1);                  // diagonal wins ties
-                    const int h2 = __vibmax_s32(h1, f, &p2);
-                    const int h = max(h2, 0);
-                    nib[c >> 3] |= ((uint32_t)!p1 | ((uint32_t)!p2 << 1) | ((uint32_t)!pe << 2) | ((uint32_t)!pf << 3))
-                                   << (4 * (c & 7));
-                    const int hg = h - go;
-                    hgd = hgu[c];
-                    hgu[c] = hg;
-                    fv[c] = f;
-                    hgl = hg;
-                    el = e;
-                }
-#pragma unroll
-                for (int wq = 0; wq < NWT; ++wq) tile[(tau * 32 + t) * NWT + wq] = nib[wq];
-                if (first && r == rows) {                           // the best cell's row
-#pragma unroll
-                    for (int c = CT - 1; c >= 0; --c) {
-                        const int col = col0 + CT * t + c;
-                        if (col < n && hgu[c] + go == vb) jfound = col + 1;
-                    }
-                }
-                diag_in = in_hg;
-                out_hg = hgl;
-                out_e = el;
+            for (int o = 16; o > 0; o >>= 1) jfound = min(jfound, __shfl_xor_sync(FULL, jfound, o));
+            first = false;
+            if (jfound == INT32_MAX) {             // cannot happen: the forward pass saw the value here
+                if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
+                break;
             }
-            __syncwarp();
-            if (first) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) jfound = min(jfound, __shfl_xor_sync(FULL, jfound, o));
-                first = false;
-                if (jfound == INT32_MAX) {             // cannot happen: the forward pass saw the value here
-                    if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
-                    break;
+            j = jfound;
+            cb = jfound;
+        }
+        // walk inside the tile: state 0 on H, 1 in an E run ('D'), 2 in an F run ('I')
+        const int jlo = col0 + 1;
+        for (;;) {
+            if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
+            if (i < ti0 || j < jlo) break;
+            if (state == 0) {
+                // a run of diagonal steps resolved at once: lane u takes the step from
+                // cell (i - u, j - u); its value is v less the scores of steps 0 .. u-1
+                const int U = min(min(32, pos), min(i - max(ti0, 1), j - max(jlo, 1)) + 1);
+                bool diag = false, eq = false;
+                int s = 0;
+                if (t < U) {
+                    const int jq = j - t - jlo;
+                    const int tq = jq / CT, cq = jq - tq * CT;
+                    const uint32_t nq = tile[(((i - t - ti0) + tq) * 32 + tq) * NWT + (cq >> 3)] >> (4 * (cq & 7));
+                    diag = (nq & 3u) == 0u;
+                    eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
+                    s = eq ? A.match : A.mismatch;
                 }
-                j = jfound;
-                cb = jfound;
+                int incl = s;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL, incl, o);
+                    if (t >= o) incl += y;
+                }
+                const bool ok = t < U && diag && v - (incl - s) != 0;
+                const unsigned run = __ballot_sync(FULL, ok);
+                const int r = run == FULL ? 32 : __ffs(~run) - 1;
+                if (r > 0) {
+                    if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
+                    v -= __shfl_sync(FULL, incl, r - 1);
+                    i -= r;
+                    j -= r;
+                    pos -= r;
+                    continue;
+                }
             }
-            // walk inside the tile: state 0 on H, 1 in an E run ('D'), 2 in an F run ('I')
-            const int jlo = col0 + 1;
-            for (;;) {
-                if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
-                if (i < ti0 || j < jlo) break;
-                if (state == 0) {
-                    // a run of diagonal steps resolved at once: lane u takes the step from
-                    // cell (i - u, j - u); its value is v less the scores of steps 0 .. u-1
-                    const int U = min(min(32, pos), min(i - max(ti0, 1), j - max(jlo, 1)) + 1);
-                    bool diag = false, eq = false;
-                    int s = 0;
-                    if (t < U) {
-                        const int jq = j - t - jlo;
-                        const int tq = jq / CT, cq = jq - tq * CT;
-                        const uint32_t nq = tile[(((i - t - ti0) + tq) * 32 + tq) * NWT + (cq >> 3)] >> (4 * (cq & 7));
-                        diag = (nq & 3u) == 0u;
-                        eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
-                        s = eq ? A.match : A.mismatch;
-                    }
-                    int incl = s;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int y = __shfl_up_sync(FULL, incl, o);
-                        if (t >= o) incl += y;
-                    }
-                    const bool ok = t < U && diag && v - (incl - s) != 0;
-                    const unsigned run = __ballot_sync(FULL, ok);
-                    const int r = run == FULL ? 32 : __ffs(~run) - 1;
-                    if (r > 0) {
-                        if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
-                        v -= __shfl_sync(FULL, incl, r - 1);
-                        i -= r;
-                        j -= r;
-                        pos -= r;
-                        continue;
-                    }
-                }
-                const int jj = j - jlo;
-                const int tt = jj / CT, c = jj - tt * CT;
-                const uint32_t nb4 = (tile[(((i - ti0) + tt) * 32 + tt) * NWT + (c >> 3)] >> (4 * (c & 7))) & 15u;
-                char op;
-                if (state == 0) {
-                    if (nb4 & 2u) {
-                        op = 'I';
-                        if (nb4 & 8u) { state = 2; v += ge; } else { v += go; }
-                        --i;
-                    } else if (nb4 & 1u) {
-                        op = 'D';
-                        if (nb4 & 4u) { state = 1; v += ge; } else { v += go; }
-                        --j;
-                    } else {
-                        const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
-                        op = ta == pc ? 'M' : 'X';
-                        v -= ta == pc ? A.match : A.mismatch;
-                        --i;
-                        --j;
-                    }
-                } else if (state == 1) {
+            const int jj = j - jlo;
+            const int tt = jj / CT, c = jj - tt * CT;
+            const uint32_t nb4 = (tile[(((i - ti0) + tt) * 32 + tt) * NWT + (c >> 3)] >> (4 * (c & 7))) & 15u;
+            char op;
+            if (state == 0) {
+                if (nb4 & 2u) {
+                    op = 'I';
+                    if (nb4 & 8u) { state = 2; v += ge; } else { v += go; }
+                    --i;
+                } else if (nb4 & 1u) {
                     op = 'D';
-                    if (nb4 & 4u) { v += ge; } else { v += go; state = 0; }
+                    if (nb4 & 4u) { state = 1; v += ge; } else { v += go; }
                     --j;
                 } else {
-                    op = 'I';
-                    if (nb4 & 8u) { v += ge; } else { v += go; state = 0; }
+                    const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
+                    op = ta == pc ? 'M' : 'X';
+                    v -= ta == pc ? A.match : A.mismatch;
                     --i;
+                    --j;
                 }
-                if (pos <= 0) {
-                    if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
-                    fin = true;
-                    break;
-                }
-                --pos;
-                if (t == 0) slotc[pos] = op;
+            } else if (state == 1) {
+                op = 'D';
+                if (nb4 & 4u) { v += ge; } else { v += go; state = 0; }
+                --j;
+            } else {
+                op = 'I';
+                if (nb4 & 8u) { v += ge; } else { v += go; state = 0; }
+                --i;
             }
-            if (!fin) {
-                if (i < ti0) ti0 = ((i - 1) / K) * K + 1;
-                tb = (j - 1) / TW;
+            if (pos <= 0) {
+                if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
+                fin = true;
+                break;
             }
+            --pos;
+            if (t == 0) slotc[pos] = op;
         }
-        if (t == 0) {
-            A.out_score[p] = vb;
-            A.out_pos[4 * p] = i;
-            A.out_pos[4 * p + 1] = j;
-            A.out_pos[4 * p + 2] = rb - 1;
-            A.out_pos[4 * p + 3] = cb - 1;
-            A.out_len[p] = m + n - pos;
+        if (!fin) {
+            if (i < ti0) ti0 = ((i - 1) / K) * K + 1;
+            tb = (j - 1) / TW;
         }
+    }
+    if (t == 0) {
+        A.out_score[p] = vb;
+        A.out_pos[4 * p] = i;
+        A.out_pos[4 * p + 1] = j;
+        A.out_pos[4 * p + 2] = rb - 1;
+        A.out_pos[4 * p + 3] = cb - 1;
+        A.out_len[p] = m + n - pos;
+    }
+}
+
+// Work items come largest first.  Items above A.coop_cells cells are taken by
+// a whole block (its 4 warps share the forward pass); from the first smaller
+// item on, each warp takes items of its own.
+template <int K, int CT>
+__global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
+{
+    constexpr int WSB = c32_warp_smem_bytes(K, CT);
+    extern __shared__ int4 c32_smem[];
+    __shared__ int s_item;
+    __shared__ int s_best[4][3];
+    const int t = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
+    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
+    unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
+
+    int first = -1;                                   // warp 0: the item that ended the block phase
+    bool more = true;
+    while (A.coop_cells >= 0) {
+        if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int w = s_item;
+        __syncthreads();
+        if (w >= A.nwork) { more = false; break; }
+        const int p = A.work[w];
+        if ((int64_t)A.D.a_len[p] * A.D.b_len[p] <= A.coop_cells) {
+            if (wib == 0) first = w;
+            break;
+        }
+        c32_pair<K, CT>(A, p, true, wib, t, bslot, wsm, s_best);
+        __syncthreads();
+    }
+    while (more) {
+        int w = first;
+        first = -1;
+        if (w < 0) {
+            if (t == 0) w = atomicAdd(A.counter, 1);
+            w = __shfl_sync(FULL, w, 0);
+        }
+        if (w >= A.nwork) break;
+        __syncwarp();
+        c32_pair<K, CT>(A, A.work[w], false, wib, t, wslot, wsm, s_best);
     }
 }
 

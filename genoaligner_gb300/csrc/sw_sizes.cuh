@@ -60,6 +60,7 @@ __host__ __device__ inline int64_t sw16ck_dir_words(int M, int N, int window)
 constexpr int C32_C = 16;                // forward columns per lane, full bands
 constexpr int C32_BW = 32 * C32_C;
 constexpr int C32_LONG_LOG2 = 24;       // default: the long-pair shape above 2^24 cells
+constexpr int C32_COOP_LOG2 = 27;       // default: long-shape pairs above 2^27 cells run on a whole block
 
 __host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
 __host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }

@@ -40,19 +40,21 @@ static ga_tune builtin()
     t.sw_window = CK_TG;
     t.sw_long_log2 = C32_LONG_LOG2;
     t.wfa_lane_smax = LANE_SMAX;
+    t.sw_coop_log2 = C32_COOP_LOG2;
     return t;
 }
 
 static bool valid(const ga_tune& t)
 {
     return (t.sw_pack16 == 0 || t.sw_pack16 == 1) && (t.sw_window == 2 || t.sw_window == 4) &&
-           t.sw_long_log2 >= 16 && t.sw_long_log2 <= 30 && t.wfa_lane_smax >= 0 && t.wfa_lane_smax <= LANE_SMAX;
+           t.sw_long_log2 >= 16 && t.sw_long_log2 <= 30 && t.wfa_lane_smax >= 0 && t.wfa_lane_smax <= LANE_SMAX &&
+           t.sw_coop_log2 >= 16 && t.sw_coop_log2 <= 40;
 }
 
 static bool same(const ga_tune& a, const ga_tune& b)
 {
     return a.sw_pack16 == b.sw_pack16 && a.sw_window == b.sw_window && a.sw_long_log2 == b.sw_long_log2 &&
-           a.wfa_lane_smax == b.wfa_lane_smax;
+           a.wfa_lane_smax == b.wfa_lane_smax && a.sw_coop_log2 == b.sw_coop_log2;
 }
 
 static int current_device()
@@ -212,6 +214,13 @@ int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int6
         vals.push_back(30);                                   // no pair in the long shape
         rc = sweep(S, &ga_tune::sw_long_log2, vals, reps, run, err);
     }
+    if (rc == GA_OK && max_cells > ((int64_t)1 << 24)) {
+        std::vector<int> vals;
+        for (int v = 24; v <= 30; v += 3)
+            if (max_cells > ((int64_t)1 << v)) vals.push_back(v);
+        vals.push_back(40);                                   // every pair on one warp
+        rc = sweep(S, &ga_tune::sw_coop_log2, vals, reps, run, err);
+    }
     if (rc != GA_OK) return rc;
     store(dev, S.best);
     report(S, chosen, trials, max_trials, n_trials);
@@ -265,15 +274,16 @@ int32_t ga_tune_save(const char* path)
     }
     FILE* f = std::fopen(path, "w");
     if (!f) return GA_INVALID_ARGUMENT;
-    std::fprintf(f, "# genoaligner_gb300 tune v1: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax\n");
+    std::fprintf(f, "# genoaligner_gb300 tune v2: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax "
+                    "sw_coop_log2\n");
     for (const auto& r : rows) {
         cudaDeviceProp p;
         if (cudaGetDeviceProperties(&p, r.first) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
-        std::fprintf(f, "%s\t%d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window, r.second.sw_long_log2,
-                     r.second.wfa_lane_smax);
+        std::fprintf(f, "%s\t%d %d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window, r.second.sw_long_log2,
+                     r.second.wfa_lane_smax, r.second.sw_coop_log2);
     }
     return std::fclose(f) == 0 ? GA_OK : GA_INVALID_ARGUMENT;
 }
@@ -290,8 +300,8 @@ int32_t ga_tune_load(const char* path)
         if (line[0] == '#' || line[0] == '\n') continue;
         char* tab = std::strchr(line, '\t');
         ga_tune t = builtin();
-        if (!tab || std::sscanf(tab + 1, "%d %d %d %d", &t.sw_pack16, &t.sw_window, &t.sw_long_log2,
-                                &t.wfa_lane_smax) != 4 || !valid(t)) {
+        if (!tab || std::sscanf(tab + 1, "%d %d %d %d %d", &t.sw_pack16, &t.sw_window, &t.sw_long_log2,
+                                &t.wfa_lane_smax, &t.sw_coop_log2) != 5 || !valid(t)) {
             ok = false;
             break;
         }

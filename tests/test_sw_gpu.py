@@ -135,3 +135,41 @@ def test_sw_fault_injection_reports_device_error():
         assert got.res["score"][0] == -1 and not got.res["resolved"][0]
     got = sw_gpu([b"ACGTACGT"], [b"ACGT"])
     assert got.status == api.Status.ok and got.res["score"][0] == 8
+
+
+def test_sw_large_host_batch_runs_in_ranges_with_same_results():
+    """A traceback batch of several Gcells runs as ranges (one per 2 Gcells)
+    on their own contexts; results (scores, spans, CIGARs at the right
+    offsets, checks) equal the device entry's single run and, on a sample, the
+    oracle's."""
+    torch = pytest.importorskip("torch")
+    ps = workloads.sw_uneven_200k(n=16000, seed=23)
+    assert int((ps.a_len.astype(np.int64) * ps.b_len).sum()) >= 4e9
+    got = api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len,
+                                    scoring=(2, -3, 3, 1), with_cigar=True)
+    assert got.status == api.Status.ok
+    b = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
+    sc = torch.empty(b.n, dtype=torch.int32, device="cuda")
+    pos = torch.empty(4 * b.n, dtype=torch.int32, device="cuda")
+    ln = torch.empty(b.n, dtype=torch.int32, device="cuda")
+    cg = torch.empty(b.out_bytes, dtype=torch.uint8, device="cuda")
+    api.sw_device(b, (2, -3, 3, 1), True, sc, pos, ln, cg, trace_cell_limit=1 << 26)
+    torch.cuda.synchronize()
+    s, p4, L = sc.cpu().numpy(), pos.cpu().numpy().reshape(-1, 4), ln.cpu().numpy()
+    oo, C = b.out_off.cpu().numpy(), cg.cpu().numpy()
+    res = got.res
+    assert np.array_equal(res["score"], s)
+    for f, k in (("start_i", 0), ("start_j", 1), ("end_i", 2), ("end_j", 3)):
+        sel = s > 0
+        assert np.array_equal(res[f][sel], p4[sel, k]), f
+    assert res["rescore_ok"][s > 0].all() and res["wellformed_ok"][s > 0].all()
+    cap = ps.a_len.astype(np.int64) + ps.b_len
+    for i in range(0, b.n, 7):
+        if s[i] > 0:
+            assert got.cigar(i) == C[oo[i] + cap[i] - L[i]: oo[i] + cap[i]].tobytes()
+    idx = np.random.default_rng(3).choice(b.n, 200, replace=False)
+    sub = ps.subset(idx)
+    ts, pp = sub.lists()
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=True)
+    assert np.array_equal(res["score"][idx], want.score)
+    assert all(got.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))

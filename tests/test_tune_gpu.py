@@ -69,19 +69,20 @@ def test_every_sw_setting_gives_the_same_results(restore_tune):
     want = oracle.sw_batch(ts, pp, scoring=scheme, with_cigar=True, trace_cell_limit=-1)
     b = _device(ts, pp)
     first = None
-    for pack16 in (1, 0):
-        for window in (2, 4):
-            for long_log2 in (16, 20, 24, 30):
-                api.tune_set(sw_pack16=pack16, sw_window=window, sw_long_log2=long_log2)
-                outs = _sw_outputs(torch, b)
-                api.sw_device(b, scheme, True, *outs)
-                res = _host(torch, outs)
-                if first is None:
-                    first = res
-                    _check_sw(res, want, b, ts, pp)
-                else:
-                    for x, y in zip(first, res):
-                        assert np.array_equal(x, y), (pack16, window, long_log2)
+    combos = [(p, w, lg, 40) for p in (1, 0) for w in (2, 4) for lg in (16, 20, 24, 30)]
+    # whole-block pairs: every long-shape pair (above 2^16 / 2^20 cells) on a block's 4 warps
+    combos += [(1, 2, 16, 16), (0, 2, 16, 16), (0, 2, 20, 18), (0, 4, 16, 20)]
+    for pack16, window, long_log2, coop in combos:
+        api.tune_set(sw_pack16=pack16, sw_window=window, sw_long_log2=long_log2, sw_coop_log2=coop)
+        outs = _sw_outputs(torch, b)
+        api.sw_device(b, scheme, True, *outs)
+        res = _host(torch, outs)
+        if first is None:
+            first = res
+            _check_sw(res, want, b, ts, pp)
+        else:
+            for x, y in zip(first, res):
+                assert np.array_equal(x, y), (pack16, window, long_log2, coop)
 
 
 def test_autotune_sw_keeps_its_fastest_candidate(restore_tune):
@@ -135,10 +136,11 @@ def test_every_wfa_lane_setting_gives_the_same_results(restore_tune):
 
 
 def test_saved_setting_loads_back(tmp_path, restore_tune):
-    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8)
+    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8, sw_coop_log2=25)
     p = tmp_path / "tune.txt"
     api.tune_save(str(p))
     api.tune_set(**api.tune_default())
     api.tune_load(str(p))
-    assert api.tune_get() == {"sw_pack16": 0, "sw_window": 4, "sw_long_log2": 20, "wfa_lane_smax": 8}
+    assert api.tune_get() == {"sw_pack16": 0, "sw_window": 4, "sw_long_log2": 20, "wfa_lane_smax": 8,
+                              "sw_coop_log2": 25}
     assert api.device_name() in p.read_text()
