@@ -730,6 +730,20 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, in
     return cudaSuccess;
 }
 
+// Device memory the checkpoint / direction tables of one call may take:
+// 60 % of what is free now plus the call's own arena (which it may replace),
+// between 4 GB and 200 GB, shared by `parts` concurrent calls.  Long pairs
+// need tens of MB per resident warp, so this bounds how many run at once.
+static int64_t sw_dir_budget(const Ctx* c, int parts)
+{
+    size_t fr = 0, tot = 0;
+    int64_t avail = (int64_t)96 << 30;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) avail = ((int64_t)fr + (int64_t)c->dev_cap) * 6 / 10;
+    else cudaGetLastError();
+    avail /= std::max(1, parts);
+    return std::max<int64_t>((int64_t)4 << 30, std::min<int64_t>(avail, (int64_t)200 << 30));
+}
+
 // Slots (resident warps) per launch and the direction-table words the launches
 // need (they run one after another on one stream and share the table).
 struct SwSlots {
@@ -737,10 +751,9 @@ struct SwSlots {
     int64_t dir_words = 0, max_slots = 4;
 };
 
-static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_count)
+static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_count, int64_t budget)
 {
     SwSlots S;
-    const int64_t budget = (int64_t)96 << 30;          // direction-table / checkpoint cap, bytes
     for (int k = 0; k < 3; ++k) {
         if (P.n32[k] > 0) {
             int s = (trace && use_sw16ck() && k < 2) ? sw32ck_max_slots(k == 1, sm_count)
@@ -813,10 +826,11 @@ static void flatten_plan(const SwPlan& P, int32_t* out)
 // One contiguous range of a checked SW batch: requests [base, base + n) of
 // the caller's batch, whose CIGAR slots start at byte cig_base of the caller's
 // buffer; `trace` is the whole batch's.  The finish callback gets the batch's
-// own indices.  Transfer byte counts go to *h2d / *d2h.
+// own indices.  Transfer byte counts go to *h2d / *d2h.  `parts` ranges run
+// at once and share the device-memory budget.
 static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base, int64_t cig_base, bool trace,
                               const ga_tune& T, int64_t cell_limit, const SwFinish& fin, const char** err,
-                              int64_t* h2d, int64_t* d2h)
+                              int64_t* h2d, int64_t* d2h, int parts)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
@@ -975,7 +989,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         return GA_OK;
     };
     if (int32_t rs = stage(true)) return rs;
-    const SwSlots S = size_sw(P, trace, T, c->sm_count);
+    const SwSlots S = size_sw(P, trace, T, c->sm_count, sw_dir_budget(c, parts));
     const uint64_t gen_before = c->dev_gen;
     auto extra_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
         Carve k(base);
@@ -1048,7 +1062,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     // range's tail leaves idle.
     constexpr int SW_CHUNKS = 8;
     const int K = (trace && n >= 8 * 1024) ? (int)std::max(1.0, std::min((double)SW_CHUNKS, cells / 2e9)) : 1;
-    if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h);
+    if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h, 1);
     int32_t cut[SW_CHUNKS + 1];
     int64_t cig_at[SW_CHUNKS + 1];
     cut[0] = 0;
@@ -1077,7 +1091,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     auto run = [&](int k) {
         cudaSetDevice(dev);
         st[k] = sw_batch_range(reqs + cut[k], cut[k + 1] - cut[k], cut[k], cig_at[k], trace, T, cell_limit, fin,
-                               &errs[k], &h2d[k], &d2h[k]);
+                               &errs[k], &h2d[k], &d2h[k], K);
     };
     std::vector<std::thread> th;
     for (int k = 0; k + 1 < K; ++k) th.emplace_back(run, k);
@@ -1394,9 +1408,10 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
     if (!r.c || !out || max < 2) return GA_INVALID_ARGUMENT;
     if (r.c->dev_gen != r.gen) return GA_INVALID_ARGUMENT;
     const int NB = route_buckets();
-    int32_t counts[64], esc[32];
+    std::vector<int32_t> counts(2 * NB + 2);
+    int32_t esc[32];
     if (cudaDeviceSynchronize() != cudaSuccess ||
-        cudaMemcpy(counts, r.counts, sizeof(int32_t) * (2 * NB + 2), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(counts.data(), r.counts, sizeof(int32_t) * (2 * NB + 2), cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(esc, r.ctr + 32, sizeof(int32_t) * 32, cudaMemcpyDeviceToHost) != cudaSuccess) {
         cudaGetLastError();
         return GA_DEVICE_ERROR;
@@ -1472,7 +1487,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             if (err) *err = E_LAUNCH;
             return GA_DEVICE_ERROR;
         }
-        const SwSlots S = size_sw(P, true, T, c->sm_count);
+        const SwSlots S = size_sw(P, true, T, c->sm_count, sw_dir_budget(c, 1));
         auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
             Carve k(base);
             k.off = plan_bytes;
@@ -1551,7 +1566,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         }
     SwPlan P;
     plan_sw(n, al.data(), bl.data(), pure.data(), skip.data(), sc, trace != 0, T, P);
-    const SwSlots S = size_sw(P, trace != 0, T, c->sm_count);
+    const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
     const int64_t nw = P.words();
     auto layout = [&](char* base, uint8_t** pp, int32_t** wk, int32_t** tb, int32_t** ctr, int32_t** edge,
                       uint32_t** dirs) {

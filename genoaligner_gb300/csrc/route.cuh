@@ -10,11 +10,11 @@ namespace ga {
 // Lane queue: pairs run one per lane, 32 per warp.  Eligible: both sides pure
 // ACGT, at most LANE_MAXLEN bases, first smax <= the tuned lane_smax, itself
 // at most LANE_SMAX (the lane kernel's shared-memory wavefront bound).
-constexpr int LANE_SMAX = 15;
+constexpr int LANE_SMAX = 31;
 constexpr int LANE_MAXLEN = 256;
 // Buckets: keys 0 .. ROUTE_BUCKETS-1 are the warp queue by bit length of the
 // predicted distance bound, ROUTE_BUCKETS + s the lane queue with first smax s.
-constexpr int ROUTE_BUCKETS = 16;
+constexpr int ROUTE_BUCKETS = 32;
 
 __device__ __forceinline__ int bitlen(unsigned x) { return 32 - __clz(x); }
 

@@ -350,7 +350,7 @@ typedef struct ga_tune {
     int32_t sw_long_log2;   /* 32-bit traceback: pairs above 2^sw_long_log2 cells take
                                the 512 x 512 tile shape, the rest 64 x 64; 16 .. 30 */
     int32_t wfa_lane_smax;  /* learned WFA: pairs whose first smax is <= this run one
-                               per lane, 32 per warp (0 = none: one pair per warp); 0 .. 15 */
+                               per lane, 32 per warp (0 = none: one pair per warp); 0 .. 31 */
     int32_t sw_coop_log2;   /* 32-bit traceback, long shape: pairs above 2^sw_coop_log2 cells
                                run on the 4 warps of a block (128 lanes per pair) instead of
                                one warp; 16 .. 40 (40: never) */
