@@ -612,6 +612,7 @@ struct SwPlan {
     int64_t n32[3] = {0, 0, 0}, n16[3] = {0, 0, 0};   // ints of each list in the flattened work array
     int64_t dir32[3] = {0, 0, 0}, dir16[3] = {0, 0, 0};
     int64_t edge_slot = 2;
+    int64_t max16_cells = 0;                          // the 16-bit list's largest item (rows x columns)
     int64_t words() const
     {
         int64_t s = 0;
@@ -686,6 +687,7 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
             P.w16[k].push_back(a);
             P.w16[k].push_back(b);
             const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
+            if (k == 0) P.max16_cells = std::max<int64_t>(P.max16_cells, (int64_t)M * N);
             P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0) ? sw16ck_dir_words(M, N, T.sw_window)
                                                                         : sw16_dir_words(M, N, kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
@@ -727,6 +729,7 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, in
         P.dir32[k] = (hres[SP_DIR + 3 + k] + 3) / 4 * 4;
     }
     P.edge_slot = std::max<int64_t>(2, hres[SP_EDGE]);
+    P.max16_cells = hres[SP_MAXC16];
     return cudaSuccess;
 }
 
@@ -792,7 +795,9 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
             A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + k; A.err = err;
-            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], T.sw_window, st)
+            A.coop_cells = (k == 0 && T.sw_coop_log2 < 40) ? ((int64_t)1 << T.sw_coop_log2) : -1;
+            const bool blocks = A.coop_cells >= 0 && P.max16_cells > A.coop_cells;
+            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], T.sw_window, blocks, st)
                                                            : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
         }

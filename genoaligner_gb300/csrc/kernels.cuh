@@ -55,6 +55,7 @@ struct Sw16Args {
     int64_t edge_slot;
     int32_t* counter;
     int32_t* err;
+    int64_t coop_cells = -1; // sw16ck: items above this many cells run on a whole block (< 0: none)
 };
 
 // The learned-bucketed WFA path (wfa_routed.cu).
@@ -117,10 +118,11 @@ cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_
 // with the checkpointed kernels only list 0 (sw16ck), 3 (sw32ck short shape)
 // and 4 (sw32ck long shape) are used.  The record `res` (SP_RES long longs):
 // per list its pair count, its length in the flattened work array and its
-// offset there, the largest per-warp memory of its items (32-bit words), and
-// the band-edge slot (2 * the longest text).
+// offset there, the largest per-warp memory of its items (32-bit words), the
+// band-edge slot (2 * the longest text), and the 16-bit list's largest item
+// (larger row count x larger column count of its two pairs).
 constexpr int SP_LISTS = 6, SP_L16 = 0, SP_L32 = 3, SP_L32LONG = 4;
-constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_RES = 25;
+constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_MAXC16 = 25, SP_RES = 26;
 struct SwPlanArgs {
     PairDesc D;                  // a = text (rows), b = pattern (columns); D.pure set
     int32_t match, mismatch, gap_open, gap_extend;
@@ -147,7 +149,8 @@ cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, con
 int sw32ck_max_slots(bool long_pairs, int sm_count);
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st);
 int sw16ck_max_slots(int sm_count, int window);
-cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, cudaStream_t st);
+// blocks: the variant with the whole-block phase (items above A.coop_cells)
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st);
 int64_t sw16_dir_words(int M, int N, int C);
 int sw16_max_slots(int C, int sm_count);
 cudaError_t launch_sw16(const Sw16Args& A, int C, int slots, cudaStream_t st);

@@ -104,7 +104,10 @@ struct FwdCtx {
 // Band starting at column b0 (0-based), CB columns per lane (the band covers
 // 32 CB columns; the last band of a pair takes the smallest CB that reaches
 // its last column).  Updates the lane's best (value, row, column) per pair.
-template <int CB>
+// COOP: the band is one of an item's bands run by the warps of a block
+// together (fwd16_coop); the warp then meets the block's barrier after every
+// 32 steps, ceil((M + 31) / 32) times per band.
+template <int CB, bool COOP>
 __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& cA, int& vB, int& rB, int& cB)
 {
     constexpr int NH = CB / 2;
@@ -161,7 +164,7 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
             in_hg = l_hg;
             in_e = l_e;
         }
-        if (i < 1 || i > M) continue;
+        if (i >= 1 && i <= M) {
         const uint32_t* pA = X.prof + (ch & 0xffffu) + t;
         const uint32_t* pB = X.prof + (ch >> 16) + t;
         uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
@@ -205,6 +208,8 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         const uint32_t imp = ((~d & K2) >> 15) * 0xffffu;
         bmax = __vmaxs2(bmax, rowmax);
         brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
+        }
+        if (COOP && ((tau & 31) == 31 || tau == steps - 1)) __syncthreads();
     }
     // merge the band into the lane's best; the column kept is the first of the
     // lane's span in this band (spans order like their columns)
@@ -236,17 +241,49 @@ __device__ __forceinline__ void ck_profile_tile(uint32_t* prof, const uint8_t* p
     }
 }
 
-// TG: tiles recomputed per window pass, the walk's and the TG - 1 to its left.
-template <int TG>
-__global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
+// The forward pass of one item by the 4 warps of a block: band b runs on warp
+// b % 4, starting at 32-step chunk start(b) = max(start(b-1) + 2, start(b-4) +
+// chunks per band), so each band's first lane reads the left edge of rows
+// 32c+1 .. 32c+32 (written by the band before it up to its step 32c + 62)
+// after the barrier that closed that band's chunk c + 1, and each warp runs
+// its bands one after the other.  Every warp meets the block barrier once per
+// chunk, idle or not: start(last band) + chunks per band times in all.
+__device__ void fwd16_coop(const FwdCtx& X, int N, int t, int wib, int& vA, int& rA, int& cA, int& vB, int& rB,
+                           int& cB)
 {
-    static_assert(TG == 2 || TG == 4, "tile groups split the warp evenly, window rows are 16-byte vectors");
-    extern __shared__ uint32_t ck_smem[];
-    const int t = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    uint32_t* wslot = A.dirs + slot * A.dir_slot;
-    uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
+    const int nck = (X.M + 62) / 32;                  // ceil((M + 31) / 32)
+    int g = 0, prev = -2, b = 0;
+    int st4[4] = {0, 0, 0, 0};
+    for (int b0 = 0; b0 < N; ++b) {
+        const int rest = N - b0;
+        const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
+        const int s = max(prev + 2, b >= 4 ? st4[b & 3] + nck : 0);
+        prev = s;
+        st4[b & 3] = s;
+        if ((b & 3) == wib) {
+            for (; g < s; ++g) __syncthreads();
+            if (cb == 16) fwd_band<16, true>(X, b0, t, vA, rA, cA, vB, rB, cB);
+            else if (cb == 8) fwd_band<8, true>(X, b0, t, vA, rA, cA, vB, rB, cB);
+            else if (cb == 4) fwd_band<4, true>(X, b0, t, vA, rA, cA, vB, rB, cB);
+            else fwd_band<2, true>(X, b0, t, vA, rA, cA, vB, rB, cB);
+            g += nck;
+        }
+        b0 += 32 * cb;
+    }
+    const int G = prev + nck;
+    for (; g < G; ++g) __syncthreads();
+}
+
+// One work item (two pairs): the forward pass (by this warp, or by the
+// block's 4 warps when coop), the best cells, the windows and walks (this
+// warp, or warp 0 of the block) and the outputs.  wslot: the item's
+// checkpoint memory (warp 0's slot when coop); prof: this warp's shared
+// memory.  In coop every warp returns after the same barriers; the caller
+// closes the item with one more barrier.
+template <int TG>
+__device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uint32_t* wslot, uint32_t* prof,
+                        int (*s_best)[6])
+{
     const int go = A.gap_open, ge = A.gap_extend;
     const int sm = A.match + go, sx = A.mismatch + go;
     // unbiased forward constants (per half)
@@ -257,358 +294,427 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
     // biased recompute constants (sw16.cu)
     const uint32_t B2 = (uint32_t)CK_BIAS * 0x10001u;
 
-    for (;;) {
-        int w = 0;
-        if (t == 0) w = atomicAdd(A.counter, 1);
-        w = __shfl_sync(FULL, w, 0);
-        if (w >= A.nwork) break;
-        __syncwarp();
-        const int pa = A.work[2 * w];
-        const bool has_b = A.work[2 * w + 1] >= 0;
-        const int pb = has_b ? A.work[2 * w + 1] : pa;
-        const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
-        const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
-        const uint8_t* textA = A.D.seq + A.D.a_off[pa];
-        const uint8_t* patA = A.D.seq + A.D.b_off[pa];
-        const uint8_t* textB = A.D.seq + A.D.a_off[pb];
-        const uint8_t* patB = A.D.seq + A.D.b_off[pb];
-        const int M = max(mA, mB), N = max(nA, nB);
-        const int ncol = ck_ncol(N);
-        const int nq = ck_rows(M);
-        // slot layout: checkpoint rows [q][col][2], column edges [k][row][2],
-        // tile tables [pair][step][lane]
-        uint32_t* ck = wslot;
-        uint32_t* ce = ck + 2 * (int64_t)nq * ncol;
-        uint32_t* tiles = ce + (2 * (int64_t)(ncol / TW) * M + 3) / 4 * 4;     // 16-byte aligned
+    const int pa = A.work[2 * w];
+    const bool has_b = A.work[2 * w + 1] >= 0;
+    const int pb = has_b ? A.work[2 * w + 1] : pa;
+    const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
+    const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
+    const uint8_t* textA = A.D.seq + A.D.a_off[pa];
+    const uint8_t* patA = A.D.seq + A.D.b_off[pa];
+    const uint8_t* textB = A.D.seq + A.D.a_off[pb];
+    const uint8_t* patB = A.D.seq + A.D.b_off[pb];
+    const int M = max(mA, mB), N = max(nA, nB);
+    const int ncol = ck_ncol(N);
+    const int nq = ck_rows(M);
+    // slot layout: checkpoint rows [q][col][2], column edges [k][row][2],
+    // tile tables [pair][step][lane]
+    uint32_t* ck = wslot;
+    uint32_t* ce = ck + 2 * (int64_t)nq * ncol;
+    uint32_t* tiles = ce + (2 * (int64_t)(ncol / TW) * M + 3) / 4 * 4;     // 16-byte aligned
 
-        // ------------------------------------------------ forward pass --
-        int vA = 0, rA = 0, cA = 0, vB = 0, rB = 0, cB = 0;          // lane's best per pair
-        {
-            FwdCtx X{textA, textB, patA, patB, mA, nA, mB, nB, M, ncol, ck, ce, prof, sm, sx, NGO2, NGE2, GO2};
+    // ------------------------------------------------ forward pass --
+    int vA = 0, rA = 0, cA = 0, vB = 0, rB = 0, cB = 0;          // lane's best per pair
+    {
+        FwdCtx X{textA, textB, patA, patB, mA, nA, mB, nB, M, ncol, ck, ce, prof, sm, sx, NGO2, NGE2, GO2};
+        if (coop) {
+            fwd16_coop(X, N, t, wib, vA, rA, cA, vB, rB, cB);
+        } else {
             for (int b0 = 0; b0 < N;) {
-                const int rest = N - b0;                              // columns from this band on
+                const int rest = N - b0;                          // columns from this band on
                 const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
-                if (cb == 16) fwd_band<16>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else if (cb == 8) fwd_band<8>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else if (cb == 4) fwd_band<4>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else fwd_band<2>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                if (cb == 16) fwd_band<16, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 8) fwd_band<8, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 4) fwd_band<4, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else fwd_band<2, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
                 b0 += 32 * cb;
             }
         }
-        // per pair over the warp: (max value, min row, min span); the best cell
-        // is the first column of that row holding the value -- in that span, as
-        // any earlier column holding it would belong to an earlier span
+    }
+    // per pair over the warp: (max value, min row, min span); the best cell
+    // is the first column of that row holding the value -- in that span, as
+    // any earlier column holding it would belong to an earlier span
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const int ov = __shfl_xor_sync(FULL, vA, o), orr = __shfl_xor_sync(FULL, rA, o), oc = __shfl_xor_sync(FULL, cA, o);
-            if (ov > 0 && ck_better(ov, orr, oc, vA, rA, cA)) { vA = ov; rA = orr; cA = oc; }
-            const int ov2 = __shfl_xor_sync(FULL, vB, o), orr2 = __shfl_xor_sync(FULL, rB, o), oc2 = __shfl_xor_sync(FULL, cB, o);
-            if (ov2 > 0 && ck_better(ov2, orr2, oc2, vB, rB, cB)) { vB = ov2; rB = orr2; cB = oc2; }
+    for (int o = 16; o > 0; o >>= 1) {
+        const int ov = __shfl_xor_sync(FULL, vA, o), orr = __shfl_xor_sync(FULL, rA, o), oc = __shfl_xor_sync(FULL, cA, o);
+        if (ov > 0 && ck_better(ov, orr, oc, vA, rA, cA)) { vA = ov; rA = orr; cA = oc; }
+        const int ov2 = __shfl_xor_sync(FULL, vB, o), orr2 = __shfl_xor_sync(FULL, rB, o), oc2 = __shfl_xor_sync(FULL, cB, o);
+        if (ov2 > 0 && ck_better(ov2, orr2, oc2, vB, rB, cB)) { vB = ov2; rB = orr2; cB = oc2; }
+    }
+    if (coop) {
+        // the block's best per pair: every warp reduces the four warps' bests in the same order
+        if (t == 0) {
+            s_best[wib][0] = vA; s_best[wib][1] = rA; s_best[wib][2] = cA;
+            s_best[wib][3] = vB; s_best[wib][4] = rB; s_best[wib][5] = cB;
         }
+        __syncthreads();
+        vA = s_best[0][0]; rA = s_best[0][1]; cA = s_best[0][2];
+        vB = s_best[0][3]; rB = s_best[0][4]; cB = s_best[0][5];
+        for (int q = 1; q < 4; ++q) {
+            if (s_best[q][0] > 0 && ck_better(s_best[q][0], s_best[q][1], s_best[q][2], vA, rA, cA)) {
+                vA = s_best[q][0]; rA = s_best[q][1]; cA = s_best[q][2];
+            }
+            if (s_best[q][3] > 0 && ck_better(s_best[q][3], s_best[q][4], s_best[q][5], vB, rB, cB)) {
+                vB = s_best[q][3]; rB = s_best[q][4]; cB = s_best[q][5];
+            }
+        }
+        if (wib != 0) return;                     // the windows and walks are warp 0's
+    }
 
-        // ----------------------------------------------------- the walks --
-        // per pair: cell, state (0 H, 1 E, 2 F), tracked value, CIGAR cursor, tile
-        int wi[2] = {rA, rB}, wj[2] = {cA, cB}, wst[2] = {0, 0}, wv[2] = {vA, vB};
-        int wpos[2] = {mA + nA, mB + nB};
-        bool done[2] = {vA <= 0, !has_b || vB <= 0};
+    // ----------------------------------------------------- the walks --
+    // per pair: cell, state (0 H, 1 E, 2 F), tracked value, CIGAR cursor, tile
+    int wi[2] = {rA, rB}, wj[2] = {cA, cB}, wst[2] = {0, 0}, wv[2] = {vA, vB};
+    int wpos[2] = {mA + nA, mB + nB};
+    bool done[2] = {vA <= 0, !has_b || vB <= 0};
 #pragma unroll
-        for (int x = 0; x < 2; ++x) {
-            if (x == 1 && !has_b) break;
-            if (t == 0) {
-                const int p = x ? pb : pa;
-                if (done[x]) {
-                    A.out_score[p] = 0;
-                    A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
-                    A.out_len[p] = 0;
-                } else {
-                    A.out_score[p] = x ? vB : vA;
-                    A.out_pos[4 * p + 2] = (x ? rB : rA) - 1;
-                }
+    for (int x = 0; x < 2; ++x) {
+        if (x == 1 && !has_b) break;
+        if (t == 0) {
+            const int p = x ? pb : pa;
+            if (done[x]) {
+                A.out_score[p] = 0;
+                A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
+                A.out_len[p] = 0;
+            } else {
+                A.out_score[p] = x ? vB : vA;
+                A.out_pos[4 * p + 2] = (x ? rB : rA) - 1;
             }
         }
-        bool first[2] = {!done[0], !done[1]};                // the best cell's column not yet found
-        const int best_of[2] = {vA, vB};
-        int ti0[2] = {1, 1}, tb[2] = {0, 0};
+    }
+    bool first[2] = {!done[0], !done[1]};                // the best cell's column not yet found
+    const int best_of[2] = {vA, vB};
+    int ti0[2] = {1, 1}, tb[2] = {0, 0};
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+        ti0[x] = done[x] ? 1 : ((wi[x] - 1) / CK_K) * CK_K + 1;
+        tb[x] = done[x] ? 0 : (wj[x] - 1) / TW;
+    }
+    // window table: H of the window's cells, [row][TG * TW columns], both
+    // pairs in the 16-bit halves (biased)
+    constexpr int WCOL = TG * TW;
+    uint32_t* Ht = tiles;
+    constexpr int LG = 32 / TG, CT = TW / LG;                   // lanes per tile group, columns per lane
+    const int g = t / LG, tl = t % LG;                          // tile group, lane in group
+    while (!(done[0] && done[1])) {
+        // ---- recompute, per pair x, the window of TG tiles tb-TG+1 .. tb over rows
+        // [ti0, wi]: group g takes tile tb - TG + 1 + g, lane tl its columns
+        // CT tl .. CT tl + CT - 1
+        const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
+        const int R = max(rows0, rows1);
+        const int steps = R + LG - 1;
+        const int tgA = tb[0] - (TG - 1) + g, tgB = tb[1] - (TG - 1) + g;   // this group's tiles
+        const int colA = TW * tgA + CT * tl, colB = TW * tgB + CT * tl;    // this lane's first columns
+        __syncwarp();
+        ck_profile_tile<CT>(prof, patA, nA, colA, 0, sm, sx, t);
+        ck_profile_tile<CT>(prof, patB, nB, colB, 1, sm, sx, t);
+        uint32_t hgu[CT], fv[CT];
+        uint32_t diag_in;
+        {
+            const int qa = (ti0[0] - 1) / CK_K - 1, qb = (ti0[1] - 1) / CK_K - 1;
+            const uint32_t* ca = ck + 2 * (int64_t)max(qa, 0) * ncol;
+            const uint32_t* cb = ck + 2 * (int64_t)max(qb, 0) * ncol;
+            const bool oka = qa >= 0 && tgA >= 0, okb = qb >= 0 && tgB >= 0;
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                const uint2 va = oka ? *reinterpret_cast<const uint2*>(ca + 2 * (colA + c)) : make_uint2(NGO2, 0u);
+                const uint2 vb = okb ? *reinterpret_cast<const uint2*>(cb + 2 * (colB + c)) : make_uint2(NGO2, 0u);
+                hgu[c] = __viaddmax_s16x2(__byte_perm(va.x, vb.x, 0x7610), B2, MIN2);
+                fv[c] = __viaddmax_s16x2(__byte_perm(va.y, vb.y, 0x7610), B2, MIN2);
+            }
+            // H[i0-1][first column - 1] - go: the left lane's last column; for a
+            // group's first lane the checkpoint left of its tile (0 on row 0 and column 0)
+            uint32_t lft = __shfl_up_sync(FULL, hgu[CT - 1], 1, LG);
+            if (tl == 0) {
+                const uint32_t ha = (qa >= 0 && tgA > 0) ? ca[2 * (colA - 1)] : NGO2;
+                const uint32_t hb = (qb >= 0 && tgB > 0) ? cb[2 * (colB - 1)] : NGO2;
+                lft = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
+            }
+            diag_in = lft;
+        }
+        // the groups' left boundaries per tile row (column edges at TW * tile),
+        // combined and biased into shared memory: edg[(group * CK_K + row) * 2]
+        uint32_t* edg = prof + 2 * 4 * (CT / 2) * 32;
+        for (int idx = t; idx < TG * CK_K; idx += 32) {
+            const int gg = idx / CK_K, r = idx - gg * CK_K;
+            const int ka = tb[0] - (TG - 1) + gg, kb = tb[1] - (TG - 1) + gg;
+            const bool ina = ka > 0 && r < rows0, inb = kb > 0 && r < rows1;
+            const uint2 la = ina ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(ka - 1) * M + (ti0[0] - 1 + r)))
+                                 : make_uint2(NGO2, 0u);
+            const uint2 lb = inb ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(kb - 1) * M + (ti0[1] - 1 + r)))
+                                 : make_uint2(NGO2, 0u);
+            edg[2 * idx] = __viaddmax_s16x2(__byte_perm(la.x, lb.x, 0x7610), B2, MIN2);
+            edg[2 * idx + 1] = __viaddmax_s16x2(__byte_perm(la.y, lb.y, 0x7610), B2, MIN2);
+        }
+        __syncwarp();
+        const uint32_t* eg = edg + 2 * g * CK_K;
+        uint32_t out_hg = B2 - GO2, out_e = B2;
+        const uint8_t* tA = textA + (ti0[0] - 1);
+        const uint8_t* tB = textB + (ti0[1] - 1);
+        // each row's profile offsets travel along a group's lanes with the
+        // boundary values; the groups' first lanes get theirs, and the row's
+        // left edge, without a branch of their own: the offsets of 32 rows at
+        // a time are read by all lanes (lane u: row 32k + u) and shuffled out
+        uint32_t ch = 0, rb_ch = 0;
+        const uint32_t* pA0 = prof + (0 * 4 * (CT / 2)) * 32 + t;
+        const uint32_t* pB0 = prof + (1 * 4 * (CT / 2)) * 32 + t;
+        uint32_t* hrow = Ht + g * TW + CT * tl;                         // + (row - 1) * WCOL
+        for (int tau = 0; tau < steps; ++tau) {
+            if ((tau & 31) == 0 && tau < R) {
+                const int r = tau + t;
+                if (r < R) {
+                    const int la = r < rows0 ? ck_code(__ldg(tA + r)) : 0;
+                    const int lb = r < rows1 ? ck_code(__ldg(tB + r)) : 0;
+                    rb_ch = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
+                }
+            }
+            uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, LG);
+            uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, LG);
+            ch = __shfl_up_sync(FULL, ch, 1, LG);
+            const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
+            const int er = min(tau, CK_K - 1);
+            const uint32_t l_hg = eg[2 * er], l_e = eg[2 * er + 1];
+            const int i = tau - tl + 1;                                  // window row, 1-based
+            if (tl == 0) {
+                ch = l_ch;
+                in_hg = l_hg;
+                in_e = l_e;
+            }
+            if (i < 1 || i > R) continue;
+            const uint32_t* pA = pA0 + (ch & 0xffffu);
+            const uint32_t* pB = pB0 + (ch >> 16);
+            uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
+            uint32_t hv[CT];
+#pragma unroll
+            for (int cc = 0; cc < CT; cc += 2) {
+                const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
+                const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int cu = cc + u;
+                    const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
+                    const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
+                    const uint32_t h1 = __viaddmax_s16x2(hgd, u ? S1 : S0, e);
+                    const uint32_t hh = __vimax3_s16x2(h1, f, B2);
+                    const uint32_t hg = hh - GO2;
+                    hv[cu] = hh;
+                    hgd = hgu[cu];
+                    hgu[cu] = hg;
+                    fv[cu] = f;
+                    hgl = hg;
+                    el = e;
+                }
+            }
+            uint4* dst = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
+#pragma unroll
+            for (int c = 0; c < CT; c += 4) dst[c >> 2] = make_uint4(hv[c], hv[c + 1], hv[c + 2], hv[c + 3]);
+            diag_in = in_hg;
+            out_hg = hgl;
+            out_e = el;
+        }
+        __syncwarp();
+        // the best cell's column (a pair's first window): first column of row i*
+        // holding the best value -- row i* is the window's last row
 #pragma unroll
         for (int x = 0; x < 2; ++x) {
-            ti0[x] = done[x] ? 1 : ((wi[x] - 1) / CK_K) * CK_K + 1;
-            tb[x] = done[x] ? 0 : (wj[x] - 1) / TW;
+            if (!first[x]) continue;
+            const int rows = x ? rows1 : rows0, n = x ? nB : nA;
+            const int wc0 = TW * (tb[x] - (TG - 1));                    // 0-based column of window column 0
+            int jf = INT32_MAX;
+            constexpr int PER = WCOL / 32;
+#pragma unroll
+            for (int c = PER - 1; c >= 0; --c) {
+                const int col = wc0 + PER * t + c;
+                if (col >= 0 && col < n) {
+                    const uint32_t w = Ht[(rows - 1) * WCOL + PER * t + c];
+                    if ((int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS == best_of[x]) jf = col + 1;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) jf = min(jf, __shfl_xor_sync(FULL, jf, o));
+            first[x] = false;
+            const int p = x ? pb : pa;
+            if (jf == INT32_MAX) {                 // cannot happen: the forward pass saw the value here
+                if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
+                done[x] = true;
+                continue;
+            }
+            wj[x] = jf;
+            if (t == 0) A.out_pos[4 * p + 3] = jf - 1;
         }
-        // window table: H of the window's cells, [row][TG * TW columns], both
-        // pairs in the 16-bit halves (biased)
-        constexpr int WCOL = TG * TW;
-        uint32_t* Ht = tiles;
-        constexpr int LG = 32 / TG, CT = TW / LG;                   // lanes per tile group, columns per lane
-        const int g = t / LG, tl = t % LG;                          // tile group, lane in group
-        while (!(done[0] && done[1])) {
-            // ---- recompute, per pair x, the window of TG tiles tb-TG+1 .. tb over rows
-            // [ti0, wi]: group g takes tile tb - TG + 1 + g, lane tl its columns
-            // CT tl .. CT tl + CT - 1
-            const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
-            const int R = max(rows0, rows1);
-            const int steps = R + LG - 1;
-            const int tgA = tb[0] - (TG - 1) + g, tgB = tb[1] - (TG - 1) + g;   // this group's tiles
-            const int colA = TW * tgA + CT * tl, colB = TW * tgB + CT * tl;    // this lane's first columns
-            __syncwarp();
-            ck_profile_tile<CT>(prof, patA, nA, colA, 0, sm, sx, t);
-            ck_profile_tile<CT>(prof, patB, nB, colB, 1, sm, sx, t);
-            uint32_t hgu[CT], fv[CT];
-            uint32_t diag_in;
-            {
-                const int qa = (ti0[0] - 1) / CK_K - 1, qb = (ti0[1] - 1) / CK_K - 1;
-                const uint32_t* ca = ck + 2 * (int64_t)max(qa, 0) * ncol;
-                const uint32_t* cb = ck + 2 * (int64_t)max(qb, 0) * ncol;
-                const bool oka = qa >= 0 && tgA >= 0, okb = qb >= 0 && tgB >= 0;
+        // ---- walk each pair inside its window, tracking the exact value of the
+        // current cell's H (state 0), E (1) or F (2).  Every decision is the
+        // reference's tie rule read off H values: H came from the diagonal iff
+        // H[i-1][j-1] + s == H (the diagonal wins ties), else from E iff E == H
+        // (E wins ties with F), else from F; a gap cell was opened iff the
+        // neighbour's H - gap_open equals it (opening wins ties).
 #pragma unroll
-                for (int c = 0; c < CT; ++c) {
-                    const uint2 va = oka ? *reinterpret_cast<const uint2*>(ca + 2 * (colA + c)) : make_uint2(NGO2, 0u);
-                    const uint2 vb = okb ? *reinterpret_cast<const uint2*>(cb + 2 * (colB + c)) : make_uint2(NGO2, 0u);
-                    hgu[c] = __viaddmax_s16x2(__byte_perm(va.x, vb.x, 0x7610), B2, MIN2);
-                    fv[c] = __viaddmax_s16x2(__byte_perm(va.y, vb.y, 0x7610), B2, MIN2);
+        for (int x = 0; x < 2; ++x) {
+            if (done[x]) continue;
+            const int p = x ? pb : pa;
+            const int m = x ? mB : mA, n = x ? nB : nA;
+            const uint8_t* text = x ? textB : textA;
+            const uint8_t* pat = x ? patB : patA;
+            char* slotc = A.out_cigar + A.D.out_off[p];
+            const int i0 = ti0[x], jlo = TW * (tb[x] - (TG - 1)) + 1;     // first window row / column
+            const int q = (i0 - 1) / CK_K - 1;                              // checkpoint row i0 - 1
+            const uint32_t* crow = ck + 2 * (int64_t)max(q, 0) * ncol;
+            const int kedge = (jlo - 1) / TW;                               // column edge at jlo - 1 (if >= 1)
+            const uint32_t* cedge = kedge > 0 ? ce + 2 * (int64_t)(kedge - 1) * M : nullptr;
+            auto half = [x](uint32_t w) { return x ? hi16s(w) : lo16s(w); };
+            // H[ii][jj] for ii in [i0 - 1, i], jj in [jlo - 1, j]
+            auto Hv = [&](int ii, int jj) -> int {
+                if (ii <= 0 || jj <= 0) return 0;
+                if (ii == i0 - 1) return half(crow[2 * (jj - 1)]) + go;
+                if (jj == jlo - 1) return half(cedge[2 * (ii - 1)]) + go;
+                const uint32_t w = Ht[(ii - i0) * WCOL + (jj - jlo)];
+                return (int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS;
+            };
+            // E[ii][jj] from the row's H values left of jj within the window and the
+            // column edge's E (E[ii][0] = 0): warp-parallel max over the gap lengths
+            auto Ev = [&](int ii, int jj) -> int {
+                const int kl = max(jlo - 1, 0);
+                int e = INT32_MIN / 2;
+                for (int k = jj - 1 - t; k >= kl; k -= 32) e = max(e, Hv(ii, k) - go - (jj - 1 - k) * ge);
+                if (t == 0) {
+                    const int eb = (kl > 0) ? half(cedge[2 * (ii - 1) + 1]) : 0;
+                    e = max(e, eb - (jj - kl) * ge);
                 }
-                // H[i0-1][first column - 1] - go: the left lane's last column; for a
-                // group's first lane the checkpoint left of its tile (0 on row 0 and column 0)
-                uint32_t lft = __shfl_up_sync(FULL, hgu[CT - 1], 1, LG);
-                if (tl == 0) {
-                    const uint32_t ha = (qa >= 0 && tgA > 0) ? ca[2 * (colA - 1)] : NGO2;
-                    const uint32_t hb = (qb >= 0 && tgB > 0) ? cb[2 * (colB - 1)] : NGO2;
-                    lft = __viaddmax_s16x2(__byte_perm(ha, hb, 0x7610), B2, MIN2);
-                }
-                diag_in = lft;
-            }
-            // the groups' left boundaries per tile row (column edges at TW * tile),
-            // combined and biased into shared memory: edg[(group * CK_K + row) * 2]
-            uint32_t* edg = prof + 2 * 4 * (CT / 2) * 32;
-            for (int idx = t; idx < TG * CK_K; idx += 32) {
-                const int gg = idx / CK_K, r = idx - gg * CK_K;
-                const int ka = tb[0] - (TG - 1) + gg, kb = tb[1] - (TG - 1) + gg;
-                const bool ina = ka > 0 && r < rows0, inb = kb > 0 && r < rows1;
-                const uint2 la = ina ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(ka - 1) * M + (ti0[0] - 1 + r)))
-                                     : make_uint2(NGO2, 0u);
-                const uint2 lb = inb ? *reinterpret_cast<const uint2*>(ce + 2 * ((int64_t)(kb - 1) * M + (ti0[1] - 1 + r)))
-                                     : make_uint2(NGO2, 0u);
-                edg[2 * idx] = __viaddmax_s16x2(__byte_perm(la.x, lb.x, 0x7610), B2, MIN2);
-                edg[2 * idx + 1] = __viaddmax_s16x2(__byte_perm(la.y, lb.y, 0x7610), B2, MIN2);
-            }
-            __syncwarp();
-            const uint32_t* eg = edg + 2 * g * CK_K;
-            uint32_t out_hg = B2 - GO2, out_e = B2;
-            const uint8_t* tA = textA + (ti0[0] - 1);
-            const uint8_t* tB = textB + (ti0[1] - 1);
-            // each row's profile offsets travel along a group's lanes with the
-            // boundary values; the groups' first lanes get theirs, and the row's
-            // left edge, without a branch of their own: the offsets of 32 rows at
-            // a time are read by all lanes (lane u: row 32k + u) and shuffled out
-            uint32_t ch = 0, rb_ch = 0;
-            const uint32_t* pA0 = prof + (0 * 4 * (CT / 2)) * 32 + t;
-            const uint32_t* pB0 = prof + (1 * 4 * (CT / 2)) * 32 + t;
-            uint32_t* hrow = Ht + g * TW + CT * tl;                         // + (row - 1) * WCOL
-            for (int tau = 0; tau < steps; ++tau) {
-                if ((tau & 31) == 0 && tau < R) {
-                    const int r = tau + t;
-                    if (r < R) {
-                        const int la = r < rows0 ? ck_code(__ldg(tA + r)) : 0;
-                        const int lb = r < rows1 ? ck_code(__ldg(tB + r)) : 0;
-                        rb_ch = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(FULL, e, o));
+                return e;
+            };
+            int i = wi[x], j = wj[x], state = wst[x], v = wv[x], pos = wpos[x];
+            bool fin = false;
+            for (;;) {
+                if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
+                if (i < i0 || j < jlo) break;                               // left the window
+                if (state == 0) {
+                    // a run of diagonal steps resolved at once: lane u takes the step from
+                    // cell (i - u, j - u), whose value is the H lane u - 1 read; the run
+                    // ends at the first step that is not diagonal or starts at H = 0
+                    const int U = min(min(32, pos), min(i - max(i0, 1), j - max(jlo, 1)) + 1);
+                    int hd = 0;
+                    bool eq = false;
+                    if (t < U) {
+                        eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
+                        hd = Hv(i - 1 - t, j - 1 - t);
+                    }
+                    int vu = __shfl_up_sync(FULL, hd, 1);
+                    if (t == 0) vu = v;
+                    const bool ok = t < U && vu != 0 && hd + (eq ? A.match : A.mismatch) == vu;
+                    const unsigned run = __ballot_sync(FULL, ok);
+                    const int r = run == FULL ? 32 : __ffs(~run) - 1;
+                    if (r > 0) {
+                        if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
+                        v = __shfl_sync(FULL, hd, r - 1);
+                        i -= r;
+                        j -= r;
+                        pos -= r;
+                        continue;
                     }
                 }
-                uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, LG);
-                uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, LG);
-                ch = __shfl_up_sync(FULL, ch, 1, LG);
-                const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
-                const int er = min(tau, CK_K - 1);
-                const uint32_t l_hg = eg[2 * er], l_e = eg[2 * er + 1];
-                const int i = tau - tl + 1;                                  // window row, 1-based
-                if (tl == 0) {
-                    ch = l_ch;
-                    in_hg = l_hg;
-                    in_e = l_e;
-                }
-                if (i < 1 || i > R) continue;
-                const uint32_t* pA = pA0 + (ch & 0xffffu);
-                const uint32_t* pB = pB0 + (ch >> 16);
-                uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
-                uint32_t hv[CT];
-#pragma unroll
-                for (int cc = 0; cc < CT; cc += 2) {
-                    const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
-                    const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int cu = cc + u;
-                        const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
-                        const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
-                        const uint32_t h1 = __viaddmax_s16x2(hgd, u ? S1 : S0, e);
-                        const uint32_t hh = __vimax3_s16x2(h1, f, B2);
-                        const uint32_t hg = hh - GO2;
-                        hv[cu] = hh;
-                        hgd = hgu[cu];
-                        hgu[cu] = hg;
-                        fv[cu] = f;
-                        hgl = hg;
-                        el = e;
-                    }
-                }
-                uint4* dst = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
-#pragma unroll
-                for (int c = 0; c < CT; c += 4) dst[c >> 2] = make_uint4(hv[c], hv[c + 1], hv[c + 2], hv[c + 3]);
-                diag_in = in_hg;
-                out_hg = hgl;
-                out_e = el;
-            }
-            __syncwarp();
-            // the best cell's column (a pair's first window): first column of row i*
-            // holding the best value -- row i* is the window's last row
-#pragma unroll
-            for (int x = 0; x < 2; ++x) {
-                if (!first[x]) continue;
-                const int rows = x ? rows1 : rows0, n = x ? nB : nA;
-                const int wc0 = TW * (tb[x] - (TG - 1));                    // 0-based column of window column 0
-                int jf = INT32_MAX;
-                constexpr int PER = WCOL / 32;
-#pragma unroll
-                for (int c = PER - 1; c >= 0; --c) {
-                    const int col = wc0 + PER * t + c;
-                    if (col >= 0 && col < n) {
-                        const uint32_t w = Ht[(rows - 1) * WCOL + PER * t + c];
-                        if ((int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS == best_of[x]) jf = col + 1;
-                    }
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) jf = min(jf, __shfl_xor_sync(FULL, jf, o));
-                first[x] = false;
-                const int p = x ? pb : pa;
-                if (jf == INT32_MAX) {                 // cannot happen: the forward pass saw the value here
-                    if (t == 0) atomicOr(A.err, ERR_BAD_INPUT);
-                    done[x] = true;
-                    continue;
-                }
-                wj[x] = jf;
-                if (t == 0) A.out_pos[4 * p + 3] = jf - 1;
-            }
-            // ---- walk each pair inside its window, tracking the exact value of the
-            // current cell's H (state 0), E (1) or F (2).  Every decision is the
-            // reference's tie rule read off H values: H came from the diagonal iff
-            // H[i-1][j-1] + s == H (the diagonal wins ties), else from E iff E == H
-            // (E wins ties with F), else from F; a gap cell was opened iff the
-            // neighbour's H - gap_open equals it (opening wins ties).
-#pragma unroll
-            for (int x = 0; x < 2; ++x) {
-                if (done[x]) continue;
-                const int p = x ? pb : pa;
-                const int m = x ? mB : mA, n = x ? nB : nA;
-                const uint8_t* text = x ? textB : textA;
-                const uint8_t* pat = x ? patB : patA;
-                char* slotc = A.out_cigar + A.D.out_off[p];
-                const int i0 = ti0[x], jlo = TW * (tb[x] - (TG - 1)) + 1;     // first window row / column
-                const int q = (i0 - 1) / CK_K - 1;                              // checkpoint row i0 - 1
-                const uint32_t* crow = ck + 2 * (int64_t)max(q, 0) * ncol;
-                const int kedge = (jlo - 1) / TW;                               // column edge at jlo - 1 (if >= 1)
-                const uint32_t* cedge = kedge > 0 ? ce + 2 * (int64_t)(kedge - 1) * M : nullptr;
-                auto half = [x](uint32_t w) { return x ? hi16s(w) : lo16s(w); };
-                // H[ii][jj] for ii in [i0 - 1, i], jj in [jlo - 1, j]
-                auto Hv = [&](int ii, int jj) -> int {
-                    if (ii <= 0 || jj <= 0) return 0;
-                    if (ii == i0 - 1) return half(crow[2 * (jj - 1)]) + go;
-                    if (jj == jlo - 1) return half(cedge[2 * (ii - 1)]) + go;
-                    const uint32_t w = Ht[(ii - i0) * WCOL + (jj - jlo)];
-                    return (int)(x ? (w >> 16) : (w & 0xffffu)) - CK_BIAS;
-                };
-                // E[ii][jj] from the row's H values left of jj within the window and the
-                // column edge's E (E[ii][0] = 0): warp-parallel max over the gap lengths
-                auto Ev = [&](int ii, int jj) -> int {
-                    const int kl = max(jlo - 1, 0);
-                    int e = INT32_MIN / 2;
-                    for (int k = jj - 1 - t; k >= kl; k -= 32) e = max(e, Hv(ii, k) - go - (jj - 1 - k) * ge);
-                    if (t == 0) {
-                        const int eb = (kl > 0) ? half(cedge[2 * (ii - 1) + 1]) : 0;
-                        e = max(e, eb - (jj - kl) * ge);
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(FULL, e, o));
-                    return e;
-                };
-                int i = wi[x], j = wj[x], state = wst[x], v = wv[x], pos = wpos[x];
-                bool fin = false;
-                for (;;) {
-                    if (i <= 0 || j <= 0 || (state == 0 && v == 0)) { fin = true; break; }
-                    if (i < i0 || j < jlo) break;                               // left the window
-                    if (state == 0) {
-                        // a run of diagonal steps resolved at once: lane u takes the step from
-                        // cell (i - u, j - u), whose value is the H lane u - 1 read; the run
-                        // ends at the first step that is not diagonal or starts at H = 0
-                        const int U = min(min(32, pos), min(i - max(i0, 1), j - max(jlo, 1)) + 1);
-                        int hd = 0;
-                        bool eq = false;
-                        if (t < U) {
-                            eq = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
-                            hd = Hv(i - 1 - t, j - 1 - t);
-                        }
-                        int vu = __shfl_up_sync(FULL, hd, 1);
-                        if (t == 0) vu = v;
-                        const bool ok = t < U && vu != 0 && hd + (eq ? A.match : A.mismatch) == vu;
-                        const unsigned run = __ballot_sync(FULL, ok);
-                        const int r = run == FULL ? 32 : __ffs(~run) - 1;
-                        if (r > 0) {
-                            if (t < r) slotc[pos - 1 - t] = eq ? 'M' : 'X';
-                            v = __shfl_sync(FULL, hd, r - 1);
-                            i -= r;
-                            j -= r;
-                            pos -= r;
-                            continue;
-                        }
-                    }
-                    char op;
-                    if (state == 0) {
-                        const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
-                        const int hd = Hv(i - 1, j - 1);
-                        if (hd + (ta == pc ? A.match : A.mismatch) == v) {
-                            op = ta == pc ? 'M' : 'X';
-                            v = hd;
-                            --i;
-                            --j;
-                        } else if (Ev(i, j) == v) {
-                            op = 'D';
-                            if (Hv(i, j - 1) - go == v) { v += go; } else { state = 1; v += ge; }
-                            --j;
-                        } else {
-                            op = 'I';
-                            if (Hv(i - 1, j) - go == v) { v += go; } else { state = 2; v += ge; }
-                            --i;
-                        }
-                    } else if (state == 1) {
+                char op;
+                if (state == 0) {
+                    const uint8_t ta = __ldg(text + i - 1), pc = __ldg(pat + j - 1);
+                    const int hd = Hv(i - 1, j - 1);
+                    if (hd + (ta == pc ? A.match : A.mismatch) == v) {
+                        op = ta == pc ? 'M' : 'X';
+                        v = hd;
+                        --i;
+                        --j;
+                    } else if (Ev(i, j) == v) {
                         op = 'D';
-                        if (Hv(i, j - 1) - go == v) { v += go; state = 0; } else { v += ge; }
+                        if (Hv(i, j - 1) - go == v) { v += go; } else { state = 1; v += ge; }
                         --j;
                     } else {
                         op = 'I';
-                        if (Hv(i - 1, j) - go == v) { v += go; state = 0; } else { v += ge; }
+                        if (Hv(i - 1, j) - go == v) { v += go; } else { state = 2; v += ge; }
                         --i;
                     }
-                    if (pos <= 0) {
-                        if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
-                        fin = true;
-                        break;
-                    }
-                    --pos;
-                    if (t == 0) slotc[pos] = op;
-                }
-                wi[x] = i; wj[x] = j; wst[x] = state; wv[x] = v; wpos[x] = pos;
-                if (fin) {
-                    done[x] = true;
-                    if (t == 0) {
-                        A.out_pos[4 * p] = i;
-                        A.out_pos[4 * p + 1] = j;
-                        A.out_len[p] = m + n - pos;
-                    }
+                } else if (state == 1) {
+                    op = 'D';
+                    if (Hv(i, j - 1) - go == v) { v += go; state = 0; } else { v += ge; }
+                    --j;
                 } else {
-                    // next window: the block above (left its top) or the tiles to the left
-                    if (i < i0) ti0[x] = ((i - 1) / CK_K) * CK_K + 1;
-                    tb[x] = (j - 1) / TW;
+                    op = 'I';
+                    if (Hv(i - 1, j) - go == v) { v += go; state = 0; } else { v += ge; }
+                    --i;
                 }
+                if (pos <= 0) {
+                    if (t == 0) atomicOr(A.err, ERR_CIGAR_OVERFLOW);
+                    fin = true;
+                    break;
+                }
+                --pos;
+                if (t == 0) slotc[pos] = op;
             }
-            __syncwarp();
+            wi[x] = i; wj[x] = j; wst[x] = state; wv[x] = v; wpos[x] = pos;
+            if (fin) {
+                done[x] = true;
+                if (t == 0) {
+                    A.out_pos[4 * p] = i;
+                    A.out_pos[4 * p + 1] = j;
+                    A.out_len[p] = m + n - pos;
+                }
+            } else {
+                // next window: the block above (left its top) or the tiles to the left
+                if (i < i0) ti0[x] = ((i - 1) / CK_K) * CK_K + 1;
+                tb[x] = (j - 1) / TW;
+            }
         }
+        __syncwarp();
+    }
+}
+
+// TG: tiles recomputed per window pass, the walk's and the TG - 1 to its left.
+// Work items come largest first.  Items above A.coop_cells cells (larger row
+// count x larger column count of the two pairs) are taken by a whole block,
+// whose 4 warps share the forward pass; from the first smaller item on, each
+// warp takes items of its own.
+// BLK: the variant with the whole-block phase; without it every warp takes
+// items of its own and no block barrier is met.
+template <int TG, bool BLK>
+__global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
+{
+    static_assert(TG == 2 || TG == 4, "tile groups split the warp evenly, window rows are 16-byte vectors");
+    extern __shared__ uint32_t ck_smem[];
+    __shared__ int s_item;
+    __shared__ int s_best[4][6];
+    const int t = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
+    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
+    uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
+
+    // one call site of ck_item, so its body is in the kernel once
+    bool block_phase = BLK && A.coop_cells >= 0;
+    for (;;) {
+        int w = -1;
+        bool coop = false;
+        if (block_phase) {
+            if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
+            __syncthreads();
+            const int wb = s_item;
+            __syncthreads();
+            if (wb >= A.nwork) break;
+            const int pa = A.work[2 * wb], pb = A.work[2 * wb + 1];
+            const int M = max(A.D.a_len[pa], pb >= 0 ? A.D.a_len[pb] : 0);
+            const int N = max(A.D.b_len[pa], pb >= 0 ? A.D.b_len[pb] : 0);
+            if ((int64_t)M * N > A.coop_cells) {
+                w = wb;
+                coop = true;
+            } else {
+                block_phase = false;                  // warp 0 keeps this item, the others draw their own
+                if (wib == 0) w = wb;
+            }
+        }
+        if (!coop && w < 0) {
+            if (t == 0) w = atomicAdd(A.counter, 1);
+            w = __shfl_sync(FULL, w, 0);
+            if (w >= A.nwork) break;
+        }
+        __syncwarp();
+        ck_item<TG>(A, w, coop, wib, t, coop ? bslot : wslot, prof, s_best);
+        if (coop) __syncthreads();
     }
 }
 
@@ -617,19 +723,24 @@ static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t
 int sw16ck_max_slots(int sm_count, int window)
 {
     int per_sm = 0;
-    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4>, 128, sw16ck_smem());
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2>, 128, sw16ck_smem());
+    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4, true>, 128, sw16ck_smem());
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2, true>, 128, sw16ck_smem());
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
-cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, cudaStream_t st)
+cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st)
 {
     if (A.nwork <= 0) return cudaSuccess;
     if (window != 2 && window != 4) return cudaErrorInvalidValue;
-    const int blocks = (slots + 3) / 4;
+    const int grid = (slots + 3) / 4;
     launch_begin(K_SW16X2_TRACE, st);
-    if (window == 4) sw16ck_kernel<4><<<blocks, 128, sw16ck_smem(), st>>>(A);
-    else sw16ck_kernel<2><<<blocks, 128, sw16ck_smem(), st>>>(A);
+    if (window == 4) {
+        if (blocks) sw16ck_kernel<4, true><<<grid, 128, sw16ck_smem(), st>>>(A);
+        else sw16ck_kernel<4, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+    } else {
+        if (blocks) sw16ck_kernel<2, true><<<grid, 128, sw16ck_smem(), st>>>(A);
+        else sw16ck_kernel<2, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+    }
     launch_end(K_SW16X2_TRACE, st);
     return cudaGetLastError();
 }

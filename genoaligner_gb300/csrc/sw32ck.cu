@@ -536,32 +536,34 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
     uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
     unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
 
-    int first = -1;                                   // warp 0: the item that ended the block phase
-    bool more = true;
-    while (A.coop_cells >= 0) {
-        if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
-        __syncthreads();
-        const int w = s_item;
-        __syncthreads();
-        if (w >= A.nwork) { more = false; break; }
-        const int p = A.work[w];
-        if ((int64_t)A.D.a_len[p] * A.D.b_len[p] <= A.coop_cells) {
-            if (wib == 0) first = w;
-            break;
+    // one call site of c32_pair, so its body is in the kernel once
+    bool block_phase = A.coop_cells >= 0;
+    for (;;) {
+        int w = -1;
+        bool coop = false;
+        if (block_phase) {
+            if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
+            __syncthreads();
+            const int wb = s_item;
+            __syncthreads();
+            if (wb >= A.nwork) break;
+            const int p = A.work[wb];
+            if ((int64_t)A.D.a_len[p] * A.D.b_len[p] > A.coop_cells) {
+                w = wb;
+                coop = true;
+            } else {
+                block_phase = false;                  // warp 0 keeps this item, the others draw their own
+                if (wib == 0) w = wb;
+            }
         }
-        c32_pair<K, CT>(A, p, true, wib, t, bslot, wsm, s_best);
-        __syncthreads();
-    }
-    while (more) {
-        int w = first;
-        first = -1;
-        if (w < 0) {
+        if (!coop && w < 0) {
             if (t == 0) w = atomicAdd(A.counter, 1);
             w = __shfl_sync(FULL, w, 0);
+            if (w >= A.nwork) break;
         }
-        if (w >= A.nwork) break;
         __syncwarp();
-        c32_pair<K, CT>(A, A.work[w], false, wib, t, wslot, wsm, s_best);
+        c32_pair<K, CT>(A, A.work[w], coop, wib, t, coop ? bslot : wslot, wsm, s_best);
+        if (coop) __syncthreads();
     }
 }
 

@@ -19,13 +19,20 @@ constexpr int SP_NB = 4096;              // size buckets per list
 // larger of their row counts and forward column extents, so the key orders by
 // column extent (ck_ncol, in 64-column steps, widest first), then by rows
 // (18 buckets per doubling, most first): neighbours then have near-equal
-// shapes, not only near-equal cell counts.
+// shapes, not only near-equal cell counts.  Pairs 1,536 columns wide and
+// more come before all others, by cells (32 buckets per doubling, largest
+// first), so the longest work starts first and whole-block items lead.
 __device__ __forceinline__ int sp_key16(int m, int n)
 {
-    const int ncls = min(31, ck_ncol(max(n, 1)) / 64);
+    const int ncls = ck_ncol(max(n, 1)) / 64;
+    if (ncls >= 24) {
+        const float lc = log2f((float)max(m, 1) * (float)max(n, 1));
+        const int e = max(0, (int)(32.0f * (lc - 20.0f)));
+        return 1023 - min(1023, e);
+    }
     const float lm = log2f((float)max(m, 16) * (1.0f / 16.0f));
     const int mb = min(127, (int)(18.0f * lm));
-    return (31 - ncls) * 128 + (127 - mb);
+    return 1024 + (23 - ncls) * 128 + (127 - mb);
 }
 
 // Bucket of a 32-bit pair of m rows and n columns, largest first.
@@ -130,7 +137,7 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
         const int32_t* srt = P.sorted + (int64_t)l * n;
         int32_t* w = P.work + P.res[SP_BASE + l];
         unsigned long long* mx = reinterpret_cast<unsigned long long*>(P.res + SP_DIR + l);
-        unsigned long long local = 0;
+        unsigned long long local = 0, cmax = 0;
         if (l < 3) {
             const long long items = (cnt + 1) / 2;
             for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < items; q += stride) {
@@ -140,6 +147,7 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
                 const int M = max(P.D.a_len[a], b >= 0 ? P.D.a_len[b] : 0);
                 const int N = max(P.D.b_len[a], b >= 0 ? P.D.b_len[b] : 0);
                 local = max(local, (unsigned long long)sw16ck_dir_words(M, N, P.window));
+                if (l == SP_L16) cmax = max(cmax, (unsigned long long)M * (unsigned long long)N);
             }
         } else {
             for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += stride) {
@@ -149,8 +157,13 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
             }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) local = max(local, __shfl_xor_sync(FULL, local, o));
+        for (int o = 16; o > 0; o >>= 1) {
+            local = max(local, __shfl_xor_sync(FULL, local, o));
+            cmax = max(cmax, __shfl_xor_sync(FULL, cmax, o));
+        }
         if ((threadIdx.x & 31) == 0 && local) atomicMax(mx, local);
+        if ((threadIdx.x & 31) == 0 && cmax)
+            atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_MAXC16), cmax);
     }
 }
 
