@@ -331,10 +331,12 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
     cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
     fn = lambda: api.sw_device(batch, SCORING, True, sc, pos, ln, cg, stream=stream.cuda_stream,
                                trace_cell_limit=-1)
-    # the device's kernel setting (variants picked per pair: 16-bit pairs two per
-    # warp, 32-bit pairs one per warp or, above the threshold, one per block),
-    # then the plain single-variant form: every pair one per warp in 32 bits
+    # the autotuner's setting for this batch (variants picked per pair: 16-bit
+    # pairs two per warp, 32-bit pairs one per warp or, above the threshold, one
+    # per block), then the plain single-variant form: every pair one per warp
+    # in 32 bits
     saved = api.tune_get()
+    chosen, trials = api.autotune_sw(batch, SCORING, sc, pos, ln, cg, reps=1)
     fn()
     ms = timed(fn, stream, 1)
     out = sc.cpu().numpy().copy(), ln.cpu().numpy().copy()
@@ -346,6 +348,7 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
     return {"workload": f"sw_long_4k ({n} of 4,096 pairs): query 2-30 kb at 10%, 0-5 kb flanks, "
                         "scoring {2,-3,3,1}, score+CIGAR, no trace-cell limit",
             "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "cells": cells,
+            "tune": {"chosen": chosen, "trials": [dict(t, ms=round(m, 1)) for t, m in trials]},
             "plain_single_variant": {"form": "every pair one per warp, int32 (sw_pack16 0, no whole-block pairs)",
                                      "gcups": cells / (ms_plain * 1e-3) / 1e9, "ms_per_step": ms_plain},
             "bit_identical_to_plain": same}

@@ -613,6 +613,7 @@ struct SwPlan {
     int64_t dir32[3] = {0, 0, 0}, dir16[3] = {0, 0, 0};
     int64_t edge_slot = 2;
     int64_t max16_cells = 0;                          // the 16-bit list's largest item (rows x columns)
+    int64_t n_opt = 0, dir_opt = 0;                   // pairs on the optimistic 16-bit rule; their 32-bit memory
     int64_t words() const
     {
         int64_t s = 0;
@@ -712,6 +713,7 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, in
     A.cell_limit = cell_limit;
     A.use16 = T.sw_pack16 ? 1 : 0;
     A.window = T.sw_window;
+    A.opt16_pct = T.sw_opt16_pct;
     A.long_log2 = T.sw_long_log2;
     A.too_large_score = too_large_score;
     A.out_score = out_score;
@@ -730,6 +732,8 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, in
     }
     P.edge_slot = std::max<int64_t>(2, hres[SP_EDGE]);
     P.max16_cells = hres[SP_MAXC16];
+    P.n_opt = hres[SP_NOPT];
+    P.dir_opt = (hres[SP_DIROPT] + 3) / 4 * 4;
     return cudaSuccess;
 }
 
@@ -751,6 +755,7 @@ static int64_t sw_dir_budget(const Ctx* c, int parts)
 // need (they run one after another on one stream and share the table).
 struct SwSlots {
     int s32[3] = {0, 0, 0}, s16[3] = {0, 0, 0};
+    int s_esc = 0;                                    // the 32-bit launch for pairs handed over by the 16-bit kernel
     int64_t dir_words = 0, max_slots = 4;
 };
 
@@ -759,10 +764,12 @@ static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_cou
     SwSlots S;
     for (int k = 0; k < 3; ++k) {
         if (P.n32[k] > 0) {
+            const int bw = 4;                                          // warp slots come in blocks of 4
             int s = (trace && use_sw16ck() && k < 2) ? sw32ck_max_slots(k == 1, sm_count)
                                                      : sw_max_slots(kWidths[k], trace, sm_count);
-            s = (int)std::min<int64_t>(s, (P.n32[k] + 3) / 4 * 4);
-            if (trace && P.dir32[k] > 0) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir32[k] * 4) / 4 * 4));
+            s = (int)std::min<int64_t>(s, (P.n32[k] + bw - 1) / bw * bw);
+            if (trace && P.dir32[k] > 0)
+                s = (int)std::min<int64_t>(s, std::max<int64_t>(bw, budget / (P.dir32[k] * 4) / bw * bw));
             S.s32[k] = s;
             if (trace) S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir32[k]);
             S.max_slots = std::max<int64_t>(S.max_slots, s);
@@ -776,17 +783,29 @@ static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_cou
             S.max_slots = std::max<int64_t>(S.max_slots, s);
         }
     }
+    if (trace && P.n_opt > 0 && P.dir_opt > 0) {
+        int s = sw32ck_max_slots(true, sm_count);                      // blocks of 4 warps
+        s = (int)std::min<int64_t>(s, (P.n_opt + 3) / 4 * 4);
+        s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir_opt * 4) / 4 * 4));
+        S.s_esc = s;
+        S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir_opt);
+        S.max_slots = std::max<int64_t>(S.max_slots, s);
+    }
     return S;
 }
 
 // Enqueue every SW launch of a plan.  `dwork` holds the plan's lists
-// concatenated in the order w16[0..2] then w32[0..2]; `ctr` has 6 zeroed ints.
+// concatenated in the order w16[0..2] then w32[0..2]; `ctr` has 8 zeroed ints;
+// esc_list (n ints, device-planned batches) takes the pairs the 16-bit kernel
+// hands to the 32-bit one.
 static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc& D, const ga_sw_scoring& sc,
                                bool trace, const ga_tune& T, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
                                int32_t* out_len, char* out_cigar, uint32_t* dirs, int32_t* edge, int32_t* ctr,
-                               int32_t* err, cudaStream_t st)
+                               int32_t* err, cudaStream_t st, int32_t* esc_list = nullptr)
 {
     int64_t base = 0;
+    // ctr: [0..5] the lists' item counters, [6] pairs handed over, [7] their counter
+    const bool opt = P.n_opt > 0 && esc_list && S.s_esc > 0;
     for (int k = 0; k < 3; ++k) {
         if (P.n16[k] > 0) {
             Sw16Args A;
@@ -796,10 +815,27 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + k; A.err = err;
             A.coop_cells = (k == 0 && T.sw_coop_log2 < 40) ? ((int64_t)1 << T.sw_coop_log2) : -1;
+            if (k == 0 && opt) {
+                A.ovf_limit = sw16_overflow_limit(sc.match);
+                A.esc_list = esc_list;
+                A.esc_count = ctr + 6;
+            }
             const bool blocks = A.coop_cells >= 0 && P.max16_cells > A.coop_cells;
             const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], T.sw_window, blocks, st)
                                                            : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
+            if (k == 0 && opt) {
+                // the pairs the 16-bit kernel handed over, on the 32-bit long shape
+                SwArgs B;
+                B.D = D; B.work = esc_list; B.nwork = 0; B.nwork_dev = ctr + 6;
+                B.match = sc.match; B.mismatch = sc.mismatch; B.gap_open = sc.gap_open; B.gap_extend = sc.gap_extend;
+                B.out_score = out_score; B.out_pos = out_pos; B.out_len = out_len; B.out_cigar = out_cigar;
+                B.dirs = dirs; B.dir_slot = P.dir_opt; B.edge = edge; B.edge_slot = P.edge_slot;
+                B.counter = ctr + 7; B.err = err;
+                B.coop_cells = T.sw_coop_log2 < 40 ? ((int64_t)1 << T.sw_coop_log2) : -1;
+                const cudaError_t e2 = launch_sw32ck(B, true, S.s_esc, st);
+                if (e2 != cudaSuccess) return e2;
+            }
         }
         base += P.n16[k];
     }
@@ -1012,7 +1048,8 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     }
     extra_layout(c->dev, &dctr, &dedge, &ddirs);
     cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
-    if (launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream) != cudaSuccess ||
+    if (launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream,
+                    dplan ? dscr : nullptr) != cudaSuccess ||
         (trace && launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
                                      dln, dcg, dvf, c->stream) != cudaSuccess)) {
         cudaGetLastError();
@@ -1519,7 +1556,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
         int32_t rc = GA_OK;
         if (launch_plan(P, S, D, sc, true, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
-                        dctr + 32, st) != cudaSuccess) {
+                        dctr + 32, st, dscr) != cudaSuccess) {
             cudaGetLastError();
             if (err) *err = E_LAUNCH;
             rc = GA_DEVICE_ERROR;

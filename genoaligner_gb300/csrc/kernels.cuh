@@ -36,6 +36,7 @@ struct SwArgs {
     int32_t* counter;
     int32_t* err;
     int64_t coop_cells = -1; // sw32ck: items above this many cells run on a whole block (< 0: none)
+    const int32_t* nwork_dev = nullptr;   // when set, the item count is read here at launch (device)
 };
 
 // Two pairs per warp in 16-bit lanes (sw16.cu): work holds 2 pair indices per
@@ -56,6 +57,9 @@ struct Sw16Args {
     int32_t* counter;
     int32_t* err;
     int64_t coop_cells = -1; // sw16ck: items above this many cells run on a whole block (< 0: none)
+    int32_t ovf_limit = 1 << 30;          // a pair whose best reaches this is handed over ...
+    int32_t* esc_list = nullptr;          // ... to the 32-bit kernel: appended here
+    int32_t* esc_count = nullptr;
 };
 
 // The learned-bucketed WFA path (wfa_routed.cu).
@@ -119,16 +123,20 @@ cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_
 // and 4 (sw32ck long shape) are used.  The record `res` (SP_RES long longs):
 // per list its pair count, its length in the flattened work array and its
 // offset there, the largest per-warp memory of its items (32-bit words), the
-// band-edge slot (2 * the longest text), and the 16-bit list's largest item
-// (larger row count x larger column count of its two pairs).
+// band-edge slot (2 * the longest text), the 16-bit list's largest item
+// (larger row count x larger column count of its two pairs), and the pairs
+// taken on the optimistic 16-bit rule only: their count and the largest
+// per-warp memory the 32-bit long-shape kernel would need for them.
 constexpr int SP_LISTS = 6, SP_L16 = 0, SP_L32 = 3, SP_L32LONG = 4;
-constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_MAXC16 = 25, SP_RES = 26;
+constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_MAXC16 = 25, SP_NOPT = 26,
+              SP_DIROPT = 27, SP_RES = 28;
 struct SwPlanArgs {
     PairDesc D;                  // a = text (rows), b = pattern (columns); D.pure set
     int32_t match, mismatch, gap_open, gap_extend;
     int64_t cell_limit;          // traceback limit in cells, < 0: none
     int32_t use16;               // the 16-bit kernels may be used
     int32_t window;              // sw16ck recompute window, tiles (2 or 4)
+    int32_t opt16_pct;           // optimistic 16-bit eligibility (sw16_eligible_opt), 100: the strict bound
     int32_t long_log2;           // sw32ck long shape above 2^long_log2 cells
     int32_t too_large_score;     // score written for pairs above cell_limit
     int32_t* out_score;

@@ -365,12 +365,17 @@ __device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uin
     int wi[2] = {rA, rB}, wj[2] = {cA, cB}, wst[2] = {0, 0}, wv[2] = {vA, vB};
     int wpos[2] = {mA + nA, mB + nB};
     bool done[2] = {vA <= 0, !has_b || vB <= 0};
+    // a pair whose best reached the limit may have passed 16 bits (a pair taken
+    // on the optimistic rule): it goes to the 32-bit kernel, which writes it
+    const bool ovf[2] = {vA >= A.ovf_limit, has_b && vB >= A.ovf_limit};
 #pragma unroll
     for (int x = 0; x < 2; ++x) {
         if (x == 1 && !has_b) break;
         if (t == 0) {
             const int p = x ? pb : pa;
-            if (done[x]) {
+            if (ovf[x]) {
+                A.esc_list[atomicAdd(A.esc_count, 1)] = p;
+            } else if (done[x]) {
                 A.out_score[p] = 0;
                 A.out_pos[4 * p] = A.out_pos[4 * p + 1] = A.out_pos[4 * p + 2] = A.out_pos[4 * p + 3] = -1;
                 A.out_len[p] = 0;
@@ -380,6 +385,8 @@ __device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uin
             }
         }
     }
+    done[0] = done[0] || ovf[0];
+    done[1] = done[1] || ovf[1];
     bool first[2] = {!done[0], !done[1]};                // the best cell's column not yet found
     const int best_of[2] = {vA, vB};
     int ti0[2] = {1, 1}, tb[2] = {0, 0};

@@ -181,9 +181,9 @@ __device__ void fwd32(const Fwd32& X, int t, int& vb, int& rb, int& cb)
     }
 }
 
-// The forward pass of one pair by the 4 warps of a block: band b runs on warp
-// b % 4, starting at 32-step chunk start(b) = max(start(b-1) + 2, start(b-4) +
-// chunks per band), so each band's first lane reads the left edge of rows
+// The forward pass of one pair by the W warps of a block (W = blockDim / 32,
+// 4 or 8): band b runs on warp b % W, starting at 32-step chunk start(b) =
+// max(start(b-1) + 2, start(b-W) + chunks per band), so each band's first lane reads the left edge of rows
 // 32c+1 .. 32c+32 (written by the band before it up to its step 32c + 62)
 // after the barrier that closed that band's chunk c + 1, and each warp runs
 // its bands one after the other.  Every warp meets the block barrier once per
@@ -191,16 +191,26 @@ __device__ void fwd32(const Fwd32& X, int t, int& vb, int& rb, int& cb)
 template <bool PROF>
 __device__ void fwd32_coop(const Fwd32& X, int t, int wib, int& vb, int& rb, int& cb)
 {
+    const int W = blockDim.x >> 5;                    // warps of the block (at most C32_MAX_WARPS)
     const int nck = (X.m + 62) / 32;                  // ceil((m + 31) / 32)
     int g = 0, prev = -2, b = 0;
-    int st4[4] = {0, 0, 0, 0};
+    int stw[C32_MAX_WARPS];                           // start of the last band of each warp
+#pragma unroll
+    for (int q = 0; q < C32_MAX_WARPS; ++q) stw[q] = 0;
     for (int b0 = 0; b0 < X.n; ++b) {
         const int rest = X.n - b0;
         const int w = rest > C32_BW ? C32_C : c32_last_cb(rest);
-        const int s = max(prev + 2, b >= 4 ? st4[b & 3] + nck : 0);
+        const int ow = b % W;
+        int own = 0;
+#pragma unroll
+        for (int q = 0; q < C32_MAX_WARPS; ++q)
+            if (q == ow) own = stw[q];
+        const int s = max(prev + 2, b >= W ? own + nck : 0);
         prev = s;
-        st4[b & 3] = s;
-        if ((b & 3) == wib) {
+#pragma unroll
+        for (int q = 0; q < C32_MAX_WARPS; ++q)
+            if (q == ow) stw[q] = s;
+        if (ow == wib) {
             for (; g < s; ++g) __syncthreads();
             if (w == 16) fwd32_band<16, PROF, true>(X, b0, t, vb, rb, cb);
             else if (w == 8) fwd32_band<8, PROF, true>(X, b0, t, vb, rb, cb);
@@ -279,7 +289,7 @@ __device__ void c32_pair(const SwArgs& A, int p, bool coop, int wib, int t, uint
         if (t == 0) { s_best[wib][0] = vb; s_best[wib][1] = rb; s_best[wib][2] = cb; }
         __syncthreads();
         vb = s_best[0][0]; rb = s_best[0][1]; cb = s_best[0][2];
-        for (int q = 1; q < 4; ++q) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
             const int ov = s_best[q][0], orr = s_best[q][1], oc = s_best[q][2];
             if (ov > 0 && c32_better(ov, orr, oc, vb, rb, cb)) { vb = ov; rb = orr; cb = oc; }
         }
@@ -524,18 +534,19 @@ __device__ void c32_pair(const SwArgs& A, int p, bool coop, int wib, int t, uint
 // a whole block (its 4 warps share the forward pass); from the first smaller
 // item on, each warp takes items of its own.
 template <int K, int CT>
-__global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
+__global__ void __launch_bounds__(128, 4) sw32ck_kernel(SwArgs A)
 {
     constexpr int WSB = c32_warp_smem_bytes(K, CT);
     extern __shared__ int4 c32_smem[];
     __shared__ int s_item;
-    __shared__ int s_best[4][3];
+    __shared__ int s_best[C32_MAX_WARPS][3];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
     uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
     unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
 
+    const int nwork = A.nwork_dev ? *A.nwork_dev : A.nwork;
     // one call site of c32_pair, so its body is in the kernel once
     bool block_phase = A.coop_cells >= 0;
     for (;;) {
@@ -546,7 +557,7 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
             __syncthreads();
             const int wb = s_item;
             __syncthreads();
-            if (wb >= A.nwork) break;
+            if (wb >= nwork) break;
             const int p = A.work[wb];
             if ((int64_t)A.D.a_len[p] * A.D.b_len[p] > A.coop_cells) {
                 w = wb;
@@ -559,7 +570,7 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
         if (!coop && w < 0) {
             if (t == 0) w = atomicAdd(A.counter, 1);
             w = __shfl_sync(FULL, w, 0);
-            if (w >= A.nwork) break;
+            if (w >= nwork) break;
         }
         __syncwarp();
         c32_pair<K, CT>(A, A.work[w], coop, wib, t, coop ? bslot : wslot, wsm, s_best);
@@ -568,7 +579,7 @@ __global__ void __launch_bounds__(128) sw32ck_kernel(SwArgs A)
 }
 
 template <int K, int CT>
-static size_t c32_smem() { return (size_t)4 * c32_warp_smem_bytes(K, CT); }
+static size_t c32_smem(int warps = 4) { return (size_t)warps * c32_warp_smem_bytes(K, CT); }
 
 int sw32ck_max_slots(bool long_pairs, int sm_count)
 {
@@ -582,12 +593,14 @@ int sw32ck_max_slots(bool long_pairs, int sm_count)
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
+// slots: warp slots of A.dirs, a multiple of 4 (blocks of 4 warps).
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st)
 {
-    if (A.nwork <= 0) return cudaSuccess;
+    if (A.nwork <= 0 && !A.nwork_dev) return cudaSuccess;
+    if (slots < 4) return cudaErrorInvalidValue;
     launch_begin(K_SW32_TRACE, st);
-    if (long_pairs) sw32ck_kernel<512, 16><<<(slots + 3) / 4, 128, c32_smem<512, 16>(), st>>>(A);
-    else sw32ck_kernel<64, 2><<<(slots + 3) / 4, 128, c32_smem<64, 2>(), st>>>(A);
+    if (long_pairs) sw32ck_kernel<512, 16><<<slots / 4, 128, c32_smem<512, 16>(), st>>>(A);
+    else sw32ck_kernel<64, 2><<<slots / 4, 128, c32_smem<64, 2>(), st>>>(A);
     launch_end(K_SW32_TRACE, st);
     return cudaGetLastError();
 }

@@ -57,8 +57,15 @@ __global__ void sp_classify_kernel(SwPlanArgs P)
             if (P.cell_limit >= 0 && m > 0 && nn > 0 && ((int64_t)m + 1) * ((int64_t)nn + 1) > P.cell_limit) {
                 P.out_score[p] = P.too_large_score;                  // too large: no trace
             } else {
-                const bool u16 = P.use16 && P.D.pure[p] && P.D.pure[n + p] &&
-                                 sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
+                const bool pure = P.use16 && P.D.pure[p] && P.D.pure[n + p];
+                const bool strict = pure && sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
+                const bool u16 = strict || (pure && sw16_eligible_opt(m, nn, P.match, P.mismatch, P.gap_open,
+                                                                      P.gap_extend, P.opt16_pct));
+                if (u16 && !strict) {           // may be handed to the 32-bit long-shape kernel
+                    atomicAdd(reinterpret_cast<unsigned long long*>(P.res + SP_NOPT), 1ull);
+                    atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_DIROPT),
+                              (unsigned long long)sw32ck_dir_words(m, nn, 0));
+                }
                 const int list = u16 ? SP_L16 : (sw32ck_long(m, nn, P.long_log2) ? SP_L32LONG : SP_L32);
                 it = list * SP_NB + (u16 ? sp_key16(m, nn) : sp_key(m, nn));
                 atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_EDGE), (unsigned long long)(2 * max(m, 0)));

@@ -22,6 +22,25 @@ __host__ __device__ inline bool sw16_eligible(int m, int n, int match, int misma
     return top < 32000;
 }
 
+// Optimistic 16-bit eligibility: the bound above with the all-match score
+// scaled by pct / 100 (pct 100: the bound itself).  A pair taken on this
+// rule alone may score past 16 bits; the kernel then sees a best value of at
+// least sw16_overflow_limit and hands the pair to the 32-bit kernel.
+__host__ __device__ inline bool sw16_eligible_opt(int m, int n, int match, int mismatch, int go, int ge, int pct)
+{
+    if (m <= 0 || n <= 0) return false;
+    if (go + ge >= BIAS16 || mismatch + go < 0 || match + go > 32000) return false;
+    const int64_t top = (int64_t)match * (m < n ? m : n) * pct / 100 + BIAS16 + go;
+    return top < 32000;
+}
+
+// A best value at or above this in the 16-bit forward pass may have passed
+// 16 bits somewhere: every cell's value is exact until an H_diag + match
+// first wraps, and that H_diag (> 32767 - match) is in the best, so a best
+// below the limit proves the whole pass (and the biased windows, values up to
+// best + BIAS16 + match) exact.
+__host__ __device__ inline int sw16_overflow_limit(int match) { return 32000 - BIAS16 - match; }
+
 // sw16ck.cu: checkpoint rows every CK_K rows, column edges every CK_TW
 // columns, recompute windows of `window` tiles of CK_K x CK_TW cells (2 or 4;
 // CK_TG is the default).
@@ -60,7 +79,8 @@ __host__ __device__ inline int64_t sw16ck_dir_words(int M, int N, int window)
 constexpr int C32_C = 16;                // forward columns per lane, full bands
 constexpr int C32_BW = 32 * C32_C;
 constexpr int C32_LONG_LOG2 = 24;       // default: the long-pair shape above 2^24 cells
-constexpr int C32_COOP_LOG2 = 27;       // default: long-shape pairs above 2^27 cells run on a whole block
+constexpr int C32_COOP_LOG2 = 27;       // default: work items above 2^27 cells run on a whole block
+constexpr int C32_MAX_WARPS = 4;        // sw32ck: warps per block
 
 __host__ __device__ inline int c32_rows(int m, int K) { return m > 1 ? (m - 1) / K : 0; }
 __host__ __device__ inline int c32_last_cb(int rest) { return rest > 8 * 32 ? 16 : (rest > 4 * 32 ? 8 : 4); }

@@ -41,6 +41,7 @@ static ga_tune builtin()
     t.sw_long_log2 = C32_LONG_LOG2;
     t.wfa_lane_smax = LANE_SMAX;
     t.sw_coop_log2 = C32_COOP_LOG2;
+    t.sw_opt16_pct = 100;
     return t;
 }
 
@@ -48,13 +49,14 @@ static bool valid(const ga_tune& t)
 {
     return (t.sw_pack16 == 0 || t.sw_pack16 == 1) && (t.sw_window == 2 || t.sw_window == 4) &&
            t.sw_long_log2 >= 16 && t.sw_long_log2 <= 30 && t.wfa_lane_smax >= 0 && t.wfa_lane_smax <= LANE_SMAX &&
-           t.sw_coop_log2 >= 16 && t.sw_coop_log2 <= 40;
+           t.sw_coop_log2 >= 16 && t.sw_coop_log2 <= 40 && t.sw_opt16_pct >= 50 && t.sw_opt16_pct <= 100;
 }
 
 static bool same(const ga_tune& a, const ga_tune& b)
 {
     return a.sw_pack16 == b.sw_pack16 && a.sw_window == b.sw_window && a.sw_long_log2 == b.sw_long_log2 &&
-           a.wfa_lane_smax == b.wfa_lane_smax && a.sw_coop_log2 == b.sw_coop_log2;
+           a.wfa_lane_smax == b.wfa_lane_smax && a.sw_coop_log2 == b.sw_coop_log2 &&
+           a.sw_opt16_pct == b.sw_opt16_pct;
 }
 
 static int current_device()
@@ -199,7 +201,11 @@ int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int6
         return GA_DEVICE_ERROR;
     }
     int64_t max_cells = 0;
-    for (int i = 0; i < n; ++i) max_cells = std::max<int64_t>(max_cells, (int64_t)std::max(al[i], 0) * std::max(bl[i], 0));
+    int max_min_len = 0;
+    for (int i = 0; i < n; ++i) {
+        max_cells = std::max<int64_t>(max_cells, (int64_t)std::max(al[i], 0) * std::max(bl[i], 0));
+        max_min_len = std::max(max_min_len, std::min(al[i], bl[i]));
+    }
     auto run = [&](const char** e) {
         return ga_sw_device(batch, scoring, 1, trace_cell_limit, out_score, out_pos, out_len, out_cigar, nullptr, e);
     };
@@ -221,6 +227,9 @@ int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int6
         vals.push_back(40);                                   // every pair on one warp
         rc = sweep(S, &ga_tune::sw_coop_log2, vals, reps, run, err);
     }
+    if (rc == GA_OK && S.best.sw_pack16 && max_min_len > 0 &&
+        (int64_t)scoring.match * max_min_len + BIAS16 + scoring.gap_open >= 32000)
+        rc = sweep(S, &ga_tune::sw_opt16_pct, {100, 85, 75, 65}, reps, run, err);
     if (rc != GA_OK) return rc;
     store(dev, S.best);
     report(S, chosen, trials, max_trials, n_trials);
@@ -274,16 +283,16 @@ int32_t ga_tune_save(const char* path)
     }
     FILE* f = std::fopen(path, "w");
     if (!f) return GA_INVALID_ARGUMENT;
-    std::fprintf(f, "# genoaligner_gb300 tune v2: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax "
-                    "sw_coop_log2\n");
+    std::fprintf(f, "# genoaligner_gb300 tune v3: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax "
+                    "sw_coop_log2 sw_opt16_pct\n");
     for (const auto& r : rows) {
         cudaDeviceProp p;
         if (cudaGetDeviceProperties(&p, r.first) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
-        std::fprintf(f, "%s\t%d %d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window, r.second.sw_long_log2,
-                     r.second.wfa_lane_smax, r.second.sw_coop_log2);
+        std::fprintf(f, "%s\t%d %d %d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window,
+                     r.second.sw_long_log2, r.second.wfa_lane_smax, r.second.sw_coop_log2, r.second.sw_opt16_pct);
     }
     return std::fclose(f) == 0 ? GA_OK : GA_INVALID_ARGUMENT;
 }
@@ -300,8 +309,8 @@ int32_t ga_tune_load(const char* path)
         if (line[0] == '#' || line[0] == '\n') continue;
         char* tab = std::strchr(line, '\t');
         ga_tune t = builtin();
-        if (!tab || std::sscanf(tab + 1, "%d %d %d %d %d", &t.sw_pack16, &t.sw_window, &t.sw_long_log2,
-                                &t.wfa_lane_smax, &t.sw_coop_log2) != 5 || !valid(t)) {
+        if (!tab || std::sscanf(tab + 1, "%d %d %d %d %d %d", &t.sw_pack16, &t.sw_window, &t.sw_long_log2,
+                                &t.wfa_lane_smax, &t.sw_coop_log2, &t.sw_opt16_pct) != 6 || !valid(t)) {
             ok = false;
             break;
         }

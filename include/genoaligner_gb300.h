@@ -351,10 +351,16 @@ typedef struct ga_tune {
                                the 512 x 512 tile shape, the rest 64 x 64; 16 .. 30 */
     int32_t wfa_lane_smax;  /* learned WFA: pairs whose first smax is <= this run one
                                per lane, 32 per warp (0 = none: one pair per warp); 0 .. 31 */
-    int32_t sw_coop_log2;   /* 32-bit traceback, long shape: pairs above 2^sw_coop_log2 cells
-                               run on the 4 warps of a block (128 lanes per pair) instead of
-                               one warp; 16 .. 40 (40: never) */
-    int32_t reserved[3];
+    int32_t sw_coop_log2;   /* SW traceback: work items above 2^sw_coop_log2 cells (a 32-bit
+                               long-shape pair, or a 16-bit item of two pairs) run their forward
+                               pass on the 4 warps of a block (128 lanes) instead of one warp;
+                               16 .. 40 (40: never) */
+    int32_t sw_opt16_pct;   /* SW traceback: a pure-ACGT pair whose all-match score scaled by
+                               sw_opt16_pct / 100 fits 16 bits runs on the 16-bit kernel; one
+                               whose best then reaches the 16-bit limit is recomputed in 32 bits
+                               (exact either way).  50 .. 100 (100: only pairs whose all-match
+                               score fits) */
+    int32_t reserved[2];
 } ga_tune;
 
 /* One timed candidate of an autotuning run. */
@@ -375,7 +381,8 @@ int32_t ga_tune_set(const ga_tune* t);
  * Each candidate runs once untimed, then `reps` timed calls (reps <= 0: 2) on
  * the library's own stream.  Coordinate search: sw_pack16, then sw_window
  * (when pack16 is chosen), then sw_long_log2 (when the batch has pairs above
- * 2^20 cells), then sw_coop_log2 (when it has pairs above 2^24 cells).  chosen (may be NULL) gets the setting kept; trials[0 ..
+ * 2^20 cells), then sw_coop_log2 (when it has pairs above 2^24 cells), then
+ * sw_opt16_pct (when it has pure pairs whose all-match score passes 16 bits).  chosen (may be NULL) gets the setting kept; trials[0 ..
  * *n_trials) (may be NULL) every candidate timed.  The outputs hold the batch's
  * results on return. */
 int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int64_t trace_cell_limit,
@@ -392,7 +399,7 @@ int32_t ga_autotune_wfa(const ga_device_batch* batch, int32_t smax, int32_t trac
                         int32_t* n_trials, const char** err);
 
 /* Write every device's stored setting to a text file (one line per device:
- * name, then the five fields in the order above), or load such a file:
+ * name, then the six fields in the order above), or load such a file:
  * lines naming the current device's model set its setting.  GA_INVALID_ARGUMENT
  * on an unreadable / malformed file (nothing is changed then). */
 int32_t ga_tune_save(const char* path);

@@ -173,3 +173,43 @@ def test_sw_large_host_batch_runs_in_ranges_with_same_results():
     want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=True)
     assert np.array_equal(res["score"][idx], want.score)
     assert all(got.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))
+
+
+def test_sw_optimistic_16bit_with_handover():
+    """Pure pairs whose all-match score passes 16 bits but whose best fits run
+    on the 16-bit kernel (sw_opt16_pct); one whose best reaches the 16-bit
+    limit (a 16.5 kb identical pair, score 33,000) is handed to the 32-bit
+    kernel.  Results equal the strict rule's run and the oracle's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    pairs = [_long_pair(rng, 17000, 500, 0.08, False), _long_pair(rng, 20000, 300, 0.10, False)]
+    q = workloads.random_bases(rng, 16500).tobytes()
+    pairs.append((workloads.random_bases(rng, 200).tobytes() + q + workloads.random_bases(rng, 200).tobytes(), q))
+    ts, pp = [x[0] for x in pairs], [x[1] for x in pairs]
+    scheme = (2, -3, 3, 1)
+    ps = workloads.from_lists("t", ts, pp)
+    b = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
+    before = api.tune_get()
+    outs = {}
+    try:
+        for pct in (75, 100):
+            api.tune_set(sw_opt16_pct=pct)
+            sc = torch.empty(b.n, dtype=torch.int32, device="cuda")
+            pos = torch.empty(4 * b.n, dtype=torch.int32, device="cuda")
+            ln = torch.empty(b.n, dtype=torch.int32, device="cuda")
+            cg = torch.zeros(b.out_bytes, dtype=torch.uint8, device="cuda")
+            api.profile(True)
+            api.sw_device(b, scheme, True, sc, pos, ln, cg, trace_cell_limit=-1)
+            torch.cuda.synchronize()
+            api.profile(False)
+            outs[pct] = (sc.cpu().numpy(), pos.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy(),
+                         set(api.profile_read()))
+    finally:
+        api.tune_set(**before)
+    assert "sw16x2_trace" in outs[75][4] and "sw32_trace" in outs[75][4]     # 16-bit run, one handed over
+    assert "sw16x2_trace" not in outs[100][4]
+    for x, y in zip(outs[75][:4], outs[100][:4]):
+        assert np.array_equal(x, y)
+    want = oracle.sw_batch(ts, pp, scoring=scheme, with_cigar=True, trace_cell_limit=-1)
+    assert list(outs[75][0]) == list(want.score)
+    assert want.score[2] == 33000

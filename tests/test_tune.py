@@ -11,7 +11,8 @@ from genoaligner_gb300 import api
 
 def test_default_setting_is_valid_and_current_without_a_stored_one():
     d = api.tune_default()
-    assert d == {"sw_pack16": 1, "sw_window": 2, "sw_long_log2": 24, "wfa_lane_smax": 31, "sw_coop_log2": 27}
+    assert d == {"sw_pack16": 1, "sw_window": 2, "sw_long_log2": 24, "wfa_lane_smax": 31, "sw_coop_log2": 27,
+                 "sw_opt16_pct": 100}
     if not api.device_available():
         assert api.tune_get() == d
 
@@ -19,7 +20,8 @@ def test_default_setting_is_valid_and_current_without_a_stored_one():
 @pytest.mark.parametrize("field,value", [("sw_pack16", 2), ("sw_window", 3), ("sw_window", 8),
                                          ("sw_long_log2", 15), ("sw_long_log2", 31),
                                          ("wfa_lane_smax", -1), ("wfa_lane_smax", 32),
-                                         ("sw_coop_log2", 15), ("sw_coop_log2", 41)])
+                                         ("sw_coop_log2", 15), ("sw_coop_log2", 41),
+                                         ("sw_opt16_pct", 49), ("sw_opt16_pct", 101)])
 def test_out_of_range_settings_are_refused(field, value):
     before = api.tune_get()
     with pytest.raises(ValueError):
@@ -32,8 +34,8 @@ def test_unknown_field_refused():
         api.tune_set(tile=3)
 
 
-@pytest.mark.parametrize("body", ["GB300\t1 2\n", "GB300 1 2 24 15 27\n", "GB300\t1 5 24 15 27\n", "GB300\tx y z w v\n",
-                                  "GB300\t1 2 24 15\n"])
+@pytest.mark.parametrize("body", ["GB300\t1 2\n", "GB300 1 2 24 15 27 75\n", "GB300\t1 5 24 15 27 75\n",
+                                  "GB300\tx y z w v u\n", "GB300\t1 2 24 15 27\n", "GB300\t1 2 24 15 27 30\n"])
 def test_malformed_settings_file_refused(tmp_path, body):
     p = tmp_path / "tune.txt"
     p.write_text("# comment\n" + body)
@@ -49,7 +51,7 @@ def test_settings_file_roundtrip_without_device(tmp_path):
     lines = [x for x in p.read_text().splitlines() if not x.startswith("#")]
     if not api.device_available():
         assert lines == []
-    p.write_text("# ok\nSomeOtherGPU\t0 4 20 0 30\n")
+    p.write_text("# ok\nSomeOtherGPU\t0 4 20 0 30 80\n")
     api.tune_load(str(p))                       # names another device: nothing applied
     if not api.device_available():
         assert api.tune_get() == api.tune_default()

@@ -136,11 +136,11 @@ def test_every_wfa_lane_setting_gives_the_same_results(restore_tune):
 
 
 def test_saved_setting_loads_back(tmp_path, restore_tune):
-    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8, sw_coop_log2=25)
+    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8, sw_coop_log2=25, sw_opt16_pct=60)
     p = tmp_path / "tune.txt"
     api.tune_save(str(p))
     api.tune_set(**api.tune_default())
     api.tune_load(str(p))
     assert api.tune_get() == {"sw_pack16": 0, "sw_window": 4, "sw_long_log2": 20, "wfa_lane_smax": 8,
-                              "sw_coop_log2": 25}
+                              "sw_coop_log2": 25, "sw_opt16_pct": 60}
     assert api.device_name() in p.read_text()
