@@ -58,7 +58,7 @@ SW_WORKLOAD = ("sw_uneven_200k: 200,000 pairs, query log-uniform 50-1,000 bp, ta
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=200_000)
@@ -101,19 +101,43 @@ def max_over_ranks(x, world):
 
 
 class Clocks:
-    """nvidia-smi sampler running across the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi sampler started before the warm-up; stop() keeps the samples
+    whose timestamps fall inside the timed region (mark_begin / mark_end)."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_ms=50):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.t0 = self.t1 = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                       "-i", str(gpu_index), "-lms", "200"], stdout=self.f,
+                                       "-i", str(gpu_index), "-lms", str(period_ms)], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+
+    def wait_first(self, limit_s=5.0):
+        """Block until the sampler wrote its first line (at most limit_s)."""
+        end = time.time() + limit_s
+        while self.p is not None and time.time() < end:
+            if os.path.getsize(self.f.name) > 0:
+                return
+            time.sleep(0.02)
+
+    def mark_begin(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
+    @staticmethod
+    def _when(ts):
+        import datetime
+        try:
+            return datetime.datetime.strptime(ts.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
 
     def stop(self):
         if self.p is None:
@@ -126,20 +150,35 @@ class Clocks:
         self.f.flush()
         self.f.seek(0)
         rows = [ln.split(",") for ln in self.f.read().strip().splitlines() if ln.strip()]
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-                for k, nm in enumerate(names):
-                    if r[5 + k].strip().lower() == "active":
-                        reasons.add(nm)
-            except (ValueError, IndexError):
-                continue
         os.unlink(self.f.name)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+        def summarise(sel):
+            sm, mx, reasons = [], [], set()
+            for r in sel:
+                try:
+                    sm.append(float(r[2]))
+                    mx.append(float(r[3]))
+                    for k, nm in enumerate(names):
+                        if r[6 + k].strip().lower() == "active":
+                            reasons.add(nm)
+                except (ValueError, IndexError):
+                    continue
+            return sm, mx, reasons
+
+        window = "timed region"
+        sel = []
+        if self.t0 is not None and self.t1 is not None:
+            for r in rows:
+                w = self._when(r[0]) if r else None
+                if w is not None and self.t0 - 0.06 <= w <= self.t1 + 0.06:
+                    sel.append(r)
+        sm, mx, reasons = summarise(sel)
+        if not sm:                      # no sample stamped inside: every sample of the run
+            window = "warm-up and timed region"
+            sm, mx, reasons = summarise(rows)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "window": window, "reasons": sorted(reasons)}
 
 
 def sw_cells(ps):
@@ -209,6 +248,11 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def extra_steps(args):
+    """Timed calls of each extra workload line: 5 to 10."""
+    return max(5, min(args.steps, 10))
+
+
 def timed(fn, stream, steps, flush=None):
     """Median CUDA-event time of `steps` calls of fn on `stream` (ms)."""
     import torch
@@ -236,7 +280,7 @@ def bench_wfa_150(api, workloads, torch, dev, stream, args, cpu):
     fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream)
     for _ in range(3):
         fn()
-    dev_ms = timed(fn, stream, max(args.steps, 5), flush)
+    dev_ms = timed(fn, stream, extra_steps(args), flush)
     reqs = api.make_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, 64, True)
     res = np.zeros(n, api.RES_DT)
     cig = np.empty(int(api.load().ga_align_cigar_bytes(reqs.ctypes.data, n)), np.uint8)
@@ -245,7 +289,7 @@ def bench_wfa_150(api, workloads, torch, dev, stream, args, cpu):
     for _ in range(3):
         call()
     t = []
-    for _ in range(max(args.steps, 5)):
+    for _ in range(extra_steps(args)):
         t0 = time.perf_counter()
         call()
         t.append(time.perf_counter() - t0)
@@ -282,7 +326,7 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
             out["tune"] = {"chosen": chosen, "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials]}
         for _ in range(3):
             fn()
-        ms = timed(fn, stream, max(args.steps, 5), flush)
+        ms = timed(fn, stream, extra_steps(args), flush)
         key = "learned" if learned else "plain"
         out[key] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms}
         scores[key] = (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy())
@@ -400,20 +444,23 @@ def main():
         tune = {"chosen": chosen, "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials],
                 "by": "ga_autotune_sw on this batch (wall time per call, coordinate search)"}
 
+    clocks = Clocks(local)
+    clocks.wait_first()
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    clocks = Clocks(local)
     barrier(world)
     torch.cuda.synchronize()
     launches0 = api.kernel_launches()
     api.profile(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.mark_begin()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark_end()
     api.profile(False)
     barrier(world)
     launches = api.kernel_launches() - launches0

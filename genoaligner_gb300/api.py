@@ -412,7 +412,7 @@ def last_transfer_bytes():
 
 KERNEL_IDS = {"pack2": 0, "wfa_score": 1, "wfa_trace": 2, "sw8_score": 3, "sw16_score": 4, "sw32_score": 5,
               "sw8_trace": 6, "sw16_trace": 7, "sw32_trace": 8, "int_peak": 9, "kmer_sketch": 10, "mlp": 11,
-              "sw16x2_trace": 12, "route": 13, "sw_plan": 14}
+              "sw16x2_trace": 12, "route": 13, "sw_plan": 14, "sw16x2_score": 15}
 
 
 def profile(on: bool):

@@ -73,7 +73,8 @@ __device__ __forceinline__ int match_run(const uint64_t* __restrict__ P, const u
 // Kernel identities for launch accounting and per-kernel timing.
 enum KernelId : int {
     K_PACK = 0, K_WFA_SCORE, K_WFA_TRACE, K_SW8_SCORE, K_SW16_SCORE, K_SW32_SCORE,
-    K_SW8_TRACE, K_SW16_TRACE, K_SW32_TRACE, K_PEAK, K_SKETCH, K_MLP, K_SW16X2_TRACE, K_ROUTE, K_SWPLAN, K_COUNT
+    K_SW8_TRACE, K_SW16_TRACE, K_SW32_TRACE, K_PEAK, K_SKETCH, K_MLP, K_SW16X2_TRACE, K_ROUTE, K_SWPLAN,
+    K_SW16X2_SCORE, K_COUNT
 };
 
 // Host side, around every launch this library makes: counts the launch and,

@@ -646,6 +646,24 @@ static void order_by_size(std::vector<int32_t>& v, const int32_t* tl, const int3
     v.swap(out);
 }
 
+// The two-pairs-per-warp kernels' list order (sw16_shape_key, the device
+// planner's): a stable counting sort, so that neighbours share a shape.
+static void order_by_shape16(std::vector<int32_t>& v, const int32_t* tl, const int32_t* pl)
+{
+    if (v.size() < 2) return;
+    constexpr int NB = 4096;
+    std::vector<uint16_t> key(v.size());
+    std::vector<int32_t> cnt(NB + 1, 0);
+    for (size_t q = 0; q < v.size(); ++q) {
+        key[q] = (uint16_t)sw16_shape_key(tl[v[q]], pl[v[q]]);
+        ++cnt[key[q] + 1];
+    }
+    for (int b = 0; b < NB; ++b) cnt[b + 1] += cnt[b];
+    std::vector<int32_t> out(v.size());
+    for (size_t q = 0; q < v.size(); ++q) out[cnt[key[q]]++] = v[q];
+    v.swap(out);
+}
+
 // Traceback kernels: the checkpointed forms (sw16ck.cu for two 16-bit pairs
 // per warp, sw32ck.cu for one 32-bit pair per warp) unless GA_SW16CK=0
 // selects the forms that store every cell's direction bits (sw16.cu, sw.cu).
@@ -666,11 +684,12 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
     const bool ck = use_sw16ck();
     for (int32_t i = 0; i < n; ++i) {
         if (skip && skip[i]) continue;
-        // the checkpointed traceback kernels choose their own lane widths: list 0
-        // (list 1: 32-bit pairs for the long-pair shape)
-        const int k = (ck && trace) ? 0 : width_index(sw_width_for(pl[i]));
-        const bool use16 = use16_ok && trace && pure && pure[i] && pure[n + i] &&
+        // the checkpointed traceback kernels and the 16-bit score-only kernel
+        // choose their own lane widths: list 0 (list 1: 32-bit pairs for the
+        // long-pair shape)
+        const bool use16 = use16_ok && (trace || ck) && pure && pure[i] && pure[n + i] &&
                            sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
+        const int k = (ck && (trace || use16)) ? 0 : width_index(sw_width_for(pl[i]));
         if (use16) e16[k].push_back(i);
         else P.w32[(ck && trace && sw32ck_long(tl[i], pl[i], T.sw_long_log2)) ? 1 : k].push_back(i);
     }
@@ -682,14 +701,16 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
         }
         P.dir32[k] = (P.dir32[k] + 3) / 4 * 4;
-        order_by_size(e16[k], tl, pl);
+        if (ck && k == 0) order_by_shape16(e16[k], tl, pl);
+        else order_by_size(e16[k], tl, pl);
         for (size_t q = 0; q < e16[k].size(); q += 2) {
             const int32_t a = e16[k][q], b = q + 1 < e16[k].size() ? e16[k][q + 1] : -1;
             P.w16[k].push_back(a);
             P.w16[k].push_back(b);
             const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
             if (k == 0) P.max16_cells = std::max<int64_t>(P.max16_cells, (int64_t)M * N);
-            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0) ? sw16ck_dir_words(M, N, T.sw_window)
+            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0)
+                                                  ? (trace ? sw16ck_dir_words(M, N, T.sw_window) : sw16so_dir_words(M, N))
                                                                         : sw16_dir_words(M, N, kWidths[k]));
             P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
         }
@@ -775,7 +796,8 @@ static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_cou
             S.max_slots = std::max<int64_t>(S.max_slots, s);
         }
         if (P.n16[k] > 0) {
-            int s = (use_sw16ck() && k == 0) ? sw16ck_max_slots(sm_count, T.sw_window) : sw16_max_slots(kWidths[k], sm_count);
+            int s = (use_sw16ck() && k == 0) ? (trace ? sw16ck_max_slots(sm_count, T.sw_window) : sw16so_max_slots(sm_count))
+                                             : sw16_max_slots(kWidths[k], sm_count);
             s = (int)std::min<int64_t>(s, (P.n16[k] / 2 + 3) / 4 * 4);
             s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
             S.s16[k] = s;
@@ -821,8 +843,9 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
                 A.esc_count = ctr + 6;
             }
             const bool blocks = A.coop_cells >= 0 && P.max16_cells > A.coop_cells;
-            const cudaError_t e = (use_sw16ck() && k == 0) ? launch_sw16ck(A, S.s16[k], T.sw_window, blocks, st)
-                                                           : launch_sw16(A, kWidths[k], S.s16[k], st);
+            const cudaError_t e = (use_sw16ck() && k == 0)
+                                      ? (trace ? launch_sw16ck(A, S.s16[k], T.sw_window, blocks, st) : launch_sw16so(A, S.s16[k], st))
+                                      : launch_sw16(A, kWidths[k], S.s16[k], st);
             if (e != cudaSuccess) return e;
             if (k == 0 && opt) {
                 // the pairs the 16-bit kernel handed over, on the 32-bit long shape
@@ -1037,7 +1060,8 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         k.off = plan_end;
         *ctr = k.take<int32_t>(8, 4);
         *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-        *dirs = trace ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        // score-only 16-bit pairs keep their band edges there too
+        *dirs = (trace || S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
         return k.off;
     };
     int32_t *dctr, *dedge;
@@ -1618,7 +1642,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         *tb = k.take<int32_t>(too_big.size() + 1);
         *ctr = k.take<int32_t>(64, 256);
         *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-        *dirs = trace ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        *dirs = (trace || S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
         return k.off;
     };
     uint8_t* dpure;
@@ -1794,7 +1818,8 @@ const char* ga_profile_kernel_name(int32_t kernel_id)
 {
     static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
                                          "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
-                                         "kmer_sketch", "mlp", "sw16x2_trace", "route", "sw_plan"};
+                                         "kmer_sketch", "mlp", "sw16x2_trace", "route", "sw_plan",
+                                         "sw16x2_score"};
     return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
 }
 

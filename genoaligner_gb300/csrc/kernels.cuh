@@ -157,6 +157,8 @@ cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, con
 int sw32ck_max_slots(bool long_pairs, int sm_count);
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st);
 int sw16ck_max_slots(int sm_count, int window);
+int sw16so_max_slots(int sm_count);
+cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st);
 // blocks: the variant with the whole-block phase (items above A.coop_cells)
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st);
 int64_t sw16_dir_words(int M, int N, int C);

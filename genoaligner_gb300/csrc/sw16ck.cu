@@ -50,6 +50,32 @@ __device__ __forceinline__ int ck_code(uint32_t c) { return (int)(((c >> 1) ^ (c
 __device__ __forceinline__ int lo16s(uint32_t x) { return (int)(int16_t)(x & 0xffffu); }
 __device__ __forceinline__ int hi16s(uint32_t x) { return (int)(int16_t)(x >> 16); }
 
+// The end-cell key of the reference's score-only kernel
+// (include/genoaligner/backend/sw_kernel_impl.hip:146, 158-167): among cells
+// holding the maximum, the smallest (bit-reversed column class (j mod 32),
+// row, column), j 0-based, i 1-based.
+__device__ __forceinline__ uint64_t c9_key(int i, int j)
+{
+    return ((uint64_t)(__brev((unsigned)j & 31u) >> 27) << 58) | ((uint64_t)(i - 1) << 29) | (uint64_t)j;
+}
+__device__ __forceinline__ uint64_t c9_join(int hi, int lo) { return ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo; }
+
+// A lane's CB columns j0 + c (CB a power of two, j0 a multiple of CB, bands
+// starting at multiples of 32): their key classes brev5(j mod 32) order like
+// c with its log2(CB) bits reversed, the rank q9_rank gives; q9_col inverts it.
+template <int CB>
+__host__ __device__ constexpr int q9_rank(int c)
+{
+    int r = 0;
+    for (int b = 1; b < CB; b <<= 1) { r = (r << 1) | (c & 1); c >>= 1; }
+    return r;
+}
+template <int CB>
+__device__ __forceinline__ int q9_col(int rank)
+{
+    return CB == 1 ? 0 : (int)(__brev((unsigned)rank) >> (32 - __builtin_ctz(CB)));
+}
+
 // (value, row, column) order of the best cell: larger value, then smaller row,
 // then smaller column.
 __device__ __forceinline__ bool ck_better(int v, int r, int c, int bv, int br, int bc)
@@ -99,7 +125,71 @@ struct FwdCtx {
     uint32_t* prof;
     int sm, sx;
     uint32_t NGO2, NGE2, GO2;
+    uint32_t* rows = nullptr; // Q9: per pair and lane, the row that last raised the lane's best
 };
+
+// Q9 end-cell bookkeeping of one pair (half h) in one lane: best value v, the
+// smallest key found among its cells (k1:k0, all ones when none), and the row
+// `pend` that last raised v, whose H - go words sit in `rows` until a tie or
+// the band's end needs its key.
+template <int CB>
+__device__ __forceinline__ void q9_store(uint32_t* dst, const uint32_t (&w)[CB])
+{
+    if constexpr (CB >= 4) {
+#pragma unroll
+        for (int q = 0; q < CB / 4; ++q)
+            reinterpret_cast<uint4*>(dst)[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    } else {
+        *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
+    }
+}
+
+// mask (key order) of the lane's columns of half h holding H = v
+template <int CB>
+__device__ __forceinline__ uint32_t q9_mask(const uint32_t (&w)[CB], int v, int h, uint32_t GO2, uint32_t valid)
+{
+    const uint32_t tgt = __vsub2((uint32_t)v * 0x10001u, GO2);
+    uint32_t m = 0u;
+#pragma unroll
+    for (int c = 0; c < CB; ++c) {
+        const uint32_t eq = __vcmpeq2(w[c], tgt);
+        m |= (h ? eq >> 31 : eq & 1u) << q9_rank<CB>(c);
+    }
+    return m & valid;
+}
+
+// merge row i's smallest key among cells of half h holding v into (k1, k0)
+template <int CB>
+__device__ __forceinline__ void q9_merge_row(const uint32_t (&w)[CB], int i, int v, int h, int j0, uint32_t GO2,
+                                             uint32_t valid, int& k1, int& k0)
+{
+    const uint32_t m = q9_mask<CB>(w, v, h, GO2, valid);
+    if (m) {
+        const uint64_t key = c9_key(i, j0 + q9_col<CB>(__ffs(m) - 1));
+        if (key < c9_join(k1, k0)) { k1 = (int)(key >> 32); k0 = (int)(uint32_t)key; }
+    }
+}
+
+// the pending row of half h (stored at src) merged into (k1, k0)
+template <int CB>
+__device__ __forceinline__ void q9_resolve(const uint32_t* src, int& pend, int v, int h, int j0, uint32_t GO2,
+                                           uint32_t valid, int& k1, int& k0)
+{
+    if (pend <= 0) return;
+    uint32_t w[CB];
+    if constexpr (CB >= 4) {
+#pragma unroll
+        for (int q = 0; q < CB / 4; ++q) {
+            const uint4 x = reinterpret_cast<const uint4*>(src)[q];
+            w[4 * q] = x.x; w[4 * q + 1] = x.y; w[4 * q + 2] = x.z; w[4 * q + 3] = x.w;
+        }
+    } else {
+        const uint2 x = *reinterpret_cast<const uint2*>(src);
+        w[0] = x.x; w[1] = x.y;
+    }
+    q9_merge_row<CB>(w, pend, v, h, j0, GO2, valid, k1, k0);
+    pend = 0;
+}
 
 // Band starting at column b0 (0-based), CB columns per lane (the band covers
 // 32 CB columns; the last band of a pair takes the smallest CB that reaches
@@ -107,8 +197,12 @@ struct FwdCtx {
 // COOP: the band is one of an item's bands run by the warps of a block
 // together (fwd16_coop); the warp then meets the block's barrier after every
 // 32 steps, ceil((M + 31) / 32) times per band.
-template <int CB, bool COOP>
-__device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& cA, int& vB, int& rB, int& cB)
+// Q9: the score-only form (sw16so_kernel): no checkpoint rows, and per pair
+// the best value with the end-cell key of the reference's score-only kernel
+// (c9_key) in (r, c) as its high and low words.
+template <int CB, bool COOP, bool Q9 = false>
+__device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& cA, int& vB, int& rB, int& cB,
+                         int* pend = nullptr)
 {
     constexpr int NH = CB / 2;
     const uint32_t MIN2 = 0x80008000u, K2 = 0x80008000u;
@@ -120,6 +214,16 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     uint32_t hgu[CB], fv[CB];
 #pragma unroll
     for (int c = 0; c < CB; ++c) { hgu[c] = NGO2; fv[c] = 0u; }
+    uint32_t validA = 0u, validB = 0u;                     // Q9: the pairs' columns, in key order
+    uint32_t* rowsA = Q9 ? X.rows + t * CK_C : nullptr;
+    uint32_t* rowsB = Q9 ? X.rows + (32 + t) * CK_C : nullptr;
+    if constexpr (Q9) {
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            validA |= (uint32_t)(c < nvA) << q9_rank<CB>(c);
+            validB |= (uint32_t)(c < nvB) << q9_rank<CB>(c);
+        }
+    }
     uint32_t diag_in = NGO2, out_hg = NGO2, out_e = 0u;
     // left boundary: the column edge at column b0
     const uint32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / TW - 1) * M : nullptr;
@@ -196,6 +300,34 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         out_hg = hgl;
         out_e = el;
         if (eout) *reinterpret_cast<uint2*>(eout + 2 * (i - 1)) = make_uint2(out_hg, out_e);
+        if constexpr (Q9) {
+            // a row whose maximum reaches a pair's best so far: that maximum
+            // sits in a column of the pair (padding columns score PAD and
+            // trail the pair's last column by a gap).  A raise stores the row
+            // and defers its key; a tie takes the keys of both rows.
+            const int ra = lo16s(rowmax), rb = hi16s(rowmax);
+            const bool ka = ra > 0 && ra >= vA && i <= X.mA, kb = rb > 0 && rb >= vB && i <= X.mB;
+            if (ka || kb) {
+                if (ka) {
+                    if (ra > vA) {
+                        vA = ra; rA = cA = -1; pend[0] = i;
+                        q9_store<CB>(rowsA, hgu);
+                    } else {
+                        q9_resolve<CB>(rowsA, pend[0], vA, 0, j0, X.GO2, validA, rA, cA);
+                        q9_merge_row<CB>(hgu, i, vA, 0, j0, X.GO2, validA, rA, cA);
+                    }
+                }
+                if (kb) {
+                    if (rb > vB) {
+                        vB = rb; rB = cB = -1; pend[1] = i;
+                        q9_store<CB>(rowsB, hgu);
+                    } else {
+                        q9_resolve<CB>(rowsB, pend[1], vB, 1, j0, X.GO2, validB, rB, cB);
+                        q9_merge_row<CB>(hgu, i, vB, 1, j0, X.GO2, validB, rB, cB);
+                    }
+                }
+            }
+        } else {
         if ((i & (CK_K - 1)) == 0 && i < M) {                     // checkpoint row i
             uint4* dst = reinterpret_cast<uint4*>(X.ck + 2 * ((int64_t)(i / CK_K - 1) * X.ncol + j0));
 #pragma unroll
@@ -209,14 +341,20 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
         bmax = __vmaxs2(bmax, rowmax);
         brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
         }
+        }
         if (COOP && ((tau & 31) == 31 || tau == steps - 1)) __syncthreads();
     }
-    // merge the band into the lane's best; the column kept is the first of the
-    // lane's span in this band (spans order like their columns)
-    const int v = lo16s(bmax), r = (int)(brow & 0xffffu);
-    if (v > 0 && ck_better(v, r, j0 + 1, vA, rA, cA)) { vA = v; rA = r; cA = j0 + 1; }
-    const int v2 = hi16s(bmax), r2 = (int)(brow >> 16);
-    if (v2 > 0 && ck_better(v2, r2, j0 + 1, vB, rB, cB)) { vB = v2; rB = r2; cB = j0 + 1; }
+    if constexpr (Q9) {                                   // the band's pending rows
+        q9_resolve<CB>(rowsA, pend[0], vA, 0, j0, X.GO2, validA, rA, cA);
+        q9_resolve<CB>(rowsB, pend[1], vB, 1, j0, X.GO2, validB, rB, cB);
+    } else {
+        // merge the band into the lane's best; the column kept is the first of
+        // the lane's span in this band (spans order like their columns)
+        const int v = lo16s(bmax), r = (int)(brow & 0xffffu);
+        if (v > 0 && ck_better(v, r, j0 + 1, vA, rA, cA)) { vA = v; rA = r; cA = j0 + 1; }
+        const int v2 = hi16s(bmax), r2 = (int)(brow >> 16);
+        if (v2 > 0 && ck_better(v2, r2, j0 + 1, vB, rB, cB)) { vB = v2; rB = r2; cB = j0 + 1; }
+    }
     __syncwarp();
 }
 
@@ -725,7 +863,93 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
     }
 }
 
+// Score-only Smith-Waterman, two pairs per warp in 16-bit halves: the forward
+// pass of sw16ck_kernel without checkpoint rows (column edges every TW columns
+// carry the band boundaries), the end cell by the reference's score-only rule
+// (c9_key).  dir_slot = sw16so_dir_words.  Outputs: score, and end_i / end_j
+// (0-based) for a positive score, -1 otherwise; start cells -1.
+__global__ void __launch_bounds__(128, 4) sw16so_kernel(Sw16Args A)
+{
+    extern __shared__ uint32_t ck_smem[];
+    const int t = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t* rows = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
+    uint32_t* ce = rows + SO_ROW_WORDS;
+    uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
+    const int go = A.gap_open, ge = A.gap_extend;
+    const int sm = A.match + go, sx = A.mismatch + go;
+    const uint32_t NGO2 = ((uint32_t)(-go) & 0xffffu) * 0x10001u;
+    const uint32_t NGE2 = ((uint32_t)(-ge) & 0xffffu) * 0x10001u;
+    const uint32_t GO2 = (uint32_t)go * 0x10001u;
+    for (;;) {
+        int w = 0;
+        if (t == 0) w = atomicAdd(A.counter, 1);
+        w = __shfl_sync(FULL, w, 0);
+        if (w >= A.nwork) break;
+        __syncwarp();
+        const int pa = A.work[2 * w];
+        const bool has_b = A.work[2 * w + 1] >= 0;
+        const int pb = has_b ? A.work[2 * w + 1] : pa;
+        const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
+        const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
+        const int M = max(mA, mB), N = max(nA, nB);
+        FwdCtx X{A.D.seq + A.D.a_off[pa], A.D.seq + A.D.a_off[pb], A.D.seq + A.D.b_off[pa], A.D.seq + A.D.b_off[pb],
+                 mA, nA, mB, nB, M, ck_ncol(N), nullptr, ce, prof, sm, sx, NGO2, NGE2, GO2, rows};
+        int vA = 0, kA1 = -1, kA0 = -1, vB = 0, kB1 = -1, kB0 = -1;    // best and its key (high, low word)
+        int pend[2] = {0, 0};
+        for (int b0 = 0; b0 < N;) {
+            const int rest = N - b0;
+            const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
+            if (cb == 16) fwd_band<16, false, true>(X, b0, t, vA, kA1, kA0, vB, kB1, kB0, pend);
+            else if (cb == 8) fwd_band<8, false, true>(X, b0, t, vA, kA1, kA0, vB, kB1, kB0, pend);
+            else if (cb == 4) fwd_band<4, false, true>(X, b0, t, vA, kA1, kA0, vB, kB1, kB0, pend);
+            else fwd_band<2, false, true>(X, b0, t, vA, kA1, kA0, vB, kB1, kB0, pend);
+            b0 += 32 * cb;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            int ov = __shfl_xor_sync(FULL, vA, o), o1 = __shfl_xor_sync(FULL, kA1, o), o0 = __shfl_xor_sync(FULL, kA0, o);
+            if (ov > vA || (ov == vA && ov > 0 && c9_join(o1, o0) < c9_join(kA1, kA0))) { vA = ov; kA1 = o1; kA0 = o0; }
+            ov = __shfl_xor_sync(FULL, vB, o); o1 = __shfl_xor_sync(FULL, kB1, o); o0 = __shfl_xor_sync(FULL, kB0, o);
+            if (ov > vB || (ov == vB && ov > 0 && c9_join(o1, o0) < c9_join(kB1, kB0))) { vB = ov; kB1 = o1; kB0 = o0; }
+        }
+        if (t == 0) {
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                if (x == 1 && !has_b) break;
+                const int p = x ? pb : pa;
+                const int v = x ? vB : vA;
+                const uint64_t key = x ? c9_join(kB1, kB0) : c9_join(kA1, kA0);
+                A.out_score[p] = v;
+                A.out_pos[4 * p] = -1;
+                A.out_pos[4 * p + 1] = -1;
+                A.out_pos[4 * p + 2] = v > 0 ? (int)((key >> 29) & 0x1fffffffu) : -1;
+                A.out_pos[4 * p + 3] = v > 0 ? (int)(key & 0x1fffffffu) : -1;
+                if (A.out_len) A.out_len[p] = 0;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t); }
+
+int sw16so_max_slots(int sm_count)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16so_kernel, 128, sw16ck_smem());
+    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+}
+
+cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st)
+{
+    if (A.nwork <= 0) return cudaSuccess;
+    if (slots < 4) return cudaErrorInvalidValue;
+    launch_begin(K_SW16X2_SCORE, st);
+    sw16so_kernel<<<slots / 4, 128, sw16ck_smem(), st>>>(A);
+    launch_end(K_SW16X2_SCORE, st);
+    return cudaGetLastError();
+}
 
 int sw16ck_max_slots(int sm_count, int window)
 {

@@ -15,25 +15,8 @@ namespace ga {
 
 constexpr int SP_NB = 4096;              // size buckets per list
 
-// Bucket of a 16-bit pair: consecutive entries share a warp and run with the
-// larger of their row counts and forward column extents, so the key orders by
-// column extent (ck_ncol, in 64-column steps, widest first), then by rows
-// (18 buckets per doubling, most first): neighbours then have near-equal
-// shapes, not only near-equal cell counts.  Pairs 1,536 columns wide and
-// more come before all others, by cells (32 buckets per doubling, largest
-// first), so the longest work starts first and whole-block items lead.
-__device__ __forceinline__ int sp_key16(int m, int n)
-{
-    const int ncls = ck_ncol(max(n, 1)) / 64;
-    if (ncls >= 24) {
-        const float lc = log2f((float)max(m, 1) * (float)max(n, 1));
-        const int e = max(0, (int)(32.0f * (lc - 20.0f)));
-        return 1023 - min(1023, e);
-    }
-    const float lm = log2f((float)max(m, 16) * (1.0f / 16.0f));
-    const int mb = min(127, (int)(18.0f * lm));
-    return 1024 + (23 - ncls) * 128 + (127 - mb);
-}
+// Bucket of a 16-bit pair (sw16_shape_key).
+__device__ __forceinline__ int sp_key16(int m, int n) { return sw16_shape_key(m, n); }
 
 // Bucket of a 32-bit pair of m rows and n columns, largest first.
 __device__ __forceinline__ int sp_key(int m, int n)

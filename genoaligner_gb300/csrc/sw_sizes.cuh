@@ -3,6 +3,7 @@
 // sw16ck.cu, sw32ck.cu), the device planner (sw_plan.cu) and the host.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 
 namespace ga {
@@ -73,6 +74,37 @@ __host__ __device__ inline int64_t sw16ck_dir_words(int M, int N, int window)
     const int64_t ncol = ck_ncol(N);
     return 2 * (int64_t)ck_rows(M) * ncol + (2 * (ncol / CK_TW) * (int64_t)M + 3) / 4 * 4 +
            (int64_t)CK_K * window * CK_TW;
+}
+
+// Bucket (0..4095, smallest first) of a 16-bit pair of m rows and n columns
+// in a list of the two-pairs-per-warp kernels: consecutive entries share a
+// warp and run with the larger of their row counts and forward column
+// extents, so the key orders by column extent (ck_ncol, in 64-column steps,
+// widest first), then by rows (18 buckets per doubling, most first):
+// neighbours then have near-equal shapes, not only near-equal cell counts.
+// Pairs 1,536 columns wide and more come before all others, by cells (32
+// buckets per doubling, largest first), so the longest work starts first and
+// whole-block items lead.
+__host__ __device__ inline int sw16_shape_key(int m, int n)
+{
+    const int ncls = ck_ncol(n > 1 ? n : 1) / 64;
+    if (ncls >= 24) {
+        const float lc = log2f((float)(m > 1 ? m : 1) * (float)(n > 1 ? n : 1));
+        const int e = (int)(32.0f * (lc - 20.0f));
+        return 1023 - (e < 0 ? 0 : (e > 1023 ? 1023 : e));
+    }
+    const float lm = log2f((float)(m > 16 ? m : 16) * (1.0f / 16.0f));
+    const int mb = (int)(18.0f * lm) < 127 ? (int)(18.0f * lm) : 127;
+    return 1024 + (23 - ncls) * 128 + (127 - mb);
+}
+
+// 32-bit words of one warp slot of the 16-bit score-only kernel (sw16so in
+// sw16ck.cu): per pair and lane the row that last raised the lane's best
+// (SO_ROW_WORDS), then the column edges that carry its band boundaries.
+constexpr int SO_ROW_WORDS = 2 * 32 * CK_C;
+__host__ __device__ inline int64_t sw16so_dir_words(int M, int N)
+{
+    return SO_ROW_WORDS + (2 * (int64_t)(ck_ncol(N) / CK_TW) * M + 3) / 4 * 4 + 4;
 }
 
 // ---- 32-bit one-pair-per-warp checkpointed kernel (sw32ck.cu) ---------------

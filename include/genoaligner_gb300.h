@@ -422,7 +422,7 @@ void ga_last_transfer_bytes(int64_t* h2d, int64_t* d2h);
 /* Per-kernel timing: ga_profile(1) resets the totals and records a CUDA event
  * pair around every launch on its launch stream until ga_profile(0);
  * ga_profile_read returns the summed device milliseconds and the launch count
- * of one kernel id (0 .. 11, names from ga_profile_kernel_name). */
+ * of one kernel id (0 .. 15, names from ga_profile_kernel_name). */
 void        ga_profile(int32_t on);
 int32_t     ga_profile_read(int32_t kernel_id, double* total_ms, int64_t* launches);
 const char* ga_profile_kernel_name(int32_t kernel_id);

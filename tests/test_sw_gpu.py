@@ -213,3 +213,21 @@ def test_sw_optimistic_16bit_with_handover():
     want = oracle.sw_batch(ts, pp, scoring=scheme, with_cigar=True, trace_cell_limit=-1)
     assert list(outs[75][0]) == list(want.score)
     assert want.score[2] == 33000
+
+
+def test_sw_score_only_uneven_and_multiband_vs_oracle():
+    """Score-only batches run two pure pairs per warp in 16 bits (multi-band
+    patterns included) and the rest in 32 bits; scores and the reference's
+    score-only end cells equal the oracle's."""
+    ps = workloads.sw_uneven_200k(n=1500, seed=29)
+    ts, pp = ps.lists()
+    rng = np.random.default_rng(30)
+    for k in range(12):                                   # patterns past one 512-column band
+        core = workloads.random_bases(rng, int(rng.integers(600, 1400))).tobytes()
+        ts.append(workloads.random_bases(rng, 100).tobytes() + core + workloads.random_bases(rng, 80).tobytes())
+        pp.append(core)
+    for k in range(0, 60, 3):                              # a few bytes outside ACGT
+        t = bytearray(ts[k]); t[len(t) // 2] = ord("N"); ts[k] = bytes(t)
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False)
+    got = sw_gpu(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False, trace_cell_limit=-1)
+    assert_sw_equal(got, want, "score-only uneven")
