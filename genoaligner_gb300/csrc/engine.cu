@@ -724,7 +724,7 @@ static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8
 
 // The checkpointed kernels' plan, built on the device (sw_plan.cu) into
 // `dwork`; reads back its record and fills P's list lengths and sizes.
-static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, int64_t cell_limit,
+static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bool trace, int64_t cell_limit,
                                   int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
                                   long long* dres, long long* hres, const ga_tune& T, cudaStream_t st, SwPlan& P)
 {
@@ -737,6 +737,8 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, in
     A.opt16_pct = T.sw_opt16_pct;
     A.long_log2 = T.sw_long_log2;
     A.too_large_score = too_large_score;
+    A.score_only = trace ? 0 : 1;
+    A.maxc = sw_maxc();
     A.out_score = out_score;
     A.work = dwork;
     A.res = dres;
@@ -974,7 +976,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     // device memory: fixed blocks, then (device-built plans) the planner's scratch,
     // then counters, band edges and direction tables (sized from the plan; a
     // first pass reserves the fixed part)
-    const bool dplan = trace && use_sw16ck();
+    const bool dplan = use_sw16ck();
     const size_t plan_off = dev_fixed;
     size_t plan_end = plan_off;
     int32_t* dscr = nullptr;
@@ -1026,7 +1028,8 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
             return GA_DEVICE_ERROR;
         }
         if (dplan) {
-            if (device_plan_sw(D, s0, cell_limit, -1, dsc, dwork, dscr, dres, hres, T, c->stream, P) != cudaSuccess) {
+            if (device_plan_sw(D, s0, trace, trace ? cell_limit : -1, -1, dsc, dwork, dscr, dres, hres, T, c->stream,
+                               P) != cudaSuccess) {
                 cudaGetLastError();
                 *err = E_LAUNCH;
                 return GA_DEVICE_ERROR;
@@ -1512,9 +1515,10 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     const ga_tune T = tune_current();
-    if (trace && use_sw16ck()) {
-        // the checkpointed kernels: purity and the plan on the device, one small
-        // record back, then the launches
+    if (use_sw16ck()) {
+        // the checkpointed kernels (score-only: sw16so and the score-only
+        // widths): purity and the plan on the device, one small record back,
+        // then the launches
         auto plan_layout = [&](char* base, uint8_t** pp, int32_t** scr, int32_t** wk, long long** res) {
             Carve k(base);
             *pp = k.take<uint8_t>(2 * (size_t)n);
@@ -1539,13 +1543,14 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         D.out_off = b->out_off; D.n = n;
         cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
         cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
-        cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
+        if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
         SwPlan P;
         auto plan = [&]() {
             plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
             D.pure = dpure;
             if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
-            return device_plan_sw(D, sc, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) == cudaSuccess;
+            return device_plan_sw(D, sc, trace != 0, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) ==
+                   cudaSuccess;
         };
         if (!plan()) {
             cudaGetLastError();
@@ -1553,7 +1558,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
             if (err) *err = E_LAUNCH;
             return GA_DEVICE_ERROR;
         }
-        const SwSlots S = size_sw(P, true, T, c->sm_count, sw_dir_budget(c, 1));
+        const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
         auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
             Carve k(base);
             k.off = plan_bytes;
@@ -1579,7 +1584,7 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         run_layout(c->dev, &dctr, &dedge, &ddirs);
         cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
         int32_t rc = GA_OK;
-        if (launch_plan(P, S, D, sc, true, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+        if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
                         dctr + 32, st, dscr) != cudaSuccess) {
             cudaGetLastError();
             if (err) *err = E_LAUNCH;

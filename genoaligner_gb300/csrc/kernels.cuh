@@ -112,6 +112,7 @@ cudaError_t launch_wfa(const WfaArgs& A, int slots, cudaStream_t st);
 
 int64_t sw_dir_words(int m, int n, int C);
 int sw_width_for(int n);
+int sw_maxc();                   // widest score-only 32-bit lane width (GA_SW_MAXC: 8, 16 or 32)
 int sw_max_slots(int C, bool trace, int sm_count);
 cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
 
@@ -139,6 +140,8 @@ struct SwPlanArgs {
     int32_t opt16_pct;           // optimistic 16-bit eligibility (sw16_eligible_opt), 100: the strict bound
     int32_t long_log2;           // sw32ck long shape above 2^long_log2 cells
     int32_t too_large_score;     // score written for pairs above cell_limit
+    int32_t score_only;          // 1: lists of the score-only kernels (sw16so; sw_kernel widths by sw_maxc)
+    int32_t maxc;                // sw_maxc() of the host
     int32_t* out_score;
     int32_t* work;               // flattened work lists (2n + 8 ints)
     long long* res;              // the record above

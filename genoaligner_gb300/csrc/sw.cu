@@ -308,13 +308,19 @@ __global__ void __launch_bounds__(128) sw_kernel(SwArgs A)
 
 // Column width per lane for a pattern of n columns: the narrowest band that
 // covers the pattern, 32*C columns per band.
-int sw_width_for(int n)
+int sw_maxc()
 {
     static const int maxc = [] {
         const char* e = getenv("GA_SW_MAXC");
         const int v = e ? atoi(e) : 8;
         return (v == 8 || v == 16) ? v : 32;
     }();
+    return maxc;
+}
+
+int sw_width_for(int n)
+{
+    const int maxc = sw_maxc();
     if (n <= 256 || maxc == 8) return 8;
     if (n <= 512 || maxc == 16) return 16;
     return 32;

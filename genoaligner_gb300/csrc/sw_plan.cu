@@ -42,14 +42,19 @@ __global__ void sp_classify_kernel(SwPlanArgs P)
             } else {
                 const bool pure = P.use16 && P.D.pure[p] && P.D.pure[n + p];
                 const bool strict = pure && sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
-                const bool u16 = strict || (pure && sw16_eligible_opt(m, nn, P.match, P.mismatch, P.gap_open,
-                                                                      P.gap_extend, P.opt16_pct));
+                const bool u16 = strict || (!P.score_only && pure && sw16_eligible_opt(m, nn, P.match, P.mismatch,
+                                                                                       P.gap_open, P.gap_extend,
+                                                                                       P.opt16_pct));
                 if (u16 && !strict) {           // may be handed to the 32-bit long-shape kernel
                     atomicAdd(reinterpret_cast<unsigned long long*>(P.res + SP_NOPT), 1ull);
                     atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_DIROPT),
                               (unsigned long long)sw32ck_dir_words(m, nn, 0));
                 }
-                const int list = u16 ? SP_L16 : (sw32ck_long(m, nn, P.long_log2) ? SP_L32LONG : SP_L32);
+                // score-only 32-bit pairs: one list per lane width of sw_kernel
+                const int C = (nn <= 256 || P.maxc == 8) ? 8 : ((nn <= 512 || P.maxc == 16) ? 16 : 32);
+                const int list = u16 ? SP_L16
+                                     : (P.score_only ? SP_L32 + (C == 8 ? 0 : (C == 16 ? 1 : 2))
+                                                     : (sw32ck_long(m, nn, P.long_log2) ? SP_L32LONG : SP_L32));
                 it = list * SP_NB + (u16 ? sp_key16(m, nn) : sp_key(m, nn));
                 atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_EDGE), (unsigned long long)(2 * max(m, 0)));
             }
@@ -136,14 +141,16 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
                 w[2 * q + 1] = b;
                 const int M = max(P.D.a_len[a], b >= 0 ? P.D.a_len[b] : 0);
                 const int N = max(P.D.b_len[a], b >= 0 ? P.D.b_len[b] : 0);
-                local = max(local, (unsigned long long)sw16ck_dir_words(M, N, P.window));
+                local = max(local, (unsigned long long)(P.score_only ? sw16so_dir_words(M, N)
+                                                                     : sw16ck_dir_words(M, N, P.window)));
                 if (l == SP_L16) cmax = max(cmax, (unsigned long long)M * (unsigned long long)N);
             }
         } else {
             for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += stride) {
                 const int a = srt[q];
                 w[q] = a;
-                local = max(local, (unsigned long long)sw32ck_dir_words(P.D.a_len[a], P.D.b_len[a], P.long_log2));
+                if (!P.score_only)
+                    local = max(local, (unsigned long long)sw32ck_dir_words(P.D.a_len[a], P.D.b_len[a], P.long_log2));
             }
         }
 #pragma unroll

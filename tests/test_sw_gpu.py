@@ -4,7 +4,7 @@ import pytest
 
 import oracle
 from genoaligner_gb300 import api, workloads
-from helpers import assert_sw_equal, sw_gpu
+from helpers import assert_sw_equal, packed, sw_gpu
 
 pytestmark = pytest.mark.gpu
 
@@ -231,3 +231,45 @@ def test_sw_score_only_uneven_and_multiband_vs_oracle():
     want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False)
     got = sw_gpu(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False, trace_cell_limit=-1)
     assert_sw_equal(got, want, "score-only uneven")
+
+
+def test_sw_device_score_only_vs_oracle():
+    """The device entry without traceback: the plan is built on the device
+    (16-bit pure pairs two per warp, the rest on the 32-bit score-only
+    kernel); score and end cell equal the oracle's, start cells are -1, and
+    pairs above the given cell limit get -2."""
+    torch = pytest.importorskip("torch")
+    ps = workloads.sw_uneven_200k(n=1200, seed=41)
+    ts, pp = ps.lists()
+    rng = np.random.default_rng(42)
+    for k in range(0, 90, 3):                              # bytes outside ACGT: 32-bit kernel
+        t = bytearray(ts[k]); t[len(t) // 3] = ord("N"); ts[k] = bytes(t)
+    for _ in range(6):                                     # wide patterns: several bands
+        core = workloads.random_bases(rng, int(rng.integers(900, 2200))).tobytes()
+        ts.append(workloads.random_bases(rng, 50).tobytes() + core)
+        pp.append(core)
+    ts += [b"", b"ACGT", b"A" * 700]
+    pp += [b"ACGT", b"", b"A" * 900]
+    # (the device entry has no batch-level shared-memory refusal of the score kernel)
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False, trace_cell_limit=-1,
+                           score_smem_limit=None)
+    x = packed(ts, pp)
+    b = api.DeviceBatchT(x.a_buf, x.a_off, x.a_len, x.b_buf, x.b_off, x.b_len)
+    n = b.n
+    sc = torch.empty(n, dtype=torch.int32, device="cuda")
+    pos = torch.empty(4 * n, dtype=torch.int32, device="cuda")
+    api.sw_device(b, (2, -3, 3, 1), False, sc, pos, None, None)
+    torch.cuda.synchronize()
+    s, p4 = sc.cpu().numpy(), pos.cpu().numpy().reshape(-1, 4)
+    assert np.array_equal(s, want.score)
+    pos_ok = want.score > 0
+    assert np.array_equal(p4[pos_ok, 2], want.end_i[pos_ok]) and np.array_equal(p4[pos_ok, 3], want.end_j[pos_ok])
+    assert (p4[:, 0] == -1).all() and (p4[:, 1] == -1).all()
+    assert (p4[~pos_ok, 2:] == -1).all()
+    # a cell limit marks the larger pairs too large
+    lim = 300 * 300
+    api.sw_device(b, (2, -3, 3, 1), False, sc, pos, None, None, trace_cell_limit=lim)
+    torch.cuda.synchronize()
+    s2 = sc.cpu().numpy()
+    big = np.array([len(t) > 0 and len(p) > 0 and (len(t) + 1) * (len(p) + 1) > lim for t, p in zip(ts, pp)])
+    assert (s2[big] == -2).all() and np.array_equal(s2[~big], want.score[~big])
