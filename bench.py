@@ -187,20 +187,26 @@ def sw_cells(ps):
 
 def cpu_baseline_sw(ps, seconds, threads):
     """The oracle (a restatement of the reference's CPU path) on a bounded
-    sample: pairs taken from a fixed random permutation until ~`seconds`."""
+    sample: pairs taken from a fixed random permutation until ~`seconds`.
+    Also returns the first chunk's indices and results, against which the
+    GPU run's outputs are checked."""
     import oracle
     order = np.random.default_rng(123).permutation(ps.n)
     done_cells, t_used, k, chunk = 0, 0.0, 0, 256
+    first = None
     while t_used < seconds and k < ps.n:
-        sub = ps.subset(order[k:k + chunk])
+        idx = order[k:k + chunk]
+        sub = ps.subset(idx)
         ts, pp = sub.lists()
         t0 = time.perf_counter()
-        oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=threads)
+        got = oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=threads)
         t_used += time.perf_counter() - t0
+        if first is None:
+            first = (idx, got)
         done_cells += sw_cells(sub)
         k += chunk
         chunk = min(chunk * 2, 8192)
-    return done_cells / t_used / 1e9, k, done_cells
+    return done_cells / t_used / 1e9, k, done_cells, first
 
 
 def cpu_baseline_wfa(ps, seconds, threads, smax=64):
@@ -398,6 +404,39 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
             "bit_identical_to_plain": same}
 
 
+def bench_sw_score_only(api, torch, dev, stream, args, ps, batch, trace_scores):
+    """The headline batch without traceback: score and end cell per pair
+    (the reference's score-only path), on the device and end to end."""
+    n = ps.n
+    cells = sw_cells(ps)
+    sc = torch.empty(n, dtype=torch.int32, device=dev)
+    pos = torch.empty(4 * n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    fn = lambda: api.sw_device(batch, SCORING, False, sc, pos, None, None, stream=stream.cuda_stream)
+    for _ in range(3):
+        fn()
+    ms = timed(fn, stream, extra_steps(args), flush)
+    same = bool(np.array_equal(sc.cpu().numpy(), trace_scores))
+    reqs = api.make_sw_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING, False)
+    res = np.zeros(n, api.SWRES_DT)
+    call = lambda: api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING,
+                                             with_cigar=False, _reqs=reqs, _res=res)
+    for _ in range(2):
+        call()
+    t = []
+    for _ in range(extra_steps(args)):
+        t0 = time.perf_counter()
+        r = call()
+        t.append(time.perf_counter() - t0)
+    e2e_ms = statistics.median(t) * 1e3
+    same = same and r.status == api.Status.ok and bool(np.array_equal(r.res["score"], trace_scores))
+    return {"workload": SW_WORKLOAD.replace("score+end+start+CIGAR", "score + end cell (score-only)"),
+            "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
+            "e2e_gcups": cells / (e2e_ms * 1e-3) / 1e9, "e2e_ms_per_step": e2e_ms,
+            "l2": "256 MB buffer written between steps",
+            "scores_equal_traceback_run": same}
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
@@ -489,14 +528,7 @@ def main():
                 "kernel_ms_per_launch": top_ms / max(1, top_n), "kernel_share": top_ms / total_ms if total_ms else None,
                 "traffic_source": "profiles/sw16ck_trace_sw_uneven.md (bytes/cell x cells per launch)"}
 
-    # correctness gate of the measured run: a sample vs the oracle
-    import oracle
-    idx = np.random.default_rng(7).choice(n, 64, replace=False)
-    sc = out_score.cpu().numpy()
-    sub = ps.subset(idx)
-    ts, pp = sub.lists()
-    want = oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True)
-    parity_ok = bool(np.array_equal(sc[idx], want.score))
+    sc = out_score.cpu().numpy()            # checked against the CPU baseline's sample below
 
     # e2e through the public C ABI with host buffers
     reqs = api.make_sw_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING, True)
@@ -513,12 +545,10 @@ def main():
     e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
     e2e_ms = max_over_ranks(e2e_ms, world)
     h2d, d2h = api.last_transfer_bytes()
-    parity_ok = parity_ok and r.status == api.Status.ok and bool(
-        np.array_equal(r.res["score"][idx], want.score)) and all(
-        r.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))
 
     extra = {}
     if not args.no_extra:
+        extra["sw_score_only"] = bench_sw_score_only(api, torch, dev, stream, args, ps, batch, sc)
         extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, rank == 0)
         extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, rank == 0)
         extra["wfa_long"] = bench_wfa_long(api, workloads, torch, dev, stream, args)
@@ -527,9 +557,13 @@ def main():
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        g, k, done = cpu_baseline_sw(ps, args.cpu_seconds, threads)
+        g, k, done, (idx, want) = cpu_baseline_sw(ps, args.cpu_seconds, threads)
         cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port",
                "sample": f"{k} pairs ({done / 1e9:.2f} Gcells) of the same batch, fixed random permutation"}
+        # the timed device run and the last e2e call against the baseline's first chunk
+        parity_ok = bool(np.array_equal(sc[idx], want.score)) and r.status == api.Status.ok and bool(
+            np.array_equal(r.res["score"][idx], want.score)) and all(
+            r.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))
 
     if rank == 0:
         line = {
@@ -547,6 +581,8 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "parity_sample_ok": parity_ok,
+            "parity_sample": "the CPU baseline's first 256 pairs: scores of the timed run, scores and CIGARs "
+                             "of the last e2e call",
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
             "extra": extra,
         }

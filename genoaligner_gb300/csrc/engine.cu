@@ -192,8 +192,10 @@ static Ctx* acquire_ctx(const char** err)
         return nullptr;
     }
     {
+        // the most recently released context first: a caller on one thread
+        // keeps reusing one warm arena
         std::lock_guard<std::mutex> lk(g_ctx_mu);
-        for (size_t i = 0; i < g_ctx_free.size(); ++i) {
+        for (size_t i = g_ctx_free.size(); i-- > 0;) {
             if (g_ctx_free[i]->device == dev) {
                 Ctx* c = g_ctx_free[i];
                 g_ctx_free.erase(g_ctx_free.begin() + (long)i);
@@ -221,14 +223,48 @@ static void release_ctx(Ctx* c)
     g_ctx_free.push_back(c);
 }
 
+// Device bytes the idle contexts of `dev` hold in their arenas.
+static size_t idle_dev_bytes(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    size_t s = 0;
+    for (Ctx* c : g_ctx_free)
+        if (c->device == dev) s += c->dev_cap;
+    return s;
+}
+
+// Free idle contexts' arenas on `dev` (least recently used first) until
+// `need` bytes are free on the device or none is left.
+static void trim_idle(int dev, size_t need)
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    for (Ctx* c : g_ctx_free) {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = 0; }
+        if (fr >= need) return;
+        if (c->device != dev || !c->dev) continue;
+        if (c->pending) { cudaEventSynchronize(c->done); c->pending = false; }
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->dev);
+        c->dev = nullptr;
+        c->dev_cap = 0;
+        ++c->dev_gen;
+    }
+}
+
 static bool ensure_dev(Ctx* c, size_t bytes)
 {
     if (bytes <= c->dev_cap) return true;
     if (c->dev) { cudaStreamSynchronize(c->stream); cudaFree(c->dev); c->dev = nullptr; c->dev_cap = 0; }
     size_t want = std::max(bytes, (size_t)(c->dev_cap * 3 / 2));
     want = (want + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = 0; }
+    const size_t margin = (size_t)256 << 20;
+    if (fr < want + margin) trim_idle(c->device, want + margin);   // idle contexts' arenas give way
     if (cudaMalloc(&c->dev, want) != cudaSuccess) {
         cudaGetLastError();
+        trim_idle(c->device, (size_t)-1);
         if (cudaMalloc(&c->dev, bytes) != cudaSuccess) { cudaGetLastError(); c->dev = nullptr; return false; }
         want = bytes;
     }
@@ -761,14 +797,16 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bo
 }
 
 // Device memory the checkpoint / direction tables of one call may take:
-// 60 % of what is free now plus the call's own arena (which it may replace),
+// 60 % of what is free now plus the call's own arena (which it may replace)
+// and the idle contexts' arenas (which give way to it, trim_idle),
 // between 4 GB and 200 GB, shared by `parts` concurrent calls.  Long pairs
 // need tens of MB per resident warp, so this bounds how many run at once.
 static int64_t sw_dir_budget(const Ctx* c, int parts)
 {
     size_t fr = 0, tot = 0;
     int64_t avail = (int64_t)96 << 30;
-    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) avail = ((int64_t)fr + (int64_t)c->dev_cap) * 6 / 10;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess)
+        avail = ((int64_t)fr + (int64_t)c->dev_cap + (int64_t)idle_dev_bytes(c->device)) * 6 / 10;
     else cudaGetLastError();
     avail /= std::max(1, parts);
     return std::max<int64_t>((int64_t)4 << 30, std::min<int64_t>(avail, (int64_t)200 << 30));
