@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the device's current kernel setting instead of autotuning on the batch")
-    ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long"],
+    ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long", "sw_score_only"],
                     help="run one of the extra workloads alone (no CPU baseline) and print its JSON")
     return ap.parse_args()
 
@@ -431,10 +431,25 @@ def bench_sw_score_only(api, torch, dev, stream, args, ps, batch, trace_scores):
     e2e_ms = statistics.median(t) * 1e3
     same = same and r.status == api.Status.ok and bool(np.array_equal(r.res["score"], trace_scores))
     return {"workload": SW_WORKLOAD.replace("score+end+start+CIGAR", "score + end cell (score-only)"),
-            "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
+            "pairs": n, "cells": cells, "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms,
             "e2e_gcups": cells / (e2e_ms * 1e-3) / 1e9, "e2e_ms_per_step": e2e_ms,
             "l2": "256 MB buffer written between steps",
             "scores_equal_traceback_run": same}
+
+
+def score_only_alone(api, workloads, torch, dev, stream, args):
+    """The score-only line on the first --pairs pairs of the headline batch
+    (one traceback call first gives the scores it is compared with)."""
+    ps = workloads.sw_uneven_200k(n=args.pairs)
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    n = ps.n
+    sc = torch.empty(n, dtype=torch.int32, device=dev)
+    pos = torch.empty(4 * n, dtype=torch.int32, device=dev)
+    ln = torch.empty(n, dtype=torch.int32, device=dev)
+    cg = torch.empty(max(batch.out_bytes, 1), dtype=torch.uint8, device=dev)
+    api.sw_device(batch, SCORING, True, sc, pos, ln, cg, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    return bench_sw_score_only(api, torch, dev, stream, args, ps, batch, sc.cpu().numpy())
 
 
 def main():
@@ -456,7 +471,8 @@ def main():
         run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, False),
                "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, False),
                "wfa_long": lambda: bench_wfa_long(api, workloads, torch, dev, stream, args),
-               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096)}[args.only]
+               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096),
+               "sw_score_only": lambda: score_only_alone(api, workloads, torch, dev, stream, args)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: run()}), flush=True)
         return

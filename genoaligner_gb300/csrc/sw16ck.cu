@@ -131,7 +131,8 @@ struct FwdCtx {
 // Q9 end-cell bookkeeping of one pair (half h) in one lane: best value v, the
 // smallest key found among its cells (k1:k0, all ones when none), and the row
 // `pend` that last raised v, whose H - go words sit in `rows` until a tie or
-// the band's end needs its key.
+// the band's end needs its key.  Rows below the warp's best of the pair (taken
+// every 32 steps) are skipped: they cannot hold the end cell.
 template <int CB>
 __device__ __forceinline__ void q9_store(uint32_t* dst, const uint32_t (&w)[CB])
 {
@@ -255,6 +256,12 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
                     rb_e = lv.y;
                 }
             }
+            if constexpr (Q9) {
+                // the pairs' best so far over the warp: a lower bound of their
+                // final best, below which no cell can be the end cell
+                pend[2] = __reduce_max_sync(FULL, vA);
+                pend[3] = __reduce_max_sync(FULL, vB);
+            }
         }
         uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1);
         uint32_t in_e = __shfl_up_sync(FULL, out_e, 1);
@@ -306,7 +313,8 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
             // trail the pair's last column by a gap).  A raise stores the row
             // and defers its key; a tie takes the keys of both rows.
             const int ra = lo16s(rowmax), rb = hi16s(rowmax);
-            const bool ka = ra > 0 && ra >= vA && i <= X.mA, kb = rb > 0 && rb >= vB && i <= X.mB;
+            const bool ka = ra > 0 && ra >= max(vA, pend[2]) && i <= X.mA;
+            const bool kb = rb > 0 && rb >= max(vB, pend[3]) && i <= X.mB;
             if (ka || kb) {
                 if (ka) {
                     if (ra > vA) {
@@ -896,7 +904,7 @@ __global__ void __launch_bounds__(128, 4) sw16so_kernel(Sw16Args A)
         FwdCtx X{A.D.seq + A.D.a_off[pa], A.D.seq + A.D.a_off[pb], A.D.seq + A.D.b_off[pa], A.D.seq + A.D.b_off[pb],
                  mA, nA, mB, nB, M, ck_ncol(N), nullptr, ce, prof, sm, sx, NGO2, NGE2, GO2, rows};
         int vA = 0, kA1 = -1, kA0 = -1, vB = 0, kB1 = -1, kB0 = -1;    // best and its key (high, low word)
-        int pend[2] = {0, 0};
+        int pend[4] = {0, 0, 0, 0};      // pending rows of A and B, the warp's best of A and B
         for (int b0 = 0; b0 < N;) {
             const int rest = N - b0;
             const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
