@@ -176,6 +176,7 @@ struct Ctx {
     uint64_t gkey[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     char* host = nullptr;
     size_t host_cap = 0;
+    int tag = -1;                   // range index of a ranged SW call that created it, else -1
 };
 
 static std::mutex g_ctx_mu;
@@ -183,7 +184,12 @@ static std::vector<Ctx*> g_ctx_free;
 
 static const char* E_NODEV = "no CUDA device is available";
 
-static Ctx* acquire_ctx(const char** err)
+// A free context of the current device: the one tagged `tag` if free (range
+// k of a ranged SW call takes the context range k had before, whose arena is
+// already sized for such a range; growing an arena frees the old one, which
+// waits for the whole device), else the most recently released one (a caller
+// on one thread keeps reusing one warm arena), else a new one.
+static Ctx* acquire_ctx(const char** err, int tag = -1)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -192,20 +198,24 @@ static Ctx* acquire_ctx(const char** err)
         return nullptr;
     }
     {
-        // the most recently released context first: a caller on one thread
-        // keeps reusing one warm arena
         std::lock_guard<std::mutex> lk(g_ctx_mu);
+        long pick = -1;
         for (size_t i = g_ctx_free.size(); i-- > 0;) {
-            if (g_ctx_free[i]->device == dev) {
-                Ctx* c = g_ctx_free[i];
-                g_ctx_free.erase(g_ctx_free.begin() + (long)i);
-                if (c->pending) { cudaEventSynchronize(c->done); c->pending = false; }
-                return c;
-            }
+            if (g_ctx_free[i]->device != dev) continue;
+            if (g_ctx_free[i]->tag == tag) { pick = (long)i; break; }
+            if (pick < 0 && (tag < 0 || g_ctx_free[i]->tag < 0)) pick = (long)i;
+        }
+        if (pick >= 0) {
+            Ctx* c = g_ctx_free[(size_t)pick];
+            g_ctx_free.erase(g_ctx_free.begin() + pick);
+            if (tag >= 0) c->tag = tag;
+            if (c->pending) { cudaEventSynchronize(c->done); c->pending = false; }
+            return c;
         }
     }
     Ctx* c = new Ctx();
     c->device = dev;
+    c->tag = tag;
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
@@ -934,7 +944,7 @@ static void flatten_plan(const SwPlan& P, int32_t* out)
 // at once and share the device-memory budget.
 static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base, int64_t cig_base, bool trace,
                               const ga_tune& T, int64_t cell_limit, const SwFinish& fin, const char** err,
-                              int64_t* h2d, int64_t* d2h, int parts)
+                              int64_t* h2d, int64_t* d2h, int parts, int range_tag = -1)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
@@ -963,7 +973,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     arena += 64;
     if (!trace) cig = 0;
 
-    Ctx* c = acquire_ctx(err);
+    Ctx* c = acquire_ctx(err, range_tag);
     if (!c) return GA_DEVICE_ERROR;
     struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
 
@@ -1162,13 +1172,13 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         *err = E_SW_SMEM;
         return GA_INVALID_ARGUMENT;
     }
-    // Large traceback batches run as up to SW_CHUNKS contiguous ranges of about
-    // equal cells (one per 2 Gcells), each on its own thread, context and
-    // stream: one range's staging and copies, and its results' finish on the
-    // host, overlap the others' kernels, whose blocks also fill the SMs a
-    // range's tail leaves idle.
+    // Large batches run as up to SW_CHUNKS contiguous ranges of about equal
+    // cells (one per 2 Gcells), each on its own thread, context and stream:
+    // one range's staging and copies, and its results' finish on the host,
+    // overlap the others' kernels, whose blocks also fill the SMs a range's
+    // tail leaves idle.
     constexpr int SW_CHUNKS = 8;
-    const int K = (trace && n >= 8 * 1024) ? (int)std::max(1.0, std::min((double)SW_CHUNKS, cells / 2e9)) : 1;
+    const int K = n >= 8 * 1024 ? (int)std::max(1.0, std::min((double)SW_CHUNKS, cells / 2e9)) : 1;
     if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h, 1);
     int32_t cut[SW_CHUNKS + 1];
     int64_t cig_at[SW_CHUNKS + 1];
@@ -1198,7 +1208,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     auto run = [&](int k) {
         cudaSetDevice(dev);
         st[k] = sw_batch_range(reqs + cut[k], cut[k + 1] - cut[k], cut[k], cig_at[k], trace, T, cell_limit, fin,
-                               &errs[k], &h2d[k], &d2h[k], K);
+                               &errs[k], &h2d[k], &d2h[k], K, k);
     };
     std::vector<std::thread> th;
     for (int k = 0; k + 1 < K; ++k) th.emplace_back(run, k);
@@ -1382,7 +1392,6 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
                              ga_batch_info* info)
 {
     const ga_sw_result dflt{-1, 0, -1, -1, -1, -1, 0, 0, 0, 0, 0};
-    for (int32_t i = 0; i < n; ++i) results[i] = dflt;
     int64_t limit = GA_SW_MAX_TRACE_CELLS;
     if (opt && opt->trace_cell_limit != 0) limit = opt->trace_cell_limit;
     bool any_cigar = false;
@@ -1393,6 +1402,7 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
         int32_t res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             ga_sw_result& r = results[i];
+            r = dflt;                               // every pair of the batch passes here once
             const int64_t q = i - v.base;           // index in the range's outputs
             const int s = v.score[q];
             if (s < 0) {                            // declared size limit
@@ -1419,7 +1429,7 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
                     rs = v.vflags[q] & 1;
                     wf = (v.vflags[q] >> 1) & 1;
                 } else {
-                    sw_validate(cigar_buf + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
+                    sw_validate(cigar_buf + v.cig_base + at, len, reqs[i].text, reqs[i].text_len, r.start_i, r.end_i,
                                 reqs[i].pattern, reqs[i].pattern_len, r.start_j, r.end_j, reqs[i].scoring, s,
                                 &rs, &wf);
                 }

@@ -175,6 +175,32 @@ def test_sw_large_host_batch_runs_in_ranges_with_same_results():
     assert all(got.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))
 
 
+def test_sw_large_score_only_batch_runs_in_ranges_with_same_results():
+    """A score-only batch of several Gcells runs as ranges too; scores and end
+    cells equal the device entry's single run and, on a sample, the oracle's."""
+    torch = pytest.importorskip("torch")
+    ps = workloads.sw_uneven_200k(n=16000, seed=24)
+    assert int((ps.a_len.astype(np.int64) * ps.b_len).sum()) >= 4e9
+    got = api.align_sw_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len,
+                                    scoring=(2, -3, 3, 1), with_cigar=False)
+    assert got.status == api.Status.ok
+    b = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
+    sc = torch.empty(b.n, dtype=torch.int32, device="cuda")
+    pos = torch.empty(4 * b.n, dtype=torch.int32, device="cuda")
+    api.sw_device(b, (2, -3, 3, 1), False, sc, pos, None, None)
+    torch.cuda.synchronize()
+    s, p4 = sc.cpu().numpy(), pos.cpu().numpy().reshape(-1, 4)
+    res = got.res
+    assert np.array_equal(res["score"], s)
+    sel = s > 0
+    assert np.array_equal(res["end_i"][sel], p4[sel, 2]) and np.array_equal(res["end_j"][sel], p4[sel, 3])
+    idx = np.random.default_rng(4).choice(b.n, 200, replace=False)
+    ts, pp = ps.subset(idx).lists()
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=False)
+    for f in ("score", "end_i", "end_j", "start_i", "start_j"):
+        assert np.array_equal(res[f][idx], getattr(want, f)), f
+
+
 def test_sw_optimistic_16bit_with_handover():
     """Pure pairs whose all-match score passes 16 bits but whose best fits run
     on the 16-bit kernel (sw_opt16_pct); one whose best reaches the 16-bit
