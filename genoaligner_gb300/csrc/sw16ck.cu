@@ -32,6 +32,11 @@
 // Recomputed values equal the forward pass's, so every decision is the one
 // the reference's stored direction bits give.  Eligibility is sw16.cu's
 // (host-side check).
+//
+// The score-only form (sw16so_kernel, at the end) runs step 1 alone, without
+// checkpoint rows, and picks the end cell by the reference's score-only rule
+// (include/genoaligner/backend/sw_kernel_impl.hip:146,158-167) instead of
+// step 2.
 #include "kernels.cuh"
 
 namespace ga {
