@@ -299,3 +299,28 @@ def test_sw_device_score_only_vs_oracle():
     s2 = sc.cpu().numpy()
     big = np.array([len(t) > 0 and len(p) > 0 and (len(t) + 1) * (len(p) + 1) > lim for t, p in zip(ts, pp)])
     assert (s2[big] == -2).all() and np.array_equal(s2[~big], want.score[~big])
+
+
+@pytest.mark.parametrize("with_cigar", [True, False])
+def test_sw_band_edge_widths_vs_oracle(with_cigar):
+    """Pattern widths at the forward bands' and tiles' edges (64-column tiles,
+    bands of 64 to 512 columns), two pairs of different widths per warp, and
+    texts of one row to several checkpoint blocks."""
+    rng = np.random.default_rng(55 + with_cigar)
+    widths = [1, 2, 31, 32, 33, 63, 64, 65, 127, 128, 129, 255, 256, 257, 511, 512, 513, 1023, 1024, 1025, 1536, 1537]
+    ts, pp = [], []
+    for w in widths:
+        for tl in (1, 65, int(rng.integers(100, 900))):
+            core = workloads.random_bases(rng, w).tobytes()
+            mut = bytearray(core)
+            for q in rng.integers(0, w, size=max(1, w // 20)):
+                mut[q] = ord("ACGT"[int(rng.integers(0, 4))])
+            t = workloads.random_bases(rng, int(rng.integers(0, 40))).tobytes() + bytes(mut)
+            ts.append(t[:tl] if tl < len(t) else t + workloads.random_bases(rng, tl - len(t)).tobytes())
+            pp.append(core)
+    # (the extension entry, limit -1: no trace-cell limit and no score-kernel shared-memory refusal)
+    want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=with_cigar, trace_cell_limit=-1,
+                           score_smem_limit=None)
+    got = sw_gpu(ts, pp, scoring=(2, -3, 3, 1), with_cigar=with_cigar, trace_cell_limit=-1)
+    assert got.status == api.Status.ok
+    assert_sw_equal(got, want, f"band edges with_cigar={with_cigar}")
