@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--pairs", type=int, default=200_000)
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=60.0,
+                    help="--impl reference: host seconds over all warm-up and timed steps")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the device's current kernel setting instead of autotuning on the batch")
     ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long", "sw_score_only"],
@@ -232,10 +234,10 @@ def run_reference(args, rank, world):
         return
     threads = os.cpu_count() or 1
     ps = workloads.sw_uneven_200k(n=args.pairs)
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    per_step = max(0.5, args.ref_seconds / max(1, args.steps + args.warmup))
     vals, samples = [], []
     for s in range(args.warmup + args.steps):
-        g, k, cells = cpu_baseline_sw(ps, per_step, threads)
+        g, k, cells, _ = cpu_baseline_sw(ps, per_step, threads)
         if s >= args.warmup:
             vals.append(g)
             samples.append((k, cells))
