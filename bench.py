@@ -327,7 +327,7 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
     for learned in ((False, True) if have_model else (False,)):
         sc = torch.empty(n, dtype=torch.int32, device=dev)
         ln = torch.empty(n, dtype=torch.int32, device=dev)
-        cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
+        cg = torch.zeros(batch.out_bytes, dtype=torch.uint8, device=dev)     # (compared whole below)
         fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
         if learned and not args.no_tune:
             chosen, trials = api.autotune_wfa(batch, 64, True, sc, ln, cg, reps=2)
@@ -356,19 +356,38 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
     return out
 
 
-def bench_wfa_long(api, workloads, torch, dev, stream, args):
+def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args):
+    """The long WFA batch at smax 2048: the plain form (one pair per warp, in
+    batch order) and the learned-bucketed form (queues by estimated distance,
+    largest first; pairs estimated at s >= 256 on whole blocks)."""
     ps = workloads.wfa_long_1k_10k()
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
-    sc = torch.empty(n, dtype=torch.int32, device=dev)
-    ln = torch.empty(n, dtype=torch.int32, device=dev)
-    cg = torch.empty(batch.out_bytes, dtype=torch.uint8, device=dev)
-    fn = lambda: api.wfa_device(batch, 2048, True, sc, ln, cg, stream=stream.cuda_stream)
-    fn()
-    ms = timed(fn, stream, 2)
-    s = sc.cpu().numpy()
-    return {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR",
-            "pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms, "unresolved": int((s < 0).sum())}
+    model = cost_model.load_default()
+    out = {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR"}
+    res = {}
+    for learned in ((False, True) if model else (False,)):
+        sc = torch.empty(n, dtype=torch.int32, device=dev)
+        ln = torch.empty(n, dtype=torch.int32, device=dev)
+        cg = torch.zeros(batch.out_bytes, dtype=torch.uint8, device=dev)     # (compared whole below)
+        fn = lambda: api.wfa_device(batch, 2048, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
+        fn()
+        ms = timed(fn, stream, 3)
+        s = sc.cpu().numpy()
+        key = "learned" if learned else "plain"
+        out[key] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms, "unresolved": int((s < 0).sum())}
+        if learned:
+            small, big, rest = api.wfa_route_stats()
+            out[key]["whole_block_pairs"] = rest[1]
+        res[key] = (s, ln.cpu().numpy(), cg.cpu().numpy())
+    # the plain form's figures stay the line's top-level figures
+    out.update({"pairs_per_s": out["plain"]["pairs_per_s"], "ms_per_step": out["plain"]["ms_per_step"],
+                "unresolved": out["plain"]["unresolved"]})
+    if "learned" in res:
+        a, b = res["plain"], res["learned"]
+        out["bit_identical"] = bool(all(np.array_equal(x, y) for x, y in zip(a, b)))
+        out["learned_over_plain"] = out["plain"]["ms_per_step"] / out["learned"]["ms_per_step"]
+    return out
 
 
 def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
@@ -472,7 +491,7 @@ def main():
         stream = torch.cuda.current_stream(dev)
         run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, False),
                "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, False),
-               "wfa_long": lambda: bench_wfa_long(api, workloads, torch, dev, stream, args),
+               "wfa_long": lambda: bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args),
                "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096),
                "sw_score_only": lambda: score_only_alone(api, workloads, torch, dev, stream, args)}[args.only]
         if rank == 0:
@@ -569,7 +588,7 @@ def main():
         extra["sw_score_only"] = bench_sw_score_only(api, torch, dev, stream, args, ps, batch, sc)
         extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, rank == 0)
         extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, rank == 0)
-        extra["wfa_long"] = bench_wfa_long(api, workloads, torch, dev, stream, args)
+        extra["wfa_long"] = bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args)
         extra["sw_long"] = bench_sw_long(api, workloads, torch, dev, stream, 4096)
 
     cpu = None

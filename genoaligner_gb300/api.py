@@ -716,7 +716,8 @@ def mlp_train_step(feat, target, lr: float) -> float:
 
 def wfa_route_stats(rounds: int = 12):
     """(lane-queue pairs, warp-queue pairs, [pairs escalated from the lane queue
-    to the warp queue, 0, ...]) of the calling thread's last learned call."""
+    to the warp queue, warp-queue pairs run on whole blocks, 0, ...]) of the
+    calling thread's last learned call."""
     out = np.zeros(2 + rounds, np.int32)
     st = load().ga_wfa_route_stats(out.ctypes.data, int(out.shape[0]))
     if st != GA_OK:

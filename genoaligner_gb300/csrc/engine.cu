@@ -407,7 +407,7 @@ static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace,
         S.item = k.take<int32_t>(n);
         S.lb = k.take<int32_t>(n);
         S.y = k.take<float>(2 * (size_t)n);
-        S.counts = k.take<int32_t>(2 * route_buckets() + 2);
+        S.counts = k.take<int32_t>(2 * route_buckets() + 4);
         S.starts = k.take<int32_t>(2 * route_buckets());
         S.big = k.take<int2>(n);
         S.small = k.take<int2>(n);
@@ -432,11 +432,12 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     if (e != cudaSuccess) return e;
     if (!learned) return launch_wfa(A, S.slots, st);
     const int NB = route_buckets();
-    if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 2), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 4), st)) != cudaSuccess) return e;
     if ((e = launch_route_model(D, smax, lane_smax, S.item, S.lb, S.y, S.counts, score, len, st)) != cudaSuccess) return e;
     if ((e = launch_route(D.n, S.item, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess) return e;
     // ctr layout: [0] warp-queue next, [1] lane-queue next, [2] escalation
-    // next, [32] escalation count
+    // next, [3] whole-block next, [32] escalation count; counts[2 NB + 2]:
+    // whole-block items (the warp queue's first ones)
     RoutedArgs R;
     R.A = A;
     R.warp_smem = S.warp_smem;
@@ -450,6 +451,8 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     R.esc_count = S.ctr + 32;
     R.esc_next = S.ctr + 2;
     R.lane_rec = S.lane_rec;
+    R.block_count = S.counts + 2 * NB + 2;
+    R.block_next = S.ctr + 3;
     return launch_routed(R, S.lane_slots, S.slots, st);
 }
 
@@ -1525,10 +1528,10 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
     if (!r.c || !out || max < 2) return GA_INVALID_ARGUMENT;
     if (r.c->dev_gen != r.gen) return GA_INVALID_ARGUMENT;
     const int NB = route_buckets();
-    std::vector<int32_t> counts(2 * NB + 2);
+    std::vector<int32_t> counts(2 * NB + 4);
     int32_t esc[32];
     if (cudaDeviceSynchronize() != cudaSuccess ||
-        cudaMemcpy(counts.data(), r.counts, sizeof(int32_t) * (2 * NB + 2), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(counts.data(), r.counts, sizeof(int32_t) * (2 * NB + 4), cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(esc, r.ctr + 32, sizeof(int32_t) * 32, cudaMemcpyDeviceToHost) != cudaSuccess) {
         cudaGetLastError();
         return GA_DEVICE_ERROR;
@@ -1537,6 +1540,7 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
     out[1] = counts[2 * NB];                  // warp queue (one pair per warp)
     int k = 2;
     if (k < max) out[k++] = esc[0];
+    if (k < max) out[k++] = counts[2 * NB + 2];   // warp-queue pairs run on whole blocks
     for (; k < max; ++k) out[k] = 0;
     return GA_OK;
 }

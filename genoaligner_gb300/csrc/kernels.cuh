@@ -74,6 +74,8 @@ struct RoutedArgs {
     int2* esc;                   // escalations from the lane queue: (pair, batch smax)
     int32_t* esc_count;
     int32_t* esc_next;
+    const int32_t* block_count;  // the first *block_count warp-queue items run on whole blocks (null: none)
+    int32_t* block_next;
     uint16_t* lane_rec;          // lane kernel: per warp slot, lane_rec_slot() walk records (trace only)
     int32_t warp_smem;           // warp kernel: shared-memory ints per warp
 };

@@ -15,6 +15,10 @@ constexpr int LANE_MAXLEN = 256;
 // Buckets: keys 0 .. ROUTE_BUCKETS-1 are the warp queue by bit length of the
 // predicted distance bound, ROUTE_BUCKETS + s the lane queue with first smax s.
 constexpr int ROUTE_BUCKETS = 32;
+// Warp-queue items whose bucket key (bit length of the estimated distance) is
+// at least BLOCK_BITS -- estimated s >= 256 -- run first, each on a whole
+// block of the warp kernel (128 threads over the diagonals of one pair).
+constexpr int BLOCK_BITS = 9;
 
 __device__ __forceinline__ int bitlen(unsigned x) { return 32 - __clz(x); }
 

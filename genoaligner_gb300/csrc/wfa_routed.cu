@@ -50,7 +50,8 @@ constexpr int LANE_HAND_DIV = 16;
 template <int G>
 __device__ __forceinline__ void gsync(unsigned gmask)
 {
-    if (G == 32) __syncwarp();
+    if (G == 128) __syncthreads();
+    else if (G == 32) __syncwarp();
     else __syncwarp(gmask);
 }
 
@@ -416,17 +417,36 @@ template <bool TRACE>
 __global__ void __launch_bounds__(128) wfa_routed_kernel(RoutedArgs R)
 {
     extern __shared__ __align__(16) int32_t rsmem[];
+    __shared__ int s_q;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int32_t* wsm = rsmem + wib * R.warp_smem;
     const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     int32_t* stk = TRACE ? R.A.stack + slot * R.A.stack_slot : nullptr;
+    // the warp queue's largest items first, each on the whole block: its 128
+    // threads split the diagonals of every step (one block barrier a step),
+    // in warp 0's shared memory and stack
+    const int nblock = R.block_count ? *R.block_count : 0;
+    if (nblock > 0) {
+        int32_t* bstk = TRACE ? R.A.stack + (int64_t)blockIdx.x * (blockDim.x >> 5) * R.A.stack_slot : nullptr;
+        for (;;) {
+            if (threadIdx.x == 0) s_q = atomicAdd(R.block_next, 1);
+            __syncthreads();
+            const int q = s_q;
+            __syncthreads();
+            if (q >= nblock) break;
+            const int2 it = R.big[q];
+            run_item<TRACE, 128>(R, it, rsmem, rsmem + 2 * it.y + 3, bstk, threadIdx.x, FULL);
+            __syncthreads();
+        }
+    }
     for (int list = 0; list < 2; ++list) {
         const int2* items = list ? R.esc : R.big;
         const int cnt = list ? *R.esc_count : *R.big_count;
         int32_t* next = list ? R.esc_next : R.big_next;
+        const int first = list ? 0 : nblock;            // (items before it ran on blocks)
         for (;;) {
             int q = 0;
-            if (lane == 0) q = atomicAdd(next, 1);
+            if (lane == 0) q = atomicAdd(next, 1) + first;
             q = __shfl_sync(FULL, q, 0);
             if (q >= cnt) break;
             __syncwarp();
@@ -451,6 +471,7 @@ __global__ void route_scan_kernel(int32_t* counts, int32_t* starts)
         for (int b = ROUTE_BUCKETS - 1; b >= 0; --b) {
             starts[q * ROUTE_BUCKETS + b] = acc;
             acc += counts[q * ROUTE_BUCKETS + b];
+            if (q == 0 && b == BLOCK_BITS) counts[2 * ROUTE_BUCKETS + 2] = acc;   // whole-block items
         }
         counts[2 * ROUTE_BUCKETS + q] = acc;
     }

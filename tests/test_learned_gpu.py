@@ -130,3 +130,25 @@ def test_trained_model_beats_lower_bound_rule():
     assert ev["mae_distance"] < 0.5 * ev["mae_distance_lower_bound_only"], ev
     assert ev["escalation_rate"] < ev["escalation_rate_lower_bound_only"], ev
     assert ev["escalation_rate"] < 0.05, ev
+
+
+def test_learned_whole_block_items_match_oracle():
+    """Long, divergent pairs at smax 2048: the warp queue's items estimated at
+    s >= 256 run on whole blocks of the warp kernel; scores and CIGARs equal
+    the oracle's and the plain path's."""
+    assert cost_model.load_default()
+    ps = workloads.wfa_long_1k_10k(n=48, seed=33)
+    pats, txts = ps.lists()
+    want = oracle.wfa_batch(pats, txts, smax=2048, with_cigar=True, max_smax=4096)
+    assert (want.score >= 256).sum() >= 5
+    got = api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=2048,
+                                 with_cigar=True, max_smax=4096, learned=True)
+    assert got.status == api.Status.ok
+    assert np.array_equal(got.res["score"], want.score)
+    assert all(got.cigar(i) == want.cigars[i] for i in range(ps.n))
+    assert np.array_equal(got.res["rescore_ok"].astype(bool), want.rescore_ok)
+    small, big, rest = api.wfa_route_stats()
+    assert rest[1] >= 3, rest                              # pairs that ran on whole blocks
+    plain = api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=2048,
+                                   with_cigar=True, max_smax=4096, learned=False)
+    assert np.array_equal(plain.res["score"], got.res["score"])
