@@ -209,27 +209,41 @@ int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int6
     auto run = [&](const char** e) {
         return ga_sw_device(batch, scoring, 1, trace_cell_limit, out_score, out_pos, out_len, out_cigar, nullptr, e);
     };
+    // coordinate search from the built-in SW setting (the WFA field kept),
+    // repeated once when the first pass moved: a field swept early (the
+    // variant) is then judged again at the later fields' best values
     Search S;
     S.best = tune_current();
-    int32_t rc = sweep(S, &ga_tune::sw_pack16, {1, 0}, reps, run, err);
-    if (rc == GA_OK && S.best.sw_pack16) rc = sweep(S, &ga_tune::sw_window, {2, 4}, reps, run, err);
-    if (rc == GA_OK && max_cells > ((int64_t)1 << 20)) {
-        std::vector<int> vals;
-        for (int v = 20; v <= 28; v += 2)
-            if (max_cells > ((int64_t)1 << v) || v == 20) vals.push_back(v);
-        vals.push_back(30);                                   // no pair in the long shape
-        rc = sweep(S, &ga_tune::sw_long_log2, vals, reps, run, err);
+    {
+        const ga_tune d = builtin();
+        S.best.sw_pack16 = d.sw_pack16; S.best.sw_window = d.sw_window; S.best.sw_long_log2 = d.sw_long_log2;
+        S.best.sw_coop_log2 = d.sw_coop_log2; S.best.sw_opt16_pct = d.sw_opt16_pct;
     }
-    if (rc == GA_OK && max_cells > ((int64_t)1 << 24)) {
-        std::vector<int> vals;
-        for (int v = 24; v <= 30; v += 3)
-            if (max_cells > ((int64_t)1 << v)) vals.push_back(v);
-        vals.push_back(40);                                   // every pair on one warp
-        rc = sweep(S, &ga_tune::sw_coop_log2, vals, reps, run, err);
-    }
-    if (rc == GA_OK && S.best.sw_pack16 && max_min_len > 0 &&
-        (int64_t)scoring.match * max_min_len + BIAS16 + scoring.gap_open >= 32000)
-        rc = sweep(S, &ga_tune::sw_opt16_pct, {100, 85, 75, 65}, reps, run, err);
+    auto pass = [&]() -> int32_t {
+        int32_t rc = sweep(S, &ga_tune::sw_pack16, {1, 0}, reps, run, err);
+        if (rc == GA_OK && S.best.sw_pack16) rc = sweep(S, &ga_tune::sw_window, {2, 4}, reps, run, err);
+        if (rc == GA_OK && max_cells > ((int64_t)1 << 20)) {
+            std::vector<int> vals;
+            for (int v = 20; v <= 28; v += 2)
+                if (max_cells > ((int64_t)1 << v) || v == 20) vals.push_back(v);
+            vals.push_back(30);                                   // no pair in the long shape
+            rc = sweep(S, &ga_tune::sw_long_log2, vals, reps, run, err);
+        }
+        if (rc == GA_OK && max_cells > ((int64_t)1 << 24)) {
+            std::vector<int> vals;
+            for (int v = 24; v <= 30; v += 3)
+                if (max_cells > ((int64_t)1 << v)) vals.push_back(v);
+            vals.push_back(40);                                   // every pair on one warp
+            rc = sweep(S, &ga_tune::sw_coop_log2, vals, reps, run, err);
+        }
+        if (rc == GA_OK && S.best.sw_pack16 && max_min_len > 0 &&
+            (int64_t)scoring.match * max_min_len + BIAS16 + scoring.gap_open >= 32000)
+            rc = sweep(S, &ga_tune::sw_opt16_pct, {100, 85, 75, 65}, reps, run, err);
+        return rc;
+    };
+    const ga_tune start = S.best;
+    int32_t rc = pass();
+    if (rc == GA_OK && !same(start, S.best)) rc = pass();
     if (rc != GA_OK) return rc;
     store(dev, S.best);
     report(S, chosen, trials, max_trials, n_trials);
