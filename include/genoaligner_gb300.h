@@ -205,7 +205,10 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max);
 
 /* SW over a device batch, score + end cell + start cell + CIGAR.
  * out_pos[4*i .. 4*i+3] = start_i, start_j, end_i, end_j.  Pairs above
- * trace_cell_limit cells (< 0: no limit) get out_score = -2 (too large). */
+ * trace_cell_limit cells (< 0: no limit) get out_score = -2 (too large).
+ * trace = 0 is the score-only form: out_len, out_cigar and batch->out_off
+ * may be null, and out_pos holds -1, -1 and the end cell of the reference's
+ * score-only kernel (-1, -1 for score 0). */
 int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_t trace,
                      int64_t trace_cell_limit, int32_t* out_score, int32_t* out_pos,
                      int32_t* out_len, char* out_cigar, void* stream, const char** err);
