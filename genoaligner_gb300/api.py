@@ -621,8 +621,11 @@ def align_sw_batch_packed(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, 
     reqs = _reqs if _reqs is not None else make_sw_requests(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring,
                                                             with_cigar)
     res = _res if _res is not None else np.zeros(n, SWRES_DT)
-    nbytes = int(L.ga_align_sw_cigar_bytes(reqs.ctypes.data, n))
-    cig = _cig if _cig is not None and _cig.shape[0] >= nbytes else np.empty(max(nbytes, 1), np.uint8)
+    if _cig is not None:                      # a caller's buffer: the library checks its size
+        cig, nbytes = _cig, int(_cig.shape[0])
+    else:
+        nbytes = int(L.ga_align_sw_cigar_bytes(reqs.ctypes.data, n))
+        cig = np.empty(max(nbytes, 1), np.uint8)
     info = BatchInfo()
     if trace_cell_limit:
         o = _opts(trace_cell_limit=trace_cell_limit)

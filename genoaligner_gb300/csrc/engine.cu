@@ -1398,7 +1398,11 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
     int64_t limit = GA_SW_MAX_TRACE_CELLS;
     if (opt && opt->trace_cell_limit != 0) limit = opt->trace_cell_limit;
     bool any_cigar = false;
-    for (int32_t i = 0; i < n; ++i) any_cigar |= reqs[i].with_cigar != 0;
+    int64_t cig_need = 0;                        // ga_align_sw_cigar_bytes, in the same pass
+    for (int32_t i = 0; i < n; ++i) {
+        any_cigar |= reqs[i].with_cigar != 0;
+        cig_need += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
+    }
     const char* err = nullptr;
     std::atomic<int32_t> resolved{0};
     auto fin = [&](int64_t lo, int64_t hi, const SwView& v) {
@@ -1443,7 +1447,7 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
         resolved.fetch_add(res);
     };
     int32_t st;
-    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < ga_align_sw_cigar_bytes(reqs, n))) {
+    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < cig_need)) {
         st = sw_check(reqs, n, &err);
         if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
     } else {
