@@ -63,7 +63,6 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=200_000)
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0,
                     help="--impl reference: host seconds over all warm-up and timed steps")
     ap.add_argument("--no-tune", action="store_true",
@@ -187,45 +186,105 @@ def sw_cells(ps):
     return int((ps.a_len.astype(np.int64) * ps.b_len.astype(np.int64)).sum())
 
 
+# ------------------------------------------------------------------ checks --
+# Comparisons of GPU outputs with the oracle's (the reference's CPU path
+# restated): every field, every pair.
+def wfa_equal_packed(got, want):
+    """A host-entry WFA result (api.PackedResult) against oracle.WfaBatch."""
+    r = got.res
+    if got.status.name != want.status:
+        return False
+    for f in ("rescore_ok", "wellformed_ok", "resolved"):
+        if not np.array_equal(r[f].astype(bool), getattr(want, f)):
+            return False
+    if not np.array_equal(r["score"], want.score):
+        return False
+    buf = got.cigar_buf
+    return all(buf[o:o + n].tobytes() == c
+               for o, n, c in zip(r["cigar_offset"].tolist(), r["cigar_len"].tolist(), want.cigars))
+
+
+def sw_equal_packed(got, want):
+    """A host-entry SW result against oracle.SwBatch."""
+    r = got.res
+    if got.status.name != want.status:
+        return False
+    for f in ("score", "start_i", "start_j", "end_i", "end_j"):
+        if not np.array_equal(r[f], getattr(want, f)):
+            return False
+    for f in ("resolved", "rescore_ok", "wellformed_ok", "too_large"):
+        if not np.array_equal(r[f].astype(bool), getattr(want, f)):
+            return False
+    buf = got.cigar_buf
+    return all(buf[o:o + n].tobytes() == c
+               for o, n, c in zip(r["cigar_offset"].tolist(), r["cigar_len"].tolist(), want.cigars))
+
+
+def slot_ends(batch):
+    """End of every pair's CIGAR slot in a device batch's output buffer."""
+    return (batch.out_off.cpu().numpy() + batch.a_len.cpu().numpy().astype(np.int64) +
+            batch.b_len.cpu().numpy().astype(np.int64))
+
+
+def wfa_equal_device(out, want):
+    """Device-entry WFA outputs (score, CIGAR length, CIGAR slots, slot ends)."""
+    sc, ln, cg, ends = out
+    if not np.array_equal(sc, want.score):
+        return False
+    lens = np.fromiter((len(c) for c in want.cigars), np.int64, count=len(want.cigars))
+    if not np.array_equal(ln.astype(np.int64), lens):
+        return False
+    return all(cg[e - n:e].tobytes() == c for e, n, c in zip(ends.tolist(), lens.tolist(), want.cigars))
+
+
+def sw_equal_device(out, want):
+    """Device-entry SW outputs (score, positions, CIGAR length, slots, slot ends)."""
+    sc, pos, ln, cg, ends = out
+    pos = pos.reshape(-1, 4)
+    if not np.array_equal(sc, want.score):
+        return False
+    for k, f in enumerate(("start_i", "start_j", "end_i", "end_j")):
+        if not np.array_equal(pos[:, k], getattr(want, f)):
+            return False
+    lens = np.fromiter((len(c) for c in want.cigars), np.int64, count=len(want.cigars))
+    if not np.array_equal(ln.astype(np.int64), lens):
+        return False
+    return all(cg[e - n:e].tobytes() == c for e, n, c in zip(ends.tolist(), lens.tolist(), want.cigars))
+
+
+# ------------------------------------------------------------ CPU baseline --
+def one_core_sample(run, n, seconds, first=64, cap=1 << 20):
+    """Units per second of `run(idx)` (which returns (units, C seconds)) on
+    one thread, over pairs of a fixed random permutation taken in growing
+    chunks until ~`seconds` of C time."""
+    order = np.random.default_rng(777).permutation(n)
+    units, used, k, chunk = 0, 0.0, 0, first
+    while used < seconds and k < n:
+        u, t = run(order[k:k + chunk])
+        units += u
+        used += t
+        k += chunk
+        chunk = min(chunk * 2, cap)
+    return units / used if used > 0 else None, k, used
+
+
 def cpu_baseline_sw(ps, seconds, threads):
-    """The oracle (a restatement of the reference's CPU path) on a bounded
-    sample: pairs taken from a fixed random permutation until ~`seconds`.
-    Also returns the first chunk's indices and results, against which the
-    GPU run's outputs are checked."""
+    """The oracle on a bounded sample of the SW batch (pairs from a fixed
+    random permutation until ~`seconds` of C time): GCUPS, pairs, cells,
+    C seconds."""
     import oracle
     order = np.random.default_rng(123).permutation(ps.n)
     done_cells, t_used, k, chunk = 0, 0.0, 0, 256
-    first = None
     while t_used < seconds and k < ps.n:
         idx = order[k:k + chunk]
         sub = ps.subset(idx)
         ts, pp = sub.lists()
-        t0 = time.perf_counter()
         got = oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=threads)
-        t_used += time.perf_counter() - t0
-        if first is None:
-            first = (idx, got)
+        t_used += got.seconds
         done_cells += sw_cells(sub)
         k += chunk
         chunk = min(chunk * 2, 8192)
-    return done_cells / t_used / 1e9, k, done_cells, first
-
-
-def cpu_baseline_wfa(ps, seconds, threads, smax=64):
-    """The oracle on a bounded sample of a WFA batch: pairs/s."""
-    import oracle
-    order = np.random.default_rng(321).permutation(ps.n)
-    done, t_used, k, chunk = 0, 0.0, 0, 2048
-    while t_used < seconds and k < ps.n:
-        sub = ps.subset(order[k:k + chunk])
-        pats, txts = sub.lists()
-        t0 = time.perf_counter()
-        oracle.wfa_batch(pats, txts, smax=smax, with_cigar=True, threads=threads, max_smax=max(smax, 511))
-        t_used += time.perf_counter() - t0
-        done += sub.n
-        k += chunk
-        chunk = min(chunk * 2, 65536)
-    return done / t_used, done
+    return done_cells / t_used / 1e9, k, done_cells, t_used
 
 
 def run_reference(args, rank, world):
@@ -237,20 +296,24 @@ def run_reference(args, rank, world):
     per_step = max(0.5, args.ref_seconds / max(1, args.steps + args.warmup))
     vals, samples = [], []
     for s in range(args.warmup + args.steps):
-        g, k, cells, _ = cpu_baseline_sw(ps, per_step, threads)
+        g, k, cells, used = cpu_baseline_sw(ps, per_step, threads)
         if s >= args.warmup:
             vals.append(g)
-            samples.append((k, cells))
+            samples.append((k, cells, used))
     v = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "GCUPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sw_cells(ps) / (v * 1e9) * 1e3,
+        "ms_per_step_is": "the whole batch's cells at the measured rate (each step times a sample)",
+        "sample_seconds_per_step": [round(x[2], 3) for x in samples],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, seed 2)",
         "config": {"workload": SW_WORKLOAD, "pairs": ps.n, "cells": sw_cells(ps)},
         "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
-                         "sample": f"per step: pairs from a fixed random permutation until ~{per_step:.0f} s of "
-                                   f"CPU time (last step {samples[-1][0]} pairs, {samples[-1][1] / 1e9:.2f} Gcells)"},
+                         "build": "oracle/ga_oracle.c, gcc -O3 (no -march: the same code on x86 and Arm)",
+                         "sample": f"per step: pairs from a fixed random permutation until ~{per_step:.1f} s of "
+                                   f"C time (last step {samples[-1][0]} pairs, {samples[-1][1] / 1e9:.2f} Gcells, "
+                                   f"{samples[-1][2]:.2f} s)"},
         "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -277,7 +340,7 @@ def timed(fn, stream, steps, flush=None):
     return statistics.median(ts)
 
 
-def bench_wfa_150(api, workloads, torch, dev, stream, args, cpu):
+def bench_wfa_150(api, workloads, torch, dev, stream, args, keep):
     ps = workloads.wfa_150bp_2pct()
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
@@ -299,98 +362,176 @@ def bench_wfa_150(api, workloads, torch, dev, stream, args, cpu):
     t = []
     for _ in range(extra_steps(args)):
         t0 = time.perf_counter()
-        call()
+        r = call()
         t.append(time.perf_counter() - t0)
     e2e_ms = statistics.median(t) * 1e3
-    out = {"workload": "wfa_150bp_2pct: 10,000 pairs, 150 bp, 2% (sub/ins/del equal), smax 64, CIGAR",
-           "pairs_per_s": n / (dev_ms * 1e-3), "ms_per_step": dev_ms,
-           "e2e_pairs_per_s": n / (e2e_ms * 1e-3), "e2e_ms_per_step": e2e_ms,
-           "l2": "256 MB buffer written between steps"}
-    if cpu:
-        pps, done = cpu_baseline_wfa(ps, 4.0, os.cpu_count() or 1)
-        out.update({"cpu_baseline_pairs_per_s": pps, "cpu_cores": os.cpu_count(), "cpu_kind": "port",
-                    "cpu_sample": f"{done} pairs"})
+    keep["wfa_150bp"] = {"ps": ps, "device": (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy(), slot_ends(batch)),
+                         "e2e": r}
+    return {"workload": "wfa_150bp_2pct: 10,000 pairs, 150 bp, 2% (sub/ins/del equal), smax 64, CIGAR",
+            "pairs_per_s": n / (dev_ms * 1e-3), "ms_per_step": dev_ms,
+            "e2e_pairs_per_s": n / (e2e_ms * 1e-3), "e2e_ms_per_step": e2e_ms,
+            "l2": "256 MB buffer written between steps"}
+
+
+ROUTE_BUCKETS = 32          # genoaligner_gb300/csrc/route.cuh
+LANE_MAXLEN = 256
+
+
+def route_report(items, score, smax, lane_smax, classes, lane_ok):
+    """How the router's queue items compare with the ones the exact distance
+    selects under the same rule (first smax = ceil(1.25 d + 2), lane queue iff
+    that is <= lane_smax for an eligible pair, warp-queue bucket = its bit
+    length; a pair unresolved at smax belongs in the warp queue at the top
+    bucket, or is proven unresolved by the bound).  Per class: pairs in each
+    queue, queue mispredictions (queue differs from the exact one), lane-queue
+    pairs first run below their distance (they escalate), warp-queue pairs
+    whose bucket differs from the exact one."""
+    d = score.astype(np.int64)
+    unres = d < 0
+    s_star = np.where(unres, smax, np.minimum(smax, np.ceil(1.25 * d + 2))).astype(np.int64)
+    lane_star = (~unres) & lane_ok & (s_star <= lane_smax)
+    bound = items < 0
+    key = items & 0xFF
+    first = items >> 8
+    lane = (~bound) & (key >= ROUTE_BUCKETS)
+    warp = (~bound) & (key < ROUTE_BUCKETS)
+    bitlen = lambda x: np.floor(np.log2(np.maximum(x, 1))).astype(np.int64) + 1
+    bucket_star = np.minimum(bitlen(s_star), ROUTE_BUCKETS - 1)
+    out = {}
+    for name, sel in classes.items():
+        nl, nw = int((lane & sel).sum()), int((warp & sel).sum())
+        qmis = int(((lane != lane_star) & ~bound & sel).sum())
+        esc = int((lane & sel & (unres | (first < d))).sum())
+        boff = int((warp & sel & ~unres & (key != bucket_star)).sum())
+        out[name] = {"pairs": int(sel.sum()), "lane_queue": nl, "warp_queue": nw,
+                     "unresolved_by_bound": int((bound & sel).sum()),
+                     "queue_mispredicted_rate": qmis / max(1, int(sel.sum())),
+                     "lane_escalation_rate": esc / max(1, nl),
+                     "warp_bucket_mispredicted_rate": boff / max(1, nw)}
     return out
 
 
-def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, cpu):
-    """1,000,000 mixed-divergence pairs: plain fixed smax 64 against the
-    learned-bucketed form, both through ga_wfa_device_ex, bit-exact check."""
-    ps = workloads.wfa_mixed()
-    n = ps.n
-    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
-    have_model = cost_model.load_default()
-    out = {"workload": "wfa_mixed_1m: 1,000,000 pairs, 150-250 bp, error 70% U[0,2%] / 25% U[2,10%] / "
-                       "5% U[10,30%], smax 64, CIGAR", "model_loaded": have_model}
-    scores = {}
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for learned in ((False, True) if have_model else (False,)):
+def wfa_arms(api, torch, dev, stream, batch, n, smax, steps, flush, tune_first, out):
+    """The plain fixed-smax form, the learned-bucketed form and the same queues
+    keyed by the lower bound alone, through ga_wfa_device_ex; device time per
+    call, route items of the routed arms, bit-identity to the plain form."""
+    res = {}
+    for arm, learned in (("plain", 0), ("learned", 1), ("bound_only", 2)):
         sc = torch.empty(n, dtype=torch.int32, device=dev)
         ln = torch.empty(n, dtype=torch.int32, device=dev)
         cg = torch.zeros(batch.out_bytes, dtype=torch.uint8, device=dev)     # (compared whole below)
-        fn = lambda: api.wfa_device(batch, 64, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
-        if learned and not args.no_tune:
-            chosen, trials = api.autotune_wfa(batch, 64, True, sc, ln, cg, reps=2)
+        fn = lambda: api.wfa_device(batch, smax, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
+        if arm == "learned" and tune_first:
+            chosen, trials = api.autotune_wfa(batch, smax, True, sc, ln, cg, reps=2)
             out["tune"] = {"chosen": chosen, "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials]}
         for _ in range(3):
             fn()
-        ms = timed(fn, stream, extra_steps(args), flush)
-        key = "learned" if learned else "plain"
-        out[key] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms}
-        scores[key] = (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy())
+        ms = timed(fn, stream, steps, flush)
+        out[arm] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms}
+        res[arm] = (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy())
         if learned:
-            small, big, esc = api.wfa_route_stats()
-            resolved = int((scores[key][0] >= 0).sum())
-            out[key].update({"lane_queue_pairs": small, "warp_queue_pairs": big, "escalated": int(esc[0]),
-                             "escalation_rate": esc[0] / max(1, small),
-                             "unresolved_by_bound_or_search": n - resolved})
-    if "learned" in scores:
-        a, b = scores["plain"], scores["learned"]
-        out["bit_identical"] = bool(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and
-                                    np.array_equal(a[2], b[2]))
-        out["learned_over_plain"] = out["learned"]["pairs_per_s"] / out["plain"]["pairs_per_s"]
-    if cpu:
-        pps, done = cpu_baseline_wfa(ps, 4.0, os.cpu_count() or 1)
-        out.update({"cpu_baseline_pairs_per_s": pps, "cpu_cores": os.cpu_count(), "cpu_kind": "port",
-                    "cpu_sample": f"{done} pairs"})
+            fn()
+            torch.cuda.synchronize()
+            small, big, rest = api.wfa_route_stats()
+            out[arm].update({"lane_queue_pairs": small, "warp_queue_pairs": big, "escalated": rest[0],
+                             "escalation_rate": rest[0] / max(1, small), "whole_block_pairs": rest[1],
+                             "unresolved_by_bound_or_search": int((res[arm][0] < 0).sum())})
+            out[arm]["_items"] = api.wfa_route_items(n)
+            out[arm]["bit_identical_to_plain"] = bool(all(np.array_equal(x, y) for x, y in zip(res["plain"], res[arm])))
+    for arm in ("learned", "bound_only"):
+        out[arm + "_over_plain"] = out["plain"]["ms_per_step"] / out[arm]["ms_per_step"]
+    return res["plain"]
+
+
+def wfa_e2e(api, ps, smax, learned, steps):
+    """The same batch through the public host entry (ga_align_batch_ex: staging,
+    copies, kernels, result checks on the device, results and CIGAR strings on
+    the host): median wall ms, bytes each way, the last result."""
+    reqs = api.make_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax, True)
+    res = np.zeros(ps.n, api.RES_DT)
+    cig = np.empty(int(api.load().ga_align_cigar_bytes(reqs.ctypes.data, ps.n)), np.uint8)
+    call = lambda: api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=smax,
+                                          max_smax=max(smax, 511), learned=learned, _reqs=reqs, _res=res, _cig=cig)
+    for _ in range(2):
+        call()
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r = call()
+        t.append(time.perf_counter() - t0)
+    h2d, d2h = api.last_transfer_bytes()
+    return statistics.median(t) * 1e3, h2d, d2h, r
+
+
+def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep):
+    """1,000,000 mixed-divergence pairs: plain fixed smax 64, the
+    learned-bucketed form and the lower-bound-only queues, bit-exact check,
+    misprediction rates per divergence class, end to end (learned form)."""
+    ps = workloads.wfa_mixed()
+    n = ps.n
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
+    out = {"workload": "wfa_mixed_1m: 1,000,000 pairs, 150-250 bp, error 70% U[0,2%] / 25% U[2,10%] / "
+                       "5% U[10,30%], smax 64, CIGAR", "model_loaded": cost_model.load_default()}
+    if not out["model_loaded"]:
+        return out
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    plain = wfa_arms(api, torch, dev, stream, batch, n, 64, extra_steps(args), flush, not args.no_tune, out)
+    rate = ps.meta["rate"]
+    classes = {"all": np.ones(n, bool), "low (<2%)": rate < 0.02, "mid (2-10%)": (rate >= 0.02) & (rate < 0.10),
+               "high (>=10%)": rate >= 0.10}
+    lane_ok = (ps.a_len <= LANE_MAXLEN) & (ps.b_len <= LANE_MAXLEN)      # every pair here is pure A/C/G/T
+    lane_smax = api.tune_get()["wfa_lane_smax"]
+    for arm in ("learned", "bound_only"):
+        out[arm]["misprediction"] = route_report(out[arm].pop("_items"), plain[0], 64, lane_smax, classes, lane_ok)
+    e2e_ms, h2d, d2h, r = wfa_e2e(api, ps, 64, True, extra_steps(args))
+    out["e2e_learned"] = {"pairs_per_s": n / (e2e_ms * 1e-3), "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                          "d2h_bytes_per_step": d2h, "entry": "ga_align_batch_ex (learned = 1)"}
+    keep["wfa_mixed_1m"] = {"ps": ps, "device": plain + (slot_ends(batch),), "e2e": r}
     return out
 
 
-def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args):
+def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep):
     """The long WFA batch at smax 2048: the plain form (one pair per warp, in
-    batch order) and the learned-bucketed form (queues by estimated distance,
-    largest first; pairs estimated at s >= 256 on whole blocks)."""
+    batch order), the learned-bucketed form (queues by estimated distance,
+    largest first; pairs estimated at s >= 256 on whole blocks) and the same
+    queues keyed by the lower bound alone."""
     ps = workloads.wfa_long_1k_10k()
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
-    model = cost_model.load_default()
-    out = {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR"}
-    res = {}
-    for learned in ((False, True) if model else (False,)):
-        sc = torch.empty(n, dtype=torch.int32, device=dev)
-        ln = torch.empty(n, dtype=torch.int32, device=dev)
-        cg = torch.zeros(batch.out_bytes, dtype=torch.uint8, device=dev)     # (compared whole below)
-        fn = lambda: api.wfa_device(batch, 2048, True, sc, ln, cg, stream=stream.cuda_stream, learned=learned)
-        fn()
-        ms = timed(fn, stream, 3)
-        s = sc.cpu().numpy()
-        key = "learned" if learned else "plain"
-        out[key] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms, "unresolved": int((s < 0).sum())}
-        if learned:
-            small, big, rest = api.wfa_route_stats()
-            out[key]["whole_block_pairs"] = rest[1]
-        res[key] = (s, ln.cpu().numpy(), cg.cpu().numpy())
-    # the plain form's figures stay the line's top-level figures
+    out = {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR",
+           "model_loaded": cost_model.load_default()}
+    if not out["model_loaded"]:
+        return out
+    plain = wfa_arms(api, torch, dev, stream, batch, n, 2048, 3, None, False, out)
+    lane_ok = np.zeros(n, bool)                    # 1-10 kb: never the lane queue
+    for arm in ("learned", "bound_only"):
+        items = out[arm].pop("_items")
+        rep = route_report(items, plain[0], 2048, 0, {"all": np.ones(n, bool)}, lane_ok)
+        d = plain[0].astype(np.int64)
+        est_block = (items >= 0) & ((items & 0xFF) < ROUTE_BUCKETS) & ((items & 0xFF) >= 9)
+        exact_block = (d < 0) | (np.ceil(1.25 * d + 2) >= 256)
+        rep["all"]["whole_block_mispredicted_rate"] = float((est_block != exact_block).mean())
+        out[arm]["misprediction"] = rep
     out.update({"pairs_per_s": out["plain"]["pairs_per_s"], "ms_per_step": out["plain"]["ms_per_step"],
-                "unresolved": out["plain"]["unresolved"]})
-    if "learned" in res:
-        a, b = res["plain"], res["learned"]
-        out["bit_identical"] = bool(all(np.array_equal(x, y) for x, y in zip(a, b)))
-        out["learned_over_plain"] = out["plain"]["ms_per_step"] / out["learned"]["ms_per_step"]
+                "unresolved": int((plain[0] < 0).sum())})
+    out["learned_over_plain"] = out["plain"]["ms_per_step"] / out["learned"]["ms_per_step"]
+    e2e_ms, h2d, d2h, r = wfa_e2e(api, ps, 2048, True, 3)
+    out["e2e_learned"] = {"pairs_per_s": n / (e2e_ms * 1e-3), "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                          "d2h_bytes_per_step": d2h, "entry": "ga_align_batch_ex (max_smax 2048, learned = 1)"}
+    keep["wfa_long"] = {"ps": ps, "device": plain + (slot_ends(batch),), "e2e": r}
     return out
 
 
-def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
+def sw_long_subset(full):
+    """The stratified subset of the long SW batch the CPU leg checks: its 64
+    largest pairs and 64 more drawn at random."""
+    cells = full.a_len.astype(np.int64) * full.b_len.astype(np.int64)
+    order = np.argsort(-cells, kind="stable")
+    rng = np.random.default_rng(55)
+    return np.concatenate([order[:64], rng.choice(order[64:], size=64, replace=False)])
+
+
+def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep):
     """The long SW batch (2-30 kb queries, 0-5 kb flanks), or its first n_pairs."""
     ps = workloads.sw_long_4k(n=n_pairs)
     cells = sw_cells(ps)
@@ -411,6 +552,11 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs):
     fn()
     ms = timed(fn, stream, 1)
     out = sc.cpu().numpy().copy(), ln.cpu().numpy().copy()
+    if n_pairs == 4096:
+        idx = sw_long_subset(ps)
+        ends = slot_ends(batch)[idx]
+        keep["sw_long"] = {"ps": ps.subset(idx), "device": (out[0][idx], pos.cpu().numpy().reshape(-1, 4)[idx],
+                                                             out[1][idx], cg.cpu().numpy(), ends)}
     api.tune_set(**dict(saved, sw_pack16=0, sw_coop_log2=40))
     fn()
     ms_plain = timed(fn, stream, 1)
@@ -458,6 +604,99 @@ def bench_sw_score_only(api, torch, dev, stream, args, ps, batch, trace_scores):
             "scores_equal_traceback_run": same}
 
 
+def cpu_and_parity(keep, ps_sw, sw_e2e, sw_dev_scores, threads):
+    """The CPU oracle on every workload, which is both the CPU baseline and the
+    full-size parity check of this run's GPU outputs.  All host threads over
+    the whole batch (the long SW batch: its stratified 128-pair subset, on as
+    many threads as host memory allows), timed on the C calls alone; one
+    thread on a bounded sample of each; edit_distance_cpu on a sample of the
+    mixed batch.  Returns (cpu figures, parity booleans)."""
+    import oracle
+    cpu, parity = {}, {}
+
+    def wfa_leg(key, smax, unit_seconds):
+        k = keep.get(key)
+        if not k:
+            return
+        ps = k["ps"]
+        pats, txts = ps.lists()
+        want = oracle.wfa_batch(pats, txts, smax=smax, with_cigar=True, threads=threads, max_smax=max(smax, 511))
+        parity[key] = {"device_plain": wfa_equal_device(k["device"], want),
+                       "e2e": wfa_equal_packed(k["e2e"], want), "pairs": ps.n}
+
+        def run(idx):
+            sub = ps.subset(idx)
+            a, b = sub.lists()
+            g = oracle.wfa_batch(a, b, smax=smax, with_cigar=True, threads=1, max_smax=max(smax, 511))
+            return sub.n, g.seconds
+        one, k1, t1 = one_core_sample(run, ps.n, unit_seconds, first=8 if smax > 511 else 256)
+        cpu[key] = {"unit": "pairs/s", "all_cores": ps.n / want.seconds, "all_cores_threads": threads,
+                    "all_cores_sample": f"the whole batch ({ps.n} pairs), {want.seconds:.2f} s",
+                    "one_core": one, "one_core_sample": f"{k1} pairs, {t1:.2f} s"}
+
+    wfa_leg("wfa_150bp", 64, 2.0)
+    wfa_leg("wfa_long", 2048, 3.0)
+    wfa_leg("wfa_mixed_1m", 64, 2.0)
+
+    # edit_distance_cpu (src/reference/edit_distance_cpu.hpp) for scale, on
+    # 20,000 pairs of the mixed batch
+    if "wfa_mixed_1m" in keep:
+        sub = keep["wfa_mixed_1m"]["ps"].subset(np.arange(20000))
+        a, b = sub.lists()
+        d1, t1 = oracle.edit_distance(a, b, threads=1, timing=True)
+        dn, tn = oracle.edit_distance(a, b, threads=threads, timing=True)
+        cpu["edit_distance_cpu"] = {"unit": "pairs/s", "one_core": sub.n / t1, "all_cores": sub.n / tn,
+                                    "all_cores_threads": threads, "sample": "the mixed batch's first 20,000 pairs",
+                                    "agrees_with_wfa_scores_within_smax": bool(np.array_equal(
+                                        np.where(dn <= 64, dn, -1), keep["wfa_mixed_1m"]["device"][0][:20000]))}
+
+    # the uneven SW batch, whole
+    ts, pp = ps_sw.lists()
+    want = oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=threads)
+    cells = sw_cells(ps_sw)
+    parity["sw_uneven_200k"] = {"e2e": sw_equal_packed(sw_e2e, want),
+                                "device_scores": bool(np.array_equal(sw_dev_scores, want.score)), "pairs": ps_sw.n}
+
+    def run_sw(idx):
+        sub = ps_sw.subset(idx)
+        a, b = sub.lists()
+        g = oracle.sw_batch(a, b, scoring=SCORING, with_cigar=True, threads=1)
+        return sw_cells(sub), g.seconds
+    one, k1, t1 = one_core_sample(run_sw, ps_sw.n, 3.0, first=64, cap=4096)
+    cpu["sw_uneven_200k"] = {"unit": "GCUPS", "all_cores": cells / want.seconds / 1e9, "all_cores_threads": threads,
+                             "all_cores_sample": f"the whole batch ({ps_sw.n} pairs, {cells / 1e9:.2f} Gcells), "
+                                                 f"{want.seconds:.2f} s",
+                             "one_core": one / 1e9 if one else None, "one_core_sample": f"{k1} pairs, {t1:.2f} s"}
+    sw_all = (cells / want.seconds / 1e9, want.seconds)
+    del want
+
+    # the long SW batch: its stratified subset
+    k = keep.get("sw_long")
+    if k:
+        ps = k["ps"]
+        cl = ps.a_len.astype(np.int64) * ps.b_len.astype(np.int64)
+        try:
+            avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+        except (ValueError, OSError):
+            avail = 16 << 30
+        th = int(max(1, min(threads, avail // 2 // int(cl.max() * 1.1))))
+        ts, pp = ps.lists()
+        want = oracle.sw_batch(ts, pp, scoring=SCORING, with_cigar=True, threads=th, trace_cell_limit=-1)
+        parity["sw_long_4k_subset"] = {"device": sw_equal_device(k["device"], want), "pairs": ps.n,
+                                       "subset": "the 64 largest pairs (0.5-1.2 Gcells) and 64 drawn at random"}
+        small = np.argsort(cl)[:3]                     # one thread: the subset's three smallest pairs
+        sub = ps.subset(small)
+        a, b = sub.lists()
+        g = oracle.sw_batch(a, b, scoring=SCORING, with_cigar=True, threads=1, trace_cell_limit=-1)
+        cpu["sw_long_4k"] = {"unit": "GCUPS", "all_cores": int(cl.sum()) / want.seconds / 1e9, "all_cores_threads": th,
+                             "all_cores_sample": f"the stratified subset ({ps.n} pairs, {cl.sum() / 1e9:.1f} Gcells), "
+                                                 f"{want.seconds:.2f} s",
+                             "one_core": sw_cells(sub) / g.seconds / 1e9,
+                             "one_core_sample": f"the subset's 3 smallest pairs, {g.seconds:.2f} s"}
+        del want
+    return cpu, parity, sw_all
+
+
 def score_only_alone(api, workloads, torch, dev, stream, args):
     """The score-only line on the first --pairs pairs of the headline batch
     (one traceback call first gives the scores it is compared with)."""
@@ -489,10 +728,11 @@ def main():
 
     if args.only:
         stream = torch.cuda.current_stream(dev)
-        run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, False),
-               "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, False),
-               "wfa_long": lambda: bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args),
-               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096),
+        keep = {}
+        run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, keep),
+               "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep),
+               "wfa_long": lambda: bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep),
+               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096, keep),
                "sw_score_only": lambda: score_only_alone(api, workloads, torch, dev, stream, args)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: run()}), flush=True)
@@ -563,9 +803,12 @@ def main():
                                "lane-instructions/s, / 6 per cell (not in MEASURED_PEAKS.json, which holds "
                                "HBM and bf16 peaks)",
                 "kernel_ms_per_launch": top_ms / max(1, top_n), "kernel_share": top_ms / total_ms if total_ms else None,
+                "frac_of_int16x2_ceiling": achieved / (2 * peak) if peak else None,
+                "int16x2_ceiling": "the 16-bit kernel's own ceiling: __viaddmax_s16x2 retires at the __viaddmax_s32 "
+                                   "rate with two cells per lane-instruction, so 2 x the int32 roofline",
                 "traffic_source": "profiles/sw16ck_trace_sw_uneven.md (bytes/cell x cells per launch)"}
 
-    sc = out_score.cpu().numpy()            # checked against the CPU baseline's sample below
+    sc = out_score.cpu().numpy()            # checked against the oracle below
 
     # e2e through the public C ABI with host buffers
     reqs = api.make_sw_requests(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, SCORING, True)
@@ -583,24 +826,24 @@ def main():
     e2e_ms = max_over_ranks(e2e_ms, world)
     h2d, d2h = api.last_transfer_bytes()
 
-    extra = {}
+    extra, keep = {}, {}
     if not args.no_extra:
         extra["sw_score_only"] = bench_sw_score_only(api, torch, dev, stream, args, ps, batch, sc)
-        extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, rank == 0)
-        extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, rank == 0)
-        extra["wfa_long"] = bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args)
-        extra["sw_long"] = bench_sw_long(api, workloads, torch, dev, stream, 4096)
+        extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, keep)
+        extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep)
+        extra["wfa_long"] = bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep)
+        extra["sw_long"] = bench_sw_long(api, workloads, torch, dev, stream, 4096, keep)
 
-    cpu = None
+    # the CPU leg (rank 0, after every GPU measurement): the oracle over each
+    # workload is the CPU baseline and the full-size parity check at once
+    cpu = cpu_all = parity = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        g, k, done, (idx, want) = cpu_baseline_sw(ps, args.cpu_seconds, threads)
+        cpu_all, parity, (g, secs) = cpu_and_parity(keep, ps, r, sc, threads)
         cpu = {"value": g, "unit": "GCUPS", "cores": threads, "kind": "port",
-               "sample": f"{k} pairs ({done / 1e9:.2f} Gcells) of the same batch, fixed random permutation"}
-        # the timed device run and the last e2e call against the baseline's first chunk
-        parity_ok = bool(np.array_equal(sc[idx], want.score)) and r.status == api.Status.ok and bool(
-            np.array_equal(r.res["score"][idx], want.score)) and all(
-            r.cigar(int(i)) == want.cigars[q] for q, i in enumerate(idx))
+               "build": "oracle/ga_oracle.c, gcc -O3 (no -march: the same code on x86 and Arm)",
+               "sample": f"the whole batch ({n} pairs, {cells / 1e9:.2f} Gcells) in one pass on all host threads, "
+                         f"{secs:.1f} s of C time"}
 
     if rank == 0:
         line = {
@@ -616,10 +859,13 @@ def main():
             "gpu_launches": launches,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "cpu_baselines": cpu_all,
             "clocks": clk,
-            "parity_sample_ok": parity_ok,
-            "parity_sample": "the CPU baseline's first 256 pairs: scores of the timed run, scores and CIGARs "
-                             "of the last e2e call",
+            "parity_full": parity,
+            "parity_ok": bool(parity) and all(v for d in parity.values() for k, v in d.items()
+                                              if isinstance(v, bool)),
+            "parity": "every workload's GPU outputs against the oracle, every field of every pair (the long SW "
+                      "batch on its stratified subset)",
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
             "extra": extra,
         }

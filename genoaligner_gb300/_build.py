@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgenoaligner_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["wfa.cu", "wfa_routed.cu", "sw.cu", "sw16.cu", "sw16ck.cu", "sw32ck.cu", "sw_plan.cu", "engine.cu", "api.cpp", "peak.cu", "learned.cu", "noalloc.cu", "tune.cu", "fasta.cpp", "qc.cu"]
+SOURCES = ["wfa.cu", "wfa_routed.cu", "sw.cu", "sw16ck.cu", "sw32ck.cu", "sw_plan.cu", "engine.cu", "api.cpp", "peak.cu", "learned.cu", "noalloc.cu", "tune.cu", "fasta.cpp", "qc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "-I" + INCLUDE, "-I" + CSRC]

@@ -25,6 +25,7 @@ import numpy as np
 from . import _build
 
 GA_OK, GA_INVALID_ARGUMENT, GA_DEVICE_ERROR = 0, 1, 2
+GA_MAX_SMAX, GA_MAX_SMAX_DEVICE = 511, 3500       # include/genoaligner_gb300.h
 K_MAX_SMAX = 511
 SW_MAX_TRACE_CELLS = 1 << 26
 
@@ -87,7 +88,7 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
            "ga_profile_kernel_name", "ga_bench_int_peak", "ga_cost_model_nparams", "ga_cost_model_set",
            "ga_cost_model_get", "ga_wfa_features", "ga_mlp_forward", "ga_mlp_gradient", "ga_mlp_train_step",
-           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_mlp_forward_fast", "ga_tune_default", "ga_tune_get",
+           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_wfa_route_items", "ga_mlp_forward_fast", "ga_tune_default", "ga_tune_get",
            "ga_tune_set", "ga_autotune_sw", "ga_autotune_wfa", "ga_tune_save", "ga_tune_load",
            "ga_fasta_read", "ga_fasta_parse", "ga_fasta_count", "ga_fasta_id", "ga_fasta_description",
            "ga_fasta_arena", "ga_fasta_offsets", "ga_fasta_lengths", "ga_fasta_pinned", "ga_fasta_upload",
@@ -161,6 +162,8 @@ def load(build: bool = True):
     L.ga_mlp_forward_fast.restype = i32
     L.ga_wfa_route_stats.argtypes = [p, i32]
     L.ga_wfa_route_stats.restype = i32
+    L.ga_wfa_route_items.argtypes = [p, i32]
+    L.ga_wfa_route_items.restype = i32
     for f in ("ga_tune_default", "ga_tune_get"):
         getattr(L, f).argtypes = [ctypes.POINTER(TuneC)]
         getattr(L, f).restype = i32
@@ -302,7 +305,9 @@ def _addr(b):
 def _opts(max_smax=0, learned=False, trace_cell_limit=0):
     o = Options()
     o.max_smax = max_smax
-    o.learned = 1 if learned else 0
+    # True / 1: queues by the cost model; 2: the same queues by the exact
+    # lower bound alone (no network)
+    o.learned = 2 if (learned == 2 and learned is not True) else (1 if learned else 0)
     o.trace_cell_limit = trace_cell_limit
     return o
 
@@ -410,11 +415,6 @@ def last_transfer_bytes():
     return int(h.value), int(d.value)
 
 
-KERNEL_IDS = {"pack2": 0, "wfa_score": 1, "wfa_trace": 2, "sw8_score": 3, "sw16_score": 4, "sw32_score": 5,
-              "sw8_trace": 6, "sw16_trace": 7, "sw32_trace": 8, "int_peak": 9, "kmer_sketch": 10, "mlp": 11,
-              "sw16x2_trace": 12, "route": 13, "sw_plan": 14, "sw16x2_score": 15}
-
-
 def profile(on: bool):
     load().ga_profile(1 if on else 0)
 
@@ -423,7 +423,11 @@ def profile_read():
     """{kernel name: (total device ms, launches)} for kernels that ran."""
     L = load()
     out = {}
-    for name, k in KERNEL_IDS.items():
+    for k in range(64):
+        name = L.ga_profile_kernel_name(k)
+        if not name:
+            break
+        name = name.decode()
         ms, n = ctypes.c_double(0), ctypes.c_int64(0)
         L.ga_profile_read(k, ctypes.byref(ms), ctypes.byref(n))
         if n.value:
@@ -726,6 +730,16 @@ def wfa_route_stats(rounds: int = 12):
     if st != GA_OK:
         raise RuntimeError(f"ga_wfa_route_stats failed ({st})")
     return int(out[0]), int(out[1]), [int(x) for x in out[2:]]
+
+
+def wfa_route_items(n: int) -> np.ndarray:
+    """Queue item of every pair of the calling thread's last learned call
+    (ga_wfa_route_items): -1 unresolved by the bound; else bucket | first smax << 8."""
+    out = np.zeros(n, np.int32)
+    st = load().ga_wfa_route_items(out.ctypes.data, int(n))
+    if st != GA_OK:
+        raise RuntimeError(f"ga_wfa_route_items failed ({st})")
+    return out
 
 
 # -------------------------------------------------------------- autotuner --

@@ -1,6 +1,7 @@
 // common.cuh -- shared device definitions for the GB300 pairwise aligner.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -71,11 +72,14 @@ __device__ __forceinline__ int match_run(const uint64_t* __restrict__ P, const u
 }
 
 // Kernel identities for launch accounting and per-kernel timing.
+// (names: ga_profile_kernel_name)
 enum KernelId : int {
-    K_PACK = 0, K_WFA_SCORE, K_WFA_TRACE, K_SW8_SCORE, K_SW16_SCORE, K_SW32_SCORE,
-    K_SW8_TRACE, K_SW16_TRACE, K_SW32_TRACE, K_PEAK, K_SKETCH, K_MLP, K_SW16X2_TRACE, K_ROUTE, K_SWPLAN,
-    K_SW16X2_SCORE, K_COUNT
+    K_PACK = 0, K_WFA_SCORE, K_WFA_TRACE, K_WFA_LANE, K_WFA_ROUTED, K_SW_SCORE, K_SW32_TRACE, K_SW16X2_TRACE,
+    K_SW16X2_SCORE, K_SWPLAN, K_VALIDATE, K_QC, K_PEAK, K_SKETCH, K_MLP, K_ROUTE, K_COUNT
 };
+
+// Streaming multiprocessors of the current device (queried once per device).
+int device_sms();
 
 // Host side, around every launch this library makes: counts the launch and,
 // while profiling is on, records CUDA events on the launch stream.

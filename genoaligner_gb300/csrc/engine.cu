@@ -68,6 +68,27 @@ void launch_end(int kernel_id, cudaStream_t st)
     t_prof_cur = ProfRec{-1, nullptr, nullptr};
 }
 
+int device_sms()
+{
+    constexpr int MAX_DEV = 64;
+    static std::atomic<int> cache[MAX_DEV];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < MAX_DEV) {
+        if (const int v = cache[dev].load(std::memory_order_relaxed)) return v;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < MAX_DEV) cache[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
 // Host-to-device / device-to-host bytes of the calling thread's last batch call.
 thread_local int64_t t_h2d = 0, t_d2h = 0;
 
@@ -417,7 +438,8 @@ static void carve_wfa(Carve& k, WfaScratch& S, int n, int64_t arena, bool trace,
 }
 
 // Every launch of one WFA batch on stream st (inputs already on the device).
-static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool trace, bool learned, int lane_smax,
+// route: 0 plain, 1 queues by the cost model, 2 queues by the lower bound alone.
+static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool trace, int route, int lane_smax,
                                int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
     D.packed = S.packed;
@@ -430,10 +452,12 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     cudaError_t e = cudaMemsetAsync(S.ctr, 0, 64 * sizeof(int32_t), st);
     if (e == cudaSuccess) e = launch_pack(D, S.seq_bytes, S.packed, S.pure, st);
     if (e != cudaSuccess) return e;
-    if (!learned) return launch_wfa(A, S.slots, st);
+    if (route == 0) return launch_wfa(A, S.slots, st);
     const int NB = route_buckets();
     if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int32_t) * (2 * NB + 4), st)) != cudaSuccess) return e;
-    if ((e = launch_route_model(D, smax, lane_smax, S.item, S.lb, S.y, S.counts, score, len, st)) != cudaSuccess) return e;
+    if ((e = launch_route_model(D, smax, lane_smax, route == 1, S.item, S.lb, S.y, S.counts, score, len, st)) !=
+        cudaSuccess)
+        return e;
     if ((e = launch_route(D.n, S.item, S.counts, S.starts, S.big, S.small, st)) != cudaSuccess) return e;
     // ctr layout: [0] warp-queue next, [1] lane-queue next, [2] escalation
     // next, [3] whole-block next, [32] escalation count; counts[2 NB + 2]:
@@ -458,18 +482,18 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
 
 // Learned path as one CUDA graph, cached per context by everything the
 // launches bake in.
-static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace, int lane_smax,
-                                 int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
+static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace, int route,
+                                 int lane_smax, int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
     const uint64_t key[8] = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
-                             (uint64_t)trace | (uint64_t)lane_smax << 8, (uint64_t)(uintptr_t)score,
+                             (uint64_t)trace | (uint64_t)lane_smax << 8 | (uint64_t)route << 16, (uint64_t)(uintptr_t)score,
                              (uint64_t)(uintptr_t)cig, (uint64_t)(uintptr_t)D.a_off};
     if (!c->gexec || std::memcmp(key, c->gkey, sizeof(key)) != 0) {
         if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, true, lane_smax, score, len, cig, err, st);
+        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, route, lane_smax, score, len, cig, err, st);
         e = cudaStreamEndCapture(st, &g);
         if (e1 != cudaSuccess || e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e1 != cudaSuccess ? e1 : e; }
         e = cudaGraphInstantiate(&c->gexec, g, 0);
@@ -489,20 +513,30 @@ struct RouteRecord {
     uint64_t gen = 0;
     const int32_t* counts = nullptr;
     const int32_t* ctr = nullptr;
+    const int32_t* item = nullptr;
+    int n = 0;
     int64_t seq_bytes = 0;
     int chunk = 1;
 };
 static thread_local RouteRecord t_route;
 
-static void note_route(Ctx* c, const WfaScratch& S)
+static void note_route(Ctx* c, const WfaScratch& S, int n)
 {
     t_route.c = c;
     t_route.gen = c->dev_gen;
     t_route.counts = S.counts;
     t_route.ctr = S.ctr;
+    t_route.item = S.item;
+    t_route.n = n;
 }
 
-int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
+int route_mode(int requested)
+{
+    if (requested == 1 && !cost_model_loaded()) return 0;
+    return (requested == 1 || requested == 2) ? requested : 0;
+}
+
+int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
                   const WfaFinish& fin, const char** err)
 {
     *err = nullptr;
@@ -514,7 +548,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
         smax = std::min(smax, (int)reqs[i].smax);
         trace |= reqs[i].with_cigar != 0;
     }
-    learned = learned && cost_model_loaded();
+    route = route_mode(route);
+    const bool learned = route != 0;
 
     // plan: 32-aligned sequence offsets, CIGAR slot offsets
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
@@ -593,9 +628,10 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, boo
     D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
     cudaError_t le;
     if (fail_here(3)) le = cudaErrorLaunchFailure;
-    else if (learned && !profiling_on()) le = run_wfa_graph(c, S, D, smax, trace, lane_smax, dsc, dln, dcg, der, c->stream);
-    else le = enqueue_wfa(S, D, smax, trace, learned, lane_smax, dsc, dln, dcg, der, c->stream);
-    if (learned) note_route(c, S);
+    else if (learned && !profiling_on())
+        le = run_wfa_graph(c, S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
+    else le = enqueue_wfa(S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
+    if (learned) note_route(c, S, n);
     if (le == cudaSuccess && trace) le = launch_wfa_validate(D, dsc, dln, dcg, dvf, c->stream);
     if (le != cudaSuccess) {
         cudaGetLastError();
@@ -652,127 +688,20 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err)
     return GA_OK;
 }
 
-// Work plan of one SW batch: pairs routed to the two-pairs-per-warp 16-bit
-// trace kernel (eligible pure-ACGT pairs) or to the 32-bit kernel, per band
-// width, largest first; per-slot direction-table and band-edge sizes.
+// Work plan of one SW batch, as the device planner left it (sw_plan.cu):
+// per list its length in the flattened work array and the largest per-warp
+// memory of its items; the band-edge slot; the 16-bit list's largest item;
+// pairs taken on the optimistic 16-bit rule and their 32-bit memory.
 struct SwPlan {
-    std::vector<int32_t> w32[3];     // pair indices, 32-bit kernel, widths 8 / 16 / 32 (host-built plans)
-    std::vector<int32_t> w16[3];     // 2 pair indices per item, 16-bit kernel (host-built plans)
-    int64_t n32[3] = {0, 0, 0}, n16[3] = {0, 0, 0};   // ints of each list in the flattened work array
-    int64_t dir32[3] = {0, 0, 0}, dir16[3] = {0, 0, 0};
+    int64_t ints[SP_LISTS] = {0, 0, 0};
+    int64_t dir[SP_LISTS] = {0, 0, 0};
     int64_t edge_slot = 2;
-    int64_t max16_cells = 0;                          // the 16-bit list's largest item (rows x columns)
-    int64_t n_opt = 0, dir_opt = 0;                   // pairs on the optimistic 16-bit rule; their 32-bit memory
-    int64_t words() const
-    {
-        int64_t s = 0;
-        for (int k = 0; k < 3; ++k) s += n32[k] + n16[k];
-        return s;
-    }
+    int64_t max16_cells = 0;
+    int64_t n_opt = 0, dir_opt = 0;
 };
 
-static const int kWidths[3] = {8, 16, 32};
-static int width_index(int C) { return C == 8 ? 0 : (C == 16 ? 1 : 2); }
-
-// Largest first, in O(n): a counting sort on a log-scale size key (64 buckets
-// per doubling of (m + 31) * n, so pairs sharing a bucket differ by < 1.1 %),
-// index order within a bucket.
-static void order_by_size(std::vector<int32_t>& v, const int32_t* tl, const int32_t* pl)
-{
-    if (v.size() < 2) return;
-    constexpr int NB = 64 * 48;
-    std::vector<uint16_t> key(v.size());
-    std::vector<int32_t> cnt(NB + 1, 0);
-    for (size_t q = 0; q < v.size(); ++q) {
-        const double c = (double)(tl[v[q]] + 31) * (double)std::max(pl[v[q]], 1);
-        const int b = std::min(NB - 1, std::max(0, (int)(std::log2(c) * 64.0)));
-        key[q] = (uint16_t)(NB - 1 - b);                 // descending size
-        ++cnt[key[q] + 1];
-    }
-    for (int b = 0; b < NB; ++b) cnt[b + 1] += cnt[b];
-    std::vector<int32_t> out(v.size());
-    for (size_t q = 0; q < v.size(); ++q) out[cnt[key[q]]++] = v[q];
-    v.swap(out);
-}
-
-// The two-pairs-per-warp kernels' list order (sw16_shape_key, the device
-// planner's): a stable counting sort, so that neighbours share a shape.
-static void order_by_shape16(std::vector<int32_t>& v, const int32_t* tl, const int32_t* pl)
-{
-    if (v.size() < 2) return;
-    constexpr int NB = 4096;
-    std::vector<uint16_t> key(v.size());
-    std::vector<int32_t> cnt(NB + 1, 0);
-    for (size_t q = 0; q < v.size(); ++q) {
-        key[q] = (uint16_t)sw16_shape_key(tl[v[q]], pl[v[q]]);
-        ++cnt[key[q] + 1];
-    }
-    for (int b = 0; b < NB; ++b) cnt[b + 1] += cnt[b];
-    std::vector<int32_t> out(v.size());
-    for (size_t q = 0; q < v.size(); ++q) out[cnt[key[q]]++] = v[q];
-    v.swap(out);
-}
-
-// Traceback kernels: the checkpointed forms (sw16ck.cu for two 16-bit pairs
-// per warp, sw32ck.cu for one 32-bit pair per warp) unless GA_SW16CK=0
-// selects the forms that store every cell's direction bits (sw16.cu, sw.cu).
-static bool use_sw16ck()
-{
-    static const bool on = [] {
-        const char* e = getenv("GA_SW16CK");
-        return !(e && e[0] == '0');
-    }();
-    return on;
-}
-
-static void plan_sw(int32_t n, const int32_t* tl, const int32_t* pl, const uint8_t* pure, const uint8_t* skip,
-                    const ga_sw_scoring& sc, bool trace, const ga_tune& T, SwPlan& P)
-{
-    std::vector<int32_t> e16[3];
-    const bool use16_ok = T.sw_pack16 != 0;
-    const bool ck = use_sw16ck();
-    for (int32_t i = 0; i < n; ++i) {
-        if (skip && skip[i]) continue;
-        // the checkpointed traceback kernels and the 16-bit score-only kernel
-        // choose their own lane widths: list 0 (list 1: 32-bit pairs for the
-        // long-pair shape)
-        const bool use16 = use16_ok && (trace || ck) && pure && pure[i] && pure[n + i] &&
-                           sw16_eligible(tl[i], pl[i], sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
-        const int k = (ck && (trace || use16)) ? 0 : width_index(sw_width_for(pl[i]));
-        if (use16) e16[k].push_back(i);
-        else P.w32[(ck && trace && sw32ck_long(tl[i], pl[i], T.sw_long_log2)) ? 1 : k].push_back(i);
-    }
-    for (int k = 0; k < 3; ++k) {
-        order_by_size(P.w32[k], tl, pl);
-        for (int32_t i : P.w32[k]) {
-            if (trace) P.dir32[k] = std::max(P.dir32[k], (ck && k < 2) ? sw32ck_dir_words(tl[i], pl[i], T.sw_long_log2)
-                                                                       : sw_dir_words(tl[i], pl[i], kWidths[k]));
-            P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)tl[i]);
-        }
-        P.dir32[k] = (P.dir32[k] + 3) / 4 * 4;
-        if (ck && k == 0) order_by_shape16(e16[k], tl, pl);
-        else order_by_size(e16[k], tl, pl);
-        for (size_t q = 0; q < e16[k].size(); q += 2) {
-            const int32_t a = e16[k][q], b = q + 1 < e16[k].size() ? e16[k][q + 1] : -1;
-            P.w16[k].push_back(a);
-            P.w16[k].push_back(b);
-            const int M = std::max(tl[a], b >= 0 ? tl[b] : 0), N = std::max(pl[a], b >= 0 ? pl[b] : 0);
-            if (k == 0) P.max16_cells = std::max<int64_t>(P.max16_cells, (int64_t)M * N);
-            P.dir16[k] = std::max(P.dir16[k], (use_sw16ck() && k == 0)
-                                                  ? (trace ? sw16ck_dir_words(M, N, T.sw_window) : sw16so_dir_words(M, N))
-                                                                        : sw16_dir_words(M, N, kWidths[k]));
-            P.edge_slot = std::max<int64_t>(P.edge_slot, 2 * (int64_t)M);
-        }
-        P.dir16[k] = (P.dir16[k] + 3) / 4 * 4;
-    }
-    for (int k = 0; k < 3; ++k) {
-        P.n32[k] = (int64_t)P.w32[k].size();
-        P.n16[k] = (int64_t)P.w16[k].size();
-    }
-}
-
-// The checkpointed kernels' plan, built on the device (sw_plan.cu) into
-// `dwork`; reads back its record and fills P's list lengths and sizes.
+// The plan, built on the device (sw_plan.cu) into `dwork`; reads back its
+// record and fills P's list lengths and sizes.
 static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bool trace, int64_t cell_limit,
                                   int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
                                   long long* dres, long long* hres, const ga_tune& T, cudaStream_t st, SwPlan& P)
@@ -787,7 +716,6 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bo
     A.long_log2 = T.sw_long_log2;
     A.too_large_score = too_large_score;
     A.score_only = trace ? 0 : 1;
-    A.maxc = sw_maxc();
     A.out_score = out_score;
     A.work = dwork;
     A.res = dres;
@@ -796,11 +724,9 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bo
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     P = SwPlan();
-    for (int k = 0; k < 3; ++k) {
-        P.n16[k] = hres[SP_INTS + k];
-        P.n32[k] = hres[SP_INTS + 3 + k];
-        P.dir16[k] = (hres[SP_DIR + k] + 3) / 4 * 4;
-        P.dir32[k] = (hres[SP_DIR + 3 + k] + 3) / 4 * 4;
+    for (int l = 0; l < SP_LISTS; ++l) {
+        P.ints[l] = hres[SP_INTS + l];
+        P.dir[l] = (hres[SP_DIR + l] + 3) / 4 * 4;
     }
     P.edge_slot = std::max<int64_t>(2, hres[SP_EDGE]);
     P.max16_cells = hres[SP_MAXC16];
@@ -828,7 +754,7 @@ static int64_t sw_dir_budget(const Ctx* c, int parts)
 // Slots (resident warps) per launch and the direction-table words the launches
 // need (they run one after another on one stream and share the table).
 struct SwSlots {
-    int s32[3] = {0, 0, 0}, s16[3] = {0, 0, 0};
+    int s[SP_LISTS] = {0, 0, 0};
     int s_esc = 0;                                    // the 32-bit launch for pairs handed over by the 16-bit kernel
     int64_t dir_words = 0, max_slots = 4;
 };
@@ -836,30 +762,24 @@ struct SwSlots {
 static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_count, int64_t budget)
 {
     SwSlots S;
-    for (int k = 0; k < 3; ++k) {
-        if (P.n32[k] > 0) {
-            const int bw = 4;                                          // warp slots come in blocks of 4
-            int s = (trace && use_sw16ck() && k < 2) ? sw32ck_max_slots(k == 1, sm_count)
-                                                     : sw_max_slots(kWidths[k], trace, sm_count);
-            s = (int)std::min<int64_t>(s, (P.n32[k] + bw - 1) / bw * bw);
-            if (trace && P.dir32[k] > 0)
-                s = (int)std::min<int64_t>(s, std::max<int64_t>(bw, budget / (P.dir32[k] * 4) / bw * bw));
-            S.s32[k] = s;
-            if (trace) S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir32[k]);
-            S.max_slots = std::max<int64_t>(S.max_slots, s);
+    for (int l = 0; l < SP_LISTS; ++l) {
+        if (P.ints[l] <= 0) continue;
+        // warp slots come in blocks of 4
+        int s;
+        if (l == SP_L16) {
+            s = trace ? sw16ck_max_slots(sm_count, T.sw_window) : sw16so_max_slots(sm_count);
+            s = (int)std::min<int64_t>(s, (P.ints[l] / 2 + 3) / 4 * 4);
+        } else {
+            s = trace ? sw32ck_max_slots(l == SP_L32LONG, sm_count) : sw_max_slots(sm_count);
+            s = (int)std::min<int64_t>(s, (P.ints[l] + 3) / 4 * 4);
         }
-        if (P.n16[k] > 0) {
-            int s = (use_sw16ck() && k == 0) ? (trace ? sw16ck_max_slots(sm_count, T.sw_window) : sw16so_max_slots(sm_count))
-                                             : sw16_max_slots(kWidths[k], sm_count);
-            s = (int)std::min<int64_t>(s, (P.n16[k] / 2 + 3) / 4 * 4);
-            s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir16[k] * 4) / 4 * 4));
-            S.s16[k] = s;
-            S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir16[k]);
-            S.max_slots = std::max<int64_t>(S.max_slots, s);
-        }
+        if (P.dir[l] > 0) s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir[l] * 4) / 4 * 4));
+        S.s[l] = s;
+        S.dir_words = std::max(S.dir_words, (int64_t)s * P.dir[l]);
+        S.max_slots = std::max<int64_t>(S.max_slots, s);
     }
     if (trace && P.n_opt > 0 && P.dir_opt > 0) {
-        int s = sw32ck_max_slots(true, sm_count);                      // blocks of 4 warps
+        int s = sw32ck_max_slots(true, sm_count);
         s = (int)std::min<int64_t>(s, (P.n_opt + 3) / 4 * 4);
         s = (int)std::min<int64_t>(s, std::max<int64_t>(4, budget / (P.dir_opt * 4) / 4 * 4));
         S.s_esc = s;
@@ -870,74 +790,63 @@ static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_cou
 }
 
 // Enqueue every SW launch of a plan.  `dwork` holds the plan's lists
-// concatenated in the order w16[0..2] then w32[0..2]; `ctr` has 8 zeroed ints;
-// esc_list (n ints, device-planned batches) takes the pairs the 16-bit kernel
-// hands to the 32-bit one.
+// concatenated in list order; `ctr` has 8 zeroed ints; esc_list (n ints)
+// takes the pairs the 16-bit kernel hands to the 32-bit one.
 static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc& D, const ga_sw_scoring& sc,
                                bool trace, const ga_tune& T, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
                                int32_t* out_len, char* out_cigar, uint32_t* dirs, int32_t* edge, int32_t* ctr,
-                               int32_t* err, cudaStream_t st, int32_t* esc_list = nullptr)
+                               int32_t* err, cudaStream_t st, int32_t* esc_list)
 {
+    // ctr: [l] list l's item counter, [6] pairs handed over, [7] their counter
+    const bool opt = trace && P.n_opt > 0 && esc_list && S.s_esc > 0;
+    const int64_t coop = T.sw_coop_log2 < 40 ? ((int64_t)1 << T.sw_coop_log2) : -1;
     int64_t base = 0;
-    // ctr: [0..5] the lists' item counters, [6] pairs handed over, [7] their counter
-    const bool opt = P.n_opt > 0 && esc_list && S.s_esc > 0;
-    for (int k = 0; k < 3; ++k) {
-        if (P.n16[k] > 0) {
-            Sw16Args A;
-            A.D = D; A.work = dwork + base; A.nwork = (int32_t)(P.n16[k] / 2);
-            A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
-            A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
-            A.dirs = dirs; A.dir_slot = P.dir16[k]; A.edge = edge; A.edge_slot = P.edge_slot;
-            A.counter = ctr + k; A.err = err;
-            A.coop_cells = (k == 0 && T.sw_coop_log2 < 40) ? ((int64_t)1 << T.sw_coop_log2) : -1;
-            if (k == 0 && opt) {
-                A.ovf_limit = sw16_overflow_limit(sc.match);
-                A.esc_list = esc_list;
-                A.esc_count = ctr + 6;
-            }
-            const bool blocks = A.coop_cells >= 0 && P.max16_cells > A.coop_cells;
-            const cudaError_t e = (use_sw16ck() && k == 0)
-                                      ? (trace ? launch_sw16ck(A, S.s16[k], T.sw_window, blocks, st) : launch_sw16so(A, S.s16[k], st))
-                                      : launch_sw16(A, kWidths[k], S.s16[k], st);
-            if (e != cudaSuccess) return e;
-            if (k == 0 && opt) {
-                // the pairs the 16-bit kernel handed over, on the 32-bit long shape
-                SwArgs B;
-                B.D = D; B.work = esc_list; B.nwork = 0; B.nwork_dev = ctr + 6;
-                B.match = sc.match; B.mismatch = sc.mismatch; B.gap_open = sc.gap_open; B.gap_extend = sc.gap_extend;
-                B.out_score = out_score; B.out_pos = out_pos; B.out_len = out_len; B.out_cigar = out_cigar;
-                B.dirs = dirs; B.dir_slot = P.dir_opt; B.edge = edge; B.edge_slot = P.edge_slot;
-                B.counter = ctr + 7; B.err = err;
-                B.coop_cells = T.sw_coop_log2 < 40 ? ((int64_t)1 << T.sw_coop_log2) : -1;
-                const cudaError_t e2 = launch_sw32ck(B, true, S.s_esc, st);
-                if (e2 != cudaSuccess) return e2;
-            }
+    if (P.ints[SP_L16] > 0) {
+        Sw16Args A;
+        A.D = D; A.work = dwork; A.nwork = (int32_t)(P.ints[SP_L16] / 2);
+        A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
+        A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
+        A.dirs = dirs; A.dir_slot = P.dir[SP_L16]; A.edge = edge; A.edge_slot = P.edge_slot;
+        A.counter = ctr + SP_L16; A.err = err;
+        A.coop_cells = coop;
+        if (opt) {
+            A.ovf_limit = sw16_overflow_limit(sc.match);
+            A.esc_list = esc_list;
+            A.esc_count = ctr + 6;
         }
-        base += P.n16[k];
+        const bool blocks = A.coop_cells >= 0 && P.max16_cells > A.coop_cells;
+        const cudaError_t e = trace ? launch_sw16ck(A, S.s[SP_L16], T.sw_window, blocks, st)
+                                    : launch_sw16so(A, S.s[SP_L16], st);
+        if (e != cudaSuccess) return e;
+        if (opt) {
+            // the pairs the 16-bit kernel handed over, on the 32-bit long shape
+            SwArgs B;
+            B.D = D; B.work = esc_list; B.nwork = 0; B.nwork_dev = ctr + 6;
+            B.match = sc.match; B.mismatch = sc.mismatch; B.gap_open = sc.gap_open; B.gap_extend = sc.gap_extend;
+            B.out_score = out_score; B.out_pos = out_pos; B.out_len = out_len; B.out_cigar = out_cigar;
+            B.dirs = dirs; B.dir_slot = P.dir_opt; B.edge = edge; B.edge_slot = P.edge_slot;
+            B.counter = ctr + 7; B.err = err;
+            B.coop_cells = coop;
+            const cudaError_t e2 = launch_sw32ck(B, true, S.s_esc, st);
+            if (e2 != cudaSuccess) return e2;
+        }
     }
-    for (int k = 0; k < 3; ++k) {
-        if (P.n32[k] > 0) {
+    base += P.ints[SP_L16];
+    for (int l = SP_L32; l <= SP_L32LONG; ++l) {
+        if (P.ints[l] > 0) {
             SwArgs A;
-            A.D = D; A.work = dwork + base; A.nwork = (int32_t)P.n32[k];
+            A.D = D; A.work = dwork + base; A.nwork = (int32_t)P.ints[l];
             A.match = sc.match; A.mismatch = sc.mismatch; A.gap_open = sc.gap_open; A.gap_extend = sc.gap_extend;
             A.out_score = out_score; A.out_pos = out_pos; A.out_len = out_len; A.out_cigar = out_cigar;
-            A.dirs = dirs; A.dir_slot = P.dir32[k]; A.edge = edge; A.edge_slot = P.edge_slot;
-            A.counter = ctr + 3 + k; A.err = err;
-            A.coop_cells = (k == 1 && T.sw_coop_log2 < 40) ? ((int64_t)1 << T.sw_coop_log2) : -1;
-            const cudaError_t e = (trace && use_sw16ck() && k < 2) ? launch_sw32ck(A, k == 1, S.s32[k], st)
-                                                                   : launch_sw(A, kWidths[k], trace, S.s32[k], st);
+            A.dirs = dirs; A.dir_slot = P.dir[l]; A.edge = edge; A.edge_slot = P.edge_slot;
+            A.counter = ctr + l; A.err = err;
+            A.coop_cells = l == SP_L32LONG ? coop : -1;
+            const cudaError_t e = trace ? launch_sw32ck(A, l == SP_L32LONG, S.s[l], st) : launch_sw(A, S.s[l], st);
             if (e != cudaSuccess) return e;
         }
-        base += P.n32[k];
+        base += P.ints[l];
     }
     return cudaSuccess;
-}
-
-static void flatten_plan(const SwPlan& P, int32_t* out)
-{
-    int64_t q = 0;
-    for (int k = 0; k < 3; ++k) for (int32_t x : P.w16[k]) out[q++] = x;
-    for (int k = 0; k < 3; ++k) for (int32_t x : P.w32[k]) out[q++] = x;
 }
 
 // One contiguous range of a checked SW batch: requests [base, base + n) of
@@ -954,13 +863,10 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     const ga_sw_scoring s0 = reqs[0].scoring;
 
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
-    std::vector<int32_t> tl(n), pl(n);
-    std::vector<uint8_t> too_big(n, 0), own(n, 0);
+    std::vector<uint8_t> own(n, 0);
     int64_t arena = 0, cig = 0;
     for (int32_t i = 0; i < n; ++i) {
         const ga_sw_request& r = reqs[i];
-        tl[i] = r.text_len;
-        pl[i] = r.pattern_len;
         // a side that repeats the previous request's (same pointer and length:
         // one reference against many, or many against one) is staged once
         if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) a_off[i] = a_off[i - 1];
@@ -969,9 +875,6 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         else { b_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 2; }
         out_off[i] = cig; cig += (int64_t)r.text_len + r.pattern_len;
         slot_end[i] = cig;
-        if (trace && cell_limit >= 0 && r.text_len > 0 && r.pattern_len > 0 &&
-            ((int64_t)r.text_len + 1) * ((int64_t)r.pattern_len + 1) > cell_limit)
-            too_big[i] = 1;
     }
     arena += 64;
     if (!trace) cig = 0;
@@ -1024,15 +927,14 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     });
     std::memset(hseq + arena - 64, 0, 64);
 
-    // device memory: fixed blocks, then (device-built plans) the planner's scratch,
-    // then counters, band edges and direction tables (sized from the plan; a
-    // first pass reserves the fixed part)
-    const bool dplan = use_sw16ck();
+    // device memory: fixed blocks, then the planner's scratch, then counters,
+    // band edges and direction tables (sized from the plan; a first pass
+    // reserves the fixed part)
     const size_t plan_off = dev_fixed;
     size_t plan_end = plan_off;
     int32_t* dscr = nullptr;
     long long* dres = nullptr;
-    if (dplan) {
+    {
         Carve k(nullptr);
         k.off = plan_off;
         k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
@@ -1041,24 +943,22 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     }
     const size_t hres_off = ((size_t)((char*)(her + 1) - c->host) + 255) & ~(size_t)255;
     if (fail_here(1) || !ensure_dev(c, plan_end + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    long long* hres = dplan ? reinterpret_cast<long long*>(c->host + hres_off) : nullptr;
+    long long* hres = reinterpret_cast<long long*>(c->host + hres_off);
     const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
     *h2d = (int64_t)in_bytes;
     PairDesc D;
     D.packed = nullptr;
     D.n = n;
     SwPlan P;
-    // inputs to the device, purity flags, and the plan (host-built, or on the
-    // device for the checkpointed kernels); again from the start if the arena moves
+    // inputs to the device, purity flags, and the plan on the device; again
+    // from the start if the arena moves
     auto stage = [&](bool first_time) -> int32_t {
         {
             Carve k(c->dev);
             in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dvf, &dcg, &der);
-            if (dplan) {
-                k.off = plan_off;
-                dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
-                dres = k.take<long long>(SP_RES);
-            }
+            k.off = plan_off;
+            dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+            dres = k.take<long long>(SP_RES);
         }
         D.seq = dseq; D.pure = dpure;
         D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
@@ -1078,30 +978,10 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
             *err = E_LAUNCH;
             return GA_DEVICE_ERROR;
         }
-        if (dplan) {
-            if (device_plan_sw(D, s0, trace, trace ? cell_limit : -1, -1, dsc, dwork, dscr, dres, hres, T, c->stream,
-                               P) != cudaSuccess) {
-                cudaGetLastError();
-                *err = E_LAUNCH;
-                return GA_DEVICE_ERROR;
-            }
-            return GA_OK;
-        }
-        if (first_time) {
-            if (cudaMemcpyAsync(hpure, dpure, 2 * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-                cudaStreamSynchronize(c->stream) != cudaSuccess) {
-                cudaGetLastError();
-                *err = E_LAUNCH;
-                return GA_DEVICE_ERROR;
-            }
-            plan_sw(n, tl.data(), pl.data(), hpure, too_big.data(), s0, trace, T, P);
-            flatten_plan(P, hwork);
-        }
-        if (P.words() > 0 &&
-            cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)P.words(), cudaMemcpyHostToDevice, c->stream) !=
-                cudaSuccess) {
+        if (device_plan_sw(D, s0, trace, trace ? cell_limit : -1, -1, dsc, dwork, dscr, dres, hres, T, c->stream,
+                           P) != cudaSuccess) {
             cudaGetLastError();
-            *err = E_H2D;
+            *err = E_LAUNCH;
             return GA_DEVICE_ERROR;
         }
         return GA_OK;
@@ -1127,7 +1007,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     extra_layout(c->dev, &dctr, &dedge, &ddirs);
     cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
     if (launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream,
-                    dplan ? dscr : nullptr) != cudaSuccess ||
+                    dscr) != cudaSuccess ||
         (trace && launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
                                      dln, dcg, dvf, c->stream) != cudaSuccess)) {
         cudaGetLastError();
@@ -1335,7 +1215,8 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
                           ga_batch_info* info)
 {
     for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
-    const int32_t max_smax = (opt && opt->max_smax > 0) ? opt->max_smax : GA_MAX_SMAX;
+    const int32_t max_smax =
+        (opt && opt->max_smax > 0) ? std::min<int32_t>(opt->max_smax, GA_MAX_SMAX_DEVICE) : GA_MAX_SMAX;
     bool any_cigar = false;
     for (int32_t i = 0; i < n; ++i) any_cigar |= reqs[i].with_cigar != 0;
     const char* err = nullptr;
@@ -1374,7 +1255,7 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
         set_info(info, st, err, 0, 0);
         return st;
     }
-    st = wfa_batch(reqs, n, max_smax, opt && opt->learned, fin, &err);
+    st = wfa_batch(reqs, n, max_smax, opt ? opt->learned : 0, fin, &err);
     if (st != GA_OK) {
         for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
         set_info(info, st, err, 0, 0);
@@ -1473,9 +1354,14 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
                          int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream, const char** err)
 {
     const char* e = nullptr;
-    if (!b || b->n < 0 || smax < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off ||
-                                                     !b->b_len || !out_score || (trace && (!out_len || !out_cigar || !b->out_off))))) {
+    if (!b || b->n < 0 || b->seq_bytes < 0 ||
+        (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len || !out_score ||
+                      (trace && (!out_len || !out_cigar || !b->out_off))))) {
         if (err) *err = "invalid device batch";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (smax < 0 || smax > GA_MAX_SMAX_DEVICE) {
+        if (err) *err = "smax out of range [0, GA_MAX_SMAX_DEVICE]";
         return GA_INVALID_ARGUMENT;
     }
     if (((uintptr_t)b->seq & 15) != 0) {
@@ -1483,7 +1369,8 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
         return GA_INVALID_ARGUMENT;
     }
     if (b->n == 0) return GA_OK;
-    const bool learned = opt && opt->learned && cost_model_loaded();
+    const int route = route_mode(opt ? opt->learned : 0);
+    const bool learned = route != 0;
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
@@ -1505,9 +1392,9 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
     if (le == cudaSuccess) {
         const int lane_smax = tune_current().wfa_lane_smax;
         if (learned && !profiling_on())
-            le = run_wfa_graph(c, S, D, smax, trace != 0, lane_smax, out_score, out_len, out_cigar, derr, st);
-        else le = enqueue_wfa(S, D, smax, trace != 0, learned, lane_smax, out_score, out_len, out_cigar, derr, st);
-        if (learned) note_route(c, S);
+            le = run_wfa_graph(c, S, D, smax, trace != 0, route, lane_smax, out_score, out_len, out_cigar, derr, st);
+        else le = enqueue_wfa(S, D, smax, trace != 0, route, lane_smax, out_score, out_len, out_cigar, derr, st);
+        if (learned) note_route(c, S, b->n);
     }
     if (le != cudaSuccess) {
         cudaGetLastError();
@@ -1549,6 +1436,18 @@ int32_t ga_wfa_route_stats(int32_t* out, int32_t max)
     return GA_OK;
 }
 
+int32_t ga_wfa_route_items(int32_t* out, int32_t n)
+{
+    const RouteRecord r = t_route;
+    if (!r.c || !out || n != r.n || r.c->dev_gen != r.gen) return GA_INVALID_ARGUMENT;
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(out, r.item, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return GA_DEVICE_ERROR;
+    }
+    return GA_OK;
+}
+
 int32_t ga_wfa_device(const ga_device_batch* b, int32_t smax, int32_t trace, int32_t* out_score,
                       int32_t* out_len, char* out_cigar, void* stream, const char** err)
 {
@@ -1560,8 +1459,9 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
                      const char** err)
 {
     const char* e = nullptr;
-    if (!b || b->n < 0 || (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len ||
-                                         !out_score || !out_pos || (trace && (!out_len || !out_cigar || !b->out_off))))) {
+    if (!b || b->n < 0 || b->seq_bytes < 0 ||
+        (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len || !out_score || !out_pos ||
+                      (trace && (!out_len || !out_cigar || !b->out_off))))) {
         if (err) *err = "invalid device batch";
         return GA_INVALID_ARGUMENT;
     }
@@ -1571,174 +1471,76 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     const ga_tune T = tune_current();
-    if (use_sw16ck()) {
-        // the checkpointed kernels (score-only: sw16so and the score-only
-        // widths): purity and the plan on the device, one small record back,
-        // then the launches
-        auto plan_layout = [&](char* base, uint8_t** pp, int32_t** scr, int32_t** wk, long long** res) {
-            Carve k(base);
-            *pp = k.take<uint8_t>(2 * (size_t)n);
-            *scr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
-            *wk = k.take<int32_t>(2 * (size_t)n + 8);
-            *res = k.take<long long>(SP_RES);
-            return k.off;
-        };
-        uint8_t* dpure;
-        int32_t *dscr, *dwork;
-        long long* dres;
-        const size_t plan_bytes = plan_layout(nullptr, &dpure, &dscr, &dwork, &dres);
-        if (!ensure_dev(c, plan_bytes + 4096) || !ensure_host(c, sizeof(long long) * SP_RES)) {
-            release_ctx(c);
-            if (err) *err = E_ALLOC;
-            return GA_DEVICE_ERROR;
-        }
-        long long* hres = reinterpret_cast<long long*>(c->host);
-        PairDesc D;
-        D.seq = b->seq; D.packed = nullptr;
-        D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
-        D.out_off = b->out_off; D.n = n;
-        cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
-        cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
-        if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
-        SwPlan P;
-        auto plan = [&]() {
-            plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
-            D.pure = dpure;
-            if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
-            return device_plan_sw(D, sc, trace != 0, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) ==
-                   cudaSuccess;
-        };
-        if (!plan()) {
-            cudaGetLastError();
-            release_ctx(c);
-            if (err) *err = E_LAUNCH;
-            return GA_DEVICE_ERROR;
-        }
-        const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
-        auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
-            Carve k(base);
-            k.off = plan_bytes;
-            *ctr = k.take<int32_t>(64, 256);
-            *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-            *dirs = k.take<uint32_t>((size_t)S.dir_words);
-            return k.off;
-        };
-        int32_t *dctr, *dedge;
-        uint32_t* ddirs;
-        const uint64_t gen_before = c->dev_gen;
-        if (!ensure_dev(c, run_layout(nullptr, &dctr, &dedge, &ddirs))) {
-            release_ctx(c);
-            if (err) *err = E_ALLOC;
-            return GA_DEVICE_ERROR;
-        }
-        if (c->dev_gen != gen_before && !plan()) {      // the arena moved: plan again in the new one
-            cudaGetLastError();
-            release_ctx(c);
-            if (err) *err = E_LAUNCH;
-            return GA_DEVICE_ERROR;
-        }
-        run_layout(c->dev, &dctr, &dedge, &ddirs);
-        cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
-        int32_t rc = GA_OK;
-        if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
-                        dctr + 32, st, dscr) != cudaSuccess) {
-            cudaGetLastError();
-            if (err) *err = E_LAUNCH;
-            rc = GA_DEVICE_ERROR;
-        }
-        if (stream) {
-            cudaEventRecord(c->done, st);
-            c->pending = true;
-        } else if (cudaStreamSynchronize(st) != cudaSuccess) {
-            cudaGetLastError();
-            if (err) *err = E_SYNC;
-            rc = GA_DEVICE_ERROR;
-        }
-        release_ctx(c);
-        return rc;
-    }
-    // purity flags on the device, then lengths and flags to the host for the plan
-    {
-        Carve k(nullptr);
-        k.take<uint8_t>(2 * (size_t)n);
-        if (!ensure_dev(c, k.off) || !ensure_host(c, 2 * (size_t)n + 8 * (size_t)n + 1024)) {
-            release_ctx(c);
-            if (err) *err = E_ALLOC;
-            return GA_DEVICE_ERROR;
-        }
-    }
-    PairDesc D;
-    D.seq = b->seq; D.packed = nullptr; D.pure = reinterpret_cast<uint8_t*>(c->dev);
-    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
-    D.out_off = b->out_off; D.n = n;
-    uint8_t* hpure = reinterpret_cast<uint8_t*>(c->host);
-    int32_t* hlen = reinterpret_cast<int32_t*>(c->host + ((2 * (size_t)n + 255) & ~(size_t)255));
-    if (launch_pack(D, b->seq_bytes, nullptr, const_cast<uint8_t*>(D.pure), st) != cudaSuccess ||
-        cudaMemcpyAsync(hpure, D.pure, 2 * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(hlen, b->a_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(hlen + n, b->b_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaGetLastError();
-        release_ctx(c);
-        if (err) *err = E_D2H;
-        return GA_DEVICE_ERROR;
-    }
-    std::vector<uint8_t> pure(hpure, hpure + 2 * (size_t)n), skip(n, 0);
-    std::vector<int32_t> al(hlen, hlen + n), bl(hlen + n, hlen + 2 * n);
-    std::vector<int32_t> too_big;
-    for (int32_t i = 0; i < n; ++i)
-        if (cell_limit >= 0 && al[i] > 0 && bl[i] > 0 && ((int64_t)al[i] + 1) * ((int64_t)bl[i] + 1) > cell_limit) {
-            skip[i] = 1;
-            too_big.push_back(i);
-        }
-    SwPlan P;
-    plan_sw(n, al.data(), bl.data(), pure.data(), skip.data(), sc, trace != 0, T, P);
-    const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
-    const int64_t nw = P.words();
-    auto layout = [&](char* base, uint8_t** pp, int32_t** wk, int32_t** tb, int32_t** ctr, int32_t** edge,
-                      uint32_t** dirs) {
+    // the checkpointed kernels (score-only: sw16so and the score-only
+    // widths): purity and the plan on the device, one small record back,
+    // then the launches
+    auto plan_layout = [&](char* base, uint8_t** pp, int32_t** scr, int32_t** wk, long long** res) {
         Carve k(base);
         *pp = k.take<uint8_t>(2 * (size_t)n);
-        *wk = k.take<int32_t>(nw + 1);
-        *tb = k.take<int32_t>(too_big.size() + 1);
-        *ctr = k.take<int32_t>(64, 256);
-        *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-        *dirs = (trace || S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        *scr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+        *wk = k.take<int32_t>(2 * (size_t)n + 8);
+        *res = k.take<long long>(SP_RES);
         return k.off;
     };
     uint8_t* dpure;
-    int32_t *dwork, *dtb, *dctr, *dedge;
-    uint32_t* ddirs;
-    const size_t need = layout(nullptr, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
-    const size_t host_need = sizeof(int32_t) * (size_t)(nw + too_big.size() + 2);
-    const uint64_t gen_before = c->dev_gen;
-    if (!ensure_dev(c, need) || !ensure_host(c, host_need)) {
+    int32_t *dscr, *dwork;
+    long long* dres;
+    const size_t plan_bytes = plan_layout(nullptr, &dpure, &dscr, &dwork, &dres);
+    if (!ensure_dev(c, plan_bytes + 4096) || !ensure_host(c, sizeof(long long) * SP_RES)) {
         release_ctx(c);
         if (err) *err = E_ALLOC;
         return GA_DEVICE_ERROR;
     }
-    layout(c->dev, &dpure, &dwork, &dtb, &dctr, &dedge, &ddirs);
-    if (c->dev_gen != gen_before) cudaMemcpyAsync(dpure, pure.data(), 2 * (size_t)n, cudaMemcpyHostToDevice, st);
-    D.pure = dpure;
-    int32_t* hwork = reinterpret_cast<int32_t*>(c->host);
-    flatten_plan(P, hwork);
-    for (size_t q = 0; q < too_big.size(); ++q) hwork[nw + q] = too_big[q];
-    if (nw + (int64_t)too_big.size() > 0)
-        cudaMemcpyAsync(dwork, hwork, sizeof(int32_t) * (size_t)nw, cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+    long long* hres = reinterpret_cast<long long*>(c->host);
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
+    D.out_off = b->out_off; D.n = n;
     cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
     cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
     if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
-    int32_t rc = GA_OK;
-    if (!too_big.empty()) {
-        // too-large pairs report score -2
-        std::vector<int32_t> m2(too_big.size(), -2);
-        for (size_t q = 0; q < too_big.size(); ++q)
-            cudaMemcpyAsync(out_score + too_big[q], &m2[q], sizeof(int32_t), cudaMemcpyHostToDevice, st);
-        cudaStreamSynchronize(st);
+    SwPlan P;
+    auto plan = [&]() {
+        plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
+        D.pure = dpure;
+        if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
+        return device_plan_sw(D, sc, trace != 0, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) ==
+               cudaSuccess;
+    };
+    if (!plan()) {
+        cudaGetLastError();
+        release_ctx(c);
+        if (err) *err = E_LAUNCH;
+        return GA_DEVICE_ERROR;
     }
+    const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
+    auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
+        Carve k(base);
+        k.off = plan_bytes;
+        *ctr = k.take<int32_t>(64, 256);
+        *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+        *dirs = k.take<uint32_t>((size_t)S.dir_words);
+        return k.off;
+    };
+    int32_t *dctr, *dedge;
+    uint32_t* ddirs;
+    const uint64_t gen_before = c->dev_gen;
+    if (!ensure_dev(c, run_layout(nullptr, &dctr, &dedge, &ddirs))) {
+        release_ctx(c);
+        if (err) *err = E_ALLOC;
+        return GA_DEVICE_ERROR;
+    }
+    if (c->dev_gen != gen_before && !plan()) {      // the arena moved: plan again in the new one
+        cudaGetLastError();
+        release_ctx(c);
+        if (err) *err = E_LAUNCH;
+        return GA_DEVICE_ERROR;
+    }
+    run_layout(c->dev, &dctr, &dedge, &ddirs);
+    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+    int32_t rc = GA_OK;
     if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
-                    dctr + 32, st) != cudaSuccess) {
+                    dctr + 32, st, dscr) != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = E_LAUNCH;
         rc = GA_DEVICE_ERROR;
@@ -1877,11 +1679,10 @@ int32_t ga_profile_read(int32_t kernel_id, double* total_ms, int64_t* launches)
 
 const char* ga_profile_kernel_name(int32_t kernel_id)
 {
-    static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "sw8_score", "sw16_score",
-                                         "sw32_score", "sw8_trace", "sw16_trace", "sw32_trace", "int_peak",
-                                         "kmer_sketch", "mlp", "sw16x2_trace", "route", "sw_plan",
-                                         "sw16x2_score"};
-    return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : "";
+    static const char* names[K_COUNT] = {"pack2", "wfa_score", "wfa_trace", "wfa_lane", "wfa_routed",
+                                         "sw32_score", "sw32_trace", "sw16x2_trace", "sw16x2_score", "sw_plan",
+                                         "validate", "gene_qc", "int_peak", "kmer_sketch", "mlp", "route"};
+    return (kernel_id >= 0 && kernel_id < K_COUNT) ? names[kernel_id] : nullptr;
 }
 
 void ga_debug_fail_next(int32_t step) { g_fail_next.store(step); }

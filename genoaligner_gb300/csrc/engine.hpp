@@ -33,7 +33,10 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err);
 // The align_batch pipeline: validation, planning, transfer, kernels, and the
 // finish callback over every pair (in parallel).  Returns a GA_* status; on
 // failure *err is a static string and the callback has not run.
-int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, bool learned,
+// route: 0 plain, 1 queues by the cost model (plain when none is loaded), 2
+// queues by the exact lower bound alone.
+int route_mode(int requested);
+int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
                   const WfaFinish& fin, const char** err);
 
 // Per-pair outputs of one range of an SW batch (requests [base, base + n)),

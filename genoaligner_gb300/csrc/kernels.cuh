@@ -39,8 +39,8 @@ struct SwArgs {
     const int32_t* nwork_dev = nullptr;   // when set, the item count is read here at launch (device)
 };
 
-// Two pairs per warp in 16-bit lanes (sw16.cu): work holds 2 pair indices per
-// item, the second -1 when the item carries one pair.
+// Two pairs per warp in 16-bit lanes (sw16ck.cu): work holds 2 pair indices
+// per item, the second -1 when the item carries one pair.
 struct Sw16Args {
     PairDesc D;
     const int32_t* work;
@@ -100,8 +100,8 @@ int routed_max_slots(int smax, bool trace, int sm_count);
 int lane_max_slots(bool trace, int sm_count);
 // Fused sketch + lower bound + cost model + queue choice (learned.cu); then
 // the queues from the per-pair items (wfa_routed.cu).
-cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, int32_t* item, int32_t* lb, float* y,
-                               int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st);
+cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, bool model, int32_t* item, int32_t* lb,
+                               float* y, int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st);
 cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* starts, int2* big, int2* small,
                          cudaStream_t st);
 // The lane kernel over R.small, then the warp kernel over R.big and the
@@ -112,27 +112,26 @@ size_t wfa_smem_bytes(int smax);
 int wfa_max_slots(int smax, bool trace, int sm_count);
 cudaError_t launch_wfa(const WfaArgs& A, int slots, cudaStream_t st);
 
-int64_t sw_dir_words(int m, int n, int C);
-int sw_width_for(int n);
-int sw_maxc();                   // widest score-only 32-bit lane width (GA_SW_MAXC: 8, 16 or 32)
-int sw_max_slots(int C, bool trace, int sm_count);
-cudaError_t launch_sw(const SwArgs& A, int C, bool trace, int slots, cudaStream_t st);
+// Score-only 32-bit kernel (sw.cu): SW_SCORE_C columns per lane.
+constexpr int SW_SCORE_C = 8;
+int sw_max_slots(int sm_count);
+cudaError_t launch_sw(const SwArgs& A, int slots, cudaStream_t st);
 
 // Checkpointed traceback kernels (sw16ck.cu: two 16-bit pairs per warp;
 // sw32ck.cu: one 32-bit pair per warp); dir_slot = their *_dir_words.
-// The device-built traceback plan (sw_plan.cu).  Lists, in launch order: the
-// 16-bit lists of widths 8 / 16 / 32 columns per lane, then the 32-bit ones;
-// with the checkpointed kernels only list 0 (sw16ck), 3 (sw32ck short shape)
-// and 4 (sw32ck long shape) are used.  The record `res` (SP_RES long longs):
+// The device-built work plan (sw_plan.cu).  Lists, in launch order: the
+// 16-bit list (sw16ck, or sw16so score-only: two pairs per item), the 32-bit
+// list (sw32ck short shape, or sw_kernel score-only) and the 32-bit long-shape
+// list (sw32ck long shape; traceback only).  The record `res` (SP_RES long longs):
 // per list its pair count, its length in the flattened work array and its
 // offset there, the largest per-warp memory of its items (32-bit words), the
 // band-edge slot (2 * the longest text), the 16-bit list's largest item
 // (larger row count x larger column count of its two pairs), and the pairs
 // taken on the optimistic 16-bit rule only: their count and the largest
 // per-warp memory the 32-bit long-shape kernel would need for them.
-constexpr int SP_LISTS = 6, SP_L16 = 0, SP_L32 = 3, SP_L32LONG = 4;
-constexpr int SP_COUNT = 0, SP_INTS = 6, SP_BASE = 12, SP_DIR = 18, SP_EDGE = 24, SP_MAXC16 = 25, SP_NOPT = 26,
-              SP_DIROPT = 27, SP_RES = 28;
+constexpr int SP_LISTS = 3, SP_L16 = 0, SP_L32 = 1, SP_L32LONG = 2;
+constexpr int SP_COUNT = 0, SP_INTS = 3, SP_BASE = 6, SP_DIR = 9, SP_EDGE = 12, SP_MAXC16 = 13, SP_NOPT = 14,
+              SP_DIROPT = 15, SP_RES = 16;
 struct SwPlanArgs {
     PairDesc D;                  // a = text (rows), b = pattern (columns); D.pure set
     int32_t match, mismatch, gap_open, gap_extend;
@@ -142,8 +141,7 @@ struct SwPlanArgs {
     int32_t opt16_pct;           // optimistic 16-bit eligibility (sw16_eligible_opt), 100: the strict bound
     int32_t long_log2;           // sw32ck long shape above 2^long_log2 cells
     int32_t too_large_score;     // score written for pairs above cell_limit
-    int32_t score_only;          // 1: lists of the score-only kernels (sw16so; sw_kernel widths by sw_maxc)
-    int32_t maxc;                // sw_maxc() of the host
+    int32_t score_only;          // 1: lists of the score-only kernels (sw16so, sw_kernel)
     int32_t* out_score;
     int32_t* work;               // flattened work lists (2n + 8 ints)
     long long* res;              // the record above
@@ -166,8 +164,5 @@ int sw16so_max_slots(int sm_count);
 cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st);
 // blocks: the variant with the whole-block phase (items above A.coop_cells)
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st);
-int64_t sw16_dir_words(int M, int N, int C);
-int sw16_max_slots(int C, int sm_count);
-cudaError_t launch_sw16(const Sw16Args& A, int C, int slots, cudaStream_t st);
 
 }  // namespace ga

@@ -462,9 +462,13 @@ __global__ void __launch_bounds__(256) mlp_forward_tc_kernel(const __nv_bfloat16
 // window's own order); the A fragments read feature k = 16 c0 + 4 c1 + c2 as
 // hist[bin][r] - hist[bin][r + 16].  Features, bf16 rounding and the network
 // are those of ga_wfa_features + ga_mlp_forward_fast, so the prediction is the
-// same; nothing but the queue item (route.cuh) leaves the kernel.
+// same; nothing but the queue item (route.cuh) leaves the kernel.  MODEL =
+// false is the same pass without the network: the queue item comes from the
+// exact lower bound alone (the prediction replaced by log2(bound + 1)), for
+// measuring what the network adds.
 constexpr int RM_WARPS = 16;
 
+template <bool MODEL>
 __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* __restrict__ w, PairDesc D, int smax,
                                                           int lane_smax,
                                                           int32_t* __restrict__ item, int32_t* __restrict__ lb_out,
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* _
     TcSmem& S = *reinterpret_cast<TcSmem*>(rm_raw);
     int* hist_all = reinterpret_cast<int*>(rm_raw + sizeof(TcSmem));
     __shared__ int local[2 * ROUTE_BUCKETS];
-    load_tc_weights(S, w);
+    if (MODEL) load_tc_weights(S, w);
     if (threadIdx.x < 2 * ROUTE_BUCKETS) local[threadIdx.x] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, g = lane >> 2, tg = lane & 3;
@@ -533,18 +537,24 @@ __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* _
             if (c == 65) return nr * (1.0f / 256.0f);
             return 0.f;
         };
-        uint32_t a[TK1 / 16][4];
-#pragma unroll
-        for (int kt = 0; kt < TK1 / 16; ++kt) {
-            const int c0 = 16 * kt + 2 * tg, c1 = c0 + 8;
-            a[kt][0] = pack_bf16(X(r0, c0, m0, n0), X(r0, c0 + 1, m0, n0));
-            a[kt][1] = pack_bf16(X(r1, c0, m1, n1), X(r1, c0 + 1, m1, n1));
-            a[kt][2] = pack_bf16(X(r0, c1, m0, n0), X(r0, c1 + 1, m0, n0));
-            a[kt][3] = pack_bf16(X(r1, c1, m1, n1), X(r1, c1 + 1, m1, n1));
-        }
         float o[4];
-        tc_tile_forward(S, a, o);
         const int lb0 = __shfl_sync(FULL, lb, r0), lb1 = __shfl_sync(FULL, lb, r1);
+        if constexpr (MODEL) {
+            uint32_t a[TK1 / 16][4];
+#pragma unroll
+            for (int kt = 0; kt < TK1 / 16; ++kt) {
+                const int c0 = 16 * kt + 2 * tg, c1 = c0 + 8;
+                a[kt][0] = pack_bf16(X(r0, c0, m0, n0), X(r0, c0 + 1, m0, n0));
+                a[kt][1] = pack_bf16(X(r1, c0, m1, n1), X(r1, c0 + 1, m1, n1));
+                a[kt][2] = pack_bf16(X(r0, c1, m0, n0), X(r0, c1 + 1, m0, n0));
+                a[kt][3] = pack_bf16(X(r1, c1, m1, n1), X(r1, c1 + 1, m1, n1));
+            }
+            tc_tile_forward(S, a, o);
+        } else {
+            (void)X;
+            o[0] = o[1] = log2f((float)lb0 + 1.f);
+            o[2] = o[3] = log2f((float)lb1 + 1.f);
+        }
         if (tg == 0) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -575,17 +585,22 @@ static size_t route_model_smem() { return sizeof(TcSmem) + (size_t)RM_WARPS * 64
 
 // The fused routing pass over a WFA batch (D.packed and D.pure set): per pair
 // the queue item, lower bound and prediction; bucket totals into counts.
-cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, int32_t* item, int32_t* lb, float* y,
-                               int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st)
+// model = false: the queue items from the lower bound alone.
+cudaError_t launch_route_model(const PairDesc& D, int smax, int lane_smax, bool model, int32_t* item, int32_t* lb,
+                               float* y, int32_t* counts, int32_t* out_score, int32_t* out_len, cudaStream_t st)
 {
     const __nv_bfloat16* w = cost_model_weights();
-    if (!w) return cudaErrorNotReady;
+    if (model && !w) return cudaErrorNotReady;
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 16 * RM_WARPS - 1) / (16 * RM_WARPS);
-    if (blocks > 152) blocks = 152;
+    blocks = std::min(blocks, device_sms());
     launch_begin(K_MLP, st);
-    route_model_kernel<<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, lane_smax, item, lb, y, counts,
-                                                                          out_score, out_len);
+    if (model)
+        route_model_kernel<true><<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, lane_smax, item, lb, y,
+                                                                                    counts, out_score, out_len);
+    else
+        route_model_kernel<false><<<blocks, 32 * RM_WARPS, route_model_smem(), st>>>(w, D, smax, lane_smax, item, lb,
+                                                                                     y, counts, out_score, out_len);
     launch_end(K_MLP, st);
     return cudaGetLastError();
 }
@@ -595,7 +610,7 @@ static cudaError_t run_forward_tc(const __nv_bfloat16* w, const float* feat, int
     if (n <= 0) return cudaSuccess;
     prepare_mlp();
     int blocks = (n + 127) / 128;
-    if (blocks > 152 * 2) blocks = 152 * 2;
+    blocks = std::min(blocks, device_sms() * 2);
     launch_begin(K_MLP, st);
     mlp_forward_tc_kernel<<<blocks, 256, sizeof(TcSmem), st>>>(w, feat, n, y);
     launch_end(K_MLP, st);
@@ -644,7 +659,10 @@ void prepare_mlp()
         cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
         cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes());
         cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
-        cudaFuncSetAttribute(route_model_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)route_model_smem());
+        cudaFuncSetAttribute(route_model_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)route_model_smem());
+        cudaFuncSetAttribute(route_model_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)route_model_smem());
     });
 }
 
@@ -653,7 +671,7 @@ static cudaError_t run_forward(const __nv_bfloat16* w, const float* feat, int n,
     if (n <= 0) return cudaSuccess;
     prepare_mlp();
     int blocks = (n + TILE - 1) / TILE;
-    if (blocks > 152 * 2) blocks = 152 * 2;
+    blocks = std::min(blocks, device_sms() * 2);
     launch_begin(K_MLP, st);
     mlp_forward_kernel<<<blocks, 256, mlp_smem_bytes(), st>>>(w, feat, n, y);
     launch_end(K_MLP, st);
@@ -667,7 +685,7 @@ static cudaError_t run_backward(const __nv_bfloat16* w, const float* feat, const
     cudaMemsetAsync(grad, 0, NPARAM * sizeof(float), st);
     cudaMemsetAsync(loss, 0, sizeof(float), st);
     int blocks = (n + TILE - 1) / TILE;
-    if (blocks > 152 * 2) blocks = 152 * 2;
+    blocks = std::min(blocks, device_sms() * 2);
     launch_begin(K_MLP, st);
     mlp_backward_kernel<<<blocks, 256, mlp_smem_bytes(), st>>>(w, feat, target, n, 1.0f / (float)n, grad, loss);
     launch_end(K_MLP, st);
@@ -678,7 +696,7 @@ cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStrea
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 7) / 8;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    blocks = std::min(blocks, device_sms() * 16);
     launch_begin(K_SKETCH, st);
     if (D.packed) sketch_packed_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
     else sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);

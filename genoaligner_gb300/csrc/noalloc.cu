@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "../../include/genoaligner_gb300.h"
 #include "kernels.cuh"
 
@@ -21,26 +23,70 @@ namespace ga {
 constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)16 << 20;   // 16 MiB per GPU
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device ordinal, looked up on the
-// first call made with that device current.  The name is a host-side stand-in
-// in host code, so only this address may be handed to a kernel.
+// Device address of g_noalloc_scratch.  In host code the array's name is a
+// host-side stand-in, so only the address cudaGetSymbolAddress returns may be
+// handed to a kernel.  The address belongs to the CUDA context the library's
+// module is loaded in: it is looked up on the first call made in a context
+// (with its device current) and kept with that context's unique id
+// (cuCtxGetId, reached through cudaGetDriverEntryPointByVersion, so the
+// library does not link the driver library).  A call in another context --
+// after cudaDeviceReset, or with a context of the caller's own made current --
+// looks it up again.  When the driver entry points cannot be had, every call
+// looks the address up (cudaGetSymbolAddress allocates nothing).
 constexpr int NOALLOC_MAX_DEVICES = 64;
+struct ScratchAddr {
+    unsigned char* addr = nullptr;
+    unsigned long long ctx_id = 0;
+};
 static std::mutex g_noalloc_mu;
-static unsigned char* g_noalloc_addr[NOALLOC_MAX_DEVICES];
+static ScratchAddr g_noalloc_addr[NOALLOC_MAX_DEVICES];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context; false when there is
+// none or the driver entry points are unavailable.
+static bool current_ctx_id(unsigned long long* id)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return false;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 static unsigned char* noalloc_scratch(int dev)
 {
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return nullptr;
+    unsigned long long id = 0;
+    bool have_id = current_ctx_id(&id);
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
-            cudaGetLastError();
-            return nullptr;
-        }
-        g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+    ScratchAddr& s = g_noalloc_addr[dev];
+    if (s.addr && have_id && s.ctx_id == id) return s.addr;
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return nullptr;
     }
-    return g_noalloc_addr[dev];
+    // the lookup makes the device's primary context current if none was
+    if (!have_id) have_id = current_ctx_id(&id);
+    s.addr = have_id ? static_cast<unsigned char*>(p) : nullptr;
+    s.ctx_id = id;
+    return static_cast<unsigned char*>(p);
 }
 
 static inline size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -53,10 +99,14 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
                                          int32_t* out_score, int32_t* out_len, char* out_cigar, void* stream,
                                          const char** err)
 {
-    if (!b || b->n < 0 || smax < 0 ||
+    if (!b || b->n < 0 || b->seq_bytes < 0 ||
         (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len || !out_score ||
                       (trace && (!out_len || !out_cigar || !b->out_off))))) {
         if (err) *err = "invalid device batch";
+        return GA_INVALID_ARGUMENT;
+    }
+    if (smax < 0 || smax > GA_MAX_SMAX_DEVICE) {
+        if (err) *err = "smax out of range [0, GA_MAX_SMAX_DEVICE]";
         return GA_INVALID_ARGUMENT;
     }
     if (((uintptr_t)b->seq & 15) != 0) {
@@ -70,7 +120,7 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
     const size_t pure_bytes = round256(2 * (size_t)b->n);
     const size_t packed_bytes = round256((size_t)packed_arena_words(b->seq_bytes) * sizeof(uint64_t));
     const size_t fixed = head + pure_bytes + packed_bytes;
-    const size_t slot_bytes = (size_t)(smax + 1) * (size_t)(smax + 1) * sizeof(int32_t);
+    const size_t slot_bytes = (size_t)((int64_t)smax + 1) * (size_t)((int64_t)smax + 1) * sizeof(int32_t);
     if (fixed + (trace ? 4 * slot_bytes : 0) > NOALLOC_SCRATCH_BYTES) {
         if (err) *err = "batch needs more than the 16 MiB no-allocation scratch: split it or use ga_wfa_device";
         return GA_INVALID_ARGUMENT;
@@ -98,6 +148,8 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
         const int64_t fit = (int64_t)((NOALLOC_SCRATCH_BYTES - fixed) / slot_bytes) / 4 * 4;
         slots = (int)std::min<int64_t>(slots, fit);
     }
+    // pairs per counter increment, as the allocating entry takes them
+    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, (int64_t)b->n / ((int64_t)slots * 8)));
     cudaStream_t st = (cudaStream_t)stream;
     // the counter and error word keep the previous call's values: clear them
     if (cudaMemsetAsync(ctr, 0, head, st) != cudaSuccess) {
@@ -112,8 +164,9 @@ extern "C" int32_t ga_wfa_device_noalloc(const ga_device_batch* b, int32_t smax,
     WfaArgs A;
     A.D = D; A.smax = smax; A.trace = trace ? 1 : 0;
     A.out_score = out_score; A.out_len = out_len; A.out_cigar = out_cigar;
-    A.stack = stk; A.stack_slot = (int64_t)(smax + 1) * (smax + 1);
+    A.stack = stk; A.stack_slot = ((int64_t)smax + 1) * ((int64_t)smax + 1);
     A.counter = ctr; A.err = ctr + 1;
+    A.chunk = chunk;
     if (launch_pack(D, b->seq_bytes, packed, pure, st) != cudaSuccess || launch_wfa(A, slots, st) != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = "kernel launch failed";

@@ -98,8 +98,8 @@ cudaError_t launch_qc(const PairDesc& D, const int32_t* score, const int32_t* po
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    launch_begin(K_SWPLAN, st);
+    blocks = std::min(blocks, device_sms() * 16);
+    launch_begin(K_QC, st);
     qc_kernel<<<blocks, 128, 0, st>>>(D, score, pos, len, cig, frame, code, out);
     launch_end(K_SWPLAN, st);
     return cudaGetLastError();

@@ -50,11 +50,8 @@ __global__ void sp_classify_kernel(SwPlanArgs P)
                     atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_DIROPT),
                               (unsigned long long)sw32ck_dir_words(m, nn, 0));
                 }
-                // score-only 32-bit pairs: one list per lane width of sw_kernel
-                const int C = (nn <= 256 || P.maxc == 8) ? 8 : ((nn <= 512 || P.maxc == 16) ? 16 : 32);
                 const int list = u16 ? SP_L16
-                                     : (P.score_only ? SP_L32 + (C == 8 ? 0 : (C == 16 ? 1 : 2))
-                                                     : (sw32ck_long(m, nn, P.long_log2) ? SP_L32LONG : SP_L32));
+                                     : ((!P.score_only && sw32ck_long(m, nn, P.long_log2)) ? SP_L32LONG : SP_L32);
                 it = list * SP_NB + (u16 ? sp_key16(m, nn) : sp_key(m, nn));
                 atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_EDGE), (unsigned long long)(2 * max(m, 0)));
             }
@@ -95,7 +92,7 @@ __global__ void sp_scan_kernel(SwPlanArgs P)
     if (threadIdx.x == 0) {
         long long base = 0;
         for (int l = 0; l < SP_LISTS; ++l) {
-            const long long ints = l < 3 ? 2 * ((total[l] + 1) / 2) : total[l];
+            const long long ints = l == SP_L16 ? 2 * ((total[l] + 1) / 2) : total[l];
             P.res[SP_COUNT + l] = total[l];
             P.res[SP_INTS + l] = ints;
             P.res[SP_BASE + l] = base;
@@ -133,7 +130,7 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
         int32_t* w = P.work + P.res[SP_BASE + l];
         unsigned long long* mx = reinterpret_cast<unsigned long long*>(P.res + SP_DIR + l);
         unsigned long long local = 0, cmax = 0;
-        if (l < 3) {
+        if (l == SP_L16) {
             const long long items = (cnt + 1) / 2;
             for (long long q = blockIdx.x * blockDim.x + threadIdx.x; q < items; q += stride) {
                 const int a = srt[2 * q], b = 2 * q + 1 < cnt ? srt[2 * q + 1] : -1;
@@ -219,11 +216,11 @@ cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, con
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    launch_begin(K_SWPLAN, st);
+    blocks = std::min(blocks, device_sms() * 16);
+    launch_begin(K_VALIDATE, st);
     sw_validate_kernel<<<blocks, 128, 0, st>>>(D, sc.match, sc.mismatch, sc.gap_open, sc.gap_extend, score, pos, len,
                                                cig, flags);
-    launch_end(K_SWPLAN, st);
+    launch_end(K_VALIDATE, st);
     return cudaGetLastError();
 }
 
@@ -240,7 +237,7 @@ cudaError_t launch_sw_plan(SwPlanArgs P, int32_t* scratch, cudaStream_t st)
     if (e == cudaSuccess) e = cudaMemsetAsync(P.res, 0, sizeof(long long) * SP_RES, st);
     if (e != cudaSuccess || n <= 0) return e;
     int blocks = (n + 255) / 256;
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    blocks = std::min(blocks, device_sms() * 8);
     launch_begin(K_SWPLAN, st);
     sp_classify_kernel<<<blocks, 256, 0, st>>>(P);
     launch_end(K_SWPLAN, st);

@@ -268,14 +268,14 @@ cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, 
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (2 * D.n + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
+    blocks = std::min(blocks, device_sms() * 32);
     if (packed) {
         // every sequence ends >= 64 bytes before the arena's end, so the whole
         // chunks cover them all and no read passes seq_bytes
         const int64_t nchunks = seq_bytes / 32;
         uint32_t* bad = reinterpret_cast<uint32_t*>(packed + nchunks + 2);
         int64_t cblocks = (nchunks + 255) / 256;
-        if (cblocks > 152 * 32) cblocks = 152 * 32;
+        cblocks = std::min<int64_t>(cblocks, device_sms() * 32);
         launch_begin(K_PACK, st);
         pack_chunks_kernel<<<(int)cblocks, 256, 0, st>>>(D.seq, nchunks, packed, bad);
         launch_end(K_PACK, st);
@@ -297,7 +297,7 @@ cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* p
     const int64_t nchunks = seq_bytes / 32;
     if (nchunks <= 0) return cudaSuccess;
     int64_t cblocks = (nchunks + 255) / 256;
-    if (cblocks > 152 * 32) cblocks = 152 * 32;
+    cblocks = std::min<int64_t>(cblocks, device_sms() * 32);
     launch_begin(K_PACK, st);
     pack_chunks_kernel<<<(int)cblocks, 256, 0, st>>>(seq, nchunks, packed, bad);
     launch_end(K_PACK, st);
@@ -348,10 +348,10 @@ cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const i
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 127) / 128;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    launch_begin(K_PACK, st);
+    blocks = std::min(blocks, device_sms() * 16);
+    launch_begin(K_VALIDATE, st);
     wfa_validate_kernel<<<blocks, 128, 0, st>>>(D, score, len, cig, flags);
-    launch_end(K_PACK, st);
+    launch_end(K_VALIDATE, st);
     return cudaGetLastError();
 }
 

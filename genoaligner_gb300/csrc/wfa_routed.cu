@@ -512,7 +512,7 @@ cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* s
 {
     if (n <= 0) return cudaSuccess;
     int blocks = (n + 255) / 256;
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    blocks = std::min(blocks, device_sms() * 8);
     launch_begin(K_ROUTE, st);
     route_scan_kernel<<<1, 32, 0, st>>>(counts, starts);
     launch_end(K_ROUTE, st);
@@ -551,17 +551,16 @@ int lane_max_slots(bool trace, int sm_count)
 
 cudaError_t launch_routed(const RoutedArgs& R, int lane_slots, int slots, cudaStream_t st)
 {
-    const int id = R.A.trace ? K_WFA_TRACE : K_WFA_SCORE;
     const size_t lsm = (size_t)4 * LANE_WARP_SMEM * sizeof(uint32_t);
-    launch_begin(id, st);
+    launch_begin(K_WFA_LANE, st);
     if (R.A.trace) wfa_lane_kernel<true><<<(lane_slots + 3) / 4, 128, lsm, st>>>(R);
     else wfa_lane_kernel<false><<<(lane_slots + 3) / 4, 128, lsm, st>>>(R);
-    launch_end(id, st);
+    launch_end(K_WFA_LANE, st);
     const size_t smem = (size_t)4 * R.warp_smem * sizeof(int32_t);
-    launch_begin(id, st);
+    launch_begin(K_WFA_ROUTED, st);
     if (R.A.trace) wfa_routed_kernel<true><<<(slots + 3) / 4, 128, smem, st>>>(R);
     else wfa_routed_kernel<false><<<(slots + 3) / 4, 128, smem, st>>>(R);
-    launch_end(id, st);
+    launch_end(K_WFA_ROUTED, st);
     return cudaGetLastError();
 }
 

@@ -34,6 +34,10 @@ extern "C" {
 
 /* Largest smax the drop-in entry accepts (src/api/api.cpp:227). */
 #define GA_MAX_SMAX 511
+/* Largest smax the extension and device-resident WFA entries accept: one
+ * warp's wavefronts (2 * (2 smax + 3) offsets) must fit the shared memory of
+ * a block of four warps. */
+#define GA_MAX_SMAX_DEVICE 3500
 /* Per-pair direction-table limit of the drop-in SW entry, in cells
  * (include/genoaligner/api.hpp:256). */
 #define GA_SW_MAX_TRACE_CELLS (1 << 26)
@@ -136,8 +140,12 @@ int32_t ga_align_sw_batch(const ga_sw_request* reqs, int32_t n, ga_sw_result* re
 /* Options of the extension entries (include/genoaligner/ext.hpp).  Zero
  * fields take the defaults noted. */
 typedef struct ga_options {
-    int32_t max_smax;          /* accepted smax bound; 0 = 511 (the drop-in bound) */
-    int32_t learned;           /* 1 = route pairs by the learned cost model */
+    int32_t max_smax;          /* accepted smax bound; 0 = 511 (the drop-in bound);
+                                  values above GA_MAX_SMAX_DEVICE count as it */
+    int32_t learned;           /* 1 = route pairs by the learned cost model;
+                                  2 = the same queues keyed by the exact q-gram
+                                  lower bound alone (no network: the ablation
+                                  that shows what the model adds) */
     int64_t trace_cell_limit;  /* SW per-pair trace limit in cells; 0 = 2^26, <0 = none */
     int32_t reserved[4];
 } ga_options;
@@ -203,6 +211,14 @@ int32_t ga_wfa_device_ex(const ga_device_batch* batch, int32_t smax, int32_t tra
  * Synchronises the device. */
 int32_t ga_wfa_route_stats(int32_t* out, int32_t max);
 
+/* Queue item of every pair of the calling thread's last learned WFA call
+ * (out[n], host memory; n must be that call's pair count): -1 = unresolved
+ * by the lower bound without search; otherwise bits 0-7 = the bucket (below
+ * 32: the warp queue, keyed by the bit length of the estimated distance; 32 +
+ * s: the lane queue with first smax s) and bits 8 and up = the smax the pair
+ * is first run with.  Synchronises the device. */
+int32_t ga_wfa_route_items(int32_t* out, int32_t n);
+
 /* SW over a device batch, score + end cell + start cell + CIGAR.
  * out_pos[4*i .. 4*i+3] = start_i, start_j, end_i, end_j.  Pairs above
  * trace_cell_limit cells (< 0: no limit) get out_score = -2 (too large).
@@ -260,12 +276,19 @@ int32_t ga_mlp_train_step(const float* features, const float* targets, int32_t n
  * (smax+1)^2 * 4 bytes; a larger batch is refused with GA_INVALID_ARGUMENT and
  * a message, before any device work.
  *
- * The first call on a device, made with that device current, resolves the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  Every call shares the one array: calls whose work can
- * overlap on the GPU (different streams, or threads that do not order their
- * calls) race on it and must be serialised by the caller.  stream NULL runs on
- * the legacy default stream and synchronises before returning. */
+ * smax above GA_MAX_SMAX_DEVICE, or a negative seq_bytes, is refused with
+ * GA_INVALID_ARGUMENT.
+ *
+ * The first call in a CUDA context (normally: the first call on a device, made
+ * with that device current) resolves the array's device address
+ * (cudaGetSymbolAddress) and keeps it with the context's id; a call in another
+ * context, such as after cudaDeviceReset, resolves it again.  Make the first
+ * call before any stream capture.  Every call shares the one array: calls
+ * whose work can overlap on the GPU (different streams, or threads that do not
+ * order their calls) race on it and must be serialised by the caller.  stream
+ * NULL runs on the legacy default stream and synchronises before returning;
+ * with a stream the call returns once its work is enqueued, and the caller
+ * orders the next call after it. */
 int32_t ga_wfa_device_noalloc(const ga_device_batch* batch, int32_t smax, int32_t trace,
                               int32_t* out_score, int32_t* out_len, char* out_cigar,
                               void* stream, const char** err);

@@ -25,6 +25,7 @@ from __future__ import annotations
 import ctypes
 import os
 import subprocess
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -76,7 +77,7 @@ def lib():
         L.ora_sw_batch.argtypes = [i32, p, p, p, p, p, p, i32, i32, i32, i32, i32, p,
                                    ctypes.c_longlong, i32, p, p, p, i32]
         L.ora_sw_batch.restype = ctypes.c_int
-        L.ora_edit_distance_batch.argtypes = [i32, p, p, p, p, p, p, p]
+        L.ora_edit_distance_batch.argtypes = [i32, p, p, p, p, p, p, p, i32]
         L.ora_edit_distance_batch.restype = ctypes.c_int
         ip = ctypes.POINTER(ctypes.c_int)
         L.ora_wfa_validate.argtypes = [ctypes.c_char_p, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, i32, ip, ip]
@@ -136,6 +137,7 @@ class WfaBatch:
     cigars: list = field(default_factory=list)
     resolved_count: int = 0
     unresolved_count: int = 0
+    seconds: float = 0.0               # wall time of the C restatement's call alone
 
 
 @dataclass
@@ -154,6 +156,7 @@ class SwBatch:
     cigars: list = field(default_factory=list)
     resolved_count: int = 0
     unresolved_count: int = 0
+    seconds: float = 0.0               # wall time of the C restatement's call alone
 
 
 def _default_wfa(n, status, error):
@@ -204,12 +207,16 @@ def wfa_batch(patterns, texts, smax=64, with_cigar=True, threads=None,
         np.cumsum(cig_len_cap[:-1], out=cig_off[1:])
     cigbuf = np.zeros(int(cig_len_cap.sum()) + 8, np.uint8)
     out = np.zeros(n, WFA_OUT)
-    rc = lib().ora_wfa_batch(n, _ptr(pbuf), _ptr(poff), _ptr(plen), _ptr(tbuf), _ptr(toff),
-                             _ptr(tlen), bsmax, int(trace), cap, _ptr(cigbuf), _ptr(cig_off),
-                             _ptr(out), threads or os.cpu_count() or 1)
+    L = lib()
+    t0 = time.perf_counter()
+    rc = L.ora_wfa_batch(n, _ptr(pbuf), _ptr(poff), _ptr(plen), _ptr(tbuf), _ptr(toff),
+                         _ptr(tlen), bsmax, int(trace), cap, _ptr(cigbuf), _ptr(cig_off),
+                         _ptr(out), threads or os.cpu_count() or 1)
+    t1 = time.perf_counter()
     if rc != 0:
         raise MemoryError("oracle worker allocation failed")
     b = WfaBatch()
+    b.seconds = t1 - t0
     b.score = out["score"].copy()
     b.resolved = out["resolved"].astype(bool)
     b.rescore_ok = out["rescore_ok"].astype(bool)
@@ -298,13 +305,17 @@ def sw_batch(texts, patterns, scoring=(2, -3, 5, 2), with_cigar=True, threads=No
     out = np.zeros(n, SW_OUT)
     m_, x_, go, ge = schemes[0]
     want_u8 = wants.astype(np.uint8)            # must outlive the call below
-    rc = lib().ora_sw_batch(n, _ptr(tbuf), _ptr(toff), _ptr(tlen), _ptr(pbuf), _ptr(poff),
-                            _ptr(plen), m_, x_, go, ge, int(trace),
-                            _ptr(want_u8), dir_limit, cap, _ptr(cigbuf),
-                            _ptr(cig_off), _ptr(out), threads or os.cpu_count() or 1)
+    L = lib()
+    t0 = time.perf_counter()
+    rc = L.ora_sw_batch(n, _ptr(tbuf), _ptr(toff), _ptr(tlen), _ptr(pbuf), _ptr(poff),
+                        _ptr(plen), m_, x_, go, ge, int(trace),
+                        _ptr(want_u8), dir_limit, cap, _ptr(cigbuf),
+                        _ptr(cig_off), _ptr(out), threads or os.cpu_count() or 1)
+    t1 = time.perf_counter()
     if rc != 0:
         raise MemoryError("oracle worker allocation failed")
     b = SwBatch()
+    b.seconds = t1 - t0
     for f in ("score", "start_i", "start_j", "end_i", "end_j"):
         setattr(b, f, out[f].copy())
     for f in ("resolved", "rescore_ok", "wellformed_ok", "too_large"):
@@ -316,12 +327,16 @@ def sw_batch(texts, patterns, scoring=(2, -3, 5, 2), with_cigar=True, threads=No
     return b
 
 
-def edit_distance(patterns, texts):
-    """Levenshtein distances by the O(mn) DP (src/reference/edit_distance_cpu.hpp)."""
+def edit_distance(patterns, texts, threads=1, timing=False):
+    """Levenshtein distances by the O(mn) DP (src/reference/edit_distance_cpu.hpp).
+    With timing=True returns (distances, seconds of the C call alone)."""
     n = len(patterns)
     pbuf, poff, plen = pack([bytes(p) for p in patterns])
     tbuf, toff, tlen = pack([bytes(t) for t in texts])
     out = np.zeros(n, np.int32)
-    lib().ora_edit_distance_batch(n, _ptr(pbuf), _ptr(poff), _ptr(plen), _ptr(tbuf),
-                                  _ptr(toff), _ptr(tlen), _ptr(out))
-    return out
+    L = lib()
+    t0 = time.perf_counter()
+    L.ora_edit_distance_batch(n, _ptr(pbuf), _ptr(poff), _ptr(plen), _ptr(tbuf),
+                              _ptr(toff), _ptr(tlen), _ptr(out), int(threads or 1))
+    t1 = time.perf_counter()
+    return (out, t1 - t0) if timing else out

@@ -691,11 +691,27 @@ int ora_sw_batch(int32_t n, const char* tbuf, const int64_t* toff, const int32_t
 /* Batch edit distance (score cross-check). */
 typedef struct { ora_job* J; int32_t* out; } ed_arg;
 
+static void* ed_worker(void* arg)
+{
+    ora_job* J = (ora_job*)arg;
+    int32_t* out = (int32_t*)J->out;
+    int lo, hi;
+    while (job_take(J, 64, &lo, &hi))
+        for (int i = lo; i < hi; ++i)
+            out[i] = ora_edit_distance(J->pbuf + J->poff[i], J->plen[i], J->tbuf + J->toff[i], J->tlen[i]);
+    return NULL;
+}
+
+/* edit_distance_cpu over a batch, on `threads` threads. */
 int ora_edit_distance_batch(int32_t n, const char* pbuf, const int64_t* poff, const int32_t* plen,
                             const char* tbuf, const int64_t* toff, const int32_t* tlen,
-                            int32_t* out)
+                            int32_t* out, int32_t threads)
 {
-    for (int i = 0; i < n; ++i)
-        out[i] = ora_edit_distance(pbuf + poff[i], plen[i], tbuf + toff[i], tlen[i]);
-    return 0;
+    ora_job J;
+    memset(&J, 0, sizeof(J));
+    J.pbuf = pbuf; J.poff = poff; J.plen = plen;
+    J.tbuf = tbuf; J.toff = toff; J.tlen = tlen;
+    J.n = n;
+    J.out = out;
+    return run_workers(&J, ed_worker, threads);
 }

@@ -81,3 +81,57 @@ def test_noalloc_refuses_oversized_batch():
     assert st == api.GA_INVALID_ARGUMENT
     assert b"16 MiB" in err.value
     assert int((got[0] == -9).sum()) == ps.n                  # nothing ran
+
+
+def test_noalloc_on_a_caller_stream_and_large_smax():
+    """A call on the caller's own stream returns once enqueued; after that
+    stream is synchronised the results equal the allocating entry's.  A trace
+    call at smax 600 (four stacks of 601^2 ints, most of the scratch) checks
+    the slot arithmetic near the array's end."""
+    torch = pytest.importorskip("torch")
+    f = _noalloc()
+    ps = workloads.wfa_mixed(n=3000, seed=21)
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device="cuda")
+    s = torch.cuda.Stream()
+    for smax in (64, 600):
+        ref = _outputs(torch, batch, -7)
+        api.wfa_device(batch, smax, True, *ref)
+        for _ in range(2):
+            got = _outputs(torch, batch, -9)
+            torch.cuda.synchronize()
+            err = ctypes.c_char_p()
+            st = f(ctypes.byref(batch.c), smax, 1, got[0].data_ptr(), got[1].data_ptr(), got[2].data_ptr(),
+                   ctypes.c_void_p(s.cuda_stream), ctypes.byref(err))
+            assert st == api.GA_OK, (smax, err.value)
+            s.synchronize()
+            assert torch.equal(got[0], ref[0]), smax
+            assert torch.equal(got[1], ref[1]), smax
+            assert torch.equal(got[2], ref[2]), smax
+
+
+def test_noalloc_empty_batch_and_refusals():
+    torch = pytest.importorskip("torch")
+    f = _noalloc()
+    ps = workloads.wfa_150bp_2pct(n=64, seed=22)
+    batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device="cuda")
+    got = _outputs(torch, batch, -9)
+    err = ctypes.c_char_p()
+    empty = api.DeviceBatch(batch.c.seq, batch.c.seq_bytes, batch.c.a_off, batch.c.a_len, batch.c.b_off,
+                            batch.c.b_len, batch.c.out_off, 0, 0)
+    assert f(ctypes.byref(empty), 64, 1, None, None, None, None, ctypes.byref(err)) == api.GA_OK
+    # an arena that does not start on a 16-byte boundary
+    odd = api.DeviceBatch(batch.c.seq + 8, batch.c.seq_bytes - 8, batch.c.a_off, batch.c.a_len, batch.c.b_off,
+                          batch.c.b_len, batch.c.out_off, batch.n, 0)
+    st = f(ctypes.byref(odd), 64, 1, got[0].data_ptr(), got[1].data_ptr(), got[2].data_ptr(), None,
+           ctypes.byref(err))
+    assert st == api.GA_INVALID_ARGUMENT and b"16-byte" in err.value
+    # smax beyond the device entries' bound, and a negative arena size
+    st = f(ctypes.byref(batch.c), api.GA_MAX_SMAX_DEVICE + 1, 0, got[0].data_ptr(), None, None, None,
+           ctypes.byref(err))
+    assert st == api.GA_INVALID_ARGUMENT
+    neg = api.DeviceBatch(batch.c.seq, -32, batch.c.a_off, batch.c.a_len, batch.c.b_off, batch.c.b_len,
+                          batch.c.out_off, batch.n, 0)
+    st = f(ctypes.byref(neg), 64, 0, got[0].data_ptr(), None, None, None, ctypes.byref(err))
+    assert st == api.GA_INVALID_ARGUMENT
+    torch.cuda.synchronize()
+    assert int((got[0] == -9).sum()) == ps.n                  # nothing ran
