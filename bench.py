@@ -69,6 +69,10 @@ def parse():
                     help="keep the device's current kernel setting instead of autotuning on the batch")
     ap.add_argument("--only", choices=["wfa_150bp", "wfa_mixed_1m", "wfa_long", "sw_long", "sw_score_only"],
                     help="run one of the extra workloads alone (no CPU baseline) and print its JSON")
+    ap.add_argument("--set-tune", default=None,
+                    help="kernel setting fields k=v[,k=v...] set before any run (and no autotuning), e.g. sw_pack16=0")
+    ap.add_argument("--only-pairs", type=int, default=None,
+                    help="with --only: the workload's first N pairs instead of all (small profiling cases)")
     return ap.parse_args()
 
 
@@ -384,7 +388,8 @@ def route_report(items, score, smax, lane_smax, classes, lane_ok):
     length; a pair unresolved at smax belongs in the warp queue at the top
     bucket, or is proven unresolved by the bound).  Per class: pairs in each
     queue, queue mispredictions (queue differs from the exact one), lane-queue
-    pairs first run below their distance (they escalate), warp-queue pairs
+    pairs whose predicted first smax is below their distance (a lane runs its
+    pair on past it: an under-prediction, not a rerun), warp-queue pairs
     whose bucket differs from the exact one."""
     d = score.astype(np.int64)
     unres = d < 0
@@ -406,7 +411,7 @@ def route_report(items, score, smax, lane_smax, classes, lane_ok):
         out[name] = {"pairs": int(sel.sum()), "lane_queue": nl, "warp_queue": nw,
                      "unresolved_by_bound": int((bound & sel).sum()),
                      "queue_mispredicted_rate": qmis / max(1, int(sel.sum())),
-                     "lane_escalation_rate": esc / max(1, nl),
+                     "lane_underpredicted_rate": esc / max(1, nl),
                      "warp_bucket_mispredicted_rate": boff / max(1, nw)}
     return out
 
@@ -463,11 +468,11 @@ def wfa_e2e(api, ps, smax, learned, steps):
     return statistics.median(t) * 1e3, h2d, d2h, r
 
 
-def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep):
+def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep, n_pairs=None):
     """1,000,000 mixed-divergence pairs: plain fixed smax 64, the
     learned-bucketed form and the lower-bound-only queues, bit-exact check,
     misprediction rates per divergence class, end to end (learned form)."""
-    ps = workloads.wfa_mixed()
+    ps = workloads.wfa_mixed(n=n_pairs or 1_000_000)
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
     out = {"workload": "wfa_mixed_1m: 1,000,000 pairs, 150-250 bp, error 70% U[0,2%] / 25% U[2,10%] / "
@@ -490,12 +495,12 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep):
     return out
 
 
-def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep):
+def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep, n_pairs=None):
     """The long WFA batch at smax 2048: the plain form (one pair per warp, in
     batch order), the learned-bucketed form (queues by estimated distance,
     largest first; pairs estimated at s >= 256 on whole blocks) and the same
     queues keyed by the lower bound alone."""
-    ps = workloads.wfa_long_1k_10k()
+    ps = workloads.wfa_long_1k_10k(n=n_pairs or 2_000)
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
     out = {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR",
@@ -531,7 +536,7 @@ def sw_long_subset(full):
     return np.concatenate([order[:64], rng.choice(order[64:], size=64, replace=False)])
 
 
-def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep):
+def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep, tune=True):
     """The long SW batch (2-30 kb queries, 0-5 kb flanks), or its first n_pairs."""
     ps = workloads.sw_long_4k(n=n_pairs)
     cells = sw_cells(ps)
@@ -548,7 +553,10 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep):
     # per block), then the plain single-variant form: every pair one per warp
     # in 32 bits
     saved = api.tune_get()
-    chosen, trials = api.autotune_sw(batch, SCORING, sc, pos, ln, cg, reps=1)
+    if tune:
+        chosen, trials = api.autotune_sw(batch, SCORING, sc, pos, ln, cg, reps=1)
+    else:
+        chosen, trials = saved, []
     fn()
     ms = timed(fn, stream, 1)
     out = sc.cpu().numpy().copy(), ln.cpu().numpy().copy()
@@ -557,6 +565,22 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep):
         ends = slot_ends(batch)[idx]
         keep["sw_long"] = {"ps": ps.subset(idx), "device": (out[0][idx], pos.cpu().numpy().reshape(-1, 4)[idx],
                                                              out[1][idx], cg.cpu().numpy(), ends)}
+    # the SW variant model's routing: pure pairs beyond the proven 16-bit
+    # bound try the 16-bit kernel when the model predicts their score fits
+    # (the two-pairs-per-warp kernel on, the tuned fields otherwise kept)
+    learned = None
+    from genoaligner_gb300 import sw_model
+    if sw_model.load_default():
+        api.tune_set(**dict(chosen, sw_pack16=1))
+        fl = lambda: api.sw_device(batch, SCORING, True, sc, pos, ln, cg, stream=stream.cuda_stream,
+                                   trace_cell_limit=-1, learned=True)
+        fl()
+        ms_l = timed(fl, stream, 1)
+        learned = {"form": "the autotuner's setting with sw_pack16 1 and the 16-bit choice by the SW variant model",
+                   "gcups": cells / (ms_l * 1e-3) / 1e9, "ms_per_step": ms_l,
+                   "bit_identical_to_tuned": bool(np.array_equal(out[0], sc.cpu().numpy()) and
+                                                  np.array_equal(out[1], ln.cpu().numpy()))}
+        api.tune_set(**chosen)
     api.tune_set(**dict(saved, sw_pack16=0, sw_coop_log2=40))
     fn()
     ms_plain = timed(fn, stream, 1)
@@ -566,6 +590,7 @@ def bench_sw_long(api, workloads, torch, dev, stream, n_pairs, keep):
                         "scoring {2,-3,3,1}, score+CIGAR, no trace-cell limit",
             "gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "cells": cells,
             "tune": {"chosen": chosen, "trials": [dict(t, ms=round(m, 1)) for t, m in trials]},
+            "learned_variant": learned,
             "plain_single_variant": {"form": "every pair one per warp, int32 (sw_pack16 0, no whole-block pairs)",
                                      "gcups": cells / (ms_plain * 1e-3) / 1e9, "ms_per_step": ms_plain},
             "bit_identical_to_plain": same}
@@ -725,14 +750,20 @@ def main():
     from genoaligner_gb300 import api, cost_model, workloads
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.set_tune:
+        fields = dict(kv.split("=") for kv in args.set_tune.split(","))
+        api.tune_set(**dict(api.tune_get(), **{k: int(v) for k, v in fields.items()}))
+        args.no_tune = True
 
     if args.only:
         stream = torch.cuda.current_stream(dev)
         keep = {}
+        m = args.only_pairs
         run = {"wfa_150bp": lambda: bench_wfa_150(api, workloads, torch, dev, stream, args, keep),
-               "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep),
-               "wfa_long": lambda: bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep),
-               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, 4096, keep),
+               "wfa_mixed_1m": lambda: bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep, m),
+               "wfa_long": lambda: bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep, m),
+               "sw_long": lambda: bench_sw_long(api, workloads, torch, dev, stream, m or 4096, keep,
+                                                not args.no_tune),
                "sw_score_only": lambda: score_only_alone(api, workloads, torch, dev, stream, args)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: run()}), flush=True)
@@ -832,7 +863,7 @@ def main():
         extra["wfa_150bp"] = bench_wfa_150(api, workloads, torch, dev, stream, args, keep)
         extra["wfa_mixed_1m"] = bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep)
         extra["wfa_long"] = bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep)
-        extra["sw_long"] = bench_sw_long(api, workloads, torch, dev, stream, 4096, keep)
+        extra["sw_long"] = bench_sw_long(api, workloads, torch, dev, stream, 4096, keep, not args.no_tune)
 
     # the CPU leg (rank 0, after every GPU measurement): the oracle over each
     # workload is the CPU baseline and the full-size parity check at once

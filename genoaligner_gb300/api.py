@@ -88,7 +88,8 @@ EXPORTS = ["ga_align_cigar_bytes", "ga_align_batch", "ga_align_sw_cigar_bytes", 
            "ga_debug_fail_next", "ga_last_transfer_bytes", "ga_profile", "ga_profile_read",
            "ga_profile_kernel_name", "ga_bench_int_peak", "ga_cost_model_nparams", "ga_cost_model_set",
            "ga_cost_model_get", "ga_wfa_features", "ga_mlp_forward", "ga_mlp_gradient", "ga_mlp_train_step",
-           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_wfa_route_items", "ga_mlp_forward_fast", "ga_tune_default", "ga_tune_get",
+           "ga_wfa_device_ex", "ga_wfa_route_stats", "ga_wfa_route_items", "ga_sw_device_ex", "ga_model_select",
+           "ga_sw_features", "ga_mlp_forward_fast", "ga_tune_default", "ga_tune_get",
            "ga_tune_set", "ga_autotune_sw", "ga_autotune_wfa", "ga_tune_save", "ga_tune_load",
            "ga_fasta_read", "ga_fasta_parse", "ga_fasta_count", "ga_fasta_id", "ga_fasta_description",
            "ga_fasta_arena", "ga_fasta_offsets", "ga_fasta_lengths", "ga_fasta_pinned", "ga_fasta_upload",
@@ -129,6 +130,9 @@ def load(build: bool = True):
     L.ga_sw_device.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, i32, i64, p, p, p, p, p,
                                ctypes.POINTER(ctypes.c_char_p)]
     L.ga_sw_device.restype = i32
+    L.ga_sw_device_ex.argtypes = [ctypes.POINTER(DeviceBatch), SwScoringC, i32, i64, ctypes.POINTER(Options), p, p,
+                                  p, p, p, ctypes.POINTER(ctypes.c_char_p)]
+    L.ga_sw_device_ex.restype = i32
     L.ga_backend_name.restype = ctypes.c_char_p
     L.ga_device_name.restype = ctypes.c_char_p
     L.ga_device_available.restype = i32
@@ -164,6 +168,10 @@ def load(build: bool = True):
     L.ga_wfa_route_stats.restype = i32
     L.ga_wfa_route_items.argtypes = [p, i32]
     L.ga_wfa_route_items.restype = i32
+    L.ga_model_select.argtypes = [i32]
+    L.ga_model_select.restype = i32
+    L.ga_sw_features.argtypes = [ctypes.POINTER(DeviceBatch), p, p]
+    L.ga_sw_features.restype = i32
     for f in ("ga_tune_default", "ga_tune_get"):
         getattr(L, f).argtypes = [ctypes.POINTER(TuneC)]
         getattr(L, f).restype = i32
@@ -350,8 +358,9 @@ def align(req: AlignRequest) -> AlignResult:
     return b.results[0] if b.results else AlignResult()
 
 
-def align_sw_batch(reqs, trace_cell_limit: int = 0) -> SWBatchResult:
-    """genoaligner::align_sw_batch (or align_sw_batch_ex with a trace limit; < 0 = none)."""
+def align_sw_batch(reqs, trace_cell_limit: int = 0, learned: bool = False) -> SWBatchResult:
+    """genoaligner::align_sw_batch (or align_sw_batch_ex with a trace limit, < 0 = none,
+    or with the SW variant model's routing)."""
     L = load()
     n = len(reqs)
     if n == 0:
@@ -368,8 +377,8 @@ def align_sw_batch(reqs, trace_cell_limit: int = 0) -> SWBatchResult:
     nbytes = int(L.ga_align_sw_cigar_bytes(arr.ctypes.data, n))
     buf = ctypes.create_string_buffer(max(nbytes, 1))
     info = BatchInfo()
-    if trace_cell_limit:
-        o = _opts(trace_cell_limit=trace_cell_limit)
+    if trace_cell_limit or learned:
+        o = _opts(learned=learned, trace_cell_limit=trace_cell_limit)
         st = L.ga_align_sw_batch_ex(arr.ctypes.data, n, res.ctypes.data, buf, nbytes, ctypes.byref(o),
                                     ctypes.byref(info))
     else:
@@ -542,14 +551,19 @@ def wfa_device(batch: DeviceBatchT, smax, trace, out_score, out_len, out_cigar, 
 
 
 def sw_device(batch: DeviceBatchT, scoring, trace, out_score, out_pos, out_len, out_cigar, stream=None,
-              trace_cell_limit=-1):
+              trace_cell_limit=-1, learned=False):
+    """ga_sw_device, or ga_sw_device_ex with learned = 1 (the SW variant
+    model routes pairs to the 16-bit kernel)."""
     err = ctypes.c_char_p()
     sc = SwScoringC(*scoring)
-    st = load().ga_sw_device(ctypes.byref(batch.c), sc, 1 if trace else 0, trace_cell_limit,
-                             out_score.data_ptr(), out_pos.data_ptr(),
-                             out_len.data_ptr() if out_len is not None else None,
-                             out_cigar.data_ptr() if out_cigar is not None else None,
-                             stream, ctypes.byref(err))
+    L = load()
+    args = (out_score.data_ptr(), out_pos.data_ptr(), out_len.data_ptr() if out_len is not None else None,
+            out_cigar.data_ptr() if out_cigar is not None else None, stream, ctypes.byref(err))
+    if learned:
+        o = _opts(learned=True)
+        st = L.ga_sw_device_ex(ctypes.byref(batch.c), sc, 1 if trace else 0, trace_cell_limit, ctypes.byref(o), *args)
+    else:
+        st = L.ga_sw_device(ctypes.byref(batch.c), sc, 1 if trace else 0, trace_cell_limit, *args)
     if st != GA_OK:
         raise RuntimeError(f"ga_sw_device failed: {err.value}")
 
@@ -618,7 +632,7 @@ def make_sw_requests(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, -3, 5
 
 
 def align_sw_batch_packed(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, -3, 5, 2), with_cigar=True,
-                          trace_cell_limit=0, _reqs=None, _res=None, _cig=None) -> PackedResult:
+                          trace_cell_limit=0, learned=False, _reqs=None, _res=None, _cig=None) -> PackedResult:
     """align_sw_batch over packed sequences (text = rows, pattern = columns)."""
     L = load()
     n = int(t_len.shape[0])
@@ -631,8 +645,8 @@ def align_sw_batch_packed(t_buf, t_off, t_len, p_buf, p_off, p_len, scoring=(2, 
         nbytes = int(L.ga_align_sw_cigar_bytes(reqs.ctypes.data, n))
         cig = np.empty(max(nbytes, 1), np.uint8)
     info = BatchInfo()
-    if trace_cell_limit:
-        o = _opts(trace_cell_limit=trace_cell_limit)
+    if trace_cell_limit or learned:
+        o = _opts(learned=learned, trace_cell_limit=trace_cell_limit)
         st = L.ga_align_sw_batch_ex(reqs.ctypes.data, n, res.ctypes.data, cig.ctypes.data, nbytes,
                                     ctypes.byref(o), ctypes.byref(info))
     else:
@@ -669,6 +683,38 @@ def cost_model_init(seed: int = 0) -> np.ndarray:
         parts.append(rng.normal(0, np.sqrt(2.0 / fan_in), size=fan_out * fan_in).astype(np.float32))
         parts.append(np.zeros(fan_out, np.float32))
     return np.concatenate(parts)
+
+
+def model_select(which: int):
+    """The model slot the calling thread's cost_model_* / mlp_* calls act on:
+    0 the WFA cost model, 1 the SW variant model."""
+    if load().ga_model_select(int(which)) != GA_OK:
+        raise ValueError(f"no model slot {which}")
+
+
+class model_slot:
+    """with model_slot(1): ... -- select a slot, then slot 0 again."""
+
+    def __init__(self, which: int):
+        self.which = which
+
+    def __enter__(self):
+        model_select(self.which)
+        return self
+
+    def __exit__(self, *exc):
+        model_select(0)
+        return False
+
+
+def sw_features(batch: "DeviceBatchT"):
+    """Features [n,66] of an SW batch for the SW variant model (torch, on the batch's device)."""
+    import torch
+    feat = torch.empty((batch.n, 66), dtype=torch.float32, device=batch.seq.device)
+    st = load().ga_sw_features(ctypes.byref(batch.c), feat.data_ptr(), None)
+    if st != GA_OK:
+        raise RuntimeError(f"ga_sw_features failed ({st})")
+    return feat
 
 
 def wfa_features(batch: "DeviceBatchT"):

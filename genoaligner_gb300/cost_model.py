@@ -4,7 +4,11 @@ The network (learned.cu) maps a pair's 66 sketch features to
 [log2(d + 1), log2((d + 1)^2 + 1)] -- the edit distance and the WFA's
 wavefront-cell work.  It is trained on the GPU by the library's own forward,
 backward and Adam kernels, on pairs labelled by the library's exact WFA
-(score-only, smax 250, so every training label is the true distance).
+(score-only at smax 250 for the short pairs and 2048 for the long ones, pairs
+unresolved there left out, so every training label is the true distance):
+2,000,000 pairs of the mixed-divergence distribution (150-250 bp) and 20,000
+pairs of the long distribution (1-10 kb, error 1-15 %, geometric indels),
+the long ones repeated 10 times in the training set.
 
 Checkpoint: an .npz with the fp32 parameters, a format version and the
 training seed; ``load_default()`` puts the committed model
@@ -23,6 +27,8 @@ from . import api, workloads
 FORMAT_VERSION = 1
 DEFAULT_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "wfa_cost_v1.npz")
 LABEL_SMAX = 250
+LABEL_SMAX_LONG = 2048
+LONG_REPEAT = 10
 
 
 def training_pairs(n: int = 2_000_000, seed: int = 1001) -> workloads.PairSet:
@@ -30,17 +36,22 @@ def training_pairs(n: int = 2_000_000, seed: int = 1001) -> workloads.PairSet:
     return workloads.wfa_mixed(n=n, seed=seed)
 
 
-def labels_and_features(ps: workloads.PairSet, chunk: int = 250_000):
-    """Exact distances (GPU WFA, score-only, smax 250) and sketch features, as
-    torch tensors on the current device: (features [n,66], targets [n,2],
-    distance [n], lower bound [n])."""
+def training_pairs_long(n: int = 20_000, seed: int = 1002) -> workloads.PairSet:
+    """Pairs of the long distribution (1-10 kb), separately seeded."""
+    return workloads.wfa_long_1k_10k(n=n, seed=seed)
+
+
+def labels_and_features(ps: workloads.PairSet, chunk: int = 250_000, label_smax: int = LABEL_SMAX):
+    """Exact distances (GPU WFA, score-only, at label_smax) and sketch
+    features, as torch tensors on the current device: (features [n,66],
+    targets [n,2], distance [n], lower bound [n])."""
     import torch
     feats, targs, dists, lbs = [], [], [], []
     for lo in range(0, ps.n, chunk):
         sub = ps if (lo == 0 and ps.n <= chunk) else _slice(ps, lo, min(ps.n, lo + chunk))
         b = api.DeviceBatchT(sub.a_buf, sub.a_off, sub.a_len, sub.b_buf, sub.b_off, sub.b_len)
         score = torch.empty(b.n, dtype=torch.int32, device="cuda")
-        api.wfa_device(b, LABEL_SMAX, False, score, None, None)
+        api.wfa_device(b, label_smax, False, score, None, None)
         f, lb = api.wfa_features(b)
         d = score.to(torch.float32)
         t = torch.stack([torch.log2(d + 1), torch.log2((d + 1) ** 2 + 1)], dim=1)
@@ -57,8 +68,9 @@ def _slice(ps: workloads.PairSet, lo: int, hi: int) -> workloads.PairSet:
 
 
 def train(feat, target, epochs: int = 3, batch: int = 8192, lr: float = 2e-3, seed: int = 1001,
-          log=None) -> dict:
-    """Adam on the library's kernels; returns the training record."""
+          log=None, decay: float = 0.3) -> dict:
+    """Adam on the library's kernels (the calling thread's selected model
+    slot), the rate times `decay` each epoch; returns the training record."""
     import torch
     api.cost_model_set(api.cost_model_init(seed))
     n = int(feat.shape[0])
@@ -67,7 +79,7 @@ def train(feat, target, epochs: int = 3, batch: int = 8192, lr: float = 2e-3, se
     t0 = time.time()
     for ep in range(epochs):
         perm = torch.randperm(n, device="cuda", generator=g)
-        step_lr = lr * (0.3 ** ep)
+        step_lr = lr * (decay ** ep)
         for lo in range(0, n - batch + 1, batch):
             idx = perm[lo:lo + batch]
             xb = feat[idx].contiguous()
@@ -125,8 +137,12 @@ def main():
     import sys
     api.load()
     t0 = time.time()
+    import torch
     ps = training_pairs()
     feat, targ, dist, lb = labels_and_features(ps)
+    lf, lt, _, _ = labels_and_features(training_pairs_long(), chunk=5000, label_smax=LABEL_SMAX_LONG)
+    feat = torch.cat([feat] + [lf] * LONG_REPEAT)
+    targ = torch.cat([targ] + [lt] * LONG_REPEAT).contiguous()
     t1 = time.time()
     rec = train(feat, targ, log=lambda s: print(s, flush=True))
     params = api.cost_model_get()
@@ -135,8 +151,12 @@ def main():
     hold = workloads.wfa_mixed(n=200_000, seed=4040)
     hf, _, hd, hl = labels_and_features(hold)
     ev = evaluate(hf, hd, hl)
+    lh = workloads.wfa_long_1k_10k(n=2_000, seed=4041)
+    lhf, _, lhd, lhl = labels_and_features(lh, chunk=5000, label_smax=LABEL_SMAX_LONG)
+    ev_long = evaluate(lhf, lhd, lhl)
     print(json.dumps({"label_seconds": t1 - t0, "train_seconds": rec["seconds"], "steps": rec["steps"],
-                      "final_loss": float(np.mean(rec["losses"][-50:])), "holdout": ev, "path": out}))
+                      "final_loss": float(np.mean(rec["losses"][-50:])), "holdout": ev, "holdout_long": ev_long,
+                      "path": out}))
 
 
 if __name__ == "__main__":

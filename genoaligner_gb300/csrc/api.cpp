@@ -45,7 +45,8 @@ BatchResult align_batch_ex(const std::vector<AlignRequest>& reqs, const AlignOpt
             r.resolved = r.score >= 0;
             res += r.resolved;
             if (v.trace && r.resolved && v.len[i] > 0) {
-                r.cigar.assign(v.cig + v.slot_end[i] - v.len[i], (size_t)v.len[i]);
+                r.cigar.resize((size_t)v.len[i]);
+                v.cigar(i, &r.cigar[0]);
                 if (v.vflags) {
                     r.rescore_ok = v.vflags[i] & 1;
                     r.wellformed_ok = (v.vflags[i] >> 1) & 1;
@@ -122,7 +123,8 @@ SWBatchResult align_sw_batch_ex(const std::vector<SWRequest>& reqs, const AlignO
             r.start_i = v.pos[4 * q];
             r.start_j = v.pos[4 * q + 1];
             if (v.len[q] > 0) {
-                r.cigar.assign(v.cig + v.slot_end[q] - v.len[q], (size_t)v.len[q]);
+                r.cigar.resize((size_t)v.len[q]);
+                v.cigar(q, &r.cigar[0]);
                 if (v.vflags) {
                     r.rescore_ok = v.vflags[q] & 1;
                     r.wellformed_ok = (v.vflags[q] >> 1) & 1;

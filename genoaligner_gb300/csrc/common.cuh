@@ -19,6 +19,7 @@ __device__ __forceinline__ bool wfa_live(int off) { return off > WFA_NULL + 1024
 enum : int {
     ERR_CIGAR_OVERFLOW = 1,   // a walk produced more ops than its slot holds
     ERR_BAD_INPUT      = 2,   // a descriptor violated the layout contract
+    ERR_SCRATCH        = 4,   // a launch's per-warp memory exceeded what it was given
 };
 
 // Sequences of pair i: a at seq[a_off[i]], b at seq[b_off[i]]; offsets are

@@ -27,6 +27,7 @@ namespace ga {
 
 // ------------------------------------------------------------ accounting --
 static std::atomic<long long> g_launches{0};
+static thread_local long long t_launches = 0;     // the calling thread's share of g_launches
 
 // Per-kernel event timing, on only between ga_profile(1) and ga_profile(0).
 struct ProfRec { int id; cudaEvent_t a, b; };
@@ -41,6 +42,7 @@ thread_local ProfRec t_prof_cur{-1, nullptr, nullptr};
 void launch_begin(int kernel_id, cudaStream_t st)
 {
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    ++t_launches;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     if (!g_prof_on) return;
     ProfRec r{kernel_id, nullptr, nullptr};
@@ -183,6 +185,27 @@ void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, in
     pool().run(n, grain, fn);
 }
 
+void expand_cigar(const uint8_t* src, int len, char* dst)
+{
+    // four ops per packed byte: one 4-byte store per byte from a 256-entry table
+    static const auto table = [] {
+        std::vector<uint32_t> t(256);
+        const char ops[4] = {'M', 'X', 'I', 'D'};
+        for (int b = 0; b < 256; ++b) {
+            unsigned char c[4];
+            for (int k = 0; k < 4; ++k) c[k] = (unsigned char)ops[(b >> (2 * k)) & 3];
+            std::memcpy(&t[(size_t)b], c, 4);
+        }
+        return t;
+    }();
+    int t = 0;
+    for (; t + 4 <= len; t += 4) std::memcpy(dst + t, &table[src[t >> 2]], 4);
+    if (t < len) {
+        const uint32_t w = table[src[t >> 2]];
+        std::memcpy(dst + t, &w, (size_t)(len - t));
+    }
+}
+
 // -------------------------------------------------------------- contexts --
 struct Ctx {
     int device = -1;
@@ -195,10 +218,30 @@ struct Ctx {
     uint64_t dev_gen = 0;           // bumped whenever the device arena is reallocated
     cudaGraphExec_t gexec = nullptr;  // the learned WFA path, captured once per launch shape
     uint64_t gkey[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    cudaGraphExec_t swexec = nullptr; // the SW device work of a call or range, captured once per launch shape
+    std::vector<uint64_t> swkey;
+    int swlaunches = 0;               // library kernels in swexec
     char* host = nullptr;
     size_t host_cap = 0;
     int tag = -1;                   // range index of a ranged SW call that created it, else -1
+    int prio = 0;                   // the stream's priority
 };
+
+// Stream priority of range `tag` of a ranged call: range 0 the greatest, each
+// later range one step lower (as far as the device's range goes), so the
+// earlier ranges' blocks are scheduled first and those ranges finish first --
+// their results copy back and are written out while the later ranges run.
+// Other calls: the default priority.
+static int ctx_priority(int tag)
+{
+    if (tag < 0) return 0;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return std::min(least, greatest + tag);
+}
 
 static std::mutex g_ctx_mu;
 static std::vector<Ctx*> g_ctx_free;
@@ -231,14 +274,28 @@ static Ctx* acquire_ctx(const char** err, int tag = -1)
             g_ctx_free.erase(g_ctx_free.begin() + pick);
             if (tag >= 0) c->tag = tag;
             if (c->pending) { cudaEventSynchronize(c->done); c->pending = false; }
+            // a range's context needs its range's priority (a call alone runs at any)
+            const int prio = tag >= 0 ? ctx_priority(tag) : c->prio;
+            if (prio != c->prio) {                     // the stream of another priority: a new one
+                cudaStream_t ns = nullptr;
+                if (cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio) == cudaSuccess) {
+                    cudaStreamSynchronize(c->stream);
+                    cudaStreamDestroy(c->stream);
+                    c->stream = ns;
+                    c->prio = prio;
+                } else {
+                    cudaGetLastError();
+                }
+            }
             return c;
         }
     }
     Ctx* c = new Ctx();
     c->device = dev;
     c->tag = tag;
+    c->prio = ctx_priority(tag);
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, c->prio) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         delete c;
@@ -355,6 +412,7 @@ static const char* E_LAUNCH = "kernel launch failed";
 static const char* E_D2H = "device-to-host copy failed";
 static const char* E_SYNC = "device execution failed";
 static const char* E_OVERFLOW = "internal error: CIGAR slot overflow";
+static const char* E_SCRATCH = "internal error: traceback memory smaller than the plan needs";
 static const char* E_HOSTMEM = "pinned host allocation failed";
 
 // -------------------------------------------------------------------- WFA --
@@ -480,6 +538,34 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     return launch_routed(R, S.lane_slots, S.slots, st);
 }
 
+// Replays `exec` when `key` (everything the enqueued launches bake in) is the
+// one it was captured for; otherwise captures enqueue() on stream st first.
+// `launches` keeps the number of library kernels the graph holds (counted
+// once per replay).
+static cudaError_t replay_graph(cudaGraphExec_t& exec, std::vector<uint64_t>& have, const std::vector<uint64_t>& key,
+                                int& launches, cudaStream_t st, const std::function<cudaError_t()>& enqueue)
+{
+    if (!exec || have != key) {
+        if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+        have.clear();
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        const long long before = t_launches;
+        const cudaError_t e1 = enqueue();
+        launches = (int)(t_launches - before);              // (nothing ran: captured only)
+        g_launches.fetch_sub(launches);
+        e = cudaStreamEndCapture(st, &g);
+        if (e1 != cudaSuccess || e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e1 != cudaSuccess ? e1 : e; }
+        e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { exec = nullptr; return e; }
+        have = key;
+    }
+    note_graph_launches(launches);
+    return cudaGraphLaunch(exec, st);
+}
+
 // Learned path as one CUDA graph, cached per context by everything the
 // launches bake in.
 static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace, int route,
@@ -551,10 +637,10 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     route = route_mode(route);
     const bool learned = route != 0;
 
-    // plan: 32-aligned sequence offsets, CIGAR slot offsets
-    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    // plan: 32-aligned sequence offsets, CIGAR slot offsets, packed CIGAR offsets
+    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n), pk_off(n);
     std::vector<uint8_t> own(n, 0);
-    int64_t arena = 0, cig = 0;
+    int64_t arena = 0, cig = 0, pkb = 0;
     for (int32_t i = 0; i < n; ++i) {
         // a side that repeats the previous request's (same pointer and length) is staged once
         const ga_align_request& r = reqs[i];
@@ -562,11 +648,13 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         else { a_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 1; }
         if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) b_off[i] = b_off[i - 1];
         else { b_off[i] = arena; arena += round32(r.text_len); own[i] |= 2; }
-        out_off[i] = cig; cig += (int64_t)reqs[i].pattern_len + reqs[i].text_len;
+        const int64_t cap = (int64_t)reqs[i].pattern_len + reqs[i].text_len;
+        out_off[i] = cig; cig += cap;
         slot_end[i] = cig;
+        pk_off[i] = pkb; pkb += (cap + 3) / 4;
     }
     arena += 64;                                     // read-past padding
-    if (!trace) cig = 0;
+    if (!trace) cig = pkb = 0;
 
     Ctx* c = acquire_ctx(err);
     if (!c) return GA_DEVICE_ERROR;
@@ -575,31 +663,35 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
 
     WfaScratch S;
     size_wfa(S, n, smax, trace, learned, c->sm_count);
-    // layout: [a_off a_len b_off b_len out_off | seq] [score len cigar checks | err] then device scratch
-    int64_t *ha, *hb, *ho, *da, *db, *dout;
+    // layout: [a_off a_len b_off b_len out_off pk_off | seq] in, [score len checks err | packed CIGARs]
+    // back, then (device) the CIGAR slots and the scratch
+    int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
     int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
-    uint8_t *hseq, *dseq, *hvf, *dvf;
-    char *hcg, *dcg;
-    auto io = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po, uint8_t** ps,
-                  int32_t** psc, int32_t** pln, char** pcg, uint8_t** pvf, int32_t** per) {
+    uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
+    char* dcg;
+    auto io = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po, int64_t** ppo,
+                  uint8_t** ps, int32_t** psc, int32_t** pln, uint8_t** pvf, int32_t** per, uint8_t** ppk) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
-        *po = k.take<int64_t>(n);
+        *po = k.take<int64_t>(n); *ppo = k.take<int64_t>(n);
         *ps = k.take<uint8_t>(arena);
-        *psc = k.take<int32_t>(n); *pln = k.take<int32_t>(n); *pcg = k.take<char>(cig + 1);
+        *psc = k.take<int32_t>(n); *pln = k.take<int32_t>(n);
         *pvf = k.take<uint8_t>(trace ? n : 0);
         *per = k.take<int32_t>(1, 4);
+        *ppk = k.take<uint8_t>((size_t)pkb, 4);
     };
     Carve hk(nullptr), dk(nullptr);
-    io(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &hvf, &her);
-    io(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &dvf, &der);
+    io(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+    io(dk, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+    dcg = dk.take<char>(cig + 1);
     carve_wfa(dk, S, n, arena, trace, learned);
     if (fail_here(1) || !ensure_dev(c, dk.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
     if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
     {
         Carve h(c->host), d(c->dev);
-        io(h, &ha, &hal, &hb, &hbl, &ho, &hseq, &hsc, &hln, &hcg, &hvf, &her);
-        io(d, &da, &dal, &db, &dbl, &dout, &dseq, &dsc, &dln, &dcg, &dvf, &der);
+        io(h, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+        io(d, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+        dcg = d.take<char>(cig + 1);
         carve_wfa(d, S, n, arena, trace, learned);
     }
 
@@ -609,7 +701,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
             const ga_align_request& r = reqs[i];
             ha[i] = a_off[i]; hal[i] = r.pattern_len;
             hb[i] = b_off[i]; hbl[i] = r.text_len;
-            ho[i] = out_off[i];
+            ho[i] = out_off[i]; hpo[i] = pk_off[i];
             if ((own[i] & 1) && r.pattern_len) std::memcpy(hseq + a_off[i], r.pattern, (size_t)r.pattern_len);
             if ((own[i] & 2) && r.text_len) std::memcpy(hseq + b_off[i], r.text, (size_t)r.text_len);
         }
@@ -633,13 +725,14 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     else le = enqueue_wfa(S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
     if (learned) note_route(c, S, n);
     if (le == cudaSuccess && trace) le = launch_wfa_validate(D, dsc, dln, dcg, dvf, c->stream);
+    if (le == cudaSuccess && trace) le = launch_cigar_pack(D, dln, dcg, dpo, dpk, c->stream);
     if (le != cudaSuccess) {
         cudaGetLastError();
         *err = E_LAUNCH;
         return GA_DEVICE_ERROR;
     }
-    // outputs are contiguous on both sides: score, len, cigar, checks, err
-    const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
+    // outputs are contiguous on both sides: score, len, checks, err, packed CIGARs
+    const size_t out_bytes = (size_t)((char*)(dpk + pkb) - (char*)dsc);
     t_d2h = (int64_t)out_bytes;
     if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -652,7 +745,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    WfaView v{hsc, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr};
+    WfaView v{hsc, hln, hpk, hpo, slot_end.data(), trace, trace ? hvf : nullptr};
     parallel_for(n, 1024, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
     return GA_OK;
 }
@@ -700,11 +793,10 @@ struct SwPlan {
     int64_t n_opt = 0, dir_opt = 0;
 };
 
-// The plan, built on the device (sw_plan.cu) into `dwork`; reads back its
-// record and fills P's list lengths and sizes.
-static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bool trace, int64_t cell_limit,
-                                  int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
-                                  long long* dres, long long* hres, const ga_tune& T, cudaStream_t st, SwPlan& P)
+// The plan, built on the device (sw_plan.cu) into `dwork`, its record into dres.
+static cudaError_t enqueue_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bool trace, int64_t cell_limit,
+                                   int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
+                                   long long* dres, const ga_tune& T, cudaStream_t st, const uint8_t* try16 = nullptr)
 {
     SwPlanArgs A;
     A.D = D;
@@ -719,7 +811,18 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bo
     A.out_score = out_score;
     A.work = dwork;
     A.res = dres;
-    cudaError_t e = launch_sw_plan(A, scratch, st);
+    A.try16 = try16;
+    return launch_sw_plan(A, scratch, st);
+}
+
+// The same, then its record read back into P's list lengths and sizes.
+static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bool trace, int64_t cell_limit,
+                                  int32_t too_large_score, int32_t* out_score, int32_t* dwork, int32_t* scratch,
+                                  long long* dres, long long* hres, const ga_tune& T, cudaStream_t st, SwPlan& P,
+                                  const uint8_t* try16 = nullptr)
+{
+    cudaError_t e =
+        enqueue_plan_sw(D, sc, trace, cell_limit, too_large_score, out_score, dwork, scratch, dres, T, st, try16);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hres, dres, sizeof(long long) * SP_RES, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
@@ -733,6 +836,54 @@ static cudaError_t device_plan_sw(const PairDesc& D, const ga_sw_scoring& sc, bo
     P.n_opt = hres[SP_NOPT];
     P.dir_opt = (hres[SP_DIROPT] + 3) / 4 * 4;
     return cudaSuccess;
+}
+
+// Upper bounds of the device-built plan from the requests' lengths alone, for
+// launches enqueued without reading the plan back.  Purity is not known on the
+// host, so every pair counts in the 16-bit list when its lengths allow it and
+// in its 32-bit list as well; per-warp memory is the largest any of those
+// pairs (or items) can need.  The kernels take the exact figures from the
+// plan on the device (plan_view); these only size the grids and the memory.
+static SwPlan bound_plan_sw(const ga_sw_request* reqs, int32_t n, bool trace, int64_t cell_limit, const ga_tune& T,
+                            bool learned)
+{
+    SwPlan P;
+    const ga_sw_scoring sc = reqs[0].scoring;
+    int maxM16 = 0, maxN16 = 0;
+    int64_t n16 = 0, cnt[SP_LISTS] = {0, 0, 0}, edge = 2;
+    for (int32_t i = 0; i < n; ++i) {
+        const int m = reqs[i].text_len, nn = reqs[i].pattern_len;
+        if (cell_limit >= 0 && m > 0 && nn > 0 && ((int64_t)m + 1) * ((int64_t)nn + 1) > cell_limit) continue;
+        const bool strict = T.sw_pack16 && sw16_eligible(m, nn, sc.match, sc.mismatch, sc.gap_open, sc.gap_extend);
+        // (the SW model may send any pair to the 16-bit kernel)
+        const bool u16 = strict || (trace && T.sw_pack16 &&
+                                    (learned ? (m > 0 && nn > 0 &&
+                                                sw16_scheme_ok(sc.match, sc.mismatch, sc.gap_open, sc.gap_extend))
+                                             : sw16_eligible_opt(m, nn, sc.match, sc.mismatch, sc.gap_open,
+                                                                 sc.gap_extend, T.sw_opt16_pct)));
+        if (u16) {
+            ++n16;
+            maxM16 = std::max(maxM16, m);
+            maxN16 = std::max(maxN16, nn);
+            if (!strict) {
+                ++P.n_opt;
+                P.dir_opt = std::max(P.dir_opt, sw32ck_dir_words(m, nn, 0));
+            }
+        }
+        const int l = (trace && sw32ck_long(m, nn, T.sw_long_log2)) ? SP_L32LONG : SP_L32;
+        ++cnt[l];
+        if (trace) P.dir[l] = std::max(P.dir[l], sw32ck_dir_words(m, nn, T.sw_long_log2));
+        edge = std::max<int64_t>(edge, 2 * (int64_t)std::max(m, 0));
+    }
+    P.ints[SP_L16] = 2 * ((n16 + 1) / 2);
+    P.dir[SP_L16] = n16 ? (trace ? sw16ck_dir_words(maxM16, maxN16, T.sw_window) : sw16so_dir_words(maxM16, maxN16)) : 0;
+    P.max16_cells = (int64_t)maxM16 * maxN16;
+    P.ints[SP_L32] = cnt[SP_L32];
+    P.ints[SP_L32LONG] = cnt[SP_L32LONG];
+    for (int l = 0; l < SP_LISTS; ++l) P.dir[l] = (P.dir[l] + 3) / 4 * 4;
+    P.dir_opt = (P.dir_opt + 3) / 4 * 4;
+    P.edge_slot = edge;
+    return P;
 }
 
 // Device memory the checkpoint / direction tables of one call may take:
@@ -792,11 +943,15 @@ static SwSlots size_sw(const SwPlan& P, bool trace, const ga_tune& T, int sm_cou
 // Enqueue every SW launch of a plan.  `dwork` holds the plan's lists
 // concatenated in list order; `ctr` has 8 zeroed ints; esc_list (n ints)
 // takes the pairs the 16-bit kernel hands to the 32-bit one.
+// With dplan set (plan mode), P holds bounds (bound_plan_sw) and every launch
+// takes its items and per-warp memory from the device-built record dplan
+// (plan_view), its memory bounded by the dir_words / edge ints S sized.
 static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc& D, const ga_sw_scoring& sc,
                                bool trace, const ga_tune& T, const int32_t* dwork, int32_t* out_score, int32_t* out_pos,
                                int32_t* out_len, char* out_cigar, uint32_t* dirs, int32_t* edge, int32_t* ctr,
-                               int32_t* err, cudaStream_t st, int32_t* esc_list)
+                               int32_t* err, cudaStream_t st, int32_t* esc_list, const long long* dplan = nullptr)
 {
+    const int64_t dir_cap = S.dir_words, edge_cap = S.max_slots * P.edge_slot;
     // ctr: [l] list l's item counter, [6] pairs handed over, [7] their counter
     const bool opt = trace && P.n_opt > 0 && esc_list && S.s_esc > 0;
     const int64_t coop = T.sw_coop_log2 < 40 ? ((int64_t)1 << T.sw_coop_log2) : -1;
@@ -809,6 +964,7 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
         A.dirs = dirs; A.dir_slot = P.dir[SP_L16]; A.edge = edge; A.edge_slot = P.edge_slot;
         A.counter = ctr + SP_L16; A.err = err;
         A.coop_cells = coop;
+        if (dplan) { A.plan = dplan; A.plan_list = SP_L16; A.dir_cap = dir_cap; A.edge_cap = 0; }
         if (opt) {
             A.ovf_limit = sw16_overflow_limit(sc.match);
             A.esc_list = esc_list;
@@ -827,6 +983,7 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             B.dirs = dirs; B.dir_slot = P.dir_opt; B.edge = edge; B.edge_slot = P.edge_slot;
             B.counter = ctr + 7; B.err = err;
             B.coop_cells = coop;
+            if (dplan) { B.plan = dplan; B.plan_list = SP_ESC; B.dir_cap = dir_cap; B.edge_cap = 0; }
             const cudaError_t e2 = launch_sw32ck(B, true, S.s_esc, st);
             if (e2 != cudaSuccess) return e2;
         }
@@ -841,6 +998,13 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
             A.dirs = dirs; A.dir_slot = P.dir[l]; A.edge = edge; A.edge_slot = P.edge_slot;
             A.counter = ctr + l; A.err = err;
             A.coop_cells = l == SP_L32LONG ? coop : -1;
+            if (dplan) {
+                A.plan = dplan;
+                A.plan_list = l;
+                A.work = dwork;
+                A.dir_cap = trace ? dir_cap : 0;
+                A.edge_cap = trace ? 0 : edge_cap;
+            }
             const cudaError_t e = trace ? launch_sw32ck(A, l == SP_L32LONG, S.s[l], st) : launch_sw(A, S.s[l], st);
             if (e != cudaSuccess) return e;
         }
@@ -856,15 +1020,15 @@ static cudaError_t launch_plan(const SwPlan& P, const SwSlots& S, const PairDesc
 // at once and share the device-memory budget.
 static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base, int64_t cig_base, bool trace,
                               const ga_tune& T, int64_t cell_limit, const SwFinish& fin, const char** err,
-                              int64_t* h2d, int64_t* d2h, int parts, int range_tag = -1)
+                              int64_t* h2d, int64_t* d2h, int parts, int range_tag, bool learned)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
     const ga_sw_scoring s0 = reqs[0].scoring;
 
-    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n);
+    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n), pk_off(n);
     std::vector<uint8_t> own(n, 0);
-    int64_t arena = 0, cig = 0;
+    int64_t arena = 0, cig = 0, pkb = 0;
     for (int32_t i = 0; i < n; ++i) {
         const ga_sw_request& r = reqs[i];
         // a side that repeats the previous request's (same pointer and length:
@@ -873,148 +1037,148 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         else { a_off[i] = arena; arena += round32(r.text_len); own[i] |= 1; }
         if (i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len) b_off[i] = b_off[i - 1];
         else { b_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 2; }
-        out_off[i] = cig; cig += (int64_t)r.text_len + r.pattern_len;
+        const int64_t cap = (int64_t)r.text_len + r.pattern_len;
+        out_off[i] = cig; cig += cap;
         slot_end[i] = cig;
+        pk_off[i] = pkb; pkb += (cap + 3) / 4;
     }
     arena += 64;
-    if (!trace) cig = 0;
+    if (!trace) cig = pkb = 0;
 
     Ctx* c = acquire_ctx(err, range_tag);
     if (!c) return GA_DEVICE_ERROR;
     struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
 
-    // Host staging: [descriptors | arena] in, [purity] back, [work lists] in,
-    // [score pos len cigar err] back.  Device: the same blocks plus scratch.
-    const int64_t max_work = 2 * (int64_t)n + 8;
-    int64_t *ha, *hb, *ho, *da, *db, *dout;
-    int32_t *hal, *hbl, *dal, *dbl, *hwork, *dwork, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der;
-    uint8_t *hseq, *dseq, *hpure, *dpure, *hvf, *dvf;
-    char *hcg, *dcg;
-    auto in_layout = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
-                         uint8_t** ps, uint8_t** pp, int32_t** pw, int32_t** psc, int32_t** ppos, int32_t** pln,
-                         uint8_t** pvf, char** pcg, int32_t** per) {
+    // Launch sizes from the lengths (bounds of the plan the device builds):
+    // every launch is enqueued without reading the plan back.
+    const bool route = learned && trace;                 // the SW model picks the 16-bit pairs
+    const SwPlan P = bound_plan_sw(reqs, n, trace, trace ? cell_limit : -1, T, route);
+    const SwSlots S = size_sw(P, trace, T, c->sm_count, sw_dir_budget(c, parts));
+
+    // Host staging: [descriptors | arena] in, [score pos len checks err | packed
+    // CIGARs] back.  Device: the same blocks, then the CIGAR slots, purity
+    // flags, the plan's work lists, its scratch and record, counters, band
+    // edges, direction tables.
+    int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
+    int32_t *hal, *hbl, *dal, *dbl, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der;
+    uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
+    char* dcg;
+    auto io_layout = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
+                         int64_t** ppo, uint8_t** ps, int32_t** psc, int32_t** ppos, int32_t** pln, uint8_t** pvf,
+                         int32_t** per, uint8_t** ppk) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
-        *po = k.take<int64_t>(n);
+        *po = k.take<int64_t>(n); *ppo = k.take<int64_t>(n);
         *ps = k.take<uint8_t>(arena);
-        *pp = k.take<uint8_t>(2 * (size_t)n);
-        *pw = k.take<int32_t>(max_work);
         *psc = k.take<int32_t>(n); *ppos = k.take<int32_t>(4 * (size_t)n);
         *pln = k.take<int32_t>(n); *pvf = k.take<uint8_t>(n);
-        *pcg = k.take<char>(cig + 1);
         *per = k.take<int32_t>(1, 4);
+        *ppk = k.take<uint8_t>((size_t)pkb, 4);
     };
-    Carve hk(nullptr), dk(nullptr);
-    in_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hvf, &hcg, &her);
-    in_layout(dk, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dvf, &dcg, &der);
-    const size_t dev_fixed = dk.off;
-    // (+ room after the staging blocks for the device plan's record)
-    if (!ensure_host(c, hk.off + 512 + sizeof(long long) * SP_RES)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
-    // stage inputs (device scratch is sized after planning)
+    uint8_t *dpure, *dtry = nullptr;
+    int32_t *dwork, *dscr, *dctr, *dedge;
+    long long* dres;
+    uint32_t* ddirs;
+    float *dfeat = nullptr, *dy = nullptr;
+    auto dev_layout = [&](char* base) {
+        Carve k(base);
+        io_layout(k, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dpos, &dln, &dvf, &der, &dpk);
+        dcg = k.take<char>(cig + 1);
+        dpure = k.take<uint8_t>(2 * (size_t)n);
+        if (route) {
+            dfeat = k.take<float>(66 * (size_t)n);
+            dy = k.take<float>(2 * (size_t)n);
+            dtry = k.take<uint8_t>((size_t)n);
+        }
+        dwork = k.take<int32_t>(2 * (size_t)n + 8);
+        dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
+        dres = k.take<long long>(SP_RES);
+        dctr = k.take<int32_t>(8, 4);
+        dedge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
+        ddirs = (S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        return k.off;
+    };
+    {
+        Carve hk(nullptr);
+        io_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
+        if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
+    }
+    if (fail_here(1) || !ensure_dev(c, dev_layout(nullptr))) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
     {
         Carve k(c->host);
-        in_layout(k, &ha, &hal, &hb, &hbl, &ho, &hseq, &hpure, &hwork, &hsc, &hpos, &hln, &hvf, &hcg, &her);
+        io_layout(k, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
     }
+    dev_layout(c->dev);
     parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
         for (int64_t i = lo; i < hi; ++i) {
             const ga_sw_request& r = reqs[i];
             ha[i] = a_off[i]; hal[i] = r.text_len;
             hb[i] = b_off[i]; hbl[i] = r.pattern_len;
-            ho[i] = out_off[i];
+            ho[i] = out_off[i]; hpo[i] = pk_off[i];
             if ((own[i] & 1) && r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
             if ((own[i] & 2) && r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
         }
     });
     std::memset(hseq + arena - 64, 0, 64);
-
-    // device memory: fixed blocks, then the planner's scratch, then counters,
-    // band edges and direction tables (sized from the plan; a first pass
-    // reserves the fixed part)
-    const size_t plan_off = dev_fixed;
-    size_t plan_end = plan_off;
-    int32_t* dscr = nullptr;
-    long long* dres = nullptr;
-    {
-        Carve k(nullptr);
-        k.off = plan_off;
-        k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
-        k.take<long long>(SP_RES);
-        plan_end = k.off;
-    }
-    const size_t hres_off = ((size_t)((char*)(her + 1) - c->host) + 255) & ~(size_t)255;
-    if (fail_here(1) || !ensure_dev(c, plan_end + 4096)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    long long* hres = reinterpret_cast<long long*>(c->host + hres_off);
-    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);
+    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);     // descriptors + arena, contiguous
     *h2d = (int64_t)in_bytes;
     PairDesc D;
     D.packed = nullptr;
     D.n = n;
-    SwPlan P;
-    // inputs to the device, purity flags, and the plan on the device; again
-    // from the start if the arena moves
-    auto stage = [&](bool first_time) -> int32_t {
-        {
-            Carve k(c->dev);
-            in_layout(k, &da, &dal, &db, &dbl, &dout, &dseq, &dpure, &dwork, &dsc, &dpos, &dln, &dvf, &dcg, &der);
-            k.off = plan_off;
-            dscr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
-            dres = k.take<long long>(SP_RES);
-        }
-        D.seq = dseq; D.pure = dpure;
-        D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
-        if ((first_time && fail_here(2)) ||
-            cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
-            cudaGetLastError();
-            *err = E_H2D;
-            return GA_DEVICE_ERROR;
-        }
-        // sentinel: too-large pairs keep score -1 (never written by a kernel)
-        cudaMemsetAsync(dsc, 0xff, sizeof(int32_t) * (size_t)n, c->stream);
-        cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, c->stream);
-        cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, c->stream);
-        cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream);
-        if ((first_time && fail_here(3)) || launch_pack(D, arena, nullptr, dpure, c->stream) != cudaSuccess) {
-            cudaGetLastError();
-            *err = E_LAUNCH;
-            return GA_DEVICE_ERROR;
-        }
-        if (device_plan_sw(D, s0, trace, trace ? cell_limit : -1, -1, dsc, dwork, dscr, dres, hres, T, c->stream,
-                           P) != cudaSuccess) {
-            cudaGetLastError();
-            *err = E_LAUNCH;
-            return GA_DEVICE_ERROR;
-        }
-        return GA_OK;
-    };
-    if (int32_t rs = stage(true)) return rs;
-    const SwSlots S = size_sw(P, trace, T, c->sm_count, sw_dir_budget(c, parts));
-    const uint64_t gen_before = c->dev_gen;
-    auto extra_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
-        Carve k(base);
-        k.off = plan_end;
-        *ctr = k.take<int32_t>(8, 4);
-        *edge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
-        // score-only 16-bit pairs keep their band edges there too
-        *dirs = (trace || S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
-        return k.off;
-    };
-    int32_t *dctr, *dedge;
-    uint32_t* ddirs;
-    if (!ensure_dev(c, extra_layout(nullptr, &dctr, &dedge, &ddirs))) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    if (c->dev_gen != gen_before) {              // the arena moved: everything again in the new one
-        if (int32_t rs = stage(false)) return rs;
+    D.seq = dseq; D.pure = dpure;
+    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
+    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *err = E_H2D;
+        return GA_DEVICE_ERROR;
     }
-    extra_layout(c->dev, &dctr, &dedge, &ddirs);
-    cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, c->stream);
-    if (launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, c->stream,
-                    dscr) != cudaSuccess ||
-        (trace && launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
-                                     dln, dcg, dvf, c->stream) != cudaSuccess)) {
+    // the device work: a fixed sequence for a given launch shape (no plan read
+    // back), so it is captured once per shape and replayed as a CUDA graph
+    auto enqueue = [&]() -> cudaError_t {
+        cudaStream_t st = c->stream;
+        // sentinel: too-large pairs keep score -1 (never written by a kernel)
+        cudaError_t e = cudaMemsetAsync(dsc, 0xff, sizeof(int32_t) * (size_t)n, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dpos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(der, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, st);
+        if (e == cudaSuccess) e = launch_pack(D, arena, nullptr, dpure, st);
+        if (e == cudaSuccess && route) e = launch_sw_route(D, s0.match, s0.gap_open, dfeat, dy, dtry, st);
+        if (e == cudaSuccess)
+            e = enqueue_plan_sw(D, s0, trace, trace ? cell_limit : -1, -1, dsc, dwork, dscr, dres, T, st, dtry);
+        if (e == cudaSuccess)
+            e = launch_plan(P, S, D, s0, trace, T, dwork, dsc, dpos, dln, dcg, ddirs, dedge, dctr, der, st, dscr, dres);
+        if (e == cudaSuccess && trace)
+            e = launch_sw_validate(D, ga_sw_scoring_t{s0.match, s0.mismatch, s0.gap_open, s0.gap_extend}, dsc, dpos,
+                                   dln, dcg, dvf, st);
+        if (e == cudaSuccess && trace) e = launch_cigar_pack(D, dln, dcg, dpo, dpk, st);
+        return e;
+    };
+    cudaError_t le = cudaErrorLaunchFailure;
+    if (!fail_here(3)) {
+        if (profiling_on()) {
+            le = enqueue();
+        } else {
+            const std::vector<uint64_t> key = {
+                c->dev_gen, (uint64_t)n, (uint64_t)arena, (uint64_t)cig, (uint64_t)trace | (uint64_t)route << 1,
+                (uint64_t)cell_limit,
+                (uint64_t)(uint32_t)s0.match | (uint64_t)(uint32_t)s0.mismatch << 32,
+                (uint64_t)(uint32_t)s0.gap_open | (uint64_t)(uint32_t)s0.gap_extend << 32,
+                (uint64_t)T.sw_pack16 | (uint64_t)T.sw_window << 8 | (uint64_t)T.sw_long_log2 << 16 |
+                    (uint64_t)T.sw_coop_log2 << 24 | (uint64_t)T.sw_opt16_pct << 32,
+                (uint64_t)P.ints[0], (uint64_t)P.ints[1], (uint64_t)P.ints[2], (uint64_t)P.dir[0],
+                (uint64_t)P.dir[1], (uint64_t)P.dir[2], (uint64_t)P.edge_slot, (uint64_t)P.max16_cells,
+                (uint64_t)P.n_opt, (uint64_t)P.dir_opt, (uint64_t)S.dir_words, (uint64_t)S.max_slots,
+                (uint64_t)S.s[0] | (uint64_t)S.s[1] << 32, (uint64_t)S.s[2] | (uint64_t)S.s_esc << 32};
+            le = replay_graph(c->swexec, c->swkey, key, c->swlaunches, c->stream, enqueue);
+        }
+    }
+    if (le != cudaSuccess) {
         cudaGetLastError();
         *err = E_LAUNCH;
         return GA_DEVICE_ERROR;
     }
-    const size_t out_bytes = (size_t)((char*)(der + 1) - (char*)dsc);
+    const size_t out_bytes = (size_t)((char*)(dpk + pkb) - (char*)dsc);
     *d2h = (int64_t)out_bytes;
     if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -1026,15 +1190,16 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         *err = E_SYNC;
         return GA_DEVICE_ERROR;
     }
-    if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    SwView v{hsc, hpos, hln, hcg, slot_end.data(), trace, trace ? hvf : nullptr, base, cig_base};
+    if (*her != 0) { *err = (*her & ERR_SCRATCH) ? E_SCRATCH : E_OVERFLOW; return GA_DEVICE_ERROR; }
+    SwView v{hsc, hpos, hln, hpk, hpo, slot_end.data(), trace, trace ? hvf : nullptr, base, cig_base};
     parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(base + lo, base + hi, v); });
     return GA_OK;
 }
 
 int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
-                 const char** err)
+                 const char** err, bool learned)
 {
+    learned = learned && sw_model_loaded();
     *err = nullptr;
     if (n <= 0) return GA_OK;
     if (int32_t st = sw_check(reqs, n, err)) return st;
@@ -1062,7 +1227,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     // tail leaves idle.
     constexpr int SW_CHUNKS = 8;
     const int K = n >= 8 * 1024 ? (int)std::max(1.0, std::min((double)SW_CHUNKS, cells / 2e9)) : 1;
-    if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h, 1);
+    if (K == 1) return sw_batch_range(reqs, n, 0, 0, trace, T, cell_limit, fin, err, &t_h2d, &t_d2h, 1, -1, learned);
     int32_t cut[SW_CHUNKS + 1];
     int64_t cig_at[SW_CHUNKS + 1];
     cut[0] = 0;
@@ -1091,7 +1256,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     auto run = [&](int k) {
         cudaSetDevice(dev);
         st[k] = sw_batch_range(reqs + cut[k], cut[k + 1] - cut[k], cut[k], cig_at[k], trace, T, cell_limit, fin,
-                               &errs[k], &h2d[k], &d2h[k], K, k);
+                               &errs[k], &h2d[k], &d2h[k], K, k, learned);
     };
     std::vector<std::thread> th;
     for (int k = 0; k + 1 < K; ++k) th.emplace_back(run, k);
@@ -1230,7 +1395,7 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
             res += r.resolved;
             if (v.trace && r.resolved && v.len[i] > 0) {
                 const int64_t at = v.slot_end[i] - v.len[i];
-                std::memcpy(cigar_buf + at, v.cig + at, (size_t)v.len[i]);
+                v.cigar(i, cigar_buf + at);
                 r.cigar_offset = at;
                 r.cigar_len = v.len[i];
                 bool rs = false, wf = false;
@@ -1309,7 +1474,7 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
             const int len = v.len[q];
             if (len > 0) {
                 const int64_t at = v.slot_end[q] - len;
-                std::memcpy(cigar_buf + v.cig_base + at, v.cig + at, (size_t)len);
+                v.cigar(q, cigar_buf + v.cig_base + at);
                 r.cigar_offset = v.cig_base + at;
                 r.cigar_len = len;
                 bool rs = false, wf = false;
@@ -1332,7 +1497,7 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
         st = sw_check(reqs, n, &err);
         if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
     } else {
-        st = sw_batch(reqs, n, limit, fin, &err);
+        st = sw_batch(reqs, n, limit, fin, &err, opt && opt->learned == 1);
     }
     if (st != GA_OK) {
         for (int32_t i = 0; i < n; ++i) results[i] = dflt;
@@ -1458,6 +1623,13 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
                      int32_t* out_score, int32_t* out_pos, int32_t* out_len, char* out_cigar, void* stream,
                      const char** err)
 {
+    return ga_sw_device_ex(b, sc, trace, cell_limit, nullptr, out_score, out_pos, out_len, out_cigar, stream, err);
+}
+
+int32_t ga_sw_device_ex(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, int64_t cell_limit,
+                        const ga_options* opt, int32_t* out_score, int32_t* out_pos, int32_t* out_len,
+                        char* out_cigar, void* stream, const char** err)
+{
     const char* e = nullptr;
     if (!b || b->n < 0 || b->seq_bytes < 0 ||
         (b->n > 0 && (!b->seq || !b->a_off || !b->a_len || !b->b_off || !b->b_len || !out_score || !out_pos ||
@@ -1469,33 +1641,76 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     const int32_t n = b->n;
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
+    struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
+    auto fail = [&](const char* msg) {
+        cudaGetLastError();
+        if (err) *err = msg;
+        return GA_DEVICE_ERROR;
+    };
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     const ga_tune T = tune_current();
-    // the checkpointed kernels (score-only: sw16so and the score-only
-    // widths): purity and the plan on the device, one small record back,
-    // then the launches
+    // the SW model picks the pairs the 16-bit kernel tries (traceback)
+    const bool route = trace && opt && opt->learned == 1 && sw_model_loaded();
+    float *dfeat = nullptr, *dy = nullptr;
+    uint8_t* dtry = nullptr;
+    // purity and the plan on the device, then the launches
     auto plan_layout = [&](char* base, uint8_t** pp, int32_t** scr, int32_t** wk, long long** res) {
         Carve k(base);
         *pp = k.take<uint8_t>(2 * (size_t)n);
         *scr = k.take<int32_t>((size_t)sw_plan_scratch_ints(n));
         *wk = k.take<int32_t>(2 * (size_t)n + 8);
         *res = k.take<long long>(SP_RES);
+        if (route) {
+            dfeat = k.take<float>(66 * (size_t)n);
+            dy = k.take<float>(2 * (size_t)n);
+            dtry = k.take<uint8_t>((size_t)n);
+        }
         return k.off;
     };
     uint8_t* dpure;
     int32_t *dscr, *dwork;
     long long* dres;
     const size_t plan_bytes = plan_layout(nullptr, &dpure, &dscr, &dwork, &dres);
-    if (!ensure_dev(c, plan_bytes + 4096) || !ensure_host(c, sizeof(long long) * SP_RES)) {
-        release_ctx(c);
-        if (err) *err = E_ALLOC;
-        return GA_DEVICE_ERROR;
-    }
+    if (!ensure_dev(c, plan_bytes + 4096) || !ensure_host(c, sizeof(long long) * SP_RES + 256)) return fail(E_ALLOC);
     long long* hres = reinterpret_cast<long long*>(c->host);
+    int32_t* herr = reinterpret_cast<int32_t*>(c->host + sizeof(long long) * SP_RES);
     PairDesc D;
     D.seq = b->seq; D.packed = nullptr;
     D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len;
     D.out_off = b->out_off; D.n = n;
+
+    // A synchronous traceback call with a cell limit replays the CUDA graph of
+    // its launch shape: the first call of a shape reads the plan back to size
+    // the per-warp memory and captures the launches in plan mode (sizes read
+    // on the device); a replay whose plan needs more memory than that (the
+    // pairs behind the same pointers grew) is flagged by the kernels
+    // (ERR_SCRATCH) and runs again through the read-back path.
+    const bool graph = !stream && trace && cell_limit >= 0 && !profiling_on();
+    std::vector<uint64_t> key;
+    if (graph) {
+        key = {0x5357445645ull, (uint64_t)n, (uint64_t)(uintptr_t)b->seq, (uint64_t)b->seq_bytes,
+               (uint64_t)(uintptr_t)b->a_off, (uint64_t)(uintptr_t)b->a_len, (uint64_t)(uintptr_t)b->b_off,
+               (uint64_t)(uintptr_t)b->b_len, (uint64_t)(uintptr_t)b->out_off, (uint64_t)(uintptr_t)out_score,
+               (uint64_t)(uintptr_t)out_pos, (uint64_t)(uintptr_t)out_len, (uint64_t)(uintptr_t)out_cigar,
+               (uint64_t)(uint32_t)sc.match | (uint64_t)(uint32_t)sc.mismatch << 32,
+               (uint64_t)(uint32_t)sc.gap_open | (uint64_t)(uint32_t)sc.gap_extend << 32, (uint64_t)cell_limit,
+               (uint64_t)T.sw_pack16 | (uint64_t)T.sw_window << 8 | (uint64_t)T.sw_long_log2 << 16 |
+                   (uint64_t)T.sw_coop_log2 << 24 | (uint64_t)T.sw_opt16_pct << 32 | (uint64_t)route << 40};
+        if (c->swexec && c->swkey.size() == key.size() + 2 && std::equal(key.begin(), key.end(), c->swkey.begin()) &&
+            c->swkey[key.size()] == c->dev_gen) {
+            int32_t* derr = reinterpret_cast<int32_t*>(c->swkey[key.size() + 1]);
+            note_graph_launches(c->swlaunches);
+            if (cudaGraphLaunch(c->swexec, st) != cudaSuccess ||
+                cudaMemcpyAsync(herr, derr, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return fail(E_SYNC);
+            if (!(*herr & ERR_SCRATCH)) return *herr ? fail(E_OVERFLOW) : GA_OK;
+            cudaGraphExecDestroy(c->swexec);           // sized for smaller pairs: plan again below
+            c->swexec = nullptr;
+            c->swkey.clear();
+        }
+    }
+
     cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
     cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
     if (out_len) cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
@@ -1504,15 +1719,11 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
         plan_layout(c->dev, &dpure, &dscr, &dwork, &dres);
         D.pure = dpure;
         if (launch_pack(D, b->seq_bytes, nullptr, dpure, st) != cudaSuccess) return false;
-        return device_plan_sw(D, sc, trace != 0, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P) ==
+        if (route && launch_sw_route(D, sc.match, sc.gap_open, dfeat, dy, dtry, st) != cudaSuccess) return false;
+        return device_plan_sw(D, sc, trace != 0, cell_limit, -2, out_score, dwork, dscr, dres, hres, T, st, P, dtry) ==
                cudaSuccess;
     };
-    if (!plan()) {
-        cudaGetLastError();
-        release_ctx(c);
-        if (err) *err = E_LAUNCH;
-        return GA_DEVICE_ERROR;
-    }
+    if (!plan()) return fail(E_LAUNCH);
     const SwSlots S = size_sw(P, trace != 0, T, c->sm_count, sw_dir_budget(c, 1));
     auto run_layout = [&](char* base, int32_t** ctr, int32_t** edge, uint32_t** dirs) {
         Carve k(base);
@@ -1525,36 +1736,46 @@ int32_t ga_sw_device(const ga_device_batch* b, ga_sw_scoring sc, int32_t trace, 
     int32_t *dctr, *dedge;
     uint32_t* ddirs;
     const uint64_t gen_before = c->dev_gen;
-    if (!ensure_dev(c, run_layout(nullptr, &dctr, &dedge, &ddirs))) {
-        release_ctx(c);
-        if (err) *err = E_ALLOC;
-        return GA_DEVICE_ERROR;
-    }
-    if (c->dev_gen != gen_before && !plan()) {      // the arena moved: plan again in the new one
-        cudaGetLastError();
-        release_ctx(c);
-        if (err) *err = E_LAUNCH;
-        return GA_DEVICE_ERROR;
-    }
+    if (!ensure_dev(c, run_layout(nullptr, &dctr, &dedge, &ddirs))) return fail(E_ALLOC);
+    if (c->dev_gen != gen_before && !plan()) return fail(E_LAUNCH);      // the arena moved: plan again in the new one
     run_layout(c->dev, &dctr, &dedge, &ddirs);
-    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
-    int32_t rc = GA_OK;
-    if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
-                    dctr + 32, st, dscr) != cudaSuccess) {
-        cudaGetLastError();
-        if (err) *err = E_LAUNCH;
-        rc = GA_DEVICE_ERROR;
+    if (graph) {
+        // the launches of this shape in plan mode, captured with the memsets,
+        // the purity pass and the planner, then replayed (this call included)
+        auto enqueue = [&]() -> cudaError_t {
+            cudaError_t x = cudaMemsetAsync(out_score, 0xff, sizeof(int32_t) * n, st);
+            if (x == cudaSuccess) x = cudaMemsetAsync(out_pos, 0xff, sizeof(int32_t) * 4 * (size_t)n, st);
+            if (x == cudaSuccess) x = cudaMemsetAsync(out_len, 0, sizeof(int32_t) * n, st);
+            if (x == cudaSuccess) x = cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+            if (x == cudaSuccess) x = launch_pack(D, b->seq_bytes, nullptr, dpure, st);
+            if (x == cudaSuccess && route) x = launch_sw_route(D, sc.match, sc.gap_open, dfeat, dy, dtry, st);
+            if (x == cudaSuccess)
+                x = enqueue_plan_sw(D, sc, true, cell_limit, -2, out_score, dwork, dscr, dres, T, st, dtry);
+            if (x == cudaSuccess)
+                x = launch_plan(P, S, D, sc, true, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+                                dctr + 32, st, dscr, dres);
+            return x;
+        };
+        std::vector<uint64_t> full = key;
+        full.push_back(c->dev_gen);
+        full.push_back((uint64_t)(uintptr_t)(dctr + 32));
+        if (replay_graph(c->swexec, c->swkey, full, c->swlaunches, st, enqueue) != cudaSuccess ||
+            cudaMemcpyAsync(herr, dctr + 32, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return fail(E_SYNC);
+        return *herr ? fail((*herr & ERR_SCRATCH) ? E_SCRATCH : E_OVERFLOW) : GA_OK;
     }
+    cudaMemsetAsync(dctr, 0, 64 * sizeof(int32_t), st);
+    if (launch_plan(P, S, D, sc, trace != 0, T, dwork, out_score, out_pos, out_len, out_cigar, ddirs, dedge, dctr,
+                    dctr + 32, st, dscr) != cudaSuccess)
+        return fail(E_LAUNCH);
     if (stream) {
         cudaEventRecord(c->done, st);
         c->pending = true;
     } else if (cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaGetLastError();
-        if (err) *err = E_SYNC;
-        rc = GA_DEVICE_ERROR;
+        return fail(E_SYNC);
     }
-    release_ctx(c);
-    return rc;
+    return GA_OK;
 }
 
 // ------------------------------------------------------------ provenance --

@@ -13,15 +13,23 @@ namespace ga {
 // (the calling thread participates).
 void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, int64_t)>& fn);
 
+// CIGARs come back from the device packed, 2 bits per op in op order
+// (M 0, X 1, I 2, D 3; op t at bits 2 (t % 4) of byte t / 4), each pair's at
+// its own byte offset: expand len ops into dst.
+void expand_cigar(const uint8_t* src, int len, char* dst);
+
 // Per-pair outputs of a WFA batch, valid during the finish callback.  The
-// CIGAR of pair i is cig[slot_end[i] - len[i] .. slot_end[i]).
+// CIGAR of pair i has len[i] ops packed at pk + pk_off[i]; its slot in the
+// caller's buffer ends at slot_end[i].
 struct WfaView {
     const int32_t* score;
     const int32_t* len;
-    const char* cig;
+    const uint8_t* pk;
+    const int64_t* pk_off;
     const int64_t* slot_end;
     bool trace;
     const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
+    void cigar(int64_t i, char* dst) const { expand_cigar(pk + pk_off[i], len[i], dst); }
 };
 using WfaFinish = std::function<void(int64_t lo, int64_t hi, const WfaView& v)>;
 
@@ -41,24 +49,26 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
 
 // Per-pair outputs of one range of an SW batch (requests [base, base + n)),
 // valid during the finish callback, which gets the batch's own indices: pair i
-// reads score[i - base] and so on; its CIGAR is cig[e - len .. e) with
-// e = slot_end[i - base], and goes to byte cig_base + e - len of the caller's
-// CIGAR buffer.
+// reads score[i - base] and so on; its CIGAR has len ops packed at
+// pk + pk_off[i - base] and goes to bytes cig_base + e - len .. cig_base + e
+// of the caller's CIGAR buffer, e = slot_end[i - base].
 struct SwView {
     const int32_t* score;     // -1 = too large
     const int32_t* pos;       // start_i, start_j, end_i, end_j per pair
     const int32_t* len;
-    const char* cig;
+    const uint8_t* pk;
+    const int64_t* pk_off;
     const int64_t* slot_end;
     bool trace;
     const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
     int64_t base;
     int64_t cig_base;
+    void cigar(int64_t q, char* dst) const { expand_cigar(pk + pk_off[q], len[q], dst); }
 };
 using SwFinish = std::function<void(int64_t lo, int64_t hi, const SwView& v)>;
 
 int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const SwFinish& fin,
-                 const char** err);
+                 const char** err, bool learned = false);
 
 // Result checks computed in the library (the reference's validate and
 // sw_validate semantics, src/api/api.cpp:84-156).

@@ -37,6 +37,13 @@ struct SwArgs {
     int32_t* err;
     int64_t coop_cells = -1; // sw32ck: items above this many cells run on a whole block (< 0: none)
     const int32_t* nwork_dev = nullptr;   // when set, the item count is read here at launch (device)
+    // Sizes read on the device (no plan read back before the launch): when
+    // plan is set, list plan_list of the device-built plan (plan_view) gives
+    // the items and the per-warp memory, and dir_cap / edge_cap (words of
+    // dirs, ints of edge) bound how many blocks run.
+    const long long* plan = nullptr;
+    int32_t plan_list = 0;
+    int64_t dir_cap = 0, edge_cap = 0;
 };
 
 // Two pairs per warp in 16-bit lanes (sw16ck.cu): work holds 2 pair indices
@@ -60,6 +67,9 @@ struct Sw16Args {
     int32_t ovf_limit = 1 << 30;          // a pair whose best reaches this is handed over ...
     int32_t* esc_list = nullptr;          // ... to the 32-bit kernel: appended here
     int32_t* esc_count = nullptr;
+    const long long* plan = nullptr;      // as in SwArgs
+    int32_t plan_list = 0;
+    int64_t dir_cap = 0, edge_cap = 0;
 };
 
 // The learned-bucketed WFA path (wfa_routed.cu).
@@ -85,13 +95,22 @@ struct RoutedArgs {
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 int64_t packed_arena_words(int64_t seq_bytes);
 cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* bad, cudaStream_t st);
+// Each pair's CIGAR (end of its slot) packed 2 bits per op at pk + pk_off[p] (wfa.cu).
+cudaError_t launch_cigar_pack(const PairDesc& D, const int32_t* len, const char* cig, const int64_t* pk_off,
+                              uint8_t* pk, cudaStream_t st);
 // WFA result checks on the device (wfa.cu): flags[p] = rescore_ok | wellformed_ok << 1.
 cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const int32_t* len, const char* cig,
                                 uint8_t* flags, cudaStream_t st);
-cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st);
+// 3-mer sketch features [n][66]; sw: the scaling of the SW variant model.
+cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st, bool sw = false);
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st);
 bool cost_model_loaded();
+bool sw_model_loaded();
 void prepare_mlp();
+// SW variant routing by the SW model: try16[p] = 1 for pairs the 16-bit
+// kernel should try (feat [n][66] and y [n][2] are scratch).
+cudaError_t launch_sw_route(const PairDesc& D, int match, int go, float* feat, float* y, uint8_t* try16,
+                            cudaStream_t st);
 int route_buckets();
 int64_t routed_stack_slot(int smax);
 int64_t lane_rec_slot();
@@ -132,6 +151,44 @@ cudaError_t launch_sw(const SwArgs& A, int slots, cudaStream_t st);
 constexpr int SP_LISTS = 3, SP_L16 = 0, SP_L32 = 1, SP_L32LONG = 2;
 constexpr int SP_COUNT = 0, SP_INTS = 3, SP_BASE = 6, SP_DIR = 9, SP_EDGE = 12, SP_MAXC16 = 13, SP_NOPT = 14,
               SP_DIROPT = 15, SP_RES = 16;
+// plan_list of the launch that takes the pairs the 16-bit kernel hands over
+constexpr int SP_ESC = SP_LISTS;
+
+// One launch's view of the plan.  Without a plan: the launch's own fields.
+// With one: the list's items (work0 + its base in the flattened lists; the
+// hand-over list: work0 itself and the count at nwork_dev), item count and
+// per-warp memory from the record, and whether this block runs: blocks past
+// dir_cap / (4 * dir_slot) (and edge_cap / (4 * edge_slot)) return at once.
+// A list whose one block of 4 warps does not fit runs nowhere and sets
+// ERR_SCRATCH.
+struct PlanView {
+    const int32_t* work;
+    int nwork;
+    int64_t dir_slot, edge_slot;
+    bool run;
+};
+__device__ __forceinline__ PlanView plan_view(const long long* plan, int list, const int32_t* work0, int nwork0,
+                                              const int32_t* nwork_dev, int64_t dir_slot0, int64_t edge_slot0,
+                                              int64_t dir_cap, int64_t edge_cap, int32_t* err)
+{
+    PlanView v{work0, nwork_dev ? *nwork_dev : nwork0, dir_slot0, edge_slot0, true};
+    if (!plan) return v;
+    if (list == SP_ESC) {
+        v.dir_slot = (plan[SP_DIROPT] + 3) / 4 * 4;
+    } else {
+        const long long ints = plan[SP_INTS + list];
+        v.work = work0 + plan[SP_BASE + list];
+        v.nwork = (int)(list == SP_L16 ? ints / 2 : ints);
+        v.dir_slot = (plan[SP_DIR + list] + 3) / 4 * 4;
+    }
+    v.edge_slot = plan[SP_EDGE] > 2 ? plan[SP_EDGE] : 2;
+    long long blocks = gridDim.x;
+    if (v.dir_slot > 0) blocks = min(blocks, (long long)(dir_cap / (4 * v.dir_slot)));
+    if (edge_cap > 0) blocks = min(blocks, (long long)(edge_cap / (4 * v.edge_slot)));
+    if (blocks < 1 && v.nwork > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_SCRATCH);
+    v.run = blockIdx.x < blocks;
+    return v;
+}
 struct SwPlanArgs {
     PairDesc D;                  // a = text (rows), b = pattern (columns); D.pure set
     int32_t match, mismatch, gap_open, gap_extend;
@@ -139,6 +196,7 @@ struct SwPlanArgs {
     int32_t use16;               // the 16-bit kernels may be used
     int32_t window;              // sw16ck recompute window, tiles (2 or 4)
     int32_t opt16_pct;           // optimistic 16-bit eligibility (sw16_eligible_opt), 100: the strict bound
+    const uint8_t* try16 = nullptr;   // when set: the optimistic rule per pair (the SW model's routing) instead
     int32_t long_log2;           // sw32ck long shape above 2^long_log2 cells
     int32_t too_large_score;     // score written for pairs above cell_limit
     int32_t score_only;          // 1: lists of the score-only kernels (sw16so, sw_kernel)

@@ -39,7 +39,7 @@ const __nv_bfloat16* cost_model_weights();
 // ------------------------------------------------------------------ sketch --
 // One warp per pair: 3-mer histograms of both sides in shared memory.
 __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restrict__ feat,
-                                                     int32_t* __restrict__ lower_bound)
+                                                     int32_t* __restrict__ lower_bound, float s_diff, float s_len)
 {
     __shared__ int hist[8][64];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -61,15 +61,15 @@ __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restri
         }
         __syncwarp();
         const int d0 = hist[wib][lane], d1 = hist[wib][lane + 32];
-        feat[(int64_t)p * NF + lane] = d0 * 0.125f;
-        feat[(int64_t)p * NF + lane + 32] = d1 * 0.125f;
+        feat[(int64_t)p * NF + lane] = d0 * s_diff;
+        feat[(int64_t)p * NF + lane + 32] = d1 * s_diff;
         int l1 = abs(d0) + abs(d1);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL, l1, o);
         if (lane == 0) {
             const int m = D.a_len[p], n = D.b_len[p];
-            feat[(int64_t)p * NF + 64] = m * (1.0f / 256.0f);
-            feat[(int64_t)p * NF + 65] = n * (1.0f / 256.0f);
+            feat[(int64_t)p * NF + 64] = m * s_len;
+            feat[(int64_t)p * NF + 65] = n * s_len;
             if (lower_bound) lower_bound[p] = max(abs(m - n), (l1 + 5) / 6);
         }
         __syncwarp();
@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(256) sketch_kernel(PairDesc D, float* __restri
 // The histogram is indexed by the window's own order, c0 + 4 c1 + 16 c2; the
 // feature order 16 c0 + 4 c1 + c2 is applied when the features are written.
 __global__ void __launch_bounds__(256) sketch_packed_kernel(PairDesc D, float* __restrict__ feat,
-                                                            int32_t* __restrict__ lower_bound)
+                                                            int32_t* __restrict__ lower_bound, float s_diff,
+                                                            float s_len)
 {
     __shared__ int hist[8][64];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -107,15 +108,15 @@ __global__ void __launch_bounds__(256) sketch_packed_kernel(PairDesc D, float* _
         const int k0 = lane, k1 = lane + 32;
         const int d0 = hist[wib][((k0 & 3) << 4) | (k0 & 12) | (k0 >> 4)];
         const int d1 = hist[wib][((k1 & 3) << 4) | (k1 & 12) | (k1 >> 4)];
-        feat[(int64_t)p * NF + k0] = d0 * 0.125f;
-        feat[(int64_t)p * NF + k1] = d1 * 0.125f;
+        feat[(int64_t)p * NF + k0] = d0 * s_diff;
+        feat[(int64_t)p * NF + k1] = d1 * s_diff;
         int l1 = abs(d0) + abs(d1);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL, l1, o);
         if (lane == 0) {
             const int m = D.a_len[p], n = D.b_len[p];
-            feat[(int64_t)p * NF + 64] = m * (1.0f / 256.0f);
-            feat[(int64_t)p * NF + 65] = n * (1.0f / 256.0f);
+            feat[(int64_t)p * NF + 64] = m * s_len;
+            feat[(int64_t)p * NF + 65] = n * s_len;
             if (lower_bound) lower_bound[p] = max(abs(m - n), (l1 + 5) / 6);
         }
         __syncwarp();
@@ -626,14 +627,21 @@ struct Model {
     int step = 0;
     bool ready = false;
 };
+// Two models per device, the same network: slot 0 the WFA cost model (edit
+// distance and wavefront work), slot 1 the Smith-Waterman variant model (best
+// score as a fraction of the all-match score).  The C API's set / get /
+// forward / gradient / train calls act on the calling thread's selected slot
+// (ga_model_select); each routing pass reads its own slot.
+constexpr int N_MODEL_SLOTS = 2;
 static std::mutex g_model_mu;
-static Model g_models[16];
+static Model g_models[16][N_MODEL_SLOTS];
+static thread_local int t_model_slot = 0;
 
-static Model* model_for_current(bool create)
+static Model* model_for(int slot, bool create)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) { cudaGetLastError(); return nullptr; }
-    Model& M = g_models[dev];
+    Model& M = g_models[dev][slot];
     if (!M.master && create) {
         if (cudaMalloc(&M.master, NPARAM * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&M.w, NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess ||
@@ -692,34 +700,74 @@ static cudaError_t run_backward(const __nv_bfloat16* w, const float* feat, const
     return cudaGetLastError();
 }
 
-cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st)
+cudaError_t launch_sketch(const PairDesc& D, float* feat, int32_t* lb, cudaStream_t st, bool sw)
 {
     if (D.n <= 0) return cudaSuccess;
     int blocks = (D.n + 7) / 8;
     blocks = std::min(blocks, device_sms() * 16);
+    // WFA pairs (150-10,000 bases): differences / 8, lengths / 256; SW pairs
+    // (text with flanks, up to tens of kb): differences / 64, lengths / 8192
+    const float s_diff = sw ? 1.0f / 64.0f : 0.125f, s_len = sw ? 1.0f / 8192.0f : 1.0f / 256.0f;
     launch_begin(K_SKETCH, st);
-    if (D.packed) sketch_packed_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
-    else sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb);
+    if (D.packed) sketch_packed_kernel<<<blocks, 256, 0, st>>>(D, feat, lb, s_diff, s_len);
+    else sketch_kernel<<<blocks, 256, 0, st>>>(D, feat, lb, s_diff, s_len);
     launch_end(K_SKETCH, st);
     return cudaGetLastError();
 }
 
-// The current device's model weights for inference, or null when none is loaded.
-const __nv_bfloat16* cost_model_weights()
+static Model* model_for_current(bool create) { return model_for(t_model_slot, create); }
+
+// A slot's weights on the current device for inference, or null when none is loaded.
+static const __nv_bfloat16* model_weights(int slot)
 {
     std::lock_guard<std::mutex> lk(g_model_mu);
-    Model* M = model_for_current(false);
+    Model* M = model_for(slot, false);
     return (M && M->ready) ? M->w : nullptr;
 }
+const __nv_bfloat16* cost_model_weights() { return model_weights(0); }
 
 bool cost_model_loaded() { return cost_model_weights() != nullptr; }
+bool sw_model_loaded() { return model_weights(1) != nullptr; }
 
-// Routing inference: the tensor-core forward pass.
+// Inference of the selected slot's model: the tensor-core forward pass.
 cudaError_t launch_mlp_forward(const float* feat, int n, float* y, cudaStream_t st)
 {
-    const __nv_bfloat16* w = cost_model_weights();
+    const __nv_bfloat16* w = model_weights(t_model_slot);
     if (!w) return cudaErrorNotReady;
     return run_forward_tc(w, feat, n, y, st);
+}
+
+// SW variant routing: features of every pair (a = text, b = pattern), the
+// SW model's prediction of the best score as a fraction of the all-match
+// score match * min(m, n), and try16[p] = 1 for a pair the 16-bit kernel
+// should try: its predicted score with a margin (x 1.15 + 8 matches) fits 16
+// bits (sw16_eligible_opt's test).  Purity and the exact hand-over at the
+// 16-bit limit are the planner's and the kernel's, so a wrong prediction only
+// costs time.
+__global__ void sw_route_kernel(PairDesc D, const float* __restrict__ y, int match, int go, uint8_t* __restrict__ try16)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
+        const int m = D.a_len[p], n = D.b_len[p];
+        const float frac = fminf(fmaxf(y[2 * (int64_t)p], 0.f), 1.f);
+        const float all = (float)match * (float)min(max(m, 0), max(n, 0));
+        const float pred = frac * all * 1.15f + 8.f * (float)match;
+        try16[p] = (m > 0 && n > 0 && pred + (float)(BIAS16 + go) < 32000.f) ? 1 : 0;
+    }
+}
+
+cudaError_t launch_sw_route(const PairDesc& D, int match, int go, float* feat, float* y, uint8_t* try16, cudaStream_t st)
+{
+    const __nv_bfloat16* w = model_weights(1);
+    if (!w) return cudaErrorNotReady;
+    if (D.n <= 0) return cudaSuccess;
+    cudaError_t e = launch_sketch(D, feat, nullptr, st, true);
+    if (e == cudaSuccess) e = run_forward_tc(w, feat, D.n, y, st);
+    if (e != cudaSuccess) return e;
+    int blocks = std::min((D.n + 255) / 256, device_sms() * 8);
+    launch_begin(K_ROUTE, st);
+    sw_route_kernel<<<blocks, 256, 0, st>>>(D, y, match, go, try16);
+    launch_end(K_ROUTE, st);
+    return cudaGetLastError();
 }
 
 }  // namespace ga
@@ -729,6 +777,13 @@ using namespace ga;
 extern "C" {
 
 int32_t ga_cost_model_nparams(void) { return NPARAM; }
+
+int32_t ga_model_select(int32_t which)
+{
+    if (which < 0 || which >= N_MODEL_SLOTS) return GA_INVALID_ARGUMENT;
+    t_model_slot = which;
+    return GA_OK;
+}
 
 int32_t ga_cost_model_set(const float* params, int32_t n)
 {
@@ -769,7 +824,19 @@ int32_t ga_wfa_features(const ga_device_batch* b, float* feat, int32_t* lower_bo
     D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
     D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len; D.out_off = b->out_off; D.n = b->n;
     cudaStream_t st = (cudaStream_t)stream;
-    if (launch_sketch(D, feat, lower_bound, st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    if (launch_sketch(D, feat, lower_bound, st, false) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    if (!stream && cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
+    return GA_OK;
+}
+
+int32_t ga_sw_features(const ga_device_batch* b, float* feat, void* stream)
+{
+    if (!b || b->n < 0 || !feat) return GA_INVALID_ARGUMENT;
+    PairDesc D;
+    D.seq = b->seq; D.packed = nullptr; D.pure = nullptr;
+    D.a_off = b->a_off; D.a_len = b->a_len; D.b_off = b->b_off; D.b_len = b->b_len; D.out_off = b->out_off; D.n = b->n;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (launch_sketch(D, feat, nullptr, st, true) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
     if (!stream && cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return GA_DEVICE_ERROR; }
     return GA_OK;
 }
@@ -778,7 +845,7 @@ int32_t ga_mlp_forward(const float* feat, int32_t n, float* y, void* stream)
 {
     if (!feat || !y || n < 0) return GA_INVALID_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
-    const __nv_bfloat16* w = cost_model_weights();
+    const __nv_bfloat16* w = model_weights(t_model_slot);
     if (!w) return GA_INVALID_ARGUMENT;
     const cudaError_t e = run_forward(w, feat, n, y, st);
     if (e == cudaErrorNotReady) return GA_INVALID_ARGUMENT;

@@ -141,23 +141,30 @@ __device__ __forceinline__ void sw_forward(const SwArgs& A, int m, int n, const 
     }
 }
 
-template <int C>
+// PLAN: items and band-edge memory from the device-built plan (plan_view).
+template <int C, bool PLAN>
 __global__ void __launch_bounds__(128) sw_kernel(SwArgs A)
 {
     extern __shared__ int4 prof_smem[];
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    int32_t* eslot = A.edge + slot * A.edge_slot;
+    PlanView V{A.work, A.nwork, A.dir_slot, A.edge_slot, true};
+    if constexpr (PLAN) {
+        V = plan_view(A.plan, A.plan_list, A.work, A.nwork, nullptr, A.dir_slot, A.edge_slot, A.dir_cap, A.edge_cap,
+                      A.err);
+        if (!V.run) return;
+    }
+    int32_t* eslot = A.edge + slot * V.edge_slot;
     int4* prof = prof_smem + wib * (C * 32);           // 4 letters x C/4 quads x 32 lanes
 
     for (;;) {
         int w = 0;
         if (t == 0) w = atomicAdd(A.counter, 1);
         w = __shfl_sync(FULL, w, 0);
-        if (w >= A.nwork) break;
+        if (w >= V.nwork) break;
         __syncwarp();
-        const int p = A.work[w];
+        const int p = V.work[w];
         const int m = A.D.a_len[p];            // rows (text)
         const int n = A.D.b_len[p];            // columns (pattern)
         const uint8_t* text = A.D.seq + A.D.a_off[p];
@@ -195,16 +202,17 @@ int sw_max_slots(int sm_count)
 {
     const size_t smem = sw_smem(SW_SCORE_C);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw_kernel<SW_SCORE_C>, 128, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw_kernel<SW_SCORE_C, false>, 128, smem);
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
 cudaError_t launch_sw(const SwArgs& A, int slots, cudaStream_t st)
 {
-    if (A.nwork <= 0) return cudaSuccess;
+    if (A.nwork <= 0 && !A.plan) return cudaSuccess;
     const int blocks = (slots + 3) / 4;
     launch_begin(K_SW_SCORE, st);
-    sw_kernel<SW_SCORE_C><<<blocks, 128, sw_smem(SW_SCORE_C), st>>>(A);
+    if (A.plan) sw_kernel<SW_SCORE_C, true><<<blocks, 128, sw_smem(SW_SCORE_C), st>>>(A);
+    else sw_kernel<SW_SCORE_C, false><<<blocks, 128, sw_smem(SW_SCORE_C), st>>>(A);
     launch_end(K_SW_SCORE, st);
     return cudaGetLastError();
 }

@@ -431,10 +431,11 @@ __device__ void fwd16_coop(const FwdCtx& X, int N, int t, int wib, int& vA, int&
 // checkpoint memory (warp 0's slot when coop); prof: this warp's shared
 // memory.  In coop every warp returns after the same barriers; the caller
 // closes the item with one more barrier.
-template <int TG>
-__device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uint32_t* wslot, uint32_t* prof,
-                        int (*s_best)[6])
+template <int TG, bool PLAN>
+__device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, int w, bool coop, int wib, int t,
+                        uint32_t* wslot, uint32_t* prof, int (*s_best)[6])
 {
+    const int32_t* work = PLAN ? pwork : A.work;
     const int go = A.gap_open, ge = A.gap_extend;
     const int sm = A.match + go, sx = A.mismatch + go;
     // unbiased forward constants (per half)
@@ -445,9 +446,9 @@ __device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uin
     // biased recompute constants (sw16.cu)
     const uint32_t B2 = (uint32_t)CK_BIAS * 0x10001u;
 
-    const int pa = A.work[2 * w];
-    const bool has_b = A.work[2 * w + 1] >= 0;
-    const int pb = has_b ? A.work[2 * w + 1] : pa;
+    const int pa = work[2 * w];
+    const bool has_b = work[2 * w + 1] >= 0;
+    const int pb = has_b ? work[2 * w + 1] : pa;
     const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
     const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
     const uint8_t* textA = A.D.seq + A.D.a_off[pa];
@@ -830,18 +831,33 @@ __device__ void ck_item(const Sw16Args& A, int w, bool coop, int wib, int t, uin
 // warp takes items of its own.
 // BLK: the variant with the whole-block phase; without it every warp takes
 // items of its own and no block barrier is met.
-template <int TG, bool BLK>
+// PLAN: items and per-warp memory from the device-built plan (plan_view),
+// the list and its length kept in shared memory; otherwise the launch's own.
+template <int TG, bool BLK, bool PLAN>
 __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
 {
     static_assert(TG == 2 || TG == 4, "tile groups split the warp evenly, window rows are 16-byte vectors");
     extern __shared__ uint32_t ck_smem[];
     __shared__ int s_item;
     __shared__ int s_best[4][6];
+    __shared__ const int32_t* s_work;
+    __shared__ int s_nwork;
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
-    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
+    int64_t dir_slot = A.dir_slot;
+    if constexpr (PLAN) {
+        const PlanView V = plan_view(A.plan, A.plan_list, A.work, A.nwork, nullptr, A.dir_slot, A.edge_slot,
+                                     A.dir_cap, A.edge_cap, A.err);
+        if (!V.run) return;
+        dir_slot = V.dir_slot;
+        if (threadIdx.x == 0) { s_work = V.work; s_nwork = V.nwork; }
+        __syncthreads();
+    }
+    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * dir_slot;
+    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * dir_slot;
     uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
+#define SW16_NWORK (PLAN ? s_nwork : A.nwork)
+#define SW16_WORK (PLAN ? s_work : A.work)
 
     // one call site of ck_item, so its body is in the kernel once
     bool block_phase = BLK && A.coop_cells >= 0;
@@ -853,8 +869,8 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
             __syncthreads();
             const int wb = s_item;
             __syncthreads();
-            if (wb >= A.nwork) break;
-            const int pa = A.work[2 * wb], pb = A.work[2 * wb + 1];
+            if (wb >= SW16_NWORK) break;
+            const int pa = SW16_WORK[2 * wb], pb = SW16_WORK[2 * wb + 1];
             const int M = max(A.D.a_len[pa], pb >= 0 ? A.D.a_len[pb] : 0);
             const int N = max(A.D.b_len[pa], pb >= 0 ? A.D.b_len[pb] : 0);
             if ((int64_t)M * N > A.coop_cells) {
@@ -868,10 +884,10 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
         if (!coop && w < 0) {
             if (t == 0) w = atomicAdd(A.counter, 1);
             w = __shfl_sync(FULL, w, 0);
-            if (w >= A.nwork) break;
+            if (w >= SW16_NWORK) break;
         }
         __syncwarp();
-        ck_item<TG>(A, w, coop, wib, t, coop ? bslot : wslot, prof, s_best);
+        ck_item<TG, PLAN>(A, s_work, w, coop, wib, t, coop ? bslot : wslot, prof, s_best);
         if (coop) __syncthreads();
     }
 }
@@ -881,12 +897,24 @@ __global__ void __launch_bounds__(128, 4) sw16ck_kernel(Sw16Args A)
 // carry the band boundaries), the end cell by the reference's score-only rule
 // (c9_key).  dir_slot = sw16so_dir_words.  Outputs: score, and end_i / end_j
 // (0-based) for a positive score, -1 otherwise; start cells -1.
+template <bool PLAN>
 __global__ void __launch_bounds__(128, 4) sw16so_kernel(Sw16Args A)
 {
     extern __shared__ uint32_t ck_smem[];
+    __shared__ const int32_t* s_work;
+    __shared__ int s_nwork;
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    uint32_t* rows = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
+    int64_t dir_slot = A.dir_slot;
+    if constexpr (PLAN) {
+        const PlanView V = plan_view(A.plan, A.plan_list, A.work, A.nwork, nullptr, A.dir_slot, A.edge_slot,
+                                     A.dir_cap, A.edge_cap, A.err);
+        if (!V.run) return;
+        dir_slot = V.dir_slot;
+        if (threadIdx.x == 0) { s_work = V.work; s_nwork = V.nwork; }
+        __syncthreads();
+    }
+    uint32_t* rows = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * dir_slot;
     uint32_t* ce = rows + SO_ROW_WORDS;
     uint32_t* prof = ck_smem + wib * CK_WARP_WORDS;
     const int go = A.gap_open, ge = A.gap_extend;
@@ -898,11 +926,11 @@ __global__ void __launch_bounds__(128, 4) sw16so_kernel(Sw16Args A)
         int w = 0;
         if (t == 0) w = atomicAdd(A.counter, 1);
         w = __shfl_sync(FULL, w, 0);
-        if (w >= A.nwork) break;
+        if (w >= SW16_NWORK) break;
         __syncwarp();
-        const int pa = A.work[2 * w];
-        const bool has_b = A.work[2 * w + 1] >= 0;
-        const int pb = has_b ? A.work[2 * w + 1] : pa;
+        const int pa = SW16_WORK[2 * w];
+        const bool has_b = SW16_WORK[2 * w + 1] >= 0;
+        const int pb = has_b ? SW16_WORK[2 * w + 1] : pa;
         const int mA = A.D.a_len[pa], nA = A.D.b_len[pa];
         const int mB = A.D.a_len[pb], nB = A.D.b_len[pb];
         const int M = max(mA, mB), N = max(nA, nB);
@@ -947,19 +975,23 @@ __global__ void __launch_bounds__(128, 4) sw16so_kernel(Sw16Args A)
 
 static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t); }
 
+#undef SW16_NWORK
+#undef SW16_WORK
+
 int sw16so_max_slots(int sm_count)
 {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16so_kernel, 128, sw16ck_smem());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16so_kernel<false>, 128, sw16ck_smem());
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
 cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st)
 {
-    if (A.nwork <= 0) return cudaSuccess;
+    if (A.nwork <= 0 && !A.plan) return cudaSuccess;
     if (slots < 4) return cudaErrorInvalidValue;
     launch_begin(K_SW16X2_SCORE, st);
-    sw16so_kernel<<<slots / 4, 128, sw16ck_smem(), st>>>(A);
+    if (A.plan) sw16so_kernel<true><<<slots / 4, 128, sw16ck_smem(), st>>>(A);
+    else sw16so_kernel<false><<<slots / 4, 128, sw16ck_smem(), st>>>(A);
     launch_end(K_SW16X2_SCORE, st);
     return cudaGetLastError();
 }
@@ -967,23 +999,28 @@ cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st)
 int sw16ck_max_slots(int sm_count, int window)
 {
     int per_sm = 0;
-    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4, true>, 128, sw16ck_smem());
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2, true>, 128, sw16ck_smem());
+    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4, true, false>, 128, sw16ck_smem());
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2, true, false>, 128, sw16ck_smem());
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
 
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st)
 {
-    if (A.nwork <= 0) return cudaSuccess;
+    if (A.nwork <= 0 && !A.plan) return cudaSuccess;
     if (window != 2 && window != 4) return cudaErrorInvalidValue;
     const int grid = (slots + 3) / 4;
     launch_begin(K_SW16X2_TRACE, st);
+    const bool plan = A.plan != nullptr;
     if (window == 4) {
-        if (blocks) sw16ck_kernel<4, true><<<grid, 128, sw16ck_smem(), st>>>(A);
-        else sw16ck_kernel<4, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+        if (blocks) plan ? sw16ck_kernel<4, true, true><<<grid, 128, sw16ck_smem(), st>>>(A)
+                         : sw16ck_kernel<4, true, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+        else plan ? sw16ck_kernel<4, false, true><<<grid, 128, sw16ck_smem(), st>>>(A)
+                  : sw16ck_kernel<4, false, false><<<grid, 128, sw16ck_smem(), st>>>(A);
     } else {
-        if (blocks) sw16ck_kernel<2, true><<<grid, 128, sw16ck_smem(), st>>>(A);
-        else sw16ck_kernel<2, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+        if (blocks) plan ? sw16ck_kernel<2, true, true><<<grid, 128, sw16ck_smem(), st>>>(A)
+                         : sw16ck_kernel<2, true, false><<<grid, 128, sw16ck_smem(), st>>>(A);
+        else plan ? sw16ck_kernel<2, false, true><<<grid, 128, sw16ck_smem(), st>>>(A)
+                  : sw16ck_kernel<2, false, false><<<grid, 128, sw16ck_smem(), st>>>(A);
     }
     launch_end(K_SW16X2_TRACE, st);
     return cudaGetLastError();

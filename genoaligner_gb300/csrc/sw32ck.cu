@@ -533,20 +533,33 @@ __device__ void c32_pair(const SwArgs& A, int p, bool coop, int wib, int t, uint
 // Work items come largest first.  Items above A.coop_cells cells are taken by
 // a whole block (its 4 warps share the forward pass); from the first smaller
 // item on, each warp takes items of its own.
-template <int K, int CT>
+// PLAN: items and per-warp memory from the device-built plan (plan_view),
+// the list and its length kept in shared memory; otherwise the launch's own.
+template <int K, int CT, bool PLAN>
 __global__ void __launch_bounds__(128, 4) sw32ck_kernel(SwArgs A)
 {
     constexpr int WSB = c32_warp_smem_bytes(K, CT);
     extern __shared__ int4 c32_smem[];
     __shared__ int s_item;
     __shared__ int s_best[C32_MAX_WARPS][3];
+    __shared__ const int32_t* s_work;
+    __shared__ int s_nwork;
     const int t = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * A.dir_slot;
-    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * A.dir_slot;
+    int64_t dir_slot = A.dir_slot;
+    if constexpr (PLAN) {
+        const PlanView V = plan_view(A.plan, A.plan_list, A.work, A.nwork, A.nwork_dev, A.dir_slot, A.edge_slot,
+                                     A.dir_cap, A.edge_cap, A.err);
+        if (!V.run) return;
+        dir_slot = V.dir_slot;
+        if (threadIdx.x == 0) { s_work = V.work; s_nwork = V.nwork; }
+        __syncthreads();
+    }
+    uint32_t* wslot = A.dirs + ((int64_t)blockIdx.x * (blockDim.x >> 5) + wib) * dir_slot;
+    uint32_t* bslot = A.dirs + (int64_t)blockIdx.x * (blockDim.x >> 5) * dir_slot;
     unsigned char* wsm = reinterpret_cast<unsigned char*>(c32_smem) + wib * WSB;
-
-    const int nwork = A.nwork_dev ? *A.nwork_dev : A.nwork;
+    const int nwork = PLAN ? s_nwork : (A.nwork_dev ? *A.nwork_dev : A.nwork);
+#define SW32_WORK (PLAN ? s_work : A.work)
     // one call site of c32_pair, so its body is in the kernel once
     bool block_phase = A.coop_cells >= 0;
     for (;;) {
@@ -558,7 +571,7 @@ __global__ void __launch_bounds__(128, 4) sw32ck_kernel(SwArgs A)
             const int wb = s_item;
             __syncthreads();
             if (wb >= nwork) break;
-            const int p = A.work[wb];
+            const int p = SW32_WORK[wb];
             if ((int64_t)A.D.a_len[p] * A.D.b_len[p] > A.coop_cells) {
                 w = wb;
                 coop = true;
@@ -573,10 +586,11 @@ __global__ void __launch_bounds__(128, 4) sw32ck_kernel(SwArgs A)
             if (w >= nwork) break;
         }
         __syncwarp();
-        c32_pair<K, CT>(A, A.work[w], coop, wib, t, coop ? bslot : wslot, wsm, s_best);
+        c32_pair<K, CT>(A, SW32_WORK[w], coop, wib, t, coop ? bslot : wslot, wsm, s_best);
         if (coop) __syncthreads();
     }
 }
+#undef SW32_WORK
 
 template <int K, int CT>
 static size_t c32_smem(int warps = 4) { return (size_t)warps * c32_warp_smem_bytes(K, CT); }
@@ -585,10 +599,13 @@ int sw32ck_max_slots(bool long_pairs, int sm_count)
 {
     int per_sm = 0;
     if (long_pairs) {
-        cudaFuncSetAttribute(sw32ck_kernel<512, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c32_smem<512, 16>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<512, 16>, 128, c32_smem<512, 16>());
+        cudaFuncSetAttribute(sw32ck_kernel<512, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)c32_smem<512, 16>());
+        cudaFuncSetAttribute(sw32ck_kernel<512, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)c32_smem<512, 16>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<512, 16, false>, 128, c32_smem<512, 16>());
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<64, 2>, 128, c32_smem<64, 2>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<64, 2, false>, 128, c32_smem<64, 2>());
     }
     return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
 }
@@ -596,11 +613,16 @@ int sw32ck_max_slots(bool long_pairs, int sm_count)
 // slots: warp slots of A.dirs, a multiple of 4 (blocks of 4 warps).
 cudaError_t launch_sw32ck(const SwArgs& A, bool long_pairs, int slots, cudaStream_t st)
 {
-    if (A.nwork <= 0 && !A.nwork_dev) return cudaSuccess;
+    if (A.nwork <= 0 && !A.nwork_dev && !A.plan) return cudaSuccess;
     if (slots < 4) return cudaErrorInvalidValue;
     launch_begin(K_SW32_TRACE, st);
-    if (long_pairs) sw32ck_kernel<512, 16><<<slots / 4, 128, c32_smem<512, 16>(), st>>>(A);
-    else sw32ck_kernel<64, 2><<<slots / 4, 128, c32_smem<64, 2>(), st>>>(A);
+    if (A.plan) {
+        if (long_pairs) sw32ck_kernel<512, 16, true><<<slots / 4, 128, c32_smem<512, 16>(), st>>>(A);
+        else sw32ck_kernel<64, 2, true><<<slots / 4, 128, c32_smem<64, 2>(), st>>>(A);
+    } else {
+        if (long_pairs) sw32ck_kernel<512, 16, false><<<slots / 4, 128, c32_smem<512, 16>(), st>>>(A);
+        else sw32ck_kernel<64, 2, false><<<slots / 4, 128, c32_smem<64, 2>(), st>>>(A);
+    }
     launch_end(K_SW32_TRACE, st);
     return cudaGetLastError();
 }

@@ -42,9 +42,11 @@ __global__ void sp_classify_kernel(SwPlanArgs P)
             } else {
                 const bool pure = P.use16 && P.D.pure[p] && P.D.pure[n + p];
                 const bool strict = pure && sw16_eligible(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend);
-                const bool u16 = strict || (!P.score_only && pure && sw16_eligible_opt(m, nn, P.match, P.mismatch,
-                                                                                       P.gap_open, P.gap_extend,
-                                                                                       P.opt16_pct));
+                const bool opt = P.try16 ? (P.try16[p] != 0 && m > 0 && nn > 0 &&
+                                            sw16_scheme_ok(P.match, P.mismatch, P.gap_open, P.gap_extend))
+                                         : sw16_eligible_opt(m, nn, P.match, P.mismatch, P.gap_open, P.gap_extend,
+                                                             P.opt16_pct);
+                const bool u16 = strict || (!P.score_only && pure && opt);
                 if (u16 && !strict) {           // may be handed to the 32-bit long-shape kernel
                     atomicAdd(reinterpret_cast<unsigned long long*>(P.res + SP_NOPT), 1ull);
                     atomicMax(reinterpret_cast<unsigned long long*>(P.res + SP_DIROPT),

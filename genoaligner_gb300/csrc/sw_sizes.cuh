@@ -1,6 +1,6 @@
 // sw_sizes.cuh -- shapes, eligibility and per-warp memory of the
-// Smith-Waterman traceback kernels, shared by the kernels (sw16.cu,
-// sw16ck.cu, sw32ck.cu), the device planner (sw_plan.cu) and the host.
+// Smith-Waterman traceback kernels, shared by the kernels (sw16ck.cu,
+// sw32ck.cu), the device planner (sw_plan.cu) and the host.
 #pragma once
 
 #include <cmath>
@@ -33,6 +33,13 @@ __host__ __device__ inline bool sw16_eligible_opt(int m, int n, int match, int m
     if (go + ge >= BIAS16 || mismatch + go < 0 || match + go > 32000) return false;
     const int64_t top = (int64_t)match * (m < n ? m : n) * pct / 100 + BIAS16 + go;
     return top < 32000;
+}
+
+// The scheme conditions of the 16-bit kernels alone (no score bound): the
+// per-pair 16-bit choice of the SW model is taken only under them.
+__host__ __device__ inline bool sw16_scheme_ok(int match, int mismatch, int go, int ge)
+{
+    return go + ge < BIAS16 && mismatch + go >= 0 && match + go <= 32000;
 }
 
 // A best value at or above this in the 16-bit forward pass may have passed

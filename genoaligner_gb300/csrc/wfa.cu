@@ -343,6 +343,47 @@ __global__ void wfa_validate_kernel(PairDesc D, const int32_t* __restrict__ scor
     }
 }
 
+// Every pair's CIGAR (the last len[p] bytes of its slot of a_len + b_len) packed
+// for the copy back, 2 bits per op in op order (M 0, X 1, I 2, D 3; op t at
+// bits 2 (t % 4) of byte t / 4), at byte pk_off[p] of pk.  One warp per pair,
+// a lane per output byte: the slot is read and the packed bytes written
+// contiguously.
+__global__ void cigar_pack_kernel(PairDesc D, const int32_t* __restrict__ len, const char* __restrict__ cig,
+                                  const int64_t* __restrict__ pk_off, uint8_t* __restrict__ pk)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nw) {
+        const int L = len[p];
+        if (L <= 0) continue;
+        const char* src = cig + D.out_off[p] + ((int64_t)D.a_len[p] + D.b_len[p]) - L;
+        uint8_t* dst = pk + pk_off[p];
+        for (int b = lane; 4 * b < L; b += 32) {
+            uint32_t v = 0;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (4 * b + t < L) {
+                    const char c = src[4 * b + t];
+                    v |= (uint32_t)(c == 'M' ? 0 : (c == 'X' ? 1 : (c == 'I' ? 2 : 3))) << (2 * t);
+                }
+            }
+            dst[b] = (uint8_t)v;
+        }
+    }
+}
+
+cudaError_t launch_cigar_pack(const PairDesc& D, const int32_t* len, const char* cig, const int64_t* pk_off,
+                              uint8_t* pk, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    int blocks = (D.n + 7) / 8;
+    blocks = std::min(blocks, device_sms() * 16);
+    launch_begin(K_VALIDATE, st);
+    cigar_pack_kernel<<<blocks, 256, 0, st>>>(D, len, cig, pk_off, pk);
+    launch_end(K_VALIDATE, st);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const int32_t* len, const char* cig,
                                 uint8_t* flags, cudaStream_t st)
 {

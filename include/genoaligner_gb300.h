@@ -229,6 +229,16 @@ int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_
                      int64_t trace_cell_limit, int32_t* out_score, int32_t* out_pos,
                      int32_t* out_len, char* out_cigar, void* stream, const char** err);
 
+/* ga_sw_device with extension options (opt may be NULL): opt->learned = 1
+ * lets the SW variant model (model slot 1, ga_model_select) choose, pair by
+ * pair, which pure-ACGT pairs beyond the proven 16-bit bound try the 16-bit
+ * two-pairs-per-warp kernel (one whose best reaches the 16-bit limit is
+ * recomputed in 32 bits); results are the same as without it.  No reference
+ * counterpart. */
+int32_t ga_sw_device_ex(const ga_device_batch* batch, ga_sw_scoring scoring, int32_t trace,
+                        int64_t trace_cell_limit, const ga_options* opt, int32_t* out_score, int32_t* out_pos,
+                        int32_t* out_len, char* out_cigar, void* stream, const char** err);
+
 /* ------------------------------------------------------- learned model -- */
 
 /* The learned cost model (no counterpart in the reference): a k-mer sketch
@@ -236,6 +246,15 @@ int32_t ga_sw_device(const ga_device_batch* batch, ga_sw_scoring scoring, int32_
  * log2(wavefront cells + 1) of a pair.  It only routes work (the smax tried
  * first, the kernel variant, the queue); results never depend on it. */
 int32_t ga_cost_model_nparams(void);
+/* The model the calling thread's ga_cost_model_set / _get, ga_mlp_* calls act
+ * on: 0 = the WFA cost model (routes learned WFA calls), 1 = the SW variant
+ * model (the same network trained to predict an SW pair's best score as a
+ * fraction of its all-match score; routes ga_sw_device_ex / the SW extension
+ * entry with learned = 1).  GA_INVALID_ARGUMENT for any other value. */
+int32_t ga_model_select(int32_t which);
+/* Features [n][66] of an SW device batch (a = text, b = pattern) for the SW
+ * variant model: 3-mer count differences / 64, lengths / 8192. */
+int32_t ga_sw_features(const ga_device_batch* batch, float* features, void* stream);
 /* Load / read the fp32 parameters of the current device's model (layout: W1
  * [128][66], b1 [128], W2 [128][128], b2 [128], W3 [2][128], b3 [2]). */
 int32_t ga_cost_model_set(const float* params, int32_t n);
@@ -377,7 +396,8 @@ typedef struct ga_tune {
     int32_t sw_long_log2;   /* 32-bit traceback: pairs above 2^sw_long_log2 cells take
                                the 512 x 512 tile shape, the rest 64 x 64; 16 .. 30 */
     int32_t wfa_lane_smax;  /* learned WFA: pairs whose first smax is <= this run one
-                               per lane, 32 per warp (0 = none: one pair per warp); 0 .. 31 */
+                               per lane, each lane taking its next pair when its own is
+                               done (0 = none: one pair per warp); 0 .. 64 */
     int32_t sw_coop_log2;   /* SW traceback: work items above 2^sw_coop_log2 cells (a 32-bit
                                long-shape pair, or a 16-bit item of two pairs) run their forward
                                pass on the 4 warps of a block (128 lanes) instead of one warp;
