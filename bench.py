@@ -71,6 +71,8 @@ def parse():
                     help="run one of the extra workloads alone (no CPU baseline) and print its JSON")
     ap.add_argument("--set-tune", default=None,
                     help="kernel setting fields k=v[,k=v...] set before any run (and no autotuning), e.g. sw_pack16=0")
+    ap.add_argument("--wfa-model", default=None,
+                    help="WFA cost-model .npz to load instead of the committed one")
     ap.add_argument("--only-pairs", type=int, default=None,
                     help="with --only: the workload's first N pairs instead of all (small profiling cases)")
     return ap.parse_args()
@@ -433,6 +435,13 @@ def wfa_arms(api, torch, dev, stream, batch, n, smax, steps, flush, tune_first, 
             fn()
         ms = timed(fn, stream, steps, flush)
         out[arm] = {"pairs_per_s": n / (ms * 1e-3), "ms_per_step": ms}
+        # one more call with per-kernel events (outside the timed calls)
+        torch.cuda.synchronize()
+        api.profile(True)
+        fn()
+        torch.cuda.synchronize()
+        api.profile(False)
+        out[arm]["kernel_ms_one_call"] = {k: round(v[0], 4) for k, v in api.profile_read().items()}
         res[arm] = (sc.cpu().numpy(), ln.cpu().numpy(), cg.cpu().numpy())
         if learned:
             fn()
@@ -476,7 +485,7 @@ def bench_wfa_mixed(api, workloads, cost_model, torch, dev, stream, args, keep, 
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
     out = {"workload": "wfa_mixed_1m: 1,000,000 pairs, 150-250 bp, error 70% U[0,2%] / 25% U[2,10%] / "
-                       "5% U[10,30%], smax 64, CIGAR", "model_loaded": cost_model.load_default()}
+                       "5% U[10,30%], smax 64, CIGAR", "model_loaded": cost_model.load_default(args.wfa_model)}
     if not out["model_loaded"]:
         return out
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -504,7 +513,7 @@ def bench_wfa_long(api, workloads, cost_model, torch, dev, stream, args, keep, n
     n = ps.n
     batch = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, device=dev)
     out = {"workload": "wfa_long_1k_10k: 2,000 pairs, 1-10 kb, error 1-15%, geometric indels, smax 2048, CIGAR",
-           "model_loaded": cost_model.load_default()}
+           "model_loaded": cost_model.load_default(args.wfa_model)}
     if not out["model_loaded"]:
         return out
     plain = wfa_arms(api, torch, dev, stream, batch, n, 2048, 3, None, False, out)

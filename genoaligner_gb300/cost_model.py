@@ -6,9 +6,9 @@ wavefront-cell work.  It is trained on the GPU by the library's own forward,
 backward and Adam kernels, on pairs labelled by the library's exact WFA
 (score-only at smax 250 for the short pairs and 2048 for the long ones, pairs
 unresolved there left out, so every training label is the true distance):
-2,000,000 pairs of the mixed-divergence distribution (150-250 bp) and 20,000
-pairs of the long distribution (1-10 kb, error 1-15 %, geometric indels),
-the long ones repeated 10 times in the training set.
+2,000,000 pairs of the mixed-divergence distribution (150-250 bp), and with
+--with-long also 20,000 pairs of the long distribution (1-10 kb, error
+1-15 %, geometric indels) repeated 3 times in the training set.
 
 Checkpoint: an .npz with the fp32 parameters, a format version and the
 training seed; ``load_default()`` puts the committed model
@@ -28,7 +28,7 @@ FORMAT_VERSION = 1
 DEFAULT_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "wfa_cost_v1.npz")
 LABEL_SMAX = 250
 LABEL_SMAX_LONG = 2048
-LONG_REPEAT = 10
+LONG_REPEAT = 3
 
 
 def training_pairs(n: int = 2_000_000, seed: int = 1001) -> workloads.PairSet:
@@ -107,11 +107,13 @@ def load(path: str = DEFAULT_PATH) -> np.ndarray:
     return p
 
 
-def load_default() -> bool:
-    """Put the committed model on the current device; False when absent."""
-    if not os.path.exists(DEFAULT_PATH):
+def load_default(path: str | None = None) -> bool:
+    """Put the committed model (or the one at `path`) on the current device;
+    False when absent."""
+    path = path or DEFAULT_PATH
+    if not os.path.exists(path):
         return False
-    api.cost_model_set(load(DEFAULT_PATH))
+    api.cost_model_set(load(path))
     return True
 
 
@@ -132,21 +134,25 @@ def evaluate(feat, dist, lb) -> dict:
 
 
 def main():
-    """Train the default model (GPU): 2,000,000 pairs, seed 1001."""
+    """Train a model (GPU): 2,000,000 pairs, seed 1001 (the committed model's
+    recipe); --with-long adds the long pairs.  Usage: python -m
+    genoaligner_gb300.cost_model [out.npz] [--with-long]"""
     import json
     import sys
-    api.load()
-    t0 = time.time()
     import torch
+    api.load()
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    t0 = time.time()
     ps = training_pairs()
     feat, targ, dist, lb = labels_and_features(ps)
-    lf, lt, _, _ = labels_and_features(training_pairs_long(), chunk=5000, label_smax=LABEL_SMAX_LONG)
-    feat = torch.cat([feat] + [lf] * LONG_REPEAT)
-    targ = torch.cat([targ] + [lt] * LONG_REPEAT).contiguous()
+    if "--with-long" in sys.argv[1:]:
+        lf, lt, _, _ = labels_and_features(training_pairs_long(), chunk=5000, label_smax=LABEL_SMAX_LONG)
+        feat = torch.cat([feat] + [lf] * LONG_REPEAT)
+        targ = torch.cat([targ] + [lt] * LONG_REPEAT).contiguous()
     t1 = time.time()
     rec = train(feat, targ, log=lambda s: print(s, flush=True))
     params = api.cost_model_get()
-    out = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_PATH
+    out = args[0] if args else DEFAULT_PATH
     save(out, params, 1001, rec)
     hold = workloads.wfa_mixed(n=200_000, seed=4040)
     hf, _, hd, hl = labels_and_features(hold)

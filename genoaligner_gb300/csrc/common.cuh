@@ -81,6 +81,11 @@ enum KernelId : int {
 
 // Streaming multiprocessors of the current device (queried once per device).
 int device_sms();
+// Resident blocks per SM of `func` at `threads` threads and `smem` bytes of
+// dynamic shared memory on the current device, cached per (device, func,
+// threads, smem); the function's dynamic shared-memory limit is raised to
+// smem first (never lowered).
+int blocks_per_sm(const void* func, int threads, size_t smem);
 
 // Host side, around every launch this library makes: counts the launch and,
 // while profiling is on, records CUDA events on the launch stream.

@@ -15,8 +15,10 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "engine.hpp"
@@ -89,6 +91,36 @@ int device_sms()
     }
     if (dev < MAX_DEV) cache[dev].store(sms, std::memory_order_relaxed);
     return sms;
+}
+
+int blocks_per_sm(const void* func, int threads, size_t smem)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, int, size_t>, int> cache;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return 1; }
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, func, threads, smem);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    if (smem > 0) {
+        // (the opt-in limit counts dynamic memory only, but a launch needs it
+        // whenever dynamic plus static memory pass 48 KB: raise it always)
+        size_t& lim = limit[std::make_pair(dev, func)];
+        if (smem > lim && cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+                              cudaSuccess)
+            lim = smem;
+        cudaGetLastError();
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 0;
+    }
+    per_sm = std::max(per_sm, 1);
+    cache[key] = per_sm;
+    return per_sm;
 }
 
 // Host-to-device / device-to-host bytes of the calling thread's last batch call.
@@ -217,7 +249,8 @@ struct Ctx {
     size_t dev_cap = 0;
     uint64_t dev_gen = 0;           // bumped whenever the device arena is reallocated
     cudaGraphExec_t gexec = nullptr;  // the learned WFA path, captured once per launch shape
-    uint64_t gkey[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<uint64_t> gkey;
+    int glaunches = 0;                // library kernels in gexec
     cudaGraphExec_t swexec = nullptr; // the SW device work of a call or range, captured once per launch shape
     std::vector<uint64_t> swkey;
     int swlaunches = 0;               // library kernels in swexec
@@ -571,24 +604,13 @@ static cudaError_t replay_graph(cudaGraphExec_t& exec, std::vector<uint64_t>& ha
 static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D, int smax, bool trace, int route,
                                  int lane_smax, int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
-    const uint64_t key[8] = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
-                             (uint64_t)trace | (uint64_t)lane_smax << 8 | (uint64_t)route << 16, (uint64_t)(uintptr_t)score,
-                             (uint64_t)(uintptr_t)cig, (uint64_t)(uintptr_t)D.a_off};
-    if (!c->gexec || std::memcmp(key, c->gkey, sizeof(key)) != 0) {
-        if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) return e;
-        const cudaError_t e1 = enqueue_wfa(S, D, smax, trace, route, lane_smax, score, len, cig, err, st);
-        e = cudaStreamEndCapture(st, &g);
-        if (e1 != cudaSuccess || e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e1 != cudaSuccess ? e1 : e; }
-        e = cudaGraphInstantiate(&c->gexec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) { c->gexec = nullptr; return e; }
-        std::memcpy(c->gkey, key, sizeof(key));
-    }
-    note_graph_launches(7);          // pack, purity, route model, scan, scatter, lane, warp
-    return cudaGraphLaunch(c->gexec, st);
+    const std::vector<uint64_t> key = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
+                                       (uint64_t)trace | (uint64_t)lane_smax << 8 | (uint64_t)route << 16,
+                                       (uint64_t)(uintptr_t)score, (uint64_t)(uintptr_t)cig,
+                                       (uint64_t)(uintptr_t)D.a_off, (uint64_t)(uintptr_t)S.packed};
+    return replay_graph(c->gexec, c->gkey, key, c->glaunches, st, [&]() {
+        return enqueue_wfa(S, D, smax, trace, route, lane_smax, score, len, cig, err, st);
+    });
 }
 
 static bool profiling_on();

@@ -7,15 +7,13 @@
 
 namespace ga {
 
-// Lane queue: pairs run one per lane.  Eligible: both sides pure ACGT, at
-// most LANE_MAXLEN bases, first smax <= the tuned lane_smax, itself at most
-// LANE_SMAX (the lane kernel's shared-memory wavefront bound; a lane runs its
-// pair up to min(batch smax, LANE_SMAX)).
-constexpr int LANE_SMAX = 64;
+// Lane queue: pairs run one per lane, 32 per warp.  Eligible: both sides pure
+// ACGT, at most LANE_MAXLEN bases, first smax <= the tuned lane_smax, itself
+// at most LANE_SMAX (the lane kernel's shared-memory wavefront bound).
+constexpr int LANE_SMAX = 31;
 constexpr int LANE_MAXLEN = 256;
 // Buckets: keys 0 .. ROUTE_BUCKETS-1 are the warp queue by bit length of the
-// predicted distance bound, ROUTE_BUCKETS + s / 2 the lane queue with first
-// smax s (both queues are taken largest key first).
+// predicted distance bound, ROUTE_BUCKETS + s the lane queue with first smax s.
 constexpr int ROUTE_BUCKETS = 32;
 // Warp-queue items whose bucket key (bit length of the estimated distance) is
 // at least BLOCK_BITS -- estimated s >= 256 -- run first, each on a whole
@@ -46,7 +44,7 @@ __device__ __forceinline__ int route_item(int m, int n, bool pure_a, bool pure_b
     if (lb > smax) return -1;
     const int s = first_smax(y0, lb, smax);
     if (s <= lane_smax && s <= LANE_SMAX && m <= LANE_MAXLEN && n <= LANE_MAXLEN && pure_a && pure_b)
-        return (ROUTE_BUCKETS + min(s >> 1, ROUTE_BUCKETS - 1)) | (s << 8);
+        return (ROUTE_BUCKETS + s) | (s << 8);
     return min(bitlen((unsigned)s), ROUTE_BUCKETS - 1) | (smax << 8);
 }
 

@@ -201,9 +201,7 @@ static size_t sw_smem(int C) { return (size_t)4 * C * 32 * sizeof(int4); }
 int sw_max_slots(int sm_count)
 {
     const size_t smem = sw_smem(SW_SCORE_C);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw_kernel<SW_SCORE_C, false>, 128, smem);
-    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+    return blocks_per_sm((const void*)sw_kernel<SW_SCORE_C, false>, 128, smem) * sm_count * 4;
 }
 
 cudaError_t launch_sw(const SwArgs& A, int slots, cudaStream_t st)

@@ -980,9 +980,7 @@ static size_t sw16ck_smem() { return (size_t)4 * CK_WARP_WORDS * sizeof(uint32_t
 
 int sw16so_max_slots(int sm_count)
 {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16so_kernel<false>, 128, sw16ck_smem());
-    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+    return blocks_per_sm((const void*)sw16so_kernel<false>, 128, sw16ck_smem()) * sm_count * 4;
 }
 
 cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st)
@@ -998,10 +996,9 @@ cudaError_t launch_sw16so(const Sw16Args& A, int slots, cudaStream_t st)
 
 int sw16ck_max_slots(int sm_count, int window)
 {
-    int per_sm = 0;
-    if (window == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<4, true, false>, 128, sw16ck_smem());
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw16ck_kernel<2, true, false>, 128, sw16ck_smem());
-    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+    const int per_sm = window == 4 ? blocks_per_sm((const void*)sw16ck_kernel<4, true, false>, 128, sw16ck_smem())
+                                   : blocks_per_sm((const void*)sw16ck_kernel<2, true, false>, 128, sw16ck_smem());
+    return per_sm * sm_count * 4;
 }
 
 cudaError_t launch_sw16ck(const Sw16Args& A, int slots, int window, bool blocks, cudaStream_t st)

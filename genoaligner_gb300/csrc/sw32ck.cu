@@ -597,17 +597,13 @@ static size_t c32_smem(int warps = 4) { return (size_t)warps * c32_warp_smem_byt
 
 int sw32ck_max_slots(bool long_pairs, int sm_count)
 {
-    int per_sm = 0;
     if (long_pairs) {
-        cudaFuncSetAttribute(sw32ck_kernel<512, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)c32_smem<512, 16>());
-        cudaFuncSetAttribute(sw32ck_kernel<512, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)c32_smem<512, 16>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<512, 16, false>, 128, c32_smem<512, 16>());
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sw32ck_kernel<64, 2, false>, 128, c32_smem<64, 2>());
+        // both variants launch with this shared memory: raise both limits
+        blocks_per_sm((const void*)sw32ck_kernel<512, 16, true>, 128, c32_smem<512, 16>());
+        return blocks_per_sm((const void*)sw32ck_kernel<512, 16, false>, 128, c32_smem<512, 16>()) * sm_count * 4;
     }
-    return (per_sm < 1 ? 1 : per_sm) * sm_count * 4;
+    blocks_per_sm((const void*)sw32ck_kernel<64, 2, true>, 128, c32_smem<64, 2>());
+    return blocks_per_sm((const void*)sw32ck_kernel<64, 2, false>, 128, c32_smem<64, 2>()) * sm_count * 4;
 }
 
 // slots: warp slots of A.dirs, a multiple of 4 (blocks of 4 warps).

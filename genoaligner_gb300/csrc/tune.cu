@@ -279,7 +279,7 @@ int32_t ga_autotune_wfa(const ga_device_batch* batch, int32_t smax, int32_t trac
     };
     Search S;
     S.best = tune_current();
-    const int32_t rc = sweep(S, &ga_tune::wfa_lane_smax, {0, 15, 31, 47, LANE_SMAX}, reps, run, err);
+    const int32_t rc = sweep(S, &ga_tune::wfa_lane_smax, {0, 8, 15, 23, LANE_SMAX}, reps, run, err);
     if (rc != GA_OK) return rc;
     store(dev, S.best);
     report(S, chosen, trials, max_trials, n_trials);

@@ -408,16 +408,9 @@ size_t wfa_smem_bytes(int smax) { return (size_t)4 * 2 * (2 * smax + 3) * sizeof
 
 int wfa_max_slots(int smax, bool trace, int sm_count)
 {
-    int per_sm = 0;
     const size_t smem = wfa_smem_bytes(smax);
-    if (trace) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_kernel<true>, 128, smem);
-    } else {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(wfa_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wfa_kernel<false>, 128, smem);
-    }
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = trace ? blocks_per_sm((const void*)wfa_kernel<true>, 128, smem)
+                             : blocks_per_sm((const void*)wfa_kernel<false>, 128, smem);
     return per_sm * sm_count * 4;
 }
 

@@ -32,27 +32,20 @@
 
 namespace ga {
 
-// Lane queue (route.cuh): every lane runs a pair of its own and takes the next
-// one from the queue when that pair is done.  Per warp in shared memory: both
-// sequences of the lanes' pairs as 32-bit words of 16 2-bit codes
-// [word][lane] (LANE_WORDS = 16 data words + 1 read by the two-word fetch
-// window) and the lanes' wavefronts [k][lane] as 16-bit offsets (a pair is at
-// most LANE_MAXLEN bases a side), updated in place.  The walk reads a 16-bit
-// record per (s, k) -- the predecessor (0 mismatch, 1 insertion, 2 deletion)
-// and the extension length -- from the lane's own stretch of the warp's
-// global stack slot, written 8 records (16 bytes) at a time.
+// Lane queue (route.cuh): per warp in shared memory, both sequences of its
+// 32 pairs as 32-bit words of 16 2-bit codes [word][lane] (LANE_WORDS = 16
+// data words + 1 read by the two-word fetch window) and one wavefront
+// [k][lane], updated in place.  The walk reads a 16-bit record per (s, k):
+// the predecessor (0 mismatch, 1 insertion, 2 deletion) and the extension
+// length, [idx][lane] in the warp's global stack slot.
 constexpr int LANE_WORDS = LANE_MAXLEN / 16 + 1;
-constexpr int LANE_WS = 2 * LANE_SMAX + 3;                                    // k = -(LANE_SMAX+1) .. LANE_SMAX+1
-constexpr int LANE_STACK = ((LANE_SMAX + 1) * (LANE_SMAX + 1) + 7) / 8 * 8;   // records per lane
-constexpr int LANE_WARP_SMEM = 2 * LANE_WORDS * 32 + LANE_WS * 32 / 2;        // 32-bit words per warp
-static_assert(LANE_WS * 32 % 2 == 0, "16-bit wavefront rows fill whole words");
-static_assert(LANE_MAXLEN + 1 < 16384, "16-bit wavefront offsets");
-// Walks run in batches: a lane whose forward pass ended waits until this many
-// lanes wait (or no lane is still in its forward pass), then they walk
-// together -- a walk alone would hold the other 31 lanes for its whole length.
-constexpr int LANE_WALK_BATCH = 16;
-constexpr int LANE_NULL = -32768;                 // unreachable; live offsets are >= 0
-__device__ __forceinline__ bool lane_live(int off) { return off > -16384; }
+constexpr int LANE_WS = 2 * LANE_SMAX + 3;
+constexpr int LANE_STACK = (LANE_SMAX + 1) * (LANE_SMAX + 1);
+constexpr int LANE_WARP_SMEM = 2 * LANE_WORDS * 32 + LANE_WS * 32;    // ints per warp
+// Hand-over rule: past wavefront LANE_HAND_S, once at most 1/LANE_HAND_DIV of
+// a warp's pairs are still unresolved, they move to the warp queue.
+constexpr int LANE_HAND_S = 6;
+constexpr int LANE_HAND_DIV = 16;
 
 template <int G>
 __device__ __forceinline__ void gsync(unsigned gmask)
@@ -118,195 +111,153 @@ __device__ __forceinline__ int lane_run(const uint32_t* SP, const uint32_t* ST, 
     return run;
 }
 
-// Record `val` at index idx of the lane's walk records: 8 records are
-// gathered in four registers and stored as one 16-byte vector.
-__device__ __forceinline__ void lane_record(uint16_t* rec, int idx, uint32_t val, uint32_t& w0, uint32_t& w1,
-                                            uint32_t& w2, uint32_t& w3)
-{
-    const int j = idx & 7;
-    const uint32_t sh = 16u * (uint32_t)(j & 1);
-    const uint32_t keep = ~(0xffffu << sh), put = (val & 0xffffu) << sh;
-    const int q = j >> 1;
-    w0 = q == 0 ? ((w0 & keep) | put) : w0;
-    w1 = q == 1 ? ((w1 & keep) | put) : w1;
-    w2 = q == 2 ? ((w2 & keep) | put) : w2;
-    w3 = q == 3 ? ((w3 & keep) | put) : w3;
-    if (j == 7) *reinterpret_cast<uint4*>(rec + (idx & ~7)) = make_uint4(w0, w1, w2, w3);
-}
-
-// Pairs of the lane queue, one per lane.  Each lane keeps its own state: the
-// pair, its wavefront s and the next diagonal k.  Every step of the loop the
-// idle lanes take the next pairs of the queue (one atomic per warp), then each
-// lane in its forward pass computes one diagonal: so a lane whose pair is done
-// does not wait for the other lanes' pairs.  The predecessor code the forward
-// pass records is the argmax the reference's walk recomputes (mismatch on >=,
-// insertion on >, deletion on >), so the walk needs no wavefront values: the
-// offset before extension is the offset minus the recorded extension length.
-// A pair runs to min(batch smax, LANE_SMAX): unresolved there it is final
-// when that is the batch smax, else it goes to the warp queue at the batch
-// smax; a pair the router should not have sent here goes there too.
+// Pairs of the lane queue, 32 per warp: each lane runs the whole forward
+// pass and walk of its own pair.  All lanes of a warp step through the same
+// (s, k) until the last of them resolves or reaches its first smax, so the
+// shared-memory wavefront [k][lane] and sequences [word][lane] are read
+// without bank conflicts and the walk records coalesce.  The predecessor code
+// the forward pass stores is the argmax the reference's walk recomputes
+// (mismatch on >=, insertion on >, deletion on >), so the walk needs no
+// wavefront values: the offset before extension is the offset minus the
+// stored extension length.
 template <bool TRACE>
-__device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec_warp, int lane)
+__device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, int lane)
 {
     const WfaArgs& A = R.A;
     const uint32_t* SP = smem + lane;
     const uint32_t* ST = smem + LANE_WORDS * 32 + lane;
-    int16_t* WF = reinterpret_cast<int16_t*>(smem + 2 * LANE_WORDS * 32) + (LANE_SMAX + 1) * 32 + lane;   // WF[k * 32]
-    uint16_t* rec = TRACE ? rec_warp + (int64_t)lane * LANE_STACK : nullptr;
+    int32_t* WF = reinterpret_cast<int32_t*>(smem + 2 * LANE_WORDS * 32) + (LANE_SMAX + 1) * 32 + lane;   // WF[k * 32]
     const int nlane = R.small_count ? *R.small_count : 0;
-    const int limit = min(A.smax, LANE_SMAX);
-    enum { IDLE = 0, FWD = 1, WAIT = 2 };
-    int state = IDLE;
-    bool drained = false;
-    int p = 0, m = 0, n = 0, s = 0, k = 0, carry = LANE_NULL, kfinal = 0, score = -1, last = 0;
-    uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
     for (;;) {
-        // idle lanes take the next pairs of the queue, warp-aggregated
-        const unsigned need = __ballot_sync(FULL, state == IDLE && !drained);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(R.small_next, __popc(need));
-            base = __shfl_sync(FULL, base, leader);
-            if (state == IDLE && !drained) {
-                const int q = base + __popc(need & ((1u << lane) - 1u));
-                if (q >= nlane) {
-                    drained = true;
-                } else {
-                    p = R.small[q].x;
-                    m = A.D.a_len[p];
-                    n = A.D.b_len[p];
-                    if (m <= 0 || n <= 0 || m > LANE_MAXLEN || n > LANE_MAXLEN || !A.D.pure[p] ||
-                        !A.D.pure[A.D.n + p]) {
-                        // the router sends only pairs that fit: anything else
-                        // goes to the warp queue at the batch smax
-                        R.esc[atomicAdd(R.esc_count, 1)] = make_int2(p, A.smax);
-                    } else {
-                        // both sequences into this lane's columns: 32-bit words
-                        // 0 .. (len-1)/16 + 1 lie in the arena
-                        const uint32_t* gP = reinterpret_cast<const uint32_t*>(A.D.packed + (A.D.a_off[p] >> 5));
-                        const uint32_t* gT = reinterpret_cast<const uint32_t*>(A.D.packed + (A.D.b_off[p] >> 5));
-                        const int lastP = ((m - 1) >> 4) + 1, lastT = ((n - 1) >> 4) + 1;
-                        uint32_t* sp = smem + lane;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(R.small_next, 32);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= nlane) break;
+        const int q = base + lane;
+        const bool have = q < nlane;
+        int p = 0, smx = 0, m = 0, n = 0;
+        bool misrouted = false;
+        if (have) {
+            const int2 it = R.small[q];
+            p = it.x;
+            smx = it.y;
+            m = A.D.a_len[p];
+            n = A.D.b_len[p];
+            // the router sends only pairs that fit; anything else goes back to
+            // the warp queue at the same smax
+            misrouted = m <= 0 || n <= 0 || m > LANE_MAXLEN || n > LANE_MAXLEN || smx < 1 || smx > LANE_SMAX ||
+                        !A.D.pure[p] || !A.D.pure[A.D.n + p];
+        }
+        const bool run = have && !misrouted;
+        // stage both sequences: 32-bit words 0 .. (len-1)/16 + 1 lie in the arena
+        {
+            const uint32_t* gP = reinterpret_cast<const uint32_t*>(A.D.packed + (run ? (A.D.a_off[p] >> 5) : 0));
+            const uint32_t* gT = reinterpret_cast<const uint32_t*>(A.D.packed + (run ? (A.D.b_off[p] >> 5) : 0));
+            const int lastP = run ? ((m - 1) >> 4) + 1 : -1, lastT = run ? ((n - 1) >> 4) + 1 : -1;
+            uint32_t* sp = smem + lane;
 #pragma unroll
-                        for (int w = 0; w < LANE_WORDS; ++w) {
-                            sp[w * 32] = w <= lastP ? __ldg(gP + w) : 0u;
-                            sp[(LANE_WORDS + w) * 32] = w <= lastT ? __ldg(gT + w) : 0u;
-                        }
-                        const int off0 = lane_run(SP, ST, 0, 0, m, n);
-                        WF[0] = (int16_t)off0;
-                        WF[-32] = (int16_t)LANE_NULL;
-                        WF[32] = (int16_t)LANE_NULL;
-                        if (TRACE) lane_record(rec, 0, (uint32_t)off0 << 2, w0, w1, w2, w3);
-                        last = 0;
-                        kfinal = n - m;
-                        if (kfinal == 0 && off0 >= n) {
-                            score = 0;
-                            state = WAIT;
-                        } else if (limit < 1) {
-                            score = -1;
-                            state = WAIT;
-                        } else {
-                            s = 1;
-                            k = -1;
-                            carry = LANE_NULL;
-                            WF[2 * 32] = (int16_t)LANE_NULL;
-                            WF[-2 * 32] = (int16_t)LANE_NULL;
-                            state = FWD;
-                        }
-                    }
-                }
+            for (int w = 0; w < LANE_WORDS; ++w) {
+                sp[w * 32] = w <= lastP ? __ldg(gP + w) : 0u;
+                sp[(LANE_WORDS + w) * 32] = w <= lastT ? __ldg(gT + w) : 0u;
             }
         }
-        const unsigned fwd = __ballot_sync(FULL, state == FWD);
-        const unsigned wait = __ballot_sync(FULL, state == WAIT);
-        if (!fwd && !wait) {
-            if (!__ballot_sync(FULL, !drained)) break;
-            continue;
+        const int kfinal = n - m;
+        int score = -1;
+        bool act = run;
+        if (run) {
+            const int off0 = lane_run(SP, ST, 0, 0, m, n);
+            WF[0] = off0;
+            WF[-32] = WFA_NULL;
+            WF[32] = WFA_NULL;
+            if (TRACE) rec[lane] = (uint16_t)(off0 << 2);
+            if (kfinal == 0 && off0 >= n) { score = 0; act = false; }
         }
-        // a batch of walks (or the last ones)
-        if (wait && (__popc(wait) >= LANE_WALK_BATCH || !fwd)) {
-            if (state == WAIT) {
-                if (TRACE) *reinterpret_cast<uint4*>(rec + (last & ~7)) = make_uint4(w0, w1, w2, w3);
-                if (!TRACE || score < 0) {
-                    A.out_score[p] = score;
-                    if (A.out_len) A.out_len[p] = 0;
-                } else {
-                    char* slot = A.out_cigar + A.D.out_off[p];
-                    int pos = m + n;
-                    if (score == 0) {
-                        pos = emit_lane(slot, pos, n, 'M', A.err);
-                    } else {
-                        // the final cell's offset is n (clipped at n, reached >= n)
-                        int ws = score, wk = kfinal, off = n;
-                        int h = off, v = off - wk;
-                        while (v > 0 && h > 0 && ws > 0) {
-                            const uint32_t r = rec[ws * ws + ws + wk];
-                            const int ext = (int)(r >> 2), code = (int)(r & 3u);
-                            pos = emit_lane(slot, pos, ext, 'M', A.err);
-                            pos = emit_lane(slot, pos, 1, code == 0 ? 'X' : (code == 1 ? 'I' : 'D'), A.err);
-                            off -= ext;
-                            if (code == 0)      { off -= 1; }
-                            else if (code == 1) { wk -= 1; off -= 1; }
-                            else                { wk += 1; }
-                            h = off;
-                            v = off - wk;
-                            --ws;
-                        }
-                        if (v > 0 && h > 0) {
-                            const int r = min(v, h);
-                            pos = emit_lane(slot, pos, r, 'M', A.err);
-                            v -= r;
-                            h -= r;
-                        }
-                        pos = emit_lane(slot, pos, v, 'D', A.err);
-                        pos = emit_lane(slot, pos, h, 'I', A.err);
-                    }
-                    A.out_score[p] = score;
-                    A.out_len[p] = m + n - pos;
-                }
-                state = IDLE;
+        // When only a few lanes are still running well after the others have
+        // resolved, they are handed to the warp queue (rerun from s = 0
+        // there): the other lanes would otherwise idle.
+        const int started = __popc(__ballot_sync(FULL, act));
+        bool handed = false;
+        for (int s = 1;; ++s) {
+            const unsigned am = __ballot_sync(FULL, act);
+            if (!am) break;
+            if (s > LANE_HAND_S && __popc(am) * LANE_HAND_DIV <= started) {
+                handed = act;
+                act = false;
+                break;
             }
-            continue;
-        }
-        // one diagonal of every lane in its forward pass
-        if (state == FWD) {
-            const int mis = WF[k * 32];
-            const int del = WF[(k + 1) * 32];
-            int x = mis + 1, code = 0;
-            if (carry + 1 > x) { x = carry + 1; code = 1; }
-            if (del > x) { x = del; code = 2; }
-            carry = mis;
-            int ext = 0;
-            if (!lane_live(x) || x > n || x - k > m) x = LANE_NULL;
-            else { ext = lane_run(SP, ST, x - k, x, m, n); x += ext; }
-            WF[k * 32] = (int16_t)x;
-            last = s * s + s + k;
-            if (TRACE) lane_record(rec, last, (uint32_t)(code | (ext << 2)), w0, w1, w2, w3);
-            if (++k > s) {                                // wavefront s done
+            if (act) {
+                WF[(s + 1) * 32] = WFA_NULL;
+                WF[-(s + 1) * 32] = WFA_NULL;
+                int carry = WFA_NULL;                            // wavefront s-1 at k-1
+                for (int k = -s; k <= s; ++k) {
+                    const int mis = WF[k * 32];
+                    const int del = WF[(k + 1) * 32];
+                    int x = mis + 1, code = 0;
+                    if (carry + 1 > x) { x = carry + 1; code = 1; }
+                    if (del > x) { x = del; code = 2; }
+                    carry = mis;
+                    int ext = 0;
+                    if (!wfa_live(x) || x > n || x - k > m) x = WFA_NULL;
+                    else { ext = lane_run(SP, ST, x - k, x, m, n); x += ext; }
+                    WF[k * 32] = x;
+                    if (TRACE) rec[(s * s + s + k) * 32 + lane] = (uint16_t)(code | (ext << 2));
+                }
                 if (kfinal >= -s && kfinal <= s) {
                     const int fo = WF[kfinal * 32];
-                    if (lane_live(fo) && fo >= n) { score = s; state = WAIT; }
+                    if (wfa_live(fo) && fo >= n) { score = s; act = false; }
                 }
-                if (state == FWD) {
-                    if (s >= limit) {
-                        if (A.smax > limit) {             // past what lanes hold: the warp queue
-                            R.esc[atomicAdd(R.esc_count, 1)] = make_int2(p, A.smax);
-                            state = IDLE;
-                        } else {
-                            score = -1;
-                            state = WAIT;
-                        }
-                    } else {
-                        ++s;
-                        k = -s;
-                        carry = LANE_NULL;
-                        WF[(s + 1) * 32] = (int16_t)LANE_NULL;
-                        WF[-(s + 1) * 32] = (int16_t)LANE_NULL;
-                    }
-                }
+                if (act && s >= smx) act = false;
             }
         }
+        // unresolved within the first smax (or handed over): escalate to the
+        // warp queue at the batch smax, warp-aggregated; unresolved at the
+        // batch smax itself: final
+        const bool esc = misrouted || handed || (run && score < 0 && smx < A.smax);
+        const unsigned em = __ballot_sync(FULL, esc);
+        if (em) {
+            int eb = 0;
+            if (lane == 0) eb = atomicAdd(R.esc_count, __popc(em));
+            eb = __shfl_sync(FULL, eb, 0);
+            if (esc) R.esc[eb + __popc(em & ((1u << lane) - 1u))] = make_int2(p, A.smax);
+        }
+        if (!have || esc) continue;
+        if (!TRACE || score < 0) {
+            A.out_score[p] = score;
+            if (A.out_len) A.out_len[p] = 0;
+            continue;
+        }
+        char* slot = A.out_cigar + A.D.out_off[p];
+        int pos = m + n;
+        if (score == 0) {
+            pos = emit_lane(slot, pos, n, 'M', A.err);
+        } else {
+            // the final cell's offset is n (clipped at n, reached >= n)
+            int s = score, k = kfinal, off = n;
+            int h = off, v = off - k;
+            while (v > 0 && h > 0 && s > 0) {
+                const uint32_t r = rec[(s * s + s + k) * 32 + lane];
+                const int ext = (int)(r >> 2), code = (int)(r & 3u);
+                pos = emit_lane(slot, pos, ext, 'M', A.err);
+                pos = emit_lane(slot, pos, 1, code == 0 ? 'X' : (code == 1 ? 'I' : 'D'), A.err);
+                off -= ext;
+                if (code == 0)      { off -= 1; }
+                else if (code == 1) { k -= 1; off -= 1; }
+                else                { k += 1; }
+                h = off;
+                v = off - k;
+                --s;
+            }
+            if (v > 0 && h > 0) {
+                const int r = min(v, h);
+                pos = emit_lane(slot, pos, r, 'M', A.err);
+                v -= r;
+                h -= r;
+            }
+            pos = emit_lane(slot, pos, v, 'D', A.err);
+            pos = emit_lane(slot, pos, h, 'I', A.err);
+        }
+        A.out_score[p] = score;
+        A.out_len[p] = m + n - pos;
     }
 }
 
@@ -578,10 +529,7 @@ int routed_warp_smem(int smax) { return (2 * (2 * smax + 3) + 3) / 4 * 4; }
 template <typename K>
 static int per_sm_for(K kernel, size_t smem)
 {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem);
-    return per_sm < 1 ? 1 : per_sm;
+    return blocks_per_sm((const void*)kernel, 128, smem);
 }
 
 int routed_max_slots(int smax, bool trace, int sm_count)

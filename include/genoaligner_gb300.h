@@ -396,8 +396,7 @@ typedef struct ga_tune {
     int32_t sw_long_log2;   /* 32-bit traceback: pairs above 2^sw_long_log2 cells take
                                the 512 x 512 tile shape, the rest 64 x 64; 16 .. 30 */
     int32_t wfa_lane_smax;  /* learned WFA: pairs whose first smax is <= this run one
-                               per lane, each lane taking its next pair when its own is
-                               done (0 = none: one pair per warp); 0 .. 64 */
+                               per lane, 32 per warp (0 = none: one pair per warp); 0 .. 31 */
     int32_t sw_coop_log2;   /* SW traceback: work items above 2^sw_coop_log2 cells (a 32-bit
                                long-shape pair, or a 16-bit item of two pairs) run their forward
                                pass on the 4 warps of a block (128 lanes) instead of one warp;

@@ -11,7 +11,7 @@ from genoaligner_gb300 import api
 
 def test_default_setting_is_valid_and_current_without_a_stored_one():
     d = api.tune_default()
-    assert d == {"sw_pack16": 1, "sw_window": 2, "sw_long_log2": 24, "wfa_lane_smax": 64, "sw_coop_log2": 27,
+    assert d == {"sw_pack16": 1, "sw_window": 2, "sw_long_log2": 24, "wfa_lane_smax": 31, "sw_coop_log2": 27,
                  "sw_opt16_pct": 100}
     if not api.device_available():
         assert api.tune_get() == d
@@ -19,7 +19,7 @@ def test_default_setting_is_valid_and_current_without_a_stored_one():
 
 @pytest.mark.parametrize("field,value", [("sw_pack16", 2), ("sw_window", 3), ("sw_window", 8),
                                          ("sw_long_log2", 15), ("sw_long_log2", 31),
-                                         ("wfa_lane_smax", -1), ("wfa_lane_smax", 65),
+                                         ("wfa_lane_smax", -1), ("wfa_lane_smax", 32),
                                          ("sw_coop_log2", 15), ("sw_coop_log2", 41),
                                          ("sw_opt16_pct", 49), ("sw_opt16_pct", 101)])
 def test_out_of_range_settings_are_refused(field, value):

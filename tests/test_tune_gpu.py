@@ -108,7 +108,7 @@ def test_every_wfa_lane_setting_gives_the_same_results(restore_tune):
     ps = workloads.wfa_mixed(n=20_000, seed=73)
     b = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
     base = None
-    for lane in (0, 4, 15, 31, 64):
+    for lane in (0, 4, 15, 31):
         api.tune_set(wfa_lane_smax=lane)
         sc = torch.full((b.n,), -7, dtype=torch.int32, device="cuda")
         ln = torch.zeros(b.n, dtype=torch.int32, device="cuda")
