@@ -262,16 +262,23 @@ def sw_equal_device(out, want):
 def one_core_sample(run, n, seconds, first=64, cap=1 << 20):
     """Units per second of `run(idx)` (which returns (units, C seconds)) on
     one thread, over pairs of a fixed random permutation taken in growing
-    chunks until ~`seconds` of C time."""
+    chunks (passing over the batch again when it is used up) until ~`seconds`
+    of C time; returns (rate, pairs run, C seconds)."""
     order = np.random.default_rng(777).permutation(n)
-    units, used, k, chunk = 0, 0.0, 0, first
-    while used < seconds and k < n:
-        u, t = run(order[k:k + chunk])
+    units, used, done, k, chunk = 0, 0.0, 0, 0, first
+    for _ in range(100_000):
+        if used >= seconds:
+            break
+        idx = order[k:k + chunk]
+        u, t = run(idx)
         units += u
         used += t
-        k += chunk
+        done += len(idx)
+        k += len(idx)
+        if k >= n:
+            k = 0
         chunk = min(chunk * 2, cap)
-    return units / used if used > 0 else None, k, used
+    return units / used if used > 0 else None, done, used
 
 
 def cpu_baseline_sw(ps, seconds, threads):
@@ -657,6 +664,13 @@ def cpu_and_parity(keep, ps_sw, sw_e2e, sw_dev_scores, threads):
         want = oracle.wfa_batch(pats, txts, smax=smax, with_cigar=True, threads=threads, max_smax=max(smax, 511))
         parity[key] = {"device_plain": wfa_equal_device(k["device"], want),
                        "e2e": wfa_equal_packed(k["e2e"], want), "pairs": ps.n}
+        # all threads: further passes over the batch until ~unit_seconds of C
+        # time (or 20 s of wall time)
+        passes, secs, w0 = 1, want.seconds, time.perf_counter()
+        while secs < unit_seconds and time.perf_counter() - w0 < 20.0:
+            secs += oracle.wfa_batch(pats, txts, smax=smax, with_cigar=True, threads=threads,
+                                     max_smax=max(smax, 511)).seconds
+            passes += 1
 
         def run(idx):
             sub = ps.subset(idx)
@@ -664,11 +678,11 @@ def cpu_and_parity(keep, ps_sw, sw_e2e, sw_dev_scores, threads):
             g = oracle.wfa_batch(a, b, smax=smax, with_cigar=True, threads=1, max_smax=max(smax, 511))
             return sub.n, g.seconds
         one, k1, t1 = one_core_sample(run, ps.n, unit_seconds, first=8 if smax > 511 else 256)
-        cpu[key] = {"unit": "pairs/s", "all_cores": ps.n / want.seconds, "all_cores_threads": threads,
-                    "all_cores_sample": f"the whole batch ({ps.n} pairs), {want.seconds:.2f} s",
+        cpu[key] = {"unit": "pairs/s", "all_cores": passes * ps.n / secs, "all_cores_threads": threads,
+                    "all_cores_sample": f"the whole batch ({ps.n} pairs) x {passes}, {secs:.2f} s",
                     "one_core": one, "one_core_sample": f"{k1} pairs, {t1:.2f} s"}
 
-    wfa_leg("wfa_150bp", 64, 2.0)
+    wfa_leg("wfa_150bp", 64, 1.0)
     wfa_leg("wfa_long", 2048, 3.0)
     wfa_leg("wfa_mixed_1m", 64, 2.0)
 

@@ -427,6 +427,20 @@ struct Carve {
 
 static inline int64_t round32(int64_t x) { return (x + 31) & ~(int64_t)31; }
 
+// The device's CIGAR lengths of pairs [lo, hi) against their slots (pair q's
+// slot ends at slot_end[q], the previous one's end is its start), checked
+// before any of them is expanded: a length outside [0, slot] means the device
+// work did not finish as enqueued, and the call fails instead of writing
+// outside the caller's buffer.
+static bool lengths_fit(const int32_t* len, const int64_t* slot_end, int64_t lo, int64_t hi)
+{
+    for (int64_t q = lo; q < hi; ++q) {
+        const int64_t cap = slot_end[q] - (q > 0 ? slot_end[q - 1] : 0);
+        if (len[q] < 0 || len[q] > cap) return false;
+    }
+    return true;
+}
+
 static bool fail_here(int step)
 {
     int want = g_fail_next.load();
@@ -447,6 +461,7 @@ static const char* E_SYNC = "device execution failed";
 static const char* E_OVERFLOW = "internal error: CIGAR slot overflow";
 static const char* E_SCRATCH = "internal error: traceback memory smaller than the plan needs";
 static const char* E_HOSTMEM = "pinned host allocation failed";
+static const char* E_BADLEN = "internal error: device returned a CIGAR longer than its slot";
 
 // -------------------------------------------------------------------- WFA --
 int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err)
@@ -579,6 +594,11 @@ static cudaError_t replay_graph(cudaGraphExec_t& exec, std::vector<uint64_t>& ha
                                 int& launches, cudaStream_t st, const std::function<cudaError_t()>& enqueue)
 {
     if (!exec || have != key) {
+        // one capture at a time in the process (the ranges of a ranged call
+        // capture their first calls from their own threads); a capture is
+        // made once per launch shape, so this costs nothing on replays
+        static std::mutex capture_mu;
+        std::lock_guard<std::mutex> lk(capture_mu);
         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
         have.clear();
         cudaGraph_t g = nullptr;
@@ -767,8 +787,14 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
+    if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
     WfaView v{hsc, hln, hpk, hpo, slot_end.data(), trace, trace ? hvf : nullptr};
-    parallel_for(n, 1024, [&](int64_t lo, int64_t hi) { fin(lo, hi, v); });
+    std::atomic<bool> bad{false};
+    parallel_for(n, 1024, [&](int64_t lo, int64_t hi) {
+        if (trace && !lengths_fit(hln, slot_end.data(), lo, hi)) { bad = true; return; }
+        fin(lo, hi, v);
+    });
+    if (bad) { *err = E_BADLEN; return GA_DEVICE_ERROR; }
     return GA_OK;
 }
 
@@ -1182,7 +1208,8 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
             le = enqueue();
         } else {
             const std::vector<uint64_t> key = {
-                c->dev_gen, (uint64_t)n, (uint64_t)arena, (uint64_t)cig, (uint64_t)trace | (uint64_t)route << 1,
+                c->dev_gen, (uint64_t)n, (uint64_t)arena, (uint64_t)cig, (uint64_t)pkb,
+                (uint64_t)trace | (uint64_t)route << 1,
                 (uint64_t)cell_limit,
                 (uint64_t)(uint32_t)s0.match | (uint64_t)(uint32_t)s0.mismatch << 32,
                 (uint64_t)(uint32_t)s0.gap_open | (uint64_t)(uint32_t)s0.gap_extend << 32,
@@ -1213,8 +1240,14 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         return GA_DEVICE_ERROR;
     }
     if (*her != 0) { *err = (*her & ERR_SCRATCH) ? E_SCRATCH : E_OVERFLOW; return GA_DEVICE_ERROR; }
+    if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
     SwView v{hsc, hpos, hln, hpk, hpo, slot_end.data(), trace, trace ? hvf : nullptr, base, cig_base};
-    parallel_for(n, 512, [&](int64_t lo, int64_t hi) { fin(base + lo, base + hi, v); });
+    std::atomic<bool> bad{false};
+    parallel_for(n, 512, [&](int64_t lo, int64_t hi) {
+        if (trace && !lengths_fit(hln, slot_end.data(), lo, hi)) { bad = true; return; }
+        fin(base + lo, base + hi, v);
+    });
+    if (bad) { *err = E_BADLEN; return GA_DEVICE_ERROR; }
     return GA_OK;
 }
 

@@ -371,6 +371,158 @@ __device__ void fwd_band(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& 
     __syncwarp();
 }
 
+// fwd_band's traceback form for a warp alone, two rows per step: lane t
+// takes rows i = 2 (tau - t) + 1 and i + 1 of its CB columns.  Row i + 1's
+// cell in column c needs only row i's cells in columns c - 1 and c, so the
+// two rows' dependency chains (E along a row, H through E) are independent at
+// equal column and interleave: twice the independent integer work per lane
+// between the same per-row shuffles and profile reads.  Values, checkpoint
+// rows, column edges and the best (value, first row) per pair are
+// fwd_band's exactly.
+template <int CB>
+__device__ void fwd_band2(const FwdCtx& X, int b0, int t, int& vA, int& rA, int& cA, int& vB, int& rB, int& cB)
+{
+    constexpr int NH = CB / 2;
+    const uint32_t MIN2 = 0x80008000u, K2 = 0x80008000u;
+    const uint32_t NGO2 = X.NGO2, NGE2 = X.NGE2;
+    const int M = X.M, mA = X.mA, mB = X.mB;
+    const int j0 = b0 + t * CB;
+    const int nvA = max(0, min(CB, X.nA - j0)), nvB = max(0, min(CB, X.nB - j0));
+    ck_profile_fwd<CB>(X.prof, X.patA, X.patB, j0, nvA, nvB, X.sm, X.sx, t);
+    uint32_t hgu[CB], fv[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) { hgu[c] = NGO2; fv[c] = 0u; }
+    // the left neighbour's H - go at the row above this step's first row; what
+    // this lane hands right for its two rows
+    uint32_t diag_in = NGO2, out_hg0 = NGO2, out_e0 = 0u, out_hg1 = NGO2, out_e1 = 0u;
+    const uint32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / TW - 1) * M : nullptr;
+    const int kout = (j0 + CB) % TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / TW : 0;
+    uint32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * M : nullptr;
+    auto row_off = [&](int r) -> uint32_t {
+        const int la = r < mA ? ck_code(__ldg(X.textA + r)) : CK_LETTERS - 1;
+        const int lb = r < mB ? ck_code(__ldg(X.textB + r)) : CK_LETTERS - 1;
+        return (uint32_t)(la * NH * 32) | ((uint32_t)((CK_LETTERS + lb) * NH * 32) << 16);
+    };
+    // lane 0's inputs of 64 rows at a time (lane u: rows 64k + 2u and + 1,
+    // 0-based), handed to lane 0 by shuffles
+    uint32_t rb_off0 = 0u, rb_hg0 = NGO2, rb_e0 = 0u, rb_off1 = 0u, rb_hg1 = NGO2, rb_e1 = 0u;
+    uint32_t ch0 = 0, ch1 = 0;
+    uint32_t bmax = 0u, brow = 0u;
+    const int steps = (M + 1) / 2 + 31;
+    for (int tau = 0; tau < steps; ++tau) {
+        if ((tau & 31) == 0 && 2 * tau < M) {
+            const int r = 2 * (tau + t);
+            if (r < M) {
+                rb_off0 = row_off(r);
+                if (left) {
+                    const uint2 lv = *reinterpret_cast<const uint2*>(left + 2 * r);
+                    rb_hg0 = lv.x;
+                    rb_e0 = lv.y;
+                }
+            }
+            if (r + 1 < M) {
+                rb_off1 = row_off(r + 1);
+                if (left) {
+                    const uint2 lv = *reinterpret_cast<const uint2*>(left + 2 * (r + 1));
+                    rb_hg1 = lv.x;
+                    rb_e1 = lv.y;
+                }
+            }
+        }
+        uint32_t in_hg0 = __shfl_up_sync(FULL, out_hg0, 1);
+        uint32_t in_e0 = __shfl_up_sync(FULL, out_e0, 1);
+        uint32_t in_hg1 = __shfl_up_sync(FULL, out_hg1, 1);
+        uint32_t in_e1 = __shfl_up_sync(FULL, out_e1, 1);
+        ch0 = __shfl_up_sync(FULL, ch0, 1);
+        ch1 = __shfl_up_sync(FULL, ch1, 1);
+        const uint32_t l_off0 = __shfl_sync(FULL, rb_off0, tau & 31);
+        const uint32_t l_hg0 = __shfl_sync(FULL, rb_hg0, tau & 31);
+        const uint32_t l_e0 = __shfl_sync(FULL, rb_e0, tau & 31);
+        const uint32_t l_off1 = __shfl_sync(FULL, rb_off1, tau & 31);
+        const uint32_t l_hg1 = __shfl_sync(FULL, rb_hg1, tau & 31);
+        const uint32_t l_e1 = __shfl_sync(FULL, rb_e1, tau & 31);
+        const int i = 2 * (tau - t) + 1;
+        if (t == 0) {
+            ch0 = l_off0; in_hg0 = l_hg0; in_e0 = l_e0;
+            ch1 = l_off1; in_hg1 = l_hg1; in_e1 = l_e1;
+        }
+        if (i >= 1 && i <= M) {
+            const uint32_t* pA0 = X.prof + (ch0 & 0xffffu) + t;
+            const uint32_t* pB0 = X.prof + (ch0 >> 16) + t;
+            const uint32_t* pA1 = X.prof + (ch1 & 0xffffu) + t;
+            const uint32_t* pB1 = X.prof + (ch1 >> 16) + t;
+            // row i: diagonal, left; row i + 1: diagonal (row i's left neighbour), left
+            uint32_t hgd0 = diag_in, hgl0 = in_hg0, el0 = in_e0;
+            uint32_t hgd1 = in_hg0, hgl1 = in_hg1, el1 = in_e1;
+            uint32_t rowmax0 = 0u, rowmax1 = 0u;
+#pragma unroll
+            for (int cc = 0; cc < CB; cc += 2) {
+                const uint32_t wa0 = pA0[(cc >> 1) * 32], wb0 = pB0[(cc >> 1) * 32];
+                const uint32_t wa1 = pA1[(cc >> 1) * 32], wb1 = pB1[(cc >> 1) * 32];
+                const uint32_t S00 = __byte_perm(wa0, wb0, 0x5410), S01 = __byte_perm(wa0, wb0, 0x7632);
+                const uint32_t S10 = __byte_perm(wa1, wb1, 0x5410), S11 = __byte_perm(wa1, wb1, 0x7632);
+                uint32_t hh0[2], hh1[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int cu = cc + u;
+                    // row i, column cu
+                    const uint32_t e0 = __viaddmax_s16x2(el0, NGE2, hgl0);
+                    const uint32_t f0 = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
+                    const uint32_t h10 = __viaddmax_s16x2(hgd0, u ? S01 : S00, e0);
+                    const uint32_t hv0 = __vimax3_s16x2_relu(h10, f0, f0);
+                    const uint32_t hg0 = __viaddmax_s16x2(hv0, NGO2, MIN2);
+                    hgd0 = hgu[cu];
+                    // row i + 1, column cu: up is row i's cell just computed
+                    const uint32_t e1 = __viaddmax_s16x2(el1, NGE2, hgl1);
+                    const uint32_t f1 = __viaddmax_s16x2(f0, NGE2, hg0);
+                    const uint32_t h11 = __viaddmax_s16x2(hgd1, u ? S11 : S10, e1);
+                    const uint32_t hv1 = __vimax3_s16x2_relu(h11, f1, f1);
+                    const uint32_t hg1 = __viaddmax_s16x2(hv1, NGO2, MIN2);
+                    hgd1 = hg0;
+                    hgu[cu] = hg1;
+                    fv[cu] = f1;
+                    hgl0 = hg0; el0 = e0;
+                    hgl1 = hg1; el1 = e1;
+                    hh0[u] = hv0;
+                    hh1[u] = hv1;
+                }
+                rowmax0 = __vimax3_s16x2(rowmax0, hh0[0], hh0[1]);
+                rowmax1 = __vimax3_s16x2(rowmax1, hh1[0], hh1[1]);
+            }
+            diag_in = in_hg1;
+            out_hg0 = hgl0; out_e0 = el0;
+            out_hg1 = hgl1; out_e1 = el1;
+            const bool two = i + 1 <= M;
+            if (eout) {
+                *reinterpret_cast<uint2*>(eout + 2 * (i - 1)) = make_uint2(out_hg0, out_e0);
+                if (two) *reinterpret_cast<uint2*>(eout + 2 * i) = make_uint2(out_hg1, out_e1);
+            }
+            if (((i + 1) & (CK_K - 1)) == 0 && i + 1 < M) {           // checkpoint row i + 1 (i is odd)
+                uint4* dst = reinterpret_cast<uint4*>(X.ck + 2 * ((int64_t)((i + 1) / CK_K - 1) * X.ncol + j0));
+#pragma unroll
+                for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_uint4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
+            }
+            {
+                const uint32_t d = bmax - rowmax0 + K2;
+                const uint32_t imp = ((~d & K2) >> 15) * 0xffffu;
+                bmax = __vmaxs2(bmax, rowmax0);
+                brow = (brow & ~imp) | ((uint32_t)i * 0x10001u & imp);
+            }
+            if (two) {
+                const uint32_t d = bmax - rowmax1 + K2;
+                const uint32_t imp = ((~d & K2) >> 15) * 0xffffu;
+                bmax = __vmaxs2(bmax, rowmax1);
+                brow = (brow & ~imp) | ((uint32_t)(i + 1) * 0x10001u & imp);
+            }
+        }
+    }
+    const int v = lo16s(bmax), r = (int)(brow & 0xffffu);
+    if (v > 0 && ck_better(v, r, j0 + 1, vA, rA, cA)) { vA = v; rA = r; cA = j0 + 1; }
+    const int v2 = hi16s(bmax), r2 = (int)(brow >> 16);
+    if (v2 > 0 && ck_better(v2, r2, j0 + 1, vB, rB, cB)) { vB = v2; rB = r2; cB = j0 + 1; }
+    __syncwarp();
+}
+
 // Tile profile of one pair for a lane of a tile group (CT columns per lane):
 // prof[((pair * 4 + letter) * CT/2 + h) * 32 + t] holds the 16-bit scores of
 // the lane's columns col0 + 2h, col0 + 2h + 1 (0-based); past the pattern's
@@ -474,10 +626,10 @@ __device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, in
             for (int b0 = 0; b0 < N;) {
                 const int rest = N - b0;                          // columns from this band on
                 const int cb = rest > CK_BW ? CK_C : ck_last_cb(rest);
-                if (cb == 16) fwd_band<16, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else if (cb == 8) fwd_band<8, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else if (cb == 4) fwd_band<4, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
-                else fwd_band<2, false>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                if (cb == 16) fwd_band2<16>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 8) fwd_band2<8>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else if (cb == 4) fwd_band2<4>(X, b0, t, vA, rA, cA, vB, rB, cB);
+                else fwd_band2<2>(X, b0, t, vA, rA, cA, vB, rB, cB);
                 b0 += 32 * cb;
             }
         }

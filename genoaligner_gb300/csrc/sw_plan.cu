@@ -8,7 +8,9 @@
 // doubling of (m + 31) * n) in four kernels -- classify and
 // count, scan, scatter, pack -- and leaves on the device the work lists in
 // the order the launches read them plus, per list, its length and the largest
-// per-warp memory its items need; the host reads back that one small record.
+// per-warp memory its items need.  The host entry's launches read that small
+// record on the device (plan mode: grids and memory sized from host bounds);
+// the device entry reads it back to size its memory exactly.
 #include "kernels.cuh"
 
 namespace ga {

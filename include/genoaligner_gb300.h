@@ -480,8 +480,11 @@ int32_t ga_bench_int_peak(int32_t variant, double* lane_ops_per_s);
 
 /* Test hook: make the next batch call fail at the named host step
  * (1 = device allocation, 2 = host-to-device copy, 3 = kernel launch,
- * 4 = device-to-host copy; 0 = off).  The call then reports device_error with
- * defaults in every result, as a real failure there would. */
+ * 4 = device-to-host copy, 5 = a traceback call's first CIGAR length replaced,
+ * after the copy back, by one past its slot; 0 = off).  The call then reports
+ * device_error with defaults in every result, as a real failure there would
+ * (step 5: the host checks every length against its slot before it writes a
+ * CIGAR). */
 void ga_debug_fail_next(int32_t step);
 
 #ifdef __cplusplus

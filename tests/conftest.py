@@ -29,3 +29,8 @@ def wfa_golden():
 @pytest.fixture(scope="session")
 def sw_golden():
     return load_golden("sw_golden.json.gz")
+
+
+@pytest.fixture(scope="session")
+def real_golden():
+    return load_golden("real_golden.json.gz")

@@ -70,3 +70,23 @@ def test_oracle_validation_refusals():
     big_t, big_p = b"A" * 8192, b"A" * 8193
     b = oracle.sw_batch([big_t], [big_p])
     assert b.too_large[0] and not b.resolved[0] and b.score[0] == -1
+
+
+def test_oracle_wfa_matches_reference_on_real_sequences(real_golden):
+    """Human and chimp mitochondrial genomes (repeats, the human N, real
+    divergence), cut as the reference's real-sequence test cuts them: the
+    oracle equals the reference's kernels field by field, and a pair is
+    unresolved exactly when its edit distance exceeds smax."""
+    for rec in real_golden:
+        pats = [_enc(p) for p, _ in rec["pairs"]]
+        txts = [_enc(t) for _, t in rec["pairs"]]
+        got = oracle.wfa_batch(pats, txts, smax=rec["smax"], with_cigar=rec["with_cigar"], threads=4)
+        assert got.status == "ok", rec["name"]
+        for i, want in enumerate(rec["results"]):
+            assert got.score[i] == want["score"], (rec["name"], i)
+            assert got.cigars[i].decode() == want["cigar"], (rec["name"], i)
+            assert got.rescore_ok[i] == bool(want["rescore_ok"]), (rec["name"], i)
+            assert got.wellformed_ok[i] == bool(want["wellformed_ok"]), (rec["name"], i)
+            d, smax = rec["edit_distance"][i], rec["smax"][i]
+            assert (got.score[i] == d) if d <= smax else (got.score[i] == -1), (rec["name"], i)
+        assert got.resolved_count == rec["resolved_count"]

@@ -128,7 +128,7 @@ def test_sw_mixed_with_cigar_batch():
 
 
 def test_sw_fault_injection_reports_device_error():
-    for step in (1, 2, 3, 4):
+    for step in (1, 2, 3, 4, 5):
         api.load().ga_debug_fail_next(step)
         got = sw_gpu([b"ACGTACGT"], [b"ACGT"])
         assert got.status == api.Status.device_error

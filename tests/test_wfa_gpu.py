@@ -136,7 +136,7 @@ def test_wfa_full_size_properties():
 
 def test_wfa_fault_injection_reports_device_error():
     pats, txts = [b"ACGT", b"AC"], [b"ACGA", b"AC"]
-    for step in (1, 2, 3, 4):
+    for step in (1, 2, 3, 4, 5):
         api.load().ga_debug_fail_next(step)
         got = wfa_gpu(pats, txts, smax=8)
         assert got.status == api.Status.device_error and got.error
