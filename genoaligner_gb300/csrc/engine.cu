@@ -427,6 +427,38 @@ struct Carve {
 
 static inline int64_t round32(int64_t x) { return (x + 31) & ~(int64_t)31; }
 
+// Requests per chunk of the host passes over a batch's requests.
+constexpr int64_t REQ_CHUNK = 1024;
+
+// fn(k, lo, hi) on chunk k = [lo, hi) of [0, n), the chunks in parallel on the
+// host pool; returns the number of chunks.
+template <class F>
+static int64_t for_chunks(int64_t n, F fn)
+{
+    const int64_t nch = (n + REQ_CHUNK - 1) / REQ_CHUNK;
+    parallel_for(nch, 1, [&](int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) fn(k, k * REQ_CHUNK, std::min(n, (k + 1) * REQ_CHUNK));
+    });
+    return nch;
+}
+
+// The first request of [0, n) for which check(i) returns an error (null when
+// it passes), as a serial scan finds it, scanned in parallel chunks: its
+// status is GA_INVALID_ARGUMENT with *err set, else GA_OK.
+template <class F>
+static int32_t first_failure(int64_t n, F check, const char** err)
+{
+    std::vector<int64_t> at((size_t)((n + REQ_CHUNK - 1) / REQ_CHUNK + 1), -1);
+    std::vector<const char*> what(at.size(), nullptr);
+    const int64_t nch = for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i)
+            if (const char* e = check(i)) { at[(size_t)k] = i; what[(size_t)k] = e; return; }
+    });
+    for (int64_t k = 0; k < nch; ++k)
+        if (at[(size_t)k] >= 0) { *err = what[(size_t)k]; return GA_INVALID_ARGUMENT; }
+    return GA_OK;
+}
+
 // The device's CIGAR lengths of pairs [lo, hi) against their slots (pair q's
 // slot ends at slot_end[q], the previous one's end is its start), checked
 // before any of them is expanded: a length outside [0, slot] means the device
@@ -464,18 +496,19 @@ static const char* E_HOSTMEM = "pinned host allocation failed";
 static const char* E_BADLEN = "internal error: device returned a CIGAR longer than its slot";
 
 // -------------------------------------------------------------------- WFA --
+// The reference's checks of one WFA request (src/api/api.cpp:234-266), in its
+// order: the error of the first it fails, null when it passes.
+static const char* wfa_request_error(const ga_align_request& r, int32_t max_smax)
+{
+    if ((r.pattern_len > 0 && !r.pattern) || (r.text_len > 0 && !r.text)) return E_NULL;
+    if (r.pattern_len < 0 || r.text_len < 0) return E_NEG;
+    if (r.smax < 0 || r.smax > max_smax) return max_smax == GA_MAX_SMAX ? E_SMAX : E_SMAX_EX;
+    return nullptr;
+}
+
 int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err)
 {
-    for (int32_t i = 0; i < n; ++i) {
-        const ga_align_request& r = reqs[i];
-        if ((r.pattern_len > 0 && !r.pattern) || (r.text_len > 0 && !r.text)) { *err = E_NULL; return GA_INVALID_ARGUMENT; }
-        if (r.pattern_len < 0 || r.text_len < 0) { *err = E_NEG; return GA_INVALID_ARGUMENT; }
-        if (r.smax < 0 || r.smax > max_smax) {
-            *err = max_smax == GA_MAX_SMAX ? E_SMAX : E_SMAX_EX;
-            return GA_INVALID_ARGUMENT;
-        }
-    }
-    return GA_OK;
+    return first_failure(n, [&](int64_t i) { return wfa_request_error(reqs[i], max_smax); }, err);
 }
 
 // Device scratch of one WFA batch: the 2-bit arena and purity flags, the
@@ -664,37 +697,71 @@ int route_mode(int requested)
     return (requested == 1 || requested == 2) ? requested : 0;
 }
 
+// One chunk of a WFA batch's requests in the first pass over them: the
+// checks, the batch smax and trace flag, and the chunk's sizes -- its own
+// sides in the staging arena (a side that repeats the previous request's, same
+// pointer and length, is staged once and shares its offset), CIGAR slots,
+// packed CIGAR bytes -- and where its last own side of each kind starts.
+struct WfaChunk {
+    int64_t arena = 0, cig = 0, pkb = 0;
+    int64_t tail_a = -1, tail_b = -1;       // from the chunk's arena start; -1: no own side of that kind
+    int32_t bad = -1;                       // first request failing the checks
+    const char* err = nullptr;
+    int smax = INT32_MAX;
+    bool trace = false;
+};
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
                   const WfaFinish& fin, const char** err)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
-    if (int32_t st = wfa_check(reqs, n, max_smax, err)) return st;
-    int smax = reqs[0].smax;
+    // pass 1, in parallel chunks: checks (the first failing request's error,
+    // as a serial pass finds it), smax, trace, own sides and sizes
+    static thread_local std::vector<uint8_t> own_v;
+    static thread_local std::vector<int64_t> slot_v;
+    own_v.resize((size_t)n);
+    slot_v.resize((size_t)n);
+    uint8_t* own = own_v.data();
+    int64_t* slot_end = slot_v.data();
+    std::vector<WfaChunk> ck((size_t)((n + REQ_CHUNK - 1) / REQ_CHUNK));
+    const int64_t nch = for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+        WfaChunk& C = ck[(size_t)k];
+        for (int64_t i = lo; i < hi; ++i) {
+            const ga_align_request& r = reqs[i];
+            if (C.bad < 0)
+                if (const char* e = wfa_request_error(r, max_smax)) { C.bad = (int32_t)i; C.err = e; }
+            C.smax = std::min(C.smax, (int)r.smax);
+            C.trace |= r.with_cigar != 0;
+            const bool oa = !(i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len);
+            const bool ob = !(i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len);
+            own[i] = (uint8_t)(oa | ob << 1);
+            if (oa) { C.tail_a = C.arena; C.arena += round32(r.pattern_len); }
+            if (ob) { C.tail_b = C.arena; C.arena += round32(r.text_len); }
+            const int64_t cap = (int64_t)r.pattern_len + r.text_len;
+            C.cig += cap;
+            C.pkb += (cap + 3) / 4;
+        }
+    });
+    int smax = INT32_MAX;
     bool trace = false;
-    for (int32_t i = 0; i < n; ++i) {
-        smax = std::min(smax, (int)reqs[i].smax);
-        trace |= reqs[i].with_cigar != 0;
+    std::vector<int64_t> base((size_t)(3 * nch)), carry((size_t)(2 * nch));
+    int64_t arena = 0, cig = 0, pkb = 0, ca = 0, cb = 0;
+    for (int64_t k = 0; k < nch; ++k) {
+        const WfaChunk& C = ck[(size_t)k];
+        if (C.bad >= 0) {
+            *err = C.err;
+            return GA_INVALID_ARGUMENT;
+        }
+        smax = std::min(smax, C.smax);
+        trace |= C.trace;
+        base[3 * k] = arena; base[3 * k + 1] = cig; base[3 * k + 2] = pkb;
+        carry[2 * k] = ca; carry[2 * k + 1] = cb;          // the previous request's side offsets
+        if (C.tail_a >= 0) ca = arena + C.tail_a;
+        if (C.tail_b >= 0) cb = arena + C.tail_b;
+        arena += C.arena; cig += C.cig; pkb += C.pkb;
     }
     route = route_mode(route);
     const bool learned = route != 0;
-
-    // plan: 32-aligned sequence offsets, CIGAR slot offsets, packed CIGAR offsets
-    std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n), pk_off(n);
-    std::vector<uint8_t> own(n, 0);
-    int64_t arena = 0, cig = 0, pkb = 0;
-    for (int32_t i = 0; i < n; ++i) {
-        // a side that repeats the previous request's (same pointer and length) is staged once
-        const ga_align_request& r = reqs[i];
-        if (i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len) a_off[i] = a_off[i - 1];
-        else { a_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 1; }
-        if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) b_off[i] = b_off[i - 1];
-        else { b_off[i] = arena; arena += round32(r.text_len); own[i] |= 2; }
-        const int64_t cap = (int64_t)reqs[i].pattern_len + reqs[i].text_len;
-        out_off[i] = cig; cig += cap;
-        slot_end[i] = cig;
-        pk_off[i] = pkb; pkb += (cap + 3) / 4;
-    }
     arena += 64;                                     // read-past padding
     if (!trace) cig = pkb = 0;
 
@@ -737,15 +804,28 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         carve_wfa(d, S, n, arena, trace, learned);
     }
 
-    // stage inputs
-    parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
+    // pass 2, in the same chunks: offsets and the staging of every own side
+    for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+        int64_t at = base[3 * k], cg = base[3 * k + 1], pk = base[3 * k + 2];
+        int64_t cur_a = carry[2 * k], cur_b = carry[2 * k + 1];
         for (int64_t i = lo; i < hi; ++i) {
             const ga_align_request& r = reqs[i];
-            ha[i] = a_off[i]; hal[i] = r.pattern_len;
-            hb[i] = b_off[i]; hbl[i] = r.text_len;
-            ho[i] = out_off[i]; hpo[i] = pk_off[i];
-            if ((own[i] & 1) && r.pattern_len) std::memcpy(hseq + a_off[i], r.pattern, (size_t)r.pattern_len);
-            if ((own[i] & 2) && r.text_len) std::memcpy(hseq + b_off[i], r.text, (size_t)r.text_len);
+            if (own[i] & 1) {
+                cur_a = at;
+                at += round32(r.pattern_len);
+                if (r.pattern_len) std::memcpy(hseq + cur_a, r.pattern, (size_t)r.pattern_len);
+            }
+            if (own[i] & 2) {
+                cur_b = at;
+                at += round32(r.text_len);
+                if (r.text_len) std::memcpy(hseq + cur_b, r.text, (size_t)r.text_len);
+            }
+            ha[i] = cur_a; hal[i] = r.pattern_len;
+            hb[i] = cur_b; hbl[i] = r.text_len;
+            const int64_t cap = (int64_t)r.pattern_len + r.text_len;
+            ho[i] = cg; cg += cap;
+            slot_end[i] = cg;
+            hpo[i] = pk; pk += (cap + 3) / 4;
         }
     });
     std::memset(hseq + arena - 64, 0, 64);
@@ -788,10 +868,10 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     }
     if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
     if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
-    WfaView v{hsc, hln, hpk, hpo, slot_end.data(), trace, trace ? hvf : nullptr};
+    WfaView v{hsc, hln, hpk, hpo, slot_end, trace, trace ? hvf : nullptr};
     std::atomic<bool> bad{false};
     parallel_for(n, 1024, [&](int64_t lo, int64_t hi) {
-        if (trace && !lengths_fit(hln, slot_end.data(), lo, hi)) { bad = true; return; }
+        if (trace && !lengths_fit(hln, slot_end, lo, hi)) { bad = true; return; }
         fin(lo, hi, v);
     });
     if (bad) { *err = E_BADLEN; return GA_DEVICE_ERROR; }
@@ -814,19 +894,19 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err)
 {
     if (n <= 0) return GA_OK;
     const ga_sw_scoring s0 = reqs[0].scoring;
-    for (int32_t i = 0; i < n; ++i) {
+    return first_failure(n, [&](int64_t i) -> const char* {
         const ga_sw_request& r = reqs[i];
-        if ((r.text_len > 0 && !r.text) || (r.pattern_len > 0 && !r.pattern)) { *err = E_NULL; return GA_INVALID_ARGUMENT; }
-        if (r.text_len < 0 || r.pattern_len < 0) { *err = E_NEG; return GA_INVALID_ARGUMENT; }
+        if ((r.text_len > 0 && !r.text) || (r.pattern_len > 0 && !r.pattern)) return E_NULL;
+        if (r.text_len < 0 || r.pattern_len < 0) return E_NEG;
         const ga_sw_scoring& s = r.scoring;
-        if (s.match <= 0) { *err = E_SW_MATCH; return GA_INVALID_ARGUMENT; }
-        if (s.mismatch >= s.match) { *err = E_SW_MISMATCH; return GA_INVALID_ARGUMENT; }
-        if (s.gap_open <= 0 || s.gap_extend <= 0) { *err = E_SW_GAPS; return GA_INVALID_ARGUMENT; }
-        if (r.with_cigar && s.gap_extend > s.gap_open) { *err = E_SW_GEGO; return GA_INVALID_ARGUMENT; }
+        if (s.match <= 0) return E_SW_MATCH;
+        if (s.mismatch >= s.match) return E_SW_MISMATCH;
+        if (s.gap_open <= 0 || s.gap_extend <= 0) return E_SW_GAPS;
+        if (r.with_cigar && s.gap_extend > s.gap_open) return E_SW_GEGO;
         if (s.match != s0.match || s.mismatch != s0.mismatch || s.gap_open != s0.gap_open ||
-            s.gap_extend != s0.gap_extend) { *err = E_SW_MIXED; return GA_INVALID_ARGUMENT; }
-    }
-    return GA_OK;
+            s.gap_extend != s0.gap_extend) return E_SW_MIXED;
+        return nullptr;
+    }, err);
 }
 
 // Work plan of one SW batch, as the device planner left it (sw_plan.cu):
@@ -1259,13 +1339,24 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
     if (n <= 0) return GA_OK;
     if (int32_t st = sw_check(reqs, n, err)) return st;
     const ga_tune T = tune_current();
+    // trace, the widest pattern and the cells, in one parallel pass
+    struct Part { bool trace = false; int max_n = 0; double cells = 0.0; };
+    std::vector<Part> part((size_t)((n + REQ_CHUNK - 1) / REQ_CHUNK + 1));
+    const int64_t nch = for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+        Part& p = part[(size_t)k];
+        for (int64_t i = lo; i < hi; ++i) {
+            p.trace |= reqs[i].with_cigar != 0;
+            p.max_n = std::max(p.max_n, (int)reqs[i].pattern_len);
+            p.cells += (double)reqs[i].text_len * (double)reqs[i].pattern_len;
+        }
+    });
     bool trace = false;
     int max_n = 0;
     double cells = 0.0;
-    for (int32_t i = 0; i < n; ++i) {
-        trace |= reqs[i].with_cigar != 0;
-        max_n = std::max(max_n, (int)reqs[i].pattern_len);
-        cells += (double)reqs[i].text_len * (double)reqs[i].pattern_len;
+    for (int64_t k = 0; k < nch; ++k) {
+        trace |= part[(size_t)k].trace;
+        max_n = std::max(max_n, part[(size_t)k].max_n);
+        cells += part[(size_t)k].cells;
     }
     // The reference's score-only kernel holds 4 warps x 2*(n+1) ints of shared
     // memory per block and refuses the batch above the per-block limit the
@@ -1397,6 +1488,25 @@ void sw_validate(const char* cg, int len, const char* T, int m, int si, int ei, 
     *rescore_ok = ok && total == score;
 }
 
+// Sum of both sides' lengths (negative ones as 0) over a batch, in parallel chunks.
+template <class R>
+static int64_t side_bytes(const R* reqs, int32_t n)
+{
+    const int64_t nch = ((int64_t)n + REQ_CHUNK - 1) / REQ_CHUNK;
+    std::vector<int64_t> part((size_t)std::max<int64_t>(nch, 1), 0);
+    parallel_for(nch, 1, [&](int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            int64_t s = 0;
+            for (int64_t i = k * REQ_CHUNK, e = std::min<int64_t>(n, (k + 1) * REQ_CHUNK); i < e; ++i)
+                s += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
+            part[(size_t)k] = s;
+        }
+    });
+    int64_t s = 0;
+    for (int64_t k = 0; k < nch; ++k) s += part[(size_t)k];
+    return s;
+}
+
 }  // namespace ga
 
 // ================================================================== C ABI ==
@@ -1406,19 +1516,9 @@ static const char* E_CIGBUF = "cigar buffer is smaller than the batch needs";
 
 extern "C" {
 
-int64_t ga_align_cigar_bytes(const ga_align_request* reqs, int32_t n)
-{
-    int64_t s = 0;
-    for (int32_t i = 0; i < n; ++i) s += std::max(0, reqs[i].pattern_len) + (int64_t)std::max(0, reqs[i].text_len);
-    return s;
-}
+int64_t ga_align_cigar_bytes(const ga_align_request* reqs, int32_t n) { return side_bytes(reqs, n); }
 
-int64_t ga_align_sw_cigar_bytes(const ga_sw_request* reqs, int32_t n)
-{
-    int64_t s = 0;
-    for (int32_t i = 0; i < n; ++i) s += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
-    return s;
-}
+int64_t ga_align_sw_cigar_bytes(const ga_sw_request* reqs, int32_t n) { return side_bytes(reqs, n); }
 
 static void set_info(ga_batch_info* info, int32_t st, const char* e, int32_t res, int32_t unres)
 {
@@ -1434,17 +1534,38 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
                           char* cigar_buf, int64_t cigar_buf_bytes, const ga_options* opt,
                           ga_batch_info* info)
 {
-    for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
+    const ga_align_result dflt{-1, 0, 0, 0, 0, 0, 0};
+    auto reset = [&] {
+        parallel_for(n, 16384, [&](int64_t lo, int64_t hi) { std::fill(results + lo, results + hi, dflt); });
+    };
     const int32_t max_smax =
         (opt && opt->max_smax > 0) ? std::min<int32_t>(opt->max_smax, GA_MAX_SMAX_DEVICE) : GA_MAX_SMAX;
+    // any CIGAR requested, and the CIGAR bytes the batch needs (ga_align_cigar_bytes), in parallel chunks
+    const int64_t nch = ((int64_t)n + REQ_CHUNK - 1) / REQ_CHUNK;
+    std::vector<int64_t> need((size_t)std::max<int64_t>(nch, 1), 0);
+    std::vector<uint8_t> want((size_t)std::max<int64_t>(nch, 1), 0);
+    parallel_for(nch, 1, [&](int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            int64_t s = 0;
+            bool w = false;
+            for (int64_t i = k * REQ_CHUNK, e = std::min<int64_t>(n, (k + 1) * REQ_CHUNK); i < e; ++i) {
+                s += std::max(0, reqs[i].pattern_len) + (int64_t)std::max(0, reqs[i].text_len);
+                w |= reqs[i].with_cigar != 0;
+            }
+            need[(size_t)k] = s;
+            want[(size_t)k] = w;
+        }
+    });
+    int64_t cig_need = 0;
     bool any_cigar = false;
-    for (int32_t i = 0; i < n; ++i) any_cigar |= reqs[i].with_cigar != 0;
+    for (int64_t k = 0; k < nch; ++k) { cig_need += need[(size_t)k]; any_cigar |= want[(size_t)k] != 0; }
     const char* err = nullptr;
     std::atomic<int32_t> resolved{0};
     auto fin = [&](int64_t lo, int64_t hi, const WfaView& v) {
         int32_t res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             ga_align_result& r = results[i];
+            r = dflt;                               // every pair of the batch passes here once
             r.score = v.score[i];
             r.resolved = r.score >= 0;
             res += r.resolved;
@@ -1468,16 +1589,17 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
         resolved.fetch_add(res);
     };
     int32_t st;
-    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < ga_align_cigar_bytes(reqs, n))) {
+    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < cig_need)) {
         // the reference's request checks come first, then the buffer contract
         st = wfa_check(reqs, n, max_smax, &err);
         if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
+        reset();
         set_info(info, st, err, 0, 0);
         return st;
     }
     st = wfa_batch(reqs, n, max_smax, opt ? opt->learned : 0, fin, &err);
     if (st != GA_OK) {
-        for (int32_t i = 0; i < n; ++i) results[i] = ga_align_result{-1, 0, 0, 0, 0, 0, 0};
+        reset();
         set_info(info, st, err, 0, 0);
         return st;
     }
@@ -1498,12 +1620,22 @@ int32_t ga_align_sw_batch_ex(const ga_sw_request* reqs, int32_t n, ga_sw_result*
     const ga_sw_result dflt{-1, 0, -1, -1, -1, -1, 0, 0, 0, 0, 0};
     int64_t limit = GA_SW_MAX_TRACE_CELLS;
     if (opt && opt->trace_cell_limit != 0) limit = opt->trace_cell_limit;
+    // any CIGAR requested, and ga_align_sw_cigar_bytes, in one parallel pass
+    std::vector<int64_t> need((size_t)((n + REQ_CHUNK - 1) / REQ_CHUNK + 1), 0);
+    std::vector<uint8_t> want(need.size(), 0);
+    const int64_t nch = for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+        int64_t s = 0;
+        bool w = false;
+        for (int64_t i = lo; i < hi; ++i) {
+            w |= reqs[i].with_cigar != 0;
+            s += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
+        }
+        need[(size_t)k] = s;
+        want[(size_t)k] = w;
+    });
     bool any_cigar = false;
-    int64_t cig_need = 0;                        // ga_align_sw_cigar_bytes, in the same pass
-    for (int32_t i = 0; i < n; ++i) {
-        any_cigar |= reqs[i].with_cigar != 0;
-        cig_need += std::max(0, reqs[i].text_len) + (int64_t)std::max(0, reqs[i].pattern_len);
-    }
+    int64_t cig_need = 0;
+    for (int64_t k = 0; k < nch; ++k) { cig_need += need[(size_t)k]; any_cigar |= want[(size_t)k] != 0; }
     const char* err = nullptr;
     std::atomic<int32_t> resolved{0};
     auto fin = [&](int64_t lo, int64_t hi, const SwView& v) {

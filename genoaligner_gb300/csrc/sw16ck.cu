@@ -711,7 +711,6 @@ __device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, in
         // CT tl .. CT tl + CT - 1
         const int rows0 = done[0] ? 0 : wi[0] - ti0[0] + 1, rows1 = done[1] ? 0 : wi[1] - ti0[1] + 1;
         const int R = max(rows0, rows1);
-        const int steps = R + LG - 1;
         const int tgA = tb[0] - (TG - 1) + g, tgB = tb[1] - (TG - 1) + g;   // this group's tiles
         const int colA = TW * tgA + CT * tl, colB = TW * tgB + CT * tl;    // this lane's first columns
         __syncwarp();
@@ -762,64 +761,95 @@ __device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, in
         const uint8_t* tB = textB + (ti0[1] - 1);
         // each row's profile offsets travel along a group's lanes with the
         // boundary values; the groups' first lanes get theirs, and the row's
-        // left edge, without a branch of their own: the offsets of 32 rows at
-        // a time are read by all lanes (lane u: row 32k + u) and shuffled out
-        uint32_t ch = 0, rb_ch = 0;
+        // left edge, without a branch of their own: the offsets of 64 rows at
+        // a time are read by all lanes (lane u: rows 64k + 2u and + 1) and
+        // shuffled out.  Two rows per step, as in fwd_band2: lane tl takes
+        // window rows i = 2 (tau - tl) + 1 and i + 1, whose dependency chains
+        // interleave.
+        uint32_t ch0 = 0, ch1 = 0, rb_ch0 = 0, rb_ch1 = 0;
+        uint32_t out_hg1 = B2 - GO2, out_e1 = B2;
         const uint32_t* pA0 = prof + (0 * 4 * (CT / 2)) * 32 + t;
         const uint32_t* pB0 = prof + (1 * 4 * (CT / 2)) * 32 + t;
         uint32_t* hrow = Ht + g * TW + CT * tl;                         // + (row - 1) * WCOL
-        for (int tau = 0; tau < steps; ++tau) {
-            if ((tau & 31) == 0 && tau < R) {
-                const int r = tau + t;
+        const int steps2 = (R + 1) / 2 + LG - 1;
+        for (int tau = 0; tau < steps2; ++tau) {
+            if ((tau & 31) == 0 && 2 * tau < R) {
+                const int r = 2 * (tau + t);
                 if (r < R) {
                     const int la = r < rows0 ? ck_code(__ldg(tA + r)) : 0;
                     const int lb = r < rows1 ? ck_code(__ldg(tB + r)) : 0;
-                    rb_ch = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
+                    rb_ch0 = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
+                }
+                if (r + 1 < R) {
+                    const int la = r + 1 < rows0 ? ck_code(__ldg(tA + r + 1)) : 0;
+                    const int lb = r + 1 < rows1 ? ck_code(__ldg(tB + r + 1)) : 0;
+                    rb_ch1 = (uint32_t)(la * (CT / 2) * 32) | ((uint32_t)(lb * (CT / 2) * 32) << 16);
                 }
             }
-            uint32_t in_hg = __shfl_up_sync(FULL, out_hg, 1, LG);
-            uint32_t in_e = __shfl_up_sync(FULL, out_e, 1, LG);
-            ch = __shfl_up_sync(FULL, ch, 1, LG);
-            const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
-            const int er = min(tau, CK_K - 1);
-            const uint32_t l_hg = eg[2 * er], l_e = eg[2 * er + 1];
-            const int i = tau - tl + 1;                                  // window row, 1-based
+            uint32_t in_hg0 = __shfl_up_sync(FULL, out_hg, 1, LG);
+            uint32_t in_e0 = __shfl_up_sync(FULL, out_e, 1, LG);
+            uint32_t in_hg1 = __shfl_up_sync(FULL, out_hg1, 1, LG);
+            uint32_t in_e1 = __shfl_up_sync(FULL, out_e1, 1, LG);
+            ch0 = __shfl_up_sync(FULL, ch0, 1, LG);
+            ch1 = __shfl_up_sync(FULL, ch1, 1, LG);
+            const uint32_t l_ch0 = __shfl_sync(FULL, rb_ch0, tau & 31);
+            const uint32_t l_ch1 = __shfl_sync(FULL, rb_ch1, tau & 31);
+            const int er0 = min(2 * tau, CK_K - 1), er1 = min(2 * tau + 1, CK_K - 1);
+            const uint32_t l_hg0 = eg[2 * er0], l_e0 = eg[2 * er0 + 1];
+            const uint32_t l_hg1 = eg[2 * er1], l_e1 = eg[2 * er1 + 1];
+            const int i = 2 * (tau - tl) + 1;                            // window rows i, i + 1 (1-based)
             if (tl == 0) {
-                ch = l_ch;
-                in_hg = l_hg;
-                in_e = l_e;
+                ch0 = l_ch0; in_hg0 = l_hg0; in_e0 = l_e0;
+                ch1 = l_ch1; in_hg1 = l_hg1; in_e1 = l_e1;
             }
             if (i < 1 || i > R) continue;
-            const uint32_t* pA = pA0 + (ch & 0xffffu);
-            const uint32_t* pB = pB0 + (ch >> 16);
-            uint32_t hgd = diag_in, hgl = in_hg, el = in_e;
-            uint32_t hv[CT];
+            const uint32_t* pA_0 = pA0 + (ch0 & 0xffffu);
+            const uint32_t* pB_0 = pB0 + (ch0 >> 16);
+            const uint32_t* pA_1 = pA0 + (ch1 & 0xffffu);
+            const uint32_t* pB_1 = pB0 + (ch1 >> 16);
+            uint32_t hgd0 = diag_in, hgl0 = in_hg0, el0 = in_e0;
+            uint32_t hgd1 = in_hg0, hgl1 = in_hg1, el1 = in_e1;
+            uint32_t hv0[CT], hv1[CT];
 #pragma unroll
             for (int cc = 0; cc < CT; cc += 2) {
-                const uint32_t wa = pA[(cc >> 1) * 32], wb = pB[(cc >> 1) * 32];
-                const uint32_t S0 = __byte_perm(wa, wb, 0x5410), S1 = __byte_perm(wa, wb, 0x7632);
+                const uint32_t wa0 = pA_0[(cc >> 1) * 32], wb0 = pB_0[(cc >> 1) * 32];
+                const uint32_t wa1 = pA_1[(cc >> 1) * 32], wb1 = pB_1[(cc >> 1) * 32];
+                const uint32_t S00 = __byte_perm(wa0, wb0, 0x5410), S01 = __byte_perm(wa0, wb0, 0x7632);
+                const uint32_t S10 = __byte_perm(wa1, wb1, 0x5410), S11 = __byte_perm(wa1, wb1, 0x7632);
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
                     const int cu = cc + u;
-                    const uint32_t e = __viaddmax_s16x2(el, NGE2, hgl);
-                    const uint32_t f = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
-                    const uint32_t h1 = __viaddmax_s16x2(hgd, u ? S1 : S0, e);
-                    const uint32_t hh = __vimax3_s16x2(h1, f, B2);
-                    const uint32_t hg = hh - GO2;
-                    hv[cu] = hh;
-                    hgd = hgu[cu];
-                    hgu[cu] = hg;
-                    fv[cu] = f;
-                    hgl = hg;
-                    el = e;
+                    const uint32_t e0 = __viaddmax_s16x2(el0, NGE2, hgl0);
+                    const uint32_t f0 = __viaddmax_s16x2(fv[cu], NGE2, hgu[cu]);
+                    const uint32_t h10 = __viaddmax_s16x2(hgd0, u ? S01 : S00, e0);
+                    const uint32_t hh0 = __vimax3_s16x2(h10, f0, B2);
+                    const uint32_t hg0 = hh0 - GO2;
+                    hv0[cu] = hh0;
+                    hgd0 = hgu[cu];
+                    const uint32_t e1 = __viaddmax_s16x2(el1, NGE2, hgl1);
+                    const uint32_t f1 = __viaddmax_s16x2(f0, NGE2, hg0);
+                    const uint32_t h11 = __viaddmax_s16x2(hgd1, u ? S11 : S10, e1);
+                    const uint32_t hh1 = __vimax3_s16x2(h11, f1, B2);
+                    const uint32_t hg1 = hh1 - GO2;
+                    hv1[cu] = hh1;
+                    hgd1 = hg0;
+                    hgu[cu] = hg1;
+                    fv[cu] = f1;
+                    hgl0 = hg0; el0 = e0;
+                    hgl1 = hg1; el1 = e1;
                 }
             }
-            uint4* dst = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
+            uint4* dst0 = reinterpret_cast<uint4*>(hrow + (i - 1) * WCOL);
 #pragma unroll
-            for (int c = 0; c < CT; c += 4) dst[c >> 2] = make_uint4(hv[c], hv[c + 1], hv[c + 2], hv[c + 3]);
-            diag_in = in_hg;
-            out_hg = hgl;
-            out_e = el;
+            for (int c = 0; c < CT; c += 4) dst0[c >> 2] = make_uint4(hv0[c], hv0[c + 1], hv0[c + 2], hv0[c + 3]);
+            if (i + 1 <= R) {
+                uint4* dst1 = reinterpret_cast<uint4*>(hrow + i * WCOL);
+#pragma unroll
+                for (int c = 0; c < CT; c += 4) dst1[c >> 2] = make_uint4(hv1[c], hv1[c + 1], hv1[c + 2], hv1[c + 3]);
+            }
+            diag_in = in_hg1;
+            out_hg = hgl0; out_e = el0;
+            out_hg1 = hgl1; out_e1 = el1;
         }
         __syncwarp();
         // the best cell's column (a pair's first window): first column of row i*

@@ -167,51 +167,75 @@ __global__ void sp_pack_kernel(SwPlanArgs P)
 
 // ------------------------------------------------------------ validation --
 // The result checks of the reference's sw_validate (src/api/api.cpp:114-156),
-// one thread per pair over its CIGAR (written at the end of its slot): the
-// ops must consume exactly the span [start, end] of both sequences, M only on
-// equal bytes and X on unequal ones (wellformed), and re-score, with each gap
-// run costing gap_open + (L - 1) * gap_extend, to the reported score
-// (rescore).  flags[p] = rescore_ok | wellformed_ok << 1 for pairs with a
-// CIGAR, 0 otherwise.
+// one warp per pair over its CIGAR (written at the end of its slot), 32 ops at
+// a time: each lane's op steps the text and/or the pattern, a warp prefix sum
+// gives its cell, and the lanes check their ops together.  The ops must
+// consume exactly the span [start, end] of both sequences, M only on equal
+// bytes and X on unequal ones (wellformed), and re-score to the reported
+// score (rescore), each gap run costing gap_open + (L - 1) * gap_extend:
+// L * gap_extend per gap op plus gap_open - gap_extend per run, a run
+// starting at an I (or D) whose previous op is not one.  flags[p] =
+// rescore_ok | wellformed_ok << 1 for pairs with a CIGAR, 0 otherwise.
 __global__ void sw_validate_kernel(PairDesc D, int match, int mismatch, int go, int ge, const int32_t* __restrict__ score,
                                    const int32_t* __restrict__ pos, const int32_t* __restrict__ len,
                                    const char* __restrict__ cig, uint8_t* __restrict__ flags)
 {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nw) {
         const int s = score[p], L = len[p];
-        if (s <= 0 || L <= 0) { flags[p] = 0; continue; }
+        if (s <= 0 || L <= 0) {
+            if (lane == 0) flags[p] = 0;
+            continue;
+        }
         const int m = D.a_len[p], n = D.b_len[p];
         const uint8_t* T = D.seq + D.a_off[p];
         const uint8_t* P = D.seq + D.b_off[p];
         const char* cg = cig + D.out_off[p] + (m + n) - L;
         const int si = pos[4 * p], sj = pos[4 * p + 1], ei = pos[4 * p + 2], ej = pos[4 * p + 3];
-        int i = si, j = sj, total = 0, gap = 0;            // gap > 0: run of I, < 0: run of D
-        bool ok = true;
-        for (int q = 0; q < L; ++q) {
-            const char op = cg[q];
-            if (op == 'M' || op == 'X') {
-                if (gap) { total -= go + ((gap > 0 ? gap : -gap) - 1) * ge; gap = 0; }
-                if (i > ei || j > ej || i >= m || j >= n || ((T[i] == P[j]) != (op == 'M'))) ok = false;
-                total += op == 'M' ? match : mismatch;
-                ++i;
-                ++j;
-            } else if (op == 'I') {
-                if (gap < 0) { total -= go + (-gap - 1) * ge; gap = 0; }
-                if (i > ei || i >= m) ok = false;
-                ++i;
-                ++gap;
-            } else if (op == 'D') {
-                if (gap > 0) { total -= go + (gap - 1) * ge; gap = 0; }
-                if (j > ej || j >= n) ok = false;
-                ++j;
-                --gap;
-            } else {
-                ok = false;
+        int i0 = si, j0 = sj, total = 0;
+        bool bad = false;
+        char prev_last = 0;                                        // the previous chunk's last op
+        for (int q0 = 0; q0 < L; q0 += 32) {
+            const int q = q0 + lane;
+            const bool in = q < L;
+            const char op = in ? cg[q] : 0;
+            const bool mx = op == 'M' || op == 'X';
+            const int di = mx || op == 'I', dj = mx || op == 'D';
+            int v = di << 16 | dj;                                 // inclusive prefix of both steps
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, v, o);
+                if (lane >= o) v += y;
             }
+            const int i = i0 + (v >> 16) - di, j = j0 + (v & 0xffff) - dj;
+            char prev = __shfl_up_sync(FULL, op, 1);
+            if (lane == 0) prev = prev_last;
+            bool b = false;
+            int sc = 0;
+            if (in) {
+                if (mx) {
+                    b = i > ei || j > ej || i >= m || j >= n || ((T[i] == P[j]) != (op == 'M'));
+                    sc = op == 'M' ? match : mismatch;
+                } else if (op == 'I') {
+                    b = i > ei || i >= m;
+                    sc = -ge - (prev != 'I' ? go - ge : 0);
+                } else if (op == 'D') {
+                    b = j > ej || j >= n;
+                    sc = -ge - (prev != 'D' ? go - ge : 0);
+                } else {
+                    b = true;
+                }
+            }
+            bad |= __any_sync(FULL, b);
+            total += __reduce_add_sync(FULL, sc);
+            const int tot = __shfl_sync(FULL, v, 31);
+            i0 += tot >> 16;
+            j0 += tot & 0xffff;
+            prev_last = __shfl_sync(FULL, op, 31);
         }
-        if (gap) total -= go + ((gap > 0 ? gap : -gap) - 1) * ge;
-        ok = ok && i == ei + 1 && j == ej + 1;
-        flags[p] = (uint8_t)((ok && total == s ? 1 : 0) | (ok ? 2 : 0));
+        const bool ok = !bad && i0 == ei + 1 && j0 == ej + 1;
+        if (lane == 0) flags[p] = (uint8_t)((ok && total == s ? 1 : 0) | (ok ? 2 : 0));
     }
 }
 
@@ -219,8 +243,7 @@ cudaError_t launch_sw_validate(const PairDesc& D, const ga_sw_scoring_t& sc, con
                                const int32_t* len, const char* cig, uint8_t* flags, cudaStream_t st)
 {
     if (D.n <= 0) return cudaSuccess;
-    int blocks = (D.n + 127) / 128;
-    blocks = std::min(blocks, device_sms() * 16);
+    const int blocks = (int)std::min<int64_t>(((int64_t)D.n + 3) / 4, (int64_t)device_sms() * 16);   // a warp per pair
     launch_begin(K_VALIDATE, st);
     sw_validate_kernel<<<blocks, 128, 0, st>>>(D, sc.match, sc.mismatch, sc.gap_open, sc.gap_extend, score, pos, len,
                                                cig, flags);

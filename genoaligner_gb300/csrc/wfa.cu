@@ -304,42 +304,56 @@ cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* p
     return cudaGetLastError();
 }
 
-// The reference's WFA result checks (validate, src/api/api.cpp:84-112), one
-// thread per pair over its CIGAR (at the end of its slot): wellformed when
-// the ops consume exactly the pattern and the text with M only on equal bytes
-// and X only on unequal ones; rescore when the X, I and D ops number the
-// score.  flags[p] = rescore_ok | wellformed_ok << 1 for pairs with a CIGAR,
-// 0 for the others.
+// The result checks of the reference's validate (src/api/api.cpp:84-112), one
+// warp per pair over its CIGAR (at the end of its slot), 32 ops at a time:
+// each lane's op steps the pattern and/or the text, a warp prefix sum gives
+// its position, and the lanes check their M / X bytes together (the ops and
+// the bytes they compare are read contiguously).  Wellformed when the ops
+// consume exactly the pattern and the text with M only on equal bytes and X
+// only on unequal ones; rescore when the X, I and D ops number the score.
+// flags[p] = rescore_ok | wellformed_ok << 1 for pairs with a CIGAR, 0 for
+// the others.
 __global__ void wfa_validate_kernel(PairDesc D, const int32_t* __restrict__ score, const int32_t* __restrict__ len,
                                     const char* __restrict__ cig, uint8_t* __restrict__ flags)
 {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.n; p += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nw) {
         const int s = score[p], L = len[p];
-        if (s < 0 || L <= 0) { flags[p] = 0; continue; }
+        if (s < 0 || L <= 0) {
+            if (lane == 0) flags[p] = 0;
+            continue;
+        }
         const int m = D.a_len[p], n = D.b_len[p];
         const uint8_t* P = D.seq + D.a_off[p];
         const uint8_t* T = D.seq + D.b_off[p];
         const char* cg = cig + D.out_off[p] + (m + n) - L;
-        int cost = 0, pi = 0, ti = 0;
-        bool ok = true;
-        for (int q = 0; q < L; ++q) {
-            const char op = cg[q];
-            if (op == 'M' || op == 'X') {
-                if (pi >= m || ti >= n || ((P[pi] == T[ti]) != (op == 'M'))) ok = false;
-                cost += op == 'X';
-                ++pi;
-                ++ti;
-            } else if (op == 'I') {
-                ++ti;
-                ++cost;
-            } else if (op == 'D') {
-                ++pi;
-                ++cost;
-            } else {
-                ok = false;
+        int pi0 = 0, ti0 = 0, cost = 0;
+        bool bad = false;
+        for (int q0 = 0; q0 < L; q0 += 32) {
+            const int q = q0 + lane;
+            const char op = q < L ? cg[q] : 'I';
+            const bool mx = op == 'M' || op == 'X';
+            const int dp = (mx || op == 'D') && q < L, dt = (mx || op == 'I') && q < L;
+            int v = dp << 16 | dt;                                 // inclusive prefix of both steps
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, v, o);
+                if (lane >= o) v += y;
             }
+            const int pi = pi0 + (v >> 16) - dp, ti = ti0 + (v & 0xffff) - dt;
+            bool b = false;
+            if (q < L) {
+                if (mx) b = pi >= m || ti >= n || ((P[pi] == T[ti]) != (op == 'M'));
+                else b = op != 'I' && op != 'D';
+            }
+            bad |= __any_sync(FULL, b);
+            cost += __popc(__ballot_sync(FULL, q < L && (op == 'X' || op == 'I' || op == 'D')));
+            const int tot = __shfl_sync(FULL, v, 31);
+            pi0 += tot >> 16;
+            ti0 += tot & 0xffff;
         }
-        flags[p] = (uint8_t)((cost == s ? 1 : 0) | (ok && pi == m && ti == n ? 2 : 0));
+        if (lane == 0) flags[p] = (uint8_t)((cost == s ? 1 : 0) | (!bad && pi0 == m && ti0 == n ? 2 : 0));
     }
 }
 
@@ -388,8 +402,7 @@ cudaError_t launch_wfa_validate(const PairDesc& D, const int32_t* score, const i
                                 uint8_t* flags, cudaStream_t st)
 {
     if (D.n <= 0) return cudaSuccess;
-    int blocks = (D.n + 127) / 128;
-    blocks = std::min(blocks, device_sms() * 16);
+    const int blocks = (int)std::min<int64_t>(((int64_t)D.n + 3) / 4, (int64_t)device_sms() * 16);   // a warp per pair
     launch_begin(K_VALIDATE, st);
     wfa_validate_kernel<<<blocks, 128, 0, st>>>(D, score, len, cig, flags);
     launch_end(K_VALIDATE, st);
