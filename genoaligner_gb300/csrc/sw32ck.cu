@@ -51,9 +51,13 @@ struct Fwd32 {
     int sm, sx, go, ge;
 };
 
-// One band of the forward pass.  COOP: the band is one of a pair's bands run
-// by the warps of a block together (fwd32_coop); the warp then meets the
-// block's barrier after every 32 steps, ceil((m + 31) / 32) times per band.
+// One band of the forward pass, two rows per step: lane t takes rows
+// i = 2 (tau - t) + 1 and i + 1 of its CB columns.  Row i + 1's cell in
+// column c needs only row i's cells in columns c - 1 and c, so the two rows'
+// dependency chains (E along a row, H through E) are independent at equal
+// column and interleave.  COOP: the band is one of a pair's bands run by the
+// warps of a block together (fwd32_coop); the warp then meets the block's
+// barrier after every 32 steps, ceil(steps / 32) times per band.
 template <int CB, bool PROF, bool COOP>
 __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int& cb)
 {
@@ -85,80 +89,115 @@ __device__ void fwd32_band(const Fwd32& X, int b0, int t, int& vb, int& rb, int&
     int hgu[CB], fv[CB];
 #pragma unroll
     for (int c = 0; c < CB; ++c) { hgu[c] = -go; fv[c] = 0; }
-    int diag_in = -go, out_hg = -go, out_e = 0;
+    // the left neighbour's H - go at the row above this step's first row; what
+    // this lane hands right for its two rows
+    int diag_in = -go, out_hg0 = -go, out_e0 = 0, out_hg1 = -go, out_e1 = 0;
     const int32_t* left = b0 > 0 ? X.ce + 2 * (int64_t)(b0 / X.TW - 1) * m : nullptr;
     const int kout = (j0 + CB) % X.TW == 0 && j0 + CB < X.ncol ? (j0 + CB) / X.TW : 0;
     int32_t* eout = kout ? X.ce + 2 * (int64_t)(kout - 1) * m : nullptr;
     // each row's text byte (its profile offset with PROF) travels along the lanes
-    // with the boundary values; lane 0's inputs of 32 rows at a time -- that and
-    // the left edge -- are read by all lanes (lane u: row 32k + u) and shuffled
-    // to lane 0 each step, so no step runs a lane-0-only branch
-    uint32_t ch = 0, rb_ch = 0;
-    int rb_hg = -go, rb_e = 0;
+    // with the boundary values; lane 0's inputs of 64 rows at a time -- that and
+    // the left edge -- are read by all lanes (lane u: rows 64k + 2u and + 1) and
+    // shuffled to lane 0 each step, so no step runs a lane-0-only branch
+    uint32_t ch0 = 0, ch1 = 0, rb_ch0 = 0, rb_ch1 = 0;
+    int rb_hg0 = -go, rb_e0 = 0, rb_hg1 = -go, rb_e1 = 0;
     int bv = 0, br = 0;                               // this band's best and the first row holding it
-    const int steps = m + 31;
+    const int steps = (m + 1) / 2 + 31;
     for (int tau = 0; tau < steps; ++tau) {
-        if ((tau & 31) == 0 && tau < m) {
-            const int r = tau + t;
+        if ((tau & 31) == 0 && 2 * tau < m) {
+            const int r = 2 * (tau + t);
             if (r < m) {
                 const uint32_t c = __ldg(X.text + r);
-                rb_ch = PROF ? (uint32_t)(c32_code(c) * NQ * 32) : c;
+                rb_ch0 = PROF ? (uint32_t)(c32_code(c) * NQ * 32) : c;
                 if (left) {
                     const int2 lv = *reinterpret_cast<const int2*>(left + 2 * r);
-                    rb_hg = lv.x;
-                    rb_e = lv.y;
+                    rb_hg0 = lv.x;
+                    rb_e0 = lv.y;
+                }
+            }
+            if (r + 1 < m) {
+                const uint32_t c = __ldg(X.text + r + 1);
+                rb_ch1 = PROF ? (uint32_t)(c32_code(c) * NQ * 32) : c;
+                if (left) {
+                    const int2 lv = *reinterpret_cast<const int2*>(left + 2 * (r + 1));
+                    rb_hg1 = lv.x;
+                    rb_e1 = lv.y;
                 }
             }
         }
-        int in_hg = __shfl_up_sync(FULL, out_hg, 1);
-        int in_e = __shfl_up_sync(FULL, out_e, 1);
-        ch = __shfl_up_sync(FULL, ch, 1);
-        const uint32_t l_ch = __shfl_sync(FULL, rb_ch, tau & 31);
-        const int l_hg = __shfl_sync(FULL, rb_hg, tau & 31);
-        const int l_e = __shfl_sync(FULL, rb_e, tau & 31);
-        const int i = tau - t + 1;
+        int in_hg0 = __shfl_up_sync(FULL, out_hg0, 1);
+        int in_e0 = __shfl_up_sync(FULL, out_e0, 1);
+        int in_hg1 = __shfl_up_sync(FULL, out_hg1, 1);
+        int in_e1 = __shfl_up_sync(FULL, out_e1, 1);
+        ch0 = __shfl_up_sync(FULL, ch0, 1);
+        ch1 = __shfl_up_sync(FULL, ch1, 1);
+        const uint32_t l_ch0 = __shfl_sync(FULL, rb_ch0, tau & 31);
+        const int l_hg0 = __shfl_sync(FULL, rb_hg0, tau & 31);
+        const int l_e0 = __shfl_sync(FULL, rb_e0, tau & 31);
+        const uint32_t l_ch1 = __shfl_sync(FULL, rb_ch1, tau & 31);
+        const int l_hg1 = __shfl_sync(FULL, rb_hg1, tau & 31);
+        const int l_e1 = __shfl_sync(FULL, rb_e1, tau & 31);
+        const int i = 2 * (tau - t) + 1;
         if (t == 0) {
-            ch = l_ch;
-            in_hg = l_hg;
-            in_e = l_e;
+            ch0 = l_ch0; in_hg0 = l_hg0; in_e0 = l_e0;
+            ch1 = l_ch1; in_hg1 = l_hg1; in_e1 = l_e1;
         }
         if (i >= 1 && i <= m) {
-        int s[CB];
-        if constexpr (PROF) {
+            int s0[CB], s1[CB];
+            if constexpr (PROF) {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                const int4 v = X.prof[ch + q * 32 + t];
-                s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+                for (int q = 0; q < NQ; ++q) {
+                    const int4 v = X.prof[ch0 + q * 32 + t];
+                    s0[4 * q] = v.x; s0[4 * q + 1] = v.y; s0[4 * q + 2] = v.z; s0[4 * q + 3] = v.w;
+                    const int4 w = X.prof[ch1 + q * 32 + t];
+                    s1[4 * q] = w.x; s1[4 * q + 1] = w.y; s1[4 * q + 2] = w.z; s1[4 * q + 3] = w.w;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < CB; ++c) {
+                    s0[c] = c < nv ? (ch0 == pb[c] ? X.sm : X.sx) : C32_PAD;
+                    s1[c] = c < nv ? (ch1 == pb[c] ? X.sm : X.sx) : C32_PAD;
+                }
             }
-        } else {
+            int hgd0 = diag_in, hgl0 = in_hg0, el0 = in_e0;
+            int hgd1 = in_hg0, hgl1 = in_hg1, el1 = in_e1;
+            int rowmax0 = 0, rowmax1 = 0;
 #pragma unroll
-            for (int c = 0; c < CB; ++c) s[c] = c < nv ? (ch == pb[c] ? X.sm : X.sx) : C32_PAD;
-        }
-        int hgd = diag_in, hgl = in_hg, el = in_e;
-        int rowmax = 0;
+            for (int c = 0; c < CB; ++c) {
+                // row i
+                const int e0 = __viaddmax_s32(el0, -ge, hgl0);        // max(E_left - ge, H_left - go)
+                const int f0 = __viaddmax_s32(fv[c], -ge, hgu[c]);    // max(F_up - ge, H_up - go)
+                const int h0 = __vimax3_s32_relu(hgd0 + s0[c], e0, f0); // max(H_diag + s, E, F, 0)
+                const int hg0 = h0 - go;
+                rowmax0 = max(rowmax0, h0);
+                hgd0 = hgu[c];
+                // row i + 1: up is row i's cell just computed
+                const int e1 = __viaddmax_s32(el1, -ge, hgl1);
+                const int f1 = __viaddmax_s32(f0, -ge, hg0);
+                const int h1 = __vimax3_s32_relu(hgd1 + s1[c], e1, f1);
+                const int hg1 = h1 - go;
+                rowmax1 = max(rowmax1, h1);
+                hgd1 = hg0;
+                hgu[c] = hg1;
+                fv[c] = f1;
+                hgl0 = hg0; el0 = e0;
+                hgl1 = hg1; el1 = e1;
+            }
+            diag_in = in_hg1;
+            out_hg0 = hgl0; out_e0 = el0;
+            out_hg1 = hgl1; out_e1 = el1;
+            const bool two = i + 1 <= m;
+            if (eout) {
+                *reinterpret_cast<int2*>(eout + 2 * (i - 1)) = make_int2(out_hg0, out_e0);
+                if (two) *reinterpret_cast<int2*>(eout + 2 * i) = make_int2(out_hg1, out_e1);
+            }
+            if (((i + 1) & (X.K - 1)) == 0 && i + 1 < m) {           // checkpoint row i + 1 (i is odd, K even)
+                int4* dst = reinterpret_cast<int4*>(X.ck + 2 * ((int64_t)((i + 1) / X.K - 1) * X.stride + j0));
 #pragma unroll
-        for (int c = 0; c < CB; ++c) {
-            const int e = __viaddmax_s32(el, -ge, hgl);           // max(E_left - ge, H_left - go)
-            const int f = __viaddmax_s32(fv[c], -ge, hgu[c]);     // max(F_up - ge, H_up - go)
-            const int h = __vimax3_s32_relu(hgd + s[c], e, f);    // max(H_diag + s, E, F, 0)
-            const int hg = h - go;
-            rowmax = max(rowmax, h);
-            hgd = hgu[c];
-            hgu[c] = hg;
-            fv[c] = f;
-            hgl = hg;
-            el = e;
-        }
-        diag_in = in_hg;
-        out_hg = hgl;
-        out_e = el;
-        if (eout) *reinterpret_cast<int2*>(eout + 2 * (i - 1)) = make_int2(out_hg, out_e);
-        if ((i & (X.K - 1)) == 0 && i < m) {
-            int4* dst = reinterpret_cast<int4*>(X.ck + 2 * ((int64_t)(i / X.K - 1) * X.stride + j0));
-#pragma unroll
-            for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_int4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
-        }
-        if (rowmax > bv) { bv = rowmax; br = i; }          // first row holding this lane's best
+                for (int c = 0; c < CB; c += 2) dst[c >> 1] = make_int4(hgu[c], fv[c], hgu[c + 1], fv[c + 1]);
+            }
+            if (rowmax0 > bv) { bv = rowmax0; br = i; }        // first row holding this lane's best
+            if (two && rowmax1 > bv) { bv = rowmax1; br = i + 1; }
         }
         if (COOP && ((tau & 31) == 31 || tau == steps - 1)) __syncthreads();
     }
@@ -184,7 +223,7 @@ __device__ void fwd32(const Fwd32& X, int t, int& vb, int& rb, int& cb)
 // The forward pass of one pair by the W warps of a block (W = blockDim / 32,
 // 4 or 8): band b runs on warp b % W, starting at 32-step chunk start(b) =
 // max(start(b-1) + 2, start(b-W) + chunks per band), so each band's first lane reads the left edge of rows
-// 32c+1 .. 32c+32 (written by the band before it up to its step 32c + 62)
+// 64c+1 .. 64c+64 (written by the band before it up to its step 32c + 62)
 // after the barrier that closed that band's chunk c + 1, and each warp runs
 // its bands one after the other.  Every warp meets the block barrier once per
 // chunk, idle or not: start(last band) + chunks per band times in all.
@@ -192,7 +231,7 @@ template <bool PROF>
 __device__ void fwd32_coop(const Fwd32& X, int t, int wib, int& vb, int& rb, int& cb)
 {
     const int W = blockDim.x >> 5;                    // warps of the block (at most C32_MAX_WARPS)
-    const int nck = (X.m + 62) / 32;                  // ceil((m + 31) / 32)
+    const int nck = ((X.m + 1) / 2 + 62) / 32;        // chunks per band: ceil(steps / 32)
     int g = 0, prev = -2, b = 0;
     int stw[C32_MAX_WARPS];                           // start of the last band of each warp
 #pragma unroll
