@@ -41,15 +41,16 @@ BatchResult align_batch_ex(const std::vector<AlignRequest>& reqs, const AlignOpt
         int res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             AlignResult& r = out.results[(size_t)i];
-            r.score = v.score[i];
+            const int64_t q = i - v.base;           // index in the range's outputs
+            r.score = v.score[q];
             r.resolved = r.score >= 0;
             res += r.resolved;
-            if (v.trace && r.resolved && v.len[i] > 0) {
-                r.cigar.resize((size_t)v.len[i]);
-                v.cigar(i, &r.cigar[0]);
+            if (v.trace && r.resolved && v.len[q] > 0) {
+                r.cigar.resize((size_t)v.len[q]);
+                v.cigar(q, &r.cigar[0]);
                 if (v.vflags) {
-                    r.rescore_ok = v.vflags[i] & 1;
-                    r.wellformed_ok = (v.vflags[i] >> 1) & 1;
+                    r.rescore_ok = v.vflags[q] & 1;
+                    r.wellformed_ok = (v.vflags[q] >> 1) & 1;
                 } else {
                     ga::wfa_validate(r.cigar.data(), (int)r.cigar.size(), r.score, reqs[(size_t)i].pattern,
                                      reqs[(size_t)i].pattern_len, reqs[(size_t)i].text, reqs[(size_t)i].text_len,

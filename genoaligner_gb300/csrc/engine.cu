@@ -710,11 +710,26 @@ struct WfaChunk {
     int smax = INT32_MAX;
     bool trace = false;
 };
+// Large host batches run as up to WFA_RANGES contiguous ranges of whole
+// chunks, each on its own thread, context and stream (range k's priority k
+// steps below range 0's): one range's staging and its results' finish on the
+// host overlap the others' copies and kernels.  No side is shared across a
+// range start (each range's arena holds all it reads).
+constexpr int WFA_RANGES = 4;
+constexpr int64_t WFA_RANGE_MIN = 262144;
+
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
                   const WfaFinish& fin, const char** err)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
+    const int64_t nch = (n + REQ_CHUNK - 1) / REQ_CHUNK;
+    const int K = n >= WFA_RANGE_MIN ? (int)std::min<int64_t>(WFA_RANGES, nch) : 1;
+    std::vector<int64_t> kc((size_t)K + 1);                      // range k: chunks [kc[k], kc[k + 1])
+    std::vector<uint8_t> range_start((size_t)nch, 0);
+    for (int k = 0; k <= K; ++k) kc[(size_t)k] = nch * k / K;
+    for (int k = 0; k < K; ++k) range_start[(size_t)kc[(size_t)k]] = 1;
+
     // pass 1, in parallel chunks: checks (the first failing request's error,
     // as a serial pass finds it), smax, trace, own sides and sizes
     static thread_local std::vector<uint8_t> own_v;
@@ -722,9 +737,9 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     own_v.resize((size_t)n);
     slot_v.resize((size_t)n);
     uint8_t* own = own_v.data();
-    int64_t* slot_end = slot_v.data();
-    std::vector<WfaChunk> ck((size_t)((n + REQ_CHUNK - 1) / REQ_CHUNK));
-    const int64_t nch = for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+    int64_t* slot_end = slot_v.data();              // per range: CIGAR slot ends from the range's first slot
+    std::vector<WfaChunk> ck((size_t)nch);
+    for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
         WfaChunk& C = ck[(size_t)k];
         for (int64_t i = lo; i < hi; ++i) {
             const ga_align_request& r = reqs[i];
@@ -732,8 +747,9 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
                 if (const char* e = wfa_request_error(r, max_smax)) { C.bad = (int32_t)i; C.err = e; }
             C.smax = std::min(C.smax, (int)r.smax);
             C.trace |= r.with_cigar != 0;
-            const bool oa = !(i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len);
-            const bool ob = !(i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len);
+            const bool fresh = i == 0 || (i == lo && range_start[(size_t)k]);
+            const bool oa = fresh || !(r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len);
+            const bool ob = fresh || !(r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len);
             own[i] = (uint8_t)(oa | ob << 1);
             if (oa) { C.tail_a = C.arena; C.arena += round32(r.pattern_len); }
             if (ob) { C.tail_b = C.arena; C.arena += round32(r.text_len); }
@@ -744,7 +760,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     });
     int smax = INT32_MAX;
     bool trace = false;
-    std::vector<int64_t> base((size_t)(3 * nch)), carry((size_t)(2 * nch));
+    std::vector<int64_t> base((size_t)(3 * (nch + 1))), carry((size_t)(2 * nch));
     int64_t arena = 0, cig = 0, pkb = 0, ca = 0, cb = 0;
     for (int64_t k = 0; k < nch; ++k) {
         const WfaChunk& C = ck[(size_t)k];
@@ -760,121 +776,161 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         if (C.tail_b >= 0) cb = arena + C.tail_b;
         arena += C.arena; cig += C.cig; pkb += C.pkb;
     }
+    base[3 * nch] = arena; base[3 * nch + 1] = cig; base[3 * nch + 2] = pkb;
     route = route_mode(route);
     const bool learned = route != 0;
-    arena += 64;                                     // read-past padding
-    if (!trace) cig = pkb = 0;
-
-    Ctx* c = acquire_ctx(err);
-    if (!c) return GA_DEVICE_ERROR;
-    struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
     const int lane_smax = tune_current().wfa_lane_smax;
 
-    WfaScratch S;
-    size_wfa(S, n, smax, trace, learned, c->sm_count);
-    // layout: [a_off a_len b_off b_len out_off pk_off | seq] in, [score len checks err | packed CIGARs]
-    // back, then (device) the CIGAR slots and the scratch
-    int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
-    int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
-    uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
-    char* dcg;
-    auto io = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po, int64_t** ppo,
-                  uint8_t** ps, int32_t** psc, int32_t** pln, uint8_t** pvf, int32_t** per, uint8_t** ppk) {
-        *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
-        *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
-        *po = k.take<int64_t>(n); *ppo = k.take<int64_t>(n);
-        *ps = k.take<uint8_t>(arena);
-        *psc = k.take<int32_t>(n); *pln = k.take<int32_t>(n);
-        *pvf = k.take<uint8_t>(trace ? n : 0);
-        *per = k.take<int32_t>(1, 4);
-        *ppk = k.take<uint8_t>((size_t)pkb, 4);
-    };
-    Carve hk(nullptr), dk(nullptr);
-    io(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
-    io(dk, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
-    dcg = dk.take<char>(cig + 1);
-    carve_wfa(dk, S, n, arena, trace, learned);
-    if (fail_here(1) || !ensure_dev(c, dk.off)) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
-    if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
-    {
-        Carve h(c->host), d(c->dev);
-        io(h, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
-        io(d, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
-        dcg = d.take<char>(cig + 1);
-        carve_wfa(d, S, n, arena, trace, learned);
-    }
+    // one range: requests of chunks [kc[k], kc[k + 1]), offsets from the range's own bases
+    std::vector<int64_t> rh2d((size_t)K, 0), rd2h((size_t)K, 0);
+    auto run_range = [&](int k, const char** rerr) -> int32_t {
+        const int64_t c0 = kc[(size_t)k], c1 = kc[(size_t)k + 1];
+        const int64_t r0 = std::min<int64_t>(n, c0 * REQ_CHUNK), r1 = std::min<int64_t>(n, c1 * REQ_CHUNK);
+        const int32_t nk = (int32_t)(r1 - r0);
+        if (nk <= 0) return GA_OK;
+        const int64_t a0 = base[3 * c0], g0 = base[3 * c0 + 1], p0 = base[3 * c0 + 2];
+        const int64_t arena_k = base[3 * c1] - a0 + 64;             // + read-past padding
+        const int64_t cig_k = trace ? base[3 * c1 + 1] - g0 : 0;
+        const int64_t pkb_k = trace ? base[3 * c1 + 2] - p0 : 0;
 
-    // pass 2, in the same chunks: offsets and the staging of every own side
-    for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
-        int64_t at = base[3 * k], cg = base[3 * k + 1], pk = base[3 * k + 2];
-        int64_t cur_a = carry[2 * k], cur_b = carry[2 * k + 1];
-        for (int64_t i = lo; i < hi; ++i) {
-            const ga_align_request& r = reqs[i];
-            if (own[i] & 1) {
-                cur_a = at;
-                at += round32(r.pattern_len);
-                if (r.pattern_len) std::memcpy(hseq + cur_a, r.pattern, (size_t)r.pattern_len);
-            }
-            if (own[i] & 2) {
-                cur_b = at;
-                at += round32(r.text_len);
-                if (r.text_len) std::memcpy(hseq + cur_b, r.text, (size_t)r.text_len);
-            }
-            ha[i] = cur_a; hal[i] = r.pattern_len;
-            hb[i] = cur_b; hbl[i] = r.text_len;
-            const int64_t cap = (int64_t)r.pattern_len + r.text_len;
-            ho[i] = cg; cg += cap;
-            slot_end[i] = cg;
-            hpo[i] = pk; pk += (cap + 3) / 4;
+        Ctx* c = acquire_ctx(rerr, K > 1 ? k : -1);
+        if (!c) return GA_DEVICE_ERROR;
+        struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
+        WfaScratch S;
+        size_wfa(S, nk, smax, trace, learned, c->sm_count);
+        // layout: [a_off a_len b_off b_len out_off pk_off | seq] in, [score len checks err | packed CIGARs]
+        // back, then (device) the CIGAR slots and the scratch
+        int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
+        int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
+        uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
+        char* dcg;
+        auto io = [&](Carve& q, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
+                      int64_t** ppo, uint8_t** ps, int32_t** psc, int32_t** pln, uint8_t** pvf, int32_t** per,
+                      uint8_t** ppk) {
+            *pa = q.take<int64_t>(nk); *pal = q.take<int32_t>(nk);
+            *pb = q.take<int64_t>(nk); *pbl = q.take<int32_t>(nk);
+            *po = q.take<int64_t>(nk); *ppo = q.take<int64_t>(nk);
+            *ps = q.take<uint8_t>(arena_k);
+            *psc = q.take<int32_t>(nk); *pln = q.take<int32_t>(nk);
+            *pvf = q.take<uint8_t>(trace ? nk : 0);
+            *per = q.take<int32_t>(1, 4);
+            *ppk = q.take<uint8_t>((size_t)pkb_k, 4);
+        };
+        Carve hk(nullptr), dk(nullptr);
+        io(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+        io(dk, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+        dcg = dk.take<char>(cig_k + 1);
+        carve_wfa(dk, S, nk, arena_k, trace, learned);
+        if (fail_here(1) || !ensure_dev(c, dk.off)) { *rerr = E_ALLOC; return GA_DEVICE_ERROR; }
+        if (!ensure_host(c, hk.off)) { *rerr = E_HOSTMEM; return GA_DEVICE_ERROR; }
+        {
+            Carve h(c->host), d(c->dev);
+            io(h, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+            io(d, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+            dcg = d.take<char>(cig_k + 1);
+            carve_wfa(d, S, nk, arena_k, trace, learned);
         }
-    });
-    std::memset(hseq + arena - 64, 0, 64);
-    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);     // descriptors + arena, contiguous
-    t_h2d = (int64_t)in_bytes;
-    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
-        cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream) != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_H2D;
-        return GA_DEVICE_ERROR;
+
+        // pass 2, in the same chunks: offsets and the staging of every own side
+        parallel_for(c1 - c0, 1, [&](int64_t j0, int64_t j1) {
+            for (int64_t kk = c0 + j0; kk < c0 + j1; ++kk) {
+                const int64_t lo = kk * REQ_CHUNK, hi = std::min<int64_t>(n, lo + REQ_CHUNK);
+                int64_t at = base[3 * kk] - a0, cg = base[3 * kk + 1] - g0, pk = base[3 * kk + 2] - p0;
+                int64_t cur_a = carry[2 * kk] - a0, cur_b = carry[2 * kk + 1] - a0;
+                for (int64_t i = lo; i < hi; ++i) {
+                    const ga_align_request& r = reqs[i];
+                    const int64_t q = i - r0;
+                    if (own[i] & 1) {
+                        cur_a = at;
+                        at += round32(r.pattern_len);
+                        if (r.pattern_len) std::memcpy(hseq + cur_a, r.pattern, (size_t)r.pattern_len);
+                    }
+                    if (own[i] & 2) {
+                        cur_b = at;
+                        at += round32(r.text_len);
+                        if (r.text_len) std::memcpy(hseq + cur_b, r.text, (size_t)r.text_len);
+                    }
+                    ha[q] = cur_a; hal[q] = r.pattern_len;
+                    hb[q] = cur_b; hbl[q] = r.text_len;
+                    const int64_t cap = (int64_t)r.pattern_len + r.text_len;
+                    ho[q] = cg; cg += cap;
+                    slot_end[i] = cg;
+                    hpo[q] = pk; pk += (cap + 3) / 4;
+                }
+            }
+        });
+        std::memset(hseq + arena_k - 64, 0, 64);
+        const size_t in_bytes = (size_t)((char*)(hseq + arena_k) - c->host);   // descriptors + arena, contiguous
+        rh2d[(size_t)k] = (int64_t)in_bytes;
+        if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+            cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *rerr = E_H2D;
+            return GA_DEVICE_ERROR;
+        }
+        PairDesc D;
+        D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
+        D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = nk;
+        cudaError_t le;
+        if (fail_here(3)) le = cudaErrorLaunchFailure;
+        else if (learned && !profiling_on())
+            le = run_wfa_graph(c, S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
+        else le = enqueue_wfa(S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
+        if (learned) note_route(c, S, nk);
+        if (le == cudaSuccess && trace) le = launch_wfa_validate(D, dsc, dln, dcg, dvf, c->stream);
+        if (le == cudaSuccess && trace) le = launch_cigar_pack(D, dln, dcg, dpo, dpk, c->stream);
+        if (le != cudaSuccess) {
+            cudaGetLastError();
+            *rerr = E_LAUNCH;
+            return GA_DEVICE_ERROR;
+        }
+        // outputs are contiguous on both sides: score, len, checks, err, packed CIGARs
+        const size_t out_bytes = (size_t)((char*)(dpk + pkb_k) - (char*)dsc);
+        rd2h[(size_t)k] = (int64_t)out_bytes;
+        if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *rerr = E_D2H;
+            return GA_DEVICE_ERROR;
+        }
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            *rerr = E_SYNC;
+            return GA_DEVICE_ERROR;
+        }
+        if (*her != 0) { *rerr = E_OVERFLOW; return GA_DEVICE_ERROR; }
+        if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
+        WfaView v{hsc, hln, hpk, hpo, slot_end + r0, trace, trace ? hvf : nullptr, r0, g0};
+        std::atomic<bool> bad{false};
+        parallel_for(nk, 1024, [&](int64_t lo, int64_t hi) {
+            if (trace && !lengths_fit(hln, slot_end + r0, lo, hi)) { bad = true; return; }
+            fin(r0 + lo, r0 + hi, v);
+        });
+        if (bad) { *rerr = E_BADLEN; return GA_DEVICE_ERROR; }
+        return GA_OK;
+    };
+    std::vector<int32_t> st((size_t)K, GA_OK);
+    std::vector<const char*> errs((size_t)K, nullptr);
+    if (K == 1) {
+        st[0] = run_range(0, &errs[0]);
+    } else {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::vector<std::thread> th;
+        for (int k = 0; k + 1 < K; ++k)
+            th.emplace_back([&, k] {
+                cudaSetDevice(dev);
+                st[(size_t)k] = run_range(k, &errs[(size_t)k]);
+            });
+        st[(size_t)K - 1] = run_range(K - 1, &errs[(size_t)K - 1]);   // this thread keeps the last range's route record
+        for (std::thread& x : th) x.join();
     }
-    PairDesc D;
-    D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
-    D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = n;
-    cudaError_t le;
-    if (fail_here(3)) le = cudaErrorLaunchFailure;
-    else if (learned && !profiling_on())
-        le = run_wfa_graph(c, S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
-    else le = enqueue_wfa(S, D, smax, trace, route, lane_smax, dsc, dln, dcg, der, c->stream);
-    if (learned) note_route(c, S, n);
-    if (le == cudaSuccess && trace) le = launch_wfa_validate(D, dsc, dln, dcg, dvf, c->stream);
-    if (le == cudaSuccess && trace) le = launch_cigar_pack(D, dln, dcg, dpo, dpk, c->stream);
-    if (le != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_LAUNCH;
-        return GA_DEVICE_ERROR;
-    }
-    // outputs are contiguous on both sides: score, len, checks, err, packed CIGARs
-    const size_t out_bytes = (size_t)((char*)(dpk + pkb) - (char*)dsc);
-    t_d2h = (int64_t)out_bytes;
-    if (fail_here(4) || cudaMemcpyAsync(hsc, dsc, out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_D2H;
-        return GA_DEVICE_ERROR;
-    }
-    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
-        cudaGetLastError();
-        *err = E_SYNC;
-        return GA_DEVICE_ERROR;
-    }
-    if (*her != 0) { *err = E_OVERFLOW; return GA_DEVICE_ERROR; }
-    if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
-    WfaView v{hsc, hln, hpk, hpo, slot_end, trace, trace ? hvf : nullptr};
-    std::atomic<bool> bad{false};
-    parallel_for(n, 1024, [&](int64_t lo, int64_t hi) {
-        if (trace && !lengths_fit(hln, slot_end, lo, hi)) { bad = true; return; }
-        fin(lo, hi, v);
-    });
-    if (bad) { *err = E_BADLEN; return GA_DEVICE_ERROR; }
+    t_h2d = t_d2h = 0;
+    for (int k = 0; k < K; ++k) { t_h2d += rh2d[(size_t)k]; t_d2h += rd2h[(size_t)k]; }
+    for (int k = 0; k < K; ++k)
+        if (st[(size_t)k] != GA_OK) {
+            *err = errs[(size_t)k];
+            return st[(size_t)k];
+        }
     return GA_OK;
 }
 
@@ -1565,21 +1621,22 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
         int32_t res = 0;
         for (int64_t i = lo; i < hi; ++i) {
             ga_align_result& r = results[i];
+            const int64_t q = i - v.base;           // index in the range's outputs
             r = dflt;                               // every pair of the batch passes here once
-            r.score = v.score[i];
+            r.score = v.score[q];
             r.resolved = r.score >= 0;
             res += r.resolved;
-            if (v.trace && r.resolved && v.len[i] > 0) {
-                const int64_t at = v.slot_end[i] - v.len[i];
-                v.cigar(i, cigar_buf + at);
+            if (v.trace && r.resolved && v.len[q] > 0) {
+                const int64_t at = v.cig_base + v.slot_end[q] - v.len[q];
+                v.cigar(q, cigar_buf + at);
                 r.cigar_offset = at;
-                r.cigar_len = v.len[i];
+                r.cigar_len = v.len[q];
                 bool rs = false, wf = false;
                 if (v.vflags) {
-                    rs = v.vflags[i] & 1;
-                    wf = (v.vflags[i] >> 1) & 1;
+                    rs = v.vflags[q] & 1;
+                    wf = (v.vflags[q] >> 1) & 1;
                 } else {
-                    wfa_validate(cigar_buf + at, v.len[i], r.score, reqs[i].pattern, reqs[i].pattern_len,
+                    wfa_validate(cigar_buf + at, v.len[q], r.score, reqs[i].pattern, reqs[i].pattern_len,
                                  reqs[i].text, reqs[i].text_len, &rs, &wf);
                 }
                 r.rescore_ok = rs;

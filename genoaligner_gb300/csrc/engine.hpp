@@ -18,9 +18,10 @@ void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, in
 // its own byte offset: expand len ops into dst.
 void expand_cigar(const uint8_t* src, int len, char* dst);
 
-// Per-pair outputs of a WFA batch, valid during the finish callback.  The
-// CIGAR of pair i has len[i] ops packed at pk + pk_off[i]; its slot in the
-// caller's buffer ends at slot_end[i].
+// Per-pair outputs of a WFA batch (or of one range of it: the batch's pairs
+// base .. base + n - 1), valid during the finish callback, indexed by
+// q = i - base.  The CIGAR of pair q has len[q] ops packed at pk + pk_off[q];
+// its slot in the caller's buffer ends at cig_base + slot_end[q].
 struct WfaView {
     const int32_t* score;
     const int32_t* len;
@@ -29,7 +30,9 @@ struct WfaView {
     const int64_t* slot_end;
     bool trace;
     const uint8_t* vflags;    // checks done on the device: rescore_ok | wellformed_ok << 1 (null: check on the host)
-    void cigar(int64_t i, char* dst) const { expand_cigar(pk + pk_off[i], len[i], dst); }
+    int64_t base;
+    int64_t cig_base;
+    void cigar(int64_t q, char* dst) const { expand_cigar(pk + pk_off[q], len[q], dst); }
 };
 using WfaFinish = std::function<void(int64_t lo, int64_t hi, const WfaView& v)>;
 

@@ -207,8 +207,9 @@ int32_t ga_wfa_device_ex(const ga_device_batch* batch, int32_t smax, int32_t tra
  * in the lane queue (one pair per lane), out[1] = pairs in the warp queue (one
  * pair per warp), out[2] = pairs the lane queue escalated to the warp queue
  * (unresolved within their first smax, or handed over), out[3] = warp-queue
- * pairs run on a whole block (estimated distance >= 256); out[4..] = 0.
- * Synchronises the device. */
+ * pairs run on a whole block (estimated distance >= 256); out[4..] = 0.  A
+ * host batch of 262,144 pairs or more runs in up to 4 ranges: the record is
+ * then its last range's.  Synchronises the device. */
 int32_t ga_wfa_route_stats(int32_t* out, int32_t max);
 
 /* Queue item of every pair of the calling thread's last learned WFA call
