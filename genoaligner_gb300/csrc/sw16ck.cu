@@ -2,7 +2,7 @@
 // lanes: a score-only forward pass that keeps checkpoints, then the walk over
 // windows of 64 x 64 tiles recomputed from them.
 //
-// Same recurrence, tie rules and walk as sw.cu and sw16.cu (the reference's
+// Same recurrence, tie rules and walk as the reference's (its
 // trace recurrence, include/genoaligner/backend/sw_kernel_impl.hip:286-329,
 // walk :198-242, best cell = first strict maximum in row-major order).  What
 // changes is where the direction bits come from.  Storing four predicate bits
@@ -30,8 +30,9 @@
 //      columns.
 //
 // Recomputed values equal the forward pass's, so every decision is the one
-// the reference's stored direction bits give.  Eligibility is sw16.cu's
-// (host-side check).
+// the reference's stored direction bits give.  Eligibility (16-bit scores
+// proven, or tried with the overflow check) is decided by the plan
+// (sw_plan.cu, sw_sizes.cuh).
 //
 // The score-only form (sw16so_kernel, at the end) runs step 1 alone, without
 // checkpoint rows, and picks the end cell by the reference's score-only rule
@@ -595,7 +596,7 @@ __device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, in
     const uint32_t NGE2 = ((uint32_t)(-ge) & 0xffffu) * 0x10001u;
     const uint32_t GO2 = (uint32_t)go * 0x10001u;
     const uint32_t MIN2 = 0x80008000u;
-    // biased recompute constants (sw16.cu)
+    // biased recompute constants (every value + BIAS16, sw_sizes.cuh)
     const uint32_t B2 = (uint32_t)CK_BIAS * 0x10001u;
 
     const int pa = work[2 * w];
