@@ -98,3 +98,21 @@ def test_no_device_is_device_error():
     b = api.align_batch([api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=8)])
     assert b.status == api.Status.device_error and b.error
     assert b.resolved_count == 0 and b.unresolved_count == 0
+
+
+def test_first_failure_across_chunks_in_request_order():
+    """Requests are checked in parallel chunks of 1,024; the error reported is
+    still the first failing request's, and every result is the default."""
+    reqs = [api.AlignRequest(b"ACGTACGT", 8, b"ACGTTCGT", 8, smax=8) for _ in range(5000)]
+    reqs[4500] = api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=600)
+    reqs[3000] = api.AlignRequest(b"ACGT", -1, b"ACGT", 4, smax=8)
+    reqs[3001] = api.AlignRequest(None, 3, b"ACG", 3, smax=8)
+    b = api.align_batch(reqs)
+    assert b.status == api.Status.invalid_argument and b.error == "negative length"
+    assert len(b.results) == 5000 and all(r.score == -1 and not r.resolved for r in b.results)
+    assert b.resolved_count == 0 and b.unresolved_count == 0
+    sw = [api.SWRequest(b"ACGTACGT", 8, b"ACGT", 4, api.SWScoring(2, -3, 5, 2)) for _ in range(5000)]
+    sw[4000] = api.SWRequest(b"ACGT", 4, None, 5, api.SWScoring(2, -3, 5, 2))
+    sw[2500] = api.SWRequest(b"ACGT", 4, b"ACGT", 4, api.SWScoring(1, -1, 2, 1))
+    b = api.align_sw_batch(sw)
+    assert b.error == "all requests in an SW batch must share one scoring scheme"
