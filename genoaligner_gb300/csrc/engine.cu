@@ -1237,7 +1237,12 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     // every launch is enqueued without reading the plan back.
     const bool route = learned && trace;                 // the SW model picks the 16-bit pairs
     const SwPlan P = bound_plan_sw(reqs, n, trace, trace ? cell_limit : -1, T, route);
-    const SwSlots S = size_sw(P, trace, T, c->sm_count, sw_dir_budget(c, parts));
+    SwSlots S = size_sw(P, trace, T, c->sm_count, sw_dir_budget(c, parts));
+    // Ranges that run beside others give their 16-bit persistent kernel three
+    // quarters of the device's blocks: the next range's pack and plan kernels
+    // then find room while this range runs, instead of waiting for its tail
+    // (200,000-pair batch end to end: 30.2 -> 29.7 ms; half the blocks: 30.3).
+    if (parts > 1 && S.s[SP_L16] > 0) S.s[SP_L16] = std::max(4, S.s[SP_L16] * 3 / 4 / 4 * 4);
 
     // Host staging: [descriptors | arena] in, [score pos len checks err | packed
     // CIGARs] back.  Device: the same blocks, then the CIGAR slots, purity
