@@ -430,6 +430,57 @@ static inline int64_t round32(int64_t x) { return (x + 31) & ~(int64_t)31; }
 // Requests per chunk of the host passes over a batch's requests.
 constexpr int64_t REQ_CHUNK = 1024;
 
+// Where a batch's own sides of one kind (patterns, or texts) lie in the
+// caller's memory, in request order: [first, end) when every side starts at
+// or after the previous one's end and less than 4,096 bytes past it -- so
+// every page of the span holds part of a side, and the span can be read as
+// one block.
+struct SideSpan {
+    uintptr_t first = 0, end = 0;
+    int64_t bytes = 0;
+    bool ok = true;
+    void add(const void* p, int32_t len)
+    {
+        if (len <= 0) return;
+        const uintptr_t a = (uintptr_t)p;
+        if (bytes == 0) first = a;
+        else if (a < end || a - end >= 4096) ok = false;
+        end = a + (uintptr_t)len;
+        bytes += len;
+    }
+    void join(const SideSpan& o)                 // this span followed by o
+    {
+        if (o.bytes == 0) return;
+        if (bytes == 0) { *this = o; return; }
+        ok = ok && o.ok && o.first >= end && o.first - end < 4096;
+        end = o.end;
+        bytes += o.bytes;
+    }
+};
+
+// Copies from pageable host memory run at close to the pinned rate where the
+// device reaches host memory through the host's page tables (coherent
+// host-device links): there the host entries copy dense caller spans straight
+// to the device instead of staging every sequence through pinned memory.
+static bool pageable_direct()
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return false; }
+    int v = cache[dev].load();
+    if (v == 0) {
+        int a = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            a = 0;
+        }
+        v = a == 1 ? 1 : 2;
+        cache[dev].store(v);
+    }
+    return v == 1;
+}
+constexpr int64_t SPAN_MIN_BYTES = (int64_t)1 << 20;    // below this, staging is cheaper than two more copies
+
 // fn(k, lo, hi) on chunk k = [lo, hi) of [0, n), the chunks in parallel on the
 // host pool; returns the number of chunks.
 template <class F>
@@ -709,6 +760,7 @@ struct WfaChunk {
     const char* err = nullptr;
     int smax = INT32_MAX;
     bool trace = false;
+    SideSpan sa, sb;                        // where its own patterns and texts lie in the caller's memory
 };
 // Large host batches run as up to WFA_RANGES contiguous ranges of whole
 // chunks, each on its own thread, context and stream (range k's priority k
@@ -751,8 +803,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
             const bool oa = fresh || !(r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len);
             const bool ob = fresh || !(r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len);
             own[i] = (uint8_t)(oa | ob << 1);
-            if (oa) { C.tail_a = C.arena; C.arena += round32(r.pattern_len); }
-            if (ob) { C.tail_b = C.arena; C.arena += round32(r.text_len); }
+            if (oa) { C.tail_a = C.arena; C.arena += round32(r.pattern_len); C.sa.add(r.pattern, r.pattern_len); }
+            if (ob) { C.tail_b = C.arena; C.arena += round32(r.text_len); C.sb.add(r.text, r.text_len); }
             const int64_t cap = (int64_t)r.pattern_len + r.text_len;
             C.cig += cap;
             C.pkb += (cap + 3) / 4;
@@ -793,23 +845,31 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         const int64_t cig_k = trace ? base[3 * c1 + 1] - g0 : 0;
         const int64_t pkb_k = trace ? base[3 * c1 + 2] - p0 : 0;
 
+        // the range's own patterns and texts: copied as the caller laid them
+        // out (two spans) and moved into place on the device, or staged here
+        SideSpan spa, spb;
+        for (int64_t kk = c0; kk < c1; ++kk) { spa.join(ck[(size_t)kk].sa); spb.join(ck[(size_t)kk].sb); }
+        const bool span = spa.ok && spb.ok && spa.bytes + spb.bytes >= SPAN_MIN_BYTES && pageable_direct();
+        const int64_t span_a = span ? (int64_t)(spa.end - spa.first) : 0, span_b = span ? (int64_t)(spb.end - spb.first) : 0;
+
         Ctx* c = acquire_ctx(rerr, K > 1 ? k : -1);
         if (!c) return GA_DEVICE_ERROR;
         struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
         WfaScratch S;
         size_wfa(S, nk, smax, trace, learned, c->sm_count);
-        // layout: [a_off a_len b_off b_len out_off pk_off | seq] in, [score len checks err | packed CIGARs]
-        // back, then (device) the CIGAR slots and the scratch
-        int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
+        // layout: [a_off a_len b_off b_len out_off pk_off (src_a src_b) | seq] in, [score len checks err |
+        // packed CIGARs] back, then (device) the CIGAR slots, the scratch and the caller's spans
+        int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo, *hsa, *hsb, *dsa, *dsb;
         int32_t *hal, *hbl, *dal, *dbl, *hsc, *hln, *dsc, *dln, *her, *der;
-        uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
+        uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk, *dspan_a, *dspan_b;
         char* dcg;
         auto io = [&](Carve& q, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
-                      int64_t** ppo, uint8_t** ps, int32_t** psc, int32_t** pln, uint8_t** pvf, int32_t** per,
-                      uint8_t** ppk) {
+                      int64_t** ppo, int64_t** psa, int64_t** psb, uint8_t** ps, int32_t** psc, int32_t** pln,
+                      uint8_t** pvf, int32_t** per, uint8_t** ppk) {
             *pa = q.take<int64_t>(nk); *pal = q.take<int32_t>(nk);
             *pb = q.take<int64_t>(nk); *pbl = q.take<int32_t>(nk);
             *po = q.take<int64_t>(nk); *ppo = q.take<int64_t>(nk);
+            *psa = q.take<int64_t>(span ? nk : 0); *psb = q.take<int64_t>(span ? nk : 0);
             *ps = q.take<uint8_t>(arena_k);
             *psc = q.take<int32_t>(nk); *pln = q.take<int32_t>(nk);
             *pvf = q.take<uint8_t>(trace ? nk : 0);
@@ -817,18 +877,22 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
             *ppk = q.take<uint8_t>((size_t)pkb_k, 4);
         };
         Carve hk(nullptr), dk(nullptr);
-        io(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
-        io(dk, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+        io(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hsa, &hsb, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+        io(dk, &da, &dal, &db, &dbl, &dout, &dpo, &dsa, &dsb, &dseq, &dsc, &dln, &dvf, &der, &dpk);
         dcg = dk.take<char>(cig_k + 1);
         carve_wfa(dk, S, nk, arena_k, trace, learned);
+        dspan_a = dk.take<uint8_t>((size_t)span_a);
+        dspan_b = dk.take<uint8_t>((size_t)span_b);
         if (fail_here(1) || !ensure_dev(c, dk.off)) { *rerr = E_ALLOC; return GA_DEVICE_ERROR; }
         if (!ensure_host(c, hk.off)) { *rerr = E_HOSTMEM; return GA_DEVICE_ERROR; }
         {
             Carve h(c->host), d(c->dev);
-            io(h, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hln, &hvf, &her, &hpk);
-            io(d, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dln, &dvf, &der, &dpk);
+            io(h, &ha, &hal, &hb, &hbl, &ho, &hpo, &hsa, &hsb, &hseq, &hsc, &hln, &hvf, &her, &hpk);
+            io(d, &da, &dal, &db, &dbl, &dout, &dpo, &dsa, &dsb, &dseq, &dsc, &dln, &dvf, &der, &dpk);
             dcg = d.take<char>(cig_k + 1);
             carve_wfa(d, S, nk, arena_k, trace, learned);
+            dspan_a = d.take<uint8_t>((size_t)span_a);
+            dspan_b = d.take<uint8_t>((size_t)span_b);
         }
 
         // pass 2, in the same chunks: offsets and the staging of every own side
@@ -840,15 +904,22 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
                 for (int64_t i = lo; i < hi; ++i) {
                     const ga_align_request& r = reqs[i];
                     const int64_t q = i - r0;
+                    if (span) { hsa[q] = -1; hsb[q] = -1; }
                     if (own[i] & 1) {
                         cur_a = at;
                         at += round32(r.pattern_len);
-                        if (r.pattern_len) std::memcpy(hseq + cur_a, r.pattern, (size_t)r.pattern_len);
+                        if (r.pattern_len > 0) {
+                            if (span) hsa[q] = (int64_t)((uintptr_t)r.pattern - spa.first);
+                            else std::memcpy(hseq + cur_a, r.pattern, (size_t)r.pattern_len);
+                        }
                     }
                     if (own[i] & 2) {
                         cur_b = at;
                         at += round32(r.text_len);
-                        if (r.text_len) std::memcpy(hseq + cur_b, r.text, (size_t)r.text_len);
+                        if (r.text_len > 0) {
+                            if (span) hsb[q] = (int64_t)((uintptr_t)r.text - spb.first);
+                            else std::memcpy(hseq + cur_b, r.text, (size_t)r.text_len);
+                        }
                     }
                     ha[q] = cur_a; hal[q] = r.pattern_len;
                     hb[q] = cur_b; hbl[q] = r.text_len;
@@ -859,18 +930,29 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
                 }
             }
         });
-        std::memset(hseq + arena_k - 64, 0, 64);
-        const size_t in_bytes = (size_t)((char*)(hseq + arena_k) - c->host);   // descriptors + arena, contiguous
-        rh2d[(size_t)k] = (int64_t)in_bytes;
-        if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
-            cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream) != cudaSuccess) {
+        if (!span) std::memset(hseq + arena_k - 64, 0, 64);
+        // descriptors (+ the arena when staged here), contiguous; the spans from the caller's memory
+        const size_t in_bytes = (size_t)((char*)(span ? hseq : hseq + arena_k) - c->host);
+        rh2d[(size_t)k] = (int64_t)in_bytes + span_a + span_b;
+        PairDesc D;
+        D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
+        D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = nk;
+        bool ok = !fail_here(2) &&
+                  cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) == cudaSuccess &&
+                  cudaMemsetAsync(der, 0, sizeof(int32_t), c->stream) == cudaSuccess;
+        if (ok && span) {
+            ok = (span_a == 0 || cudaMemcpyAsync(dspan_a, (const void*)spa.first, (size_t)span_a,
+                                                 cudaMemcpyHostToDevice, c->stream) == cudaSuccess) &&
+                 (span_b == 0 || cudaMemcpyAsync(dspan_b, (const void*)spb.first, (size_t)span_b,
+                                                 cudaMemcpyHostToDevice, c->stream) == cudaSuccess) &&
+                 launch_gather_sides(D, dseq, dspan_a, dspan_b, dsa, dsb, c->stream) == cudaSuccess &&
+                 cudaMemsetAsync(dseq + arena_k - 64, 0, 64, c->stream) == cudaSuccess;
+        }
+        if (!ok) {
             cudaGetLastError();
             *rerr = E_H2D;
             return GA_DEVICE_ERROR;
         }
-        PairDesc D;
-        D.seq = dseq; D.packed = nullptr; D.pure = nullptr;
-        D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout; D.n = nk;
         cudaError_t le;
         if (fail_here(3)) le = cudaErrorLaunchFailure;
         else if (learned && !profiling_on())
@@ -1213,14 +1295,15 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     std::vector<int64_t> a_off(n), b_off(n), out_off(n), slot_end(n), pk_off(n);
     std::vector<uint8_t> own(n, 0);
     int64_t arena = 0, cig = 0, pkb = 0;
+    SideSpan spa, spb;                          // where the own texts and patterns lie in the caller's memory
     for (int32_t i = 0; i < n; ++i) {
         const ga_sw_request& r = reqs[i];
         // a side that repeats the previous request's (same pointer and length:
         // one reference against many, or many against one) is staged once
         if (i > 0 && r.text == reqs[i - 1].text && r.text_len == reqs[i - 1].text_len) a_off[i] = a_off[i - 1];
-        else { a_off[i] = arena; arena += round32(r.text_len); own[i] |= 1; }
+        else { a_off[i] = arena; arena += round32(r.text_len); own[i] |= 1; spa.add(r.text, r.text_len); }
         if (i > 0 && r.pattern == reqs[i - 1].pattern && r.pattern_len == reqs[i - 1].pattern_len) b_off[i] = b_off[i - 1];
-        else { b_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 2; }
+        else { b_off[i] = arena; arena += round32(r.pattern_len); own[i] |= 2; spb.add(r.pattern, r.pattern_len); }
         const int64_t cap = (int64_t)r.text_len + r.pattern_len;
         out_off[i] = cig; cig += cap;
         slot_end[i] = cig;
@@ -1228,6 +1311,10 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     }
     arena += 64;
     if (!trace) cig = pkb = 0;
+    // the own sides copied as the caller laid them out (two spans) and moved
+    // into place on the device, or staged here
+    const bool span = spa.ok && spb.ok && spa.bytes + spb.bytes >= SPAN_MIN_BYTES && pageable_direct();
+    const int64_t span_a = span ? (int64_t)(spa.end - spa.first) : 0, span_b = span ? (int64_t)(spb.end - spb.first) : 0;
 
     Ctx* c = acquire_ctx(err, range_tag);
     if (!c) return GA_DEVICE_ERROR;
@@ -1244,20 +1331,21 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     // (200,000-pair batch end to end: 30.2 -> 29.7 ms; half the blocks: 30.3).
     if (parts > 1 && S.s[SP_L16] > 0) S.s[SP_L16] = std::max(4, S.s[SP_L16] * 3 / 4 / 4 * 4);
 
-    // Host staging: [descriptors | arena] in, [score pos len checks err | packed
-    // CIGARs] back.  Device: the same blocks, then the CIGAR slots, purity
-    // flags, the plan's work lists, its scratch and record, counters, band
-    // edges, direction tables.
-    int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo;
+    // Host staging: [descriptors (span offsets) | arena] in, [score pos len
+    // checks err | packed CIGARs] back.  Device: the same blocks, then the CIGAR
+    // slots, purity flags, the plan's work lists, its scratch and record,
+    // counters, band edges, direction tables, the caller's spans.
+    int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo, *hsa, *hsb, *dsa, *dsb;
     int32_t *hal, *hbl, *dal, *dbl, *hsc, *hpos, *hln, *dsc, *dpos, *dln, *her, *der;
-    uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk;
+    uint8_t *hseq, *dseq, *hvf, *dvf, *hpk, *dpk, *dspan_a, *dspan_b;
     char* dcg;
     auto io_layout = [&](Carve& k, int64_t** pa, int32_t** pal, int64_t** pb, int32_t** pbl, int64_t** po,
-                         int64_t** ppo, uint8_t** ps, int32_t** psc, int32_t** ppos, int32_t** pln, uint8_t** pvf,
-                         int32_t** per, uint8_t** ppk) {
+                         int64_t** ppo, int64_t** psa, int64_t** psb, uint8_t** ps, int32_t** psc, int32_t** ppos,
+                         int32_t** pln, uint8_t** pvf, int32_t** per, uint8_t** ppk) {
         *pa = k.take<int64_t>(n); *pal = k.take<int32_t>(n);
         *pb = k.take<int64_t>(n); *pbl = k.take<int32_t>(n);
         *po = k.take<int64_t>(n); *ppo = k.take<int64_t>(n);
+        *psa = k.take<int64_t>(span ? n : 0); *psb = k.take<int64_t>(span ? n : 0);
         *ps = k.take<uint8_t>(arena);
         *psc = k.take<int32_t>(n); *ppos = k.take<int32_t>(4 * (size_t)n);
         *pln = k.take<int32_t>(n); *pvf = k.take<uint8_t>(n);
@@ -1271,7 +1359,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
     float *dfeat = nullptr, *dy = nullptr;
     auto dev_layout = [&](char* base) {
         Carve k(base);
-        io_layout(k, &da, &dal, &db, &dbl, &dout, &dpo, &dseq, &dsc, &dpos, &dln, &dvf, &der, &dpk);
+        io_layout(k, &da, &dal, &db, &dbl, &dout, &dpo, &dsa, &dsb, &dseq, &dsc, &dpos, &dln, &dvf, &der, &dpk);
         dcg = k.take<char>(cig + 1);
         dpure = k.take<uint8_t>(2 * (size_t)n);
         if (route) {
@@ -1285,17 +1373,19 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         dctr = k.take<int32_t>(8, 4);
         dedge = k.take<int32_t>((size_t)S.max_slots * P.edge_slot);
         ddirs = (S.dir_words > 0) ? k.take<uint32_t>((size_t)S.dir_words) : nullptr;
+        dspan_a = k.take<uint8_t>((size_t)span_a);
+        dspan_b = k.take<uint8_t>((size_t)span_b);
         return k.off;
     };
     {
         Carve hk(nullptr);
-        io_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
+        io_layout(hk, &ha, &hal, &hb, &hbl, &ho, &hpo, &hsa, &hsb, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
         if (!ensure_host(c, hk.off)) { *err = E_HOSTMEM; return GA_DEVICE_ERROR; }
     }
     if (fail_here(1) || !ensure_dev(c, dev_layout(nullptr))) { *err = E_ALLOC; return GA_DEVICE_ERROR; }
     {
         Carve k(c->host);
-        io_layout(k, &ha, &hal, &hb, &hbl, &ho, &hpo, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
+        io_layout(k, &ha, &hal, &hb, &hbl, &ho, &hpo, &hsa, &hsb, &hseq, &hsc, &hpos, &hln, &hvf, &her, &hpk);
     }
     dev_layout(c->dev);
     parallel_for(n, 2048, [&](int64_t lo, int64_t hi) {
@@ -1304,19 +1394,29 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
             ha[i] = a_off[i]; hal[i] = r.text_len;
             hb[i] = b_off[i]; hbl[i] = r.pattern_len;
             ho[i] = out_off[i]; hpo[i] = pk_off[i];
-            if ((own[i] & 1) && r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
-            if ((own[i] & 2) && r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
+            if (span) {
+                hsa[i] = (own[i] & 1) && r.text_len > 0 ? (int64_t)((uintptr_t)r.text - spa.first) : -1;
+                hsb[i] = (own[i] & 2) && r.pattern_len > 0 ? (int64_t)((uintptr_t)r.pattern - spb.first) : -1;
+            } else {
+                if ((own[i] & 1) && r.text_len) std::memcpy(hseq + a_off[i], r.text, (size_t)r.text_len);
+                if ((own[i] & 2) && r.pattern_len) std::memcpy(hseq + b_off[i], r.pattern, (size_t)r.pattern_len);
+            }
         }
     });
-    std::memset(hseq + arena - 64, 0, 64);
-    const size_t in_bytes = (size_t)((char*)(hseq + arena) - c->host);     // descriptors + arena, contiguous
-    *h2d = (int64_t)in_bytes;
+    if (!span) std::memset(hseq + arena - 64, 0, 64);
+    // descriptors (+ the arena when staged here), contiguous; the spans from the caller's memory
+    const size_t in_bytes = (size_t)((char*)(span ? hseq : hseq + arena) - c->host);
+    *h2d = (int64_t)in_bytes + span_a + span_b;
     PairDesc D;
     D.packed = nullptr;
     D.n = n;
     D.seq = dseq; D.pure = dpure;
     D.a_off = da; D.a_len = dal; D.b_off = db; D.b_len = dbl; D.out_off = dout;
-    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+    if (fail_here(2) || cudaMemcpyAsync(c->dev, c->host, in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+        (span_a > 0 && cudaMemcpyAsync(dspan_a, (const void*)spa.first, (size_t)span_a, cudaMemcpyHostToDevice,
+                                       c->stream) != cudaSuccess) ||
+        (span_b > 0 && cudaMemcpyAsync(dspan_b, (const void*)spb.first, (size_t)span_b, cudaMemcpyHostToDevice,
+                                       c->stream) != cudaSuccess)) {
         cudaGetLastError();
         *err = E_H2D;
         return GA_DEVICE_ERROR;
@@ -1331,6 +1431,8 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         if (e == cudaSuccess) e = cudaMemsetAsync(dln, 0, sizeof(int32_t) * (size_t)n, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(der, 0, sizeof(int32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(dctr, 0, sizeof(int32_t) * 8, st);
+        if (e == cudaSuccess && span) e = launch_gather_sides(D, dseq, dspan_a, dspan_b, dsa, dsb, st);
+        if (e == cudaSuccess && span) e = cudaMemsetAsync(dseq + arena - 64, 0, 64, st);
         if (e == cudaSuccess) e = launch_pack(D, arena, nullptr, dpure, st);
         if (e == cudaSuccess && route) e = launch_sw_route(D, s0.match, s0.gap_open, dfeat, dy, dtry, st);
         if (e == cudaSuccess)
@@ -1350,7 +1452,7 @@ static int32_t sw_batch_range(const ga_sw_request* reqs, int32_t n, int64_t base
         } else {
             const std::vector<uint64_t> key = {
                 c->dev_gen, (uint64_t)n, (uint64_t)arena, (uint64_t)cig, (uint64_t)pkb,
-                (uint64_t)trace | (uint64_t)route << 1,
+                (uint64_t)trace | (uint64_t)route << 1 | (uint64_t)span << 2, (uint64_t)span_a, (uint64_t)span_b,
                 (uint64_t)cell_limit,
                 (uint64_t)(uint32_t)s0.match | (uint64_t)(uint32_t)s0.mismatch << 32,
                 (uint64_t)(uint32_t)s0.gap_open | (uint64_t)(uint32_t)s0.gap_extend << 32,

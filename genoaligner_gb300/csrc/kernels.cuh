@@ -95,6 +95,12 @@ struct RoutedArgs {
 cudaError_t launch_pack(const PairDesc& D, int64_t seq_bytes, uint64_t* packed, uint8_t* pure, cudaStream_t st);
 int64_t packed_arena_words(int64_t seq_bytes);
 cudaError_t launch_pack_arena(const uint8_t* seq, int64_t seq_bytes, uint64_t* packed, uint32_t* bad, cudaStream_t st);
+// Sequences copied to the device as the caller laid them out -- one span per
+// side, the sides' bytes in request order -- moved into the staging arena: pair
+// p's side a from span_a + src_a[p] to seq + a_off[p] (a_len bytes) where
+// src_a[p] >= 0, side b likewise; seq is D.seq, writable (wfa.cu).
+cudaError_t launch_gather_sides(const PairDesc& D, uint8_t* seq, const uint8_t* span_a, const uint8_t* span_b,
+                                const int64_t* src_a, const int64_t* src_b, cudaStream_t st);
 // Each pair's CIGAR (end of its slot) packed 2 bits per op at pk + pk_off[p] (wfa.cu).
 cudaError_t launch_cigar_pack(const PairDesc& D, const int32_t* len, const char* cig, const int64_t* pk_off,
                               uint8_t* pk, cudaStream_t st);

@@ -386,6 +386,38 @@ __global__ void cigar_pack_kernel(PairDesc D, const int32_t* __restrict__ len, c
     }
 }
 
+// A warp per pair, each side's bytes copied 32 at a time (one sector read and
+// written per step; the destination is 32-byte aligned).
+__global__ void gather_sides_kernel(PairDesc D, uint8_t* __restrict__ seq, const uint8_t* __restrict__ span_a,
+                                    const uint8_t* __restrict__ span_b, const int64_t* __restrict__ src_a,
+                                    const int64_t* __restrict__ src_b)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < D.n; p += nw) {
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int64_t src = side ? src_b[p] : src_a[p];
+            if (src < 0) continue;
+            const int len = side ? D.b_len[p] : D.a_len[p];
+            const uint8_t* s = (side ? span_b : span_a) + src;
+            uint8_t* d = seq + (side ? D.b_off[p] : D.a_off[p]);
+            for (int k = lane; k < len; k += 32) d[k] = s[k];
+        }
+    }
+}
+
+cudaError_t launch_gather_sides(const PairDesc& D, uint8_t* seq, const uint8_t* span_a, const uint8_t* span_b,
+                                const int64_t* src_a, const int64_t* src_b, cudaStream_t st)
+{
+    if (D.n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>(((int64_t)D.n + 3) / 4, (int64_t)device_sms() * 16);   // a warp per pair
+    launch_begin(K_PACK, st);
+    gather_sides_kernel<<<blocks, 128, 0, st>>>(D, seq, span_a, span_b, src_a, src_b);
+    launch_end(K_PACK, st);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_cigar_pack(const PairDesc& D, const int32_t* len, const char* cig, const int64_t* pk_off,
                               uint8_t* pk, cudaStream_t st)
 {
