@@ -989,6 +989,51 @@ __device__ void ck_item(const Sw16Args& A, const int32_t* __restrict__ pwork, in
                 --pos;
                 if (t == 0) slotc[pos] = op;
             }
+            // Diagonal shortcut.  Standing in H on a checkpoint row (where the
+            // walk leaves a window at its top): if the straight diagonal up to
+            // the next checkpoint row (or to row or column 0, where H is 0)
+            // scores exactly the current value, it is the walk's own path.  H
+            // at each cell is at least its diagonal predecessor's plus the
+            // step's score, so along such a diagonal every predecessor holds
+            // exactly the partial sum, each step is diagonal (the diagonal wins
+            // ties) and no window is needed for it.  Taken while every cell it
+            // steps from stays above 0 (a 0 ends the walk: the window path
+            // finds it).  (Hops that also end on column edges measured no
+            // faster on the 200,000-pair batch.)
+            while (!fin && state == 0 && v > 0 && i >= 1 && j >= 1 && (i & (CK_K - 1)) == 0) {
+                const int L = min(min(CK_K, i), j);                     // steps (at most 64)
+                if (L > pos) break;
+                const int ie = i - L, je = j - L;                            // the end cell
+                const int he = (ie == 0 || je == 0)
+                                   ? 0 : half(ck[2 * ((int64_t)(ie / CK_K - 1) * ncol + (je - 1))]) + go;
+                bool e0 = false, e1 = false;
+                int p0 = 0, p1 = 0;                                          // step t, step t + 32: its score
+                if (t < L) {
+                    e0 = __ldg(text + i - 1 - t) == __ldg(pat + j - 1 - t);
+                    p0 = e0 ? A.match : A.mismatch;
+                }
+                if (t + 32 < L) {
+                    e1 = __ldg(text + i - 33 - t) == __ldg(pat + j - 33 - t);
+                    p1 = e1 ? A.match : A.mismatch;
+                }
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {                          // inclusive prefix sums
+                    const int y0 = __shfl_up_sync(FULL, p0, o), y1 = __shfl_up_sync(FULL, p1, o);
+                    if (t >= o) { p0 += y0; p1 += y1; }
+                }
+                p1 += __shfl_sync(FULL, p0, 31);
+                const int total = __shfl_sync(FULL, p1, 31);
+                // the cell after step u holds v - prefix(u); all before the end cell must stay above 0
+                const bool low = (t < L - 1 && v - p0 <= 0) || (t + 32 < L - 1 && v - p1 <= 0);
+                if (v - total != he || __any_sync(FULL, low)) break;
+                if (t < L) slotc[pos - 1 - t] = e0 ? 'M' : 'X';
+                if (t + 32 < L) slotc[pos - 33 - t] = e1 ? 'M' : 'X';
+                pos -= L;
+                i = ie;
+                j = je;
+                v = he;
+                if (i <= 0 || j <= 0 || v == 0) fin = true;
+            }
             wi[x] = i; wj[x] = j; wst[x] = state; wv[x] = v; wpos[x] = pos;
             if (fin) {
                 done[x] = true;
