@@ -50,7 +50,7 @@ OPS_PER_CELL = 6
 # DRAM bytes per cell of the two-pairs-per-warp trace kernel, from
 # profiles/sw16ck_trace_sw_uneven.md (ncu, 20,000-pair sample of the same
 # batch: read + write bytes / cells; traffic grows with the cells processed)
-SW16CK_DRAM_BYTES_PER_CELL = 0.2576
+SW16CK_DRAM_BYTES_PER_CELL = 0.2348
 SW_WORKLOAD = ("sw_uneven_200k: 200,000 pairs, query log-uniform 50-1,000 bp, target = query at 5% "
                "(sub/ins/del 60/20/20) between U{0..500} flanks, scoring {2,-3,3,1}, score+end+start+CIGAR")
 
