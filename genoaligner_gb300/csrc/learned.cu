@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(512) route_model_kernel(const __nv_bfloat16* _
                     const int cnt = min(16, L - 2 - q);
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
-                        if (i < cnt) atomicAdd(&H[(int)((v >> (2 * i)) & 63u) * 32], 1);   // no return: no wait
+                        if (i < cnt) ++H[(int)((v >> (2 * i)) & 63u) * 32];   // the lane's own column: no atomic
                 }
             }
         }
