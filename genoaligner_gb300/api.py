@@ -65,14 +65,16 @@ class SwScoringC(ctypes.Structure):
 class TuneC(ctypes.Structure):
     _fields_ = [("sw_pack16", ctypes.c_int32), ("sw_window", ctypes.c_int32),
                 ("sw_long_log2", ctypes.c_int32), ("wfa_lane_smax", ctypes.c_int32),
-                ("sw_coop_log2", ctypes.c_int32), ("sw_opt16_pct", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("sw_coop_log2", ctypes.c_int32), ("sw_opt16_pct", ctypes.c_int32), ("wfa_group", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 1)]
 
 
 class TuneTrialC(ctypes.Structure):
     _fields_ = [("tune", TuneC), ("ms", ctypes.c_double)]
 
 
-TUNE_FIELDS = ("sw_pack16", "sw_window", "sw_long_log2", "wfa_lane_smax", "sw_coop_log2", "sw_opt16_pct")
+TUNE_FIELDS = ("sw_pack16", "sw_window", "sw_long_log2", "wfa_lane_smax", "sw_coop_log2", "sw_opt16_pct",
+               "wfa_group")
 
 
 class DeviceBatch(ctypes.Structure):

@@ -583,18 +583,21 @@ struct WfaScratch {
     int lane_slots = 0;              // learned: warp slots of the lane kernel
     int64_t stack_slot = 0;
     int warp_smem = 0;
+    int group = 32;                  // learned: lanes per warp-queue pair
     int64_t seq_bytes = 0;
     int chunk = 1;
 };
 
-static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, int sm_count)
+// group: the tuned lanes per warp-queue pair (ga_tune.wfa_group).
+static void size_wfa(WfaScratch& S, int n, int smax, bool trace, bool learned, int sm_count, int group)
 {
     if (learned) {
         prepare_mlp();
-        S.slots = (int)std::min<int64_t>(routed_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
+        S.group = routed_group(smax, group);
+        S.slots = (int)std::min<int64_t>(routed_max_slots(smax, trace, sm_count, S.group), ((int64_t)n + 3) / 4 * 4);
         S.lane_slots = (int)std::min<int64_t>(lane_max_slots(trace, sm_count), ((int64_t)n + 127) / 128 * 4);
-        S.stack_slot = routed_stack_slot(smax);
-        S.warp_smem = routed_warp_smem(smax);
+        S.stack_slot = routed_stack_slot(smax, S.group);
+        S.warp_smem = routed_warp_smem(smax, S.group);
     } else {
         S.slots = (int)std::min<int64_t>(wfa_max_slots(smax, trace, sm_count), ((int64_t)n + 3) / 4 * 4);
         S.stack_slot = (int64_t)(smax + 1) * (smax + 1);
@@ -655,6 +658,7 @@ static cudaError_t enqueue_wfa(const WfaScratch& S, PairDesc D, int smax, bool t
     RoutedArgs R;
     R.A = A;
     R.warp_smem = S.warp_smem;
+    R.group = S.group;
     R.big = S.big;
     R.big_count = S.counts + 2 * NB;
     R.big_next = S.ctr;
@@ -709,7 +713,8 @@ static cudaError_t run_wfa_graph(Ctx* c, const WfaScratch& S, const PairDesc& D,
                                  int lane_smax, int32_t* score, int32_t* len, char* cig, int32_t* err, cudaStream_t st)
 {
     const std::vector<uint64_t> key = {c->dev_gen, (uint64_t)D.n, (uint64_t)(uintptr_t)D.seq, (uint64_t)smax,
-                                       (uint64_t)trace | (uint64_t)lane_smax << 8 | (uint64_t)route << 16,
+                                       (uint64_t)trace | (uint64_t)lane_smax << 8 | (uint64_t)route << 16 |
+                                           (uint64_t)S.group << 24,
                                        (uint64_t)(uintptr_t)score, (uint64_t)(uintptr_t)cig,
                                        (uint64_t)(uintptr_t)D.a_off, (uint64_t)(uintptr_t)S.packed};
     return replay_graph(c->gexec, c->gkey, key, c->glaunches, st, [&]() {
@@ -831,7 +836,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     base[3 * nch] = arena; base[3 * nch + 1] = cig; base[3 * nch + 2] = pkb;
     route = route_mode(route);
     const bool learned = route != 0;
-    const int lane_smax = tune_current().wfa_lane_smax;
+    const ga_tune tuned = tune_current();
+    const int lane_smax = tuned.wfa_lane_smax;
 
     // one range: requests of chunks [kc[k], kc[k + 1]), offsets from the range's own bases
     std::vector<int64_t> rh2d((size_t)K, 0), rd2h((size_t)K, 0);
@@ -856,7 +862,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         if (!c) return GA_DEVICE_ERROR;
         struct Guard { Ctx* c; ~Guard() { release_ctx(c); } } guard{c};
         WfaScratch S;
-        size_wfa(S, nk, smax, trace, learned, c->sm_count);
+        size_wfa(S, nk, smax, trace, learned, c->sm_count, tuned.wfa_group);
         // layout: [a_off a_len b_off b_len out_off pk_off (src_a src_b) | seq] in, [score len checks err |
         // packed CIGARs] back, then (device) the CIGAR slots, the scratch and the caller's spans
         int64_t *ha, *hb, *ho, *hpo, *da, *db, *dout, *dpo, *hsa, *hsb, *dsa, *dsb;
@@ -1891,8 +1897,9 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
     Ctx* c = acquire_ctx(&e);
     if (!c) { if (err) *err = e; return GA_DEVICE_ERROR; }
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const ga_tune tuned = tune_current();
     WfaScratch S;
-    size_wfa(S, b->n, smax, trace != 0, learned, c->sm_count);
+    size_wfa(S, b->n, smax, trace != 0, learned, c->sm_count, tuned.wfa_group);
     Carve k(nullptr);
     carve_wfa(k, S, b->n, b->seq_bytes, trace != 0, learned);
     k.take<int32_t>(1, 4);                                           // error word
@@ -1907,7 +1914,7 @@ int32_t ga_wfa_device_ex(const ga_device_batch* b, int32_t smax, int32_t trace, 
     int32_t rc = GA_OK;
     cudaError_t le = cudaMemsetAsync(derr, 0, sizeof(int32_t), st);
     if (le == cudaSuccess) {
-        const int lane_smax = tune_current().wfa_lane_smax;
+        const int lane_smax = tuned.wfa_lane_smax;
         if (learned && !profiling_on())
             le = run_wfa_graph(c, S, D, smax, trace != 0, route, lane_smax, out_score, out_len, out_cigar, derr, st);
         else le = enqueue_wfa(S, D, smax, trace != 0, route, lane_smax, out_score, out_len, out_cigar, derr, st);

@@ -88,6 +88,7 @@ struct RoutedArgs {
     int32_t* block_next;
     uint16_t* lane_rec;          // lane kernel: per warp slot, lane_rec_slot() walk records (trace only)
     int32_t warp_smem;           // warp kernel: shared-memory ints per warp
+    int32_t group;               // warp kernel: lanes per warp-queue pair (8, 16 or 32; routed_group)
 };
 
 // Packs seq into the 2-bit arena `packed` (packed_arena_words(seq_bytes)
@@ -118,10 +119,12 @@ void prepare_mlp();
 cudaError_t launch_sw_route(const PairDesc& D, int match, int go, float* feat, float* y, uint8_t* try16,
                             cudaStream_t st);
 int route_buckets();
-int64_t routed_stack_slot(int smax);
+// Warp-queue lanes per pair for a batch smax and a tuned group size.
+int routed_group(int smax, int group);
+int64_t routed_stack_slot(int smax, int group);
 int64_t lane_rec_slot();
-int routed_warp_smem(int smax);
-int routed_max_slots(int smax, bool trace, int sm_count);
+int routed_warp_smem(int smax, int group);
+int routed_max_slots(int smax, bool trace, int sm_count, int group);
 int lane_max_slots(bool trace, int sm_count);
 // Fused sketch + lower bound + cost model + queue choice (learned.cu); then
 // the queues from the per-pair items (wfa_routed.cu).

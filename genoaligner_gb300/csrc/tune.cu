@@ -4,8 +4,9 @@
 // A setting (ga_tune) chooses how work is laid onto the GPU -- 16-bit pairs
 // two per warp (inter-sequence) or one per warp in 32 bits (intra-sequence),
 // the traceback window's tile count and so its lanes and columns per tile, the
-// cell count where 32-bit pairs switch to the long tile shape, and which
-// learned-WFA pairs run one per lane -- and never what is computed: every
+// cell count where 32-bit pairs switch to the long tile shape, which
+// learned-WFA pairs run one per lane and how many lanes the others get -- and
+// never what is computed: every
 // kernel variant gives the same results.  The search is coordinate-wise: one
 // field at a time over its candidates, the others held at the best so far,
 // each candidate timed end to end through the public device entry (one
@@ -42,6 +43,7 @@ static ga_tune builtin()
     t.wfa_lane_smax = LANE_SMAX;
     t.sw_coop_log2 = C32_COOP_LOG2;
     t.sw_opt16_pct = 100;
+    t.wfa_group = 16;
     return t;
 }
 
@@ -49,14 +51,15 @@ static bool valid(const ga_tune& t)
 {
     return (t.sw_pack16 == 0 || t.sw_pack16 == 1) && (t.sw_window == 2 || t.sw_window == 4) &&
            t.sw_long_log2 >= 16 && t.sw_long_log2 <= 30 && t.wfa_lane_smax >= 0 && t.wfa_lane_smax <= LANE_SMAX &&
-           t.sw_coop_log2 >= 16 && t.sw_coop_log2 <= 40 && t.sw_opt16_pct >= 50 && t.sw_opt16_pct <= 100;
+           t.sw_coop_log2 >= 16 && t.sw_coop_log2 <= 40 && t.sw_opt16_pct >= 50 && t.sw_opt16_pct <= 100 &&
+           (t.wfa_group == 8 || t.wfa_group == 16 || t.wfa_group == 32);
 }
 
 static bool same(const ga_tune& a, const ga_tune& b)
 {
     return a.sw_pack16 == b.sw_pack16 && a.sw_window == b.sw_window && a.sw_long_log2 == b.sw_long_log2 &&
            a.wfa_lane_smax == b.wfa_lane_smax && a.sw_coop_log2 == b.sw_coop_log2 &&
-           a.sw_opt16_pct == b.sw_opt16_pct;
+           a.sw_opt16_pct == b.sw_opt16_pct && a.wfa_group == b.wfa_group;
 }
 
 static int current_device()
@@ -279,7 +282,8 @@ int32_t ga_autotune_wfa(const ga_device_batch* batch, int32_t smax, int32_t trac
     };
     Search S;
     S.best = tune_current();
-    const int32_t rc = sweep(S, &ga_tune::wfa_lane_smax, {0, 8, 15, 23, LANE_SMAX}, reps, run, err);
+    int32_t rc = sweep(S, &ga_tune::wfa_lane_smax, {0, 8, 15, 23, LANE_SMAX}, reps, run, err);
+    if (rc == GA_OK && routed_group(smax, 8) == 8) rc = sweep(S, &ga_tune::wfa_group, {32, 16, 8}, reps, run, err);
     if (rc != GA_OK) return rc;
     store(dev, S.best);
     report(S, chosen, trials, max_trials, n_trials);
@@ -297,16 +301,17 @@ int32_t ga_tune_save(const char* path)
     }
     FILE* f = std::fopen(path, "w");
     if (!f) return GA_INVALID_ARGUMENT;
-    std::fprintf(f, "# genoaligner_gb300 tune v3: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax "
-                    "sw_coop_log2 sw_opt16_pct\n");
+    std::fprintf(f, "# genoaligner_gb300 tune v4: device name <TAB> sw_pack16 sw_window sw_long_log2 wfa_lane_smax "
+                    "sw_coop_log2 sw_opt16_pct wfa_group\n");
     for (const auto& r : rows) {
         cudaDeviceProp p;
         if (cudaGetDeviceProperties(&p, r.first) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
-        std::fprintf(f, "%s\t%d %d %d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window,
-                     r.second.sw_long_log2, r.second.wfa_lane_smax, r.second.sw_coop_log2, r.second.sw_opt16_pct);
+        std::fprintf(f, "%s\t%d %d %d %d %d %d %d\n", p.name, r.second.sw_pack16, r.second.sw_window,
+                     r.second.sw_long_log2, r.second.wfa_lane_smax, r.second.sw_coop_log2, r.second.sw_opt16_pct,
+                     r.second.wfa_group);
     }
     return std::fclose(f) == 0 ? GA_OK : GA_INVALID_ARGUMENT;
 }
@@ -323,8 +328,12 @@ int32_t ga_tune_load(const char* path)
         if (line[0] == '#' || line[0] == '\n') continue;
         char* tab = std::strchr(line, '\t');
         ga_tune t = builtin();
-        if (!tab || std::sscanf(tab + 1, "%d %d %d %d %d %d", &t.sw_pack16, &t.sw_window, &t.sw_long_log2,
-                                &t.wfa_lane_smax, &t.sw_coop_log2, &t.sw_opt16_pct) != 6 || !valid(t)) {
+        // six fields (files written before wfa_group existed: the built-in group) or seven
+        const int got = tab ? std::sscanf(tab + 1, "%d %d %d %d %d %d %d", &t.sw_pack16, &t.sw_window,
+                                          &t.sw_long_log2, &t.wfa_lane_smax, &t.sw_coop_log2, &t.sw_opt16_pct,
+                                          &t.wfa_group)
+                            : 0;
+        if ((got != 6 && got != 7) || !valid(t)) {
             ok = false;
             break;
         }

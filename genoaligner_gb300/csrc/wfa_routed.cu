@@ -1,6 +1,6 @@
-// wfa_routed.cu -- the learned-bucketed WFA path: routing and a persistent
-// kernel over two bucketed queues, one served by whole warps, one by single
-// lanes.
+// wfa_routed.cu -- the learned-bucketed WFA path: routing and two persistent
+// kernels over two bucketed queues, one served by single lanes, one by
+// groups of lanes, warps or whole blocks.
 //
 // Same recurrence and walk as wfa.cu (the reference's wfa_trace_kernel,
 // include/genoaligner/backend/wfa_kernel.hip:119-145, 338-437); what changes is
@@ -14,14 +14,19 @@
 //     pure-ACGT pair of at most LANE_MAXLEN bases a side whose first smax is
 //     <= LANE_SMAX goes to the lane queue: one pair per lane, 32 pairs per
 //     warp in lockstep over (s, k), sequences and wavefront staged in shared
-//     memory.  Every other pair goes to the warp queue (one pair per warp,
-//     lanes over the diagonals of a wavefront);
-//   * the router sorts both queues by first smax, largest first (a counting
-//     sort in three kernels), so the 32 pairs of a lane batch cost alike;
-//   * a pair not resolved within its first smax escalates: it is appended to
-//     an escalation list with smax doubled (capped at the batch smax) and the
-//     next launch of the same kernel takes that list as its warp queue; a
-//     pair still unresolved at the batch smax is final.
+//     memory.  Every other pair goes to the warp queue, with the batch smax:
+//     one pair per group of lanes (8 or 16 lanes, several pairs per warp
+//     stepping through their wavefronts together, at batch smax <= 128; else
+//     one pair per warp), lanes over the diagonals of a wavefront; items
+//     estimated at s >= 256 first on whole blocks;
+//   * the router sorts both queues, largest first -- the lane queue by first
+//     smax, the warp queue by the bit length of the estimate -- with a
+//     counting sort (bucket counts in the route pass, then a scan and a
+//     scatter), so the pairs of a lane batch or of a warp cost alike;
+//   * a lane-queue pair not resolved within its first smax escalates: it is
+//     appended to an escalation list with the batch smax, which the warp
+//     kernel takes after its own queue (it starts again from s = 0); a pair
+//     unresolved at the batch smax is final.
 //
 // Results do not depend on the smax a pair is tried with: wavefront s is the
 // same for every smax >= s, so a pair resolved at any smax >= d returns the
@@ -261,6 +266,60 @@ __device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, i
     }
 }
 
+// The walk of a resolved pair (score >= 0) on the G lanes of its group, from
+// the wavefront stack the forward pass left (stk[s * s + s + k]: wavefront s
+// at diagonal k), written backwards from the end of the pair's CIGAR slot.
+// Every lane of the group runs the same walk; the runs are written by all of
+// them.  Returns the position of the CIGAR's first op in the slot.
+template <int G>
+__device__ int walk_g(const WfaArgs& A, int p, int score, int kfinal, int m, int n, const int32_t* stk, int gl)
+{
+    char* slot = A.out_cigar + A.D.out_off[p];
+    int pos = m + n;
+    if (score == 0) {
+        pos = emit_run_g<G>(slot, pos, n, 'M', gl, A.err);
+    } else {
+        int s = score, k = kfinal;
+        int off = stk[s * s + s + k];
+        int h = off, v = off - k;
+        pos = emit_run_g<G>(slot, pos, v - m, 'D', gl, A.err);
+        pos = emit_run_g<G>(slot, pos, h - n, 'I', gl, A.err);
+        v = min(v, m);
+        h = min(h, n);
+        while (v > 0 && h > 0 && s > 0) {
+            const int sp = s - 1;
+            const int32_t* W = stk + sp * sp + sp;
+            const int c_mis = (k >= -sp && k <= sp) ? W[k] + 1 : WFA_NULL;
+            const int c_ins = (k - 1 >= -sp && k - 1 <= sp) ? W[k - 1] + 1 : WFA_NULL;
+            const int c_del = (k + 1 >= -sp && k + 1 <= sp) ? W[k + 1] : WFA_NULL;
+            int best = WFA_NULL;
+            char op = 0;
+            if (wfa_live(c_mis) && c_mis >= best) { best = c_mis; op = 'X'; }
+            if (wfa_live(c_ins) && c_ins > best)  { best = c_ins; op = 'I'; }
+            if (wfa_live(c_del) && c_del > best)  { best = c_del; op = 'D'; }
+            if (!op) break;
+            pos = emit_run_g<G>(slot, pos, off - best, 'M', gl, A.err);
+            pos = emit_run_g<G>(slot, pos, 1, op, gl, A.err);
+            off = best;
+            if (op == 'X')      { off -= 1; }
+            else if (op == 'I') { k -= 1; off -= 1; }
+            else                { k += 1; }
+            h = off;
+            v = off - k;
+            --s;
+        }
+        if (v > 0 && h > 0) {
+            const int run = min(v, h);
+            pos = emit_run_g<G>(slot, pos, run, 'M', gl, A.err);
+            v -= run;
+            h -= run;
+        }
+        pos = emit_run_g<G>(slot, pos, v, 'D', gl, A.err);
+        pos = emit_run_g<G>(slot, pos, h, 'I', gl, A.err);
+    }
+    return pos;
+}
+
 // One pair on a group of G lanes with the given smax.  Returns the score
 // (-1 when unresolved within smax); writes the outputs only when the pair is
 // resolved or `final`.
@@ -314,50 +373,8 @@ __device__ int wfa_pair_g(const RoutedArgs& R, int p, int smax, bool final, cons
         }
         return score;
     }
-    char* slot = A.out_cigar + A.D.out_off[p];
-    int pos = m + n;
-    if (score == 0) {
-        pos = emit_run_g<G>(slot, pos, n, 'M', gl, A.err);
-    } else {
-        gsync<G>(gmask);
-        int s = score, k = kfinal;
-        int off = stk[s * s + s + k];
-        int h = off, v = off - k;
-        pos = emit_run_g<G>(slot, pos, v - m, 'D', gl, A.err);
-        pos = emit_run_g<G>(slot, pos, h - n, 'I', gl, A.err);
-        v = min(v, m);
-        h = min(h, n);
-        while (v > 0 && h > 0 && s > 0) {
-            const int sp = s - 1;
-            const int32_t* W = stk + sp * sp + sp;
-            const int c_mis = (k >= -sp && k <= sp) ? W[k] + 1 : WFA_NULL;
-            const int c_ins = (k - 1 >= -sp && k - 1 <= sp) ? W[k - 1] + 1 : WFA_NULL;
-            const int c_del = (k + 1 >= -sp && k + 1 <= sp) ? W[k + 1] : WFA_NULL;
-            int best = WFA_NULL;
-            char op = 0;
-            if (wfa_live(c_mis) && c_mis >= best) { best = c_mis; op = 'X'; }
-            if (wfa_live(c_ins) && c_ins > best)  { best = c_ins; op = 'I'; }
-            if (wfa_live(c_del) && c_del > best)  { best = c_del; op = 'D'; }
-            if (!op) break;
-            pos = emit_run_g<G>(slot, pos, off - best, 'M', gl, A.err);
-            pos = emit_run_g<G>(slot, pos, 1, op, gl, A.err);
-            off = best;
-            if (op == 'X')      { off -= 1; }
-            else if (op == 'I') { k -= 1; off -= 1; }
-            else                { k += 1; }
-            h = off;
-            v = off - k;
-            --s;
-        }
-        if (v > 0 && h > 0) {
-            const int run = min(v, h);
-            pos = emit_run_g<G>(slot, pos, run, 'M', gl, A.err);
-            v -= run;
-            h -= run;
-        }
-        pos = emit_run_g<G>(slot, pos, v, 'D', gl, A.err);
-        pos = emit_run_g<G>(slot, pos, h, 'I', gl, A.err);
-    }
+    if (score > 0) gsync<G>(gmask);
+    const int pos = walk_g<G>(A, p, score, n - m, m, n, stk, gl);
     if (gl == 0) {
         A.out_score[p] = score;
         A.out_len[p] = m + n - pos;
@@ -397,6 +414,106 @@ __device__ void run_item(const RoutedArgs& R, int2 item, int32_t* wf0, int32_t* 
     }
 }
 
+// Warp-queue items on groups of G lanes (G = 8 or 16), 32 / G pairs per warp:
+// the warp takes 32 / G consecutive items of a list (the lists are sorted by
+// predicted distance, so the pairs of a warp cost alike) and its groups step
+// through s together -- every group at the same s has the same 2s + 1
+// diagonals, so the groups' loops stay converged -- each lane over the
+// diagonals k = gl - s, gl - s + G, ...  A group whose pair resolves idles
+// until the last pair of the warp resolves or reaches the batch smax, then
+// the groups walk their own pairs.  Items of these lists carry the batch smax
+// and are final.  Each group has its own two wavefronts in the warp's shared
+// memory and its own stack of (smax + 1)^2 offsets in the warp's stack slot.
+template <bool TRACE, int G>
+__device__ void group_phase(const RoutedArgs& R, const int2* __restrict__ items, int cnt, int32_t* next, int first,
+                            int32_t* wsm, int32_t* wstk, int lane)
+{
+    constexpr int NG = 32 / G;
+    const WfaArgs& A = R.A;
+    const int grp = lane / G, gl = lane % G;
+    const int smax = A.smax;
+    const int WS = 2 * smax + 3, base = smax + 1;
+    int32_t* const wfa = wsm + grp * 2 * WS;
+    int32_t* const wfb = wfa + WS;
+    int32_t* const stk = TRACE ? wstk + grp * (int64_t)(smax + 1) * (smax + 1) : nullptr;
+    for (;;) {
+        int q0 = 0;
+        if (lane == 0) q0 = atomicAdd(next, NG);
+        q0 = __shfl_sync(FULL, q0, 0) + first;
+        if (q0 >= cnt) break;
+        const int q = q0 + grp;
+        int p = 0, m = 0, n = 0;
+        bool have = q < cnt;
+        if (have) {
+            p = items[q].x;
+            m = A.D.a_len[p];
+            n = A.D.b_len[p];
+            if (m <= 0 || n <= 0) {
+                const int len = m <= 0 ? max(n, 0) : m;
+                if (TRACE) emit_run_g<G>(A.out_cigar + A.D.out_off[p], len, len, m <= 0 ? 'I' : 'D', gl, A.err);
+                if (gl == 0) {
+                    A.out_score[p] = len;
+                    if (A.out_len) A.out_len[p] = TRACE ? len : 0;
+                }
+                have = false;
+            }
+        }
+        // 2-bit codes when both sides are pure ACGT, else bytes
+        const bool packed = have && A.D.pure[p] && A.D.pure[A.D.n + p];
+        const uint64_t* P = nullptr;
+        const uint64_t* T = nullptr;
+        if (have) {
+            P = packed ? A.D.packed + (A.D.a_off[p] >> 5) : reinterpret_cast<const uint64_t*>(A.D.seq + A.D.a_off[p]);
+            T = packed ? A.D.packed + (A.D.b_off[p] >> 5) : reinterpret_cast<const uint64_t*>(A.D.seq + A.D.b_off[p]);
+        }
+        for (int t = gl; t < WS; t += G) { wfa[t] = WFA_NULL; wfb[t] = WFA_NULL; }
+        int off0 = 0;
+        if (have) off0 = packed ? match_run<2>(P, T, 0, 0, m, n) : match_run<8>(P, T, 0, 0, m, n);
+        __syncwarp();
+        if (have && gl == 0) {
+            wfa[base] = off0;
+            if (TRACE) stk[0] = off0;
+        }
+        const int kfinal = n - m;
+        int score = -1;
+        bool act = have && kfinal >= -smax && kfinal <= smax;
+        if (have && kfinal == 0 && off0 >= n) { score = 0; act = false; }
+        int32_t* prev = wfa;
+        int32_t* cur = wfb;
+        for (int s = 1; s <= smax; ++s) {
+            if (!__any_sync(FULL, act)) break;
+            __syncwarp();
+            if (act) {
+                for (int k = gl - s; k <= s; k += G) {
+                    const int ins = prev[base + k - 1];
+                    const int del = prev[base + k + 1];
+                    const int mis = prev[base + k];
+                    int x = max(del, max(ins, mis) + 1);
+                    if (!wfa_live(x) || x > n || x - k > m) x = WFA_NULL;
+                    else x += packed ? match_run<2>(P, T, x - k, x, m, n) : match_run<8>(P, T, x - k, x, m, n);
+                    cur[base + k] = x;
+                    if (TRACE) stk[s * s + s + k] = x;
+                }
+            }
+            __syncwarp();
+            if (act && kfinal >= -s && kfinal <= s) {
+                const int fo = cur[base + kfinal];
+                if (wfa_live(fo) && fo >= n) { score = s; act = false; }
+            }
+            int32_t* t = prev; prev = cur; cur = t;
+        }
+        if (have) {
+            int len = 0;
+            if (TRACE && score >= 0) len = m + n - walk_g<G>(A, p, score, kfinal, m, n, stk, gl);
+            if (gl == 0) {
+                A.out_score[p] = score;
+                if (A.out_len) A.out_len[p] = len;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Lane queue, one pair per lane (persistent, 32 pairs per grab).  Runs
 // before the warp kernel so that its escalations are complete when that
 // kernel reaches them.
@@ -410,10 +527,10 @@ __global__ void __launch_bounds__(128) wfa_lane_kernel(RoutedArgs R)
     lane_phase<TRACE>(R, lsmem + wib * LANE_WARP_SMEM, rec, lane);
 }
 
-// Warp queue, one pair per warp (persistent): the routed pairs largest first,
-// then the lane queue's escalations.  Every item runs with the batch smax and
-// is final.
-template <bool TRACE>
+// Warp queue (persistent): the routed pairs largest first, then the lane
+// queue's escalations, one pair per warp (G = 32) or per group of G lanes.
+// Every item runs with the batch smax and is final.
+template <bool TRACE, int G>
 __global__ void __launch_bounds__(128) wfa_routed_kernel(RoutedArgs R)
 {
     extern __shared__ __align__(16) int32_t rsmem[];
@@ -444,6 +561,11 @@ __global__ void __launch_bounds__(128) wfa_routed_kernel(RoutedArgs R)
         const int cnt = list ? *R.esc_count : *R.big_count;
         int32_t* next = list ? R.esc_next : R.big_next;
         const int first = list ? 0 : nblock;            // (items before it ran on blocks)
+        if constexpr (G < 32) {
+            group_phase<TRACE, G>(R, items, cnt, next, first, wsm, stk, lane);
+            __syncwarp();
+            continue;
+        }
         for (;;) {
             int q = 0;
             if (lane == 0) q = atomicAdd(next, 1) + first;
@@ -501,8 +623,18 @@ __global__ void route_scatter_kernel(int n, const int32_t* __restrict__ item, in
 
 int route_buckets() { return ROUTE_BUCKETS; }
 
-// Stack ints per warp slot of the warp kernel: one pair at the batch smax.
-int64_t routed_stack_slot(int smax) { return (int64_t)(smax + 1) * (smax + 1); }
+// Lanes per warp-queue pair the warp kernel uses: `group` (8, 16 or 32) when
+// the two wavefronts of 32 / group pairs at the batch smax fit a warp's share
+// of shared memory comfortably (smax <= GROUP_SMAX_MAX), else 32.
+constexpr int GROUP_SMAX_MAX = 128;
+int routed_group(int smax, int group)
+{
+    return (group == 8 || group == 16) && smax <= GROUP_SMAX_MAX ? group : 32;
+}
+
+// Stack ints per warp slot of the warp kernel: one pair per group at the batch
+// smax.
+int64_t routed_stack_slot(int smax, int group) { return (int64_t)(32 / group) * (smax + 1) * (smax + 1); }
 
 // 16-bit walk records per warp slot of the lane kernel.
 int64_t lane_rec_slot() { return (int64_t)LANE_STACK * 32; }
@@ -522,9 +654,9 @@ cudaError_t launch_route(int n, const int32_t* item, int32_t* counts, int32_t* s
     return cudaGetLastError();
 }
 
-// Shared-memory ints per warp of the warp kernel (a multiple of 4, so every
-// warp's area is 16-byte aligned).
-int routed_warp_smem(int smax) { return (2 * (2 * smax + 3) + 3) / 4 * 4; }
+// Shared-memory ints per warp of the warp kernel: two wavefronts per group (a
+// multiple of 4, so every warp's area is 16-byte aligned).
+int routed_warp_smem(int smax, int group) { return ((32 / group) * 2 * (2 * smax + 3) + 3) / 4 * 4; }
 
 template <typename K>
 static int per_sm_for(K kernel, size_t smem)
@@ -532,10 +664,18 @@ static int per_sm_for(K kernel, size_t smem)
     return blocks_per_sm((const void*)kernel, 128, smem);
 }
 
-int routed_max_slots(int smax, bool trace, int sm_count)
+template <bool TRACE>
+static const void* routed_kernel(int group)
 {
-    const size_t smem = (size_t)4 * routed_warp_smem(smax) * sizeof(int32_t);
-    const int per_sm = trace ? per_sm_for(wfa_routed_kernel<true>, smem) : per_sm_for(wfa_routed_kernel<false>, smem);
+    if (group == 8) return (const void*)wfa_routed_kernel<TRACE, 8>;
+    if (group == 16) return (const void*)wfa_routed_kernel<TRACE, 16>;
+    return (const void*)wfa_routed_kernel<TRACE, 32>;
+}
+
+int routed_max_slots(int smax, bool trace, int sm_count, int group)
+{
+    const size_t smem = (size_t)4 * routed_warp_smem(smax, group) * sizeof(int32_t);
+    const int per_sm = blocks_per_sm(trace ? routed_kernel<true>(group) : routed_kernel<false>(group), 128, smem);
     return per_sm * sm_count * 4;
 }
 
@@ -554,9 +694,18 @@ cudaError_t launch_routed(const RoutedArgs& R, int lane_slots, int slots, cudaSt
     else wfa_lane_kernel<false><<<(lane_slots + 3) / 4, 128, lsm, st>>>(R);
     launch_end(K_WFA_LANE, st);
     const size_t smem = (size_t)4 * R.warp_smem * sizeof(int32_t);
+    const int blocks = (slots + 3) / 4;
     launch_begin(K_WFA_ROUTED, st);
-    if (R.A.trace) wfa_routed_kernel<true><<<(slots + 3) / 4, 128, smem, st>>>(R);
-    else wfa_routed_kernel<false><<<(slots + 3) / 4, 128, smem, st>>>(R);
+    if (R.group == 8) {
+        if (R.A.trace) wfa_routed_kernel<true, 8><<<blocks, 128, smem, st>>>(R);
+        else wfa_routed_kernel<false, 8><<<blocks, 128, smem, st>>>(R);
+    } else if (R.group == 16) {
+        if (R.A.trace) wfa_routed_kernel<true, 16><<<blocks, 128, smem, st>>>(R);
+        else wfa_routed_kernel<false, 16><<<blocks, 128, smem, st>>>(R);
+    } else {
+        if (R.A.trace) wfa_routed_kernel<true, 32><<<blocks, 128, smem, st>>>(R);
+        else wfa_routed_kernel<false, 32><<<blocks, 128, smem, st>>>(R);
+    }
     launch_end(K_WFA_ROUTED, st);
     return cudaGetLastError();
 }

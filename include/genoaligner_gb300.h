@@ -407,7 +407,10 @@ typedef struct ga_tune {
                                whose best then reaches the 16-bit limit is recomputed in 32 bits
                                (exact either way).  50 .. 100 (100: only pairs whose all-match
                                score fits) */
-    int32_t reserved[2];
+    int32_t wfa_group;      /* learned WFA at batch smax <= 128: lanes per warp-queue pair,
+                               8 or 16 (32 / wfa_group pairs per warp, stepping through the
+                               wavefronts together) or 32 (one pair per warp); larger smax: 32 */
+    int32_t reserved[1];
 } ga_tune;
 
 /* One timed candidate of an autotuning run. */
@@ -439,14 +442,15 @@ int32_t ga_autotune_sw(const ga_device_batch* batch, ga_sw_scoring scoring, int6
 
 /* The same for the learned WFA path (arguments as ga_wfa_device_ex with
  * opt->learned = 1; the cost model must be loaded): candidates for
- * wfa_lane_smax. */
+ * wfa_lane_smax, then (smax <= 128) wfa_group. */
 int32_t ga_autotune_wfa(const ga_device_batch* batch, int32_t smax, int32_t trace,
                         int32_t* out_score, int32_t* out_len, char* out_cigar,
                         int32_t reps, ga_tune* chosen, ga_tune_trial* trials, int32_t max_trials,
                         int32_t* n_trials, const char** err);
 
 /* Write every device's stored setting to a text file (one line per device:
- * name, then the six fields in the order above), or load such a file:
+ * name, then the seven fields in the order above; files with the first six
+ * load with the built-in wfa_group), or load such a file:
  * lines naming the current device's model set its setting.  GA_INVALID_ARGUMENT
  * on an unreadable / malformed file (nothing is changed then). */
 int32_t ga_tune_save(const char* path);

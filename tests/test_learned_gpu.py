@@ -152,3 +152,49 @@ def test_learned_whole_block_items_match_oracle():
     plain = api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=2048,
                                    with_cigar=True, max_smax=4096, learned=False)
     assert np.array_equal(plain.res["score"], got.res["score"])
+
+
+@pytest.mark.parametrize("group", [8, 16, 32])
+def test_warp_queue_group_sizes_match_oracle(group):
+    """The warp queue's pairs on groups of 8 or 16 lanes (several pairs per
+    warp, stepping through the wavefronts together) or on whole warps: pairs
+    with bytes outside ACGT (byte compare), empty sides, pairs longer than the
+    lane queue takes, unresolved pairs and the mixed batch's divergent ones,
+    every field against the oracle."""
+    assert cost_model.load_default()
+    before = api.tune_get()
+    ps = workloads.wfa_mixed(n=4000, seed=74)
+    pats, txts = ps.lists()
+    rng = np.random.default_rng(75)
+    bases = np.frombuffer(b"ACGT", np.uint8)
+    for k in range(0, 200, 5):                        # an N or a lower-case base in one side
+        b = bytearray(txts[k])
+        b[int(rng.integers(0, len(b)))] = ord("N") if k % 2 else ord("a")
+        txts[k] = bytes(b)
+    pats[200], txts[200] = b"", b"ACGTACGT"
+    pats[201], txts[201] = b"ACGTA", b""
+    pats[202], txts[202] = b"", b""
+    for k in range(210, 260):                         # 300-600 bases, 5-12 % point changes
+        L = int(rng.integers(300, 601))
+        s = bases[rng.integers(0, 4, L)].tobytes()
+        t = bytearray(s)
+        for i in rng.choice(L, size=int(L * rng.uniform(0.05, 0.12)), replace=False):
+            t[i] = bases[(bases.tolist().index(t[i]) + 1 + int(rng.integers(0, 3))) % 4]
+        pats[k], txts[k] = s, bytes(t)
+    for k in range(260, 280):                         # unrelated: unresolved at smax 64
+        pats[k] = bases[rng.integers(0, 4, 180)].tobytes()
+        txts[k] = bases[rng.integers(0, 4, 200)].tobytes()
+    ps = workloads.from_lists("wfa_group_cases", pats, txts)
+    want = oracle.wfa_batch(pats, txts, smax=64, with_cigar=True)
+    assert (want.score < 0).sum() >= 20 and (want.score > 30).sum() >= 50
+    try:
+        for lane in (0, 31):
+            api.tune_set(wfa_lane_smax=lane, wfa_group=group)
+            got = api.align_batch_packed(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len, smax=64,
+                                         with_cigar=True, learned=True)
+            assert got.status == api.Status.ok
+            assert np.array_equal(got.res["score"], want.score), (group, lane)
+            assert all(got.cigar(i) == want.cigars[i] for i in range(ps.n)), (group, lane)
+            assert np.array_equal(got.res["rescore_ok"].astype(bool), want.rescore_ok), (group, lane)
+    finally:
+        api.tune_set(**before)

@@ -12,7 +12,7 @@ from genoaligner_gb300 import api
 def test_default_setting_is_valid_and_current_without_a_stored_one():
     d = api.tune_default()
     assert d == {"sw_pack16": 1, "sw_window": 2, "sw_long_log2": 24, "wfa_lane_smax": 31, "sw_coop_log2": 27,
-                 "sw_opt16_pct": 100}
+                 "sw_opt16_pct": 100, "wfa_group": 16}
     if not api.device_available():
         assert api.tune_get() == d
 
@@ -21,7 +21,8 @@ def test_default_setting_is_valid_and_current_without_a_stored_one():
                                          ("sw_long_log2", 15), ("sw_long_log2", 31),
                                          ("wfa_lane_smax", -1), ("wfa_lane_smax", 32),
                                          ("sw_coop_log2", 15), ("sw_coop_log2", 41),
-                                         ("sw_opt16_pct", 49), ("sw_opt16_pct", 101)])
+                                         ("sw_opt16_pct", 49), ("sw_opt16_pct", 101),
+                                         ("wfa_group", 4), ("wfa_group", 12), ("wfa_group", 64)])
 def test_out_of_range_settings_are_refused(field, value):
     before = api.tune_get()
     with pytest.raises(ValueError):
@@ -35,7 +36,8 @@ def test_unknown_field_refused():
 
 
 @pytest.mark.parametrize("body", ["GB300\t1 2\n", "GB300 1 2 24 15 27 75\n", "GB300\t1 5 24 15 27 75\n",
-                                  "GB300\tx y z w v u\n", "GB300\t1 2 24 15 27\n", "GB300\t1 2 24 15 27 30\n"])
+                                  "GB300\tx y z w v u\n", "GB300\t1 2 24 15 27\n", "GB300\t1 2 24 15 27 30\n",
+                                  "GB300\t1 2 24 15 27 100 12\n"])
 def test_malformed_settings_file_refused(tmp_path, body):
     p = tmp_path / "tune.txt"
     p.write_text("# comment\n" + body)

@@ -108,8 +108,8 @@ def test_every_wfa_lane_setting_gives_the_same_results(restore_tune):
     ps = workloads.wfa_mixed(n=20_000, seed=73)
     b = api.DeviceBatchT(ps.a_buf, ps.a_off, ps.a_len, ps.b_buf, ps.b_off, ps.b_len)
     base = None
-    for lane in (0, 4, 15, 31):
-        api.tune_set(wfa_lane_smax=lane)
+    for lane, group in ((0, 32), (0, 16), (0, 8), (4, 8), (15, 16), (31, 32), (31, 8)):
+        api.tune_set(wfa_lane_smax=lane, wfa_group=group)
         sc = torch.full((b.n,), -7, dtype=torch.int32, device="cuda")
         ln = torch.zeros(b.n, dtype=torch.int32, device="cuda")
         cg = torch.zeros(b.out_bytes, dtype=torch.uint8, device="cuda")
@@ -124,23 +124,24 @@ def test_every_wfa_lane_setting_gives_the_same_results(restore_tune):
             base = res
         else:
             for x, y in zip(base, res):
-                assert np.array_equal(x, y), lane
+                assert np.array_equal(x, y), (lane, group)
     sc = torch.full((b.n,), -7, dtype=torch.int32, device="cuda")
     ln = torch.zeros(b.n, dtype=torch.int32, device="cuda")
     cg = torch.zeros(b.out_bytes, dtype=torch.uint8, device="cuda")
     chosen, trials = api.autotune_wfa(b, 64, True, sc, ln, cg, reps=1)
-    assert api.tune_get() == chosen and len(trials) == 5
+    assert api.tune_get() == chosen and len(trials) == 7      # 5 lane bounds, then the 2 other group sizes
     assert min(trials, key=lambda x: x[1])[0] == chosen
     for x, y in zip(base, _host(torch, (sc, ln, cg))):
         assert np.array_equal(x, y)
 
 
 def test_saved_setting_loads_back(tmp_path, restore_tune):
-    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8, sw_coop_log2=25, sw_opt16_pct=60)
+    api.tune_set(sw_pack16=0, sw_window=4, sw_long_log2=20, wfa_lane_smax=8, sw_coop_log2=25, sw_opt16_pct=60,
+                 wfa_group=16)
     p = tmp_path / "tune.txt"
     api.tune_save(str(p))
     api.tune_set(**api.tune_default())
     api.tune_load(str(p))
     assert api.tune_get() == {"sw_pack16": 0, "sw_window": 4, "sw_long_log2": 20, "wfa_lane_smax": 8,
-                              "sw_coop_log2": 25, "sw_opt16_pct": 60}
+                              "sw_coop_log2": 25, "sw_opt16_pct": 60, "wfa_group": 16}
     assert api.device_name() in p.read_text()
