@@ -39,14 +39,18 @@ namespace ga {
 
 // Lane queue (route.cuh): per warp in shared memory, both sequences of its
 // 32 pairs as 32-bit words of 16 2-bit codes [word][lane] (LANE_WORDS = 16
-// data words + 1 read by the two-word fetch window) and one wavefront
-// [k][lane], updated in place.  The walk reads a 16-bit record per (s, k):
+// data words + 1 read by the two-word fetch window) and one wavefront of
+// 16-bit offsets [k][lane] (offsets are at most LANE_MAXLEN; LANE_NULL marks
+// a dead diagonal), updated in place.  The walk reads a 16-bit record per (s, k):
 // the predecessor (0 mismatch, 1 insertion, 2 deletion) and the extension
 // length, [idx][lane] in the warp's global stack slot.
 constexpr int LANE_WORDS = LANE_MAXLEN / 16 + 1;
 constexpr int LANE_WS = 2 * LANE_SMAX + 3;
 constexpr int LANE_STACK = (LANE_SMAX + 1) * (LANE_SMAX + 1);
-constexpr int LANE_WARP_SMEM = 2 * LANE_WORDS * 32 + LANE_WS * 32;    // ints per warp
+constexpr int LANE_WARP_SMEM = 2 * LANE_WORDS * 32 + LANE_WS * 16;    // ints per warp
+// Dead-diagonal offset of the lane wavefront: below every live offset (>= 0),
+// and NULL + 1 stays negative, so x < 0 is the liveness test.
+constexpr int LANE_NULL = -16384;
 // Hand-over rule: past wavefront LANE_HAND_S, once at most 1/LANE_HAND_DIV of
 // a warp's pairs are still unresolved, they move to the warp queue.
 constexpr int LANE_HAND_S = 6;
@@ -131,7 +135,7 @@ __device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, i
     const WfaArgs& A = R.A;
     const uint32_t* SP = smem + lane;
     const uint32_t* ST = smem + LANE_WORDS * 32 + lane;
-    int32_t* WF = reinterpret_cast<int32_t*>(smem + 2 * LANE_WORDS * 32) + (LANE_SMAX + 1) * 32 + lane;   // WF[k * 32]
+    int16_t* WF = reinterpret_cast<int16_t*>(smem + 2 * LANE_WORDS * 32) + (LANE_SMAX + 1) * 32 + lane;   // WF[k * 32]
     const int nlane = R.small_count ? *R.small_count : 0;
     for (;;) {
         int base = 0;
@@ -171,9 +175,9 @@ __device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, i
         bool act = run;
         if (run) {
             const int off0 = lane_run(SP, ST, 0, 0, m, n);
-            WF[0] = off0;
-            WF[-32] = WFA_NULL;
-            WF[32] = WFA_NULL;
+            WF[0] = (int16_t)off0;
+            WF[-32] = LANE_NULL;
+            WF[32] = LANE_NULL;
             if (TRACE) rec[lane] = (uint16_t)(off0 << 2);
             if (kfinal == 0 && off0 >= n) { score = 0; act = false; }
         }
@@ -191,9 +195,9 @@ __device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, i
                 break;
             }
             if (act) {
-                WF[(s + 1) * 32] = WFA_NULL;
-                WF[-(s + 1) * 32] = WFA_NULL;
-                int carry = WFA_NULL;                            // wavefront s-1 at k-1
+                WF[(s + 1) * 32] = LANE_NULL;
+                WF[-(s + 1) * 32] = LANE_NULL;
+                int carry = LANE_NULL;                           // wavefront s-1 at k-1
                 for (int k = -s; k <= s; ++k) {
                     const int mis = WF[k * 32];
                     const int del = WF[(k + 1) * 32];
@@ -202,14 +206,14 @@ __device__ void lane_phase(const RoutedArgs& R, uint32_t* smem, uint16_t* rec, i
                     if (del > x) { x = del; code = 2; }
                     carry = mis;
                     int ext = 0;
-                    if (!wfa_live(x) || x > n || x - k > m) x = WFA_NULL;
+                    if (x < 0 || x > n || x - k > m) x = LANE_NULL;
                     else { ext = lane_run(SP, ST, x - k, x, m, n); x += ext; }
-                    WF[k * 32] = x;
+                    WF[k * 32] = (int16_t)x;
                     if (TRACE) rec[(s * s + s + k) * 32 + lane] = (uint16_t)(code | (ext << 2));
                 }
                 if (kfinal >= -s && kfinal <= s) {
                     const int fo = WF[kfinal * 32];
-                    if (wfa_live(fo) && fo >= n) { score = s; act = false; }
+                    if (fo >= n) { score = s; act = false; }
                 }
                 if (act && s >= smx) act = false;
             }
