@@ -53,8 +53,8 @@ def test_settings_file_roundtrip_without_device(tmp_path):
     lines = [x for x in p.read_text().splitlines() if not x.startswith("#")]
     if not api.device_available():
         assert lines == []
-    p.write_text("# ok\nSomeOtherGPU\t0 4 20 0 30 80\n")
-    api.tune_load(str(p))                       # names another device: nothing applied
+    p.write_text("# ok\nSomeOtherGPU\t0 4 20 0 30 80\nOtherGPU2\t0 4 20 0 30 80 8\n")
+    api.tune_load(str(p))                       # six or seven fields; other devices: nothing applied
     if not api.device_available():
         assert api.tune_get() == api.tune_default()
 
