@@ -205,7 +205,7 @@ int32_t ga_wfa_device_ex(const ga_device_batch* batch, int32_t smax, int32_t tra
 
 /* Routing record of the calling thread's last learned WFA call: out[0] = pairs
  * in the lane queue (one pair per lane), out[1] = pairs in the warp queue (one
- * pair per warp), out[2] = pairs the lane queue escalated to the warp queue
+ * pair per warp or per group of lanes), out[2] = pairs the lane queue escalated to the warp queue
  * (unresolved within their first smax, or handed over), out[3] = warp-queue
  * pairs run on a whole block (estimated distance >= 256); out[4..] = 0.  A
  * host batch of 262,144 pairs or more runs in up to 4 ranges: the record is
