@@ -129,6 +129,11 @@ thread_local int64_t t_h2d = 0, t_d2h = 0;
 static std::atomic<int> g_fail_next{0};
 
 // ----------------------------------------------------------- thread pool --
+// One job at a time: the calling thread and every worker that wakes while the
+// job is open take chunks of `grain` from a shared counter.  The job closes
+// when the caller runs out of chunks; the caller then waits only for the
+// workers that joined it (a worker that wakes after the close skips the job),
+// so a small job does not wait for all workers to be scheduled.
 class Pool {
 public:
     Pool()
@@ -159,13 +164,15 @@ public:
             n_ = n;
             grain_ = grain;
             next_.store(0);
-            busy_ = (int)threads_.size();
+            open_ = true;
+            joined_ = 0;
             ++gen_;
         }
         cv_.notify_all();
         drain();
         std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&] { return busy_ == 0; });
+        open_ = false;                                      // every chunk is taken
+        done_cv_.wait(lk, [&] { return joined_ == 0; });    // and the joined workers' chunks are done
         fn_ = nullptr;
     }
 
@@ -187,11 +194,13 @@ private:
                 cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
                 if (stop_) return;
                 seen = gen_;
+                if (!open_) continue;                       // woke after the job closed
+                ++joined_;
             }
             drain();
             {
                 std::lock_guard<std::mutex> lk(mu_);
-                if (--busy_ == 0) done_cv_.notify_all();
+                if (--joined_ == 0) done_cv_.notify_all();
             }
         }
     }
@@ -201,7 +210,8 @@ private:
     const std::function<void(int64_t, int64_t)>* fn_ = nullptr;
     int64_t n_ = 0, grain_ = 1;
     std::atomic<int64_t> next_{0};
-    int busy_ = 0;
+    int joined_ = 0;
+    bool open_ = false;
     uint64_t gen_ = 0;
     bool stop_ = false;
 };
@@ -545,6 +555,7 @@ static const char* E_OVERFLOW = "internal error: CIGAR slot overflow";
 static const char* E_SCRATCH = "internal error: traceback memory smaller than the plan needs";
 static const char* E_HOSTMEM = "pinned host allocation failed";
 static const char* E_BADLEN = "internal error: device returned a CIGAR longer than its slot";
+static const char* E_CIGBUF = "cigar buffer is smaller than the batch needs";
 
 // -------------------------------------------------------------------- WFA --
 // The reference's checks of one WFA request (src/api/api.cpp:234-266), in its
@@ -555,11 +566,6 @@ static const char* wfa_request_error(const ga_align_request& r, int32_t max_smax
     if (r.pattern_len < 0 || r.text_len < 0) return E_NEG;
     if (r.smax < 0 || r.smax > max_smax) return max_smax == GA_MAX_SMAX ? E_SMAX : E_SMAX_EX;
     return nullptr;
-}
-
-int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err)
-{
-    return first_failure(n, [&](int64_t i) { return wfa_request_error(reqs[i], max_smax); }, err);
 }
 
 // Device scratch of one WFA batch: the 2-bit arena and purity flags, the
@@ -776,7 +782,7 @@ constexpr int WFA_RANGES = 4;
 constexpr int64_t WFA_RANGE_MIN = 262144;
 
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
-                  const WfaFinish& fin, const char** err)
+                  const WfaFinish& fin, const char** err, int64_t cig_cap)
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
@@ -834,6 +840,10 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         arena += C.arena; cig += C.cig; pkb += C.pkb;
     }
     base[3 * nch] = arena; base[3 * nch + 1] = cig; base[3 * nch + 2] = pkb;
+    if (trace && (cig_cap < 0 || cig > cig_cap)) {
+        *err = E_CIGBUF;
+        return GA_INVALID_ARGUMENT;
+    }
     route = route_mode(route);
     const bool learned = route != 0;
     const ga_tune tuned = tune_current();
@@ -1682,8 +1692,6 @@ static int64_t side_bytes(const R* reqs, int32_t n)
 // ================================================================== C ABI ==
 using namespace ga;
 
-static const char* E_CIGBUF = "cigar buffer is smaller than the batch needs";
-
 extern "C" {
 
 int64_t ga_align_cigar_bytes(const ga_align_request* reqs, int32_t n) { return side_bytes(reqs, n); }
@@ -1710,25 +1718,6 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
     };
     const int32_t max_smax =
         (opt && opt->max_smax > 0) ? std::min<int32_t>(opt->max_smax, GA_MAX_SMAX_DEVICE) : GA_MAX_SMAX;
-    // any CIGAR requested, and the CIGAR bytes the batch needs (ga_align_cigar_bytes), in parallel chunks
-    const int64_t nch = ((int64_t)n + REQ_CHUNK - 1) / REQ_CHUNK;
-    std::vector<int64_t> need((size_t)std::max<int64_t>(nch, 1), 0);
-    std::vector<uint8_t> want((size_t)std::max<int64_t>(nch, 1), 0);
-    parallel_for(nch, 1, [&](int64_t k0, int64_t k1) {
-        for (int64_t k = k0; k < k1; ++k) {
-            int64_t s = 0;
-            bool w = false;
-            for (int64_t i = k * REQ_CHUNK, e = std::min<int64_t>(n, (k + 1) * REQ_CHUNK); i < e; ++i) {
-                s += std::max(0, reqs[i].pattern_len) + (int64_t)std::max(0, reqs[i].text_len);
-                w |= reqs[i].with_cigar != 0;
-            }
-            need[(size_t)k] = s;
-            want[(size_t)k] = w;
-        }
-    });
-    int64_t cig_need = 0;
-    bool any_cigar = false;
-    for (int64_t k = 0; k < nch; ++k) { cig_need += need[(size_t)k]; any_cigar |= want[(size_t)k] != 0; }
     const char* err = nullptr;
     std::atomic<int32_t> resolved{0};
     auto fin = [&](int64_t lo, int64_t hi, const WfaView& v) {
@@ -1759,16 +1748,11 @@ int32_t ga_align_batch_ex(const ga_align_request* reqs, int32_t n, ga_align_resu
         }
         resolved.fetch_add(res);
     };
-    int32_t st;
-    if (any_cigar && (cigar_buf == nullptr || cigar_buf_bytes < cig_need)) {
-        // the reference's request checks come first, then the buffer contract
-        st = wfa_check(reqs, n, max_smax, &err);
-        if (st == GA_OK) { st = GA_INVALID_ARGUMENT; err = E_CIGBUF; }
-        reset();
-        set_info(info, st, err, 0, 0);
-        return st;
-    }
-    st = wfa_batch(reqs, n, max_smax, opt ? opt->learned : 0, fin, &err);
+    // the reference's request checks come first, then the buffer contract
+    // (the CIGAR bytes the batch needs, ga_align_cigar_bytes), both in the
+    // entry's first pass over the requests
+    const int32_t st = wfa_batch(reqs, n, max_smax, opt ? opt->learned : 0, fin, &err,
+                                 cigar_buf ? cigar_buf_bytes : -1);
     if (st != GA_OK) {
         reset();
         set_info(info, st, err, 0, 0);

@@ -36,9 +36,9 @@ struct WfaView {
 };
 using WfaFinish = std::function<void(int64_t lo, int64_t hi, const WfaView& v)>;
 
-// The reference's request checks, in its order and with its messages
-// (src/api/api.cpp:246-266 and 600-616 with sw_scheme_ok :515-536).
-int32_t wfa_check(const ga_align_request* reqs, int32_t n, int32_t max_smax, const char** err);
+// The reference's SW request checks, in its order and with its messages
+// (src/api/api.cpp:600-616 with sw_scheme_ok :515-536); the WFA ones
+// (:246-266) run inside wfa_batch's first pass.
 int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err);
 
 // The align_batch pipeline: validation, planning, transfer, kernels, and the
@@ -47,8 +47,11 @@ int32_t sw_check(const ga_sw_request* reqs, int32_t n, const char** err);
 // route: 0 plain, 1 queues by the cost model (plain when none is loaded), 2
 // queues by the exact lower bound alone.
 int route_mode(int requested);
+// cig_cap: bytes of the caller's CIGAR buffer (-1: no buffer); a batch whose
+// CIGARs need more fails with GA_INVALID_ARGUMENT after the request checks
+// (which come first), before any device work.
 int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int route,
-                  const WfaFinish& fin, const char** err);
+                  const WfaFinish& fin, const char** err, int64_t cig_cap = INT64_MAX);
 
 // Per-pair outputs of one range of an SW batch (requests [base, base + n)),
 // valid during the finish callback, which gets the batch's own indices: pair i

@@ -116,3 +116,43 @@ def test_first_failure_across_chunks_in_request_order():
     sw[2500] = api.SWRequest(b"ACGT", 4, b"ACGT", 4, api.SWScoring(1, -1, 2, 1))
     b = api.align_sw_batch(sw)
     assert b.error == "all requests in an SW batch must share one scoring scheme"
+
+
+def test_wfa_cigar_buffer_contract():
+    """ga_align_batch needs a CIGAR buffer of ga_align_cigar_bytes bytes when any
+    request asks for a CIGAR; a smaller or missing one is refused before any
+    device work -- after the request checks, whose error comes first."""
+    import ctypes
+    import numpy as np
+    L = api.load()
+    rng = np.random.default_rng(3)
+    n = 3000                                            # three request chunks
+    p = rng.integers(0, 4, size=n * 20).astype(np.uint8)
+    buf = np.frombuffer(b"ACGT", np.uint8)[p]
+    off = np.arange(n, dtype=np.int64) * 20
+    ln = np.full(n, 20, np.int32)
+    res = np.zeros(n, api.RES_DT)
+
+    def call(reqs, cig, nbytes):
+        info = api.BatchInfo()
+        st = L.ga_align_batch(reqs.ctypes.data, n, res.ctypes.data, cig, nbytes, ctypes.byref(info))
+        return st, info.error.decode() if info.error else None
+
+    reqs = api.make_requests(buf, off, ln, buf, off, ln, 8, True)
+    need = int(L.ga_align_cigar_bytes(reqs.ctypes.data, n))
+    assert need == n * 40
+    small = np.empty(need - 1, np.uint8)
+    st, err = call(reqs, small.ctypes.data, need - 1)
+    assert st == api.GA_INVALID_ARGUMENT and err == "cigar buffer is smaller than the batch needs"
+    assert (res["score"] == -1).all()
+    st, err = call(reqs, None, 0)
+    assert st == api.GA_INVALID_ARGUMENT and err == "cigar buffer is smaller than the batch needs"
+    # a failing request decides first
+    bad = reqs.copy()
+    bad["smax"][2500] = 600
+    st, err = call(bad, small.ctypes.data, need - 1)
+    assert st == api.GA_INVALID_ARGUMENT and err == "smax out of range [0, 511]"
+    # no CIGAR asked for: no buffer needed (past the checks, a device is needed)
+    plain = api.make_requests(buf, off, ln, buf, off, ln, 8, False)
+    st, err = call(plain, None, 0)
+    assert st != api.GA_INVALID_ARGUMENT, err
