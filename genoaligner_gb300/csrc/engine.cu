@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -132,10 +133,13 @@ static std::atomic<int> g_fail_next{0};
 // One job at a time: the calling thread and every worker that wakes while the
 // job is open take chunks of `grain` from a shared counter.  The job closes
 // when the caller runs out of chunks; the caller then waits only for the
-// workers that joined it (a worker that wakes after the close skips the job),
-// so a small job does not wait for all workers to be scheduled.
+// workers that joined it (a worker that wakes after the close skips the job).
+// A worker that finishes a job watches for the next one for SPIN_US before it
+// sleeps: a call's host passes come tens of microseconds apart, and waking
+// sleeping threads costs about as much as a small pass itself.
 class Pool {
 public:
+    static constexpr int SPIN_US = 200;
     Pool()
     {
         unsigned hc = std::thread::hardware_concurrency();
@@ -147,7 +151,8 @@ public:
     {
         {
             std::lock_guard<std::mutex> lk(mu_);
-            stop_ = true;
+            stop_.store(true);
+            gen_.fetch_add(1);
         }
         cv_.notify_all();
         for (auto& t : threads_) t.join();
@@ -158,6 +163,7 @@ public:
         if (grain < 1) grain = 1;
         if (threads_.empty() || n <= grain) { fn(0, n); return; }
         std::lock_guard<std::mutex> one(job_mu_);          // one parallel job at a time
+        bool wake;
         {
             std::lock_guard<std::mutex> lk(mu_);
             fn_ = &fn;
@@ -166,9 +172,10 @@ public:
             next_.store(0);
             open_ = true;
             joined_ = 0;
-            ++gen_;
+            gen_.fetch_add(1);
+            wake = sleeping_ > 0;
         }
-        cv_.notify_all();
+        if (wake) cv_.notify_all();
         drain();
         std::unique_lock<std::mutex> lk(mu_);
         open_ = false;                                      // every chunk is taken
@@ -189,11 +196,23 @@ private:
     {
         uint64_t seen = 0;
         for (;;) {
+            // watch for a new job for a while, then sleep until one comes
+            const auto t0 = std::chrono::steady_clock::now();
+            for (int it = 0; gen_.load() == seen; ++it) {
+                if ((it & 63) == 63 &&
+                    std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(SPIN_US))
+                    break;
+                std::this_thread::yield();
+            }
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
-                if (stop_) return;
-                seen = gen_;
+                if (gen_.load() == seen) {
+                    ++sleeping_;
+                    cv_.wait(lk, [&] { return gen_.load() != seen; });
+                    --sleeping_;
+                }
+                if (stop_.load()) return;
+                seen = gen_.load();
                 if (!open_) continue;                       // woke after the job closed
                 ++joined_;
             }
@@ -210,10 +229,10 @@ private:
     const std::function<void(int64_t, int64_t)>* fn_ = nullptr;
     int64_t n_ = 0, grain_ = 1;
     std::atomic<int64_t> next_{0};
-    int joined_ = 0;
+    std::atomic<uint64_t> gen_{0};
+    std::atomic<bool> stop_{false};
+    int joined_ = 0, sleeping_ = 0;
     bool open_ = false;
-    uint64_t gen_ = 0;
-    bool stop_ = false;
 };
 
 static Pool& pool()
@@ -439,6 +458,9 @@ static inline int64_t round32(int64_t x) { return (x + 31) & ~(int64_t)31; }
 
 // Requests per chunk of the host passes over a batch's requests.
 constexpr int64_t REQ_CHUNK = 1024;
+// The WFA entry's chunk: smaller for small batches, whose passes would
+// otherwise be a few chunks, each a whole thread's serial work.
+static inline int64_t wfa_chunk(int64_t n) { return n < 65536 ? 256 : REQ_CHUNK; }
 
 // Where a batch's own sides of one kind (patterns, or texts) lie in the
 // caller's memory, in request order: [first, end) when every side starts at
@@ -491,14 +513,15 @@ static bool pageable_direct()
 }
 constexpr int64_t SPAN_MIN_BYTES = (int64_t)1 << 20;    // below this, staging is cheaper than two more copies
 
-// fn(k, lo, hi) on chunk k = [lo, hi) of [0, n), the chunks in parallel on the
-// host pool; returns the number of chunks.
+// fn(k, lo, hi) on chunk k = [lo, hi) of [0, n) (chunks of `chunk`
+// requests), the chunks in parallel on the host pool; returns the number of
+// chunks.
 template <class F>
-static int64_t for_chunks(int64_t n, F fn)
+static int64_t for_chunks(int64_t n, F fn, int64_t chunk = REQ_CHUNK)
 {
-    const int64_t nch = (n + REQ_CHUNK - 1) / REQ_CHUNK;
+    const int64_t nch = (n + chunk - 1) / chunk;
     parallel_for(nch, 1, [&](int64_t k0, int64_t k1) {
-        for (int64_t k = k0; k < k1; ++k) fn(k, k * REQ_CHUNK, std::min(n, (k + 1) * REQ_CHUNK));
+        for (int64_t k = k0; k < k1; ++k) fn(k, k * chunk, std::min(n, (k + 1) * chunk));
     });
     return nch;
 }
@@ -786,7 +809,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
 {
     *err = nullptr;
     if (n <= 0) return GA_OK;
-    const int64_t nch = (n + REQ_CHUNK - 1) / REQ_CHUNK;
+    const int64_t CH = wfa_chunk(n);                          // requests per chunk
+    const int64_t nch = (n + CH - 1) / CH;
     const int K = n >= WFA_RANGE_MIN ? (int)std::min<int64_t>(WFA_RANGES, nch) : 1;
     std::vector<int64_t> kc((size_t)K + 1);                      // range k: chunks [kc[k], kc[k + 1])
     std::vector<uint8_t> range_start((size_t)nch, 0);
@@ -802,7 +826,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     uint8_t* own = own_v.data();
     int64_t* slot_end = slot_v.data();              // per range: CIGAR slot ends from the range's first slot
     std::vector<WfaChunk> ck((size_t)nch);
-    for_chunks(n, [&](int64_t k, int64_t lo, int64_t hi) {
+    const auto pass1 = [&](int64_t k, int64_t lo, int64_t hi) {
         WfaChunk& C = ck[(size_t)k];
         for (int64_t i = lo; i < hi; ++i) {
             const ga_align_request& r = reqs[i];
@@ -820,7 +844,8 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
             C.cig += cap;
             C.pkb += (cap + 3) / 4;
         }
-    });
+    };
+    for_chunks(n, pass1, CH);
     int smax = INT32_MAX;
     bool trace = false;
     std::vector<int64_t> base((size_t)(3 * (nch + 1))), carry((size_t)(2 * nch));
@@ -853,7 +878,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     std::vector<int64_t> rh2d((size_t)K, 0), rd2h((size_t)K, 0);
     auto run_range = [&](int k, const char** rerr) -> int32_t {
         const int64_t c0 = kc[(size_t)k], c1 = kc[(size_t)k + 1];
-        const int64_t r0 = std::min<int64_t>(n, c0 * REQ_CHUNK), r1 = std::min<int64_t>(n, c1 * REQ_CHUNK);
+        const int64_t r0 = std::min<int64_t>(n, c0 * CH), r1 = std::min<int64_t>(n, c1 * CH);
         const int32_t nk = (int32_t)(r1 - r0);
         if (nk <= 0) return GA_OK;
         const int64_t a0 = base[3 * c0], g0 = base[3 * c0 + 1], p0 = base[3 * c0 + 2];
@@ -914,7 +939,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         // pass 2, in the same chunks: offsets and the staging of every own side
         parallel_for(c1 - c0, 1, [&](int64_t j0, int64_t j1) {
             for (int64_t kk = c0 + j0; kk < c0 + j1; ++kk) {
-                const int64_t lo = kk * REQ_CHUNK, hi = std::min<int64_t>(n, lo + REQ_CHUNK);
+                const int64_t lo = kk * CH, hi = std::min<int64_t>(n, lo + CH);
                 int64_t at = base[3 * kk] - a0, cg = base[3 * kk + 1] - g0, pk = base[3 * kk + 2] - p0;
                 int64_t cur_a = carry[2 * kk] - a0, cur_b = carry[2 * kk + 1] - a0;
                 for (int64_t i = lo; i < hi; ++i) {
@@ -999,7 +1024,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
         if (trace && fail_here(5)) hln[0] = INT32_MAX;       // test hook: a length past its slot
         WfaView v{hsc, hln, hpk, hpo, slot_end + r0, trace, trace ? hvf : nullptr, r0, g0};
         std::atomic<bool> bad{false};
-        parallel_for(nk, 1024, [&](int64_t lo, int64_t hi) {
+        parallel_for(nk, CH, [&](int64_t lo, int64_t hi) {
             if (trace && !lengths_fit(hln, slot_end + r0, lo, hi)) { bad = true; return; }
             fin(r0 + lo, r0 + hi, v);
         });

@@ -101,8 +101,8 @@ def test_no_device_is_device_error():
 
 
 def test_first_failure_across_chunks_in_request_order():
-    """Requests are checked in parallel chunks of 1,024; the error reported is
-    still the first failing request's, and every result is the default."""
+    """Requests are checked in parallel chunks; the error reported is still
+    the first failing request's, and every result is the default."""
     reqs = [api.AlignRequest(b"ACGTACGT", 8, b"ACGTTCGT", 8, smax=8) for _ in range(5000)]
     reqs[4500] = api.AlignRequest(b"ACGT", 4, b"ACGT", 4, smax=600)
     reqs[3000] = api.AlignRequest(b"ACGT", -1, b"ACGT", 4, smax=8)
