@@ -42,7 +42,7 @@ def test_wfa_spans_and_staging_agree():
 
 
 def test_sw_spans_and_staging_agree():
-    ps = workloads.sw_uneven_200k(n=3000, seed=72)
+    ps = workloads.sw_uneven_200k(n=5000, seed=72)          # 5.4 MB of sequence: above the span threshold
     ts, pp = ps.lists()
     want = oracle.sw_batch(ts, pp, scoring=(2, -3, 3, 1), with_cigar=True)
     for layout in (ps, _reversed_layout(ps)):
