@@ -136,10 +136,13 @@ static std::atomic<int> g_fail_next{0};
 // workers that joined it (a worker that wakes after the close skips the job).
 // A worker that finishes a job watches for the next one for SPIN_US before it
 // sleeps: a call's host passes come tens of microseconds apart, and waking
-// sleeping threads costs about as much as a small pass itself.
+// sleeping threads costs about as much as a small pass itself.  While a call
+// runs its ranges on threads of their own (quiet() > 0) the workers sleep at
+// once instead, leaving the cores to those threads.
 class Pool {
 public:
     static constexpr int SPIN_US = 200;
+    std::atomic<int>& quiet() { return quiet_; }
     Pool()
     {
         unsigned hc = std::thread::hardware_concurrency();
@@ -198,7 +201,7 @@ private:
         for (;;) {
             // watch for a new job for a while, then sleep until one comes
             const auto t0 = std::chrono::steady_clock::now();
-            for (int it = 0; gen_.load() == seen; ++it) {
+            for (int it = 0; gen_.load() == seen && quiet_.load() == 0; ++it) {
                 if ((it & 63) == 63 &&
                     std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(SPIN_US))
                     break;
@@ -231,6 +234,7 @@ private:
     std::atomic<int64_t> next_{0};
     std::atomic<uint64_t> gen_{0};
     std::atomic<bool> stop_{false};
+    std::atomic<int> quiet_{0};
     int joined_ = 0, sleeping_ = 0;
     bool open_ = false;
 };
@@ -245,6 +249,13 @@ void parallel_for(int64_t n, int64_t grain, const std::function<void(int64_t, in
 {
     pool().run(n, grain, fn);
 }
+
+// Held while a call runs its ranges on threads of its own: the pool's idle
+// workers sleep instead of watching for the next job.
+struct PoolQuiet {
+    PoolQuiet() { pool().quiet().fetch_add(1); }
+    ~PoolQuiet() { pool().quiet().fetch_sub(1); }
+};
 
 void expand_cigar(const uint8_t* src, int len, char* dst)
 {
@@ -1041,6 +1052,7 @@ int32_t wfa_batch(const ga_align_request* reqs, int32_t n, int32_t max_smax, int
     } else {
         int dev = 0;
         cudaGetDevice(&dev);
+        PoolQuiet quiet;
         std::vector<std::thread> th;
         for (int k = 0; k + 1 < K; ++k)
             th.emplace_back([&, k] {
@@ -1612,6 +1624,7 @@ int32_t sw_batch(const ga_sw_request* reqs, int32_t n, int64_t cell_limit, const
         st[k] = sw_batch_range(reqs + cut[k], cut[k + 1] - cut[k], cut[k], cig_at[k], trace, T, cell_limit, fin,
                                &errs[k], &h2d[k], &d2h[k], K, k, learned);
     };
+    PoolQuiet quiet;
     std::vector<std::thread> th;
     for (int k = 0; k + 1 < K; ++k) th.emplace_back(run, k);
     run(K - 1);
