@@ -156,3 +156,41 @@ def test_wfa_cigar_buffer_contract():
     plain = api.make_requests(buf, off, ln, buf, off, ln, 8, False)
     st, err = call(plain, None, 0)
     assert st != api.GA_INVALID_ARGUMENT, err
+
+
+def test_request_checks_from_many_threads():
+    """Host passes from several calling threads at once share the library's
+    thread pool (one job at a time, each caller waiting only for the workers
+    that joined its job): every call still reports its own batch's first
+    failing request."""
+    import threading
+    import numpy as np
+    L = api.load()
+    n = 5000
+    buf = np.frombuffer(b"ACGT" * 5, np.uint8).copy()
+    off = np.zeros(n, np.int64)
+    ln = np.full(n, 20, np.int32)
+    failures = []
+
+    def worker(t):
+        import ctypes
+        rng = np.random.default_rng(100 + t)
+        res = np.zeros(n, api.RES_DT)
+        for _ in range(40):
+            reqs = api.make_requests(buf, off, ln, buf, off, ln, 8, False)
+            k = int(rng.integers(0, n))
+            reqs["smax"][k] = 600
+            if k + 1 < n:
+                reqs["pattern_len"][k + 1] = -1
+            info = api.BatchInfo()
+            st = L.ga_align_batch(reqs.ctypes.data, n, res.ctypes.data, None, 0, ctypes.byref(info))
+            if st != api.GA_INVALID_ARGUMENT or info.error != b"smax out of range [0, 511]" or \
+                    not (res["score"] == -1).all():
+                failures.append((t, k, st, info.error))
+
+    ts = [threading.Thread(target=worker, args=(t,)) for t in range(6)]
+    for x in ts:
+        x.start()
+    for x in ts:
+        x.join()
+    assert not failures, failures[:3]
